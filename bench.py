@@ -1,0 +1,317 @@
+#!/usr/bin/env python3
+"""Benchmark: Flying Edges on a 512^3 float32 value-noise volume, isovalue 0.
+
+One step = one full extraction (passes 1-4) of the volume.
+  value     Mcells/s with the volume resident in HBM (device entry point,
+            iso_extract_device_async, K steps between two CUDA events)
+  e2e       Mcells/s through the host entry point (iso_extract_host): pinned
+            host volume copied in, mesh copied back to pinned host buffers,
+            every step
+  roofline  the dominant kernel (largest summed time), timed with CUDA events
+            recorded between kernels on the extraction stream during the
+            timed region; algorithmic bytes per launch:
+              classify       4 N                 (volume read)
+              fe_generate    4 N + 24 V + 12 T   (volume read, points+normals, uint32 triangles)
+            the whole extraction is B = 8 N + 24 V + 12 T
+  cpu_baseline  the oracle port of the reference's OpenMP Flying Edges on
+            all host cores, full volume, repeated for a bounded time.
+
+--impl reference runs that CPU implementation alone, rank 0 only.
+Under torchrun (N > 1) every rank extracts its own replica (no collective in
+the data path); value = all ranks' cells / the slowest rank's time.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+DIMS = (512, 512, 512)
+ISO = 0.0
+NOISE = dict(octaves=4, period=64, seed=1)
+METRIC = "Mcells/s"
+PEAKS = ROOT / "MEASURED_PEAKS.json"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--algorithm", default="fe", choices=["fe", "mc"])
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def cells():
+    return (DIMS[0] - 1) * (DIMS[1] - 1) * (DIMS[2] - 1)
+
+
+def workload_config(algo):
+    return {"workload": "%s_512cube_value_noise_iso0" % ("flying_edges" if algo == "fe" else "marching_cubes"),
+            "dims": list(DIMS), "isovalue": ISO, "field": "4-octave value noise, base period 64, gain 0.5, seed 1",
+            "algorithm": "flying_edges" if algo == "fe" else "marching_cubes",
+            "index_bytes": 4, "l2": "inputs larger than L2 (537 MB volume, 129 MB L2)"}
+
+
+def hbm_peak():
+    if PEAKS.exists():
+        d = json.loads(PEAKS.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.path = Path("/tmp/miniiso_clocks_%d_%d.csv" % (os.getpid(), gpu))
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        self.path.unlink(missing_ok=True)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(vol, seconds):
+    """Oracle port of the reference OpenMP Flying Edges, all host cores."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    import oracle_lib
+
+    cores = os.cpu_count() or 1
+    runs, total = 0, 0.0
+    while runs == 0 or total < seconds:
+        oracle_lib.fe(vol, ISO, nthreads=cores)
+        total += oracle_lib.fe_wall_seconds()
+        runs += 1
+        if runs >= 50:
+            break
+    per = total / runs
+    return {"value": cells() / per / 1e6, "unit": METRIC, "cores": cores, "kind": "port",
+            "sample": "full 512^3 volume, %d extraction(s), %.2f s each (oracle port of "
+                      "flyingEdges/openmp, %d OpenMP threads)" % (runs, per, cores)}
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    import miniisosurface_gb300 as M
+
+    sys.path.insert(0, str(ROOT / "tests"))
+    import oracle_lib
+
+    vol = M.generate_value_noise(DIMS, **NOISE)
+    cores = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        oracle_lib.fe(vol, ISO, nthreads=cores)
+    t = 0.0
+    for _ in range(args.steps):
+        oracle_lib.fe(vol, ISO, nthreads=cores)
+        t += oracle_lib.fe_wall_seconds()
+    value = cells() * args.steps / t / 1e6
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": workload_config("fe"), "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": "port",
+                             "sample": "full 512^3 volume per step, %d steps (oracle port of flyingEdges/openmp,"
+                                       " %d OpenMP threads; the reference programs are x86 builds from the "
+                                       "reference sources and the reference tree is not on this host)"
+                                       % (args.steps, cores)},
+            "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+    if args.impl == "reference":
+        run_reference(args, rank)
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    import torch
+
+    import miniisosurface_gb300 as M
+    from miniisosurface_gb300 import _lib
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    lib = _lib.load()
+    algo = M.FLYING_EDGES if args.algorithm == "fe" else M.MARCHING_CUBES
+
+    vol_host = M.generate_value_noise(DIMS, **NOISE)
+    N = vol_host.size
+    pinned = torch.from_numpy(vol_host.reshape(-1)).pin_memory()
+    dvol = pinned.to(dev)
+    ctx = M.Context(local)
+    grid = M.make_grid(DIMS)
+    V, T = M.count_device(dvol, DIMS, ISO, algo, ctx=ctx)
+    out = M.DeviceMesh(V, T, 4, dev)
+    desc = out.descriptor()
+    res = torch.zeros(4, dtype=torch.int64).pin_memory()
+    stream = torch.cuda.current_stream(dev)
+    sh = C.c_void_p(stream.cuda_stream)
+
+    def step():
+        st = lib.iso_extract_device_async(ctx.handle, algo, dvol.data_ptr(), C.byref(grid), C.c_float(ISO),
+                                          C.byref(desc), C.c_void_p(res.data_ptr()), sh)
+        if st != 0:
+            _lib.check(st, ctx.handle)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    assert int(res[0]) == V and int(res[1]) == T
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    lib.iso_ctx_profile(ctx.handle, 1)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    t_wall = time.perf_counter()
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall
+    if dist:
+        dist.barrier()
+    lib.iso_ctx_profile(ctx.handle, 0)
+    ms_pass = (C.c_double * 6)()
+    n_pass = (C.c_int64 * 6)()
+    _lib.check(lib.iso_ctx_profile_read(ctx.handle, ms_pass, n_pass), ctx.handle)
+    ms = e0.elapsed_time(e1)
+
+    # e2e: host volume in, host mesh out, every step
+    h_pts = torch.empty((V, 3), dtype=torch.float32).pin_memory()
+    h_nrm = torch.empty((V, 3), dtype=torch.float32).pin_memory()
+    h_tri = torch.empty((T, 3), dtype=torch.int32).pin_memory()
+    hm = _lib.IsoMesh()
+    hm.points, hm.normals, hm.tris = h_pts.data_ptr(), h_nrm.data_ptr(), h_tri.data_ptr()
+    hm.index_bytes, hm.cap_points, hm.cap_tris = 4, V, T
+
+    def host_step():
+        st = lib.iso_extract_host(ctx.handle, algo, pinned.data_ptr(), C.byref(grid), C.c_float(ISO),
+                                  C.byref(hm), sh)
+        _lib.check(st, ctx.handle)
+
+    host_step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        host_step()
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    clk = clocks.stop()
+
+    # max over ranks
+    times = torch.tensor([ms, e2e_s], dtype=torch.float64, device=dev)
+    if dist:
+        dist.all_reduce(times, op=dist.ReduceOp.MAX)
+    ms, e2e_s = float(times[0]), float(times[1])
+
+    if rank == 0:
+        C_cells = cells()
+        value = C_cells * args.steps * world / (ms / 1e3) / 1e6
+        e2e_value = C_cells * args.e2e_steps * world / e2e_s / 1e6
+        peak, peak_kind = hbm_peak()
+        B_total = 8 * N + 24 * V + 12 * T
+        names = _lib.PASS_NAMES
+        per = {names[p]: {"ms_total": ms_pass[p], "launches": int(n_pass[p]),
+                          "us_per_launch": 1e3 * ms_pass[p] / n_pass[p] if n_pass[p] else None}
+               for p in range(6) if n_pass[p]}
+        alg_bytes = {"classify": 4 * N, "count": 0, "scan": 0, "fe_generate": 4 * N + 24 * V + 12 * T,
+                     "mc_vertices": 4 * N + 24 * V, "mc_triangles": 12 * T}
+        dom = max(per, key=lambda k: per[k]["ms_total"])
+        dom_s = per[dom]["us_per_launch"] * 1e-6
+        achieved = alg_bytes[dom] / dom_s / 1e9
+        prof_ms = sum(v["ms_total"] for v in per.values())
+        traffic_path = ROOT / "profiles" / "traffic.json"
+        traffic = None
+        if traffic_path.exists():
+            traffic = json.loads(traffic_path.read_text()).get(dom)
+        line = {
+            "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": workload_config(args.algorithm),
+            "mesh": {"vertices": V, "triangles": T, "cells": C_cells},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+                         "algorithmic_bytes_per_launch": alg_bytes[dom]},
+            "pipeline": {"bytes_per_step": B_total, "achieved_GBps": B_total / (ms / args.steps / 1e3) / 1e9,
+                         "frac": B_total / (ms / args.steps / 1e3) / 1e9 / peak,
+                         "per_pass": per, "event_overhead_ms_per_step": (ms - prof_ms) / args.steps},
+            "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": 4 * N,
+                    "d2h_bytes_per_step": 24 * V + 12 * T, "ms_per_step": 1e3 * e2e_s / args.e2e_steps},
+            "gpu_launches": int(sum(n_pass[p] for p in range(6))),
+            "clocks": clk,
+        }
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(vol_host, args.cpu_seconds)
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,182 @@
+/*
+ * miniiso.h -- C ABI of the GB300 isosurface extractor.
+ *
+ * Drop-in boundary for miniIsosurface's serial extraction calls:
+ *
+ *   Flying Edges  FlyingEdgesAlgorithm(image, isoval); pass1(); pass2();
+ *                 pass3(); pass4(); moveOutput()
+ *                 (flyingEdges/serial/FlyingEdgesAlgorithm.h:29-49,
+ *                  called from flyingEdges/serial/main.cpp:114-155)
+ *   Marching Cubes  MarchingCubes(image, isoval) -> TriangleMesh
+ *                 (marchingCubes/serial/main.cpp:42-44, called at :287)
+ *
+ * Input: a float32 volume, x fastest (data[k*nx*ny + j*nx + i]), its
+ * spacing and origin (util::Image3D, flyingEdges/util/Image3D.h:26-85).
+ * Output: points and normals (V x 3 float, AoS) and triangles (T x 3 vertex
+ * indices, 32- or 64-bit), as util::TriangleMesh (TriangleMesh.h:24-90).
+ * Triangle count, order, connectivity and vertex numbering are identical to
+ * the reference; points and normals are bit-identical float32.
+ *
+ * Plain pointers and sizes only; no exceptions cross this boundary; every
+ * call returns an iso_status.  One iso_ctx per host thread (a context is not
+ * thread-safe; distinct contexts are).  All device work runs on the CUDA
+ * stream passed in (NULL = legacy default stream).
+ */
+#ifndef MINIISO_H
+#define MINIISO_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum iso_status {
+    ISO_OK = 0,
+    ISO_ERR_INVALID_ARG = 1, /* bad pointer, dimension, algorithm or index width */
+    ISO_ERR_OOM = 2,         /* device or pinned host allocation failed */
+    ISO_ERR_CUDA = 3,        /* a CUDA call failed; see iso_ctx_last_error */
+    ISO_ERR_CAPACITY = 4,    /* output buffers too small; n_points/n_tris hold the sizes needed */
+    ISO_ERR_OVERFLOW = 5,    /* more than 2^32-1 vertices with 32-bit indices */
+    ISO_ERR_TIMEOUT = 6,     /* a bounded device-side wait gave up */
+    ISO_ERR_IO = 7,          /* file cannot be opened / read / written (util::file_not_found) */
+    ISO_ERR_FORMAT = 8,      /* malformed VTK file (util::bad_format, LoadImage.h:45-133) */
+    ISO_ERR_STATE = 9        /* pass called out of order */
+} iso_status;
+
+typedef enum iso_algorithm {
+    ISO_FLYING_EDGES = 0,    /* vertex order of flyingEdges/serial */
+    ISO_MARCHING_CUBES = 1   /* vertex order of marchingCubes/serial */
+} iso_algorithm;
+
+/* Geometry of a structured-points volume (Image3D's dims, spacing, zeroPos). */
+typedef struct iso_grid {
+    int64_t dims[3];
+    float spacing[3];
+    float origin[3];
+} iso_grid;
+
+/* Output mesh.  The caller owns the buffers (device or host, depending on
+ * the call) and states their capacities in elements (points, triangles);
+ * the library fills n_points / n_tris.  tris holds 3 indices per triangle of
+ * index_bytes bytes each (4 or 8; 8 matches the reference's size_t). */
+typedef struct iso_mesh {
+    float* points;
+    float* normals;
+    void* tris;
+    int32_t index_bytes;
+    int64_t cap_points;
+    int64_t cap_tris;
+    int64_t n_points;
+    int64_t n_tris;
+} iso_mesh;
+
+typedef struct iso_ctx iso_ctx;
+
+const char* iso_status_string(iso_status s);
+/* Library version string. */
+const char* iso_version(void);
+
+/* Context: device, case tables, scratch, pinned staging. */
+iso_status iso_ctx_create(int device, iso_ctx** out);
+iso_status iso_ctx_destroy(iso_ctx* ctx);
+const char* iso_ctx_last_error(const iso_ctx* ctx);
+/* Device-memory bytes currently held by the context's scratch. */
+int64_t iso_ctx_scratch_bytes(const iso_ctx* ctx);
+
+/* Per-pass device timing of the one-shot entry points (no counterpart in
+ * the reference, whose util::Timer brackets each pass on the host,
+ * flyingEdges/serial/main.cpp:120-158).  While enabled, CUDA events are
+ * recorded on the extraction stream between consecutive kernels.
+ * iso_ctx_profile_read synchronises on them, returns the summed
+ * milliseconds and launch counts per pass (ISO_PASS_*) and clears them. */
+enum {
+    ISO_PASS_CLASSIFY = 0,     /* pass 1 */
+    ISO_PASS_COUNT = 1,        /* pass 2 */
+    ISO_PASS_SCAN = 2,         /* pass 3 */
+    ISO_PASS_FE_GENERATE = 3,  /* pass 4, Flying Edges */
+    ISO_PASS_MC_VERTICES = 4,  /* pass 4, Marching Cubes vertices */
+    ISO_PASS_MC_TRIANGLES = 5, /* pass 4, Marching Cubes triangles */
+    ISO_NUM_PASSES = 6
+};
+iso_status iso_ctx_profile(iso_ctx* ctx, int enable);
+iso_status iso_ctx_profile_read(iso_ctx* ctx, double* ms, int64_t* launches);
+
+/* Count only: passes 1-3 (FlyingEdgesAlgorithm.cpp:23-269).  Returns the
+ * exact output sizes.  volume is a device pointer. */
+iso_status iso_count_device(iso_ctx* ctx, iso_algorithm algo, const float* volume, const iso_grid* grid,
+                            float isoval, int64_t* n_points, int64_t* n_tris, void* stream);
+
+/* Full extraction, volume and output in device memory.  Synchronises the
+ * stream before returning.  If the buffers are too small nothing is written,
+ * ISO_ERR_CAPACITY is returned and out->n_points / n_tris hold the sizes
+ * needed.  Replaces the four passes + moveOutput() of
+ * flyingEdges/serial/main.cpp:114-155 (ISO_FLYING_EDGES) and the
+ * MarchingCubes() call of marchingCubes/serial/main.cpp:287
+ * (ISO_MARCHING_CUBES). */
+iso_status iso_extract_device(iso_ctx* ctx, iso_algorithm algo, const float* volume, const iso_grid* grid,
+                              float isoval, iso_mesh* out, void* stream);
+
+/* Same, without the final synchronisation: all work is queued on `stream`;
+ * the sizes land in *result_host (3 x int64: points, triangles, status) when
+ * the stream reaches that point.  result_host must stay valid until then
+ * (pinned memory gives a true asynchronous copy). */
+iso_status iso_extract_device_async(iso_ctx* ctx, iso_algorithm algo, const float* volume, const iso_grid* grid,
+                                    float isoval, iso_mesh* out, int64_t* result_host, void* stream);
+
+/* Host in, host out: copies the volume to the device, extracts, and copies
+ * the mesh back into the caller's host buffers (pinned buffers give the full
+ * link bandwidth).  This is the whole reference call, util::Image3D in and
+ * util::TriangleMesh out. */
+iso_status iso_extract_host(iso_ctx* ctx, iso_algorithm algo, const float* volume, const iso_grid* grid,
+                            float isoval, iso_mesh* out, void* stream);
+
+/* Flying Edges pass by pass, mirroring FlyingEdgesAlgorithm
+ * (flyingEdges/serial/FlyingEdgesAlgorithm.h:29-49).  The volume is a host
+ * pointer that must stay valid until iso_fe_pass4 (the reference keeps a
+ * reference to the image); it is uploaded by iso_fe_pass1. */
+typedef struct iso_fe iso_fe;
+iso_status iso_fe_create(iso_ctx* ctx, const float* host_volume, const iso_grid* grid, float isoval,
+                         iso_fe** out);
+iso_status iso_fe_pass1(iso_fe* fe);  /* classification + trims      (:23-66)   */
+iso_status iso_fe_pass2(iso_fe* fe);  /* cube cases, per-row counts   (:72-190)  */
+iso_status iso_fe_pass3(iso_fe* fe);  /* prefix sums, output sizes    (:196-269) */
+iso_status iso_fe_pass4(iso_fe* fe);  /* points, normals, triangles   (:275-497) */
+/* Sizes known after pass 3. */
+iso_status iso_fe_sizes(const iso_fe* fe, int64_t* n_points, int64_t* n_tris);
+/* gridEdges {xl, xr, xstart, ystart, zstart} x ny*nz (after pass 2: counts;
+ * after pass 3: offsets) and triCounter x (ny-1)*(nz-1), into host arrays. */
+iso_status iso_fe_grid_edges(iso_fe* fe, uint64_t* grid_edges, uint64_t* tri_counter);
+/* moveOutput() (:503-508): copies the mesh into the caller's host buffers. */
+iso_status iso_fe_move_output(iso_fe* fe, iso_mesh* out);
+iso_status iso_fe_destroy(iso_fe* fe);
+
+/* ---- VTK legacy IO (flyingEdges/util/LoadImage.h, SaveTriangleMesh.h) ---- */
+
+/* Reads a BINARY STRUCTURED_POINTS file (char, short, unsigned_short, int,
+ * float or double scalars, big-endian) into float32.  Call with data == NULL
+ * to get the grid only; then again with a buffer of dims product floats. */
+iso_status iso_vtk_read_image(const char* path, iso_grid* grid, float* data);
+/* Writes a mesh in the reference's POLYDATA layout (big-endian floats,
+ * POLYGONS with 8-byte indices, NORMALS) -- byte-identical to
+ * util::saveTriangleMesh.  Host buffers. */
+iso_status iso_vtk_write_mesh(const char* path, const iso_mesh* mesh);
+/* Writes a float32 volume as BINARY STRUCTURED_POINTS (big-endian). */
+iso_status iso_vtk_write_image(const char* path, const iso_grid* grid, const float* data);
+
+/* ---- synthetic volumes of the benchmark configurations ---- */
+
+/* Sum of nblobs isotropic Gaussians exp(-|x-c|^2 / (2 s^2)), amplitude 1,
+ * centres uniform in the box, s uniform in [0.05, 0.15] x mean side. */
+iso_status iso_generate_blobs(const int64_t dims[3], int nblobs, uint64_t seed, float* host_out);
+/* Octave value noise: trilinear interpolation of a seeded uniform[-1,1]
+ * lattice, base period `period` cells, halved per octave, gain 0.5. */
+iso_status iso_generate_value_noise(const int64_t dims[3], int octaves, int period, uint64_t seed,
+                                    float* host_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MINIISO_H */

@@ -1,0 +1,367 @@
+"""Host-side mirror of miniIsosurface's extraction interface over the C ABI.
+
+Reference names are kept so that code written against the reference reads the
+same:
+
+  util::Image3D            -> Image3D          (flyingEdges/util/Image3D.h:26-85)
+  util::TriangleMesh       -> TriangleMesh     (flyingEdges/util/TriangleMesh.h:24-90)
+  FlyingEdgesAlgorithm     -> FlyingEdgesAlgorithm, pass1()..pass4(), moveOutput()
+                              (flyingEdges/serial/FlyingEdgesAlgorithm.h:29-49)
+  MarchingCubes(image, v)  -> MarchingCubes     (marchingCubes/serial/main.cpp:42-44)
+  util::loadImage          -> loadImage         (flyingEdges/util/LoadImage.h:168-198)
+  util::saveTriangleMesh   -> saveTriangleMesh  (flyingEdges/util/SaveTriangleMesh.h:33-118)
+
+All compute runs in libminiiso.so on the GPU; there is no CPU path.  IO
+errors raise file_not_found / bad_format like util/Errors.h:26-48.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _lib
+from ._lib import IsoGrid, IsoMesh, check, load
+
+FLYING_EDGES = _lib.ISO_FLYING_EDGES
+MARCHING_CUBES = _lib.ISO_MARCHING_CUBES
+
+
+class file_not_found(FileNotFoundError):
+    """util::file_not_found (flyingEdges/util/Errors.h:26-36)."""
+
+
+class bad_format(ValueError):
+    """util::bad_format (flyingEdges/util/Errors.h:38-48)."""
+
+
+def _algo(a):
+    if a in (FLYING_EDGES, "fe", "flying_edges", "FlyingEdges"):
+        return FLYING_EDGES
+    if a in (MARCHING_CUBES, "mc", "marching_cubes", "MarchingCubes"):
+        return MARCHING_CUBES
+    raise ValueError("unknown algorithm %r" % (a,))
+
+
+def _ptr(x):
+    """Address of a numpy array or torch tensor (host or device)."""
+    if x is None:
+        return None
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr()
+    return x.ctypes.data
+
+
+def make_grid(dims, spacing=(1.0, 1.0, 1.0), origin=(0.0, 0.0, 0.0)):
+    g = IsoGrid()
+    for a in range(3):
+        g.dims[a] = int(dims[a])
+        g.spacing[a] = float(spacing[a])
+        g.origin[a] = float(origin[a])
+    return g
+
+
+class Context:
+    """An iso_ctx: one device, its case tables and reusable scratch."""
+
+    def __init__(self, device=0):
+        lib = load()
+        h = C.c_void_p()
+        check(lib.iso_ctx_create(int(device), C.byref(h)))
+        self.handle = h
+        self.device = device
+
+    def close(self):
+        if self.handle:
+            load().iso_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def scratch_bytes(self):
+        return int(load().iso_ctx_scratch_bytes(self.handle))
+
+
+_DEFAULT = {}
+
+
+def default_context(device=0):
+    ctx = _DEFAULT.get(device)
+    if ctx is None:
+        ctx = _DEFAULT[device] = Context(device)
+    return ctx
+
+
+class Image3D:
+    """Volume on the host: float32 values x fastest, spacing, zero position."""
+
+    def __init__(self, data, spacing, zeroPos, dimensions):
+        dims = [int(d) for d in dimensions]
+        arr = np.ascontiguousarray(np.asarray(data, dtype=np.float32).reshape(-1))
+        if arr.size != dims[0] * dims[1] * dims[2]:
+            raise ValueError("data has %d values, dimensions %s need %d" % (arr.size, dims, np.prod(dims)))
+        self.data = arr
+        # scalar_t is float (FlyingEdges_Config.h:22): keep float32 values
+        self.spacing = tuple(float(np.float32(s)) for s in spacing)
+        self.zeroPos = tuple(float(np.float32(z)) for z in zeroPos)
+        self.dims = tuple(dims)
+
+    @classmethod
+    def from_array(cls, vol, spacing=(1.0, 1.0, 1.0), origin=(0.0, 0.0, 0.0)):
+        """vol indexed [k][j][i] (z, y, x)."""
+        nz, ny, nx = vol.shape
+        return cls(vol.reshape(-1), spacing, origin, (nx, ny, nz))
+
+    def xdimension(self):
+        return self.dims[0]
+
+    def ydimension(self):
+        return self.dims[1]
+
+    def zdimension(self):
+        return self.dims[2]
+
+    def getSpacing(self):
+        return self.spacing
+
+    def getZeroPos(self):
+        return self.zeroPos
+
+    def pointer(self):
+        return self.data
+
+    def grid(self):
+        return make_grid(self.dims, self.spacing, self.zeroPos)
+
+    def array(self):
+        return self.data.reshape(self.dims[2], self.dims[1], self.dims[0])
+
+
+class TriangleMesh:
+    """points / normals (V, 3) float32 and triangles (T, 3) vertex indices."""
+
+    def __init__(self, points, normals, triangles):
+        self.points = points
+        self.normals = normals
+        self.triangles = triangles
+
+    def numberOfVertices(self):
+        return int(self.points.shape[0])
+
+    def numberOfTriangles(self):
+        return int(self.triangles.shape[0])
+
+
+def _host_mesh_buffers(nv, nt, index_bytes):
+    pts = np.empty((max(nv, 1), 3), np.float32)
+    nrm = np.empty((max(nv, 1), 3), np.float32)
+    tri = np.empty((max(nt, 1), 3), np.uint64 if index_bytes == 8 else np.uint32)
+    m = IsoMesh()
+    m.points, m.normals, m.tris = pts.ctypes.data, nrm.ctypes.data, tri.ctypes.data
+    m.index_bytes = index_bytes
+    m.cap_points, m.cap_tris = nv, nt
+    return m, pts, nrm, tri
+
+
+def extract(image, isoval, algorithm=FLYING_EDGES, index_bytes=8, ctx=None):
+    """One extraction, host volume in, host TriangleMesh out (iso_extract_host)."""
+    lib = load()
+    ctx = ctx or default_context()
+    algo = _algo(algorithm)
+    g = image.grid()
+    nv, nt = 0, 0
+    for _ in range(2):
+        m, pts, nrm, tri = _host_mesh_buffers(nv, nt, index_bytes)
+        st = lib.iso_extract_host(ctx.handle, algo, _ptr(image.data), C.byref(g), C.c_float(isoval),
+                                  C.byref(m), None)
+        if st == _lib.ISO_ERR_CAPACITY:
+            nv, nt = m.n_points, m.n_tris
+            continue
+        check(st, ctx.handle)
+        return TriangleMesh(pts[: m.n_points], nrm[: m.n_points], tri[: m.n_tris])
+    raise RuntimeError("output size changed between two extractions of the same volume")
+
+
+def MarchingCubes(image, isoval, ctx=None):
+    """marchingCubes/serial/main.cpp:42-192: mesh with MC vertex numbering."""
+    return extract(image, isoval, MARCHING_CUBES, 8, ctx)
+
+
+class FlyingEdgesAlgorithm:
+    """flyingEdges/serial/FlyingEdgesAlgorithm.h:29-49, backed by the GPU passes."""
+
+    def __init__(self, image, isoval, ctx=None):
+        lib = load()
+        self._ctx = ctx or default_context()
+        self._image = image  # the reference keeps a reference to the image too
+        self._grid = image.grid()
+        self.isoval = float(isoval)
+        h = C.c_void_p()
+        check(lib.iso_fe_create(self._ctx.handle, _ptr(image.data), C.byref(self._grid), C.c_float(isoval),
+                                C.byref(h)), self._ctx.handle)
+        self._h = h
+
+    def __del__(self):
+        try:
+            if self._h:
+                load().iso_fe_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+    def _call(self, fn):
+        check(fn(self._h), self._ctx.handle)
+
+    def pass1(self):
+        self._call(load().iso_fe_pass1)
+
+    def pass2(self):
+        self._call(load().iso_fe_pass2)
+
+    def pass3(self):
+        self._call(load().iso_fe_pass3)
+
+    def pass4(self):
+        self._call(load().iso_fe_pass4)
+
+    def sizes(self):
+        nv, nt = C.c_int64(), C.c_int64()
+        check(load().iso_fe_sizes(self._h, C.byref(nv), C.byref(nt)), self._ctx.handle)
+        return nv.value, nt.value
+
+    def gridEdges(self):
+        """(ny*nz, 5) records {xl, xr, xstart, ystart, zstart} and triCounter."""
+        nx, ny, nz = self._image.dims
+        ge = np.zeros((ny * nz, 5), np.uint64)
+        tc = np.zeros(max((ny - 1) * (nz - 1), 1), np.uint64)
+        check(load().iso_fe_grid_edges(self._h, ge.ctypes.data, tc.ctypes.data), self._ctx.handle)
+        return ge, tc[: (ny - 1) * (nz - 1)]
+
+    def moveOutput(self, index_bytes=8):
+        nv, nt = self.sizes()
+        m, pts, nrm, tri = _host_mesh_buffers(nv, nt, index_bytes)
+        check(load().iso_fe_move_output(self._h, C.byref(m)), self._ctx.handle)
+        return TriangleMesh(pts[:nv], nrm[:nv], tri[:nt])
+
+
+class DeviceMesh:
+    """Mesh in device memory (torch tensors with spare capacity)."""
+
+    def __init__(self, cap_points, cap_tris, index_bytes=4, device="cuda"):
+        import torch
+        self.index_bytes = index_bytes
+        self.points = torch.empty((max(cap_points, 1), 3), dtype=torch.float32, device=device)
+        self.normals = torch.empty((max(cap_points, 1), 3), dtype=torch.float32, device=device)
+        self.tris = torch.empty((max(cap_tris, 1), 3), dtype=torch.int32 if index_bytes == 4 else torch.int64,
+                                device=device)
+        self.n_points = 0
+        self.n_tris = 0
+
+    def descriptor(self):
+        m = IsoMesh()
+        m.points, m.normals, m.tris = _ptr(self.points), _ptr(self.normals), _ptr(self.tris)
+        m.index_bytes = self.index_bytes
+        m.cap_points = self.points.shape[0]
+        m.cap_tris = self.tris.shape[0]
+        return m
+
+
+def extract_device(volume, dims, isoval, algorithm=FLYING_EDGES, spacing=(1, 1, 1), origin=(0, 0, 0),
+                   out=None, index_bytes=4, ctx=None, stream=None):
+    """Extraction of a device-resident volume (a CUDA float32 tensor, x fastest).
+
+    Returns a DeviceMesh; `out` is reused when its capacity suffices and is
+    re-allocated (exact size) otherwise.
+    """
+    import torch
+    lib = load()
+    ctx = ctx or default_context(volume.device.index or 0)
+    algo = _algo(algorithm)
+    g = make_grid(dims, spacing, origin)
+    if not volume.is_cuda or volume.dtype != torch.float32 or not volume.is_contiguous():
+        raise ValueError("volume must be a contiguous float32 CUDA tensor")
+    s = stream if stream is not None else torch.cuda.current_stream(volume.device).cuda_stream
+    if out is None:
+        out = DeviceMesh(0, 0, index_bytes, volume.device)
+    for _ in range(2):
+        m = out.descriptor()
+        st = lib.iso_extract_device(ctx.handle, algo, _ptr(volume), C.byref(g), C.c_float(isoval), C.byref(m),
+                                    C.c_void_p(s))
+        if st == _lib.ISO_ERR_CAPACITY:
+            out = DeviceMesh(m.n_points, m.n_tris, out.index_bytes, volume.device)
+            continue
+        check(st, ctx.handle)
+        out.n_points, out.n_tris = m.n_points, m.n_tris
+        return out
+    raise RuntimeError("output size changed between two extractions of the same volume")
+
+
+def count_device(volume, dims, isoval, algorithm=FLYING_EDGES, ctx=None, stream=None):
+    """Passes 1-3 only: exact (n_points, n_tris) of a device-resident volume."""
+    import torch
+    lib = load()
+    ctx = ctx or default_context(volume.device.index or 0)
+    g = make_grid(dims)
+    s = stream if stream is not None else torch.cuda.current_stream(volume.device).cuda_stream
+    nv, nt = C.c_int64(), C.c_int64()
+    check(lib.iso_count_device(ctx.handle, _algo(algorithm), _ptr(volume), C.byref(g), C.c_float(isoval),
+                               C.byref(nv), C.byref(nt), C.c_void_p(s)), ctx.handle)
+    return nv.value, nt.value
+
+
+# ---------------------------------------------------------------------------
+# VTK IO and synthetic volumes
+# ---------------------------------------------------------------------------
+def _io_check(st, path):
+    if st == _lib.ISO_ERR_IO:
+        raise file_not_found(path)
+    if st == _lib.ISO_ERR_FORMAT:
+        raise bad_format(path)
+    check(st)
+
+
+def loadImage(path):
+    lib = load()
+    g = IsoGrid()
+    p = os.fsencode(path)
+    _io_check(lib.iso_vtk_read_image(p, C.byref(g), None), path)
+    dims = [g.dims[a] for a in range(3)]
+    data = np.empty(int(np.prod(dims)), np.float32)
+    _io_check(lib.iso_vtk_read_image(p, C.byref(g), data.ctypes.data), path)
+    return Image3D(data, list(g.spacing), list(g.origin), dims)
+
+
+def saveImage(image, path):
+    g = image.grid()
+    _io_check(load().iso_vtk_write_image(os.fsencode(path), C.byref(g), image.data.ctypes.data), path)
+
+
+def saveTriangleMesh(mesh, path):
+    pts = np.ascontiguousarray(mesh.points, np.float32)
+    nrm = np.ascontiguousarray(mesh.normals, np.float32)
+    tri = np.ascontiguousarray(mesh.triangles)
+    m = IsoMesh()
+    m.points, m.normals, m.tris = pts.ctypes.data, nrm.ctypes.data, tri.ctypes.data
+    m.index_bytes = tri.dtype.itemsize
+    m.n_points, m.n_tris = pts.shape[0], tri.shape[0]
+    m.cap_points, m.cap_tris = m.n_points, m.n_tris
+    _io_check(load().iso_vtk_write_mesh(os.fsencode(path), C.byref(m)), path)
+
+
+def generate_blobs(dims, nblobs=8, seed=0):
+    """[k][j][i] float32 array: sum of nblobs Gaussian blobs."""
+    d = (C.c_int64 * 3)(*[int(x) for x in dims])
+    out = np.empty((dims[2], dims[1], dims[0]), np.float32)
+    check(load().iso_generate_blobs(d, int(nblobs), C.c_uint64(seed), out.ctypes.data))
+    return out
+
+
+def generate_value_noise(dims, octaves=4, period=64, seed=0):
+    """[k][j][i] float32 array: octave value noise in about [-2, 2]."""
+    d = (C.c_int64 * 3)(*[int(x) for x in dims])
+    out = np.empty((dims[2], dims[1], dims[0]), np.float32)
+    check(load().iso_generate_value_noise(d, int(octaves), int(period), C.c_uint64(seed), out.ctypes.data))
+    return out

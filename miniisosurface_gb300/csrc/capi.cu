@@ -1,0 +1,732 @@
+// C ABI of the extractor: contexts, scratch, the extraction entry points and
+// the pass-by-pass Flying Edges object.  See include/miniiso.h.
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/miniiso.h"
+#include "case_table.h"
+#include "iso_device.cuh"
+#include "iso_kernels.h"
+
+using iso::CaseTables;
+using iso::FeBuffers;
+using iso::Grid;
+
+struct iso_ctx {
+    int device = 0;
+    int nsm = 0;
+    CaseTables* d_cases = nullptr;
+    // scratch of the one-shot entry points
+    void* scratch = nullptr;
+    size_t scratch_bytes = 0;
+    uint32_t* fe2mc = nullptr;
+    long long fe2mc_cap = 0;
+    // staging for the host entry points
+    float* d_volume = nullptr;
+    size_t d_volume_bytes = 0;
+    float* d_points = nullptr;
+    float* d_normals = nullptr;
+    void* d_tris = nullptr;
+    long long d_cap_points = 0, d_cap_tris = 0;
+    int d_index_bytes = 0;
+    unsigned long long* h_totals = nullptr;  // pinned, 4 entries
+    std::string last_error;
+    // per-pass timing (iso_ctx_profile)
+    bool profiling = false;
+    std::vector<cudaEvent_t> event_pool;
+    size_t events_used = 0;
+    struct Span { int pass; cudaEvent_t begin, end; };
+    std::vector<Span> spans;
+};
+
+struct iso_fe {
+    iso_ctx* ctx = nullptr;
+    const float* host_volume = nullptr;
+    iso_grid grid{};
+    Grid g{};
+    float isoval = 0.f;
+    int stage = 0;
+    float* d_volume = nullptr;
+    void* scratch = nullptr;
+    FeBuffers buf{};
+    long long n_points = 0, n_tris = 0;
+    float* d_points = nullptr;
+    float* d_normals = nullptr;
+    uint64_t* d_tris = nullptr;
+};
+
+namespace {
+
+const char* kVersion = "miniiso-gb300 0.1 (sm_103a)";
+
+iso_status cuda_fail(iso_ctx* ctx, cudaError_t e, const char* what)
+{
+    if (ctx) {
+        ctx->last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    }
+    return e == cudaErrorMemoryAllocation ? ISO_ERR_OOM : ISO_ERR_CUDA;
+}
+
+#define ISO_CUDA(ctx, call)                                      \
+    do {                                                         \
+        cudaError_t e_ = (call);                                 \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+    } while (0)
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Derived per-case tables: the packed triangle lists, the first-appearance
+// edge order (marching cubes numbering) and the cut-edge masks.
+void build_case_tables(CaseTables& t)
+{
+    for (int c = 0; c < 256; ++c) {
+        const uint64_t w = kIsoCaseTris[c];
+        t.tris[c] = w;
+        uint16_t cut = 0;
+        for (int e = 0; e < 12; ++e) {
+            if (((c >> kIsoEdgeLo[e]) & 1) != ((c >> kIsoEdgeHi[e]) & 1)) cut |= (uint16_t)(1u << e);
+        }
+        t.cut[c] = cut;
+        uint64_t order = 0;
+        int n = 0;
+        uint16_t seen = 0;
+        for (int q = 0; q < 3 * iso_case_ntris(w); ++q) {
+            const int e = iso_case_edge(w, q);
+            if (!((seen >> e) & 1)) {
+                seen |= (uint16_t)(1u << e);
+                order |= (uint64_t)e << (4 * n);
+                ++n;
+            }
+        }
+        t.order[c] = order | ((uint64_t)n << 60);
+    }
+}
+
+bool make_grid(const iso_grid* gr, Grid& g)
+{
+    for (int a = 0; a < 3; ++a) {
+        if (gr->dims[a] < 1 || gr->dims[a] > (1ll << 30)) return false;
+    }
+    g.nx = (int)gr->dims[0];
+    g.ny = (int)gr->dims[1];
+    g.nz = (int)gr->dims[2];
+    g.W = (g.nx + 31) / 32;
+    g.R = (long long)g.ny * g.nz;
+    if ((long long)g.W * g.R > (1ll << 40)) return false;
+    for (int a = 0; a < 3; ++a) {
+        g.sp[a] = gr->spacing[a];
+        g.zp[a] = gr->origin[a];
+    }
+    return true;
+}
+
+bool empty_grid(const Grid& g) { return g.nx < 2 || g.ny < 2 || g.nz < 2; }
+
+size_t scratch_size(const Grid& g)
+{
+    const size_t R = (size_t)g.R, T = (size_t)iso::num_tiles(g);
+    return align256(R * g.W * 4) + align256(R * 16) + align256(R * 8) + align256(R * 4) + align256(R * 16) +
+           align256(3 * T * 8) + align256(4 * 8);
+}
+
+void carve(void* base, const Grid& g, FeBuffers& b)
+{
+    const size_t R = (size_t)g.R, T = (size_t)iso::num_tiles(g);
+    char* p = static_cast<char*>(base);
+    b.bits = reinterpret_cast<uint32_t*>(p); p += align256(R * g.W * 4);
+    b.rowcnt = reinterpret_cast<uint4*>(p); p += align256(R * 16);
+    b.trims = reinterpret_cast<uint2*>(p); p += align256(R * 8);
+    b.mccnt = reinterpret_cast<uint32_t*>(p); p += align256(R * 4);
+    b.rowpre = reinterpret_cast<uint4*>(p); p += align256(R * 16);
+    b.tiles = reinterpret_cast<unsigned long long*>(p); p += align256(3 * T * 8);
+    b.totals = reinterpret_cast<unsigned long long*>(p);
+}
+
+iso_status ensure_scratch(iso_ctx* ctx, const Grid& g, FeBuffers& b, cudaStream_t s)
+{
+    const size_t need = scratch_size(g);
+    if (need > ctx->scratch_bytes) {
+        if (ctx->scratch) {
+            ISO_CUDA(ctx, cudaStreamSynchronize(s));
+            cudaFree(ctx->scratch);
+            ctx->scratch = nullptr;
+            ctx->scratch_bytes = 0;
+        }
+        const size_t alloc = need + need / 4;
+        ISO_CUDA(ctx, cudaMalloc(&ctx->scratch, alloc));
+        ctx->scratch_bytes = alloc;
+    }
+    carve(ctx->scratch, g, b);
+    b.fe2mc = ctx->fe2mc;
+    return ISO_OK;
+}
+
+iso_status ensure_fe2mc(iso_ctx* ctx, long long cap, cudaStream_t s)
+{
+    if (cap > ctx->fe2mc_cap) {
+        if (ctx->fe2mc) {
+            ISO_CUDA(ctx, cudaStreamSynchronize(s));
+            cudaFree(ctx->fe2mc);
+            ctx->fe2mc = nullptr;
+            ctx->fe2mc_cap = 0;
+        }
+        const long long alloc = cap + cap / 4 + 1024;
+        ISO_CUDA(ctx, cudaMalloc(&ctx->fe2mc, (size_t)alloc * 4));
+        ctx->fe2mc_cap = alloc;
+    }
+    return ISO_OK;
+}
+
+iso_status check_mesh(const iso_mesh* m)
+{
+    if (!m) return ISO_ERR_INVALID_ARG;
+    if (m->index_bytes != 4 && m->index_bytes != 8) return ISO_ERR_INVALID_ARG;
+    if (m->cap_points < 0 || m->cap_tris < 0) return ISO_ERR_INVALID_ARG;
+    if (m->cap_points > 0 && (!m->points || !m->normals)) return ISO_ERR_INVALID_ARG;
+    if (m->cap_tris > 0 && !m->tris) return ISO_ERR_INVALID_ARG;
+    return ISO_OK;
+}
+
+// Largest vertex count a mesh may hold (32-bit indices address < 2^32).
+long long vertex_limit(const iso_mesh* m, long long cap)
+{
+    const long long lim = m->index_bytes == 4 ? 0xffffffffll : (1ll << 62);
+    return cap < lim ? cap : lim;
+}
+
+// Events between consecutive kernels while profiling.
+cudaEvent_t next_event(iso_ctx* ctx)
+{
+    if (ctx->events_used == ctx->event_pool.size()) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+        ctx->event_pool.push_back(e);
+    }
+    return ctx->event_pool[ctx->events_used++];
+}
+
+struct PassMarks {
+    iso_ctx* ctx;
+    cudaStream_t s;
+    cudaEvent_t last = nullptr;
+    PassMarks(iso_ctx* c, cudaStream_t st) : ctx(c), s(st)
+    {
+        if (ctx->profiling && (last = next_event(ctx))) cudaEventRecord(last, s);
+    }
+    void mark(int pass)
+    {
+        if (!ctx->profiling || !last) return;
+        cudaEvent_t e = next_event(ctx);
+        if (!e) return;
+        cudaEventRecord(e, s);
+        ctx->spans.push_back({pass, last, e});
+        last = e;
+    }
+};
+
+// Queue passes 1-3 (and pass 4 unless count_only) for one extraction.
+iso_status enqueue(iso_ctx* ctx, iso_algorithm algo, const float* vol, const Grid& g, float iso, FeBuffers& b,
+                   const iso_mesh* out, bool count_only, cudaStream_t s)
+{
+    PassMarks pm(ctx, s);
+    iso::launch_classify(vol, b.bits, g, iso, ctx->nsm, s);
+    pm.mark(ISO_PASS_CLASSIFY);
+    iso::launch_count(b.bits, g, ctx->d_cases, algo == ISO_MARCHING_CUBES, b, s);
+    pm.mark(ISO_PASS_COUNT);
+    iso::launch_scan_tiles(g, b, s);
+    pm.mark(ISO_PASS_SCAN);
+    if (!count_only) {
+        const long long capV = vertex_limit(out, out->cap_points);
+        const long long capT = out->cap_tris;
+        if (algo == ISO_FLYING_EDGES) {
+            if (out->index_bytes == 4)
+                iso::launch_fe_generate<uint32_t>(vol, b.bits, g, iso, ctx->d_cases, b, capV, capT, out->points,
+                                                  out->normals, static_cast<uint32_t*>(out->tris), ctx->nsm, s);
+            else
+                iso::launch_fe_generate<uint64_t>(vol, b.bits, g, iso, ctx->d_cases, b, capV, capT, out->points,
+                                                  out->normals, static_cast<uint64_t*>(out->tris), ctx->nsm, s);
+            pm.mark(ISO_PASS_FE_GENERATE);
+        } else {
+            const long long capM = capV < 0xffffffffll ? capV : 0xffffffffll;  // fe2mc holds 32-bit ids
+            iso::launch_mc_vertices(vol, b.bits, g, iso, ctx->d_cases, b, capM, capT, out->points, out->normals,
+                                    ctx->nsm, s);
+            pm.mark(ISO_PASS_MC_VERTICES);
+            if (out->index_bytes == 4)
+                iso::launch_mc_triangles<uint32_t>(b.bits, g, ctx->d_cases, b, capM, capT,
+                                                   static_cast<uint32_t*>(out->tris), ctx->nsm, s);
+            else
+                iso::launch_mc_triangles<uint64_t>(b.bits, g, ctx->d_cases, b, capM, capT,
+                                                   static_cast<uint64_t*>(out->tris), ctx->nsm, s);
+            pm.mark(ISO_PASS_MC_TRIANGLES);
+        }
+    }
+    ISO_CUDA(ctx, cudaGetLastError());
+    return ISO_OK;
+}
+
+iso_status finish_counts(iso_ctx* ctx, const iso_mesh* out, long long V, long long T, int64_t* nV, int64_t* nT)
+{
+    *nV = V;
+    *nT = T;
+    if (out && out->index_bytes == 4 && V > 0xffffffffll) {
+        ctx->last_error = "more than 2^32-1 vertices: use 64-bit indices";
+        return ISO_ERR_OVERFLOW;
+    }
+    if (out && (V > out->cap_points || T > out->cap_tris)) {
+        ctx->last_error = "output buffers too small";
+        return ISO_ERR_CAPACITY;
+    }
+    return ISO_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* iso_status_string(iso_status s)
+{
+    switch (s) {
+        case ISO_OK: return "ok";
+        case ISO_ERR_INVALID_ARG: return "invalid argument";
+        case ISO_ERR_OOM: return "out of memory";
+        case ISO_ERR_CUDA: return "CUDA error";
+        case ISO_ERR_CAPACITY: return "output buffers too small";
+        case ISO_ERR_OVERFLOW: return "index overflow";
+        case ISO_ERR_TIMEOUT: return "device wait timed out";
+        case ISO_ERR_IO: return "file error";
+        case ISO_ERR_FORMAT: return "bad file format";
+        case ISO_ERR_STATE: return "call out of order";
+    }
+    return "unknown status";
+}
+
+const char* iso_version(void) { return kVersion; }
+
+iso_status iso_ctx_create(int device, iso_ctx** out)
+{
+    if (!out) return ISO_ERR_INVALID_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || device < 0 || device >= ndev) return e != cudaSuccess ? ISO_ERR_CUDA : ISO_ERR_INVALID_ARG;
+    iso_ctx* ctx = new (std::nothrow) iso_ctx();
+    if (!ctx) return ISO_ERR_OOM;
+    ctx->device = device;
+    iso_status st = ISO_OK;
+    do {
+        if ((e = cudaSetDevice(device)) != cudaSuccess) { st = cuda_fail(ctx, e, "cudaSetDevice"); break; }
+        if ((e = cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess) {
+            st = cuda_fail(ctx, e, "cudaDeviceGetAttribute");
+            break;
+        }
+        CaseTables h;
+        build_case_tables(h);
+        if ((e = cudaMalloc(&ctx->d_cases, sizeof(CaseTables))) != cudaSuccess) { st = cuda_fail(ctx, e, "cudaMalloc"); break; }
+        if ((e = cudaMemcpy(ctx->d_cases, &h, sizeof(CaseTables), cudaMemcpyHostToDevice)) != cudaSuccess) {
+            st = cuda_fail(ctx, e, "cudaMemcpy");
+            break;
+        }
+        if ((e = cudaMallocHost(&ctx->h_totals, 4 * sizeof(unsigned long long))) != cudaSuccess) {
+            st = cuda_fail(ctx, e, "cudaMallocHost");
+            break;
+        }
+    } while (0);
+    if (st != ISO_OK) {
+        iso_ctx_destroy(ctx);
+        return st;
+    }
+    *out = ctx;
+    return ISO_OK;
+}
+
+iso_status iso_ctx_destroy(iso_ctx* ctx)
+{
+    if (!ctx) return ISO_OK;
+    cudaSetDevice(ctx->device);
+    cudaDeviceSynchronize();
+    cudaFree(ctx->d_cases);
+    cudaFree(ctx->scratch);
+    cudaFree(ctx->fe2mc);
+    cudaFree(ctx->d_volume);
+    cudaFree(ctx->d_points);
+    cudaFree(ctx->d_normals);
+    cudaFree(ctx->d_tris);
+    if (ctx->h_totals) cudaFreeHost(ctx->h_totals);
+    for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
+    delete ctx;
+    return ISO_OK;
+}
+
+const char* iso_ctx_last_error(const iso_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "no context"; }
+
+int64_t iso_ctx_scratch_bytes(const iso_ctx* ctx)
+{
+    return ctx ? (int64_t)(ctx->scratch_bytes + (size_t)ctx->fe2mc_cap * 4) : 0;
+}
+
+iso_status iso_ctx_profile(iso_ctx* ctx, int enable)
+{
+    if (!ctx) return ISO_ERR_INVALID_ARG;
+    ctx->profiling = enable != 0;
+    return ISO_OK;
+}
+
+iso_status iso_ctx_profile_read(iso_ctx* ctx, double* ms, int64_t* launches)
+{
+    if (!ctx || !ms || !launches) return ISO_ERR_INVALID_ARG;
+    for (int p = 0; p < ISO_NUM_PASSES; ++p) {
+        ms[p] = 0.0;
+        launches[p] = 0;
+    }
+    iso_status st = ISO_OK;
+    for (const auto& sp : ctx->spans) {
+        cudaError_t e = cudaEventSynchronize(sp.end);
+        float t = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&t, sp.begin, sp.end);
+        if (e != cudaSuccess) {
+            st = cuda_fail(ctx, e, "iso_ctx_profile_read");
+            continue;
+        }
+        ms[sp.pass] += t;
+        launches[sp.pass] += 1;
+    }
+    ctx->spans.clear();
+    ctx->events_used = 0;
+    return st;
+}
+
+iso_status iso_count_device(iso_ctx* ctx, iso_algorithm algo, const float* volume, const iso_grid* grid,
+                            float isoval, int64_t* n_points, int64_t* n_tris, void* stream)
+{
+    if (!ctx || !grid || !n_points || !n_tris) return ISO_ERR_INVALID_ARG;
+    if (algo != ISO_FLYING_EDGES && algo != ISO_MARCHING_CUBES) return ISO_ERR_INVALID_ARG;
+    Grid g;
+    if (!make_grid(grid, g)) return ISO_ERR_INVALID_ARG;
+    *n_points = 0;
+    *n_tris = 0;
+    if (empty_grid(g)) return ISO_OK;
+    if (!volume) return ISO_ERR_INVALID_ARG;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    ISO_CUDA(ctx, cudaSetDevice(ctx->device));
+    FeBuffers b;
+    iso_status st = ensure_scratch(ctx, g, b, s);
+    if (st != ISO_OK) return st;
+    st = enqueue(ctx, algo, volume, g, isoval, b, nullptr, true, s);
+    if (st != ISO_OK) return st;
+    ISO_CUDA(ctx, cudaMemcpyAsync(ctx->h_totals, b.totals, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    ISO_CUDA(ctx, cudaStreamSynchronize(s));
+    *n_points = (int64_t)ctx->h_totals[0];
+    *n_tris = (int64_t)ctx->h_totals[1];
+    return ISO_OK;
+}
+
+iso_status iso_extract_device_async(iso_ctx* ctx, iso_algorithm algo, const float* volume, const iso_grid* grid,
+                                    float isoval, iso_mesh* out, int64_t* result_host, void* stream)
+{
+    if (!ctx || !grid || !result_host) return ISO_ERR_INVALID_ARG;
+    if (algo != ISO_FLYING_EDGES && algo != ISO_MARCHING_CUBES) return ISO_ERR_INVALID_ARG;
+    iso_status st = check_mesh(out);
+    if (st != ISO_OK) return st;
+    Grid g;
+    if (!make_grid(grid, g)) return ISO_ERR_INVALID_ARG;
+    result_host[0] = result_host[1] = 0;
+    if (empty_grid(g)) return ISO_OK;
+    if (!volume) return ISO_ERR_INVALID_ARG;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    ISO_CUDA(ctx, cudaSetDevice(ctx->device));
+    FeBuffers b;
+    st = ensure_scratch(ctx, g, b, s);
+    if (st != ISO_OK) return st;
+    if (algo == ISO_MARCHING_CUBES) {
+        st = ensure_fe2mc(ctx, out->cap_points, s);
+        if (st != ISO_OK) return st;
+        b.fe2mc = ctx->fe2mc;
+    }
+    st = enqueue(ctx, algo, volume, g, isoval, b, out, false, s);
+    if (st != ISO_OK) return st;
+    ISO_CUDA(ctx, cudaMemcpyAsync(result_host, b.totals, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    return ISO_OK;
+}
+
+iso_status iso_extract_device(iso_ctx* ctx, iso_algorithm algo, const float* volume, const iso_grid* grid,
+                              float isoval, iso_mesh* out, void* stream)
+{
+    if (!ctx) return ISO_ERR_INVALID_ARG;
+    iso_status st = check_mesh(out);
+    if (st != ISO_OK) return st;
+    out->n_points = out->n_tris = 0;
+    st = iso_extract_device_async(ctx, algo, volume, grid, isoval, out, reinterpret_cast<int64_t*>(ctx->h_totals),
+                                  stream);
+    if (st != ISO_OK) return st;
+    ISO_CUDA(ctx, cudaStreamSynchronize(static_cast<cudaStream_t>(stream)));
+    return finish_counts(ctx, out, (long long)ctx->h_totals[0], (long long)ctx->h_totals[1], &out->n_points,
+                         &out->n_tris);
+}
+
+iso_status iso_extract_host(iso_ctx* ctx, iso_algorithm algo, const float* volume, const iso_grid* grid,
+                            float isoval, iso_mesh* out, void* stream)
+{
+    if (!ctx || !grid) return ISO_ERR_INVALID_ARG;
+    if (algo != ISO_FLYING_EDGES && algo != ISO_MARCHING_CUBES) return ISO_ERR_INVALID_ARG;
+    iso_status st = check_mesh(out);
+    if (st != ISO_OK) return st;
+    Grid g;
+    if (!make_grid(grid, g)) return ISO_ERR_INVALID_ARG;
+    out->n_points = out->n_tris = 0;
+    if (empty_grid(g)) return ISO_OK;
+    if (!volume) return ISO_ERR_INVALID_ARG;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    ISO_CUDA(ctx, cudaSetDevice(ctx->device));
+    const size_t vbytes = (size_t)g.nx * g.ny * g.nz * sizeof(float);
+    if (vbytes > ctx->d_volume_bytes) {
+        ISO_CUDA(ctx, cudaStreamSynchronize(s));
+        cudaFree(ctx->d_volume);
+        ctx->d_volume = nullptr;
+        ctx->d_volume_bytes = 0;
+        ISO_CUDA(ctx, cudaMalloc(&ctx->d_volume, vbytes));
+        ctx->d_volume_bytes = vbytes;
+    }
+    ISO_CUDA(ctx, cudaMemcpyAsync(ctx->d_volume, volume, vbytes, cudaMemcpyHostToDevice, s));
+    FeBuffers b;
+    st = ensure_scratch(ctx, g, b, s);
+    if (st != ISO_OK) return st;
+    st = enqueue(ctx, algo, ctx->d_volume, g, isoval, b, nullptr, true, s);
+    if (st != ISO_OK) return st;
+    ISO_CUDA(ctx, cudaMemcpyAsync(ctx->h_totals, b.totals, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    ISO_CUDA(ctx, cudaStreamSynchronize(s));
+    const long long V = (long long)ctx->h_totals[0], T = (long long)ctx->h_totals[1];
+    st = finish_counts(ctx, out, V, T, &out->n_points, &out->n_tris);
+    if (st != ISO_OK) return st;
+    // device output staging, grown on demand
+    if (V > ctx->d_cap_points || T > ctx->d_cap_tris || out->index_bytes != ctx->d_index_bytes) {
+        cudaFree(ctx->d_points);
+        cudaFree(ctx->d_normals);
+        cudaFree(ctx->d_tris);
+        ctx->d_points = ctx->d_normals = nullptr;
+        ctx->d_tris = nullptr;
+        ctx->d_cap_points = ctx->d_cap_tris = 0;
+        const long long cv = V + V / 4 + 1024, ct = T + T / 4 + 1024;
+        ISO_CUDA(ctx, cudaMalloc(&ctx->d_points, (size_t)cv * 12));
+        ISO_CUDA(ctx, cudaMalloc(&ctx->d_normals, (size_t)cv * 12));
+        ISO_CUDA(ctx, cudaMalloc(&ctx->d_tris, (size_t)ct * 3 * out->index_bytes));
+        ctx->d_cap_points = cv;
+        ctx->d_cap_tris = ct;
+        ctx->d_index_bytes = out->index_bytes;
+    }
+    iso_mesh dm{};
+    dm.points = ctx->d_points;
+    dm.normals = ctx->d_normals;
+    dm.tris = ctx->d_tris;
+    dm.index_bytes = out->index_bytes;
+    dm.cap_points = ctx->d_cap_points;
+    dm.cap_tris = ctx->d_cap_tris;
+    PassMarks pm(ctx, s);
+    if (algo == ISO_FLYING_EDGES) {
+        if (dm.index_bytes == 4)
+            iso::launch_fe_generate<uint32_t>(ctx->d_volume, b.bits, g, isoval, ctx->d_cases, b, dm.cap_points,
+                                              dm.cap_tris, dm.points, dm.normals, static_cast<uint32_t*>(dm.tris),
+                                              ctx->nsm, s);
+        else
+            iso::launch_fe_generate<uint64_t>(ctx->d_volume, b.bits, g, isoval, ctx->d_cases, b, dm.cap_points,
+                                              dm.cap_tris, dm.points, dm.normals, static_cast<uint64_t*>(dm.tris),
+                                              ctx->nsm, s);
+        pm.mark(ISO_PASS_FE_GENERATE);
+    } else {
+        st = ensure_fe2mc(ctx, V, s);
+        if (st != ISO_OK) return st;
+        b.fe2mc = ctx->fe2mc;
+        iso::launch_mc_vertices(ctx->d_volume, b.bits, g, isoval, ctx->d_cases, b, dm.cap_points, dm.cap_tris,
+                                dm.points, dm.normals, ctx->nsm, s);
+        pm.mark(ISO_PASS_MC_VERTICES);
+        if (dm.index_bytes == 4)
+            iso::launch_mc_triangles<uint32_t>(b.bits, g, ctx->d_cases, b, dm.cap_points, dm.cap_tris,
+                                               static_cast<uint32_t*>(dm.tris), ctx->nsm, s);
+        else
+            iso::launch_mc_triangles<uint64_t>(b.bits, g, ctx->d_cases, b, dm.cap_points, dm.cap_tris,
+                                               static_cast<uint64_t*>(dm.tris), ctx->nsm, s);
+        pm.mark(ISO_PASS_MC_TRIANGLES);
+    }
+    ISO_CUDA(ctx, cudaGetLastError());
+    if (V > 0) {
+        ISO_CUDA(ctx, cudaMemcpyAsync(out->points, dm.points, (size_t)V * 12, cudaMemcpyDeviceToHost, s));
+        ISO_CUDA(ctx, cudaMemcpyAsync(out->normals, dm.normals, (size_t)V * 12, cudaMemcpyDeviceToHost, s));
+    }
+    if (T > 0) {
+        ISO_CUDA(ctx, cudaMemcpyAsync(out->tris, dm.tris, (size_t)T * 3 * out->index_bytes, cudaMemcpyDeviceToHost, s));
+    }
+    ISO_CUDA(ctx, cudaStreamSynchronize(s));
+    return ISO_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Pass-by-pass Flying Edges (FlyingEdgesAlgorithm.h:29-49)
+// ---------------------------------------------------------------------------
+iso_status iso_fe_create(iso_ctx* ctx, const float* host_volume, const iso_grid* grid, float isoval, iso_fe** out)
+{
+    if (!ctx || !grid || !out) return ISO_ERR_INVALID_ARG;
+    *out = nullptr;
+    Grid g;
+    if (!make_grid(grid, g)) return ISO_ERR_INVALID_ARG;
+    if (!empty_grid(g) && !host_volume) return ISO_ERR_INVALID_ARG;
+    iso_fe* fe = new (std::nothrow) iso_fe();
+    if (!fe) return ISO_ERR_OOM;
+    fe->ctx = ctx;
+    fe->host_volume = host_volume;
+    fe->grid = *grid;
+    fe->g = g;
+    fe->isoval = isoval;
+    *out = fe;
+    return ISO_OK;
+}
+
+iso_status iso_fe_pass1(iso_fe* fe)
+{
+    if (!fe) return ISO_ERR_INVALID_ARG;
+    if (fe->stage != 0) return ISO_ERR_STATE;
+    iso_ctx* ctx = fe->ctx;
+    fe->stage = 1;
+    if (empty_grid(fe->g)) return ISO_OK;
+    ISO_CUDA(ctx, cudaSetDevice(ctx->device));
+    const Grid& g = fe->g;
+    const size_t vbytes = (size_t)g.nx * g.ny * g.nz * sizeof(float);
+    ISO_CUDA(ctx, cudaMalloc(&fe->d_volume, vbytes));
+    ISO_CUDA(ctx, cudaMalloc(&fe->scratch, scratch_size(g)));
+    carve(fe->scratch, g, fe->buf);
+    ISO_CUDA(ctx, cudaMemcpy(fe->d_volume, fe->host_volume, vbytes, cudaMemcpyHostToDevice));
+    iso::launch_classify(fe->d_volume, fe->buf.bits, g, fe->isoval, ctx->nsm, 0);
+    ISO_CUDA(ctx, cudaGetLastError());
+    ISO_CUDA(ctx, cudaDeviceSynchronize());
+    return ISO_OK;
+}
+
+iso_status iso_fe_pass2(iso_fe* fe)
+{
+    if (!fe) return ISO_ERR_INVALID_ARG;
+    if (fe->stage != 1) return ISO_ERR_STATE;
+    fe->stage = 2;
+    if (empty_grid(fe->g)) return ISO_OK;
+    iso_ctx* ctx = fe->ctx;
+    ISO_CUDA(ctx, cudaSetDevice(ctx->device));
+    iso::launch_count(fe->buf.bits, fe->g, ctx->d_cases, false, fe->buf, 0);
+    ISO_CUDA(ctx, cudaGetLastError());
+    ISO_CUDA(ctx, cudaDeviceSynchronize());
+    return ISO_OK;
+}
+
+iso_status iso_fe_pass3(iso_fe* fe)
+{
+    if (!fe) return ISO_ERR_INVALID_ARG;
+    if (fe->stage != 2) return ISO_ERR_STATE;
+    fe->stage = 3;
+    if (empty_grid(fe->g)) return ISO_OK;
+    iso_ctx* ctx = fe->ctx;
+    ISO_CUDA(ctx, cudaSetDevice(ctx->device));
+    iso::launch_scan_tiles(fe->g, fe->buf, 0);
+    ISO_CUDA(ctx, cudaGetLastError());
+    unsigned long long tot[3];
+    ISO_CUDA(ctx, cudaMemcpy(tot, fe->buf.totals, sizeof(tot), cudaMemcpyDeviceToHost));
+    fe->n_points = (long long)tot[0];
+    fe->n_tris = (long long)tot[1];
+    // allocation of the output, as the reference does at the end of pass 3
+    ISO_CUDA(ctx, cudaMalloc(&fe->d_points, (size_t)(fe->n_points + 1) * 12));
+    ISO_CUDA(ctx, cudaMalloc(&fe->d_normals, (size_t)(fe->n_points + 1) * 12));
+    ISO_CUDA(ctx, cudaMalloc(&fe->d_tris, (size_t)(fe->n_tris + 1) * 24));
+    return ISO_OK;
+}
+
+iso_status iso_fe_pass4(iso_fe* fe)
+{
+    if (!fe) return ISO_ERR_INVALID_ARG;
+    if (fe->stage != 3) return ISO_ERR_STATE;
+    fe->stage = 4;
+    if (empty_grid(fe->g)) return ISO_OK;
+    iso_ctx* ctx = fe->ctx;
+    ISO_CUDA(ctx, cudaSetDevice(ctx->device));
+    iso::launch_fe_generate<uint64_t>(fe->d_volume, fe->buf.bits, fe->g, fe->isoval, ctx->d_cases, fe->buf,
+                                      fe->n_points, fe->n_tris, fe->d_points, fe->d_normals, fe->d_tris, ctx->nsm,
+                                      0);
+    ISO_CUDA(ctx, cudaGetLastError());
+    ISO_CUDA(ctx, cudaDeviceSynchronize());
+    return ISO_OK;
+}
+
+iso_status iso_fe_sizes(const iso_fe* fe, int64_t* n_points, int64_t* n_tris)
+{
+    if (!fe || !n_points || !n_tris) return ISO_ERR_INVALID_ARG;
+    if (fe->stage < 3) return ISO_ERR_STATE;
+    *n_points = fe->n_points;
+    *n_tris = fe->n_tris;
+    return ISO_OK;
+}
+
+iso_status iso_fe_grid_edges(iso_fe* fe, uint64_t* grid_edges, uint64_t* tri_counter)
+{
+    if (!fe || !grid_edges || !tri_counter) return ISO_ERR_INVALID_ARG;
+    if (fe->stage < 2) return ISO_ERR_STATE;
+    const Grid& g = fe->g;
+    if (empty_grid(g)) return ISO_OK;
+    iso_ctx* ctx = fe->ctx;
+    ISO_CUDA(ctx, cudaSetDevice(ctx->device));
+    const size_t nge = (size_t)g.R * 5, ntc = (size_t)(g.ny - 1) * (g.nz - 1);
+    unsigned long long* d = nullptr;
+    ISO_CUDA(ctx, cudaMalloc(&d, (nge + ntc) * 8));
+    iso::launch_fe_grid_edges(g, fe->buf, fe->stage >= 3 ? 1 : 0, d, d + nge, 0);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(grid_edges, d, nge * 8, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(tri_counter, d + nge, ntc * 8, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "iso_fe_grid_edges");
+    return ISO_OK;
+}
+
+iso_status iso_fe_move_output(iso_fe* fe, iso_mesh* out)
+{
+    if (!fe) return ISO_ERR_INVALID_ARG;
+    iso_status st = check_mesh(out);
+    if (st != ISO_OK) return st;
+    if (fe->stage != 4) return ISO_ERR_STATE;
+    iso_ctx* ctx = fe->ctx;
+    out->n_points = fe->n_points;
+    out->n_tris = fe->n_tris;
+    if (fe->n_points > out->cap_points || fe->n_tris > out->cap_tris) return ISO_ERR_CAPACITY;
+    if (out->index_bytes == 4 && fe->n_points > 0xffffffffll) return ISO_ERR_OVERFLOW;
+    if (fe->n_points == 0 && fe->n_tris == 0) return ISO_OK;
+    ISO_CUDA(ctx, cudaSetDevice(ctx->device));
+    ISO_CUDA(ctx, cudaMemcpy(out->points, fe->d_points, (size_t)fe->n_points * 12, cudaMemcpyDeviceToHost));
+    ISO_CUDA(ctx, cudaMemcpy(out->normals, fe->d_normals, (size_t)fe->n_points * 12, cudaMemcpyDeviceToHost));
+    if (out->index_bytes == 8) {
+        ISO_CUDA(ctx, cudaMemcpy(out->tris, fe->d_tris, (size_t)fe->n_tris * 24, cudaMemcpyDeviceToHost));
+    } else {
+        // narrow on the host: the pass-by-pass path keeps the reference's size_t
+        uint64_t* tmp = new (std::nothrow) uint64_t[(size_t)fe->n_tris * 3 + 1];
+        if (!tmp) return ISO_ERR_OOM;
+        cudaError_t e = cudaMemcpy(tmp, fe->d_tris, (size_t)fe->n_tris * 24, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) {
+            delete[] tmp;
+            return cuda_fail(ctx, e, "cudaMemcpy");
+        }
+        uint32_t* o = static_cast<uint32_t*>(out->tris);
+        for (size_t q = 0; q < (size_t)fe->n_tris * 3; ++q) o[q] = (uint32_t)tmp[q];
+        delete[] tmp;
+    }
+    return ISO_OK;
+}
+
+iso_status iso_fe_destroy(iso_fe* fe)
+{
+    if (!fe) return ISO_OK;
+    cudaSetDevice(fe->ctx->device);
+    cudaFree(fe->d_volume);
+    cudaFree(fe->scratch);
+    cudaFree(fe->d_points);
+    cudaFree(fe->d_normals);
+    cudaFree(fe->d_tris);
+    delete fe;
+    return ISO_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,336 @@
+// Device-side helpers shared by the Flying Edges and Marching Cubes kernels.
+//
+// Data layout in HBM (one extraction):
+//   volume  float32[nz][ny][nx]                  x fastest (Image3D.h:26-85)
+//   bits    uint32[R][W]   R = ny*nz grid rows, W = ceil(nx/32) words per row;
+//                          bit i of row r is "value(i, r) >= isovalue"
+//   rowcnt  uint4[R]       per grid row: cut x/y/z edges owned by the row,
+//                          triangles of cell row (j,k)
+//   mccnt   uint32[R]      marching cubes: vertices owned by cell row (j,k)
+//   rowpre  uint4[R]       exclusive prefix of (vertices, triangles, mc
+//                          vertices) inside the row's tile
+//   tiles   u64[3*ntiles]  per tile of kTileRows rows: totals, then offsets
+//
+// All interpolation arithmetic goes through the _rn intrinsics so that no
+// multiply-add is ever contracted: that reproduces the float32 results of the
+// reference CPU code bit for bit.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "case_table.h"
+
+namespace iso {
+
+constexpr int kTileRows = 256;     // grid rows per count/scan tile
+constexpr int kThreads = 256;      // threads per CTA of the row kernels
+
+struct Grid {
+    int nx, ny, nz;
+    int W;                 // 32-bit words per bit row
+    long long R;           // grid rows = ny*nz
+    float sp[3], zp[3];
+};
+
+// Per-case data derived from the packed triangle table when a context is
+// created, resident in device memory and staged into shared memory per CTA.
+struct CaseTables {
+    uint64_t tris[256];    // packed triangle lists (case_table.h)
+    uint64_t order[256];   // cube edges in order of first appearance in the
+                           // triangle list, packed like tris (count in 60..63)
+    uint16_t cut[256];     // 12-bit mask of the cut cube edges of the case
+};
+
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
+
+__device__ __forceinline__ uint32_t lowmask(int pos)  // bits [0, pos), pos in [0, 32]
+{
+    return (uint32_t)((1ull << pos) - 1ull);
+}
+
+// Mask of valid bit positions of word w when only indices < limit exist.
+__device__ __forceinline__ uint32_t validmask(int w, int limit)
+{
+    int rem = limit - 32 * w;
+    if (rem >= 32) return 0xffffffffu;
+    if (rem <= 0) return 0u;
+    return lowmask(rem);
+}
+
+// Group-level (width G lanes) inclusive scan.
+template <int G>
+__device__ __forceinline__ uint32_t group_incl_scan(uint32_t v, int lig, unsigned mask)
+{
+#pragma unroll
+    for (int d = 1; d < G; d <<= 1) {
+        uint32_t t = __shfl_up_sync(mask, v, d, G);
+        if (lig >= d) v += t;
+    }
+    return v;
+}
+
+template <int G>
+__device__ __forceinline__ uint32_t group_bcast(uint32_t v, int src, unsigned mask)
+{
+    return __shfl_sync(mask, v, src, G);
+}
+
+template <int G>
+__device__ __forceinline__ uint32_t group_min(uint32_t v, unsigned mask)
+{
+#pragma unroll
+    for (int d = G / 2; d > 0; d >>= 1) v = min(v, __shfl_xor_sync(mask, v, d, G));
+    return v;
+}
+
+template <int G>
+__device__ __forceinline__ uint32_t group_max(uint32_t v, unsigned mask)
+{
+#pragma unroll
+    for (int d = G / 2; d > 0; d >>= 1) v = max(v, __shfl_xor_sync(mask, v, d, G));
+    return v;
+}
+
+// Value of the volume at grid point (i, j, k).
+__device__ __forceinline__ float vload(const float* __restrict__ vol, const Grid& g, int i, int j, int k)
+{
+    return __ldg(vol + ((long long)k * g.ny + j) * g.nx + i);
+}
+
+// One component of the (negated, unnormalised) gradient at a grid point along
+// one axis: Image3D::computeGradient (flyingEdges/util/Image3D.cpp:116-188).
+// prev/here/next are the values at p-1, p, p+1 along that axis.
+__device__ __forceinline__ float grad_component(float prev, float here, float next, int p, int n, float sp)
+{
+    if (p == 0) return fdiv(fsub(here, next), sp);
+    if (p == n - 1) return fdiv(fsub(prev, here), sp);
+    return fdiv(fsub(prev, next), fmul(2.0f, sp));
+}
+
+__device__ __forceinline__ float3 gradient_at(const float* __restrict__ vol, const Grid& g, int i, int j, int k)
+{
+    const long long sy = g.nx, sz = (long long)g.nx * g.ny;
+    const float* p = vol + (long long)k * sz + (long long)j * sy + i;
+    float here = __ldg(p);
+    float xm = i > 0 ? __ldg(p - 1) : 0.f, xp = i < g.nx - 1 ? __ldg(p + 1) : 0.f;
+    float ym = j > 0 ? __ldg(p - sy) : 0.f, yp = j < g.ny - 1 ? __ldg(p + sy) : 0.f;
+    float zm = k > 0 ? __ldg(p - sz) : 0.f, zp = k < g.nz - 1 ? __ldg(p + sz) : 0.f;
+    float3 r;
+    r.x = grad_component(xm, here, xp, i, g.nx, g.sp[0]);
+    r.y = grad_component(ym, here, yp, j, g.ny, g.sp[1]);
+    r.z = grad_component(zm, here, zp, k, g.nz, g.sp[2]);
+    return r;
+}
+
+// Coordinate of grid index p along axis a when the cube that computes the
+// vertex has base index `base` and the point is at offset p-base (0 or 1) from
+// it: Image3D::getPosCube (flyingEdges/util/Image3D.cpp:45-87) forms
+// zeroPos + base*spacing and adds spacing once for the far corner.
+__device__ __forceinline__ float cube_coord(int base, int off, float zp, float sp)
+{
+    float c = fadd(zp, fmul((float)base, sp));
+    return off ? fadd(c, sp) : c;
+}
+
+// interpolate() of FlyingEdgesAlgorithm.cpp:637-647 for one component.
+__device__ __forceinline__ float lerp_ref(float a, float b, float w)
+{
+    return fadd(a, fmul(w, fsub(b, a)));
+}
+
+// Point and normal of the vertex on the edge from grid point (i,j,k) along
+// `axis` (0=x,1=y,2=z), computed by the cube whose base is (ci,cj,ck).
+// The edge runs from its lower to its higher grid point, as every entry of
+// edgeVertices does (MarchingCubesTables.h:563).
+__device__ __forceinline__ void edge_vertex(const float* __restrict__ vol, const Grid& g, float iso,
+                                            int axis, int i, int j, int k, int ci, int cj, int ck,
+                                            float3& pos, float3& nrm)
+{
+    const int i1 = i + (axis == 0), j1 = j + (axis == 1), k1 = k + (axis == 2);
+    const float v0 = vload(vol, g, i, j, k);
+    const float v1 = vload(vol, g, i1, j1, k1);
+    const float w = fdiv(fsub(iso, v0), fsub(v1, v0));
+    const float ax0 = cube_coord(ci, i - ci, g.zp[0], g.sp[0]);
+    const float ay0 = cube_coord(cj, j - cj, g.zp[1], g.sp[1]);
+    const float az0 = cube_coord(ck, k - ck, g.zp[2], g.sp[2]);
+    const float ax1 = cube_coord(ci, i1 - ci, g.zp[0], g.sp[0]);
+    const float ay1 = cube_coord(cj, j1 - cj, g.zp[1], g.sp[1]);
+    const float az1 = cube_coord(ck, k1 - ck, g.zp[2], g.sp[2]);
+    pos.x = lerp_ref(ax0, ax1, w);
+    pos.y = lerp_ref(ay0, ay1, w);
+    pos.z = lerp_ref(az0, az1, w);
+    const float3 g0 = gradient_at(vol, g, i, j, k);
+    const float3 g1 = gradient_at(vol, g, i1, j1, k1);
+    nrm.x = lerp_ref(g0.x, g1.x, w);
+    nrm.y = lerp_ref(g0.y, g1.y, w);
+    nrm.z = lerp_ref(g0.z, g1.z, w);
+}
+
+// ---------------------------------------------------------------------------
+// Row context: the four bit rows a cell row touches, one 32-bit word per lane.
+//   A = (j,k)  B = (j+1,k)  C = (j,k+1)  D = (j+1,k+1)
+// "sh" words hold bit i+1 at position i (the next word supplies bit 31).
+// ---------------------------------------------------------------------------
+struct RowWords {
+    uint32_t a, b, c, d;
+    uint32_t ash, bsh, csh, dsh;
+};
+
+__device__ __forceinline__ uint32_t load_word(const uint32_t* __restrict__ row, int w, int W, bool ok)
+{
+    return (ok && w < W) ? __ldg(row + w) : 0u;
+}
+
+__device__ __forceinline__ RowWords load_row_words(const uint32_t* __restrict__ bits, const Grid& g,
+                                                   long long r, int w, bool valid, bool hasY, bool hasZ)
+{
+    RowWords rw;
+    const uint32_t* A = bits + r * g.W;
+    const uint32_t* B = A + g.W;
+    const uint32_t* C = A + (long long)g.ny * g.W;
+    const uint32_t* D = C + g.W;
+    const bool cell = hasY && hasZ;
+    rw.a = load_word(A, w, g.W, valid);
+    rw.b = load_word(B, w, g.W, hasY);
+    rw.c = load_word(C, w, g.W, hasZ);
+    rw.d = load_word(D, w, g.W, cell);
+    const uint32_t an = load_word(A, w + 1, g.W, valid);
+    const uint32_t bn = load_word(B, w + 1, g.W, hasY);
+    const uint32_t cn = load_word(C, w + 1, g.W, hasZ);
+    const uint32_t dn = load_word(D, w + 1, g.W, cell);
+    rw.ash = (rw.a >> 1) | (an << 31);
+    rw.bsh = (rw.b >> 1) | (bn << 31);
+    rw.csh = (rw.c >> 1) | (cn << 31);
+    rw.dsh = (rw.d >> 1) | (dn << 31);
+    return rw;
+}
+
+// Cells i of the word whose 8 corners are not all on the same side.
+__device__ __forceinline__ uint32_t active_cells(const RowWords& rw, uint32_t cellvalid)
+{
+    const uint32_t and4 = rw.a & rw.b & rw.c & rw.d;
+    const uint32_t and4s = rw.ash & rw.bsh & rw.csh & rw.dsh;
+    const uint32_t or4 = rw.a | rw.b | rw.c | rw.d;
+    const uint32_t or4s = rw.ash | rw.bsh | rw.csh | rw.dsh;
+    return ~((and4 & and4s) | ~(or4 | or4s)) & cellvalid;
+}
+
+// Cube case of cell i of the word: bit v set <=> corner v >= isovalue
+// (calcCubeCase, FlyingEdgesAlgorithm.cpp:576-604; findCaseId, util.h:24-42).
+__device__ __forceinline__ int cube_case(const RowWords& rw, int bit)
+{
+    return (int)(((rw.a >> bit) & 1u) | (((rw.ash >> bit) & 1u) << 1) | (((rw.bsh >> bit) & 1u) << 2) |
+                 (((rw.b >> bit) & 1u) << 3) | (((rw.c >> bit) & 1u) << 4) | (((rw.csh >> bit) & 1u) << 5) |
+                 (((rw.dsh >> bit) & 1u) << 6) | (((rw.d >> bit) & 1u) << 7));
+}
+
+// The eight cut masks of a cell row (one word of each), from which the
+// Flying Edges vertex id of any of the 12 edges of a cell is a popc rank.
+struct CutMasks {
+    uint32_t xA, xB, xC, xD;   // x-edges of rows A..D, bit i = edge (i, i+1)
+    uint32_t yA, yC;           // y-edges A->B and C->D, bit i = point i
+    uint32_t zA, zB;           // z-edges A->C and B->D, bit i = point i
+};
+
+__device__ __forceinline__ CutMasks cut_masks(const RowWords& rw, uint32_t evalid, uint32_t pvalid, bool hasY,
+                                              bool hasZ)
+{
+    const bool cell = hasY && hasZ;
+    CutMasks m;
+    m.xA = (rw.a ^ rw.ash) & evalid;
+    m.yA = hasY ? ((rw.a ^ rw.b) & pvalid) : 0u;
+    m.zA = hasZ ? ((rw.a ^ rw.c) & pvalid) : 0u;
+    m.xB = cell ? ((rw.b ^ rw.bsh) & evalid) : 0u;
+    m.xC = cell ? ((rw.c ^ rw.csh) & evalid) : 0u;
+    m.xD = cell ? ((rw.d ^ rw.dsh) & evalid) : 0u;
+    m.yC = cell ? ((rw.c ^ rw.d) & pvalid) : 0u;
+    m.zB = cell ? ((rw.b ^ rw.d) & pvalid) : 0u;
+    return m;
+}
+
+// Flying Edges vertex ids of the first cut edge of each mask at this word
+// (row start + prefix inside the row).
+struct CutBases {
+    unsigned long long xA, xB, xC, xD, yA, yC, zA, zB;
+};
+
+// Flying Edges vertex id of cube edge e of cell `bit` of the word.
+__device__ __forceinline__ unsigned long long fe_edge_id(const CutMasks& m, const CutBases& b, int e, int bit)
+{
+    switch (e) {
+        case 0: return b.xA + __popc(m.xA & lowmask(bit));
+        case 2: return b.xB + __popc(m.xB & lowmask(bit));
+        case 4: return b.xC + __popc(m.xC & lowmask(bit));
+        case 6: return b.xD + __popc(m.xD & lowmask(bit));
+        case 3: return b.yA + __popc(m.yA & lowmask(bit));
+        case 1: return b.yA + __popc(m.yA & lowmask(bit + 1));
+        case 7: return b.yC + __popc(m.yC & lowmask(bit));
+        case 5: return b.yC + __popc(m.yC & lowmask(bit + 1));
+        case 8: return b.zA + __popc(m.zA & lowmask(bit));
+        case 9: return b.zA + __popc(m.zA & lowmask(bit + 1));
+        case 10: return b.zB + __popc(m.zB & lowmask(bit));
+        default: return b.zB + __popc(m.zB & lowmask(bit + 1));
+    }
+}
+
+// Low grid point and axis of cube edge e of cell (0,0,0).
+__device__ __forceinline__ void cube_edge_geometry(int e, int& dx, int& dy, int& dz, int& axis)
+{
+    // e:      0  1  2  3  4  5  6  7  8  9 10 11
+    // dx:     0  1  0  0  0  1  0  0  0  1  0  1
+    // dy:     0  0  1  0  0  0  1  0  0  0  1  1
+    // dz:     0  0  0  0  1  1  1  1  0  0  0  0
+    // axis:   x  y  x  y  x  y  x  y  z  z  z  z
+    dx = (0xA22 >> e) & 1;
+    dy = (0xC44 >> e) & 1;
+    dz = (0x0F0 >> e) & 1;
+    axis = e >= 8 ? 2 : (e & 1);
+}
+
+// Shared memory copy of the case tables.
+struct SharedCases {
+    uint64_t tris[256];
+    uint64_t order[256];
+    uint16_t cut[256];
+};
+
+__device__ __forceinline__ void stage_cases(SharedCases& s, const CaseTables* __restrict__ t, bool need_order)
+{
+    for (int c = threadIdx.x; c < 256; c += blockDim.x) {
+        s.tris[c] = t->tris[c];
+        if (need_order) {
+            s.order[c] = t->order[c];
+            s.cut[c] = t->cut[c];
+        }
+    }
+    __syncthreads();
+}
+
+// Start offset of grid row r in one of the scanned count arrays
+// (comp 0: Flying Edges vertices, 1: triangles, 2: MC vertices).
+__device__ __forceinline__ unsigned long long row_base(const unsigned long long* __restrict__ tiles_a,
+                                                       const uint4* __restrict__ rowpre, long long r, int comp)
+{
+    const uint4 p = __ldg(&rowpre[r]);
+    return __ldg(tiles_a + r / kTileRows) + (comp == 0 ? p.x : (comp == 1 ? p.y : p.z));
+}
+
+// Marching-cubes owned-edge mask of a cell (first-reference rule of
+// marchingCubes/serial/main.cpp:139-177): an edge belongs to the adjacent
+// cell with the smallest linear index.  Interior cells own e5, e6, e11.
+__device__ __forceinline__ uint32_t mc_owned_edges(bool i0, bool j0, bool k0)
+{
+    uint32_t m = (1u << 5) | (1u << 6) | (1u << 11);
+    if (k0) m |= (1u << 1) | (1u << 2);
+    if (j0) m |= (1u << 4) | (1u << 9);
+    if (j0 && k0) m |= 1u << 0;
+    if (i0) m |= (1u << 7) | (1u << 10);
+    if (i0 && k0) m |= 1u << 3;
+    if (i0 && j0) m |= 1u << 8;
+    return m;
+}
+
+}  // namespace iso

@@ -1,0 +1,210 @@
+/*
+ * Marching Cubes oracle -- TEST INFRASTRUCTURE ONLY (see oracle.h).
+ *
+ * Restates marchingCubes/serial/main.cpp:42-192: cells are visited in
+ * (k, j, i) order; a vertex is created the first time a triangle corner
+ * references its global edge (marchingCubes/util/Image3D.cpp:168-256), using
+ * the cube of the referencing cell for position and gradient
+ * (marchingCubes/util/Image3D.cpp:22-166, util.h:24-54).  The reference's
+ * std::unordered_map is replaced by an open-addressing table with the same
+ * lookup semantics.
+ */
+#include "oracle.h"
+#include "case_table.h"
+
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+static const unsigned char kLo[12] = {0, 1, 3, 0, 4, 5, 7, 4, 0, 1, 3, 2};
+static const unsigned char kHi[12] = {1, 2, 2, 3, 5, 6, 6, 7, 4, 5, 7, 6};
+
+static double g_mc_wall;
+
+static double now_s(void)
+{
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+typedef struct {
+    size_t* keys;   /* key+1, 0 = empty */
+    size_t* vals;
+    size_t cap, size;
+} edge_map;
+
+static size_t mix(size_t x)
+{
+    x ^= x >> 33; x *= 0xff51afd7ed558ccdULL;
+    x ^= x >> 33; x *= 0xc4ceb9fe1a85ec53ULL;
+    x ^= x >> 33;
+    return x;
+}
+
+static void map_init(edge_map* m, size_t cap)
+{
+    m->cap = 1024;
+    while (m->cap < cap) m->cap <<= 1;
+    m->keys = (size_t*)calloc(m->cap, sizeof(size_t));
+    m->vals = (size_t*)malloc(m->cap * sizeof(size_t));
+    m->size = 0;
+}
+
+static void map_grow(edge_map* m);
+
+/* Returns 1 and sets *val when present, else inserts (key -> val_if_new). */
+static int map_find_or_insert(edge_map* m, size_t key, size_t val_if_new, size_t* val)
+{
+    if (2 * (m->size + 1) > m->cap) map_grow(m);
+    size_t mask = m->cap - 1, h = mix(key) & mask;
+    for (;;) {
+        if (m->keys[h] == 0) {
+            m->keys[h] = key + 1;
+            m->vals[h] = val_if_new;
+            m->size++;
+            *val = val_if_new;
+            return 0;
+        }
+        if (m->keys[h] == key + 1) { *val = m->vals[h]; return 1; }
+        h = (h + 1) & mask;
+    }
+}
+
+static void map_grow(edge_map* m)
+{
+    edge_map n;
+    map_init(&n, m->cap * 2);
+    for (size_t s = 0; s < m->cap; ++s) {
+        if (m->keys[s]) {
+            size_t v;
+            map_find_or_insert(&n, m->keys[s] - 1, m->vals[s], &v);
+        }
+    }
+    free(m->keys); free(m->vals);
+    *m = n;
+}
+
+typedef struct {
+    float* p; size_t n, cap;
+} fvec;
+typedef struct {
+    size_t* p; size_t n, cap;
+} svec;
+
+static void fpush3(fvec* v, const float x[3])
+{
+    if (v->n + 3 > v->cap) {
+        v->cap = v->cap ? 2 * v->cap : 3 * 1024;
+        v->p = (float*)realloc(v->p, v->cap * sizeof(float));
+    }
+    v->p[v->n++] = x[0]; v->p[v->n++] = x[1]; v->p[v->n++] = x[2];
+}
+static void spush(svec* v, size_t x)
+{
+    if (v->n + 1 > v->cap) {
+        v->cap = v->cap ? 2 * v->cap : 1024;
+        v->p = (size_t*)realloc(v->p, v->cap * sizeof(size_t));
+    }
+    v->p[v->n++] = x;
+}
+
+int oracle_mc_run(const float* data, const size_t dims[3], const float spacing[3],
+                  const float origin[3], float iso, oracle_mesh* out)
+{
+    memset(out, 0, sizeof(*out));
+    size_t nx = dims[0], ny = dims[1], nz = dims[2];
+    if (nx < 2 || ny < 2 || nz < 2) { g_mc_wall = 0.0; return 0; }
+    double t0 = now_s();
+    size_t nX = (nx - 1) * ny * nz, nY = nx * (ny - 1) * nz;
+    edge_map map;
+    map_init(&map, 1 << 16);
+    fvec pts = {0}, nrm = {0};
+    svec tris = {0}, eov = {0};
+    size_t pt_idx = 0;
+    static const int dx[8] = {0, 1, 1, 0, 0, 1, 1, 0};
+    static const int dy[8] = {0, 0, 1, 1, 0, 0, 1, 1};
+    static const int dz[8] = {0, 0, 0, 0, 1, 1, 1, 1};
+    /* per cube edge: offset of the edge's low end, and axis */
+    static const int ex[12] = {0, 1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 1};
+    static const int ey[12] = {0, 0, 1, 0, 0, 0, 1, 0, 0, 0, 1, 1};
+    static const int ez[12] = {0, 0, 0, 0, 1, 1, 1, 1, 0, 0, 0, 0};
+    static const int axis[12] = {0, 1, 0, 1, 0, 1, 0, 1, 2, 2, 2, 2};
+#define V(i, j, k) data[(k) * nx * ny + (j) * nx + (i)]
+    for (size_t k = 0; k + 1 < nz; ++k)
+    for (size_t j = 0; j + 1 < ny; ++j)
+    for (size_t i = 0; i + 1 < nx; ++i) {
+        float vals[8];
+        int c = 0;
+        for (int v = 0; v < 8; ++v) {
+            vals[v] = V(i + dx[v], j + dy[v], k + dz[v]);
+            if (vals[v] >= iso) c |= 1 << v;   /* util::findCaseId, util.h:24-42 */
+        }
+        if (c == 0 || c == 255) continue;
+        /* getPosCube (marchingCubes/util/Image3D.cpp:22-65) */
+        float xpos = origin[0] + (float)i * spacing[0];
+        float ypos = origin[1] + (float)j * spacing[1];
+        float zpos = origin[2] + (float)k * spacing[2];
+        float x1 = xpos + spacing[0], y1 = ypos + spacing[1], z1 = zpos + spacing[2];
+        float pc[8][3] = {{xpos, ypos, zpos}, {x1, ypos, zpos}, {x1, y1, zpos}, {xpos, y1, zpos},
+                          {xpos, ypos, z1}, {x1, ypos, z1}, {x1, y1, z1}, {xpos, y1, z1}};
+        /* getGradCube / computeGradient (Image3D.cpp:67-166) */
+        float gc[8][3];
+        for (int v = 0; v < 8; ++v) {
+            size_t p[3] = {i + dx[v], j + dy[v], k + dz[v]};
+            size_t n[3] = {nx, ny, nz};
+            for (int a = 0; a < 3; ++a) {
+                size_t q0[3] = {p[0], p[1], p[2]}, q1[3] = {p[0], p[1], p[2]};
+                float run;
+                if (p[a] == 0) { q0[a] = 1; q1[a] = 0; run = spacing[a]; }
+                else if (p[a] == n[a] - 1) { q1[a] = p[a] - 1; run = spacing[a]; }
+                else { q0[a] = p[a] + 1; q1[a] = p[a] - 1; run = 2 * spacing[a]; }
+                gc[v][a] = (V(q1[0], q1[1], q1[2]) - V(q0[0], q0[1], q0[2])) / run;
+            }
+        }
+        int ntri = (int)strlen(kOracleCases[c]) / 3;
+        for (int t = 0; t < ntri; ++t) {
+            size_t tri[3];
+            for (int q = 0; q < 3; ++q) {
+                char ch = kOracleCases[c][3 * t + q];
+                int e = ch <= '9' ? ch - '0' : ch - 'a' + 10;
+                size_t x = i + ex[e], y = j + ey[e], z = k + ez[e];
+                size_t gid;
+                if (axis[e] == 0) gid = x + (nx - 1) * y + ny * (nx - 1) * z;
+                else if (axis[e] == 1) gid = nX + x + nx * y + nx * (ny - 1) * z;
+                else gid = nX + nY + x + nx * y + nx * ny * z;
+                size_t found;
+                if (map_find_or_insert(&map, gid, pt_idx, &found)) {
+                    tri[q] = found;
+                } else {
+                    tri[q] = pt_idx++;
+                    int v1 = kLo[e], v2 = kHi[e];
+                    float w = (iso - vals[v1]) / (vals[v2] - vals[v1]);
+                    float np[3], nn[3];
+                    for (int a = 0; a < 3; ++a) {
+                        np[a] = pc[v1][a] + (w * (pc[v2][a] - pc[v1][a]));
+                        nn[a] = gc[v1][a] + (w * (gc[v2][a] - gc[v1][a]));
+                    }
+                    fpush3(&pts, np);
+                    fpush3(&nrm, nn);
+                    spush(&eov, gid);
+                }
+            }
+            if (tri[0] != tri[1] && tri[1] != tri[2] && tri[2] != tri[0]) {
+                spush(&tris, tri[0]); spush(&tris, tri[1]); spush(&tris, tri[2]);
+            }
+        }
+    }
+#undef V
+    free(map.keys); free(map.vals);
+    out->n_points = pt_idx;
+    out->n_tris = tris.n / 3;
+    out->points = pts.p ? pts.p : (float*)calloc(1, sizeof(float));
+    out->normals = nrm.p ? nrm.p : (float*)calloc(1, sizeof(float));
+    out->tris = tris.p ? tris.p : (size_t*)calloc(1, sizeof(size_t));
+    out->edge_of_vertex = eov.p ? eov.p : (size_t*)calloc(1, sizeof(size_t));
+    g_mc_wall = now_s() - t0;
+    return 0;
+}
+
+double oracle_mc_last_wall_seconds(void) { return g_mc_wall; }

@@ -1,0 +1,77 @@
+/*
+ * Oracle for the isosurface hot path -- TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C restatement of miniIsosurface's serial Flying Edges
+ * (flyingEdges/serial/FlyingEdgesAlgorithm.cpp) and serial Marching Cubes
+ * (marchingCubes/serial/main.cpp:42-192).  It is used by the tests, by
+ * smoke() and by the CPU-baseline leg of bench.py as the checker and as the
+ * CPU timing baseline.  Nothing in the product links or calls it.
+ *
+ * Parity pin: the restatement is checked against the reference executables
+ * themselves (compiled from the reference sources by oracle/build_ref.sh)
+ * and against the committed golden fixtures in tests/golden/.
+ *
+ * Floating point follows the reference exactly: float32 arithmetic, no FMA
+ * contraction (this library is compiled with -ffp-contract=off).
+ */
+#ifndef ISO_ORACLE_H
+#define ISO_ORACLE_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* One output mesh: points / normals V x 3 float (AoS), tris T x 3 size_t.
+ * edge_of_vertex[v] is the global edge id the vertex lies on, numbered like
+ * marchingCubes/util/Image3D.cpp:210-256 (x-edges, then y-edges, then z). */
+typedef struct oracle_mesh {
+    size_t n_points;
+    size_t n_tris;
+    float* points;
+    float* normals;
+    size_t* tris;
+    size_t* edge_of_vertex;
+} oracle_mesh;
+
+typedef struct oracle_fe oracle_fe;
+
+/* Flying Edges, pass by pass (flyingEdges/serial/FlyingEdgesAlgorithm.h:29-49). */
+oracle_fe* oracle_fe_create(const float* data, const size_t dims[3],
+                            const float spacing[3], const float origin[3],
+                            float isoval, int nthreads);
+void oracle_fe_pass1(oracle_fe* fe);
+void oracle_fe_pass2(oracle_fe* fe);
+void oracle_fe_pass3(oracle_fe* fe);
+void oracle_fe_pass4(oracle_fe* fe);
+/* gridEdges as ny*nz records {xl, xr, xstart, ystart, zstart}. */
+void oracle_fe_grid_edges(const oracle_fe* fe, size_t* out);
+/* triCounter, (ny-1)*(nz-1) entries (counts after pass 2, offsets after pass 3). */
+void oracle_fe_tri_counter(const oracle_fe* fe, size_t* out);
+/* cubeCases, (nx-1)*(ny-1)*(nz-1) bytes (only trimmed ranges are written). */
+void oracle_fe_cube_cases(const oracle_fe* fe, unsigned char* out);
+/* moveOutput(): hands the mesh over; the oracle keeps nothing. */
+void oracle_fe_take(oracle_fe* fe, oracle_mesh* out);
+void oracle_fe_destroy(oracle_fe* fe);
+
+/* All four passes in one call. */
+int oracle_fe_run(const float* data, const size_t dims[3], const float spacing[3],
+                  const float origin[3], float isoval, int nthreads, oracle_mesh* out);
+
+/* Serial marching cubes with first-reference vertex numbering. */
+int oracle_mc_run(const float* data, const size_t dims[3], const float spacing[3],
+                  const float origin[3], float isoval, oracle_mesh* out);
+
+void oracle_mesh_free(oracle_mesh* m);
+
+/* Seconds of wall time of the last oracle_fe_run / oracle_mc_run call
+ * (extraction only, like the reference's "Total Program WALL Time"). */
+double oracle_last_wall_seconds(void);
+double oracle_mc_last_wall_seconds(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

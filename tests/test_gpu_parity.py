@@ -1,0 +1,259 @@
+"""GPU parity: the CUDA path (through the C ABI) against the oracle.
+
+Bar: triangle count, connectivity and vertex numbering bit-exact; points and
+normals bit-identical float32 (the kernels evaluate the reference's float
+formulas in the same order with no FMA contraction; the stated tolerance of
+2 ulp is never needed).
+"""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+import oracle_lib
+
+pytestmark = pytest.mark.gpu
+
+POS_ULP_TOL = 0  # measured: 0 ulp; the contract allows 2
+
+
+def ulp_diff(a, b):
+    ia = a.view(np.int32).astype(np.int64)
+    ib = b.view(np.int32).astype(np.int64)
+    ia = np.where(ia < 0, np.int64(-2**31) - ia, ia)
+    ib = np.where(ib < 0, np.int64(-2**31) - ib, ib)
+    return np.abs(ia - ib)
+
+
+def assert_same_mesh(got, ref, what=""):
+    p, n, t = got
+    rp, rn, rt = ref[:3]
+    assert p.shape == rp.shape, "%s vertex count %s vs %s" % (what, p.shape, rp.shape)
+    assert t.shape == rt.shape, "%s triangle count %s vs %s" % (what, t.shape, rt.shape)
+    assert np.array_equal(t.astype(np.uint64), rt.astype(np.uint64)), "%s connectivity differs" % what
+    if p.size:
+        assert ulp_diff(p, rp).max() <= POS_ULP_TOL, "%s points differ" % what
+        assert ulp_diff(n, rn).max() <= POS_ULP_TOL, "%s normals differ" % what
+
+
+def gpu_extract(M, vol, iso, algo, spacing=(1, 1, 1), origin=(0, 0, 0), index_bytes=4, offset=0):
+    import torch
+
+    nz, ny, nx = vol.shape
+    flat = torch.from_numpy(np.ascontiguousarray(vol).reshape(-1)).cuda()
+    if offset:
+        buf = torch.empty(flat.numel() + offset, dtype=torch.float32, device="cuda")
+        buf[offset:] = flat
+        flat = buf[offset:]
+    mesh = M.extract_device(flat, (nx, ny, nz), iso, algo, spacing, origin, index_bytes=index_bytes)
+    torch.cuda.synchronize()
+    return (mesh.points[: mesh.n_points].cpu().numpy(), mesh.normals[: mesh.n_points].cpu().numpy(),
+            mesh.tris[: mesh.n_tris].cpu().numpy().astype(np.uint64))
+
+
+def both(M, vol, iso, spacing=(1, 1, 1), origin=(0, 0, 0), **kw):
+    got = gpu_extract(M, vol, iso, M.FLYING_EDGES, spacing, origin, **kw)
+    assert_same_mesh(got, oracle_lib.fe(vol, iso, spacing, origin), "FE")
+    got = gpu_extract(M, vol, iso, M.MARCHING_CUBES, spacing, origin, **kw)
+    assert_same_mesh(got, oracle_lib.mc(vol, iso, spacing, origin), "MC")
+
+
+@pytest.fixture(scope="module")
+def M(cuda):
+    import miniisosurface_gb300 as M
+    return M
+
+
+def test_blobs_config0_128(M):
+    vol = M.generate_blobs((128, 128, 128), 8, seed=0)
+    both(M, vol, 0.5)
+
+
+def test_blobs_spacing_origin(M):
+    vol = M.generate_blobs((40, 33, 27), 8, seed=3)
+    both(M, vol, 0.5, (0.1, 0.37, 1.3), (-2.5, 0.3, 7.1))
+    both(M, vol, 0.31, (2.0, 0.5, 0.03125), (1e3, -7.25, 0.0))
+
+
+def test_noise_nonaligned_rows(M):
+    vol = M.generate_value_noise((61, 47, 35), 4, 16, seed=5)
+    both(M, vol, 0.0)
+    both(M, vol, 0.2, (0.3, 0.3, 0.3), (0.1, 0.2, 0.3))
+
+
+def test_unaligned_volume_pointer(M):
+    vol = M.generate_value_noise((64, 20, 20), 3, 8, seed=9)
+    both(M, vol, 0.05, offset=1)
+
+
+def test_wide_rows_multi_chunk(M):
+    # nx > 32*32 points: rows span several 32-word chunks
+    vol = M.generate_value_noise((1500, 5, 4), 4, 16, seed=11)
+    both(M, vol, 0.0)
+    vol = M.generate_value_noise((1029, 3, 3), 4, 8, seed=12)
+    both(M, vol, 0.1)
+
+
+@pytest.mark.parametrize("dims", [(2, 2, 2), (2, 9, 5), (3, 2, 7), (33, 2, 2), (5, 6, 2), (31, 32, 33), (32, 17, 9),
+                                  (65, 3, 4), (97, 11, 13)])
+def test_random_small(M, dims):
+    rng = np.random.default_rng(sum(dims))
+    nx, ny, nz = dims
+    for trial in range(3):
+        vol = rng.standard_normal((nz, ny, nx)).astype(np.float32)
+        iso = float(rng.uniform(-0.5, 0.5))
+        both(M, vol, iso, tuple(rng.uniform(0.1, 2.0, 3)), tuple(rng.uniform(-5, 5, 3)))
+
+
+def test_ties_equal_isovalue(M):
+    # integer field, isovalue hit exactly: classification uses >=
+    rng = np.random.default_rng(1)
+    vol = rng.integers(-2, 3, size=(13, 11, 17)).astype(np.float32)
+    for iso in (-1.0, 0.0, 1.0, 2.0):
+        both(M, vol, iso)
+
+
+def test_all_256_cube_cases(M):
+    for c in range(256):
+        vol = np.zeros((2, 2, 2), np.float32)
+        corner = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)]
+        for v, (i, j, k) in enumerate(corner):
+            vol[k, j, i] = 1.0 + 0.25 * v if (c >> v) & 1 else -1.0 - 0.125 * v
+        both(M, vol, 0.0)
+
+
+def test_empty_meshes(M):
+    vol = np.ones((8, 9, 10), np.float32)
+    for iso in (0.5, 2.0):          # all above / all below
+        both(M, vol, iso)
+    for dims in [(1, 5, 5), (5, 1, 5), (5, 5, 1)]:   # degenerate grids
+        vol = np.random.default_rng(0).standard_normal(dims[::-1]).astype(np.float32)
+        got = gpu_extract(M, vol, 0.0, M.FLYING_EDGES)
+        assert got[0].shape == (0, 3) and got[2].shape == (0, 3)
+
+
+def test_index_widths_agree(M):
+    vol = M.generate_value_noise((48, 40, 36), 4, 16, seed=2)
+    for algo in (M.FLYING_EDGES, M.MARCHING_CUBES):
+        a = gpu_extract(M, vol, 0.0, algo, index_bytes=4)
+        b = gpu_extract(M, vol, 0.0, algo, index_bytes=8)
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y)
+
+
+def test_host_entry_point(M):
+    vol = M.generate_blobs((50, 41, 37), 8, seed=4)
+    img = M.Image3D.from_array(vol, (0.5, 0.5, 2.0), (1.0, -1.0, 0.5))
+    for algo, ref in ((M.FLYING_EDGES, oracle_lib.fe), (M.MARCHING_CUBES, oracle_lib.mc)):
+        m = M.extract(img, 0.5, algo)
+        assert_same_mesh((m.points, m.normals, m.triangles), ref(vol, 0.5, img.spacing, img.zeroPos))
+    m = M.MarchingCubes(img, 0.5)
+    assert_same_mesh((m.points, m.normals, m.triangles), oracle_lib.mc(vol, 0.5, img.spacing, img.zeroPos))
+
+
+def test_fe_pass_by_pass_state(M):
+    """gridEdges (xl, xr, xstart, ystart, zstart) and triCounter after pass 2
+    and pass 3 equal the reference algorithm's state."""
+    vol = M.generate_value_noise((45, 30, 22), 4, 16, seed=8)
+    img = M.Image3D.from_array(vol)
+    fe = M.FlyingEdgesAlgorithm(img, 0.1)
+    fe.pass1()
+    fe.pass2()
+    ge2, tc2 = fe.gridEdges()
+    fe.pass3()
+    ge3, tc3 = fe.gridEdges()
+    fe.pass4()
+    mesh = fe.moveOutput()
+    rge2, rtc2, rge3, rtc3 = oracle_lib.fe_passes(vol, 0.1)
+    assert np.array_equal(ge2, rge2)
+    assert np.array_equal(tc2, rtc2)
+    assert np.array_equal(ge3, rge3)
+    assert np.array_equal(tc3, rtc3)
+    assert_same_mesh((mesh.points, mesh.normals, mesh.triangles), oracle_lib.fe(vol, 0.1))
+
+
+def test_capacity_error_reports_sizes(M):
+    import torch
+    from miniisosurface_gb300 import _lib
+
+    vol = M.generate_blobs((32, 32, 32), 8, seed=1)
+    flat = torch.from_numpy(vol.reshape(-1)).cuda()
+    small = M.DeviceMesh(10, 10, 4)
+    m = small.descriptor()
+    g = M.make_grid((32, 32, 32))
+    lib = _lib.load()
+    ctx = M.default_context(0)
+    st = lib.iso_extract_device(ctx.handle, M.FLYING_EDGES, flat.data_ptr(), C.byref(g), C.c_float(0.5),
+                                C.byref(m), None)
+    assert st == _lib.ISO_ERR_CAPACITY
+    rp, rn, rt, _ = oracle_lib.fe(vol, 0.5)
+    assert (m.n_points, m.n_tris) == (rp.shape[0], rt.shape[0])
+    nv, nt = M.count_device(flat, (32, 32, 32), 0.5)
+    assert (nv, nt) == (rp.shape[0], rt.shape[0])
+
+
+def test_fp64_interpolation_error(M):
+    """Max error of the float32 points/normals against the same formulas in
+    double precision (reported; bounded by a few float32 ulps of the field)."""
+    vol = M.generate_blobs((64, 64, 64), 8, seed=2)
+    sp, org = (0.7, 0.3, 1.1), (-1.0, 2.0, 0.5)
+    p, n, t = gpu_extract(M, vol, 0.5, M.FLYING_EDGES, sp, org)
+    _, _, _, eov = oracle_lib.fe(vol, 0.5, sp, org)
+    nz, ny, nx = vol.shape
+    nX = (nx - 1) * ny * nz
+    nY = nx * (ny - 1) * nz
+    e = eov.astype(np.int64)
+    axis = np.where(e < nX, 0, np.where(e < nX + nY, 1, 2))
+    loc = np.where(axis == 0, e, np.where(axis == 1, e - nX, e - nX - nY))
+    ex = np.array([nx - 1, nx, nx])[axis]
+    ey = np.array([ny, ny - 1, ny])[axis]
+    i = loc % ex
+    j = (loc // ex) % ey
+    k = loc // (ex * ey)
+    V = vol.astype(np.float64)
+    d = np.stack([axis == 0, axis == 1, axis == 2], 1).astype(np.int64)
+    lo = np.stack([i, j, k], 1)
+    hi = lo + d
+    v0 = V[lo[:, 2], lo[:, 1], lo[:, 0]]
+    v1 = V[hi[:, 2], hi[:, 1], hi[:, 0]]
+    w = (0.5 - v0) / (v1 - v0)
+    spd, orgd = np.array(sp, np.float64), np.array(org, np.float64)
+    pos = orgd + (lo + w[:, None] * d) * spd
+    perr = np.abs(pos - p).max()
+    scale = np.abs(pos).max()
+
+    def grad(ijk):
+        g = np.zeros((len(ijk), 3))
+        dims = (nx, ny, nz)
+        for a in range(3):
+            q0, q1 = ijk.copy(), ijk.copy()
+            run = np.full(len(ijk), 2 * spd[a])
+            first = ijk[:, a] == 0
+            last = ijk[:, a] == dims[a] - 1
+            q0[:, a] = np.where(last, ijk[:, a], ijk[:, a] + 1)
+            q1[:, a] = np.where(first, ijk[:, a], ijk[:, a] - 1)
+            run = np.where(first | last, spd[a], run)
+            g[:, a] = (V[q1[:, 2], q1[:, 1], q1[:, 0]] - V[q0[:, 2], q0[:, 1], q0[:, 0]]) / run
+        return g
+
+    g0, g1 = grad(lo), grad(hi)
+    nrm = g0 + w[:, None] * (g1 - g0)
+    nerr = np.abs(nrm - n).max()
+    nscale = np.abs(nrm).max()
+    print("fp64 max abs error: points %.3g (of %.3g), normals %.3g (of %.3g)" % (perr, scale, nerr, nscale))
+    eps = np.finfo(np.float32).eps
+    assert perr <= 8 * eps * scale
+    assert nerr <= 64 * eps * nscale
+
+
+def test_noise_512_bitexact(M):
+    """The bench workload: 512^3 value noise at isovalue 0, FE and MC."""
+    vol = M.generate_value_noise((512, 512, 512), 4, 64, seed=1)
+    got = gpu_extract(M, vol, 0.0, M.FLYING_EDGES)
+    ref = oracle_lib.fe(vol, 0.0, nthreads=os.cpu_count())
+    assert_same_mesh(got, ref, "FE 512")
+    del got, ref
+    got = gpu_extract(M, vol, 0.0, M.MARCHING_CUBES)
+    ref = oracle_lib.mc(vol, 0.0)
+    assert_same_mesh(got, ref, "MC 512")

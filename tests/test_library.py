@@ -1,0 +1,128 @@
+"""CPU: the C ABI library loads and exports what include/miniiso.h declares;
+host-only parts of it (tables, VTK IO, generators, argument checks) work."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+REF_TABLES = Path("/root/reference/flyingEdges/util/MarchingCubesTables.h")
+
+
+def declared_functions():
+    names = set()
+    for h in sorted((ROOT / "include").glob("*.h")):
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        names |= set(re.findall(r"\b(iso_[a-z0-9_]+)\s*\(", text))
+    return sorted(names)
+
+
+def test_library_exports_every_declared_symbol(built):
+    lib = C.CDLL(str(built))
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+    from miniisosurface_gb300 import _lib
+    assert set(_lib.SIGNATURES) >= set(declared_functions())
+
+
+def test_version_and_status_strings(built):
+    from miniisosurface_gb300 import _lib
+    lib = _lib.load()
+    assert b"sm_103a" in lib.iso_version()
+    assert lib.iso_status_string(4) == b"output buffers too small"
+
+
+def _case_tables():
+    text = (ROOT / "miniisosurface_gb300" / "csrc" / "case_table.h").read_text()
+    words = [int(w, 16) for w in re.findall(r"0x([0-9a-f]{16})ull", text)]
+    assert len(words) == 256
+    return [[(w >> (4 * t)) & 15 for t in range(3 * (w >> 60))] for w in words]
+
+
+def test_packed_table_matches_oracle_table():
+    text = (ROOT / "oracle" / "case_table.h").read_text()
+    strings = re.findall(r'"([0-9a-f]*)"', text)
+    assert [[int(ch, 16) for ch in s] for s in strings] == _case_tables()
+
+
+@pytest.mark.skipif(not REF_TABLES.exists(), reason="reference checkout not present")
+def test_packed_table_matches_reference_header():
+    import sys
+    sys.path.insert(0, str(ROOT / "miniisosurface_gb300" / "csrc"))
+    from gen_case_table import parse_case_triangles
+    text = REF_TABLES.read_text()
+    assert parse_case_triangles(text) == _case_tables()
+    # numTris and isCut are derived, not copied: check the derivation
+    lo = [0, 1, 3, 0, 4, 5, 7, 4, 0, 1, 3, 2]
+    hi = [1, 2, 2, 3, 5, 6, 6, 7, 4, 5, 7, 6]
+    nt = text[text.index("numTris"):]
+    nt = [int(x) for x in nt[nt.index("{") + 1: nt.index("}")].replace("\n", " ").split(",") if x.strip()]
+    tables = _case_tables()
+    assert all(nt[c] == len(tables[c]) // 3 for c in range(256))
+    ic = text[text.index("isCut"):]
+    rows = re.findall(r"\{([^{}]*)\}", ic[ic.index("{") + 1:])[:256]
+    ic = [[int(x) for x in r.split(",")] for r in rows]
+    assert all(ic[c][e] == int(((c >> lo[e]) & 1) != ((c >> hi[e]) & 1)) for c in range(256) for e in range(12))
+
+
+def test_generators_deterministic(built):
+    import miniisosurface_gb300 as M
+    a = M.generate_value_noise((33, 20, 17), 4, 8, seed=4)
+    b = M.generate_value_noise((33, 20, 17), 4, 8, seed=4)
+    c = M.generate_value_noise((33, 20, 17), 4, 8, seed=5)
+    assert np.array_equal(a, b) and not np.array_equal(a, c)
+    assert -2.0 <= a.min() and a.max() <= 2.0
+    blobs = M.generate_blobs((30, 30, 30), 8, seed=1)
+    assert blobs.min() >= 0.0 and 0.3 < blobs.max() < 8.0
+
+
+def test_vtk_image_roundtrip_and_errors(built, tmp_path):
+    import miniisosurface_gb300 as M
+    vol = M.generate_blobs((12, 10, 8), 8, seed=3)
+    img = M.Image3D.from_array(vol, (0.1, 0.2, 0.3), (-1.5, 2.25, 1e-3))
+    p = tmp_path / "img.vtk"
+    M.saveImage(img, str(p))
+    back = M.loadImage(str(p))
+    assert back.dims == (12, 10, 8)
+    assert np.array_equal(back.data, img.data)
+    assert back.spacing == img.spacing and back.zeroPos == img.zeroPos
+    with pytest.raises(M.file_not_found):
+        M.loadImage(str(tmp_path / "missing.vtk"))
+    bad = tmp_path / "bad.vtk"
+    bad.write_bytes(b"# vtk\nx\nASCII\nDATASET STRUCTURED_POINTS\n")
+    with pytest.raises(M.bad_format):
+        M.loadImage(str(bad))
+
+
+def test_vtk_typed_scalars(built, tmp_path):
+    """short / unsigned_short / int / double / char scalars are converted to
+    float as in ConvertBuffer.h:45-72."""
+    import miniisosurface_gb300 as M
+    vals = np.arange(-12, 12, dtype=np.int64).reshape(2, 3, 4)
+    for name, dt in (("short", ">i2"), ("int", ">i4"), ("double", ">f8"), ("char", "i1")):
+        p = tmp_path / ("%s.vtk" % name)
+        with open(p, "wb") as f:
+            f.write(b"# vtk DataFile Version 3.0\nt\nBINARY\nDATASET STRUCTURED_POINTS\n"
+                    b"DIMENSIONS 4 3 2\nSPACING 1 1 1\nORIGIN 0 0 0\nPOINT_DATA 24\n")
+            f.write(("SCALARS s %s\nLOOKUP_TABLE default\n" % name).encode())
+            f.write(vals.astype(dt).tobytes())
+        img = M.loadImage(str(p))
+        assert np.array_equal(img.data, vals.reshape(-1).astype(np.float32)), name
+    p = tmp_path / "us.vtk"
+    with open(p, "wb") as f:
+        f.write(b"# vtk DataFile Version 3.0\nt\nBINARY\nDATASET STRUCTURED_POINTS\n"
+                b"DIMENSIONS 4 3 2\nSPACING 1 1 1\nORIGIN 0 0 0\nPOINT_DATA 24\n"
+                b"SCALARS s unsigned_short\nLOOKUP_TABLE default\n")
+        f.write(np.arange(24, dtype=">u2").tobytes() * 1)
+    assert np.array_equal(M.loadImage(str(p)).data, np.arange(24, dtype=np.float32))
+
+
+def test_invalid_arguments_rejected_without_gpu_work(built):
+    from miniisosurface_gb300 import _lib
+    lib = _lib.load()
+    assert lib.iso_ctx_create(0, None) == _lib.ISO_ERR_INVALID_ARG
+    assert lib.iso_extract_device(None, 0, None, None, C.c_float(0), None, None) == _lib.ISO_ERR_INVALID_ARG
+    d = (C.c_int64 * 3)(4, 4, 4)
+    assert lib.iso_generate_value_noise(d, 0, 8, 1, None) == _lib.ISO_ERR_INVALID_ARG

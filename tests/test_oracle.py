@@ -1,0 +1,127 @@
+"""CPU: the oracle pinned against the reference.
+
+1. Golden fixtures (tests/golden/golden.json), produced by running the
+   reference programs compiled from the miniIsosurface sources.
+2. When oracle/_ref/ exists (built here from the reference sources): the
+   reference programs themselves on further seeded volumes, including the
+   OpenMP Flying Edges variant.
+"""
+import hashlib
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle_lib
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+def sha(b):
+    return hashlib.sha256(b).hexdigest()
+
+
+def golden_cases():
+    return json.loads((GOLDEN / "golden.json").read_text())
+
+
+def golden_volume(rec):
+    import miniisosurface_gb300 as M
+
+    if "npy" in rec:
+        vol = np.load(GOLDEN / rec["npy"])
+    else:
+        g = rec["gen"]
+        if g["kind"] == "blobs":
+            vol = M.generate_blobs(g["dims"], g["nblobs"], g["seed"])
+        else:
+            vol = M.generate_value_noise(g["dims"], g["octaves"], g["period"], g["seed"])
+    assert sha(np.ascontiguousarray(vol, "<f4").tobytes()) == rec["volume_sha256"], "input volume drifted"
+    return vol
+
+
+def digest(p, n, t):
+    return dict(n_points=int(p.shape[0]), n_tris=int(t.shape[0]),
+                points=sha(np.ascontiguousarray(p, "<f4").tobytes()),
+                normals=sha(np.ascontiguousarray(n, "<f4").tobytes()),
+                tris=sha(np.ascontiguousarray(t, "<u8").tobytes()))
+
+
+@pytest.mark.parametrize("rec", golden_cases(), ids=lambda r: r["name"])
+def test_oracle_matches_golden(built, rec):
+    vol = golden_volume(rec)
+    for algo, fn in (("fe", oracle_lib.fe), ("mc", oracle_lib.mc)):
+        p, n, t, _ = fn(vol, rec["iso"], rec["spacing"], rec["origin"])
+        d = digest(p, n, t)
+        for key in d:
+            assert d[key] == rec[algo][key], "%s %s %s" % (rec["name"], algo, key)
+
+
+@pytest.mark.parametrize("rec", golden_cases(), ids=lambda r: r["name"])
+def test_mesh_writer_byte_identical_to_reference(built, rec, tmp_path):
+    """util::saveTriangleMesh layout, byte for byte (sha256 of the reference file)."""
+    import miniisosurface_gb300 as M
+
+    vol = golden_volume(rec)
+    for algo, fn in (("fe", oracle_lib.fe), ("mc", oracle_lib.mc)):
+        p, n, t, _ = fn(vol, rec["iso"], rec["spacing"], rec["origin"])
+        path = tmp_path / ("%s.vtk" % algo)
+        M.saveTriangleMesh(M.TriangleMesh(p, n, t), str(path))
+        assert sha(path.read_bytes()) == rec[algo]["vtk"]
+
+
+def test_openmp_oracle_equals_serial(built):
+    import miniisosurface_gb300 as M
+
+    vol = M.generate_value_noise((70, 60, 50), 4, 16, seed=3)
+    a = oracle_lib.fe(vol, 0.0, nthreads=1)
+    b = oracle_lib.fe(vol, 0.0, nthreads=4)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+
+
+needs_ref = pytest.mark.skipif(not oracle_lib.ref_available(), reason="reference programs not built here")
+
+
+@needs_ref
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_oracle_vs_reference_programs(built, seed):
+    import miniisosurface_gb300 as M
+
+    rng = np.random.default_rng(seed)
+    dims = tuple(int(x) for x in rng.integers(2, 40, 3))
+    vol = M.generate_value_noise(dims, 4, 8, seed=seed)
+    iso = float(rng.uniform(-0.3, 0.3))
+    # float32 values: the VTK header text then parses back to the same floats
+    sp = tuple(float(np.float32(x)) for x in rng.uniform(0.1, 3, 3))
+    org = tuple(float(np.float32(x)) for x in rng.uniform(-10, 10, 3))
+    for prog, fn in (("flyingEdgesSerial", oracle_lib.fe), ("mcSerial", oracle_lib.mc),
+                     ("flyingEdgesOpenMP", oracle_lib.fe)):
+        rp, rn, rt, _, _ = oracle_lib.run_ref(prog, vol, iso, sp, org, threads=3)
+        p, n, t, _ = fn(vol, iso, sp, org)
+        assert np.array_equal(rt, t), prog
+        assert np.array_equal(rp.view(np.uint32), p.view(np.uint32)), prog
+        assert np.array_equal(rn.view(np.uint32), n.view(np.uint32)), prog
+
+
+@needs_ref
+def test_product_image_writer_readable_by_reference(built, tmp_path):
+    """A volume written by iso_vtk_write_image loads in the reference loader."""
+    import subprocess
+
+    import miniisosurface_gb300 as M
+
+    vol = M.generate_blobs((20, 18, 16), 8, seed=2)
+    img = M.Image3D.from_array(vol, (0.5, 1.5, 2.0), (1, 2, 3))
+    path = tmp_path / "v.vtk"
+    M.saveImage(img, str(path))
+    out = tmp_path / "m.vtk"
+    subprocess.run([str(oracle_lib.REF_DIR / "flyingEdgesSerial"), "-i", str(path), "-o", str(out), "-v", "0.5",
+                    "-y", str(tmp_path / "y.yaml")], check=True, capture_output=True)
+    rp, rn, rt = oracle_lib.read_polydata(out)
+    p, n, t, _ = oracle_lib.fe(vol, 0.5, img.spacing, img.zeroPos)
+    assert np.array_equal(rt, t) and np.array_equal(rp, p) and np.array_equal(rn, n)
+    back = M.loadImage(str(path))
+    assert back.dims == img.dims and np.array_equal(back.data, img.data)
+    assert back.spacing == img.spacing and back.zeroPos == img.zeroPos
