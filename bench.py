@@ -10,7 +10,7 @@ One step = one full extraction (passes 1-4) of the volume.
   roofline  the dominant kernel (largest summed time), timed with CUDA events
             recorded between kernels on the extraction stream during the
             timed region; algorithmic bytes per launch:
-              classify       4 N                 (volume read)
+              count          4 N                 (volume read; passes 1+2 fused)
               fe_generate    4 N + 24 V + 12 T   (volume read, points+normals, uint32 triangles)
             the whole extraction is B = 8 N + 24 V + 12 T
   cpu_baseline  the oracle port of the reference's OpenMP Flying Edges on
@@ -279,7 +279,7 @@ def main():
         per = {names[p]: {"ms_total": ms_pass[p], "launches": int(n_pass[p]),
                           "us_per_launch": 1e3 * ms_pass[p] / n_pass[p] if n_pass[p] else None}
                for p in range(6) if n_pass[p]}
-        alg_bytes = {"classify": 4 * N, "count": 0, "scan": 0, "fe_generate": 4 * N + 24 * V + 12 * T,
+        alg_bytes = {"classify": 4 * N, "count": 4 * N, "scan": 0, "fe_generate": 4 * N + 24 * V + 12 * T,
                      "mc_vertices": 4 * N + 24 * V, "mc_triangles": 12 * T}
         dom = max(per, key=lambda k: per[k]["ms_total"])
         dom_s = per[dom]["us_per_launch"] * 1e-6
@@ -303,7 +303,8 @@ def main():
                          "per_pass": per, "event_overhead_ms_per_step": (ms - prof_ms) / args.steps},
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": 4 * N,
                     "d2h_bytes_per_step": 24 * V + 12 * T, "ms_per_step": 1e3 * e2e_s / args.e2e_steps},
-            "gpu_launches": int(sum(n_pass[p] for p in range(6))),
+            # count + scan + row starts + generate per step (scan/row starts share one mark)
+            "gpu_launches": int(sum(n_pass[p] for p in range(6)) + n_pass[2]),
             "clocks": clk,
         }
         if not args.no_cpu_baseline:

@@ -92,9 +92,9 @@ int64_t iso_ctx_scratch_bytes(const iso_ctx* ctx);
  * iso_ctx_profile_read synchronises on them, returns the summed
  * milliseconds and launch counts per pass (ISO_PASS_*) and clears them. */
 enum {
-    ISO_PASS_CLASSIFY = 0,     /* pass 1 */
-    ISO_PASS_COUNT = 1,        /* pass 2 */
-    ISO_PASS_SCAN = 2,         /* pass 3 */
+    ISO_PASS_CLASSIFY = 0,     /* pass 1: fused into ISO_PASS_COUNT, never reported */
+    ISO_PASS_COUNT = 1,        /* passes 1+2: classification and counts */
+    ISO_PASS_SCAN = 2,         /* pass 3: offsets */
     ISO_PASS_FE_GENERATE = 3,  /* pass 4, Flying Edges */
     ISO_PASS_MC_VERTICES = 4,  /* pass 4, Marching Cubes vertices */
     ISO_PASS_MC_TRIANGLES = 5, /* pass 4, Marching Cubes triangles */
@@ -119,9 +119,12 @@ iso_status iso_extract_device(iso_ctx* ctx, iso_algorithm algo, const float* vol
                               float isoval, iso_mesh* out, void* stream);
 
 /* Same, without the final synchronisation: all work is queued on `stream`;
- * the sizes land in *result_host (3 x int64: points, triangles, status) when
- * the stream reaches that point.  result_host must stay valid until then
- * (pinned memory gives a true asynchronous copy). */
+ * result_host (4 x int64) receives, when the stream reaches that point, the
+ * vertex count, the triangle count, a reserved value and the device status
+ * (0, or ISO_ERR_TIMEOUT when a bounded device-side wait gave up).  Nothing
+ * is written to the mesh when the counts exceed its capacities.  result_host
+ * must stay valid until then (pinned memory gives a true asynchronous copy).
+ * Calls on one context share its scratch: queue them on one stream. */
 iso_status iso_extract_device_async(iso_ctx* ctx, iso_algorithm algo, const float* volume, const iso_grid* grid,
                                     float isoval, iso_mesh* out, int64_t* result_host, void* stream);
 

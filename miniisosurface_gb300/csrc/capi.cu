@@ -34,6 +34,7 @@ struct iso_ctx {
     long long d_cap_points = 0, d_cap_tris = 0;
     int d_index_bytes = 0;
     unsigned long long* h_totals = nullptr;  // pinned, 4 entries
+    int reverse = 1;  // pass 4 walks the planes backwards (the count pass leaves the last ones in L2)
     std::string last_error;
     // per-pass timing (iso_ctx_profile)
     bool profiling = false;
@@ -126,29 +127,31 @@ bool make_grid(const iso_grid* gr, Grid& g)
 
 bool empty_grid(const Grid& g) { return g.nx < 2 || g.ny < 2 || g.nz < 2; }
 
-size_t scratch_size(const Grid& g)
+size_t scratch_size(const Grid& g, const iso::CountPlan& cp)
 {
-    const size_t R = (size_t)g.R, T = (size_t)iso::num_tiles(g);
-    return align256(R * g.W * 4) + align256(R * 16) + align256(R * 8) + align256(R * 4) + align256(R * 16) +
-           align256(3 * T * 8) + align256(4 * 8);
+    const size_t R = (size_t)g.R;
+    return align256(R * 16) + align256(R * 8) + align256(R * 4) + align256(3 * (size_t)cp.ngroups * 8) +
+           3 * align256(R * 8) + align256(4 * 8) + align256(R * (size_t)g.W * 4);
 }
 
-void carve(void* base, const Grid& g, FeBuffers& b)
+void carve(void* base, const Grid& g, const iso::CountPlan& cp, FeBuffers& b)
 {
-    const size_t R = (size_t)g.R, T = (size_t)iso::num_tiles(g);
+    const size_t R = (size_t)g.R;
     char* p = static_cast<char*>(base);
-    b.bits = reinterpret_cast<uint32_t*>(p); p += align256(R * g.W * 4);
     b.rowcnt = reinterpret_cast<uint4*>(p); p += align256(R * 16);
     b.trims = reinterpret_cast<uint2*>(p); p += align256(R * 8);
     b.mccnt = reinterpret_cast<uint32_t*>(p); p += align256(R * 4);
-    b.rowpre = reinterpret_cast<uint4*>(p); p += align256(R * 16);
-    b.tiles = reinterpret_cast<unsigned long long*>(p); p += align256(3 * T * 8);
-    b.totals = reinterpret_cast<unsigned long long*>(p);
+    b.groups = reinterpret_cast<unsigned long long*>(p); p += align256(3 * (size_t)cp.ngroups * 8);
+    b.vstart = reinterpret_cast<unsigned long long*>(p); p += align256(R * 8);
+    b.tstart = reinterpret_cast<unsigned long long*>(p); p += align256(R * 8);
+    b.mstart = reinterpret_cast<unsigned long long*>(p); p += align256(R * 8);
+    b.totals = reinterpret_cast<unsigned long long*>(p); p += align256(4 * 8);
+    b.bits = reinterpret_cast<uint32_t*>(p);
 }
 
-iso_status ensure_scratch(iso_ctx* ctx, const Grid& g, FeBuffers& b, cudaStream_t s)
+iso_status ensure_scratch(iso_ctx* ctx, const Grid& g, const iso::CountPlan& cp, FeBuffers& b, cudaStream_t s)
 {
-    const size_t need = scratch_size(g);
+    const size_t need = scratch_size(g, cp);
     if (need > ctx->scratch_bytes) {
         if (ctx->scratch) {
             ISO_CUDA(ctx, cudaStreamSynchronize(s));
@@ -160,7 +163,7 @@ iso_status ensure_scratch(iso_ctx* ctx, const Grid& g, FeBuffers& b, cudaStream_
         ISO_CUDA(ctx, cudaMalloc(&ctx->scratch, alloc));
         ctx->scratch_bytes = alloc;
     }
-    carve(ctx->scratch, g, b);
+    carve(ctx->scratch, g, cp, b);
     b.fe2mc = ctx->fe2mc;
     return ISO_OK;
 }
@@ -228,50 +231,84 @@ struct PassMarks {
     }
 };
 
-// Queue passes 1-3 (and pass 4 unless count_only) for one extraction.
-iso_status enqueue(iso_ctx* ctx, iso_algorithm algo, const float* vol, const Grid& g, float iso, FeBuffers& b,
-                   const iso_mesh* out, bool count_only, cudaStream_t s)
+// Plans of one extraction.
+struct Plans {
+    iso::CountPlan cp;
+    iso::GenPlan gp;
+};
+
+Plans make_plans(const iso_ctx* ctx, const Grid& g)
 {
-    PassMarks pm(ctx, s);
-    iso::launch_classify(vol, b.bits, g, iso, ctx->nsm, s);
-    pm.mark(ISO_PASS_CLASSIFY);
-    iso::launch_count(b.bits, g, ctx->d_cases, algo == ISO_MARCHING_CUBES, b, s);
-    pm.mark(ISO_PASS_COUNT);
-    iso::launch_scan_tiles(g, b, s);
-    pm.mark(ISO_PASS_SCAN);
-    if (!count_only) {
-        const long long capV = vertex_limit(out, out->cap_points);
-        const long long capT = out->cap_tris;
-        if (algo == ISO_FLYING_EDGES) {
-            if (out->index_bytes == 4)
-                iso::launch_fe_generate<uint32_t>(vol, b.bits, g, iso, ctx->d_cases, b, capV, capT, out->points,
-                                                  out->normals, static_cast<uint32_t*>(out->tris), ctx->nsm, s);
-            else
-                iso::launch_fe_generate<uint64_t>(vol, b.bits, g, iso, ctx->d_cases, b, capV, capT, out->points,
-                                                  out->normals, static_cast<uint64_t*>(out->tris), ctx->nsm, s);
-            pm.mark(ISO_PASS_FE_GENERATE);
-        } else {
-            const long long capM = capV < 0xffffffffll ? capV : 0xffffffffll;  // fe2mc holds 32-bit ids
-            iso::launch_mc_vertices(vol, b.bits, g, iso, ctx->d_cases, b, capM, capT, out->points, out->normals,
-                                    ctx->nsm, s);
-            pm.mark(ISO_PASS_MC_VERTICES);
-            if (out->index_bytes == 4)
-                iso::launch_mc_triangles<uint32_t>(b.bits, g, ctx->d_cases, b, capM, capT,
-                                                   static_cast<uint32_t*>(out->tris), ctx->nsm, s);
-            else
-                iso::launch_mc_triangles<uint64_t>(b.bits, g, ctx->d_cases, b, capM, capT,
-                                                   static_cast<uint64_t*>(out->tris), ctx->nsm, s);
-            pm.mark(ISO_PASS_MC_TRIANGLES);
-        }
-    }
-    ISO_CUDA(ctx, cudaGetLastError());
-    return ISO_OK;
+    Plans p;
+    p.cp = iso::count_plan(g, ctx->nsm);
+    p.gp = iso::gen_plan(g, ctx->nsm);
+    return p;
 }
 
-iso_status finish_counts(iso_ctx* ctx, const iso_mesh* out, long long V, long long T, int64_t* nV, int64_t* nT)
+// Passes 1-3: counts, scan, row starts.
+void enqueue_count(iso_ctx* ctx, iso_algorithm algo, const float* vol, const Grid& g, float iso, const Plans& pl,
+                   FeBuffers& b, cudaStream_t s, PassMarks& pm)
+{
+    const bool mc = algo == ISO_MARCHING_CUBES;
+    iso::launch_count(vol, g, iso, ctx->d_cases, mc, mc || !pl.gp.fits, pl.cp, b, s);
+    pm.mark(ISO_PASS_COUNT);
+    iso::launch_scan(pl.cp, b, s);
+    iso::launch_row_starts(g, pl.cp, mc, b, s);
+    pm.mark(ISO_PASS_SCAN);
+}
+
+// Pass 4 into the mesh buffers of `out` (device memory).
+void enqueue_generate(iso_ctx* ctx, iso_algorithm algo, const float* vol, const Grid& g, float iso, const Plans& pl,
+                      const FeBuffers& b, const iso_mesh* out, cudaStream_t s, PassMarks& pm)
+{
+    const long long capV = vertex_limit(out, out->cap_points);
+    const long long capT = out->cap_tris;
+    const bool i4 = out->index_bytes == 4;
+    if (algo == ISO_FLYING_EDGES) {
+        if (pl.gp.fits) {
+            if (i4)
+                iso::launch_fe_gen_cols<uint32_t>(vol, g, iso, ctx->d_cases, b, pl.gp, capV, capT, out->points,
+                                                  out->normals, static_cast<uint32_t*>(out->tris), ctx->reverse, s);
+            else
+                iso::launch_fe_gen_cols<uint64_t>(vol, g, iso, ctx->d_cases, b, pl.gp, capV, capT, out->points,
+                                                  out->normals, static_cast<uint64_t*>(out->tris), ctx->reverse, s);
+        } else {
+            if (i4)
+                iso::launch_fe_gen_rows<uint32_t>(vol, g, iso, ctx->d_cases, b, capV, capT, out->points, out->normals,
+                                                  static_cast<uint32_t*>(out->tris), ctx->nsm, s);
+            else
+                iso::launch_fe_gen_rows<uint64_t>(vol, g, iso, ctx->d_cases, b, capV, capT, out->points, out->normals,
+                                                  static_cast<uint64_t*>(out->tris), ctx->nsm, s);
+        }
+        pm.mark(ISO_PASS_FE_GENERATE);
+    } else {
+        const long long capM = capV < 0xffffffffll ? capV : 0xffffffffll;  // fe2mc holds 32-bit ids
+        if (pl.gp.fits)
+            iso::launch_mc_gen_cols(vol, g, iso, ctx->d_cases, b, pl.gp, capM, capT, out->points, out->normals,
+                                    ctx->reverse, s);
+        else
+            iso::launch_mc_vertices_rows(vol, g, iso, ctx->d_cases, b, capM, capT, out->points, out->normals,
+                                         ctx->nsm, s);
+        pm.mark(ISO_PASS_MC_VERTICES);
+        if (i4)
+            iso::launch_mc_triangles<uint32_t>(g, ctx->d_cases, b, capM, capT, static_cast<uint32_t*>(out->tris),
+                                               ctx->nsm, s);
+        else
+            iso::launch_mc_triangles<uint64_t>(g, ctx->d_cases, b, capM, capT, static_cast<uint64_t*>(out->tris),
+                                               ctx->nsm, s);
+        pm.mark(ISO_PASS_MC_TRIANGLES);
+    }
+}
+
+iso_status finish_counts(iso_ctx* ctx, const iso_mesh* out, long long V, long long T, long long status, int64_t* nV,
+                         int64_t* nT)
 {
     *nV = V;
     *nT = T;
+    if (status != 0) {
+        ctx->last_error = "a device-side wait timed out";
+        return ISO_ERR_TIMEOUT;
+    }
     if (out && out->index_bytes == 4 && V > 0xffffffffll) {
         ctx->last_error = "more than 2^32-1 vertices: use 64-bit indices";
         return ISO_ERR_OVERFLOW;
@@ -412,12 +449,14 @@ iso_status iso_count_device(iso_ctx* ctx, iso_algorithm algo, const float* volum
     if (!volume) return ISO_ERR_INVALID_ARG;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     ISO_CUDA(ctx, cudaSetDevice(ctx->device));
+    const Plans pl = make_plans(ctx, g);
     FeBuffers b;
-    iso_status st = ensure_scratch(ctx, g, b, s);
+    iso_status st = ensure_scratch(ctx, g, pl.cp, b, s);
     if (st != ISO_OK) return st;
-    st = enqueue(ctx, algo, volume, g, isoval, b, nullptr, true, s);
-    if (st != ISO_OK) return st;
-    ISO_CUDA(ctx, cudaMemcpyAsync(ctx->h_totals, b.totals, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    PassMarks pm(ctx, s);
+    enqueue_count(ctx, algo, volume, g, isoval, pl, b, s, pm);
+    ISO_CUDA(ctx, cudaGetLastError());
+    ISO_CUDA(ctx, cudaMemcpyAsync(ctx->h_totals, b.totals, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
     ISO_CUDA(ctx, cudaStreamSynchronize(s));
     *n_points = (int64_t)ctx->h_totals[0];
     *n_tris = (int64_t)ctx->h_totals[1];
@@ -433,22 +472,25 @@ iso_status iso_extract_device_async(iso_ctx* ctx, iso_algorithm algo, const floa
     if (st != ISO_OK) return st;
     Grid g;
     if (!make_grid(grid, g)) return ISO_ERR_INVALID_ARG;
-    result_host[0] = result_host[1] = 0;
+    result_host[0] = result_host[1] = result_host[2] = result_host[3] = 0;
     if (empty_grid(g)) return ISO_OK;
     if (!volume) return ISO_ERR_INVALID_ARG;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     ISO_CUDA(ctx, cudaSetDevice(ctx->device));
+    const Plans pl = make_plans(ctx, g);
     FeBuffers b;
-    st = ensure_scratch(ctx, g, b, s);
+    st = ensure_scratch(ctx, g, pl.cp, b, s);
     if (st != ISO_OK) return st;
     if (algo == ISO_MARCHING_CUBES) {
         st = ensure_fe2mc(ctx, out->cap_points, s);
         if (st != ISO_OK) return st;
         b.fe2mc = ctx->fe2mc;
     }
-    st = enqueue(ctx, algo, volume, g, isoval, b, out, false, s);
-    if (st != ISO_OK) return st;
-    ISO_CUDA(ctx, cudaMemcpyAsync(result_host, b.totals, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    PassMarks pm(ctx, s);
+    enqueue_count(ctx, algo, volume, g, isoval, pl, b, s, pm);
+    enqueue_generate(ctx, algo, volume, g, isoval, pl, b, out, s, pm);
+    ISO_CUDA(ctx, cudaGetLastError());
+    ISO_CUDA(ctx, cudaMemcpyAsync(result_host, b.totals, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
     return ISO_OK;
 }
 
@@ -459,12 +501,11 @@ iso_status iso_extract_device(iso_ctx* ctx, iso_algorithm algo, const float* vol
     iso_status st = check_mesh(out);
     if (st != ISO_OK) return st;
     out->n_points = out->n_tris = 0;
-    st = iso_extract_device_async(ctx, algo, volume, grid, isoval, out, reinterpret_cast<int64_t*>(ctx->h_totals),
-                                  stream);
+    int64_t* res = reinterpret_cast<int64_t*>(ctx->h_totals);
+    st = iso_extract_device_async(ctx, algo, volume, grid, isoval, out, res, stream);
     if (st != ISO_OK) return st;
     ISO_CUDA(ctx, cudaStreamSynchronize(static_cast<cudaStream_t>(stream)));
-    return finish_counts(ctx, out, (long long)ctx->h_totals[0], (long long)ctx->h_totals[1], &out->n_points,
-                         &out->n_tris);
+    return finish_counts(ctx, out, res[0], res[1], res[3], &out->n_points, &out->n_tris);
 }
 
 iso_status iso_extract_host(iso_ctx* ctx, iso_algorithm algo, const float* volume, const iso_grid* grid,
@@ -491,15 +532,17 @@ iso_status iso_extract_host(iso_ctx* ctx, iso_algorithm algo, const float* volum
         ctx->d_volume_bytes = vbytes;
     }
     ISO_CUDA(ctx, cudaMemcpyAsync(ctx->d_volume, volume, vbytes, cudaMemcpyHostToDevice, s));
+    const Plans pl = make_plans(ctx, g);
     FeBuffers b;
-    st = ensure_scratch(ctx, g, b, s);
+    st = ensure_scratch(ctx, g, pl.cp, b, s);
     if (st != ISO_OK) return st;
-    st = enqueue(ctx, algo, ctx->d_volume, g, isoval, b, nullptr, true, s);
-    if (st != ISO_OK) return st;
-    ISO_CUDA(ctx, cudaMemcpyAsync(ctx->h_totals, b.totals, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    PassMarks pm(ctx, s);
+    enqueue_count(ctx, algo, ctx->d_volume, g, isoval, pl, b, s, pm);
+    ISO_CUDA(ctx, cudaGetLastError());
+    ISO_CUDA(ctx, cudaMemcpyAsync(ctx->h_totals, b.totals, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
     ISO_CUDA(ctx, cudaStreamSynchronize(s));
     const long long V = (long long)ctx->h_totals[0], T = (long long)ctx->h_totals[1];
-    st = finish_counts(ctx, out, V, T, &out->n_points, &out->n_tris);
+    st = finish_counts(ctx, out, V, T, 0, &out->n_points, &out->n_tris);
     if (st != ISO_OK) return st;
     // device output staging, grown on demand
     if (V > ctx->d_cap_points || T > ctx->d_cap_tris || out->index_bytes != ctx->d_index_bytes) {
@@ -524,32 +567,12 @@ iso_status iso_extract_host(iso_ctx* ctx, iso_algorithm algo, const float* volum
     dm.index_bytes = out->index_bytes;
     dm.cap_points = ctx->d_cap_points;
     dm.cap_tris = ctx->d_cap_tris;
-    PassMarks pm(ctx, s);
-    if (algo == ISO_FLYING_EDGES) {
-        if (dm.index_bytes == 4)
-            iso::launch_fe_generate<uint32_t>(ctx->d_volume, b.bits, g, isoval, ctx->d_cases, b, dm.cap_points,
-                                              dm.cap_tris, dm.points, dm.normals, static_cast<uint32_t*>(dm.tris),
-                                              ctx->nsm, s);
-        else
-            iso::launch_fe_generate<uint64_t>(ctx->d_volume, b.bits, g, isoval, ctx->d_cases, b, dm.cap_points,
-                                              dm.cap_tris, dm.points, dm.normals, static_cast<uint64_t*>(dm.tris),
-                                              ctx->nsm, s);
-        pm.mark(ISO_PASS_FE_GENERATE);
-    } else {
-        st = ensure_fe2mc(ctx, V, s);
+    if (algo == ISO_MARCHING_CUBES) {
+        st = ensure_fe2mc(ctx, dm.cap_points, s);
         if (st != ISO_OK) return st;
         b.fe2mc = ctx->fe2mc;
-        iso::launch_mc_vertices(ctx->d_volume, b.bits, g, isoval, ctx->d_cases, b, dm.cap_points, dm.cap_tris,
-                                dm.points, dm.normals, ctx->nsm, s);
-        pm.mark(ISO_PASS_MC_VERTICES);
-        if (dm.index_bytes == 4)
-            iso::launch_mc_triangles<uint32_t>(b.bits, g, ctx->d_cases, b, dm.cap_points, dm.cap_tris,
-                                               static_cast<uint32_t*>(dm.tris), ctx->nsm, s);
-        else
-            iso::launch_mc_triangles<uint64_t>(b.bits, g, ctx->d_cases, b, dm.cap_points, dm.cap_tris,
-                                               static_cast<uint64_t*>(dm.tris), ctx->nsm, s);
-        pm.mark(ISO_PASS_MC_TRIANGLES);
     }
+    enqueue_generate(ctx, algo, ctx->d_volume, g, isoval, pl, b, &dm, s, pm);
     ISO_CUDA(ctx, cudaGetLastError());
     if (V > 0) {
         ISO_CUDA(ctx, cudaMemcpyAsync(out->points, dm.points, (size_t)V * 12, cudaMemcpyDeviceToHost, s));
@@ -558,12 +581,15 @@ iso_status iso_extract_host(iso_ctx* ctx, iso_algorithm algo, const float* volum
     if (T > 0) {
         ISO_CUDA(ctx, cudaMemcpyAsync(out->tris, dm.tris, (size_t)T * 3 * out->index_bytes, cudaMemcpyDeviceToHost, s));
     }
+    ISO_CUDA(ctx, cudaMemcpyAsync(ctx->h_totals, b.totals, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
     ISO_CUDA(ctx, cudaStreamSynchronize(s));
-    return ISO_OK;
+    return finish_counts(ctx, out, V, T, (long long)ctx->h_totals[3], &out->n_points, &out->n_tris);
 }
 
 // ---------------------------------------------------------------------------
-// Pass-by-pass Flying Edges (FlyingEdgesAlgorithm.h:29-49)
+// Pass-by-pass Flying Edges (FlyingEdgesAlgorithm.h:29-49).  Passes 1 and 2
+// run as one fused kernel here (classification feeds the counts directly):
+// iso_fe_pass1 launches it, iso_fe_pass2 only advances the state.
 // ---------------------------------------------------------------------------
 iso_status iso_fe_create(iso_ctx* ctx, const float* host_volume, const iso_grid* grid, float isoval, iso_fe** out)
 {
@@ -593,11 +619,12 @@ iso_status iso_fe_pass1(iso_fe* fe)
     ISO_CUDA(ctx, cudaSetDevice(ctx->device));
     const Grid& g = fe->g;
     const size_t vbytes = (size_t)g.nx * g.ny * g.nz * sizeof(float);
+    const Plans pl = make_plans(ctx, g);
     ISO_CUDA(ctx, cudaMalloc(&fe->d_volume, vbytes));
-    ISO_CUDA(ctx, cudaMalloc(&fe->scratch, scratch_size(g)));
-    carve(fe->scratch, g, fe->buf);
+    ISO_CUDA(ctx, cudaMalloc(&fe->scratch, scratch_size(g, pl.cp)));
+    carve(fe->scratch, g, pl.cp, fe->buf);
     ISO_CUDA(ctx, cudaMemcpy(fe->d_volume, fe->host_volume, vbytes, cudaMemcpyHostToDevice));
-    iso::launch_classify(fe->d_volume, fe->buf.bits, g, fe->isoval, ctx->nsm, 0);
+    iso::launch_count(fe->d_volume, g, fe->isoval, ctx->d_cases, false, !pl.gp.fits, pl.cp, fe->buf, 0);
     ISO_CUDA(ctx, cudaGetLastError());
     ISO_CUDA(ctx, cudaDeviceSynchronize());
     return ISO_OK;
@@ -608,12 +635,6 @@ iso_status iso_fe_pass2(iso_fe* fe)
     if (!fe) return ISO_ERR_INVALID_ARG;
     if (fe->stage != 1) return ISO_ERR_STATE;
     fe->stage = 2;
-    if (empty_grid(fe->g)) return ISO_OK;
-    iso_ctx* ctx = fe->ctx;
-    ISO_CUDA(ctx, cudaSetDevice(ctx->device));
-    iso::launch_count(fe->buf.bits, fe->g, ctx->d_cases, false, fe->buf, 0);
-    ISO_CUDA(ctx, cudaGetLastError());
-    ISO_CUDA(ctx, cudaDeviceSynchronize());
     return ISO_OK;
 }
 
@@ -625,9 +646,11 @@ iso_status iso_fe_pass3(iso_fe* fe)
     if (empty_grid(fe->g)) return ISO_OK;
     iso_ctx* ctx = fe->ctx;
     ISO_CUDA(ctx, cudaSetDevice(ctx->device));
-    iso::launch_scan_tiles(fe->g, fe->buf, 0);
+    const Plans pl = make_plans(ctx, fe->g);
+    iso::launch_scan(pl.cp, fe->buf, 0);
+    iso::launch_row_starts(fe->g, pl.cp, false, fe->buf, 0);
     ISO_CUDA(ctx, cudaGetLastError());
-    unsigned long long tot[3];
+    unsigned long long tot[4];
     ISO_CUDA(ctx, cudaMemcpy(tot, fe->buf.totals, sizeof(tot), cudaMemcpyDeviceToHost));
     fe->n_points = (long long)tot[0];
     fe->n_tris = (long long)tot[1];
@@ -646,11 +669,23 @@ iso_status iso_fe_pass4(iso_fe* fe)
     if (empty_grid(fe->g)) return ISO_OK;
     iso_ctx* ctx = fe->ctx;
     ISO_CUDA(ctx, cudaSetDevice(ctx->device));
-    iso::launch_fe_generate<uint64_t>(fe->d_volume, fe->buf.bits, fe->g, fe->isoval, ctx->d_cases, fe->buf,
-                                      fe->n_points, fe->n_tris, fe->d_points, fe->d_normals, fe->d_tris, ctx->nsm,
-                                      0);
+    const Plans pl = make_plans(ctx, fe->g);
+    iso_mesh dm{};
+    dm.points = fe->d_points;
+    dm.normals = fe->d_normals;
+    dm.tris = fe->d_tris;
+    dm.index_bytes = 8;
+    dm.cap_points = fe->n_points;
+    dm.cap_tris = fe->n_tris;
+    PassMarks pm(ctx, 0);
+    enqueue_generate(ctx, ISO_FLYING_EDGES, fe->d_volume, fe->g, fe->isoval, pl, fe->buf, &dm, 0, pm);
     ISO_CUDA(ctx, cudaGetLastError());
-    ISO_CUDA(ctx, cudaDeviceSynchronize());
+    unsigned long long tot[4];
+    ISO_CUDA(ctx, cudaMemcpy(tot, fe->buf.totals, sizeof(tot), cudaMemcpyDeviceToHost));
+    if (tot[3] != 0) {
+        ctx->last_error = "a device-side wait timed out";
+        return ISO_ERR_TIMEOUT;
+    }
     return ISO_OK;
 }
 
@@ -674,7 +709,7 @@ iso_status iso_fe_grid_edges(iso_fe* fe, uint64_t* grid_edges, uint64_t* tri_cou
     const size_t nge = (size_t)g.R * 5, ntc = (size_t)(g.ny - 1) * (g.nz - 1);
     unsigned long long* d = nullptr;
     ISO_CUDA(ctx, cudaMalloc(&d, (nge + ntc) * 8));
-    iso::launch_fe_grid_edges(g, fe->buf, fe->stage >= 3 ? 1 : 0, d, d + nge, 0);
+    iso::launch_grid_edges(g, fe->buf, fe->stage >= 3 ? 1 : 0, d, d + nge, 0);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpy(grid_edges, d, nge * 8, cudaMemcpyDeviceToHost);
     if (e == cudaSuccess) e = cudaMemcpy(tri_counter, d + nge, ntc * 8, cudaMemcpyDeviceToHost);

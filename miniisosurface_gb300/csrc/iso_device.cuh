@@ -2,14 +2,16 @@
 //
 // Data layout in HBM (one extraction):
 //   volume  float32[nz][ny][nx]                  x fastest (Image3D.h:26-85)
-//   bits    uint32[R][W]   R = ny*nz grid rows, W = ceil(nx/32) words per row;
-//                          bit i of row r is "value(i, r) >= isovalue"
-//   rowcnt  uint4[R]       per grid row: cut x/y/z edges owned by the row,
-//                          triangles of cell row (j,k)
+//   rowcnt  uint4[R]       per grid row r = k*ny + j (R = ny*nz): cut x / y / z
+//                          edges owned by the row, triangles of cell row (j,k)
+//   trims   uint2[R]       xl, xr of the row (FlyingEdgesAlgorithm.cpp:47-65)
 //   mccnt   uint32[R]      marching cubes: vertices owned by cell row (j,k)
-//   rowpre  uint4[R]       exclusive prefix of (vertices, triangles, mc
-//                          vertices) inside the row's tile
-//   tiles   u64[3*ntiles]  per tile of kTileRows rows: totals, then offsets
+//   groups  u64[3][ngroups] per group (plane k, block of J rows): totals of
+//                          (vertices, triangles, mc vertices), scanned in place
+//   vstart, tstart, mstart  u64[R]  first vertex / triangle / mc vertex of a row
+//   bits    uint32[R][W]   W = ceil(nx/32); bit i of row r = value >= isovalue
+//                          (written only when a row-wise kernel needs it)
+//   totals  u64[4]         vertices, triangles, mc vertices, device status
 //
 // All interpolation arithmetic goes through the _rn intrinsics so that no
 // multiply-add is ever contracted: that reproduces the float32 results of the
@@ -309,13 +311,80 @@ __device__ __forceinline__ void stage_cases(SharedCases& s, const CaseTables* __
     __syncthreads();
 }
 
-// Start offset of grid row r in one of the scanned count arrays
-// (comp 0: Flying Edges vertices, 1: triangles, 2: MC vertices).
-__device__ __forceinline__ unsigned long long row_base(const unsigned long long* __restrict__ tiles_a,
-                                                       const uint4* __restrict__ rowpre, long long r, int comp)
+// ---------------------------------------------------------------------------
+// Asynchronous global -> shared copies (TMA bulk engine or cp.async) with
+// mbarrier completion, and bounded waits.
+// ---------------------------------------------------------------------------
+constexpr unsigned kWaitLimit = 1u << 22;   // try_wait rounds before giving up
+constexpr unsigned long long kStatusTimeout = 6;  // ISO_ERR_TIMEOUT
+
+__device__ __forceinline__ unsigned smem_u32(const void* p)
 {
-    const uint4 p = __ldg(&rowpre[r]);
-    return __ldg(tiles_a + r / kTileRows) + (comp == 0 ? p.x : (comp == 1 ? p.y : p.z));
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init()
+{
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// One bulk copy (16-byte aligned addresses, size a multiple of 16).
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void cp_async4(void* dst, const void* src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+
+// Arrive on `bar` once all cp.async of this thread have landed.
+__device__ __forceinline__ void cp_async_arrive(uint64_t* bar)
+{
+    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity)
+{
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait for phase `parity` of `bar`.  Returns false after kWaitLimit
+// rounds (the caller records a timeout status and stops issuing work).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity)
+{
+    for (unsigned n = 0; n < kWaitLimit; ++n) {
+        if (mbar_try_wait(bar, parity)) return true;
+    }
+    return false;
 }
 
 // Marching-cubes owned-edge mask of a cell (first-reference rule of

@@ -1,5 +1,6 @@
 // Host-side declarations of the kernel launchers (internal to the library).
 #pragma once
+#include <cstddef>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -9,36 +10,66 @@ struct Grid;
 struct CaseTables;
 
 // Scratch of one extraction (device memory, owned by the caller of the
-// launchers).  Sizes for R grid rows, W words per row, T = ceil(R/256) tiles.
+// launchers).  R = ny*nz grid rows, W = ceil(nx/32) words per row.
 struct FeBuffers {
-    uint32_t* bits = nullptr;              // R * W   "value >= isovalue" bits
-    uint4* rowcnt = nullptr;               // R       x/y/z cuts, triangles
-    uint2* trims = nullptr;                // R       xl, xr (pass 1 trims)
-    uint32_t* mccnt = nullptr;             // R       MC vertices per cell row
-    uint4* rowpre = nullptr;               // R       in-tile prefixes
-    unsigned long long* tiles = nullptr;   // 3 * T   tile totals -> offsets
-    unsigned long long* totals = nullptr;  // 3       vertices, triangles, mc vertices
-    uint32_t* fe2mc = nullptr;             // capV    FE vertex index -> MC index
+    uint4* rowcnt = nullptr;               // R      x/y/z cuts, triangles
+    uint2* trims = nullptr;                // R      xl, xr (pass 1 trims)
+    uint32_t* mccnt = nullptr;             // R      MC vertices per cell row
+    unsigned long long* groups = nullptr;  // 3*ngroups  group totals -> offsets
+    unsigned long long* vstart = nullptr;  // R      first vertex of the row
+    unsigned long long* tstart = nullptr;  // R      first triangle of cell row
+    unsigned long long* mstart = nullptr;  // R      first MC vertex of cell row
+    unsigned long long* totals = nullptr;  // 4      vertices, triangles, mc vertices, status
+    uint32_t* bits = nullptr;              // R*W    bit rows (row-wise kernels only)
+    uint32_t* fe2mc = nullptr;             // >= V   FE vertex index -> MC index
+};
+
+// Work split of the counting pass: blocks of J = 256/G grid rows, columns of
+// KC planes, one CTA per (block, column).
+struct CountPlan {
+    int G = 1, J = 1, nyb = 1, KC = 1, nkc = 1;
+    long long ngroups = 0;
+    size_t smem = 0;
+};
+
+// Work split of the column-marching generate kernels.
+struct GenPlan {
+    int G = 32, J = 8, nyb = 1, KC = 1, nkc = 1;
+    size_t smem = 0;
+    bool fits = false;  // false: use the row-wise kernels
 };
 
 int lanes_per_row(int W);
-long long num_tiles(const Grid& g);
+CountPlan count_plan(const Grid& g, int nsm);
+GenPlan gen_plan(const Grid& g, int nsm);
 
-void launch_classify(const float* vol, uint32_t* bits, const Grid& g, float iso, int nsm, cudaStream_t s);
-void launch_count(const uint32_t* bits, const Grid& g, const CaseTables* cases, bool mc, FeBuffers& b,
-                  cudaStream_t s);
-void launch_scan_tiles(const Grid& g, FeBuffers& b, cudaStream_t s);
+// passes 1-3
+void launch_count(const float* vol, const Grid& g, float iso, const CaseTables* cases, bool mc, bool write_bits,
+                  const CountPlan& p, FeBuffers& b, cudaStream_t s);
+void launch_scan(const CountPlan& p, FeBuffers& b, cudaStream_t s);
+void launch_row_starts(const Grid& g, const CountPlan& p, bool mc, FeBuffers& b, cudaStream_t s);
+void launch_grid_edges(const Grid& g, const FeBuffers& b, int scanned, unsigned long long* ge,
+                       unsigned long long* tri_counter, cudaStream_t s);
+
+// pass 4, column-marching (volume slabs staged in shared memory)
 template <typename IndexT>
-void launch_fe_generate(const float* vol, const uint32_t* bits, const Grid& g, float iso, const CaseTables* cases,
-                        const FeBuffers& b, long long capV, long long capT, float* points, float* normals,
-                        IndexT* tris, int nsm, cudaStream_t s);
-void launch_mc_vertices(const float* vol, const uint32_t* bits, const Grid& g, float iso, const CaseTables* cases,
-                        const FeBuffers& b, long long capV, long long capT, float* points, float* normals, int nsm,
+void launch_fe_gen_cols(const float* vol, const Grid& g, float iso, const CaseTables* cases, const FeBuffers& b,
+                        const GenPlan& p, long long capV, long long capT, float* points, float* normals,
+                        IndexT* tris, int reverse, cudaStream_t s);
+void launch_mc_gen_cols(const float* vol, const Grid& g, float iso, const CaseTables* cases, const FeBuffers& b,
+                        const GenPlan& p, long long capV, long long capT, float* points, float* normals, int reverse,
                         cudaStream_t s);
+
+// pass 4, row-wise (bit rows from the count pass)
 template <typename IndexT>
-void launch_mc_triangles(const uint32_t* bits, const Grid& g, const CaseTables* cases, const FeBuffers& b,
-                         long long capV, long long capT, IndexT* tris, int nsm, cudaStream_t s);
-void launch_fe_grid_edges(const Grid& g, const FeBuffers& b, int scanned, unsigned long long* ge,
-                          unsigned long long* tri_counter, cudaStream_t s);
+void launch_fe_gen_rows(const float* vol, const Grid& g, float iso, const CaseTables* cases, const FeBuffers& b,
+                        long long capV, long long capT, float* points, float* normals, IndexT* tris, int nsm,
+                        cudaStream_t s);
+void launch_mc_vertices_rows(const float* vol, const Grid& g, float iso, const CaseTables* cases,
+                             const FeBuffers& b, long long capV, long long capT, float* points, float* normals,
+                             int nsm, cudaStream_t s);
+template <typename IndexT>
+void launch_mc_triangles(const Grid& g, const CaseTables* cases, const FeBuffers& b, long long capV, long long capT,
+                         IndexT* tris, int nsm, cudaStream_t s);
 
 }  // namespace iso
