@@ -130,8 +130,9 @@ bool empty_grid(const Grid& g) { return g.nx < 2 || g.ny < 2 || g.nz < 2; }
 size_t scratch_size(const Grid& g, const iso::CountPlan& cp)
 {
     const size_t R = (size_t)g.R;
-    return align256(R * 16) + align256(R * 8) + align256(R * 4) + align256(3 * (size_t)cp.ngroups * 8) +
-           3 * align256(R * 8) + align256(4 * 8) + align256(R * (size_t)g.W * 4);
+    return align256(R * 16) + align256(R * 8) + align256(R * 4) + align256(R * 16) +
+           align256(3 * (size_t)cp.ngroups * 4) + align256(3 * (size_t)cp.ngroups * 8) + align256(4 * 8) +
+           align256(R * (size_t)g.W * 4);
 }
 
 void carve(void* base, const Grid& g, const iso::CountPlan& cp, FeBuffers& b)
@@ -141,10 +142,9 @@ void carve(void* base, const Grid& g, const iso::CountPlan& cp, FeBuffers& b)
     b.rowcnt = reinterpret_cast<uint4*>(p); p += align256(R * 16);
     b.trims = reinterpret_cast<uint2*>(p); p += align256(R * 8);
     b.mccnt = reinterpret_cast<uint32_t*>(p); p += align256(R * 4);
-    b.groups = reinterpret_cast<unsigned long long*>(p); p += align256(3 * (size_t)cp.ngroups * 8);
-    b.vstart = reinterpret_cast<unsigned long long*>(p); p += align256(R * 8);
-    b.tstart = reinterpret_cast<unsigned long long*>(p); p += align256(R * 8);
-    b.mstart = reinterpret_cast<unsigned long long*>(p); p += align256(R * 8);
+    b.rowpre = reinterpret_cast<uint4*>(p); p += align256(R * 16);
+    b.gsum = reinterpret_cast<uint32_t*>(p); p += align256(3 * (size_t)cp.ngroups * 4);
+    b.goff = reinterpret_cast<unsigned long long*>(p); p += align256(3 * (size_t)cp.ngroups * 8);
     b.totals = reinterpret_cast<unsigned long long*>(p); p += align256(4 * 8);
     b.bits = reinterpret_cast<uint32_t*>(p);
 }
@@ -253,7 +253,6 @@ void enqueue_count(iso_ctx* ctx, iso_algorithm algo, const float* vol, const Gri
     iso::launch_count(vol, g, iso, ctx->d_cases, mc, mc || !pl.gp.fits, pl.cp, b, s);
     pm.mark(ISO_PASS_COUNT);
     iso::launch_scan(pl.cp, b, s);
-    iso::launch_row_starts(g, pl.cp, mc, b, s);
     pm.mark(ISO_PASS_SCAN);
 }
 
@@ -267,34 +266,34 @@ void enqueue_generate(iso_ctx* ctx, iso_algorithm algo, const float* vol, const 
     if (algo == ISO_FLYING_EDGES) {
         if (pl.gp.fits) {
             if (i4)
-                iso::launch_fe_gen_cols<uint32_t>(vol, g, iso, ctx->d_cases, b, pl.gp, capV, capT, out->points,
+                iso::launch_fe_gen_cols<uint32_t>(vol, g, iso, ctx->d_cases, b, pl.cp, pl.gp, capV, capT, out->points,
                                                   out->normals, static_cast<uint32_t*>(out->tris), ctx->reverse, s);
             else
-                iso::launch_fe_gen_cols<uint64_t>(vol, g, iso, ctx->d_cases, b, pl.gp, capV, capT, out->points,
+                iso::launch_fe_gen_cols<uint64_t>(vol, g, iso, ctx->d_cases, b, pl.cp, pl.gp, capV, capT, out->points,
                                                   out->normals, static_cast<uint64_t*>(out->tris), ctx->reverse, s);
         } else {
             if (i4)
-                iso::launch_fe_gen_rows<uint32_t>(vol, g, iso, ctx->d_cases, b, capV, capT, out->points, out->normals,
+                iso::launch_fe_gen_rows<uint32_t>(vol, g, iso, ctx->d_cases, b, pl.cp, capV, capT, out->points, out->normals,
                                                   static_cast<uint32_t*>(out->tris), ctx->nsm, s);
             else
-                iso::launch_fe_gen_rows<uint64_t>(vol, g, iso, ctx->d_cases, b, capV, capT, out->points, out->normals,
+                iso::launch_fe_gen_rows<uint64_t>(vol, g, iso, ctx->d_cases, b, pl.cp, capV, capT, out->points, out->normals,
                                                   static_cast<uint64_t*>(out->tris), ctx->nsm, s);
         }
         pm.mark(ISO_PASS_FE_GENERATE);
     } else {
         const long long capM = capV < 0xffffffffll ? capV : 0xffffffffll;  // fe2mc holds 32-bit ids
         if (pl.gp.fits)
-            iso::launch_mc_gen_cols(vol, g, iso, ctx->d_cases, b, pl.gp, capM, capT, out->points, out->normals,
+            iso::launch_mc_gen_cols(vol, g, iso, ctx->d_cases, b, pl.cp, pl.gp, capM, capT, out->points, out->normals,
                                     ctx->reverse, s);
         else
-            iso::launch_mc_vertices_rows(vol, g, iso, ctx->d_cases, b, capM, capT, out->points, out->normals,
+            iso::launch_mc_vertices_rows(vol, g, iso, ctx->d_cases, b, pl.cp, capM, capT, out->points, out->normals,
                                          ctx->nsm, s);
         pm.mark(ISO_PASS_MC_VERTICES);
         if (i4)
-            iso::launch_mc_triangles<uint32_t>(g, ctx->d_cases, b, capM, capT, static_cast<uint32_t*>(out->tris),
+            iso::launch_mc_triangles<uint32_t>(g, ctx->d_cases, b, pl.cp, capM, capT, static_cast<uint32_t*>(out->tris),
                                                ctx->nsm, s);
         else
-            iso::launch_mc_triangles<uint64_t>(g, ctx->d_cases, b, capM, capT, static_cast<uint64_t*>(out->tris),
+            iso::launch_mc_triangles<uint64_t>(g, ctx->d_cases, b, pl.cp, capM, capT, static_cast<uint64_t*>(out->tris),
                                                ctx->nsm, s);
         pm.mark(ISO_PASS_MC_TRIANGLES);
     }
@@ -648,7 +647,6 @@ iso_status iso_fe_pass3(iso_fe* fe)
     ISO_CUDA(ctx, cudaSetDevice(ctx->device));
     const Plans pl = make_plans(ctx, fe->g);
     iso::launch_scan(pl.cp, fe->buf, 0);
-    iso::launch_row_starts(fe->g, pl.cp, false, fe->buf, 0);
     ISO_CUDA(ctx, cudaGetLastError());
     unsigned long long tot[4];
     ISO_CUDA(ctx, cudaMemcpy(tot, fe->buf.totals, sizeof(tot), cudaMemcpyDeviceToHost));
@@ -709,7 +707,7 @@ iso_status iso_fe_grid_edges(iso_fe* fe, uint64_t* grid_edges, uint64_t* tri_cou
     const size_t nge = (size_t)g.R * 5, ntc = (size_t)(g.ny - 1) * (g.nz - 1);
     unsigned long long* d = nullptr;
     ISO_CUDA(ctx, cudaMalloc(&d, (nge + ntc) * 8));
-    iso::launch_grid_edges(g, fe->buf, fe->stage >= 3 ? 1 : 0, d, d + nge, 0);
+    iso::launch_grid_edges(g, make_plans(ctx, g).cp, fe->buf, fe->stage >= 3 ? 1 : 0, d, d + nge, 0);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpy(grid_edges, d, nge * 8, cudaMemcpyDeviceToHost);
     if (e == cudaSuccess) e = cudaMemcpy(tri_counter, d + nge, ntc * 8, cudaMemcpyDeviceToHost);

@@ -11,86 +11,38 @@
 //                  triangles of cell row (j,k) and, for Marching Cubes, the
 //                  vertices cell row (j,k) owns.  Per (plane, block) totals go
 //                  to `groups`.
+//                  Each row also gets its exclusive prefix inside its group.
 //   k_scan_groups  exclusive scan of the group totals (one CTA); groups are in
-//                  (k, block) order, which is the reference's (k, j) row order.
-//   k_row_starts   first vertex / triangle / MC vertex of every row
-//                  (the gridEdge xstart and triCounter offsets after pass 3).
+//                  (k, block) order, which is the reference's (k, j) row order,
+//                  so the first vertex / triangle / MC vertex of a row (the
+//                  gridEdge xstart and triCounter offsets after pass 3) is
+//                  group offset + row prefix (RowStarts).
 #include "iso_device.cuh"
 #include "iso_kernels.h"
 
 namespace iso {
 
-// Bits of the (J+1) rows j0.. of plane p into dst[jj*W + w] (rows >= nbr are
-// not touched).  All threads of the CTA take part.
+// Bits of the rows j0 .. j0+nbr-1 of plane p into dst[jj*W + w].
 template <bool VEC4>
 __device__ __forceinline__ void classify_rows(const float* __restrict__ vol, const Grid& g, float iso, int p, int j0,
                                               int nbr, uint32_t* __restrict__ dst)
 {
-    const float* base = vol + ((long long)p * g.ny + j0) * g.nx;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (VEC4) {
-        const int nq = g.nx >> 2, nq8 = (nq + 7) & ~7;
-        const int total = nbr * nq8;
-        constexpr int U = 4;
-        for (int f0 = 0; f0 < total; f0 += U * kThreads) {
-            float4 v[U];
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const int f = f0 + u * kThreads + tid;
-                const int jj = f / nq8, q = f - jj * nq8;
-                v[u] = (f < total && q < nq) ? __ldg(reinterpret_cast<const float4*>(base + (long long)jj * g.nx) + q)
-                                             : make_float4(0.f, 0.f, 0.f, 0.f);
-            }
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const int f = f0 + u * kThreads + tid;
-                const int jj = f / nq8, q = f - jj * nq8;
-                const bool ok = f < total && q < nq;
-                uint32_t nib = ok ? ((uint32_t)(v[u].x >= iso) | ((uint32_t)(v[u].y >= iso) << 1) |
-                                     ((uint32_t)(v[u].z >= iso) << 2) | ((uint32_t)(v[u].w >= iso) << 3))
-                                  : 0u;
-                uint32_t word = nib << (4 * (lane & 7));
-                word |= __shfl_xor_sync(0xffffffffu, word, 1);
-                word |= __shfl_xor_sync(0xffffffffu, word, 2);
-                word |= __shfl_xor_sync(0xffffffffu, word, 4);
-                if ((lane & 7) == 0 && ok) dst[jj * g.W + (q >> 3)] = word;
-            }
-        }
-    } else {
-        const int total = nbr * g.W;
-        constexpr int U = 4;
-        for (int f0 = 0; f0 < total; f0 += U * (kThreads / 32)) {
-            float v[U];
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const int f = f0 + u * (kThreads / 32) + warp;
-                const int jj = f / g.W, w = f - jj * g.W, i = 32 * w + lane;
-                v[u] = (f < total && i < g.nx) ? __ldg(base + (long long)jj * g.nx + i) : 0.f;
-            }
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const int f = f0 + u * (kThreads / 32) + warp;
-                const int jj = f / g.W, w = f - jj * g.W, i = 32 * w + lane;
-                const uint32_t word = __ballot_sync(0xffffffffu, f < total && i < g.nx && v[u] >= iso);
-                if (lane == 0 && f < total) dst[f] = word;
-            }
-        }
-    }
+    classify_block<VEC4, false>(vol + ((long long)p * g.ny + j0) * g.nx, g.nx, g.W, nbr, iso, dst);
 }
 
 template <int G, bool MC, bool VEC4>
 __global__ void __launch_bounds__(kThreads) k_count_cols(const float* __restrict__ vol, Grid g, float iso, int KC,
                                                          int nyb, const CaseTables* __restrict__ cases,
                                                          uint4* __restrict__ rowcnt, uint2* __restrict__ trims,
-                                                         uint32_t* __restrict__ mccnt,
-                                                         unsigned long long* __restrict__ groups, long long ngroups,
+                                                         uint32_t* __restrict__ mccnt, uint4* __restrict__ rowpre,
+                                                         uint32_t* __restrict__ gsum, long long ngroups,
                                                          uint32_t* __restrict__ bits_out)
 {
     constexpr int J = kThreads / G;  // grid rows per block
     extern __shared__ uint32_t s_dyn[];
     __shared__ uint8_t s_ntris[256];
     __shared__ uint16_t s_cut[256];
-    __shared__ unsigned long long s_sum[3];
+    __shared__ uint32_t s_rc[3][J];
     uint32_t* s_bits0 = s_dyn;
     uint32_t* s_bits1 = s_dyn + (J + 1) * g.W;
     for (int c = threadIdx.x; c < 256; c += blockDim.x) {
@@ -109,7 +61,6 @@ __global__ void __launch_bounds__(kThreads) k_count_cols(const float* __restrict
     for (int k = kb; k < ke; ++k) {
         uint32_t* P0 = (k & 1) ? s_bits1 : s_bits0;        // plane k
         uint32_t* P1 = (k & 1) ? s_bits0 : s_bits1;        // plane k+1
-        if (tid < 3) s_sum[tid] = 0;
         if (k + 1 < g.nz) classify_rows<VEC4>(vol, g, iso, k + 1, j0, nbr, P1);
         __syncthreads();
 
@@ -170,105 +121,122 @@ __global__ void __launch_bounds__(kThreads) k_count_cols(const float* __restrict
         }
         first = group_min<G>(first, 0xffffffffu);
         last = group_max<G>(last, 0xffffffffu);
-        if (lig == 0 && valid) {
-            const long long r = (long long)k * g.ny + j;
-            rowcnt[r] = make_uint4(xc, yc, zc, tc);
-            trims[r] = make_uint2(first == 0xffffffffu ? (uint32_t)g.nx : first, last);
-            if (MC) mccnt[r] = mc;
-            atomicAdd(&s_sum[0], (unsigned long long)(xc + yc + zc));
-            atomicAdd(&s_sum[1], (unsigned long long)tc);
-            if (MC) atomicAdd(&s_sum[2], (unsigned long long)mc);
+        if (lig == 0) {
+            if (valid) {
+                const long long r = (long long)k * g.ny + j;
+                rowcnt[r] = make_uint4(xc, yc, zc, tc);
+                trims[r] = make_uint2(first == 0xffffffffu ? (uint32_t)g.nx : first, last);
+                if (MC) mccnt[r] = mc;
+            }
+            s_rc[0][jj] = valid ? xc + yc + zc : 0u;
+            s_rc[1][jj] = valid ? tc : 0u;
+            s_rc[2][jj] = valid ? mc : 0u;
         }
         __syncthreads();
-        if (tid < 3) groups[tid * ngroups + (long long)k * nyb + jb] = s_sum[tid];
+        // exclusive prefix of the block's rows (warp 0) and the group totals
+        if (tid < 32) {
+            uint32_t run[3] = {0, 0, 0};
+            for (int base = 0; base < J; base += 32) {
+                const int q = base + tid;
+                uint32_t v[3], inc[3];
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    v[a] = q < J ? s_rc[a][q] : 0u;
+                    inc[a] = v[a];
+                }
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1) {
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) {
+                        const uint32_t t = __shfl_up_sync(0xffffffffu, inc[a], d);
+                        if (tid >= d) inc[a] += t;
+                    }
+                }
+                if (q < JB) {
+                    rowpre[(long long)k * g.ny + j0 + q] =
+                        make_uint4(run[0] + inc[0] - v[0], run[1] + inc[1] - v[1], run[2] + inc[2] - v[2], 0u);
+                }
+#pragma unroll
+                for (int a = 0; a < 3; ++a) run[a] += __shfl_sync(0xffffffffu, inc[a], 31);
+            }
+            if (tid < 3) gsum[tid * ngroups + (long long)k * nyb + jb] = run[tid];
+        }
+        __syncthreads();
     }
 }
 
-// Exclusive scan of three arrays of n u64 (in place) + grand totals; one CTA.
-__global__ void __launch_bounds__(1024) k_scan_groups(unsigned long long* __restrict__ a, long long n,
+// Exclusive scan of the group totals (three arrays of n u32) into 64-bit
+// offsets, plus the grand totals; one CTA.  Each thread owns kScanPer
+// consecutive groups of a segment of 1024*kScanPer; segments are walked with
+// a running carry.
+constexpr int kScanPer = 16;
+
+__global__ void __launch_bounds__(1024) k_scan_groups(const uint32_t* __restrict__ gsum, long long n,
+                                                      unsigned long long* __restrict__ goff,
                                                       unsigned long long* __restrict__ totals)
 {
     __shared__ unsigned long long s_w[3][32];
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    const long long per = (n + blockDim.x - 1) / blockDim.x;
-    const long long b = t * per, e = min(n, b + per);
-    unsigned long long s[3] = {0, 0, 0}, incl[3];
-    for (long long q = b; q < e; ++q) {
+    unsigned long long carry[3] = {0, 0, 0};
+    for (long long seg = 0; seg < n; seg += 1024LL * kScanPer) {
+        const long long b = seg + (long long)t * kScanPer;
+        uint32_t v[3][kScanPer];
+        unsigned long long s[3] = {0, 0, 0};
 #pragma unroll
-        for (int x = 0; x < 3; ++x) s[x] += a[x * n + q];
-    }
+        for (int a = 0; a < 3; ++a) {
 #pragma unroll
-    for (int x = 0; x < 3; ++x) incl[x] = s[x];
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-#pragma unroll
-        for (int x = 0; x < 3; ++x) {
-            const unsigned long long y = __shfl_up_sync(0xffffffffu, incl[x], d);
-            if (lane >= d) incl[x] += y;
+            for (int q = 0; q < kScanPer; ++q) {
+                v[a][q] = b + q < n ? __ldg(&gsum[a * n + b + q]) : 0u;
+                s[a] += v[a][q];
+            }
         }
-    }
-    if (lane == 31) {
+        unsigned long long inc[3] = {s[0], s[1], s[2]};
 #pragma unroll
-        for (int x = 0; x < 3; ++x) s_w[x][warp] = incl[x];
-    }
-    __syncthreads();
-    unsigned long long run[3] = {0, 0, 0}, tot[3] = {0, 0, 0};
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+        for (int d = 1; d < 32; d <<= 1) {
 #pragma unroll
-        for (int x = 0; x < 3; ++x) {
-            if (w < warp) run[x] += s_w[x][w];
-            tot[x] += s_w[x][w];
+            for (int a = 0; a < 3; ++a) {
+                const unsigned long long y = __shfl_up_sync(0xffffffffu, inc[a], d);
+                if (lane >= d) inc[a] += y;
+            }
         }
-    }
+        if (lane == 31) {
 #pragma unroll
-    for (int x = 0; x < 3; ++x) run[x] += incl[x] - s[x];
-    for (long long q = b; q < e; ++q) {
-#pragma unroll
-        for (int x = 0; x < 3; ++x) {
-            const unsigned long long y = a[x * n + q];
-            a[x * n + q] = run[x];
-            run[x] += y;
+            for (int a = 0; a < 3; ++a) s_w[a][warp] = inc[a];
         }
+        __syncthreads();
+        unsigned long long before[3] = {0, 0, 0}, tot[3] = {0, 0, 0};
+        for (int w = 0; w < 32; ++w) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                if (w < warp) before[a] += s_w[a][w];
+                tot[a] += s_w[a][w];
+            }
+        }
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            unsigned long long run = carry[a] + before[a] + inc[a] - s[a];
+#pragma unroll
+            for (int q = 0; q < kScanPer; ++q) {
+                if (b + q < n) goff[a * n + b + q] = run;
+                run += v[a][q];
+            }
+            carry[a] += tot[a];
+        }
+        __syncthreads();
     }
     if (t == 0) {
-        totals[0] = tot[0];
-        totals[1] = tot[1];
-        totals[2] = tot[2];
+        totals[0] = carry[0];
+        totals[1] = carry[1];
+        totals[2] = carry[2];
         totals[3] = 0;  // device status, set by the generate kernels
-    }
-}
-
-// One thread per group (plane k, block of J rows): row starts in order.
-__global__ void k_row_starts(Grid g, int J, int nyb, const unsigned long long* __restrict__ groups, long long ngroups,
-                             const uint4* __restrict__ rowcnt, const uint32_t* __restrict__ mccnt,
-                             unsigned long long* __restrict__ vstart, unsigned long long* __restrict__ tstart,
-                             unsigned long long* __restrict__ mstart)
-{
-    const long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gi >= ngroups) return;
-    const int k = (int)(gi / nyb), jb = (int)(gi % nyb);
-    const int j0 = jb * J, JB = min(J, g.ny - j0);
-    unsigned long long v = groups[gi], t = groups[ngroups + gi], m = groups[2 * ngroups + gi];
-    for (int jj = 0; jj < JB; ++jj) {
-        const long long r = (long long)k * g.ny + j0 + jj;
-        const uint4 c = rowcnt[r];
-        vstart[r] = v;
-        tstart[r] = t;
-        v += (unsigned long long)c.x + c.y + c.z;
-        t += c.w;
-        if (mstart) {
-            mstart[r] = m;
-            m += mccnt[r];
-        }
     }
 }
 
 // gridEdge records {xl, xr, xstart, ystart, zstart} and triCounter for
 // inspection (counts before the scan, offsets after it).
-__global__ void k_grid_edges(Grid g, const uint4* __restrict__ rowcnt, const uint2* __restrict__ trims,
-                             const unsigned long long* __restrict__ vstart,
-                             const unsigned long long* __restrict__ tstart, int scanned,
-                             unsigned long long* __restrict__ ge, unsigned long long* __restrict__ tri_counter)
+__global__ void k_grid_edges(Grid g, RowStarts rs, const uint4* __restrict__ rowcnt, const uint2* __restrict__ trims,
+                             int scanned, unsigned long long* __restrict__ ge,
+                             unsigned long long* __restrict__ tri_counter)
 {
     const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= g.R) return;
@@ -278,13 +246,13 @@ __global__ void k_grid_edges(Grid g, const uint4* __restrict__ rowcnt, const uin
     o[0] = tr.x;
     o[1] = tr.y;
     if (scanned) {
-        const unsigned long long b = vstart[r];
+        const unsigned long long b = rs.get(r, 0);
         o[2] = b; o[3] = b + c.x; o[4] = b + c.x + c.y;
     } else {
         o[2] = c.x; o[3] = c.y; o[4] = c.z;
     }
     const int j = (int)(r % g.ny), k = (int)(r / g.ny);
-    if (j < g.ny - 1 && k < g.nz - 1) tri_counter[(long long)k * (g.ny - 1) + j] = scanned ? tstart[r] : c.w;
+    if (j < g.ny - 1 && k < g.nz - 1) tri_counter[(long long)k * (g.ny - 1) + j] = scanned ? rs.get(r, 1) : c.w;
 }
 
 // ---------------------------------------------------------------------------
@@ -335,13 +303,13 @@ static void count_cols_vec(bool vec4, const CountPlan& p, const float* vol, cons
     if (vec4) {
         auto kern = k_count_cols<G, MC, true>;
         if (p.smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.smem);
-        kern<<<blocks, kThreads, p.smem, s>>>(vol, g, iso, p.KC, p.nyb, cases, b.rowcnt, b.trims, b.mccnt, b.groups,
-                                              p.ngroups, bo);
+        kern<<<blocks, kThreads, p.smem, s>>>(vol, g, iso, p.KC, p.nyb, cases, b.rowcnt, b.trims, b.mccnt, b.rowpre,
+                                              b.gsum, p.ngroups, bo);
     } else {
         auto kern = k_count_cols<G, MC, false>;
         if (p.smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.smem);
-        kern<<<blocks, kThreads, p.smem, s>>>(vol, g, iso, p.KC, p.nyb, cases, b.rowcnt, b.trims, b.mccnt, b.groups,
-                                              p.ngroups, bo);
+        kern<<<blocks, kThreads, p.smem, s>>>(vol, g, iso, p.KC, p.nyb, cases, b.rowcnt, b.trims, b.mccnt, b.rowpre,
+                                              b.gsum, p.ngroups, bo);
     }
 }
 
@@ -358,21 +326,28 @@ void launch_count(const float* vol, const Grid& g, float iso, const CaseTables* 
 
 void launch_scan(const CountPlan& p, FeBuffers& b, cudaStream_t s)
 {
-    k_scan_groups<<<1, 1024, 0, s>>>(b.groups, p.ngroups, b.totals);
+    k_scan_groups<<<1, 1024, 0, s>>>(b.gsum, p.ngroups, b.goff, b.totals);
 }
 
-void launch_row_starts(const Grid& g, const CountPlan& p, bool mc, FeBuffers& b, cudaStream_t s)
+RowStarts row_starts(const Grid& g, const CountPlan& p, const FeBuffers& b)
 {
-    const unsigned blocks = (unsigned)((p.ngroups + 255) / 256);
-    k_row_starts<<<blocks, 256, 0, s>>>(g, p.J, p.nyb, b.groups, p.ngroups, b.rowcnt, b.mccnt, b.vstart, b.tstart,
-                                        mc ? b.mstart : nullptr);
+    RowStarts rs;
+    rs.goff = b.goff;
+    rs.rowpre = b.rowpre;
+    rs.ngroups = p.ngroups;
+    rs.ny = g.ny;
+    rs.nyb = p.nyb;
+    int sh = 0;
+    while ((1 << sh) < p.J) ++sh;
+    rs.jshift = sh;
+    return rs;
 }
 
-void launch_grid_edges(const Grid& g, const FeBuffers& b, int scanned, unsigned long long* ge,
+void launch_grid_edges(const Grid& g, const CountPlan& p, const FeBuffers& b, int scanned, unsigned long long* ge,
                        unsigned long long* tri_counter, cudaStream_t s)
 {
     const long long blocks = (g.R + 255) / 256;
-    k_grid_edges<<<(unsigned)blocks, 256, 0, s>>>(g, b.rowcnt, b.trims, b.vstart, b.tstart, scanned, ge,
+    k_grid_edges<<<(unsigned)blocks, 256, 0, s>>>(g, row_starts(g, p, b), b.rowcnt, b.trims, scanned, ge,
                                                   tri_counter);
 }
 

@@ -149,8 +149,7 @@ __device__ __forceinline__ int search_le(const uint32_t* __restrict__ F, int n, 
 template <int G, bool MC, typename IndexT, bool BULK>
 __global__ void __launch_bounds__(kThreads) k_gen_cols(
     const float* __restrict__ vol, Grid g, float iso, int KC, int nyb, const CaseTables* __restrict__ cases,
-    const uint4* __restrict__ rowcnt, const uint32_t* __restrict__ mccnt, const unsigned long long* __restrict__ vstart,
-    const unsigned long long* __restrict__ tstart, const unsigned long long* __restrict__ mstart,
+    const uint4* __restrict__ rowcnt, const uint32_t* __restrict__ mccnt, RowStarts rs,
     unsigned long long* __restrict__ totals, long long capV, long long capT, float* __restrict__ points,
     float* __restrict__ normals, IndexT* __restrict__ tris, uint32_t* __restrict__ fe2mc, int reverse)
 {
@@ -178,6 +177,7 @@ __global__ void __launch_bounds__(kThreads) k_gen_cols(
     const int tid = threadIdx.x, lane = tid & 31, lig = lane & (G - 1);
     const int nchunks = (W + G - 1) / G;
     const int nfl = nbr * g.nx;
+    const float invW = 1.0f / (float)W, inv3W = 1.0f / (float)(3 * W);
 
     if (tid == 0) {
         for (int s = 0; s < kSlots; ++s) mbar_init(&S.mbar[s], BULK ? 1u : (unsigned)kThreads);
@@ -231,44 +231,20 @@ __global__ void __launch_bounds__(kThreads) k_gen_cols(
         const float* slab = S.slots + (size_t)(p % kSlots) * L.slab_floats;
         uint32_t* bits = S.bits(b);
         // (a) bit mask from the slab
-        if ((g.nx & 3) == 0) {
-            const int nq = g.nx >> 2, nq8 = (nq + 7) & ~7, total = nbr * nq8;
-            for (int f0 = 0; f0 < total; f0 += kThreads) {
-                const int f = f0 + tid, jj = f / nq8, q = f - jj * nq8;
-                const bool ok = f < total && q < nq;
-                uint32_t nib = 0;
-                if (ok) {
-                    const float4 v = reinterpret_cast<const float4*>(slab + jj * g.nx)[q];
-                    nib = (uint32_t)(v.x >= iso) | ((uint32_t)(v.y >= iso) << 1) | ((uint32_t)(v.z >= iso) << 2) |
-                          ((uint32_t)(v.w >= iso) << 3);
-                }
-                uint32_t word = nib << (4 * (lane & 7));
-                word |= __shfl_xor_sync(0xffffffffu, word, 1);
-                word |= __shfl_xor_sync(0xffffffffu, word, 2);
-                word |= __shfl_xor_sync(0xffffffffu, word, 4);
-                if ((lane & 7) == 0 && ok) bits[jj * W + (q >> 3)] = word;
-            }
-        } else {
-            const int warp = tid >> 5, total = nbr * W;
-            for (int f0 = 0; f0 < total; f0 += kThreads / 32) {
-                const int f = f0 + warp, jj = f / W, w = f - jj * W, i = 32 * w + lane;
-                const bool ok = f < total && i < g.nx;
-                const uint32_t word = __ballot_sync(0xffffffffu, ok && slab[jj * g.nx + i] >= iso);
-                if (lane == 0 && f < total) bits[f] = word;
-            }
-        }
+        if ((g.nx & 3) == 0) classify_block<true, true>(slab, g.nx, W, nbr, iso, bits);
+        else classify_block<false, true>(slab, g.nx, W, nbr, iso, bits);
         // (b) first vertex ids of the rows (gridEdge xstart/ystart/zstart)
         if (tid < nbr) {
             const long long r = (long long)p * g.ny + j0 + tid;
             const uint4 c = __ldg(&rowcnt[r]);
-            const unsigned long long x0 = __ldg(&vstart[r]);
+            const unsigned long long x0 = rs.get(p, j0 + tid, 0);
             S.xs(b)[tid] = x0;
             S.ys(b)[tid] = x0 + c.x;
             S.zs(b)[tid] = x0 + c.x + c.y;
             S.ze(b)[tid] = x0 + c.x + c.y + c.z;
             if (tid < JB) {
-                S.ts(b)[tid] = __ldg(&tstart[r]);
-                if (MC) S.ms(b)[tid] = __ldg(&mstart[r]);
+                S.ts(b)[tid] = rs.get(p, j0 + tid, 1);
+                if (MC) S.ms(b)[tid] = rs.get(p, j0 + tid, 2);
             }
         }
         __syncthreads();
@@ -342,7 +318,8 @@ __global__ void __launch_bounds__(kThreads) k_gen_cols(
             const int nF = JB * 3 * W;
             const unsigned long long vbase = S.xs(b0)[0];
             for (int q = tid; q < nF; q += kThreads) {
-                const int jj = q / (3 * W), rem = q - jj * 3 * W, axis = rem / W, w = rem - axis * W;
+                const int jj = fastdiv(q, 3 * W, inv3W), rem = q - jj * 3 * W, axis = fastdiv(rem, W, invW),
+                          w = rem - axis * W;
                 const unsigned long long st = axis == 0 ? S.xs(b0)[jj] : (axis == 1 ? S.ys(b0)[jj] : S.zs(b0)[jj]);
                 const uint32_t pre = axis == 0 ? S.px(b0)[jj * W + w] : (axis == 1 ? S.py(b0)[jj * W + w] : S.pz()[jj * W + w]);
                 S.F[q] = (uint32_t)(st - vbase) + pre;
@@ -351,7 +328,8 @@ __global__ void __launch_bounds__(kThreads) k_gen_cols(
             const uint32_t nv = (uint32_t)(S.ze(b0)[JB - 1] - vbase);
             for (uint32_t e = tid; e < nv; e += kThreads) {
                 const int idx = search_le(S.F, nF, e);
-                const int jj = idx / (3 * W), rem = idx - jj * 3 * W, axis = rem / W, w = rem - axis * W;
+                const int jj = fastdiv(idx, 3 * W, inv3W), rem = idx - jj * 3 * W, axis = fastdiv(rem, W, invW),
+                          w = rem - axis * W;
                 const uint32_t m = axis == 0 ? S.mx(b0)[jj * W + w] : (axis == 1 ? S.my(b0)[jj * W + w] : S.mz()[jj * W + w]);
                 const int bit = (int)__fns(m, 0, (int)(e - S.F[idx]) + 1);
                 const int i = 32 * w + bit, j = j0 + jj;
@@ -440,13 +418,13 @@ __global__ void __launch_bounds__(kThreads) k_gen_cols(
             const int ncr = min(JB, g.ny - 1 - j0);  // cell rows in the block
             __syncthreads();
             const unsigned long long mbase = S.ms(b0)[0];
-            const uint32_t nv = ncr > 0 ? (uint32_t)(__ldg(&mstart[(long long)k * g.ny + j0 + ncr - 1]) +
+            const uint32_t nv = ncr > 0 ? (uint32_t)(rs.get(k, j0 + ncr - 1, 2) +
                                                      __ldg(&mccnt[(long long)k * g.ny + j0 + ncr - 1]) - mbase)
                                         : 0u;
             const int nF = ncr * W;
             for (uint32_t e = tid; e < nv; e += kThreads) {
                 const int idx = search_le(S.F, nF, e);
-                const int jr = idx / W, w = idx - jr * W, jrow = j0 + jr;
+                const int jr = fastdiv(idx, W, invW), w = idx - jr * W, jrow = j0 + jr;
                 uint32_t rank = e - S.F[idx];
                 const uint32_t* A = S.bits(b0) + jr * W;
                 const uint32_t* Cc = S.bits(b1) + jr * W;
@@ -511,18 +489,18 @@ __global__ void __launch_bounds__(kThreads) k_gen_cols(
 
 template <bool MC, typename IndexT>
 void launch_gen_cols_impl(const float* vol, const Grid& g, float iso, const CaseTables* cases, const FeBuffers& b,
-                          const GenPlan& p, long long capV, long long capT, float* points, float* normals,
-                          IndexT* tris, int reverse, cudaStream_t s)
+                          const CountPlan& cp, const GenPlan& p, long long capV, long long capT, float* points,
+                          float* normals, IndexT* tris, int reverse, cudaStream_t s)
 {
+    const RowStarts rs = row_starts(g, cp, b);
     const bool bulk = (g.nx % 4 == 0) && ((reinterpret_cast<uintptr_t>(vol) & 15) == 0);
     const unsigned blocks = (unsigned)(p.nyb * p.nkc);
 #define ISO_GEN_LAUNCH(GG)                                                                                       \
     {                                                                                                            \
         auto kern = bulk ? k_gen_cols<GG, MC, IndexT, true> : k_gen_cols<GG, MC, IndexT, false>;                \
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.smem);                   \
-        kern<<<blocks, kThreads, p.smem, s>>>(vol, g, iso, p.KC, p.nyb, cases, b.rowcnt, b.mccnt, b.vstart,      \
-                                              b.tstart, b.mstart, b.totals, capV, capT, points, normals, tris,  \
-                                              b.fe2mc, reverse);                                                 \
+        kern<<<blocks, kThreads, p.smem, s>>>(vol, g, iso, p.KC, p.nyb, cases, b.rowcnt, b.mccnt, rs, b.totals,   \
+                                              capV, capT, points, normals, tris, b.fe2mc, reverse);              \
     }
     switch (p.G) {
         case 4: ISO_GEN_LAUNCH(4) break;

@@ -37,17 +37,17 @@ GenPlan gen_plan(const Grid& g, int nsm)
 
 template <typename IndexT>
 void launch_fe_gen_cols(const float* vol, const Grid& g, float iso, const CaseTables* cases, const FeBuffers& b,
-                        const GenPlan& p, long long capV, long long capT, float* points, float* normals,
-                        IndexT* tris, int reverse, cudaStream_t s)
+                        const CountPlan& cp, const GenPlan& p, long long capV, long long capT, float* points,
+                        float* normals, IndexT* tris, int reverse, cudaStream_t s)
 {
-    launch_gen_cols_impl<false, IndexT>(vol, g, iso, cases, b, p, capV, capT, points, normals, tris, reverse, s);
+    launch_gen_cols_impl<false, IndexT>(vol, g, iso, cases, b, cp, p, capV, capT, points, normals, tris, reverse, s);
 }
 
 template void launch_fe_gen_cols<uint32_t>(const float*, const Grid&, float, const CaseTables*, const FeBuffers&,
-                                           const GenPlan&, long long, long long, float*, float*, uint32_t*, int,
-                                           cudaStream_t);
+                                           const CountPlan&, const GenPlan&, long long, long long, float*, float*,
+                                           uint32_t*, int, cudaStream_t);
 template void launch_fe_gen_cols<uint64_t>(const float*, const Grid&, float, const CaseTables*, const FeBuffers&,
-                                           const GenPlan&, long long, long long, float*, float*, uint64_t*, int,
-                                           cudaStream_t);
+                                           const CountPlan&, const GenPlan&, long long, long long, float*, float*,
+                                           uint64_t*, int, cudaStream_t);
 
 }  // namespace iso

@@ -11,8 +11,7 @@ namespace iso {
 template <int G, typename IndexT, bool EMIT_VERTS, bool MAPPED>
 __global__ void __launch_bounds__(kThreads) k_gen_rows(
     const float* __restrict__ vol, const uint32_t* __restrict__ bits, Grid g, float iso,
-    const CaseTables* __restrict__ cases, const uint4* __restrict__ rowcnt,
-    const unsigned long long* __restrict__ vstart, const unsigned long long* __restrict__ tstart,
+    const CaseTables* __restrict__ cases, const uint4* __restrict__ rowcnt, RowStarts rs,
     const unsigned long long* __restrict__ totals,
     long long capV, long long capT, float* __restrict__ points, float* __restrict__ normals,
     IndexT* __restrict__ tris, const uint32_t* __restrict__ fe2mc)
@@ -41,19 +40,19 @@ __global__ void __launch_bounds__(kThreads) k_gen_rows(
         unsigned long long tb = 0;
         if (valid) {
             const uint4 cA = __ldg(&rowcnt[r]);
-            base.xA = __ldg(&vstart[r]);
+            base.xA = rs.get(r, 0);
             base.yA = base.xA + cA.x;
             base.zA = base.yA + cA.y;
             if (cell) {
                 const long long rB = r + 1, rC = r + g.ny, rD = rC + 1;
                 const uint4 cB = __ldg(&rowcnt[rB]);
                 const uint4 cC = __ldg(&rowcnt[rC]);
-                base.xB = __ldg(&vstart[rB]);
+                base.xB = rs.get(rB, 0);
                 base.zB = base.xB + cB.x + cB.y;
-                base.xC = __ldg(&vstart[rC]);
+                base.xC = rs.get(rC, 0);
                 base.yC = base.xC + cC.x;
-                base.xD = __ldg(&vstart[rD]);
-                tb = __ldg(&tstart[r]);
+                base.xD = rs.get(rD, 0);
+                tb = rs.get(r, 1);
             }
         }
         const int cj = min(j, g.ny - 2), ck = min(k, g.nz - 2);
@@ -133,8 +132,7 @@ __global__ void __launch_bounds__(kThreads) k_gen_rows(
 template <int G>
 __global__ void __launch_bounds__(kThreads) k_mc_vertices_rows(
     const float* __restrict__ vol, const uint32_t* __restrict__ bits, Grid g, float iso,
-    const CaseTables* __restrict__ cases, const uint4* __restrict__ rowcnt,
-    const unsigned long long* __restrict__ vstart, const unsigned long long* __restrict__ mstart,
+    const CaseTables* __restrict__ cases, const uint4* __restrict__ rowcnt, RowStarts rs,
     const unsigned long long* __restrict__ totals,
     long long capV, long long capT, float* __restrict__ points, float* __restrict__ normals,
     uint32_t* __restrict__ fe2mc)
@@ -165,15 +163,15 @@ __global__ void __launch_bounds__(kThreads) k_mc_vertices_rows(
             const long long rB = r + 1, rC = r + g.ny, rD = rC + 1;
             const uint4 cB = __ldg(&rowcnt[rB]);
             const uint4 cC = __ldg(&rowcnt[rC]);
-            base.xA = __ldg(&vstart[r]);
+            base.xA = rs.get(r, 0);
             base.yA = base.xA + cA.x;
             base.zA = base.yA + cA.y;
-            base.xB = __ldg(&vstart[rB]);
+            base.xB = rs.get(rB, 0);
             base.zB = base.xB + cB.x + cB.y;
-            base.xC = __ldg(&vstart[rC]);
+            base.xC = rs.get(rC, 0);
             base.yC = base.xC + cC.x;
-            base.xD = __ldg(&vstart[rD]);
-            mb = __ldg(&mstart[r]);
+            base.xD = rs.get(rD, 0);
+            mb = rs.get(r, 2);
         }
         for (int ch = 0; ch < nchunks; ++ch) {
             const int w = ch * G + lig;
@@ -263,41 +261,44 @@ static long long row_blocks(const Grid& g, int nsm)
 
 template <typename IndexT>
 void launch_fe_gen_rows(const float* vol, const Grid& g, float iso, const CaseTables* cases, const FeBuffers& b,
-                        long long capV, long long capT, float* points, float* normals, IndexT* tris, int nsm,
-                        cudaStream_t s)
+                        const CountPlan& cp, long long capV, long long capT, float* points, float* normals,
+                        IndexT* tris, int nsm, cudaStream_t s)
 {
     const unsigned blocks = (unsigned)row_blocks(g, nsm);
+    const RowStarts rs = row_starts(g, cp, b);
     ISO_DISPATCH_G(lanes_per_row(g.W), (k_gen_rows<kG, IndexT, true, false><<<blocks, kThreads, 0, s>>>(
-                                           vol, b.bits, g, iso, cases, b.rowcnt, b.vstart, b.tstart, b.totals, capV,
-                                           capT, points, normals, tris, nullptr)));
+                                           vol, b.bits, g, iso, cases, b.rowcnt, rs, b.totals, capV, capT, points,
+                                           normals, tris, nullptr)));
 }
 
 template <typename IndexT>
-void launch_mc_triangles(const Grid& g, const CaseTables* cases, const FeBuffers& b, long long capV, long long capT,
-                         IndexT* tris, int nsm, cudaStream_t s)
+void launch_mc_triangles(const Grid& g, const CaseTables* cases, const FeBuffers& b, const CountPlan& cp,
+                         long long capV, long long capT, IndexT* tris, int nsm, cudaStream_t s)
 {
     const unsigned blocks = (unsigned)row_blocks(g, nsm);
+    const RowStarts rs = row_starts(g, cp, b);
     ISO_DISPATCH_G(lanes_per_row(g.W), (k_gen_rows<kG, IndexT, false, true><<<blocks, kThreads, 0, s>>>(
-                                           nullptr, b.bits, g, 0.f, cases, b.rowcnt, b.vstart, b.tstart, b.totals,
-                                           capV, capT, nullptr, nullptr, tris, b.fe2mc)));
+                                           nullptr, b.bits, g, 0.f, cases, b.rowcnt, rs, b.totals, capV, capT,
+                                           nullptr, nullptr, tris, b.fe2mc)));
 }
 
 void launch_mc_vertices_rows(const float* vol, const Grid& g, float iso, const CaseTables* cases,
-                             const FeBuffers& b, long long capV, long long capT, float* points, float* normals,
-                             int nsm, cudaStream_t s)
+                             const FeBuffers& b, const CountPlan& cp, long long capV, long long capT, float* points,
+                             float* normals, int nsm, cudaStream_t s)
 {
     const unsigned blocks = (unsigned)row_blocks(g, nsm);
+    const RowStarts rs = row_starts(g, cp, b);
     ISO_DISPATCH_G(lanes_per_row(g.W), (k_mc_vertices_rows<kG><<<blocks, kThreads, 0, s>>>(
-                                           vol, b.bits, g, iso, cases, b.rowcnt, b.vstart, b.mstart, b.totals, capV,
-                                           capT, points, normals, b.fe2mc)));
+                                           vol, b.bits, g, iso, cases, b.rowcnt, rs, b.totals, capV, capT, points,
+                                           normals, b.fe2mc)));
 }
 
 #define ISO_INST(IndexT)                                                                                        \
     template void launch_fe_gen_rows<IndexT>(const float*, const Grid&, float, const CaseTables*,              \
-                                             const FeBuffers&, long long, long long, float*, float*, IndexT*,  \
-                                             int, cudaStream_t);                                               \
-    template void launch_mc_triangles<IndexT>(const Grid&, const CaseTables*, const FeBuffers&, long long,     \
-                                              long long, IndexT*, int, cudaStream_t);
+                                             const FeBuffers&, const CountPlan&, long long, long long, float*, \
+                                             float*, IndexT*, int, cudaStream_t);                              \
+    template void launch_mc_triangles<IndexT>(const Grid&, const CaseTables*, const FeBuffers&,               \
+                                              const CountPlan&, long long, long long, IndexT*, int, cudaStream_t);
 ISO_INST(uint32_t)
 ISO_INST(uint64_t)
 #undef ISO_INST

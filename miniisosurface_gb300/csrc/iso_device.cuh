@@ -6,9 +6,10 @@
 //                          edges owned by the row, triangles of cell row (j,k)
 //   trims   uint2[R]       xl, xr of the row (FlyingEdgesAlgorithm.cpp:47-65)
 //   mccnt   uint32[R]      marching cubes: vertices owned by cell row (j,k)
-//   groups  u64[3][ngroups] per group (plane k, block of J rows): totals of
-//                          (vertices, triangles, mc vertices), scanned in place
-//   vstart, tstart, mstart  u64[R]  first vertex / triangle / mc vertex of a row
+//   gsum    u32[3][ngroups] per group (plane k, block of J rows): totals of
+//                          (vertices, triangles, mc vertices)
+//   goff    u64[3][ngroups] exclusive scan of gsum
+//   rowpre  uint4[R]       the row's exclusive prefix inside its group
 //   bits    uint32[R][W]   W = ceil(nx/32); bit i of row r = value >= isovalue
 //                          (written only when a row-wise kernel needs it)
 //   totals  u64[4]         vertices, triangles, mc vertices, device status
@@ -259,23 +260,112 @@ struct CutBases {
     unsigned long long xA, xB, xC, xD, yA, yC, zA, zB;
 };
 
-// Flying Edges vertex id of cube edge e of cell `bit` of the word.
+// Flying Edges vertex id of cube edge e of cell `bit` of the word, without
+// branches (lanes of a warp usually ask for different edges):
+//   e : 0  1  2  3  4  5  6  7  8  9  10 11
+//   mask xA yA xB yA xC yC xD yC zA zA zB zB    (index 0..7 below)
+//   +1  .  1  .  .  .  1  .  .  .  1  .  1      (edge at point i+1)
 __device__ __forceinline__ unsigned long long fe_edge_id(const CutMasks& m, const CutBases& b, int e, int bit)
 {
-    switch (e) {
-        case 0: return b.xA + __popc(m.xA & lowmask(bit));
-        case 2: return b.xB + __popc(m.xB & lowmask(bit));
-        case 4: return b.xC + __popc(m.xC & lowmask(bit));
-        case 6: return b.xD + __popc(m.xD & lowmask(bit));
-        case 3: return b.yA + __popc(m.yA & lowmask(bit));
-        case 1: return b.yA + __popc(m.yA & lowmask(bit + 1));
-        case 7: return b.yC + __popc(m.yC & lowmask(bit));
-        case 5: return b.yC + __popc(m.yC & lowmask(bit + 1));
-        case 8: return b.zA + __popc(m.zA & lowmask(bit));
-        case 9: return b.zA + __popc(m.zA & lowmask(bit + 1));
-        case 10: return b.zB + __popc(m.zB & lowmask(bit));
-        default: return b.zB + __popc(m.zB & lowmask(bit + 1));
+    // mask index per edge: xA=0 xB=1 xC=2 xD=3 yA=4 yC=5 zA=6 zB=7
+    const int sel = (int)((0x776653524140ull >> (4 * e)) & 7u);
+    const int off = (0xA22 >> e) & 1;
+    const uint32_t mk = sel == 0 ? m.xA : sel == 1 ? m.xB : sel == 2 ? m.xC : sel == 3 ? m.xD
+                      : sel == 4 ? m.yA : sel == 5 ? m.yC : sel == 6 ? m.zA : m.zB;
+    const unsigned long long bs = sel == 0 ? b.xA : sel == 1 ? b.xB : sel == 2 ? b.xC : sel == 3 ? b.xD
+                                : sel == 4 ? b.yA : sel == 5 ? b.yC : sel == 6 ? b.zA : b.zB;
+    return bs + __popc(mk & lowmask(bit + off));
+}
+
+// Walks the flattened index f = tid, tid + step, tid + 2*step, ... of a
+// (row, column) grid with `ncol` columns without dividing in the loop.
+struct RowColWalk {
+    int row, col, drow, dcol, ncol;
+    __device__ __forceinline__ RowColWalk(int start, int step, int ncol_)
+        : row(start / ncol_), col(start % ncol_), drow(step / ncol_), dcol(step % ncol_), ncol(ncol_) {}
+    __device__ __forceinline__ void advance()
+    {
+        row += drow;
+        col += dcol;
+        if (col >= ncol) {
+            col -= ncol;
+            ++row;
+        }
     }
+};
+
+// Bit mask "value >= iso" of rows [0, nrows) of nx values each (row stride
+// nx) into dst[row * W + w].  All threads of the CTA take part; SHARED
+// selects a shared-memory source (plain loads) or a global one (__ldg).
+template <bool VEC4, bool SHARED>
+__device__ __forceinline__ void classify_block(const float* __restrict__ src, int nx, int W, int nrows, float iso,
+                                               uint32_t* __restrict__ dst)
+{
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (VEC4) {
+        const int nq = nx >> 2, nq8 = (nq + 7) & ~7;
+        constexpr int U = 4;
+        RowColWalk it(tid, kThreads, nq8);
+        const int total = nrows * nq8;
+        for (int f0 = 0; f0 < total; f0 += U * kThreads) {
+            float4 v[U];
+            RowColWalk at = it;
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const bool ok = at.row < nrows && at.col < nq;
+                const float4* p = reinterpret_cast<const float4*>(src + (size_t)at.row * nx) + at.col;
+                v[u] = ok ? (SHARED ? *p : __ldg(p)) : make_float4(0.f, 0.f, 0.f, 0.f);
+                at.advance();
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const bool ok = it.row < nrows && it.col < nq;
+                const uint32_t nib = ok ? ((uint32_t)(v[u].x >= iso) | ((uint32_t)(v[u].y >= iso) << 1) |
+                                           ((uint32_t)(v[u].z >= iso) << 2) | ((uint32_t)(v[u].w >= iso) << 3))
+                                        : 0u;
+                uint32_t word = nib << (4 * (lane & 7));
+                word |= __shfl_xor_sync(0xffffffffu, word, 1);
+                word |= __shfl_xor_sync(0xffffffffu, word, 2);
+                word |= __shfl_xor_sync(0xffffffffu, word, 4);
+                if ((lane & 7) == 0 && ok) dst[it.row * W + (it.col >> 3)] = word;
+                it.advance();
+            }
+        }
+    } else {
+        constexpr int U = 4, NW = kThreads / 32;
+        RowColWalk it(warp, NW, W);
+        const int total = nrows * W;
+        for (int f0 = 0; f0 < total; f0 += U * NW) {
+            float v[U];
+            RowColWalk at = it;
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int i = 32 * at.col + lane;
+                const bool ok = at.row < nrows && i < nx;
+                const float* p = src + (size_t)at.row * nx + i;
+                v[u] = ok ? (SHARED ? *p : __ldg(p)) : 0.f;
+                at.advance();
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int i = 32 * it.col + lane;
+                const bool ok = it.row < nrows && i < nx;
+                const uint32_t word = __ballot_sync(0xffffffffu, ok && v[u] >= iso);
+                if (lane == 0 && it.row < nrows) dst[it.row * W + it.col] = word;
+                it.advance();
+            }
+        }
+    }
+}
+
+// q = x / d for 0 <= x < 2^22 using a float reciprocal inv = 1/d and one
+// correction step (no integer division in hot loops).
+__device__ __forceinline__ int fastdiv(int x, int d, float inv)
+{
+    int q = __float2int_rz((float)x * inv);
+    if (q * d > x) --q;
+    else if ((q + 1) * d <= x) ++q;
+    return q;
 }
 
 // Low grid point and axis of cube edge e of cell (0,0,0).
@@ -386,6 +476,28 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity)
     }
     return false;
 }
+
+// First vertex (comp 0), triangle (1) or MC vertex (2) of grid row r =
+// k*ny + j: offset of its counting group (plane k, block j >> jshift) plus
+// the row's exclusive prefix inside the group.
+struct RowStarts {
+    const unsigned long long* goff;  // 3 x ngroups
+    const uint4* rowpre;             // R
+    long long ngroups;
+    int ny, nyb, jshift;
+    __device__ __forceinline__ unsigned long long get(int k, int j, int comp) const
+    {
+        const long long r = (long long)k * ny + j;
+        const uint4 p = __ldg(&rowpre[r]);
+        return __ldg(&goff[comp * ngroups + (long long)k * nyb + (j >> jshift)]) +
+               (comp == 0 ? p.x : (comp == 1 ? p.y : p.z));
+    }
+    __device__ __forceinline__ unsigned long long get(long long r, int comp) const
+    {
+        const int k = (int)(r / ny);
+        return get(k, (int)(r - (long long)k * ny), comp);
+    }
+};
 
 // Marching-cubes owned-edge mask of a cell (first-reference rule of
 // marchingCubes/serial/main.cpp:139-177): an edge belongs to the adjacent

@@ -8,6 +8,7 @@ namespace iso {
 
 struct Grid;
 struct CaseTables;
+struct RowStarts;
 
 // Scratch of one extraction (device memory, owned by the caller of the
 // launchers).  R = ny*nz grid rows, W = ceil(nx/32) words per row.
@@ -15,10 +16,9 @@ struct FeBuffers {
     uint4* rowcnt = nullptr;               // R      x/y/z cuts, triangles
     uint2* trims = nullptr;                // R      xl, xr (pass 1 trims)
     uint32_t* mccnt = nullptr;             // R      MC vertices per cell row
-    unsigned long long* groups = nullptr;  // 3*ngroups  group totals -> offsets
-    unsigned long long* vstart = nullptr;  // R      first vertex of the row
-    unsigned long long* tstart = nullptr;  // R      first triangle of cell row
-    unsigned long long* mstart = nullptr;  // R      first MC vertex of cell row
+    uint4* rowpre = nullptr;               // R      row prefix inside its group (v, t, m)
+    uint32_t* gsum = nullptr;              // 3*ngroups  group totals
+    unsigned long long* goff = nullptr;    // 3*ngroups  group offsets
     unsigned long long* totals = nullptr;  // 4      vertices, triangles, mc vertices, status
     uint32_t* bits = nullptr;              // R*W    bit rows (row-wise kernels only)
     uint32_t* fe2mc = nullptr;             // >= V   FE vertex index -> MC index
@@ -47,29 +47,30 @@ GenPlan gen_plan(const Grid& g, int nsm);
 void launch_count(const float* vol, const Grid& g, float iso, const CaseTables* cases, bool mc, bool write_bits,
                   const CountPlan& p, FeBuffers& b, cudaStream_t s);
 void launch_scan(const CountPlan& p, FeBuffers& b, cudaStream_t s);
-void launch_row_starts(const Grid& g, const CountPlan& p, bool mc, FeBuffers& b, cudaStream_t s);
-void launch_grid_edges(const Grid& g, const FeBuffers& b, int scanned, unsigned long long* ge,
+void launch_grid_edges(const Grid& g, const CountPlan& p, const FeBuffers& b, int scanned, unsigned long long* ge,
                        unsigned long long* tri_counter, cudaStream_t s);
+// Row-start accessor of a counted extraction.
+RowStarts row_starts(const Grid& g, const CountPlan& p, const FeBuffers& b);
 
 // pass 4, column-marching (volume slabs staged in shared memory)
 template <typename IndexT>
 void launch_fe_gen_cols(const float* vol, const Grid& g, float iso, const CaseTables* cases, const FeBuffers& b,
-                        const GenPlan& p, long long capV, long long capT, float* points, float* normals,
-                        IndexT* tris, int reverse, cudaStream_t s);
+                        const CountPlan& cp, const GenPlan& p, long long capV, long long capT, float* points,
+                        float* normals, IndexT* tris, int reverse, cudaStream_t s);
 void launch_mc_gen_cols(const float* vol, const Grid& g, float iso, const CaseTables* cases, const FeBuffers& b,
-                        const GenPlan& p, long long capV, long long capT, float* points, float* normals, int reverse,
-                        cudaStream_t s);
+                        const CountPlan& cp, const GenPlan& p, long long capV, long long capT, float* points,
+                        float* normals, int reverse, cudaStream_t s);
 
 // pass 4, row-wise (bit rows from the count pass)
 template <typename IndexT>
 void launch_fe_gen_rows(const float* vol, const Grid& g, float iso, const CaseTables* cases, const FeBuffers& b,
-                        long long capV, long long capT, float* points, float* normals, IndexT* tris, int nsm,
-                        cudaStream_t s);
+                        const CountPlan& cp, long long capV, long long capT, float* points, float* normals,
+                        IndexT* tris, int nsm, cudaStream_t s);
 void launch_mc_vertices_rows(const float* vol, const Grid& g, float iso, const CaseTables* cases,
-                             const FeBuffers& b, long long capV, long long capT, float* points, float* normals,
-                             int nsm, cudaStream_t s);
+                             const FeBuffers& b, const CountPlan& cp, long long capV, long long capT, float* points,
+                             float* normals, int nsm, cudaStream_t s);
 template <typename IndexT>
-void launch_mc_triangles(const Grid& g, const CaseTables* cases, const FeBuffers& b, long long capV, long long capT,
-                         IndexT* tris, int nsm, cudaStream_t s);
+void launch_mc_triangles(const Grid& g, const CaseTables* cases, const FeBuffers& b, const CountPlan& cp,
+                         long long capV, long long capT, IndexT* tris, int nsm, cudaStream_t s);
 
 }  // namespace iso
