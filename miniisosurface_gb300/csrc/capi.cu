@@ -250,7 +250,7 @@ void enqueue_count(iso_ctx* ctx, iso_algorithm algo, const float* vol, const Gri
                    FeBuffers& b, cudaStream_t s, PassMarks& pm)
 {
     const bool mc = algo == ISO_MARCHING_CUBES;
-    iso::launch_count(vol, g, iso, ctx->d_cases, mc, mc || !pl.gp.fits, pl.cp, b, s);
+    iso::launch_count(vol, g, iso, ctx->d_cases, mc, pl.cp, b, s);
     pm.mark(ISO_PASS_COUNT);
     iso::launch_scan(pl.cp, b, s);
     pm.mark(ISO_PASS_SCAN);
@@ -266,11 +266,11 @@ void enqueue_generate(iso_ctx* ctx, iso_algorithm algo, const float* vol, const 
     if (algo == ISO_FLYING_EDGES) {
         if (pl.gp.fits) {
             if (i4)
-                iso::launch_fe_gen_cols<uint32_t>(vol, g, iso, ctx->d_cases, b, pl.cp, pl.gp, capV, capT, out->points,
-                                                  out->normals, static_cast<uint32_t*>(out->tris), ctx->reverse, s);
+                iso::launch_fe_gen_warps<uint32_t>(vol, g, iso, ctx->d_cases, b, pl.cp, pl.gp, capV, capT, out->points,
+                                                   out->normals, static_cast<uint32_t*>(out->tris), ctx->reverse, s);
             else
-                iso::launch_fe_gen_cols<uint64_t>(vol, g, iso, ctx->d_cases, b, pl.cp, pl.gp, capV, capT, out->points,
-                                                  out->normals, static_cast<uint64_t*>(out->tris), ctx->reverse, s);
+                iso::launch_fe_gen_warps<uint64_t>(vol, g, iso, ctx->d_cases, b, pl.cp, pl.gp, capV, capT, out->points,
+                                                   out->normals, static_cast<uint64_t*>(out->tris), ctx->reverse, s);
         } else {
             if (i4)
                 iso::launch_fe_gen_rows<uint32_t>(vol, g, iso, ctx->d_cases, b, pl.cp, capV, capT, out->points, out->normals,
@@ -283,18 +283,27 @@ void enqueue_generate(iso_ctx* ctx, iso_algorithm algo, const float* vol, const 
     } else {
         const long long capM = capV < 0xffffffffll ? capV : 0xffffffffll;  // fe2mc holds 32-bit ids
         if (pl.gp.fits)
-            iso::launch_mc_gen_cols(vol, g, iso, ctx->d_cases, b, pl.cp, pl.gp, capM, capT, out->points, out->normals,
-                                    ctx->reverse, s);
+            iso::launch_mc_gen_warps(vol, g, iso, ctx->d_cases, b, pl.cp, pl.gp, capM, capT, out->points, out->normals,
+                                     ctx->reverse, s);
         else
             iso::launch_mc_vertices_rows(vol, g, iso, ctx->d_cases, b, pl.cp, capM, capT, out->points, out->normals,
                                          ctx->nsm, s);
         pm.mark(ISO_PASS_MC_VERTICES);
-        if (i4)
-            iso::launch_mc_triangles<uint32_t>(g, ctx->d_cases, b, pl.cp, capM, capT, static_cast<uint32_t*>(out->tris),
-                                               ctx->nsm, s);
-        else
-            iso::launch_mc_triangles<uint64_t>(g, ctx->d_cases, b, pl.cp, capM, capT, static_cast<uint64_t*>(out->tris),
-                                               ctx->nsm, s);
+        if (pl.gp.fits) {
+            if (i4)
+                iso::launch_mc_tri_warps<uint32_t>(g, ctx->d_cases, b, pl.cp, pl.gp, capM, capT,
+                                                   static_cast<uint32_t*>(out->tris), s);
+            else
+                iso::launch_mc_tri_warps<uint64_t>(g, ctx->d_cases, b, pl.cp, pl.gp, capM, capT,
+                                                   static_cast<uint64_t*>(out->tris), s);
+        } else {
+            if (i4)
+                iso::launch_mc_triangles<uint32_t>(g, ctx->d_cases, b, pl.cp, capM, capT,
+                                                   static_cast<uint32_t*>(out->tris), ctx->nsm, s);
+            else
+                iso::launch_mc_triangles<uint64_t>(g, ctx->d_cases, b, pl.cp, capM, capT,
+                                                   static_cast<uint64_t*>(out->tris), ctx->nsm, s);
+        }
         pm.mark(ISO_PASS_MC_TRIANGLES);
     }
 }
@@ -623,7 +632,7 @@ iso_status iso_fe_pass1(iso_fe* fe)
     ISO_CUDA(ctx, cudaMalloc(&fe->scratch, scratch_size(g, pl.cp)));
     carve(fe->scratch, g, pl.cp, fe->buf);
     ISO_CUDA(ctx, cudaMemcpy(fe->d_volume, fe->host_volume, vbytes, cudaMemcpyHostToDevice));
-    iso::launch_count(fe->d_volume, g, fe->isoval, ctx->d_cases, false, !pl.gp.fits, pl.cp, fe->buf, 0);
+    iso::launch_count(fe->d_volume, g, fe->isoval, ctx->d_cases, false, pl.cp, fe->buf, 0);
     ISO_CUDA(ctx, cudaGetLastError());
     ISO_CUDA(ctx, cudaDeviceSynchronize());
     return ISO_OK;

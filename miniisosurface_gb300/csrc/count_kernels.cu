@@ -22,29 +22,31 @@
 
 namespace iso {
 
-// Bits of the rows j0 .. j0+nbr-1 of plane p into dst[jj*W + w].
-template <bool VEC4>
-__device__ __forceinline__ void classify_rows(const float* __restrict__ vol, const Grid& g, float iso, int p, int j0,
-                                              int nbr, uint32_t* __restrict__ dst)
-{
-    classify_block<VEC4, false>(vol + ((long long)p * g.ny + j0) * g.nx, g.nx, g.W, nbr, iso, dst);
-}
+// How the count pass reads a plane of its block: staged through a shared-
+// memory slab ring by the TMA bulk engine (rows 16-byte aligned) or by
+// cp.async, or read directly (rows too wide to stage).
+enum SlabMode { kSlabBulk = 0, kSlabCpAsync = 1, kSlabDirect = 2 };
 
-template <int G, bool MC, bool VEC4>
+template <int G, bool MC, int MODE>
 __global__ void __launch_bounds__(kThreads) k_count_cols(const float* __restrict__ vol, Grid g, float iso, int KC,
-                                                         int nyb, const CaseTables* __restrict__ cases,
+                                                         int nyb, int NS, int slab_floats,
+                                                         const CaseTables* __restrict__ cases,
                                                          uint4* __restrict__ rowcnt, uint2* __restrict__ trims,
                                                          uint32_t* __restrict__ mccnt, uint4* __restrict__ rowpre,
                                                          uint32_t* __restrict__ gsum, long long ngroups,
-                                                         uint32_t* __restrict__ bits_out)
+                                                         uint32_t* __restrict__ bits_out,
+                                                         unsigned long long* __restrict__ totals)
 {
     constexpr int J = kThreads / G;  // grid rows per block
-    extern __shared__ uint32_t s_dyn[];
+    constexpr bool STAGED = MODE != kSlabDirect;
+    extern __shared__ __align__(128) unsigned char s_raw[];
     __shared__ uint8_t s_ntris[256];
     __shared__ uint16_t s_cut[256];
     __shared__ uint32_t s_rc[3][J];
-    uint32_t* s_bits0 = s_dyn;
-    uint32_t* s_bits1 = s_dyn + (J + 1) * g.W;
+    float* slots = reinterpret_cast<float*>(s_raw);
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(s_raw + (size_t)NS * slab_floats * 4);
+    uint32_t* s_bits0 = reinterpret_cast<uint32_t*>(mbar + (STAGED ? NS : 0));
+    uint32_t* s_bits1 = s_bits0 + (J + 1) * g.W;
     for (int c = threadIdx.x; c < 256; c += blockDim.x) {
         s_ntris[c] = (uint8_t)iso_case_ntris(cases->tris[c]);
         s_cut[c] = cases->cut[c];
@@ -55,14 +57,69 @@ __global__ void __launch_bounds__(kThreads) k_count_cols(const float* __restrict
     const int tid = threadIdx.x, lane = tid & 31, lig = lane & (G - 1);
     const int jj = tid / G;  // the row this group counts
     const int nchunks = (g.W + G - 1) / G;
+    const int nfl = nbr * g.nx;
+    const bool vec4 = (g.nx & 3) == 0 && (STAGED || (reinterpret_cast<uintptr_t>(vol) & 15) == 0);
 
-    classify_rows<VEC4>(vol, g, iso, kb, j0, nbr, (kb & 1) ? s_bits1 : s_bits0);
+    if (STAGED && tid == 0) {
+        for (int s = 0; s < NS; ++s) mbar_init(&mbar[s], MODE == kSlabBulk ? 1u : (unsigned)kThreads);
+        fence_mbar_init();
+    }
     __syncthreads();
-    for (int k = kb; k < ke; ++k) {
-        uint32_t* P0 = (k & 1) ? s_bits1 : s_bits0;        // plane k
-        uint32_t* P1 = (k & 1) ? s_bits0 : s_bits1;        // plane k+1
-        if (k + 1 < g.nz) classify_rows<VEC4>(vol, g, iso, k + 1, j0, nbr, P1);
+    uint32_t pending = 0, parity = 0;  // per slot: copy in flight / next wait parity
+    auto issue = [&](int p) {
+        if (!STAGED || p > ke || p >= g.nz) return;
+        const int s = p % NS;
+        slab_copy<MODE == kSlabBulk>(slots + (size_t)s * slab_floats, vol + ((long long)p * g.ny + j0) * g.nx, nfl,
+                                     &mbar[s], tid, kThreads);
+        pending |= 1u << s;
+    };
+    auto wait = [&](int p) -> bool {
+        if (!STAGED) return true;
+        const int s = p % NS;
+        const bool ok = mbar_wait(&mbar[s], (parity >> s) & 1u);
+        parity ^= 1u << s;
+        pending &= ~(1u << s);
+        return ok;
+    };
+    auto drain = [&]() {
+        for (int s = 0; s < NS; ++s) {
+            if ((pending >> s) & 1u) {
+                mbar_wait(&mbar[s], (parity >> s) & 1u);
+                parity ^= 1u << s;
+                pending &= ~(1u << s);
+            }
+        }
+    };
+    // bit rows of plane p (slab or volume) into dst
+    auto classify = [&](int p, uint32_t* dst) {
+        if (STAGED) {
+            const float* src = slots + (size_t)(p % NS) * slab_floats;
+            if (vec4) classify_block<true, true>(src, g.nx, g.W, nbr, iso, dst);
+            else classify_block<false, true>(src, g.nx, g.W, nbr, iso, dst);
+        } else {
+            const float* src = vol + ((long long)p * g.ny + j0) * g.nx;
+            if (vec4) classify_block<true, false>(src, g.nx, g.W, nbr, iso, dst);
+            else classify_block<false, false>(src, g.nx, g.W, nbr, iso, dst);
+        }
+    };
+
+    for (int q = 0; q < NS; ++q) issue(kb + q);
+    bool alive = __syncthreads_and(wait(kb));
+    if (alive) {
+        classify(kb, (kb & 1) ? s_bits1 : s_bits0);
         __syncthreads();
+        issue(kb + NS);
+    }
+    for (int k = kb; k < ke && alive; ++k) {
+        uint32_t* P0 = (k & 1) ? s_bits1 : s_bits0;  // plane k
+        uint32_t* P1 = (k & 1) ? s_bits0 : s_bits1;  // plane k+1
+        if (k + 1 < g.nz) {
+            alive = __syncthreads_and(wait(k + 1));
+            if (!alive) break;
+            classify(k + 1, P1);
+        }
+        __syncthreads();
+        issue(k + 1 + NS);  // the slot of plane k+1 is free again
 
         const bool valid = jj < JB;
         const int j = j0 + jj;
@@ -109,7 +166,7 @@ __global__ void __launch_bounds__(kThreads) k_count_cols(const float* __restrict
                     if (MC) mc += __popc(mc_owned_edges(32 * w + bit == 0, j == 0, k == 0) & s_cut[c]);
                 }
             }
-            if (bits_out && in) bits_out[((long long)k * g.ny + j) * g.W + w] = rw.a;
+            if (in) bits_out[((long long)k * g.ny + j) * g.W + w] = rw.a;
         }
 #pragma unroll
         for (int d = G / 2; d > 0; d >>= 1) {
@@ -161,15 +218,16 @@ __global__ void __launch_bounds__(kThreads) k_count_cols(const float* __restrict
             }
             if (tid < 3) gsum[tid * ngroups + (long long)k * nyb + jb] = run[tid];
         }
-        __syncthreads();
     }
+    if (!alive && tid == 0) atomicOr(&totals[3], kStatusTimeout);
+    drain();
 }
 
 // Exclusive scan of the group totals (three arrays of n u32) into 64-bit
 // offsets, plus the grand totals; one CTA.  Each thread owns kScanPer
 // consecutive groups of a segment of 1024*kScanPer; segments are walked with
 // a running carry.
-constexpr int kScanPer = 16;
+constexpr int kScanPer = 8;
 
 __global__ void __launch_bounds__(1024) k_scan_groups(const uint32_t* __restrict__ gsum, long long n,
                                                       unsigned long long* __restrict__ goff,
@@ -228,7 +286,6 @@ __global__ void __launch_bounds__(1024) k_scan_groups(const uint32_t* __restrict
         totals[0] = carry[0];
         totals[1] = carry[1];
         totals[2] = carry[2];
-        totals[3] = 0;  // device status, set by the generate kernels
     }
 }
 
@@ -265,14 +322,34 @@ int lanes_per_row(int W)
     return G;
 }
 
+// Blocks of J = 256/G rows with G >= lanes per row, G doubled until the
+// slab ring (3 slabs of J+1 rows) fits kCountSmem so that several CTAs share
+// an SM; columns of KC planes, ~8 CTAs per SM in total.
+constexpr size_t kCountSmem = 64 * 1024;
+constexpr int kCountSlots = 3;
+
 CountPlan count_plan(const Grid& g, int nsm)
 {
     CountPlan p;
-    p.G = lanes_per_row(g.W);
-    p.J = kThreads / p.G;
+    int G = lanes_per_row(g.W);
+    for (;;) {
+        const int J = kThreads / G;
+        const size_t slab = ((size_t)(J + 1) * g.nx + 31) & ~(size_t)31;
+        const size_t smem = kCountSlots * slab * 4 + kCountSlots * 8 + 2 * (size_t)(J + 1) * g.W * 4;
+        if (smem <= kCountSmem || G == 32) {
+            p.G = G;
+            p.J = J;
+            p.slab_floats = (int)slab;
+            p.staged = smem <= 2 * kCountSmem;
+            p.NS = p.staged ? kCountSlots : 0;
+            p.smem = p.staged ? smem : 2 * (size_t)(J + 1) * g.W * 4;
+            if (!p.staged) p.slab_floats = 0;
+            break;
+        }
+        G *= 2;
+    }
     p.nyb = (g.ny + p.J - 1) / p.J;
-    // columns of KC planes: enough CTAs for ~8 per SM, at least 8 planes deep
-    long long target = (long long)nsm * 8;
+    const long long target = (long long)nsm * 8;
     int nkc = (int)((target + p.nyb - 1) / p.nyb);
     if (nkc < 1) nkc = 1;
     p.KC = (g.nz + nkc - 1) / nkc;
@@ -280,7 +357,6 @@ CountPlan count_plan(const Grid& g, int nsm)
     if (p.KC > g.nz) p.KC = g.nz;
     p.nkc = (g.nz + p.KC - 1) / p.KC;
     p.ngroups = (long long)g.nz * p.nyb;
-    p.smem = (size_t)2 * (p.J + 1) * g.W * sizeof(uint32_t);
     return p;
 }
 
@@ -294,33 +370,35 @@ CountPlan count_plan(const Grid& g, int nsm)
         default: { constexpr int kG = 32; __VA_ARGS__; } break; \
     }
 
-template <int G, bool MC>
-static void count_cols_vec(bool vec4, const CountPlan& p, const float* vol, const Grid& g, float iso,
-                           const CaseTables* cases, FeBuffers& b, bool write_bits, cudaStream_t s)
+template <int G, bool MC, int MODE>
+static void count_launch(const CountPlan& p, const float* vol, const Grid& g, float iso, const CaseTables* cases,
+                         FeBuffers& b, cudaStream_t s)
 {
-    const unsigned blocks = (unsigned)(p.nyb * p.nkc);
-    uint32_t* bo = write_bits ? b.bits : nullptr;
-    if (vec4) {
-        auto kern = k_count_cols<G, MC, true>;
-        if (p.smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.smem);
-        kern<<<blocks, kThreads, p.smem, s>>>(vol, g, iso, p.KC, p.nyb, cases, b.rowcnt, b.trims, b.mccnt, b.rowpre,
-                                              b.gsum, p.ngroups, bo);
-    } else {
-        auto kern = k_count_cols<G, MC, false>;
-        if (p.smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.smem);
-        kern<<<blocks, kThreads, p.smem, s>>>(vol, g, iso, p.KC, p.nyb, cases, b.rowcnt, b.trims, b.mccnt, b.rowpre,
-                                              b.gsum, p.ngroups, bo);
-    }
+    auto kern = k_count_cols<G, MC, MODE>;
+    if (p.smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.smem);
+    kern<<<(unsigned)(p.nyb * p.nkc), kThreads, p.smem, s>>>(vol, g, iso, p.KC, p.nyb, p.NS, p.slab_floats, cases,
+                                                              b.rowcnt, b.trims, b.mccnt, b.rowpre, b.gsum,
+                                                              p.ngroups, b.bits, b.totals);
 }
 
-void launch_count(const float* vol, const Grid& g, float iso, const CaseTables* cases, bool mc, bool write_bits,
+template <int G, bool MC>
+static void count_mode(const CountPlan& p, const float* vol, const Grid& g, float iso, const CaseTables* cases,
+                       FeBuffers& b, cudaStream_t s)
+{
+    const bool bulk = (g.nx % 4 == 0) && ((reinterpret_cast<uintptr_t>(vol) & 15) == 0);
+    if (!p.staged) count_launch<G, MC, kSlabDirect>(p, vol, g, iso, cases, b, s);
+    else if (bulk) count_launch<G, MC, kSlabBulk>(p, vol, g, iso, cases, b, s);
+    else count_launch<G, MC, kSlabCpAsync>(p, vol, g, iso, cases, b, s);
+}
+
+void launch_count(const float* vol, const Grid& g, float iso, const CaseTables* cases, bool mc,
                   const CountPlan& p, FeBuffers& b, cudaStream_t s)
 {
-    const bool vec4 = (g.nx % 4 == 0) && ((reinterpret_cast<uintptr_t>(vol) & 15) == 0);
+    cudaMemsetAsync(b.totals + 3, 0, sizeof(unsigned long long), s);  // device status
     if (mc) {
-        ISO_DISPATCH_G(p.G, (count_cols_vec<kG, true>(vec4, p, vol, g, iso, cases, b, write_bits, s)));
+        ISO_DISPATCH_G(p.G, (count_mode<kG, true>(p, vol, g, iso, cases, b, s)));
     } else {
-        ISO_DISPATCH_G(p.G, (count_cols_vec<kG, false>(vec4, p, vol, g, iso, cases, b, write_bits, s)));
+        ISO_DISPATCH_G(p.G, (count_mode<kG, false>(p, vol, g, iso, cases, b, s)));
     }
 }
 

@@ -1,0 +1,46 @@
+// Flying Edges pass 4 (warp-per-row kernel of gen_warps.cuh) and the plan of
+// the warp-per-row kernels.
+#include "gen_warps.cuh"
+
+namespace iso {
+
+// Shared memory of the slab ring; above kGenTwoPerSm only one CTA fits per SM,
+// above kGenMaxSmem (or rows wider than 32 words) the row-wise kernels are used.
+constexpr size_t kGenTwoPerSm = 104 * 1024;
+constexpr size_t kGenMaxSmem = 200 * 1024;
+
+GenPlan gen_plan(const Grid& g, int nsm)
+{
+    GenPlan p;
+    p.J = kGenRows;
+    p.nyb = (g.ny + p.J - 1) / p.J;
+    p.slab_floats = (int)((((size_t)(p.J + 3) * g.nx) + 31) & ~(size_t)31);
+    p.smem = (size_t)kGenSlots * p.slab_floats * 4 + 2 * kGenSlots * 8;
+    p.fits = g.W <= 32 && p.smem <= kGenMaxSmem;
+    const long long resident = (long long)nsm * (p.smem <= kGenTwoPerSm ? 2 : 1);
+    int nkc = (int)((4 * resident + p.nyb - 1) / p.nyb);
+    if (nkc < 1) nkc = 1;
+    p.KC = (g.nz + nkc - 1) / nkc;
+    if (p.KC < 4) p.KC = 4;
+    if (p.KC > g.nz) p.KC = g.nz;
+    p.nkc = (g.nz + p.KC - 1) / p.KC;
+    return p;
+}
+
+template <typename IndexT>
+void launch_fe_gen_warps(const float* vol, const Grid& g, float iso, const CaseTables* cases, const FeBuffers& b,
+                         const CountPlan& cp, const GenPlan& p, long long capV, long long capT, float* points,
+                         float* normals, IndexT* tris, int reverse, cudaStream_t s)
+{
+    launch_gen_warps_impl<kGenFE, IndexT>(vol, g, iso, cases, b, cp, p, capV, capT, points, normals, tris, reverse,
+                                          s);
+}
+
+template void launch_fe_gen_warps<uint32_t>(const float*, const Grid&, float, const CaseTables*, const FeBuffers&,
+                                            const CountPlan&, const GenPlan&, long long, long long, float*, float*,
+                                            uint32_t*, int, cudaStream_t);
+template void launch_fe_gen_warps<uint64_t>(const float*, const Grid&, float, const CaseTables*, const FeBuffers&,
+                                            const CountPlan&, const GenPlan&, long long, long long, float*, float*,
+                                            uint64_t*, int, cudaStream_t);
+
+}  // namespace iso

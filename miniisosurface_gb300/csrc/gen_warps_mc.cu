@@ -1,0 +1,32 @@
+// Marching Cubes pass 4 (warp-per-row kernels of gen_warps.cuh): vertices in
+// owner order with the Flying Edges -> MC index map, then the triangles with
+// their corners mapped.
+#include "gen_warps.cuh"
+
+namespace iso {
+
+void launch_mc_gen_warps(const float* vol, const Grid& g, float iso, const CaseTables* cases, const FeBuffers& b,
+                         const CountPlan& cp, const GenPlan& p, long long capV, long long capT, float* points,
+                         float* normals, int reverse, cudaStream_t s)
+{
+    launch_gen_warps_impl<kGenMC, uint32_t>(vol, g, iso, cases, b, cp, p, capV, capT, points, normals, nullptr,
+                                            reverse, s);
+}
+
+template <typename IndexT>
+void launch_mc_tri_warps(const Grid& g, const CaseTables* cases, const FeBuffers& b, const CountPlan& cp,
+                         const GenPlan& p, long long capV, long long capT, IndexT* tris, cudaStream_t s)
+{
+    GenPlan q = p;
+    q.slab_floats = 0;
+    q.smem = 0;
+    launch_gen_warps_impl<kGenTri, IndexT>(nullptr, g, 0.f, cases, b, cp, q, capV, capT, nullptr, nullptr, tris, 0,
+                                           s);
+}
+
+template void launch_mc_tri_warps<uint32_t>(const Grid&, const CaseTables*, const FeBuffers&, const CountPlan&,
+                                            const GenPlan&, long long, long long, uint32_t*, cudaStream_t);
+template void launch_mc_tri_warps<uint64_t>(const Grid&, const CaseTables*, const FeBuffers&, const CountPlan&,
+                                            const GenPlan&, long long, long long, uint64_t*, cudaStream_t);
+
+}  // namespace iso

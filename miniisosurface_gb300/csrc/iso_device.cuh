@@ -467,6 +467,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity)
     return ok != 0;
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 // Bounded wait for phase `parity` of `bar`.  Returns false after kWaitLimit
 // rounds (the caller records a timeout status and stops issuing work).
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity)
@@ -476,6 +481,26 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity)
     }
     return false;
 }
+
+// Copy of rows of a plane slab into shared memory: one bulk copy (TMA engine)
+// when 16-byte aligned, else cp.async by all `nthreads` threads of `tid`.
+// Completion is signalled on `bar`, which must expect 1 arrival (BULK) or
+// nthreads arrivals (cp.async).
+template <bool BULK>
+__device__ __forceinline__ void slab_copy(float* dst, const float* src, int nfl, uint64_t* bar, int tid, int nthreads)
+{
+    if (BULK) {
+        if (tid == 0) {
+            fence_proxy_async();
+            mbar_arrive_expect_tx(bar, (unsigned)nfl * 4u);
+            bulk_copy_g2s(dst, src, (unsigned)nfl * 4u, bar);
+        }
+    } else {
+        for (int q = tid; q < nfl; q += nthreads) cp_async4(dst + q, src + q);
+        cp_async_arrive(bar);
+    }
+}
+
 
 // First vertex (comp 0), triangle (1) or MC vertex (2) of grid row r =
 // k*ny + j: offset of its counting group (plane k, block j >> jshift) plus

@@ -28,13 +28,17 @@ struct FeBuffers {
 // KC planes, one CTA per (block, column).
 struct CountPlan {
     int G = 1, J = 1, nyb = 1, KC = 1, nkc = 1;
+    int NS = 0, slab_floats = 0;  // slab ring (NS slots), 0 when planes are read directly
+    bool staged = false;
     long long ngroups = 0;
     size_t smem = 0;
 };
 
-// Work split of the column-marching generate kernels.
+// Work split of the warp-per-row generate kernels: blocks of J = 8 rows,
+// columns of KC planes, a ring of slabs of J+3 rows.
 struct GenPlan {
-    int G = 32, J = 8, nyb = 1, KC = 1, nkc = 1;
+    int J = 8, nyb = 1, KC = 1, nkc = 1;
+    int slab_floats = 0;
     size_t smem = 0;
     bool fits = false;  // false: use the row-wise kernels
 };
@@ -44,7 +48,7 @@ CountPlan count_plan(const Grid& g, int nsm);
 GenPlan gen_plan(const Grid& g, int nsm);
 
 // passes 1-3
-void launch_count(const float* vol, const Grid& g, float iso, const CaseTables* cases, bool mc, bool write_bits,
+void launch_count(const float* vol, const Grid& g, float iso, const CaseTables* cases, bool mc,
                   const CountPlan& p, FeBuffers& b, cudaStream_t s);
 void launch_scan(const CountPlan& p, FeBuffers& b, cudaStream_t s);
 void launch_grid_edges(const Grid& g, const CountPlan& p, const FeBuffers& b, int scanned, unsigned long long* ge,
@@ -52,14 +56,17 @@ void launch_grid_edges(const Grid& g, const CountPlan& p, const FeBuffers& b, in
 // Row-start accessor of a counted extraction.
 RowStarts row_starts(const Grid& g, const CountPlan& p, const FeBuffers& b);
 
-// pass 4, column-marching (volume slabs staged in shared memory)
+// pass 4, warp per row (volume slabs staged in shared memory)
 template <typename IndexT>
-void launch_fe_gen_cols(const float* vol, const Grid& g, float iso, const CaseTables* cases, const FeBuffers& b,
-                        const CountPlan& cp, const GenPlan& p, long long capV, long long capT, float* points,
-                        float* normals, IndexT* tris, int reverse, cudaStream_t s);
-void launch_mc_gen_cols(const float* vol, const Grid& g, float iso, const CaseTables* cases, const FeBuffers& b,
-                        const CountPlan& cp, const GenPlan& p, long long capV, long long capT, float* points,
-                        float* normals, int reverse, cudaStream_t s);
+void launch_fe_gen_warps(const float* vol, const Grid& g, float iso, const CaseTables* cases, const FeBuffers& b,
+                         const CountPlan& cp, const GenPlan& p, long long capV, long long capT, float* points,
+                         float* normals, IndexT* tris, int reverse, cudaStream_t s);
+void launch_mc_gen_warps(const float* vol, const Grid& g, float iso, const CaseTables* cases, const FeBuffers& b,
+                         const CountPlan& cp, const GenPlan& p, long long capV, long long capT, float* points,
+                         float* normals, int reverse, cudaStream_t s);
+template <typename IndexT>
+void launch_mc_tri_warps(const Grid& g, const CaseTables* cases, const FeBuffers& b, const CountPlan& cp,
+                         const GenPlan& p, long long capV, long long capT, IndexT* tris, cudaStream_t s);
 
 // pass 4, row-wise (bit rows from the count pass)
 template <typename IndexT>
