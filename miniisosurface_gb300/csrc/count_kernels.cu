@@ -375,7 +375,7 @@ static void count_launch(const CountPlan& p, const float* vol, const Grid& g, fl
                          FeBuffers& b, cudaStream_t s)
 {
     auto kern = k_count_cols<G, MC, MODE>;
-    if (p.smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.smem);
+    allow_smem(kern, p.smem);
     kern<<<(unsigned)(p.nyb * p.nkc), kThreads, p.smem, s>>>(vol, g, iso, p.KC, p.nyb, p.NS, p.slab_floats, cases,
                                                               b.rowcnt, b.trims, b.mccnt, b.rowpre, b.gsum,
                                                               p.ngroups, b.bits, b.totals);

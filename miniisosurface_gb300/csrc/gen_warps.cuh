@@ -457,7 +457,7 @@ void launch_gen_warps_impl(const float* vol, const Grid& g, float iso, const Cas
     const bool bulk = (g.nx % 4 == 0) && ((reinterpret_cast<uintptr_t>(vol) & 15) == 0);
     const unsigned blocks = (unsigned)(p.nyb * p.nkc);
     auto kern = bulk ? k_gen_warps<MODE, IndexT, true> : k_gen_warps<MODE, IndexT, false>;
-    if (p.smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.smem);
+    allow_smem(kern, p.smem);
     kern<<<blocks, kThreads, p.smem, s>>>(vol, b.bits, g, iso, p.KC, p.nyb, p.slab_floats, cases, b.rowcnt, rs,
                                           b.totals, capV, capT, points, normals, tris, b.fe2mc, reverse);
 }

@@ -44,6 +44,14 @@ struct GenPlan {
 };
 
 int lanes_per_row(int W);
+
+// Opt a kernel into `dyn` bytes of dynamic shared memory (needed once the
+// dynamic plus static shared memory passes the 48 KB default).
+template <typename K>
+inline void allow_smem(K kern, size_t dyn)
+{
+    if (dyn > 16 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+}
 CountPlan count_plan(const Grid& g, int nsm);
 GenPlan gen_plan(const Grid& g, int nsm);
 
