@@ -131,7 +131,8 @@ size_t scratch_size(const Grid& g, const iso::CountPlan& cp)
 {
     const size_t R = (size_t)g.R;
     return align256(R * 16) + align256(R * 8) + align256(R * 4) + align256(R * 16) +
-           align256(3 * (size_t)cp.ngroups * 4) + align256(3 * (size_t)cp.ngroups * 8) + align256(4 * 8) +
+           align256(3 * (size_t)cp.ngroups * 4) + align256(3 * (size_t)cp.ngroups * 8) +
+           align256(3 * (size_t)iso::scan_segments(cp) * 8) + align256(4 * 8) +
            align256(R * (size_t)g.W * 4);
 }
 
@@ -145,6 +146,7 @@ void carve(void* base, const Grid& g, const iso::CountPlan& cp, FeBuffers& b)
     b.rowpre = reinterpret_cast<uint4*>(p); p += align256(R * 16);
     b.gsum = reinterpret_cast<uint32_t*>(p); p += align256(3 * (size_t)cp.ngroups * 4);
     b.goff = reinterpret_cast<unsigned long long*>(p); p += align256(3 * (size_t)cp.ngroups * 8);
+    b.part = reinterpret_cast<unsigned long long*>(p); p += align256(3 * (size_t)iso::scan_segments(cp) * 8);
     b.totals = reinterpret_cast<unsigned long long*>(p); p += align256(4 * 8);
     b.bits = reinterpret_cast<uint32_t*>(p);
 }

@@ -12,7 +12,7 @@
 //                  vertices cell row (j,k) owns.  Per (plane, block) totals go
 //                  to `groups`.
 //                  Each row also gets its exclusive prefix inside its group.
-//   k_scan_groups  exclusive scan of the group totals (one CTA); groups are in
+//   k_scan_*       exclusive scan of the group totals; groups are in
 //                  (k, block) order, which is the reference's (k, j) row order,
 //                  so the first vertex / triangle / MC vertex of a row (the
 //                  gridEdge xstart and triCounter offsets after pass 3) is
@@ -224,68 +224,91 @@ __global__ void __launch_bounds__(kThreads) k_count_cols(const float* __restrict
 }
 
 // Exclusive scan of the group totals (three arrays of n u32) into 64-bit
-// offsets, plus the grand totals; one CTA.  Each thread owns kScanPer
-// consecutive groups of a segment of 1024*kScanPer; segments are walked with
-// a running carry.
+// offsets, in two launches over segments of kSeg groups (256 threads x 8):
+//   k_scan_partial  one CTA per segment: segment totals
+//   k_scan_final    one CTA per segment: offset of the segment (sum of the
+//                   totals before it) + scan inside it; grand totals.
 constexpr int kScanPer = 8;
+constexpr int kSeg = kThreads * kScanPer;
 
-__global__ void __launch_bounds__(1024) k_scan_groups(const uint32_t* __restrict__ gsum, long long n,
-                                                      unsigned long long* __restrict__ goff,
-                                                      unsigned long long* __restrict__ totals)
+__device__ __forceinline__ void load_segment(const uint32_t* __restrict__ gsum, long long n, long long b,
+                                             uint32_t (&v)[3][kScanPer], unsigned long long (&s)[3])
 {
-    __shared__ unsigned long long s_w[3][32];
-    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    unsigned long long carry[3] = {0, 0, 0};
-    for (long long seg = 0; seg < n; seg += 1024LL * kScanPer) {
-        const long long b = seg + (long long)t * kScanPer;
-        uint32_t v[3][kScanPer];
-        unsigned long long s[3] = {0, 0, 0};
 #pragma unroll
-        for (int a = 0; a < 3; ++a) {
+    for (int a = 0; a < 3; ++a) {
+        s[a] = 0;
 #pragma unroll
-            for (int q = 0; q < kScanPer; ++q) {
-                v[a][q] = b + q < n ? __ldg(&gsum[a * n + b + q]) : 0u;
-                s[a] += v[a][q];
-            }
+        for (int q = 0; q < kScanPer; ++q) {
+            v[a][q] = b + q < n ? __ldg(&gsum[a * n + b + q]) : 0u;
+            s[a] += v[a][q];
         }
-        unsigned long long inc[3] = {s[0], s[1], s[2]};
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_scan_partial(const uint32_t* __restrict__ gsum, long long n,
+                                                           unsigned long long* __restrict__ part, int nseg)
+{
+    __shared__ unsigned long long s_w[3][kThreads / 32];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    uint32_t v[3][kScanPer];
+    unsigned long long s[3];
+    load_segment(gsum, n, (long long)blockIdx.x * kSeg + (long long)t * kScanPer, v, s);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) s[a] += __shfl_xor_sync(0xffffffffu, s[a], d);
+        if (lane == 0) s_w[a][warp] = s[a];
+    }
+    __syncthreads();
+    if (t < 3) {
+        unsigned long long tot = 0;
+        for (int w = 0; w < kThreads / 32; ++w) tot += s_w[t][w];
+        part[t * nseg + blockIdx.x] = tot;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_scan_final(const uint32_t* __restrict__ gsum, long long n,
+                                                         const unsigned long long* __restrict__ part, int nseg,
+                                                         unsigned long long* __restrict__ goff,
+                                                         unsigned long long* __restrict__ totals)
+{
+    __shared__ unsigned long long s_w[3][kThreads / 32];
+    __shared__ unsigned long long s_base[3];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    if (t < 3) {
+        unsigned long long b = 0, tot = 0;
+        for (int q = 0; q < nseg; ++q) {
+            const unsigned long long x = part[t * nseg + q];
+            if (q < (int)blockIdx.x) b += x;
+            tot += x;
+        }
+        s_base[t] = b;
+        if (blockIdx.x == 0) totals[t] = tot;
+    }
+    const long long b = (long long)blockIdx.x * kSeg + (long long)t * kScanPer;
+    uint32_t v[3][kScanPer];
+    unsigned long long s[3], inc[3];
+    load_segment(gsum, n, b, v, s);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        inc[a] = s[a];
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
-#pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                const unsigned long long y = __shfl_up_sync(0xffffffffu, inc[a], d);
-                if (lane >= d) inc[a] += y;
-            }
+            const unsigned long long y = __shfl_up_sync(0xffffffffu, inc[a], d);
+            if (lane >= d) inc[a] += y;
         }
-        if (lane == 31) {
-#pragma unroll
-            for (int a = 0; a < 3; ++a) s_w[a][warp] = inc[a];
-        }
-        __syncthreads();
-        unsigned long long before[3] = {0, 0, 0}, tot[3] = {0, 0, 0};
-        for (int w = 0; w < 32; ++w) {
-#pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                if (w < warp) before[a] += s_w[a][w];
-                tot[a] += s_w[a][w];
-            }
-        }
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            unsigned long long run = carry[a] + before[a] + inc[a] - s[a];
-#pragma unroll
-            for (int q = 0; q < kScanPer; ++q) {
-                if (b + q < n) goff[a * n + b + q] = run;
-                run += v[a][q];
-            }
-            carry[a] += tot[a];
-        }
-        __syncthreads();
+        if (lane == 31) s_w[a][warp] = inc[a];
     }
-    if (t == 0) {
-        totals[0] = carry[0];
-        totals[1] = carry[1];
-        totals[2] = carry[2];
+    __syncthreads();
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        unsigned long long run = s_base[a] + inc[a] - s[a];
+        for (int w = 0; w < warp; ++w) run += s_w[a][w];
+#pragma unroll
+        for (int q = 0; q < kScanPer; ++q) {
+            if (b + q < n) goff[a * n + b + q] = run;
+            run += v[a][q];
+        }
     }
 }
 
@@ -402,9 +425,13 @@ void launch_count(const float* vol, const Grid& g, float iso, const CaseTables* 
     }
 }
 
+int scan_segments(const CountPlan& p) { return (int)((p.ngroups + kSeg - 1) / kSeg); }
+
 void launch_scan(const CountPlan& p, FeBuffers& b, cudaStream_t s)
 {
-    k_scan_groups<<<1, 1024, 0, s>>>(b.gsum, p.ngroups, b.goff, b.totals);
+    const int nseg = scan_segments(p);
+    k_scan_partial<<<nseg, kThreads, 0, s>>>(b.gsum, p.ngroups, b.part, nseg);
+    k_scan_final<<<nseg, kThreads, 0, s>>>(b.gsum, p.ngroups, b.part, nseg, b.goff, b.totals);
 }
 
 RowStarts row_starts(const Grid& g, const CountPlan& p, const FeBuffers& b)
@@ -430,3 +457,5 @@ void launch_grid_edges(const Grid& g, const CountPlan& p, const FeBuffers& b, in
 }
 
 }  // namespace iso
+
+ISO_WAIT_STATS_ACCESSOR(iso_dbg_count_waits)

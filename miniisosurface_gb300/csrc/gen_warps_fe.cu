@@ -44,3 +44,5 @@ template void launch_fe_gen_warps<uint64_t>(const float*, const Grid&, float, co
                                             uint64_t*, int, cudaStream_t);
 
 }  // namespace iso
+
+ISO_WAIT_STATS_ACCESSOR(iso_dbg_gen_waits)

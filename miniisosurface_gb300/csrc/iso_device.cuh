@@ -472,14 +472,48 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar)
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
+#ifdef ISO_WAIT_STATS
+// Diagnostic build only: try_wait rounds and cycles spent in mbar_wait (per
+// translation unit), read back through the accessor each unit defines.
+__device__ unsigned long long g_wait_rounds, g_wait_cycles, g_wait_calls;
+#define ISO_WAIT_STATS_ACCESSOR(name)                                                  \
+    extern "C" void name(unsigned long long* o)                                      \
+    {                                                                                  \
+        cudaMemcpyFromSymbol(o, g_wait_rounds, 8);                                     \
+        cudaMemcpyFromSymbol(o + 1, g_wait_cycles, 8);                                 \
+        cudaMemcpyFromSymbol(o + 2, g_wait_calls, 8);                                  \
+        unsigned long long z = 0;                                                      \
+        cudaMemcpyToSymbol(g_wait_rounds, &z, 8);                                      \
+        cudaMemcpyToSymbol(g_wait_cycles, &z, 8);                                      \
+        cudaMemcpyToSymbol(g_wait_calls, &z, 8);                                       \
+    }
+#else
+#define ISO_WAIT_STATS_ACCESSOR(name)
+#endif
+
 // Bounded wait for phase `parity` of `bar`.  Returns false after kWaitLimit
 // rounds (the caller records a timeout status and stops issuing work).
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity)
 {
+#ifdef ISO_WAIT_STATS
+    const long long t0 = clock64();
+    for (unsigned n = 0; n < kWaitLimit; ++n) {
+        if (mbar_try_wait(bar, parity)) {
+            if ((threadIdx.x & 31) == 0) {
+                atomicAdd(&g_wait_rounds, (unsigned long long)n + 1);
+                atomicAdd(&g_wait_cycles, (unsigned long long)(clock64() - t0));
+                atomicAdd(&g_wait_calls, 1ull);
+            }
+            return true;
+        }
+    }
+    return false;
+#else
     for (unsigned n = 0; n < kWaitLimit; ++n) {
         if (mbar_try_wait(bar, parity)) return true;
     }
     return false;
+#endif
 }
 
 // Copy of rows of a plane slab into shared memory: one bulk copy (TMA engine)

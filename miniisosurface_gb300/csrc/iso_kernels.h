@@ -19,6 +19,7 @@ struct FeBuffers {
     uint4* rowpre = nullptr;               // R      row prefix inside its group (v, t, m)
     uint32_t* gsum = nullptr;              // 3*ngroups  group totals
     unsigned long long* goff = nullptr;    // 3*ngroups  group offsets
+    unsigned long long* part = nullptr;    // 3*nseg     scan segment totals
     unsigned long long* totals = nullptr;  // 4      vertices, triangles, mc vertices, status
     uint32_t* bits = nullptr;              // R*W    bit rows (row-wise kernels only)
     uint32_t* fe2mc = nullptr;             // >= V   FE vertex index -> MC index
@@ -59,6 +60,7 @@ GenPlan gen_plan(const Grid& g, int nsm);
 void launch_count(const float* vol, const Grid& g, float iso, const CaseTables* cases, bool mc,
                   const CountPlan& p, FeBuffers& b, cudaStream_t s);
 void launch_scan(const CountPlan& p, FeBuffers& b, cudaStream_t s);
+int scan_segments(const CountPlan& p);
 void launch_grid_edges(const Grid& g, const CountPlan& p, const FeBuffers& b, int scanned, unsigned long long* ge,
                        unsigned long long* tri_counter, cudaStream_t s);
 // Row-start accessor of a counted extraction.
