@@ -479,13 +479,13 @@ __device__ unsigned long long g_wait_rounds, g_wait_cycles, g_wait_calls;
 #define ISO_WAIT_STATS_ACCESSOR(name)                                                  \
     extern "C" void name(unsigned long long* o)                                      \
     {                                                                                  \
-        cudaMemcpyFromSymbol(o, g_wait_rounds, 8);                                     \
-        cudaMemcpyFromSymbol(o + 1, g_wait_cycles, 8);                                 \
-        cudaMemcpyFromSymbol(o + 2, g_wait_calls, 8);                                  \
+        cudaMemcpyFromSymbol(o, iso::g_wait_rounds, 8);                                \
+        cudaMemcpyFromSymbol(o + 1, iso::g_wait_cycles, 8);                            \
+        cudaMemcpyFromSymbol(o + 2, iso::g_wait_calls, 8);                             \
         unsigned long long z = 0;                                                      \
-        cudaMemcpyToSymbol(g_wait_rounds, &z, 8);                                      \
-        cudaMemcpyToSymbol(g_wait_cycles, &z, 8);                                      \
-        cudaMemcpyToSymbol(g_wait_calls, &z, 8);                                       \
+        cudaMemcpyToSymbol(iso::g_wait_rounds, &z, 8);                                 \
+        cudaMemcpyToSymbol(iso::g_wait_cycles, &z, 8);                                 \
+        cudaMemcpyToSymbol(iso::g_wait_calls, &z, 8);                                  \
     }
 #else
 #define ISO_WAIT_STATS_ACCESSOR(name)
