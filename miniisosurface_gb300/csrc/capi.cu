@@ -130,10 +130,8 @@ bool empty_grid(const Grid& g) { return g.nx < 2 || g.ny < 2 || g.nz < 2; }
 size_t scratch_size(const Grid& g, const iso::CountPlan& cp)
 {
     const size_t R = (size_t)g.R;
-    return align256(R * 16) + align256(R * 8) + align256(R * 4) + align256(R * 16) +
-           align256(3 * (size_t)cp.ngroups * 4) + align256(3 * (size_t)cp.ngroups * 8) +
-           align256(3 * (size_t)iso::scan_segments(cp) * 8) + align256(4 * 8) +
-           align256(R * (size_t)g.W * 4);
+    return align256(R * 16) + align256(R * 8) + align256(R * 4) + align256(3 * R * 8) +
+           align256(3 * (size_t)cp.nseg * 8) + align256(4 * 8) + align256(R * (size_t)g.W * 4);
 }
 
 void carve(void* base, const Grid& g, const iso::CountPlan& cp, FeBuffers& b)
@@ -143,10 +141,8 @@ void carve(void* base, const Grid& g, const iso::CountPlan& cp, FeBuffers& b)
     b.rowcnt = reinterpret_cast<uint4*>(p); p += align256(R * 16);
     b.trims = reinterpret_cast<uint2*>(p); p += align256(R * 8);
     b.mccnt = reinterpret_cast<uint32_t*>(p); p += align256(R * 4);
-    b.rowpre = reinterpret_cast<uint4*>(p); p += align256(R * 16);
-    b.gsum = reinterpret_cast<uint32_t*>(p); p += align256(3 * (size_t)cp.ngroups * 4);
-    b.goff = reinterpret_cast<unsigned long long*>(p); p += align256(3 * (size_t)cp.ngroups * 8);
-    b.part = reinterpret_cast<unsigned long long*>(p); p += align256(3 * (size_t)iso::scan_segments(cp) * 8);
+    b.starts = reinterpret_cast<unsigned long long*>(p); p += align256(3 * R * 8);
+    b.part = reinterpret_cast<unsigned long long*>(p); p += align256(3 * (size_t)cp.nseg * 8);
     b.totals = reinterpret_cast<unsigned long long*>(p); p += align256(4 * 8);
     b.bits = reinterpret_cast<uint32_t*>(p);
 }
@@ -254,7 +250,7 @@ void enqueue_count(iso_ctx* ctx, iso_algorithm algo, const float* vol, const Gri
     const bool mc = algo == ISO_MARCHING_CUBES;
     iso::launch_count(vol, g, iso, ctx->d_cases, mc, pl.cp, b, s);
     pm.mark(ISO_PASS_COUNT);
-    iso::launch_scan(pl.cp, b, s);
+    iso::launch_scan(g, pl.cp, mc, b, s);
     pm.mark(ISO_PASS_SCAN);
 }
 
@@ -657,7 +653,7 @@ iso_status iso_fe_pass3(iso_fe* fe)
     iso_ctx* ctx = fe->ctx;
     ISO_CUDA(ctx, cudaSetDevice(ctx->device));
     const Plans pl = make_plans(ctx, fe->g);
-    iso::launch_scan(pl.cp, fe->buf, 0);
+    iso::launch_scan(fe->g, pl.cp, false, fe->buf, 0);
     ISO_CUDA(ctx, cudaGetLastError());
     unsigned long long tot[4];
     ISO_CUDA(ctx, cudaMemcpy(tot, fe->buf.totals, sizeof(tot), cudaMemcpyDeviceToHost));

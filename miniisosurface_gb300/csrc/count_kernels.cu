@@ -2,257 +2,344 @@
 // on sm_103a, with pass 1 (x-edge classification, trims) fused into pass 2
 // (cube cases, per-row counts):
 //
-//   k_count_cols   one CTA per column = block of J grid rows x KC planes.  It
-//                  marches along z: classifies plane k+1 straight from the
-//                  volume into a bit-per-point mask in shared memory (the
-//                  reference's edgeCases bytes are never materialised), then
-//                  counts, for each grid row (j,k) of the block, its cut x, y
-//                  and z edges (the vertices it owns), the trims xl/xr, the
-//                  triangles of cell row (j,k) and, for Marching Cubes, the
-//                  vertices cell row (j,k) owns.  Per (plane, block) totals go
-//                  to `groups`.
-//                  Each row also gets its exclusive prefix inside its group.
-//   k_scan_*       exclusive scan of the group totals; groups are in
-//                  (k, block) order, which is the reference's (k, j) row order,
-//                  so the first vertex / triangle / MC vertex of a row (the
-//                  gridEdge xstart and triCounter offsets after pass 3) is
-//                  group offset + row prefix (RowStarts).
+//   k_count_warps  a CTA owns a block of 8 grid rows (one warp per row) and a
+//                  run of KC planes and marches along z.  Each warp classifies
+//                  its rows j and j+1 of plane k+1 straight from the volume
+//                  (loads for plane k+2 already in flight) into bit-per-point
+//                  words held one per lane -- the reference's edgeCases bytes
+//                  are never materialised -- and counts for grid row (j,k) its
+//                  cut x, y and z edges (the vertices it owns), the trims
+//                  xl/xr, the triangles of cell row (j,k) and, for Marching
+//                  Cubes, the vertices cell row (j,k) owns.  It writes the bit
+//                  words for pass 4.  No warp waits for another.  Rows of
+//                  up to 64 words; k_count_wide walks longer rows in chunks.
+//   k_scan_*       exclusive scans of the per-row counts in (k, j) order, the
+//                  reference's row order: the first vertex / triangle / MC
+//                  vertex of every row (gridEdge xstart and triCounter after
+//                  pass 3) and the totals.
 #include "iso_device.cuh"
 #include "iso_kernels.h"
 
 namespace iso {
 
-// How the count pass reads a plane of its block: staged through a shared-
-// memory slab ring by the TMA bulk engine (rows 16-byte aligned) or by
-// cp.async, or read directly (rows too wide to stage).
-enum SlabMode { kSlabBulk = 0, kSlabCpAsync = 1, kSlabDirect = 2 };
+constexpr int kCountRows = 8;  // grid rows per CTA, one per warp
 
-template <int G, bool MC, int MODE>
-__global__ void __launch_bounds__(kThreads) k_count_cols(const float* __restrict__ vol, Grid g, float iso, int KC,
-                                                         int nyb, int NS, int slab_floats,
-                                                         const CaseTables* __restrict__ cases,
-                                                         uint4* __restrict__ rowcnt, uint2* __restrict__ trims,
-                                                         uint32_t* __restrict__ mccnt, uint4* __restrict__ rowpre,
-                                                         uint32_t* __restrict__ gsum, long long ngroups,
-                                                         uint32_t* __restrict__ bits_out,
-                                                         unsigned long long* __restrict__ totals)
+// Raw values of one row held by a warp: lane l holds float4 l + 32u.
+template <int U>
+struct RowVals {
+    float4 v[U];
+};
+
+template <int U>
+__device__ __forceinline__ void load_row_vec4(const float* __restrict__ row, int nq, int lane, bool ok, RowVals<U>& r)
 {
-    constexpr int J = kThreads / G;  // grid rows per block
-    constexpr bool STAGED = MODE != kSlabDirect;
-    extern __shared__ __align__(128) unsigned char s_raw[];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const int q = lane + 32 * u;
+        r.v[u] = (ok && q < nq) ? __ldg(reinterpret_cast<const float4*>(row) + q) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+}
+
+// Bit words "value >= iso" of a row: word w ends up in lane w % 32, slot w / 32.
+template <int U, int NW>
+__device__ __forceinline__ void words_vec4(const RowVals<U>& r, int nq, int lane, float iso, uint32_t (&out)[NW])
+{
+#pragma unroll
+    for (int q = 0; q < NW; ++q) out[q] = 0u;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const int f = lane + 32 * u;
+        const float4 v = r.v[u];
+        const uint32_t nib = f < nq ? ((uint32_t)(v.x >= iso) | ((uint32_t)(v.y >= iso) << 1) |
+                                       ((uint32_t)(v.z >= iso) << 2) | ((uint32_t)(v.w >= iso) << 3))
+                                    : 0u;
+        uint32_t word = nib << (4 * (lane & 7));
+        word |= __shfl_xor_sync(0xffffffffu, word, 1);
+        word |= __shfl_xor_sync(0xffffffffu, word, 2);
+        word |= __shfl_xor_sync(0xffffffffu, word, 4);
+        // lanes 8g..8g+7 now hold word 4u+g; lane L wants word L + 32q
+        const uint32_t x = __shfl_sync(0xffffffffu, word, 8 * (lane & 3));
+#pragma unroll
+        for (int q = 0; q < NW; ++q) {
+            if (u == (lane >> 2) + 8 * q) out[q] = x;
+        }
+    }
+}
+
+template <int NW>
+__device__ __forceinline__ void words_scalar(const float* __restrict__ row, int nx, int W, bool ok, int lane, float iso,
+                                             uint32_t (&out)[NW])
+{
+#pragma unroll
+    for (int q = 0; q < NW; ++q) out[q] = 0u;
+    for (int w = 0; w < W; ++w) {
+        const int i = 32 * w + lane;
+        const float v = (ok && i < nx) ? __ldg(row + i) : 0.f;
+        const uint32_t m = __ballot_sync(0xffffffffu, ok && i < nx && v >= iso);
+#pragma unroll
+        for (int q = 0; q < NW; ++q) {
+            if (w == lane + 32 * q) out[q] = m;
+        }
+    }
+}
+
+// Next word (the source of bit i+1) of the lane's slot q.
+template <int NW>
+__device__ __forceinline__ uint32_t next_word(const uint32_t (&w)[NW], int q, int lane)
+{
+    const uint32_t dn = __shfl_down_sync(0xffffffffu, w[q], 1);
+    const uint32_t wrap = __shfl_sync(0xffffffffu, w[q + 1 < NW ? q + 1 : q], 0);
+    if (lane < 31) return dn;
+    return q + 1 < NW ? wrap : 0u;
+}
+
+// Counts of one grid row, accumulated word by word in each lane.
+struct RowCounts {
+    uint32_t xc = 0, yc = 0, zc = 0, tc = 0, mc = 0, first = 0xffffffffu, last = 0;
+};
+
+// Counts of word w of grid row (j,k): cut x / y / z edges the row owns, the
+// trim candidates, the triangles (and MC vertices) of its cells.
+template <bool MC>
+__device__ __forceinline__ void count_word(const RowWords& rw, int w, const Grid& g, int j, int k, bool hasY,
+                                           bool hasZ, const uint8_t* s_ntris, const uint16_t* s_cut, RowCounts& rc)
+{
+    const uint32_t evalid = validmask(w, g.nx - 1);  // x-edges / cells: i <= nx-2
+    const uint32_t pvalid = validmask(w, g.nx);      // points: i <= nx-1
+    const uint32_t xm = (rw.a ^ rw.ash) & evalid;
+    const uint32_t ym = hasY ? ((rw.a ^ rw.b) & pvalid) : 0u;
+    const uint32_t zm = hasZ ? ((rw.a ^ rw.c) & pvalid) : 0u;
+    rc.xc += __popc(xm);
+    rc.yc += __popc(ym);
+    rc.zc += __popc(zm);
+    // isCutEdge (FlyingEdgesAlgorithm.cpp:515-554): edge i is marked when
+    // it is cut or the y / z edge at its left point is.
+    const uint32_t marked = xm | ((ym | zm) & evalid);
+    if (marked) {
+        rc.first = min(rc.first, (uint32_t)(32 * w + __ffs(marked) - 1));
+        rc.last = max(rc.last, (uint32_t)(32 * w + 32 - __clz(marked)));
+    }
+    if (hasY && hasZ) {
+        for (uint32_t act = active_cells(rw, evalid); act; act &= act - 1) {
+            const int bit = __ffs(act) - 1;
+            const int c = cube_case(rw, bit);
+            rc.tc += s_ntris[c];
+            if (MC) rc.mc += __popc(mc_owned_edges(32 * w + bit == 0, j == 0, k == 0) & s_cut[c]);
+        }
+    }
+}
+
+// Warp totals of row r; lane 0 stores them.
+template <bool MC>
+__device__ __forceinline__ void finish_row(RowCounts& rc, int lane, long long r, const Grid& g,
+                                           uint4* __restrict__ rowcnt, uint2* __restrict__ trims,
+                                           uint32_t* __restrict__ mccnt)
+{
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        rc.xc += __shfl_xor_sync(0xffffffffu, rc.xc, d);
+        rc.yc += __shfl_xor_sync(0xffffffffu, rc.yc, d);
+        rc.zc += __shfl_xor_sync(0xffffffffu, rc.zc, d);
+        rc.tc += __shfl_xor_sync(0xffffffffu, rc.tc, d);
+        if (MC) rc.mc += __shfl_xor_sync(0xffffffffu, rc.mc, d);
+        rc.first = min(rc.first, __shfl_xor_sync(0xffffffffu, rc.first, d));
+        rc.last = max(rc.last, __shfl_xor_sync(0xffffffffu, rc.last, d));
+    }
+    if (lane == 0) {
+        rowcnt[r] = make_uint4(rc.xc, rc.yc, rc.zc, rc.tc);
+        trims[r] = make_uint2(rc.first == 0xffffffffu ? (uint32_t)g.nx : rc.first, rc.last);
+        if (MC) mccnt[r] = rc.mc;
+    }
+}
+
+template <bool MC, bool VEC4, int U, int NW>
+__global__ void __launch_bounds__(kThreads) k_count_warps(const float* __restrict__ vol, Grid g, float iso, int KC,
+                                                          int nyb, const CaseTables* __restrict__ cases,
+                                                          uint4* __restrict__ rowcnt, uint2* __restrict__ trims,
+                                                          uint32_t* __restrict__ mccnt, uint32_t* __restrict__ bits_out)
+{
     __shared__ uint8_t s_ntris[256];
     __shared__ uint16_t s_cut[256];
-    __shared__ uint32_t s_rc[3][J];
-    float* slots = reinterpret_cast<float*>(s_raw);
-    uint64_t* mbar = reinterpret_cast<uint64_t*>(s_raw + (size_t)NS * slab_floats * 4);
-    uint32_t* s_bits0 = reinterpret_cast<uint32_t*>(mbar + (STAGED ? NS : 0));
-    uint32_t* s_bits1 = s_bits0 + (J + 1) * g.W;
     for (int c = threadIdx.x; c < 256; c += blockDim.x) {
         s_ntris[c] = (uint8_t)iso_case_ntris(cases->tris[c]);
         s_cut[c] = cases->cut[c];
     }
-    const int jb = blockIdx.x % nyb, kc = blockIdx.x / nyb;
-    const int j0 = jb * J, JB = min(J, g.ny - j0), nbr = min(J + 1, g.ny - j0);
-    const int kb = kc * KC, ke = min(kb + KC, g.nz);
-    const int tid = threadIdx.x, lane = tid & 31, lig = lane & (G - 1);
-    const int jj = tid / G;  // the row this group counts
-    const int nchunks = (g.W + G - 1) / G;
-    const int nfl = nbr * g.nx;
-    const bool vec4 = (g.nx & 3) == 0 && (STAGED || (reinterpret_cast<uintptr_t>(vol) & 15) == 0);
-
-    if (STAGED && tid == 0) {
-        for (int s = 0; s < NS; ++s) mbar_init(&mbar[s], MODE == kSlabBulk ? 1u : (unsigned)kThreads);
-        fence_mbar_init();
-    }
     __syncthreads();
-    uint32_t pending = 0, parity = 0;  // per slot: copy in flight / next wait parity
-    auto issue = [&](int p) {
-        if (!STAGED || p > ke || p >= g.nz) return;
-        const int s = p % NS;
-        slab_copy<MODE == kSlabBulk>(slots + (size_t)s * slab_floats, vol + ((long long)p * g.ny + j0) * g.nx, nfl,
-                                     &mbar[s], tid, kThreads);
-        pending |= 1u << s;
-    };
-    auto wait = [&](int p) -> bool {
-        if (!STAGED) return true;
-        const int s = p % NS;
-        const bool ok = mbar_wait(&mbar[s], (parity >> s) & 1u);
-        parity ^= 1u << s;
-        pending &= ~(1u << s);
-        return ok;
-    };
-    auto drain = [&]() {
-        for (int s = 0; s < NS; ++s) {
-            if ((pending >> s) & 1u) {
-                mbar_wait(&mbar[s], (parity >> s) & 1u);
-                parity ^= 1u << s;
-                pending &= ~(1u << s);
-            }
-        }
-    };
-    // bit rows of plane p (slab or volume) into dst
-    auto classify = [&](int p, uint32_t* dst) {
-        if (STAGED) {
-            const float* src = slots + (size_t)(p % NS) * slab_floats;
-            if (vec4) classify_block<true, true>(src, g.nx, g.W, nbr, iso, dst);
-            else classify_block<false, true>(src, g.nx, g.W, nbr, iso, dst);
-        } else {
-            const float* src = vol + ((long long)p * g.ny + j0) * g.nx;
-            if (vec4) classify_block<true, false>(src, g.nx, g.W, nbr, iso, dst);
-            else classify_block<false, false>(src, g.nx, g.W, nbr, iso, dst);
-        }
-    };
+    const int jb = blockIdx.x % nyb, kc = blockIdx.x / nyb;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int j = jb * kCountRows + warp;
+    if (j >= g.ny) return;
+    const int kb = kc * KC, ke = min(kb + KC, g.nz);
+    const bool hasY = j < g.ny - 1;
+    const int jy = hasY ? j + 1 : j;  // row B (a valid address even when B does not exist)
+    const int nq = g.nx >> 2;
+    auto rowptr = [&](int k, int jj) { return vol + ((long long)k * g.ny + jj) * g.nx; };
 
-    for (int q = 0; q < NS; ++q) issue(kb + q);
-    bool alive = __syncthreads_and(wait(kb));
-    if (alive) {
-        classify(kb, (kb & 1) ? s_bits1 : s_bits0);
-        __syncthreads();
-        issue(kb + NS);
+    // words of rows A = (j,k), B = (j+1,k); Cw, Dw = the same rows at plane k+1
+    uint32_t A[NW], B[NW], Cw[NW], Dw[NW];
+    RowVals<U> pc, pd;  // raw values of plane k+1 (VEC4), loaded one step ahead
+    if (VEC4) {
+        RowVals<U> ra, rbv;
+        load_row_vec4<U>(rowptr(kb, j), nq, lane, true, ra);
+        load_row_vec4<U>(rowptr(kb, jy), nq, lane, hasY, rbv);
+        if (kb + 1 < g.nz) {
+            load_row_vec4<U>(rowptr(kb + 1, j), nq, lane, true, pc);
+            load_row_vec4<U>(rowptr(kb + 1, jy), nq, lane, hasY, pd);
+        }
+        words_vec4<U, NW>(ra, nq, lane, iso, A);
+        words_vec4<U, NW>(rbv, nq, lane, iso, B);
+    } else {
+        words_scalar<NW>(rowptr(kb, j), g.nx, g.W, true, lane, iso, A);
+        words_scalar<NW>(rowptr(kb, jy), g.nx, g.W, hasY, lane, iso, B);
     }
-    for (int k = kb; k < ke && alive; ++k) {
-        uint32_t* P0 = (k & 1) ? s_bits1 : s_bits0;  // plane k
-        uint32_t* P1 = (k & 1) ? s_bits0 : s_bits1;  // plane k+1
-        if (k + 1 < g.nz) {
-            alive = __syncthreads_and(wait(k + 1));
-            if (!alive) break;
-            classify(k + 1, P1);
+    for (int k = kb; k < ke; ++k) {
+        const bool hasZ = k + 1 < g.nz, cell = hasY && hasZ;
+        if (VEC4) {
+            words_vec4<U, NW>(pc, nq, lane, iso, Cw);
+            words_vec4<U, NW>(pd, nq, lane, iso, Dw);
+            if (k + 2 < g.nz && k + 1 < ke) {  // plane k+2 for the next step
+                load_row_vec4<U>(rowptr(k + 2, j), nq, lane, true, pc);
+                load_row_vec4<U>(rowptr(k + 2, jy), nq, lane, hasY, pd);
+            }
+        } else if (hasZ) {
+            words_scalar<NW>(rowptr(k + 1, j), g.nx, g.W, true, lane, iso, Cw);
+            words_scalar<NW>(rowptr(k + 1, jy), g.nx, g.W, hasY, lane, iso, Dw);
         }
-        __syncthreads();
-        issue(k + 1 + NS);  // the slot of plane k+1 is free again
-
-        const bool valid = jj < JB;
-        const int j = j0 + jj;
-        const bool hasY = valid && j < g.ny - 1;
-        const bool hasZ = valid && k < g.nz - 1;
-        const bool cell = hasY && hasZ;
-        const uint32_t* A = P0 + jj * g.W;
-        const uint32_t* B = A + g.W;
-        const uint32_t* Cc = P1 + jj * g.W;
-        const uint32_t* D = Cc + g.W;
-        uint32_t xc = 0, yc = 0, zc = 0, tc = 0, mc = 0, first = 0xffffffffu, last = 0;
-        for (int ch = 0; ch < nchunks; ++ch) {
-            const int w = ch * G + lig;
-            const bool in = valid && w < g.W, in1 = valid && w + 1 < g.W;
+        if (!hasZ) {
+#pragma unroll
+            for (int q = 0; q < NW; ++q) Cw[q] = Dw[q] = 0u;
+        }
+        RowCounts rc;
+        const long long r = (long long)k * g.ny + j;
+#pragma unroll
+        for (int q = 0; q < NW; ++q) {
+            const int w = lane + 32 * q;
             RowWords rw;
-            rw.a = in ? A[w] : 0u;
-            rw.b = (in && hasY) ? B[w] : 0u;
-            rw.c = (in && hasZ) ? Cc[w] : 0u;
-            rw.d = (in && cell) ? D[w] : 0u;
-            rw.ash = (rw.a >> 1) | ((in1 ? A[w + 1] : 0u) << 31);
-            rw.bsh = (rw.b >> 1) | ((in1 && hasY ? B[w + 1] : 0u) << 31);
-            rw.csh = (rw.c >> 1) | ((in1 && hasZ ? Cc[w + 1] : 0u) << 31);
-            rw.dsh = (rw.d >> 1) | ((in1 && cell ? D[w + 1] : 0u) << 31);
-            const uint32_t evalid = validmask(w, g.nx - 1);   // x-edges / cells: i <= nx-2
-            const uint32_t pvalid = validmask(w, g.nx);       // points: i <= nx-1
-            const uint32_t xm = (rw.a ^ rw.ash) & evalid;
-            const uint32_t ym = hasY ? ((rw.a ^ rw.b) & pvalid) : 0u;
-            const uint32_t zm = hasZ ? ((rw.a ^ rw.c) & pvalid) : 0u;
-            xc += __popc(xm);
-            yc += __popc(ym);
-            zc += __popc(zm);
-            // isCutEdge (FlyingEdgesAlgorithm.cpp:515-554): edge i is marked when
-            // it is cut or the y / z edge at its left point is.
-            const uint32_t marked = xm | ((ym | zm) & evalid);
-            if (marked) {
-                first = min(first, (uint32_t)(32 * w + __ffs(marked) - 1));
-                last = max(last, (uint32_t)(32 * w + 32 - __clz(marked)));
-            }
-            if (cell) {
-                for (uint32_t act = active_cells(rw, evalid); act; act &= act - 1) {
-                    const int bit = __ffs(act) - 1;
-                    const int c = cube_case(rw, bit);
-                    tc += s_ntris[c];
-                    if (MC) mc += __popc(mc_owned_edges(32 * w + bit == 0, j == 0, k == 0) & s_cut[c]);
-                }
-            }
-            if (in) bits_out[((long long)k * g.ny + j) * g.W + w] = rw.a;
+            rw.a = A[q];
+            rw.b = B[q];
+            rw.c = Cw[q];
+            rw.d = Dw[q];
+            rw.ash = (rw.a >> 1) | (next_word<NW>(A, q, lane) << 31);
+            rw.bsh = (rw.b >> 1) | (next_word<NW>(B, q, lane) << 31);
+            rw.csh = (rw.c >> 1) | (next_word<NW>(Cw, q, lane) << 31);
+            rw.dsh = (rw.d >> 1) | (next_word<NW>(Dw, q, lane) << 31);
+            count_word<MC>(rw, w, g, j, k, hasY, hasZ, s_ntris, s_cut, rc);
+            if (w < g.W) bits_out[r * g.W + w] = rw.a;
         }
+        finish_row<MC>(rc, lane, r, g, rowcnt, trims, mccnt);
 #pragma unroll
-        for (int d = G / 2; d > 0; d >>= 1) {
-            xc += __shfl_xor_sync(0xffffffffu, xc, d, G);
-            yc += __shfl_xor_sync(0xffffffffu, yc, d, G);
-            zc += __shfl_xor_sync(0xffffffffu, zc, d, G);
-            tc += __shfl_xor_sync(0xffffffffu, tc, d, G);
-            if (MC) mc += __shfl_xor_sync(0xffffffffu, mc, d, G);
-        }
-        first = group_min<G>(first, 0xffffffffu);
-        last = group_max<G>(last, 0xffffffffu);
-        if (lig == 0) {
-            if (valid) {
-                const long long r = (long long)k * g.ny + j;
-                rowcnt[r] = make_uint4(xc, yc, zc, tc);
-                trims[r] = make_uint2(first == 0xffffffffu ? (uint32_t)g.nx : first, last);
-                if (MC) mccnt[r] = mc;
-            }
-            s_rc[0][jj] = valid ? xc + yc + zc : 0u;
-            s_rc[1][jj] = valid ? tc : 0u;
-            s_rc[2][jj] = valid ? mc : 0u;
-        }
-        __syncthreads();
-        // exclusive prefix of the block's rows (warp 0) and the group totals
-        if (tid < 32) {
-            uint32_t run[3] = {0, 0, 0};
-            for (int base = 0; base < J; base += 32) {
-                const int q = base + tid;
-                uint32_t v[3], inc[3];
-#pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    v[a] = q < J ? s_rc[a][q] : 0u;
-                    inc[a] = v[a];
-                }
-#pragma unroll
-                for (int d = 1; d < 32; d <<= 1) {
-#pragma unroll
-                    for (int a = 0; a < 3; ++a) {
-                        const uint32_t t = __shfl_up_sync(0xffffffffu, inc[a], d);
-                        if (tid >= d) inc[a] += t;
-                    }
-                }
-                if (q < JB) {
-                    rowpre[(long long)k * g.ny + j0 + q] =
-                        make_uint4(run[0] + inc[0] - v[0], run[1] + inc[1] - v[1], run[2] + inc[2] - v[2], 0u);
-                }
-#pragma unroll
-                for (int a = 0; a < 3; ++a) run[a] += __shfl_sync(0xffffffffu, inc[a], 31);
-            }
-            if (tid < 3) gsum[tid * ngroups + (long long)k * nyb + jb] = run[tid];
+        for (int q = 0; q < NW; ++q) {
+            A[q] = Cw[q];
+            B[q] = Dw[q];
         }
     }
-    if (!alive && tid == 0) atomicOr(&totals[3], kStatusTimeout);
-    drain();
 }
 
-// Exclusive scan of the group totals (three arrays of n u32) into 64-bit
-// offsets, in two launches over segments of kSeg groups (256 threads x 8):
+// Word c*32 + lane of a row and, uniform over the warp, word c*32 + 32 (the
+// source of lane 31's bit 32): 33 coalesced 128-byte loads.
+__device__ __forceinline__ void chunk_words(const float* __restrict__ row, bool ok, int c, int nx, int lane, float iso,
+                                            uint32_t& word, uint32_t& next)
+{
+    word = 0u;
+    for (int t = 0; t <= 32; ++t) {
+        const long long i = 32ll * (32 * c + t) + lane;
+        const bool in = ok && i < nx;
+        const uint32_t m = __ballot_sync(0xffffffffu, in && __ldg(row + i) >= iso);
+        if (t == lane) word = m;
+        next = m;
+    }
+}
+
+// Rows longer than 64 words (nx > 2048): the same counts as k_count_warps,
+// the row walked in chunks of 32 words, the four rows of a step re-read from
+// the volume for every plane (twice the reads of the narrow kernel).
+template <bool MC>
+__global__ void __launch_bounds__(kThreads) k_count_wide(const float* __restrict__ vol, Grid g, float iso, int KC,
+                                                         int nyb, const CaseTables* __restrict__ cases,
+                                                         uint4* __restrict__ rowcnt, uint2* __restrict__ trims,
+                                                         uint32_t* __restrict__ mccnt, uint32_t* __restrict__ bits_out)
+{
+    __shared__ uint8_t s_ntris[256];
+    __shared__ uint16_t s_cut[256];
+    for (int c = threadIdx.x; c < 256; c += blockDim.x) {
+        s_ntris[c] = (uint8_t)iso_case_ntris(cases->tris[c]);
+        s_cut[c] = cases->cut[c];
+    }
+    __syncthreads();
+    const int jb = blockIdx.x % nyb, kc = blockIdx.x / nyb;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int j = jb * kCountRows + warp;
+    if (j >= g.ny) return;
+    const int kb = kc * KC, ke = min(kb + KC, g.nz);
+    const bool hasY = j < g.ny - 1;
+    const int jy = hasY ? j + 1 : j;
+    const int nchunks = (g.W + 31) / 32;
+    auto rowptr = [&](int k, int jj) { return vol + ((long long)k * g.ny + jj) * g.nx; };
+    for (int k = kb; k < ke; ++k) {
+        const bool hasZ = k + 1 < g.nz;
+        const int kz = hasZ ? k + 1 : k;
+        RowCounts rc;
+        const long long r = (long long)k * g.ny + j;
+        for (int c = 0; c < nchunks; ++c) {
+            RowWords rw;
+            uint32_t na, nb, nc, nd;
+            chunk_words(rowptr(k, j), true, c, g.nx, lane, iso, rw.a, na);
+            chunk_words(rowptr(k, jy), hasY, c, g.nx, lane, iso, rw.b, nb);
+            chunk_words(rowptr(kz, j), hasZ, c, g.nx, lane, iso, rw.c, nc);
+            chunk_words(rowptr(kz, jy), hasY && hasZ, c, g.nx, lane, iso, rw.d, nd);
+            const uint32_t da = __shfl_down_sync(0xffffffffu, rw.a, 1), db = __shfl_down_sync(0xffffffffu, rw.b, 1);
+            const uint32_t dc = __shfl_down_sync(0xffffffffu, rw.c, 1), dd = __shfl_down_sync(0xffffffffu, rw.d, 1);
+            rw.ash = (rw.a >> 1) | ((lane < 31 ? da : na) << 31);
+            rw.bsh = (rw.b >> 1) | ((lane < 31 ? db : nb) << 31);
+            rw.csh = (rw.c >> 1) | ((lane < 31 ? dc : nc) << 31);
+            rw.dsh = (rw.d >> 1) | ((lane < 31 ? dd : nd) << 31);
+            const int w = 32 * c + lane;
+            count_word<MC>(rw, w, g, j, k, hasY, hasZ, s_ntris, s_cut, rc);
+            if (w < g.W) bits_out[r * g.W + w] = rw.a;
+        }
+        finish_row<MC>(rc, lane, r, g, rowcnt, trims, mccnt);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Exclusive scans of the per-row counts (vertices = x+y+z cuts, triangles,
+// MC vertices) over the R = ny*nz rows, in two launches over segments of
+// kSeg rows (256 threads x 8):
 //   k_scan_partial  one CTA per segment: segment totals
-//   k_scan_final    one CTA per segment: offset of the segment (sum of the
-//                   totals before it) + scan inside it; grand totals.
+//   k_scan_final    one CTA per segment: offset of the segment + scan inside
+//                   it -> starts[3][R]; grand totals.
+// ---------------------------------------------------------------------------
 constexpr int kScanPer = 8;
 constexpr int kSeg = kThreads * kScanPer;
 
-__device__ __forceinline__ void load_segment(const uint32_t* __restrict__ gsum, long long n, long long b,
-                                             uint32_t (&v)[3][kScanPer], unsigned long long (&s)[3])
+template <bool MC>
+__device__ __forceinline__ void load_counts(const uint4* __restrict__ rowcnt, const uint32_t* __restrict__ mccnt,
+                                            long long R, long long b, uint32_t (&v)[3][kScanPer],
+                                            unsigned long long (&s)[3])
 {
+    s[0] = s[1] = s[2] = 0;
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        s[a] = 0;
+    for (int q = 0; q < kScanPer; ++q) {
+        const bool ok = b + q < R;
+        const uint4 c = ok ? __ldg(&rowcnt[b + q]) : make_uint4(0, 0, 0, 0);
+        v[0][q] = c.x + c.y + c.z;
+        v[1][q] = c.w;
+        v[2][q] = (MC && ok) ? __ldg(&mccnt[b + q]) : 0u;
 #pragma unroll
-        for (int q = 0; q < kScanPer; ++q) {
-            v[a][q] = b + q < n ? __ldg(&gsum[a * n + b + q]) : 0u;
-            s[a] += v[a][q];
-        }
+        for (int a = 0; a < 3; ++a) s[a] += v[a][q];
     }
 }
 
-__global__ void __launch_bounds__(kThreads) k_scan_partial(const uint32_t* __restrict__ gsum, long long n,
+template <bool MC>
+__global__ void __launch_bounds__(kThreads) k_scan_partial(const uint4* __restrict__ rowcnt,
+                                                           const uint32_t* __restrict__ mccnt, long long R,
                                                            unsigned long long* __restrict__ part, int nseg)
 {
     __shared__ unsigned long long s_w[3][kThreads / 32];
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     uint32_t v[3][kScanPer];
     unsigned long long s[3];
-    load_segment(gsum, n, (long long)blockIdx.x * kSeg + (long long)t * kScanPer, v, s);
+    load_counts<MC>(rowcnt, mccnt, R, (long long)blockIdx.x * kSeg + (long long)t * kScanPer, v, s);
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
 #pragma unroll
@@ -267,9 +354,11 @@ __global__ void __launch_bounds__(kThreads) k_scan_partial(const uint32_t* __res
     }
 }
 
-__global__ void __launch_bounds__(kThreads) k_scan_final(const uint32_t* __restrict__ gsum, long long n,
+template <bool MC>
+__global__ void __launch_bounds__(kThreads) k_scan_final(const uint4* __restrict__ rowcnt,
+                                                         const uint32_t* __restrict__ mccnt, long long R,
                                                          const unsigned long long* __restrict__ part, int nseg,
-                                                         unsigned long long* __restrict__ goff,
+                                                         unsigned long long* __restrict__ starts,
                                                          unsigned long long* __restrict__ totals)
 {
     __shared__ unsigned long long s_w[3][kThreads / 32];
@@ -288,7 +377,7 @@ __global__ void __launch_bounds__(kThreads) k_scan_final(const uint32_t* __restr
     const long long b = (long long)blockIdx.x * kSeg + (long long)t * kScanPer;
     uint32_t v[3][kScanPer];
     unsigned long long s[3], inc[3];
-    load_segment(gsum, n, b, v, s);
+    load_counts<MC>(rowcnt, mccnt, R, b, v, s);
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         inc[a] = s[a];
@@ -301,12 +390,12 @@ __global__ void __launch_bounds__(kThreads) k_scan_final(const uint32_t* __restr
     }
     __syncthreads();
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
+    for (int a = 0; a < (MC ? 3 : 2); ++a) {
         unsigned long long run = s_base[a] + inc[a] - s[a];
         for (int w = 0; w < warp; ++w) run += s_w[a][w];
 #pragma unroll
         for (int q = 0; q < kScanPer; ++q) {
-            if (b + q < n) goff[a * n + b + q] = run;
+            if (b + q < R) starts[a * R + b + q] = run;
             run += v[a][q];
         }
     }
@@ -345,33 +434,14 @@ int lanes_per_row(int W)
     return G;
 }
 
-// Blocks of J = 256/G rows with G >= lanes per row, G doubled until the
-// slab ring (3 slabs of J+1 rows) fits kCountSmem so that several CTAs share
-// an SM; columns of KC planes, ~8 CTAs per SM in total.
-constexpr size_t kCountSmem = 64 * 1024;
-constexpr int kCountSlots = 3;
-
 CountPlan count_plan(const Grid& g, int nsm)
 {
     CountPlan p;
-    int G = lanes_per_row(g.W);
-    for (;;) {
-        const int J = kThreads / G;
-        const size_t slab = ((size_t)(J + 1) * g.nx + 31) & ~(size_t)31;
-        const size_t smem = kCountSlots * slab * 4 + kCountSlots * 8 + 2 * (size_t)(J + 1) * g.W * 4;
-        if (smem <= kCountSmem || G == 32) {
-            p.G = G;
-            p.J = J;
-            p.slab_floats = (int)slab;
-            p.staged = smem <= 2 * kCountSmem;
-            p.NS = p.staged ? kCountSlots : 0;
-            p.smem = p.staged ? smem : 2 * (size_t)(J + 1) * g.W * 4;
-            if (!p.staged) p.slab_floats = 0;
-            break;
-        }
-        G *= 2;
-    }
+    p.J = kCountRows;
     p.nyb = (g.ny + p.J - 1) / p.J;
+    p.vec_u = 1;
+    while (p.vec_u * 128 < g.nx) p.vec_u <<= 1;  // float4 per lane for one row
+    // ~8 CTAs per SM in total, at least 8 planes per column
     const long long target = (long long)nsm * 8;
     int nkc = (int)((target + p.nyb - 1) / p.nyb);
     if (nkc < 1) nkc = 1;
@@ -379,72 +449,64 @@ CountPlan count_plan(const Grid& g, int nsm)
     if (p.KC < 8) p.KC = 8;
     if (p.KC > g.nz) p.KC = g.nz;
     p.nkc = (g.nz + p.KC - 1) / p.KC;
-    p.ngroups = (long long)g.nz * p.nyb;
+    p.nseg = (int)((g.R + kSeg - 1) / kSeg);
     return p;
 }
 
-#define ISO_DISPATCH_G(G, ...)                                  \
-    switch (G) {                                                \
-        case 1: { constexpr int kG = 1; __VA_ARGS__; } break;   \
-        case 2: { constexpr int kG = 2; __VA_ARGS__; } break;   \
-        case 4: { constexpr int kG = 4; __VA_ARGS__; } break;   \
-        case 8: { constexpr int kG = 8; __VA_ARGS__; } break;   \
-        case 16: { constexpr int kG = 16; __VA_ARGS__; } break; \
-        default: { constexpr int kG = 32; __VA_ARGS__; } break; \
-    }
-
-template <int G, bool MC, int MODE>
+template <bool MC>
 static void count_launch(const CountPlan& p, const float* vol, const Grid& g, float iso, const CaseTables* cases,
                          FeBuffers& b, cudaStream_t s)
 {
-    auto kern = k_count_cols<G, MC, MODE>;
-    allow_smem(kern, p.smem);
-    kern<<<(unsigned)(p.nyb * p.nkc), kThreads, p.smem, s>>>(vol, g, iso, p.KC, p.nyb, p.NS, p.slab_floats, cases,
-                                                              b.rowcnt, b.trims, b.mccnt, b.rowpre, b.gsum,
-                                                              p.ngroups, b.bits, b.totals);
-}
-
-template <int G, bool MC>
-static void count_mode(const CountPlan& p, const float* vol, const Grid& g, float iso, const CaseTables* cases,
-                       FeBuffers& b, cudaStream_t s)
-{
-    const bool bulk = (g.nx % 4 == 0) && ((reinterpret_cast<uintptr_t>(vol) & 15) == 0);
-    if (!p.staged) count_launch<G, MC, kSlabDirect>(p, vol, g, iso, cases, b, s);
-    else if (bulk) count_launch<G, MC, kSlabBulk>(p, vol, g, iso, cases, b, s);
-    else count_launch<G, MC, kSlabCpAsync>(p, vol, g, iso, cases, b, s);
+    const unsigned blocks = (unsigned)(p.nyb * p.nkc);
+    const bool vec4 = g.W <= 64 && (g.nx % 4 == 0) && ((reinterpret_cast<uintptr_t>(vol) & 15) == 0);
+#define ISO_COUNT(VEC, UU, NWW)                                                                                \
+    k_count_warps<MC, VEC, UU, NWW><<<blocks, kThreads, 0, s>>>(vol, g, iso, p.KC, p.nyb, cases, b.rowcnt,     \
+                                                                b.trims, b.mccnt, b.bits)
+    if (vec4) {
+        switch (p.vec_u) {
+            case 1: ISO_COUNT(true, 1, 1); break;
+            case 2: ISO_COUNT(true, 2, 1); break;
+            case 4: ISO_COUNT(true, 4, 1); break;
+            case 8: ISO_COUNT(true, 8, 1); break;
+            default: ISO_COUNT(true, 16, 2); break;
+        }
+    } else if (g.W <= 32) {
+        ISO_COUNT(false, 1, 1);
+    } else if (g.W <= 64) {
+        ISO_COUNT(false, 1, 2);
+    } else {
+        k_count_wide<MC><<<blocks, kThreads, 0, s>>>(vol, g, iso, p.KC, p.nyb, cases, b.rowcnt, b.trims, b.mccnt,
+                                                     b.bits);
+    }
+#undef ISO_COUNT
 }
 
 void launch_count(const float* vol, const Grid& g, float iso, const CaseTables* cases, bool mc,
                   const CountPlan& p, FeBuffers& b, cudaStream_t s)
 {
     cudaMemsetAsync(b.totals + 3, 0, sizeof(unsigned long long), s);  // device status
-    if (mc) {
-        ISO_DISPATCH_G(p.G, (count_mode<kG, true>(p, vol, g, iso, cases, b, s)));
-    } else {
-        ISO_DISPATCH_G(p.G, (count_mode<kG, false>(p, vol, g, iso, cases, b, s)));
-    }
+    if (mc) count_launch<true>(p, vol, g, iso, cases, b, s);
+    else count_launch<false>(p, vol, g, iso, cases, b, s);
 }
 
-int scan_segments(const CountPlan& p) { return (int)((p.ngroups + kSeg - 1) / kSeg); }
-
-void launch_scan(const CountPlan& p, FeBuffers& b, cudaStream_t s)
+void launch_scan(const Grid& g, const CountPlan& p, bool mc, FeBuffers& b, cudaStream_t s)
 {
-    const int nseg = scan_segments(p);
-    k_scan_partial<<<nseg, kThreads, 0, s>>>(b.gsum, p.ngroups, b.part, nseg);
-    k_scan_final<<<nseg, kThreads, 0, s>>>(b.gsum, p.ngroups, b.part, nseg, b.goff, b.totals);
+    if (mc) {
+        k_scan_partial<true><<<p.nseg, kThreads, 0, s>>>(b.rowcnt, b.mccnt, g.R, b.part, p.nseg);
+        k_scan_final<true><<<p.nseg, kThreads, 0, s>>>(b.rowcnt, b.mccnt, g.R, b.part, p.nseg, b.starts, b.totals);
+    } else {
+        k_scan_partial<false><<<p.nseg, kThreads, 0, s>>>(b.rowcnt, b.mccnt, g.R, b.part, p.nseg);
+        k_scan_final<false><<<p.nseg, kThreads, 0, s>>>(b.rowcnt, b.mccnt, g.R, b.part, p.nseg, b.starts, b.totals);
+    }
 }
 
 RowStarts row_starts(const Grid& g, const CountPlan& p, const FeBuffers& b)
 {
+    (void)p;
     RowStarts rs;
-    rs.goff = b.goff;
-    rs.rowpre = b.rowpre;
-    rs.ngroups = p.ngroups;
+    rs.starts = b.starts;
+    rs.R = g.R;
     rs.ny = g.ny;
-    rs.nyb = p.nyb;
-    int sh = 0;
-    while ((1 << sh) < p.J) ++sh;
-    rs.jshift = sh;
     return rs;
 }
 
@@ -456,6 +518,6 @@ void launch_grid_edges(const Grid& g, const CountPlan& p, const FeBuffers& b, in
                                                   tri_counter);
 }
 
-}  // namespace iso
-
 ISO_WAIT_STATS_ACCESSOR(iso_dbg_count_waits)
+
+}  // namespace iso

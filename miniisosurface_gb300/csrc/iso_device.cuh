@@ -6,10 +6,8 @@
 //                          edges owned by the row, triangles of cell row (j,k)
 //   trims   uint2[R]       xl, xr of the row (FlyingEdgesAlgorithm.cpp:47-65)
 //   mccnt   uint32[R]      marching cubes: vertices owned by cell row (j,k)
-//   gsum    u32[3][ngroups] per group (plane k, block of J rows): totals of
-//                          (vertices, triangles, mc vertices)
-//   goff    u64[3][ngroups] exclusive scan of gsum
-//   rowpre  uint4[R]       the row's exclusive prefix inside its group
+//   starts  u64[3][R]      first vertex / triangle / mc vertex of each row
+//                          (exclusive scans of the counts in row order)
 //   bits    uint32[R][W]   W = ceil(nx/32); bit i of row r = value >= isovalue
 //                          (written only when a row-wise kernel needs it)
 //   totals  u64[4]         vertices, triangles, mc vertices, device status
@@ -537,24 +535,18 @@ __device__ __forceinline__ void slab_copy(float* dst, const float* src, int nfl,
 
 
 // First vertex (comp 0), triangle (1) or MC vertex (2) of grid row r =
-// k*ny + j: offset of its counting group (plane k, block j >> jshift) plus
-// the row's exclusive prefix inside the group.
+// k*ny + j, from the scanned starts[3][R].
 struct RowStarts {
-    const unsigned long long* goff;  // 3 x ngroups
-    const uint4* rowpre;             // R
-    long long ngroups;
-    int ny, nyb, jshift;
-    __device__ __forceinline__ unsigned long long get(int k, int j, int comp) const
-    {
-        const long long r = (long long)k * ny + j;
-        const uint4 p = __ldg(&rowpre[r]);
-        return __ldg(&goff[comp * ngroups + (long long)k * nyb + (j >> jshift)]) +
-               (comp == 0 ? p.x : (comp == 1 ? p.y : p.z));
-    }
+    const unsigned long long* starts;
+    long long R;
+    int ny;
     __device__ __forceinline__ unsigned long long get(long long r, int comp) const
     {
-        const int k = (int)(r / ny);
-        return get(k, (int)(r - (long long)k * ny), comp);
+        return __ldg(&starts[comp * R + r]);
+    }
+    __device__ __forceinline__ unsigned long long get(int k, int j, int comp) const
+    {
+        return get((long long)k * ny + j, comp);
     }
 };
 

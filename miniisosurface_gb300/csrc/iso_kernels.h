@@ -16,23 +16,20 @@ struct FeBuffers {
     uint4* rowcnt = nullptr;               // R      x/y/z cuts, triangles
     uint2* trims = nullptr;                // R      xl, xr (pass 1 trims)
     uint32_t* mccnt = nullptr;             // R      MC vertices per cell row
-    uint4* rowpre = nullptr;               // R      row prefix inside its group (v, t, m)
-    uint32_t* gsum = nullptr;              // 3*ngroups  group totals
-    unsigned long long* goff = nullptr;    // 3*ngroups  group offsets
-    unsigned long long* part = nullptr;    // 3*nseg     scan segment totals
+    unsigned long long* starts = nullptr;  // 3*R    first vertex, triangle, MC vertex of each row
+    unsigned long long* part = nullptr;    // 3*nseg scan segment totals
     unsigned long long* totals = nullptr;  // 4      vertices, triangles, mc vertices, status
     uint32_t* bits = nullptr;              // R*W    bit rows (row-wise kernels only)
     uint32_t* fe2mc = nullptr;             // >= V   FE vertex index -> MC index
 };
 
-// Work split of the counting pass: blocks of J = 256/G grid rows, columns of
-// KC planes, one CTA per (block, column).
+// Work split of the counting pass: blocks of J = 8 grid rows (a warp per
+// row), columns of KC planes, one CTA per (block, column); nseg segments of
+// the row scans.
 struct CountPlan {
-    int G = 1, J = 1, nyb = 1, KC = 1, nkc = 1;
-    int NS = 0, slab_floats = 0;  // slab ring (NS slots), 0 when planes are read directly
-    bool staged = false;
-    long long ngroups = 0;
-    size_t smem = 0;
+    int J = 8, nyb = 1, KC = 1, nkc = 1;
+    int vec_u = 1;  // float4 loads per lane for one row (rows up to 64 words)
+    int nseg = 1;
 };
 
 // Work split of the warp-per-row generate kernels: blocks of J = 8 rows,
@@ -59,8 +56,7 @@ GenPlan gen_plan(const Grid& g, int nsm);
 // passes 1-3
 void launch_count(const float* vol, const Grid& g, float iso, const CaseTables* cases, bool mc,
                   const CountPlan& p, FeBuffers& b, cudaStream_t s);
-void launch_scan(const CountPlan& p, FeBuffers& b, cudaStream_t s);
-int scan_segments(const CountPlan& p);
+void launch_scan(const Grid& g, const CountPlan& p, bool mc, FeBuffers& b, cudaStream_t s);
 void launch_grid_edges(const Grid& g, const CountPlan& p, const FeBuffers& b, int scanned, unsigned long long* ge,
                        unsigned long long* tri_counter, cudaStream_t s);
 // Row-start accessor of a counted extraction.

@@ -93,6 +93,11 @@ def test_wide_rows_multi_chunk(M):
     both(M, vol, 0.0)
     vol = M.generate_value_noise((1029, 3, 3), 4, 8, seed=12)
     both(M, vol, 0.1)
+    # nx > 64*32 points: the chunked count kernel
+    vol = M.generate_value_noise((2300, 4, 3), 4, 16, seed=13)
+    both(M, vol, 0.0)
+    vol = M.generate_value_noise((4099, 2, 3), 4, 8, seed=14)
+    both(M, vol, -0.05)
 
 
 @pytest.mark.parametrize("dims", [(2, 2, 2), (2, 9, 5), (3, 2, 7), (33, 2, 2), (5, 6, 2), (31, 32, 33), (32, 17, 9),
