@@ -42,7 +42,8 @@ typedef enum iso_status {
     ISO_ERR_TIMEOUT = 6,     /* a bounded device-side wait gave up */
     ISO_ERR_IO = 7,          /* file cannot be opened / read / written (util::file_not_found) */
     ISO_ERR_FORMAT = 8,      /* malformed VTK file (util::bad_format, LoadImage.h:45-133) */
-    ISO_ERR_STATE = 9        /* pass called out of order */
+    ISO_ERR_STATE = 9,       /* pass called out of order */
+    ISO_ERR_TOO_LARGE = 10   /* grid beyond the fixed scratch of iso_count_device_noalloc */
 } iso_status;
 
 typedef enum iso_algorithm {
@@ -107,6 +108,24 @@ iso_status iso_ctx_profile_read(iso_ctx* ctx, double* ms, int64_t* launches);
  * exact output sizes.  volume is a device pointer. */
 iso_status iso_count_device(iso_ctx* ctx, iso_algorithm algo, const float* volume, const iso_grid* grid,
                             float isoval, int64_t* n_points, int64_t* n_tris, void* stream);
+
+/* Allocation-free count (no counterpart in the reference): the sizes
+ * iso_count_device returns, for callers that must not allocate device memory
+ * while they size a mesh (a solver that reserved the device for its own
+ * pool, an allocator sizing a mesh before carving it from its arena, loops
+ * that a device-wide cudaFree would stall).  No context: all scratch is a
+ * fixed 16 MiB device array reserved when the library's module loads, so
+ * grids of more than ISO_NOALLOC_MAX_ROWS rows (ny * nz) are rejected with
+ * ISO_ERR_TOO_LARGE.  Runs on the calling thread's current device; volume
+ * and counts are device pointers on it.  Enqueues the count on `stream` and
+ * returns: counts[0] = vertices, counts[1] = triangles once the stream gets
+ * there.  The first call on a device does a one-time set-up (symbol lookup
+ * and a synchronous copy of the case tables), so make it before any stream
+ * capture.  Calls on one device must not overlap (other streams or host
+ * threads): they share the scratch. */
+#define ISO_NOALLOC_MAX_ROWS (1 << 20)
+iso_status iso_count_device_noalloc(iso_algorithm algo, const float* volume, const iso_grid* grid, float isoval,
+                                    int64_t* counts, void* stream);
 
 /* Full extraction, volume and output in device memory.  Synchronises the
  * stream before returning.  If the buffers are too small nothing is written,

@@ -18,6 +18,8 @@ ISO_ERR_TIMEOUT = 6
 ISO_ERR_IO = 7
 ISO_ERR_FORMAT = 8
 ISO_ERR_STATE = 9
+ISO_ERR_TOO_LARGE = 10
+ISO_NOALLOC_MAX_ROWS = 1 << 20
 
 PASS_NAMES = ("classify", "count", "scan", "fe_generate", "mc_vertices", "mc_triangles")
 
@@ -47,6 +49,8 @@ SIGNATURES = {
     "iso_ctx_profile_read": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
     "iso_count_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.POINTER(IsoGrid), C.c_float,
                                    C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.c_void_p]),
+    "iso_count_device_noalloc": (C.c_int, [C.c_int, C.c_void_p, C.POINTER(IsoGrid), C.c_float, C.c_void_p,
+                                           C.c_void_p]),
     "iso_extract_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.POINTER(IsoGrid), C.c_float,
                                      C.POINTER(IsoMesh), C.c_void_p]),
     "iso_extract_device_async": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.POINTER(IsoGrid), C.c_float,

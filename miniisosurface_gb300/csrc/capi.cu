@@ -343,6 +343,7 @@ const char* iso_status_string(iso_status s)
         case ISO_ERR_IO: return "file error";
         case ISO_ERR_FORMAT: return "bad file format";
         case ISO_ERR_STATE: return "call out of order";
+        case ISO_ERR_TOO_LARGE: return "grid larger than the fixed scratch of the allocation-free entry point";
     }
     return "unknown status";
 }
