@@ -13,17 +13,26 @@
 // memory; the gradient neighbours at planes k-1 and k+2 come from L2.
 //
 // Per step a warp handles grid row (j, k) with one 32-bit word of the bit
-// mask written by the count pass per lane:
-//   masks + popc prefixes (warp scans) of the 8 cut masks of the cell row;
+// mask written by the count pass per lane (the bit words and row starts of
+// the next step load while this one runs):
+//   the 8 cut masks of the cell row and their popc prefixes (warp scans)
+//   give, per word, the id of each mask's first cut edge relative to the
+//   row's first vertex; the warp keeps them in shared memory (mb), so any
+//   lane numbers any edge of any cell with one 8-byte load and a popc;
 //   FE  : the row's vertices, one per lane (a shuffle binary search maps the
 //         lane's vertex rank to a word and __fns to a bit), written to
-//         consecutive ids; then the row's active cells, one per lane, each
-//         writing its triangles (corner ids = popc ranks)
-//   MC  : the vertices owned by cell row (j, k) in owner-cell /
-//         first-appearance order (marchingCubes/serial/main.cpp:139-177),
-//         one per lane, and the Flying Edges -> MC index map
-//   TRI : (no volume) triangles with corners mapped through that map.
+//         consecutive ids;
+//   the active cells of the cell row are compacted, 32 at a time, into the
+//   warp's cell list (i, cube case), then
+//   FE, TRI: their triangles are listed as (cell, triangle) pairs and written
+//         one triangle per lane, consecutive lanes storing consecutive
+//         triangles (TRI, without volume, maps the corners through the
+//         Flying Edges -> MC index map);
+//   MC  : the vertices the cells own, in owner-cell / first-appearance order
+//         (marchingCubes/serial/main.cpp:139-177), one per lane, and that map.
 #pragma once
+#include <cmath>
+
 #include "iso_device.cuh"
 #include "iso_kernels.h"
 
@@ -31,6 +40,9 @@ namespace iso {
 
 constexpr int kGenRows = 8;    // grid rows per CTA, one per warp
 constexpr int kGenSlots = 4;   // planes k, k+1 resident; k+2, k+3 in flight
+constexpr int kGenCells = 32;  // cells per batch
+constexpr int kGenTris = 5 * kGenCells;    // triangles of a batch, at most
+constexpr int kGenOwned = 12 * kGenCells;  // MC vertices owned by a batch, at most
 enum GenMode { kGenFE = 0, kGenMC = 1, kGenTri = 2 };
 
 struct GenSlab {
@@ -46,51 +58,128 @@ __host__ __device__ inline GenSlab gen_slab_rows(int j0, int ny)
     return s;
 }
 
-// Values of the volume around the row while planes k and k+1 are staged.
-struct WarpSlab {
-    const float* vol;
-    const float* sk;   // slab of plane k, indexed by (j - jlo) * nx + i
-    const float* sk1;  // slab of plane k+1
-    int k, jlo, nx, ny;
-    __device__ __forceinline__ float operator()(int i, int j, int p) const
+// Per-warp scratch in shared memory, after the slab ring and its barriers:
+//   mb[8][W]   {cut mask, id of its first cut edge - the row's first vertex}
+//              per mask (xA xB xC xD yA yC zA zB) and word
+//   cell[32]   the batch's active cells: i | cube case << 16
+//   list[...]  FE / TRI: the batch's triangles, cell | triangle << 5 (u8);
+//              MC: the batch's owned vertices, cell | cube edge << 5 (u16)
+__host__ __device__ inline size_t gen_warp_scratch_bytes(int W, int mode)
+{
+    const size_t list = mode == kGenMC ? (size_t)kGenOwned * 2 : (size_t)kGenTris;
+    return ((size_t)8 * W * 8 + kGenCells * 4 + list + 15) & ~(size_t)15;
+}
+
+// Bytes of the slab ring and its barriers.
+__host__ __device__ inline size_t gen_ring_bytes(int slab_floats)
+{
+    return (size_t)kGenSlots * slab_floats * 4 + 2 * kGenSlots * 8;
+}
+
+// Divisors of the gradient: the reference divides by the spacing (one-sided
+// differences at the faces) or by twice the spacing.  When every spacing is
+// a power of two, dividing equals multiplying by the exact reciprocal: both
+// round the same real number.
+struct GradScale {
+    float sp[3], inv1[3], inv2[3];
+    int exact;
+};
+
+inline GradScale make_grad_scale(const Grid& g)
+{
+    GradScale s;
+    s.exact = 1;
+    for (int a = 0; a < 3; ++a) {
+        const float sp = g.sp[a];
+        int e = 0;
+        const float m = std::frexp(sp, &e);  // sp = m * 2^e, m in [0.5, 1)
+        const bool pow2 = sp > 0.f && m == 0.5f && e >= -124 && e <= 126;
+        if (!pow2) s.exact = 0;
+        s.sp[a] = sp;
+        s.inv1[a] = pow2 ? std::ldexp(1.0f, 1 - e) : 0.f;  // 1 / sp
+        s.inv2[a] = pow2 ? std::ldexp(1.0f, -e) : 0.f;     // 1 / (2 sp)
+    }
+    return s;
+}
+
+// grad_component() of iso_device.cuh along axis a (negated central
+// difference, one-sided at the faces).
+__device__ __forceinline__ float grad_axis(float prev, float here, float next, int p, int n, int a,
+                                           const GradScale& gs)
+{
+    const bool lo = p == 0, hi = p == n - 1;
+    const float num = lo ? fsub(here, next) : (hi ? fsub(prev, here) : fsub(prev, next));
+    const bool one = lo || hi;
+    if (gs.exact) {
+        const float r1 = a == 0 ? gs.inv1[0] : (a == 1 ? gs.inv1[1] : gs.inv1[2]);
+        const float r2 = a == 0 ? gs.inv2[0] : (a == 1 ? gs.inv2[1] : gs.inv2[2]);
+        return fmul(num, one ? r1 : r2);
+    }
+    const float sp = a == 0 ? gs.sp[0] : (a == 1 ? gs.sp[1] : gs.sp[2]);
+    return fdiv(num, one ? sp : fmul(2.0f, sp));
+}
+
+// The four planes around step k (index dp = plane - k + 1: k-1, k, k+1,
+// k+2), each addressed from row jlo: the staged planes in shared memory, the
+// others in global memory.  Planes outside the grid alias a valid one and
+// are never read.
+struct Planes {
+    const float* p0;
+    const float* p1;
+    const float* p2;
+    const float* p3;
+    int jlo, nx;
+    __device__ __forceinline__ float operator()(int i, int j, int dp) const
     {
-        if (p == k) return sk[(j - jlo) * nx + i];
-        if (p == k + 1) return sk1[(j - jlo) * nx + i];
-        return __ldg(vol + ((long long)p * ny + j) * nx + i);
+        const float* b = dp == 0 ? p0 : (dp == 1 ? p1 : (dp == 2 ? p2 : p3));
+        return b[(j - jlo) * nx + i];
     }
 };
 
-template <typename Acc>
-__device__ __forceinline__ float3 gradient_acc(const Acc& acc, const Grid& g, int i, int j, int k)
+// edge_vertex() of iso_device.cuh through the planes: the vertex on the edge
+// from P0 = (i, j, plane kk = k + dp - 1) along `axis`, computed by the cube
+// with base (ci, cj, ck).  The gradients are evaluated in the frame
+// (a, b, c) = (axis, axis+1, axis+2), so lanes with different axes run the
+// same instructions; the two endpoints share the edge's own values.
+__device__ __forceinline__ void vertex_on_edge(const Planes& pl, const Grid& g, const GradScale& gs, float iso,
+                                               int axis, int i, int j, int dp, int kk, int ci, int cj, int ck,
+                                               float3& pos, float3& nrm)
 {
-    const float here = acc(i, j, k);
-    const float xm = i > 0 ? acc(i - 1, j, k) : 0.f, xp = i < g.nx - 1 ? acc(i + 1, j, k) : 0.f;
-    const float ym = j > 0 ? acc(i, j - 1, k) : 0.f, yp = j < g.ny - 1 ? acc(i, j + 1, k) : 0.f;
-    const float zm = k > 0 ? acc(i, j, k - 1) : 0.f, zp = k < g.nz - 1 ? acc(i, j, k + 1) : 0.f;
-    float3 r;
-    r.x = grad_component(xm, here, xp, i, g.nx, g.sp[0]);
-    r.y = grad_component(ym, here, yp, j, g.ny, g.sp[1]);
-    r.z = grad_component(zm, here, zp, k, g.nz, g.sp[2]);
-    return r;
-}
-
-// edge_vertex() of iso_device.cuh with values from an accessor.
-template <typename Acc>
-__device__ __forceinline__ void edge_vertex_acc(const Acc& acc, const Grid& g, float iso, int axis, int i, int j,
-                                                int k, int ci, int cj, int ck, float3& pos, float3& nrm)
-{
-    const int i1 = i + (axis == 0), j1 = j + (axis == 1), k1 = k + (axis == 2);
-    const float v0 = acc(i, j, k);
-    const float v1 = acc(i1, j1, k1);
+    const int ex = axis == 0, ey = axis == 1, ez = axis == 2;
+    const int bx = axis == 2, by = axis == 0, bz = axis == 1;  // b = axis+1
+    const int cx = axis == 1, cy = axis == 2, cz = axis == 0;  // c = axis+2
+    const int ab = axis == 2 ? 0 : axis + 1, ac = axis == 0 ? 2 : axis - 1;
+    const int i1 = i + ex, j1 = j + ey, dp1 = dp + ez, kk1 = kk + ez;
+    const int pa = axis == 0 ? i : (axis == 1 ? j : kk);
+    const int pb = axis == 0 ? j : (axis == 1 ? kk : i);
+    const int pc = axis == 0 ? kk : (axis == 1 ? i : j);
+    const int na = axis == 0 ? g.nx : (axis == 1 ? g.ny : g.nz);
+    const int nb = axis == 0 ? g.ny : (axis == 1 ? g.nz : g.nx);
+    const int nc = axis == 0 ? g.nz : (axis == 1 ? g.nx : g.ny);
+    const float v0 = pl(i, j, dp);
+    const float v1 = pl(i1, j1, dp1);
+    const float am = pa > 0 ? pl(i - ex, j - ey, dp - ez) : 0.f;
+    const float ap = pa + 1 < na - 1 ? pl(i1 + ex, j1 + ey, dp1 + ez) : 0.f;
+    const bool blo = pb > 0, bhi = pb < nb - 1, clo = pc > 0, chi = pc < nc - 1;
+    const float b0m = blo ? pl(i - bx, j - by, dp - bz) : 0.f;
+    const float b0p = bhi ? pl(i + bx, j + by, dp + bz) : 0.f;
+    const float c0m = clo ? pl(i - cx, j - cy, dp - cz) : 0.f;
+    const float c0p = chi ? pl(i + cx, j + cy, dp + cz) : 0.f;
+    const float b1m = blo ? pl(i1 - bx, j1 - by, dp1 - bz) : 0.f;
+    const float b1p = bhi ? pl(i1 + bx, j1 + by, dp1 + bz) : 0.f;
+    const float c1m = clo ? pl(i1 - cx, j1 - cy, dp1 - cz) : 0.f;
+    const float c1p = chi ? pl(i1 + cx, j1 + cy, dp1 + cz) : 0.f;
     const float w = fdiv(fsub(iso, v0), fsub(v1, v0));
     pos.x = lerp_ref(cube_coord(ci, i - ci, g.zp[0], g.sp[0]), cube_coord(ci, i1 - ci, g.zp[0], g.sp[0]), w);
     pos.y = lerp_ref(cube_coord(cj, j - cj, g.zp[1], g.sp[1]), cube_coord(cj, j1 - cj, g.zp[1], g.sp[1]), w);
-    pos.z = lerp_ref(cube_coord(ck, k - ck, g.zp[2], g.sp[2]), cube_coord(ck, k1 - ck, g.zp[2], g.sp[2]), w);
-    const float3 g0 = gradient_acc(acc, g, i, j, k);
-    const float3 g1 = gradient_acc(acc, g, i1, j1, k1);
-    nrm.x = lerp_ref(g0.x, g1.x, w);
-    nrm.y = lerp_ref(g0.y, g1.y, w);
-    nrm.z = lerp_ref(g0.z, g1.z, w);
+    pos.z = lerp_ref(cube_coord(ck, kk - ck, g.zp[2], g.sp[2]), cube_coord(ck, kk1 - ck, g.zp[2], g.sp[2]), w);
+    const float ga =
+        lerp_ref(grad_axis(am, v0, v1, pa, na, axis, gs), grad_axis(v0, v1, ap, pa + 1, na, axis, gs), w);
+    const float gb = lerp_ref(grad_axis(b0m, v0, b0p, pb, nb, ab, gs), grad_axis(b1m, v1, b1p, pb, nb, ab, gs), w);
+    const float gc = lerp_ref(grad_axis(c0m, v0, c0p, pc, nc, ac, gs), grad_axis(c1m, v1, c1p, pc, nc, ac, gs), w);
+    nrm.x = axis == 0 ? ga : (axis == 1 ? gc : gb);
+    nrm.y = axis == 1 ? ga : (axis == 2 ? gc : gb);
+    nrm.z = axis == 2 ? ga : (axis == 0 ? gc : gb);
 }
 
 __device__ __forceinline__ void store_vertex(float* __restrict__ points, float* __restrict__ normals,
@@ -104,20 +193,6 @@ __device__ __forceinline__ void store_vertex(float* __restrict__ points, float* 
     normals[3 * id + 2] = n.z;
 }
 
-// Largest lane w < W with pre(w) <= r, where pre is a per-lane non-decreasing
-// prefix with pre(0) == 0 (all 32 lanes must call).
-__device__ __forceinline__ int lane_search(uint32_t pre, uint32_t r, int W)
-{
-    int lo = 0;
-#pragma unroll
-    for (int step = 16; step > 0; step >>= 1) {
-        const int mid = lo + step;
-        const uint32_t v = __shfl_sync(0xffffffffu, pre, mid & 31);
-        if (mid < W && v <= r) lo = mid;
-    }
-    return lo;
-}
-
 // Inclusive warp scan.
 __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v, int lane)
 {
@@ -129,50 +204,39 @@ __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v, int lane)
     return v;
 }
 
-// The four bit words of the lane (rows A, B, C, D of the cell row) and their
-// i+1 neighbours, fetched from lane `src`.
-__device__ __forceinline__ RowWords words_from(const RowWords& mine, int src)
+// Flying Edges id of cube edge e of the cell at bit `bit` of word w, relative
+// to the row's first vertex, from the warp's mask table:
+//   e : 0  1  2  3  4  5  6  7  8  9  10 11
+//   mask xA yA xB yA xC yC xD yC zA zA zB zB    (index 0..7 below)
+//   +1  .  1  .  .  .  1  .  .  .  1  .  1      (edge at point i+1)
+__device__ __forceinline__ uint32_t fe_edge_rel(const uint2* mb, int W, int e, int w, int bit)
 {
-    RowWords r;
-    r.a = __shfl_sync(0xffffffffu, mine.a, src);
-    r.b = __shfl_sync(0xffffffffu, mine.b, src);
-    r.c = __shfl_sync(0xffffffffu, mine.c, src);
-    r.d = __shfl_sync(0xffffffffu, mine.d, src);
-    r.ash = __shfl_sync(0xffffffffu, mine.ash, src);
-    r.bsh = __shfl_sync(0xffffffffu, mine.bsh, src);
-    r.csh = __shfl_sync(0xffffffffu, mine.csh, src);
-    r.dsh = __shfl_sync(0xffffffffu, mine.dsh, src);
-    return r;
-}
-
-__device__ __forceinline__ CutMasks masks_from(const CutMasks& mine, int src)
-{
-    CutMasks m;
-    m.xA = __shfl_sync(0xffffffffu, mine.xA, src);
-    m.xB = __shfl_sync(0xffffffffu, mine.xB, src);
-    m.xC = __shfl_sync(0xffffffffu, mine.xC, src);
-    m.xD = __shfl_sync(0xffffffffu, mine.xD, src);
-    m.yA = __shfl_sync(0xffffffffu, mine.yA, src);
-    m.yC = __shfl_sync(0xffffffffu, mine.yC, src);
-    m.zA = __shfl_sync(0xffffffffu, mine.zA, src);
-    m.zB = __shfl_sync(0xffffffffu, mine.zB, src);
-    return m;
+    const int sel = (int)((0x776653524140ull >> (4 * e)) & 7u);
+    const int off = (0xA22 >> e) & 1;
+    const uint2 p = mb[sel * W + w];
+    return p.y + __popc(p.x & lowmask(bit + off));
 }
 
 template <int MODE, typename IndexT, bool BULK>
-__global__ void __launch_bounds__(kThreads) k_gen_warps(
-    const float* __restrict__ vol, const uint32_t* __restrict__ bits, Grid g, float iso, int KC, int nyb,
-    int slab_floats, const CaseTables* __restrict__ cases, const uint4* __restrict__ rowcnt, RowStarts rs,
-    unsigned long long* __restrict__ totals, long long capV, long long capT, float* __restrict__ points,
+__global__ void __launch_bounds__(kThreads, 2) k_gen_warps(
+    const float* __restrict__ vol, const uint32_t* __restrict__ bits, Grid g, GradScale gs, float iso, int KC,
+    int nyb, int slab_floats, int ws_bytes, const CaseTables* __restrict__ cases, const uint4* __restrict__ rowcnt,
+    RowStarts rs, unsigned long long* __restrict__ totals, long long capV, long long capT, float* __restrict__ points,
     float* __restrict__ normals, IndexT* __restrict__ tris, uint32_t* __restrict__ fe2mc, int reverse)
 {
     constexpr bool VOL = MODE != kGenTri;
     constexpr int NS = kGenSlots;
     extern __shared__ __align__(128) unsigned char s_raw[];
     __shared__ SharedCases s_cases;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int W = g.W;
     float* slots = reinterpret_cast<float*>(s_raw);
     uint64_t* full = reinterpret_cast<uint64_t*>(s_raw + (size_t)NS * slab_floats * 4);
     uint64_t* empty = full + NS;
+    unsigned char* ws = s_raw + (VOL ? gen_ring_bytes(slab_floats) : 0) + (size_t)warp * ws_bytes;
+    uint2* mb = reinterpret_cast<uint2*>(ws);
+    uint32_t* cell = reinterpret_cast<uint32_t*>(ws + (size_t)8 * W * 8);
+    unsigned char* list = ws + (size_t)8 * W * 8 + kGenCells * 4;
     stage_cases(s_cases, cases, MODE == kGenMC);  // includes __syncthreads
     if ((long long)totals[0] > capV || (long long)totals[1] > capT) return;  // caller grows buffers
 
@@ -181,8 +245,6 @@ __global__ void __launch_bounds__(kThreads) k_gen_warps(
     const int kc = reverse ? nkc - 1 - (int)(blockIdx.x / nyb) : (int)(blockIdx.x / nyb);
     const int j0 = jb * kGenRows;
     const int kb = kc * KC, ke = min(kb + KC, g.nz);
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int W = g.W;
     const int j = j0 + warp;
     const bool row_ok = j < g.ny;
     const GenSlab sl = gen_slab_rows(j0, g.ny);
@@ -224,10 +286,50 @@ __global__ void __launch_bounds__(kThreads) k_gen_warps(
     const bool in = lane < W, in1 = lane + 1 < W;
     const uint32_t evalid = validmask(lane, g.nx - 1);  // x-edges / cells: i <= nx-2
     const uint32_t pvalid = validmask(lane, g.nx);      // points: i <= nx-1
+    const bool hasY = j < g.ny - 1;
+
+    // Bit words of rows (j, p) and (j+1, p).
+    auto load_words = [&](int p, uint32_t& wa, uint32_t& wb) {
+        const bool okp = row_ok && p < g.nz;
+        const long long r = (long long)p * g.ny + j;
+        wa = (in && okp) ? __ldg(&bits[r * W + lane]) : 0u;
+        wb = (in && okp && hasY) ? __ldg(&bits[(r + 1) * W + lane]) : 0u;
+    };
+    // Row starts of step p, one per lane: lanes 0..3 the first vertex of rows
+    // A = (j,p), B = (j+1,p), C = (j,p+1), D = (j+1,p+1); lane 4 the first
+    // triangle (FE, TRI) or MC vertex (MC) of cell row A; lane 5 the x + y
+    // cuts of row B.
+    auto load_starts = [&](int p) -> unsigned long long {
+        const int dk = (lane >> 1) & 1, dj = lane & 1;
+        const bool hasZp = p + 1 < g.nz;
+        bool ok = row_ok && lane < 6;
+        if (lane < 4) ok = ok && (dj == 0 || hasY) && (dk == 0 || hasZp);
+        if (lane == 5) ok = ok && hasY;
+        if (!ok) return 0ull;
+        const long long rA = (long long)p * g.ny + j;
+        if (lane == 5) {
+            const uint2 c = __ldg(reinterpret_cast<const uint2*>(&rowcnt[rA + 1]));
+            return (unsigned long long)c.x + c.y;
+        }
+        const long long r = lane < 4 ? rA + (long long)dk * g.ny + dj : rA;
+        return rs.get(r, lane < 4 ? 0 : (MODE == kGenMC ? 2 : 1));
+    };
+
+    uint32_t wA = 0, wB = 0, wC = 0, wD = 0;
+    load_words(kb, wA, wB);
+    load_words(kb + 1, wC, wD);
+    unsigned long long st = load_starts(kb);
 
     for (int k = kb; k < ke && alive; ++k) {
         if (VOL && warp == 0) alive = issue_upto(k + NS - 1) && alive;
         const bool hasZ = k + 1 < g.nz;
+        // the next step's words and starts, in flight while this step runs
+        uint32_t nC = 0, nD = 0;
+        unsigned long long nst = 0;
+        if (k + 1 < ke) {
+            load_words(k + 2, nC, nD);
+            nst = load_starts(k + 1);
+        }
         if (VOL) {
             bool ok = wait_plane(k);
             if (hasZ) ok = ok && wait_plane(k + 1);
@@ -238,25 +340,12 @@ __global__ void __launch_bounds__(kThreads) k_gen_warps(
             break;
         }
         if (row_ok) {
-            const bool hasY = j < g.ny - 1, cell = hasY && hasZ;
-            // ---- bit words of rows A = (j,k), B = (j+1,k), C = (j,k+1), D = (j+1,k+1)
-            const long long rA = (long long)k * g.ny + j;
+            const bool cellrow = hasY && hasZ;
             RowWords rw;
-            rw.a = in ? __ldg(&bits[rA * W + lane]) : 0u;
-            rw.b = (in && hasY) ? __ldg(&bits[(rA + 1) * W + lane]) : 0u;
-            rw.c = (in && hasZ) ? __ldg(&bits[(rA + g.ny) * W + lane]) : 0u;
-            rw.d = (in && cell) ? __ldg(&bits[(rA + g.ny + 1) * W + lane]) : 0u;
-            // row starts: lanes 0..5 fetch, then broadcast
-            unsigned long long st = 0;
-            if (lane == 0) st = rs.get(k, j, 0);
-            else if (lane == 1 && hasY) st = rs.get(k, j + 1, 0);
-            else if (lane == 2 && hasZ) st = rs.get(k + 1, j, 0);
-            else if (lane == 3 && cell) st = rs.get(k + 1, j + 1, 0);
-            else if (lane == 4) st = rs.get(k, j, MODE == kGenMC ? 2 : 1);
-            else if (lane == 5 && hasY) {
-                const uint4 cb = __ldg(&rowcnt[rA + 1]);
-                st = (unsigned long long)cb.x + cb.y;
-            }
+            rw.a = wA;
+            rw.b = wB;
+            rw.c = hasZ ? wC : 0u;
+            rw.d = cellrow ? wD : 0u;
             const uint32_t an = __shfl_down_sync(0xffffffffu, rw.a, 1);
             const uint32_t bn = __shfl_down_sync(0xffffffffu, rw.b, 1);
             const uint32_t cn = __shfl_down_sync(0xffffffffu, rw.c, 1);
@@ -277,168 +366,157 @@ __global__ void __launch_bounds__(kThreads) k_gen_warps(
             const uint32_t t0 = __shfl_sync(0xffffffffu, i0, 31), t2 = __shfl_sync(0xffffffffu, i2, 31);
             const uint32_t t1 = __shfl_sync(0xffffffffu, i1, 31), t3 = __shfl_sync(0xffffffffu, i3, 31);
             const unsigned long long xsA = __shfl_sync(0xffffffffu, st, 0);
-            const unsigned long long xsB = __shfl_sync(0xffffffffu, st, 1);
-            const unsigned long long xsC = __shfl_sync(0xffffffffu, st, 2);
-            const unsigned long long xsD = __shfl_sync(0xffffffffu, st, 3);
+            const uint32_t dB = (uint32_t)(__shfl_sync(0xffffffffu, st, 1) - xsA);
+            const uint32_t dC = (uint32_t)(__shfl_sync(0xffffffffu, st, 2) - xsA);
+            const uint32_t dD = (uint32_t)(__shfl_sync(0xffffffffu, st, 3) - xsA);
             const unsigned long long ts = __shfl_sync(0xffffffffu, st, 4);
-            const unsigned long long cntB = __shfl_sync(0xffffffffu, st, 5);
+            const uint32_t cntB = (uint32_t)__shfl_sync(0xffffffffu, st, 5);
             const uint32_t nxA = t0 & 0xffffu, nyA = t2 & 0xffffu, nzA = t3 & 0xffffu, nxC = t1 & 0xffffu;
-            CutBases base;  // this lane's word
-            base.xA = xsA + (e0 & 0xffffu);
-            base.xB = xsB + (e0 >> 16);
-            base.xC = xsC + (e1 & 0xffffu);
-            base.xD = xsD + (e1 >> 16);
-            base.yA = xsA + nxA + (e2 & 0xffffu);
-            base.yC = xsC + nxC + (e2 >> 16);
-            base.zA = xsA + nxA + nyA + (e3 & 0xffffu);
-            base.zB = xsB + cntB + (e3 >> 16);
+            if (in) {  // first ids of the word's cut edges, relative to xsA
+                mb[0 * W + lane] = make_uint2(m.xA, e0 & 0xffffu);
+                mb[1 * W + lane] = make_uint2(m.xB, dB + (e0 >> 16));
+                mb[2 * W + lane] = make_uint2(m.xC, dC + (e1 & 0xffffu));
+                mb[3 * W + lane] = make_uint2(m.xD, dD + (e1 >> 16));
+                mb[4 * W + lane] = make_uint2(m.yA, nxA + (e2 & 0xffffu));
+                mb[5 * W + lane] = make_uint2(m.yC, dC + nxC + (e2 >> 16));
+                mb[6 * W + lane] = make_uint2(m.zA, nxA + nyA + (e3 & 0xffffu));
+                mb[7 * W + lane] = make_uint2(m.zB, dB + cntB + (e3 >> 16));
+            }
+            __syncwarp();
+            Planes pl{};
+            if (VOL) {
+                const float* sk = slots + (size_t)(k % NS) * slab_floats;
+                pl.p1 = sk;
+                pl.p2 = hasZ ? slots + (size_t)((k + 1) % NS) * slab_floats : sk;
+                pl.p0 = k > 0 ? vol + ((long long)(k - 1) * g.ny + sl.jlo) * g.nx : sk;
+                pl.p3 = k + 2 < g.nz ? vol + ((long long)(k + 2) * g.ny + sl.jlo) * g.nx : pl.p2;
+                pl.jlo = sl.jlo;
+                pl.nx = g.nx;
+            }
 
-            if (MODE == kGenFE || MODE == kGenMC) {
-                const float* sk = slots + (size_t)(k % NS) * slab_floats;
-                const float* sk1 = slots + (size_t)((k + 1) % NS) * slab_floats;
-                const WarpSlab acc{vol, sk, sk1, k, sl.jlo, g.nx, g.ny};
-                if (MODE == kGenFE) {
-                    // ---- vertices of grid row (j, k): x, y then z sections
-                    const uint32_t nv = nxA + nyA + nzA;
-                    const int ck = min(k, g.nz - 2), cj = min(j, g.ny - 2);
-                    for (uint32_t v0 = 0; v0 < nv; v0 += 32) {
-                        const uint32_t v = v0 + lane;
-                        const int axis = v < nxA ? 0 : (v < nxA + nyA ? 1 : 2);
-                        const uint32_t r = v - (axis == 0 ? 0u : (axis == 1 ? nxA : nxA + nyA));
-                        const uint32_t ex = e0 & 0xffffu, ey = e2 & 0xffffu, ez = e3 & 0xffffu;
-                        // word holding rank r of the axis' cut mask
-                        int lo = 0;
-#pragma unroll
-                        for (int step = 16; step > 0; step >>= 1) {
-                            const int mid = lo + step;
-                            const uint32_t px = __shfl_sync(0xffffffffu, ex, mid & 31);
-                            const uint32_t py = __shfl_sync(0xffffffffu, ey, mid & 31);
-                            const uint32_t pz = __shfl_sync(0xffffffffu, ez, mid & 31);
-                            const uint32_t pv = axis == 0 ? px : (axis == 1 ? py : pz);
-                            if (mid < W && pv <= r) lo = mid;
-                        }
-                        const uint32_t mxw = __shfl_sync(0xffffffffu, m.xA, lo);
-                        const uint32_t myw = __shfl_sync(0xffffffffu, m.yA, lo);
-                        const uint32_t mzw = __shfl_sync(0xffffffffu, m.zA, lo);
-                        const uint32_t pxw = __shfl_sync(0xffffffffu, ex, lo);
-                        const uint32_t pyw = __shfl_sync(0xffffffffu, ey, lo);
-                        const uint32_t pzw = __shfl_sync(0xffffffffu, ez, lo);
-                        if (v < nv) {
-                            const uint32_t mw = axis == 0 ? mxw : (axis == 1 ? myw : mzw);
-                            const uint32_t pw = axis == 0 ? pxw : (axis == 1 ? pyw : pzw);
-                            const int bit = (int)__fns(mw, 0, (int)(r - pw) + 1);
-                            const int i = 32 * lo + bit;
-                            float3 p, n;
-                            edge_vertex_acc(acc, g, iso, axis, i, j, k, axis == 0 ? i : min(i, g.nx - 2),
-                                            axis == 1 ? j : cj, axis == 2 ? k : ck, p, n);
-                            store_vertex(points, normals, xsA + v, p, n);
-                        }
-                    }
-                }
-            }
-            if (cell && (MODE == kGenFE || MODE == kGenTri)) {
-                // ---- triangles of cell row (j, k): one active cell per lane
-                const uint32_t act = in ? active_cells(rw, evalid) : 0u;
-                const uint32_t na = __popc(act);
-                const uint32_t ia = warp_incl_scan(na, lane);
-                const uint32_t ea = ia - na, tot = __shfl_sync(0xffffffffu, ia, 31);
-                unsigned long long tcur = ts;
-                for (uint32_t c0 = 0; c0 < tot; c0 += 32) {
-                    const uint32_t cidx = c0 + lane;
-                    const int w = lane_search(ea, cidx, W);
-                    const RowWords ww = words_from(rw, w);
-                    const uint32_t aw = __shfl_sync(0xffffffffu, act, w);
-                    const uint32_t eaw = __shfl_sync(0xffffffffu, ea, w);
-                    const CutMasks mw = masks_from(m, w);
-                    CutBases bw;
-                    bw.xA = __shfl_sync(0xffffffffu, base.xA, w);
-                    bw.xB = __shfl_sync(0xffffffffu, base.xB, w);
-                    bw.xC = __shfl_sync(0xffffffffu, base.xC, w);
-                    bw.xD = __shfl_sync(0xffffffffu, base.xD, w);
-                    bw.yA = __shfl_sync(0xffffffffu, base.yA, w);
-                    bw.yC = __shfl_sync(0xffffffffu, base.yC, w);
-                    bw.zA = __shfl_sync(0xffffffffu, base.zA, w);
-                    bw.zB = __shfl_sync(0xffffffffu, base.zB, w);
-                    const bool live = cidx < tot;
-                    const int bit = live ? (int)__fns(aw, 0, (int)(cidx - eaw) + 1) : 0;
-                    const uint64_t tl = s_cases.tris[live ? cube_case(ww, bit) : 0];
-                    const uint32_t nt = live ? (uint32_t)iso_case_ntris(tl) : 0u;
-                    const uint32_t it = warp_incl_scan(nt, lane);
-                    const unsigned long long t = tcur + (it - nt);
-                    for (int q = 0; q < 3 * (int)nt; ++q) {
-                        const unsigned long long id = fe_edge_id(mw, bw, iso_case_edge(tl, q), bit);
-                        tris[3 * t + q] = MODE == kGenTri ? (IndexT)__ldg(fe2mc + id) : (IndexT)id;
-                    }
-                    tcur += __shfl_sync(0xffffffffu, it, 31);
-                }
-            }
-            if (MODE == kGenMC && cell) {
-                // ---- MC vertices owned by cell row (j, k), owner order
-                const float* sk = slots + (size_t)(k % NS) * slab_floats;
-                const float* sk1 = slots + (size_t)((k + 1) % NS) * slab_floats;
-                const WarpSlab acc{vol, sk, sk1, k, sl.jlo, g.nx, g.ny};
-                const uint32_t act = in ? active_cells(rw, evalid) : 0u;
-                uint32_t no = 0;
-                for (uint32_t a = act; a; a &= a - 1) {
-                    const int bit = __ffs(a) - 1;
-                    no += __popc(mc_owned_edges(32 * lane + bit == 0, j == 0, k == 0) & s_cases.cut[cube_case(rw, bit)]);
-                }
-                const uint32_t io = warp_incl_scan(no, lane);
-                const uint32_t eo = io - no, tot = __shfl_sync(0xffffffffu, io, 31);
-                for (uint32_t v0 = 0; v0 < tot; v0 += 32) {
+            if (MODE == kGenFE) {
+                // ---- vertices of grid row (j, k): x, y then z sections
+                const uint32_t nv = nxA + nyA + nzA;
+                const int ck = min(k, g.nz - 2), cj = min(j, g.ny - 2);
+                // word prefixes of the x, y and z sections in one word: 10 + 11 + 11 bits
+                const uint32_t P = (e0 & 0x3ffu) | ((e2 & 0x7ffu) << 10) | ((e3 & 0x7ffu) << 21);
+                for (uint32_t v0 = 0; v0 < nv; v0 += 32) {
                     const uint32_t v = v0 + lane;
-                    const int w = lane_search(eo, v, W);
-                    const RowWords ww = words_from(rw, w);
-                    const uint32_t aw = __shfl_sync(0xffffffffu, act, w);
-                    const uint32_t eow = __shfl_sync(0xffffffffu, eo, w);
-                    const CutMasks mw = masks_from(m, w);
-                    CutBases bw;
-                    bw.xA = __shfl_sync(0xffffffffu, base.xA, w);
-                    bw.xB = __shfl_sync(0xffffffffu, base.xB, w);
-                    bw.xC = __shfl_sync(0xffffffffu, base.xC, w);
-                    bw.xD = __shfl_sync(0xffffffffu, base.xD, w);
-                    bw.yA = __shfl_sync(0xffffffffu, base.yA, w);
-                    bw.yC = __shfl_sync(0xffffffffu, base.yC, w);
-                    bw.zA = __shfl_sync(0xffffffffu, base.zA, w);
-                    bw.zB = __shfl_sync(0xffffffffu, base.zB, w);
-                    if (v < tot) {
-                        uint32_t rank = v - eow;
-                        int bit = 0, c = 0;
-                        uint32_t own = 0;
-                        for (uint32_t a = aw; a; a &= a - 1) {  // the cell holding this vertex
-                            bit = __ffs(a) - 1;
-                            c = cube_case(ww, bit);
-                            own = mc_owned_edges(32 * w + bit == 0, j == 0, k == 0) & s_cases.cut[c];
-                            const uint32_t n = __popc(own);
-                            if (rank < n) break;
-                            rank -= n;
-                        }
-                        const uint64_t ord = s_cases.order[c];
-                        int e12 = 0;
-                        for (int q = 0; q < iso_case_ntris(ord); ++q) {  // rank-th owned edge
-                            const int ed = iso_case_edge(ord, q);
-                            if ((own >> ed) & 1u) {
-                                if (rank == 0) {
-                                    e12 = ed;
-                                    break;
+                    const int axis = v < nxA ? 0 : (v < nxA + nyA ? 1 : 2);
+                    const uint32_t r = v - (axis == 0 ? 0u : (axis == 1 ? nxA : nxA + nyA));
+                    const int sh = axis == 0 ? 0 : (axis == 1 ? 10 : 21);
+                    const uint32_t fm = axis == 0 ? 0x3ffu : 0x7ffu;
+                    int lo = 0;
+#pragma unroll
+                    for (int step = 16; step > 0; step >>= 1) {
+                        const int mid = lo + step;
+                        const uint32_t pv = (__shfl_sync(0xffffffffu, P, mid & 31) >> sh) & fm;
+                        if (mid < W && pv <= r) lo = mid;
+                    }
+                    if (v < nv) {
+                        const uint2 e = mb[(axis == 0 ? 0 : (axis == 1 ? 4 : 6)) * W + lo];
+                        const int bit = (int)__fns(e.x, 0, (int)(v - e.y) + 1);
+                        const int i = 32 * lo + bit;
+                        float3 p, n;
+                        vertex_on_edge(pl, g, gs, iso, axis, i, j, 1, k, axis == 0 ? i : min(i, g.nx - 2),
+                                       axis == 1 ? j : cj, axis == 2 ? k : ck, p, n);
+                        store_vertex(points, normals, xsA + v, p, n);
+                    }
+                }
+            }
+            if (cellrow) {
+                // ---- active cells of cell row (j, k), compacted 32 at a time
+                uint32_t rem = in ? active_cells(rw, evalid) : 0u;
+                const uint32_t na = __popc(rem);
+                const uint32_t ia = warp_incl_scan(na, lane);
+                uint32_t rank = ia - na;
+                const uint32_t tot = __shfl_sync(0xffffffffu, ia, 31);
+                unsigned long long tcur = ts;  // FE / TRI: next triangle; MC: next vertex
+                for (uint32_t c0 = 0; c0 < tot; c0 += kGenCells) {
+                    while (rem != 0u && rank < c0 + kGenCells) {
+                        const int bit = __ffs(rem) - 1;
+                        cell[rank - c0] = (uint32_t)(32 * lane + bit) | ((uint32_t)cube_case(rw, bit) << 16);
+                        rem &= rem - 1u;
+                        ++rank;
+                    }
+                    __syncwarp();
+                    const uint32_t nc = min(tot - c0, (uint32_t)kGenCells);
+                    const bool live = (uint32_t)lane < nc;
+                    const uint32_t rec = live ? cell[lane] : 0u;
+                    const int cs = (int)(rec >> 16);
+                    if (MODE == kGenFE || MODE == kGenTri) {
+                        const uint32_t nt = live ? (uint32_t)iso_case_ntris(s_cases.tris[cs]) : 0u;
+                        const uint32_t it = warp_incl_scan(nt, lane);
+                        const uint32_t ntb = __shfl_sync(0xffffffffu, it, 31);
+                        for (uint32_t q = 0; q < nt; ++q) list[it - nt + q] = (unsigned char)(lane | (q << 5));
+                        __syncwarp();
+                        for (uint32_t tb = 0; tb < ntb; tb += 32) {
+                            const uint32_t t = tb + lane;
+                            if (t < ntb) {
+                                const uint32_t tr = list[t];
+                                const uint32_t cr = cell[tr & 31u];
+                                const int q = (int)(tr >> 5);
+                                const int ci = (int)(cr & 0xffffu);
+                                const uint64_t tl = s_cases.tris[cr >> 16];
+                                const int w = ci >> 5, bit = ci & 31;
+                                IndexT* o = tris + 3 * (tcur + t);
+#pragma unroll
+                                for (int c = 0; c < 3; ++c) {
+                                    const unsigned long long id =
+                                        xsA + fe_edge_rel(mb, W, iso_case_edge(tl, 3 * q + c), w, bit);
+                                    o[c] = MODE == kGenTri ? (IndexT)__ldg(fe2mc + id) : (IndexT)id;
                                 }
-                                --rank;
                             }
                         }
-                        int dx, dy, dz, axis;
-                        cube_edge_geometry(e12, dx, dy, dz, axis);
-                        const int i = 32 * w + bit;
-                        float3 p, n;
-                        edge_vertex_acc(acc, g, iso, axis, i + dx, j + dy, k + dz, i, j, k, p, n);
-                        const unsigned long long id = ts + v;
-                        store_vertex(points, normals, id, p, n);
-                        fe2mc[fe_edge_id(mw, bw, e12, bit)] = (uint32_t)id;
+                        tcur += ntb;
+                    } else {
+                        // ---- MC vertices owned by the batch's cells: cell order, then order of
+                        // first appearance in the cell's triangle list
+                        const int ci = (int)(rec & 0xffffu);
+                        const uint32_t own =
+                            live ? (mc_owned_edges(ci == 0, j == 0, k == 0) & s_cases.cut[cs]) : 0u;
+                        const uint32_t no = __popc(own);
+                        const uint32_t io = warp_incl_scan(no, lane);
+                        const uint32_t nob = __shfl_sync(0xffffffffu, io, 31);
+                        uint16_t* vl = reinterpret_cast<uint16_t*>(list);
+                        if (own) {
+                            const uint64_t ord = s_cases.order[cs];
+                            uint32_t o = io - no;
+                            for (int q = 0; q < iso_case_ntris(ord); ++q) {
+                                const int ed = iso_case_edge(ord, q);
+                                if ((own >> ed) & 1u) vl[o++] = (uint16_t)(lane | (ed << 5));
+                            }
+                        }
+                        __syncwarp();
+                        for (uint32_t vb = 0; vb < nob; vb += 32) {
+                            const uint32_t v = vb + lane;
+                            if (v < nob) {
+                                const uint32_t vr = vl[v];
+                                const uint32_t cr = cell[vr & 31u];
+                                const int e12 = (int)(vr >> 5);
+                                const int i = (int)(cr & 0xffffu);
+                                int dx, dy, dz, axis;
+                                cube_edge_geometry(e12, dx, dy, dz, axis);
+                                float3 p, n;
+                                vertex_on_edge(pl, g, gs, iso, axis, i + dx, j + dy, 1 + dz, k + dz, i, j, k, p, n);
+                                const unsigned long long id = tcur + v;
+                                store_vertex(points, normals, id, p, n);
+                                fe2mc[xsA + fe_edge_rel(mb, W, e12, i >> 5, i & 31)] = (uint32_t)id;
+                            }
+                        }
+                        tcur += nob;
                     }
+                    __syncwarp();  // the next batch overwrites the lists
                 }
             }
         }
         __syncwarp();
         if (VOL && lane == 0) mbar_arrive(&empty[k % NS]);  // this warp is done with plane k
+        wA = wC;
+        wB = wD;
+        wC = nC;
+        wD = nD;
+        st = nst;
     }
     if (!alive && tid == 0) atomicOr(&totals[3], kStatusTimeout);
     if (VOL && warp == 0) {  // copies still in flight must land before the CTA exits
@@ -454,12 +532,15 @@ void launch_gen_warps_impl(const float* vol, const Grid& g, float iso, const Cas
                            float* normals, IndexT* tris, int reverse, cudaStream_t s)
 {
     const RowStarts rs = row_starts(g, cp, b);
-    const bool bulk = (g.nx % 4 == 0) && ((reinterpret_cast<uintptr_t>(vol) & 15) == 0);
+    const bool bulk = MODE != kGenTri && (g.nx % 4 == 0) && ((reinterpret_cast<uintptr_t>(vol) & 15) == 0);
     const unsigned blocks = (unsigned)(p.nyb * p.nkc);
+    const int ws_bytes = (int)gen_warp_scratch_bytes(g.W, MODE);
+    const int slab = MODE == kGenTri ? 0 : p.slab_floats;
+    const size_t smem = (MODE == kGenTri ? 0 : gen_ring_bytes(slab)) + (size_t)kGenRows * ws_bytes;
     auto kern = bulk ? k_gen_warps<MODE, IndexT, true> : k_gen_warps<MODE, IndexT, false>;
-    allow_smem(kern, p.smem);
-    kern<<<blocks, kThreads, p.smem, s>>>(vol, b.bits, g, iso, p.KC, p.nyb, p.slab_floats, cases, b.rowcnt, rs,
-                                          b.totals, capV, capT, points, normals, tris, b.fe2mc, reverse);
+    allow_smem(kern, smem);
+    kern<<<blocks, kThreads, smem, s>>>(vol, b.bits, g, make_grad_scale(g), iso, p.KC, p.nyb, slab, ws_bytes, cases,
+                                        b.rowcnt, rs, b.totals, capV, capT, points, normals, tris, b.fe2mc, reverse);
 }
 
 }  // namespace iso

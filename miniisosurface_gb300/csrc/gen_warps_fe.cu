@@ -4,9 +4,10 @@
 
 namespace iso {
 
-// Shared memory of the slab ring; above kGenTwoPerSm only one CTA fits per SM,
-// above kGenMaxSmem (or rows wider than 32 words) the row-wise kernels are used.
-constexpr size_t kGenTwoPerSm = 104 * 1024;
+// Dynamic shared memory (slab ring + warp scratch); above kGenTwoPerSm only
+// one CTA fits per SM, above kGenMaxSmem (or rows wider than 32 words) the
+// row-wise kernels are used.
+constexpr size_t kGenTwoPerSm = 108 * 1024;
 constexpr size_t kGenMaxSmem = 200 * 1024;
 
 GenPlan gen_plan(const Grid& g, int nsm)
@@ -15,8 +16,10 @@ GenPlan gen_plan(const Grid& g, int nsm)
     p.J = kGenRows;
     p.nyb = (g.ny + p.J - 1) / p.J;
     p.slab_floats = (int)((((size_t)(p.J + 3) * g.nx) + 31) & ~(size_t)31);
-    p.smem = (size_t)kGenSlots * p.slab_floats * 4 + 2 * kGenSlots * 8;
-    p.fits = g.W <= 32 && p.smem <= kGenMaxSmem;
+    p.smem = gen_ring_bytes(p.slab_floats) + (size_t)kGenRows * gen_warp_scratch_bytes(g.W, kGenMC);
+    // relative vertex ids of a cell row (up to two planes of vertices) in 32 bits
+    const bool rel32 = 6.0 * g.nx * g.ny < 4294967295.0;
+    p.fits = g.W <= 32 && p.smem <= kGenMaxSmem && rel32;
     const long long resident = (long long)nsm * (p.smem <= kGenTwoPerSm ? 2 : 1);
     int nkc = (int)((4 * resident + p.nyb - 1) / p.nyb);
     if (nkc < 1) nkc = 1;
