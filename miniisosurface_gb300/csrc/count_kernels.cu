@@ -135,16 +135,13 @@ __device__ __forceinline__ void finish_row(RowCounts& rc, int lane, long long r,
                                            uint4* __restrict__ rowcnt, uint2* __restrict__ trims,
                                            uint32_t* __restrict__ mccnt)
 {
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) {
-        rc.xc += __shfl_xor_sync(0xffffffffu, rc.xc, d);
-        rc.yc += __shfl_xor_sync(0xffffffffu, rc.yc, d);
-        rc.zc += __shfl_xor_sync(0xffffffffu, rc.zc, d);
-        rc.tc += __shfl_xor_sync(0xffffffffu, rc.tc, d);
-        if (MC) rc.mc += __shfl_xor_sync(0xffffffffu, rc.mc, d);
-        rc.first = min(rc.first, __shfl_xor_sync(0xffffffffu, rc.first, d));
-        rc.last = max(rc.last, __shfl_xor_sync(0xffffffffu, rc.last, d));
-    }
+    rc.xc = __reduce_add_sync(0xffffffffu, rc.xc);
+    rc.yc = __reduce_add_sync(0xffffffffu, rc.yc);
+    rc.zc = __reduce_add_sync(0xffffffffu, rc.zc);
+    rc.tc = __reduce_add_sync(0xffffffffu, rc.tc);
+    if (MC) rc.mc = __reduce_add_sync(0xffffffffu, rc.mc);
+    rc.first = __reduce_min_sync(0xffffffffu, rc.first);
+    rc.last = __reduce_max_sync(0xffffffffu, rc.last);
     if (lane == 0) {
         rowcnt[r] = make_uint4(rc.xc, rc.yc, rc.zc, rc.tc);
         trims[r] = make_uint2(rc.first == 0xffffffffu ? (uint32_t)g.nx : rc.first, rc.last);
@@ -232,6 +229,132 @@ __global__ void __launch_bounds__(kThreads) k_count_warps(const float* __restric
             A[q] = Cw[q];
             B[q] = Dw[q];
         }
+    }
+}
+
+// Rows of up to 16 words (nx <= 512): two rows per warp, one per half-warp
+// (lanes 16h .. 16h+15 hold words 0..15 of row j0 + 2*warp + h), so no lane
+// idles on words past the row.  The same counts as k_count_warps.
+constexpr int kPairRows = 2 * kCountRows;  // grid rows per CTA
+
+template <int U>
+__device__ __forceinline__ void load_half_vec4(const float* __restrict__ row, int nq, int l16, bool ok, RowVals<U>& r)
+{
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const int q = l16 + 16 * u;
+        r.v[u] = (ok && q < nq) ? __ldg(reinterpret_cast<const float4*>(row) + q) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+}
+
+// Bit words of the half-warp's row: word w in lane 16h + w.
+template <int U>
+__device__ __forceinline__ uint32_t words_half(const RowVals<U>& r, int nq, int lane, float iso)
+{
+    const int l16 = lane & 15;
+    uint32_t out = 0u;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const int f = l16 + 16 * u;
+        const float4 v = r.v[u];
+        const uint32_t nib = f < nq ? ((uint32_t)(v.x >= iso) | ((uint32_t)(v.y >= iso) << 1) |
+                                       ((uint32_t)(v.z >= iso) << 2) | ((uint32_t)(v.w >= iso) << 3))
+                                    : 0u;
+        uint32_t word = nib << (4 * (lane & 7));
+        word |= __shfl_xor_sync(0xffffffffu, word, 1);
+        word |= __shfl_xor_sync(0xffffffffu, word, 2);
+        word |= __shfl_xor_sync(0xffffffffu, word, 4);
+        // lanes 16h + 8g .. +7 hold word 2u + g of row h; lane 16h + w wants word w
+        const uint32_t x = __shfl_sync(0xffffffffu, word, (lane & 16) | ((lane & 1) << 3));
+        if (u == (l16 >> 1)) out = x;
+    }
+    return out;
+}
+
+template <bool MC, int U>
+__global__ void __launch_bounds__(kThreads, 2) k_count_pairs(const float* __restrict__ vol, Grid g, float iso, int KC,
+                                                          int nyb, const CaseTables* __restrict__ cases,
+                                                          uint4* __restrict__ rowcnt, uint2* __restrict__ trims,
+                                                          uint32_t* __restrict__ mccnt, uint32_t* __restrict__ bits_out)
+{
+    __shared__ uint8_t s_ntris[256];
+    __shared__ uint16_t s_cut[256];
+    for (int c = threadIdx.x; c < 256; c += blockDim.x) {
+        s_ntris[c] = (uint8_t)iso_case_ntris(cases->tris[c]);
+        s_cut[c] = cases->cut[c];
+    }
+    __syncthreads();
+    const int jb = blockIdx.x % nyb, kc = blockIdx.x / nyb;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, h = lane >> 4, l16 = lane & 15;
+    const int jw = jb * kPairRows + 2 * warp;
+    if (jw >= g.ny) return;  // both halves past the grid
+    const int j = jw + h;
+    const bool row_ok = j < g.ny;
+    const int jr = row_ok ? j : jw;  // a valid row address for a half without a row
+    const int kb = kc * KC, ke = min(kb + KC, g.nz);
+    const bool hasY = row_ok && j < g.ny - 1;
+    const int jy = hasY ? j + 1 : jr;
+    const int nq = g.nx >> 2;
+    auto rowptr = [&](int k, int jj) { return vol + ((long long)k * g.ny + jj) * g.nx; };
+
+    uint32_t A, B, Cw, Dw;
+    RowVals<U> pc, pd;
+    {
+        RowVals<U> ra, rbv;
+        load_half_vec4<U>(rowptr(kb, jr), nq, l16, row_ok, ra);
+        load_half_vec4<U>(rowptr(kb, jy), nq, l16, hasY, rbv);
+        if (kb + 1 < g.nz) {
+            load_half_vec4<U>(rowptr(kb + 1, jr), nq, l16, row_ok, pc);
+            load_half_vec4<U>(rowptr(kb + 1, jy), nq, l16, hasY, pd);
+        }
+        A = words_half<U>(ra, nq, lane, iso);
+        B = words_half<U>(rbv, nq, lane, iso);
+    }
+    for (int k = kb; k < ke; ++k) {
+        const bool hasZ = k + 1 < g.nz;
+        Cw = words_half<U>(pc, nq, lane, iso);
+        Dw = words_half<U>(pd, nq, lane, iso);
+        if (k + 2 < g.nz && k + 1 < ke) {
+            load_half_vec4<U>(rowptr(k + 2, jr), nq, l16, row_ok, pc);
+            load_half_vec4<U>(rowptr(k + 2, jy), nq, l16, hasY, pd);
+        }
+        if (!hasZ) Cw = Dw = 0u;
+        RowCounts rc;
+        RowWords rw;
+        rw.a = A;
+        rw.b = B;
+        rw.c = Cw;
+        rw.d = Dw;
+        const uint32_t an = __shfl_down_sync(0xffffffffu, rw.a, 1, 16), bn = __shfl_down_sync(0xffffffffu, rw.b, 1, 16);
+        const uint32_t cn = __shfl_down_sync(0xffffffffu, rw.c, 1, 16), dn = __shfl_down_sync(0xffffffffu, rw.d, 1, 16);
+        const bool nxt = l16 < 15;
+        rw.ash = (rw.a >> 1) | ((nxt ? an : 0u) << 31);
+        rw.bsh = (rw.b >> 1) | ((nxt ? bn : 0u) << 31);
+        rw.csh = (rw.c >> 1) | ((nxt ? cn : 0u) << 31);
+        rw.dsh = (rw.d >> 1) | ((nxt ? dn : 0u) << 31);
+        if (row_ok) count_word<MC>(rw, l16, g, j, k, hasY, hasZ, s_ntris, s_cut, rc);
+        const long long r = (long long)k * g.ny + j;
+        if (row_ok && l16 < g.W) bits_out[r * g.W + l16] = rw.a;
+        // both rows' totals at once: row h in bits 16h .. 16h+15 (each below 2^16)
+        const int sh = 16 * h;
+        const uint32_t sx = __reduce_add_sync(0xffffffffu, rc.xc << sh);
+        const uint32_t sy = __reduce_add_sync(0xffffffffu, rc.yc << sh);
+        const uint32_t sz = __reduce_add_sync(0xffffffffu, rc.zc << sh);
+        const uint32_t st = __reduce_add_sync(0xffffffffu, rc.tc << sh);
+        const uint32_t sm = MC ? __reduce_add_sync(0xffffffffu, rc.mc << sh) : 0u;
+        const uint32_t f0 = __reduce_min_sync(0xffffffffu, h ? 0xffffffffu : rc.first);
+        const uint32_t f1 = __reduce_min_sync(0xffffffffu, h ? rc.first : 0xffffffffu);
+        const uint32_t x0 = __reduce_max_sync(0xffffffffu, h ? 0u : rc.last);
+        const uint32_t x1 = __reduce_max_sync(0xffffffffu, h ? rc.last : 0u);
+        if (row_ok && l16 == 0) {
+            const uint32_t first = h ? f1 : f0, last = h ? x1 : x0;
+            rowcnt[r] = make_uint4((sx >> sh) & 0xffffu, (sy >> sh) & 0xffffu, (sz >> sh) & 0xffffu,
+                                   (st >> sh) & 0xffffu);
+            trims[r] = make_uint2(first == 0xffffffffu ? (uint32_t)g.nx : first, last);
+            if (MC) mccnt[r] = (sm >> sh) & 0xffffu;
+        }
+        A = Cw;
+        B = Dw;
     }
 }
 
@@ -459,6 +582,20 @@ static void count_launch(const CountPlan& p, const float* vol, const Grid& g, fl
 {
     const unsigned blocks = (unsigned)(p.nyb * p.nkc);
     const bool vec4 = g.W <= 64 && (g.nx % 4 == 0) && ((reinterpret_cast<uintptr_t>(vol) & 15) == 0);
+    if (vec4 && g.W <= 16) {  // two rows per warp
+        const int nyb2 = (g.ny + kPairRows - 1) / kPairRows;
+        const unsigned blocks2 = (unsigned)(nyb2 * p.nkc);
+        const int nq = g.nx >> 2;
+#define ISO_PAIRS(UU)                                                                                          \
+    k_count_pairs<MC, UU><<<blocks2, kThreads, 0, s>>>(vol, g, iso, p.KC, nyb2, cases, b.rowcnt, b.trims, b.mccnt, \
+                                                       b.bits)
+        if (nq <= 16) ISO_PAIRS(1);
+        else if (nq <= 32) ISO_PAIRS(2);
+        else if (nq <= 64) ISO_PAIRS(4);
+        else ISO_PAIRS(8);
+#undef ISO_PAIRS
+        return;
+    }
 #define ISO_COUNT(VEC, UU, NWW)                                                                                \
     k_count_warps<MC, VEC, UU, NWW><<<blocks, kThreads, 0, s>>>(vol, g, iso, p.KC, p.nyb, cases, b.rowcnt,     \
                                                                 b.trims, b.mccnt, b.bits)
