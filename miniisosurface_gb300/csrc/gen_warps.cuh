@@ -38,27 +38,15 @@
 
 namespace iso {
 
-constexpr int kGenRows = 8;    // grid rows per CTA, one per warp
-constexpr int kGenSlots = 4;   // planes k, k+1 resident; k+2, k+3 in flight
+constexpr int kGenRows = 8;       // grid rows per CTA, one per warp
+constexpr int kGenCtasPerSm = 3;  // resident CTAs per SM the kernel is built for
+constexpr int kGenPrefetch = 3;   // planes of L2 prefetch ahead of the step
 constexpr int kGenCells = 32;  // cells per batch
 constexpr int kGenTris = 5 * kGenCells;    // triangles of a batch, at most
 constexpr int kGenOwned = 12 * kGenCells;  // MC vertices owned by a batch, at most
 enum GenMode { kGenFE = 0, kGenMC = 1, kGenTri = 2 };
 
-struct GenSlab {
-    int jlo, nrows;  // first row and number of rows of a slab
-};
-
-__host__ __device__ inline GenSlab gen_slab_rows(int j0, int ny)
-{
-    GenSlab s;
-    s.jlo = j0 > 0 ? j0 - 1 : 0;
-    const int jhi = min(j0 + kGenRows + 2, ny);
-    s.nrows = jhi - s.jlo;
-    return s;
-}
-
-// Per-warp scratch in shared memory, after the slab ring and its barriers:
+// Per-warp scratch in shared memory:
 //   mb[8][W]   {cut mask, id of its first cut edge - the row's first vertex}
 //              per mask (xA xB xC xD yA yC zA zB) and word
 //   cell[32]   the batch's active cells: i | cube case << 16
@@ -68,12 +56,6 @@ __host__ __device__ inline size_t gen_warp_scratch_bytes(int W, int mode)
 {
     const size_t list = mode == kGenMC ? (size_t)kGenOwned * 2 : (size_t)kGenTris;
     return ((size_t)8 * W * 8 + kGenCells * 4 + list + 15) & ~(size_t)15;
-}
-
-// Bytes of the slab ring and its barriers.
-__host__ __device__ inline size_t gen_ring_bytes(int slab_floats)
-{
-    return (size_t)kGenSlots * slab_floats * 4 + 2 * kGenSlots * 8;
 }
 
 // Divisors of the gradient: the reference divides by the spacing (one-sided
@@ -218,26 +200,32 @@ __device__ __forceinline__ uint32_t fe_edge_rel(const uint2* mb, int W, int e, i
 }
 
 template <int MODE, typename IndexT, bool BULK>
-__global__ void __launch_bounds__(kThreads, 2) k_gen_warps(
+__global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
     const float* __restrict__ vol, const uint32_t* __restrict__ bits, Grid g, GradScale gs, float iso, int KC,
-    int nyb, int slab_floats, int ws_bytes, const CaseTables* __restrict__ cases, const uint4* __restrict__ rowcnt,
-    RowStarts rs, unsigned long long* __restrict__ totals, long long capV, long long capT, float* __restrict__ points,
+    int nyb, int ws_bytes, const CaseTables* __restrict__ cases, const uint4* __restrict__ rowcnt, RowStarts rs,
+    unsigned long long* __restrict__ totals, long long capV, long long capT, float* __restrict__ points,
     float* __restrict__ normals, IndexT* __restrict__ tris, uint32_t* __restrict__ fe2mc, int reverse)
 {
     constexpr bool VOL = MODE != kGenTri;
-    constexpr int NS = kGenSlots;
-    extern __shared__ __align__(128) unsigned char s_raw[];
-    __shared__ SharedCases s_cases;
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    __shared__ uint64_t s_tris[MODE == kGenMC ? 1 : 256];
+    __shared__ uint64_t s_order[MODE == kGenMC ? 256 : 1];
+    __shared__ uint16_t s_cut[MODE == kGenMC ? 256 : 1];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int W = g.W;
-    float* slots = reinterpret_cast<float*>(s_raw);
-    uint64_t* full = reinterpret_cast<uint64_t*>(s_raw + (size_t)NS * slab_floats * 4);
-    uint64_t* empty = full + NS;
-    unsigned char* ws = s_raw + (VOL ? gen_ring_bytes(slab_floats) : 0) + (size_t)warp * ws_bytes;
+    unsigned char* ws = s_raw + (size_t)warp * ws_bytes;
     uint2* mb = reinterpret_cast<uint2*>(ws);
     uint32_t* cell = reinterpret_cast<uint32_t*>(ws + (size_t)8 * W * 8);
     unsigned char* list = ws + (size_t)8 * W * 8 + kGenCells * 4;
-    stage_cases(s_cases, cases, MODE == kGenMC);  // includes __syncthreads
+    for (int c = tid; c < 256; c += kThreads) {
+        if (MODE == kGenMC) {
+            s_order[c] = cases->order[c];
+            s_cut[c] = cases->cut[c];
+        } else {
+            s_tris[c] = cases->tris[c];
+        }
+    }
+    __syncthreads();  // the only CTA barrier: from here on every warp runs alone
     if ((long long)totals[0] > capV || (long long)totals[1] > capT) return;  // caller grows buffers
 
     const int nkc = gridDim.x / nyb;
@@ -246,51 +234,35 @@ __global__ void __launch_bounds__(kThreads, 2) k_gen_warps(
     const int j0 = jb * kGenRows;
     const int kb = kc * KC, ke = min(kb + KC, g.nz);
     const int j = j0 + warp;
-    const bool row_ok = j < g.ny;
-    const GenSlab sl = gen_slab_rows(j0, g.ny);
-    const int nfl = sl.nrows * g.nx;
+    if (j >= g.ny) return;
+    const int jlo = j0 > 0 ? j0 - 1 : 0;  // planes are addressed from this row
+    const long long plane = (long long)g.ny * g.nx;
+    auto plane_ptr = [&](int p) { return vol + (long long)p * plane + (long long)jlo * g.nx; };
 
-    if (VOL && tid == 0) {
-        for (int s = 0; s < NS; ++s) {
-            mbar_init(&full[s], BULK ? 1u : 32u);
-            mbar_init(&empty[s], (unsigned)kGenRows);
+    // L2 prefetch (TMA bulk prefetch when rows are 16-byte aligned) of this
+    // warp's rows j, j+1 of plane p, kGenPrefetch planes ahead of use.
+    const bool hasY = j < g.ny - 1;
+    auto prefetch_plane = [&](int p) {
+        if (!VOL || p >= g.nz) return;
+        const float* r0 = vol + (long long)p * plane + (long long)j * g.nx;
+        const int nrows = hasY ? 2 : 1;
+        if (BULK) {
+            if (lane == 0) bulk_prefetch_l2(r0, (unsigned)(nrows * g.nx * 4));
+        } else {
+            for (int q = lane * 32; q < nrows * g.nx; q += 32 * 32) prefetch_l2_line(r0 + q);
         }
-        fence_mbar_init();
-    }
-    __syncthreads();
-
-    // ---- slab ring.  Plane p lives in slot p % NS; its use index in the slot
-    // is (p - kb) / NS, which gives the phase parity of both barriers.
-    bool alive = true;
-    uint32_t issued = 0;  // producer: planes issued so far, as kb + issued
-    auto issue_upto = [&](int plast) -> bool {  // warp 0 only: issue planes <= plast
-        bool ok = true;
-        const int pmax = min(plast, min(ke, g.nz - 1));
-        while (ok && kb + (int)issued <= pmax) {
-            const int p = kb + (int)issued;
-            const int s = p % NS;
-            if (p - kb >= NS) ok = mbar_wait(&empty[s], (((p - kb) / NS) - 1) & 1);  // previous plane released
-            if (ok) {
-                slab_copy<BULK>(slots + (size_t)s * slab_floats, vol + ((long long)p * g.ny + sl.jlo) * g.nx, nfl,
-                                &full[s], lane, 32);
-            }
-            ++issued;
-        }
-        return ok;
     };
-    auto wait_plane = [&](int p) -> bool { return mbar_wait(&full[p % NS], ((p - kb) / NS) & 1); };
-
-    if (VOL && warp == 0) alive = issue_upto(kb + NS - 2);
-    alive = __syncthreads_and(alive);
+    for (int p = kb - 1; p < kb + kGenPrefetch; ++p) {
+        if (p >= 0) prefetch_plane(p);
+    }
 
     const bool in = lane < W, in1 = lane + 1 < W;
     const uint32_t evalid = validmask(lane, g.nx - 1);  // x-edges / cells: i <= nx-2
     const uint32_t pvalid = validmask(lane, g.nx);      // points: i <= nx-1
-    const bool hasY = j < g.ny - 1;
 
     // Bit words of rows (j, p) and (j+1, p).
     auto load_words = [&](int p, uint32_t& wa, uint32_t& wb) {
-        const bool okp = row_ok && p < g.nz;
+        const bool okp = p < g.nz;
         const long long r = (long long)p * g.ny + j;
         wa = (in && okp) ? __ldg(&bits[r * W + lane]) : 0u;
         wb = (in && okp && hasY) ? __ldg(&bits[(r + 1) * W + lane]) : 0u;
@@ -302,7 +274,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_gen_warps(
     auto load_starts = [&](int p) -> unsigned long long {
         const int dk = (lane >> 1) & 1, dj = lane & 1;
         const bool hasZp = p + 1 < g.nz;
-        bool ok = row_ok && lane < 6;
+        bool ok = lane < 6;
         if (lane < 4) ok = ok && (dj == 0 || hasY) && (dk == 0 || hasZp);
         if (lane == 5) ok = ok && hasY;
         if (!ok) return 0ull;
@@ -320,9 +292,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_gen_warps(
     load_words(kb + 1, wC, wD);
     unsigned long long st = load_starts(kb);
 
-    for (int k = kb; k < ke && alive; ++k) {
-        if (VOL && warp == 0) alive = issue_upto(k + NS - 1) && alive;
+    for (int k = kb; k < ke; ++k) {
         const bool hasZ = k + 1 < g.nz;
+        prefetch_plane(k + kGenPrefetch);
         // the next step's words and starts, in flight while this step runs
         uint32_t nC = 0, nD = 0;
         unsigned long long nst = 0;
@@ -330,199 +302,179 @@ __global__ void __launch_bounds__(kThreads, 2) k_gen_warps(
             load_words(k + 2, nC, nD);
             nst = load_starts(k + 1);
         }
-        if (VOL) {
-            bool ok = wait_plane(k);
-            if (hasZ) ok = ok && wait_plane(k + 1);
-            alive = alive && ok;
-        }
-        if (!__all_sync(0xffffffffu, alive)) {
-            alive = false;
-            break;
-        }
-        if (row_ok) {
-            const bool cellrow = hasY && hasZ;
-            RowWords rw;
-            rw.a = wA;
-            rw.b = wB;
-            rw.c = hasZ ? wC : 0u;
-            rw.d = cellrow ? wD : 0u;
-            const uint32_t an = __shfl_down_sync(0xffffffffu, rw.a, 1);
-            const uint32_t bn = __shfl_down_sync(0xffffffffu, rw.b, 1);
-            const uint32_t cn = __shfl_down_sync(0xffffffffu, rw.c, 1);
-            const uint32_t dn = __shfl_down_sync(0xffffffffu, rw.d, 1);
-            rw.ash = (rw.a >> 1) | ((in1 ? an : 0u) << 31);
-            rw.bsh = (rw.b >> 1) | ((in1 ? bn : 0u) << 31);
-            rw.csh = (rw.c >> 1) | ((in1 ? cn : 0u) << 31);
-            rw.dsh = (rw.d >> 1) | ((in1 ? dn : 0u) << 31);
-            const CutMasks m = cut_masks(rw, evalid, pvalid, hasY, hasZ);
-            // popc prefixes, two 16-bit counts per scan
-            const uint32_t p0 = __popc(m.xA) | (__popc(m.xB) << 16);
-            const uint32_t p1 = __popc(m.xC) | (__popc(m.xD) << 16);
-            const uint32_t p2 = __popc(m.yA) | (__popc(m.yC) << 16);
-            const uint32_t p3 = __popc(m.zA) | (__popc(m.zB) << 16);
-            const uint32_t i0 = warp_incl_scan(p0, lane), i1 = warp_incl_scan(p1, lane);
-            const uint32_t i2 = warp_incl_scan(p2, lane), i3 = warp_incl_scan(p3, lane);
-            const uint32_t e0 = i0 - p0, e1 = i1 - p1, e2 = i2 - p2, e3 = i3 - p3;
-            const uint32_t t0 = __shfl_sync(0xffffffffu, i0, 31), t2 = __shfl_sync(0xffffffffu, i2, 31);
-            const uint32_t t1 = __shfl_sync(0xffffffffu, i1, 31), t3 = __shfl_sync(0xffffffffu, i3, 31);
-            const unsigned long long xsA = __shfl_sync(0xffffffffu, st, 0);
-            const uint32_t dB = (uint32_t)(__shfl_sync(0xffffffffu, st, 1) - xsA);
-            const uint32_t dC = (uint32_t)(__shfl_sync(0xffffffffu, st, 2) - xsA);
-            const uint32_t dD = (uint32_t)(__shfl_sync(0xffffffffu, st, 3) - xsA);
-            const unsigned long long ts = __shfl_sync(0xffffffffu, st, 4);
-            const uint32_t cntB = (uint32_t)__shfl_sync(0xffffffffu, st, 5);
-            const uint32_t nxA = t0 & 0xffffu, nyA = t2 & 0xffffu, nzA = t3 & 0xffffu, nxC = t1 & 0xffffu;
-            if (in) {  // first ids of the word's cut edges, relative to xsA
-                mb[0 * W + lane] = make_uint2(m.xA, e0 & 0xffffu);
-                mb[1 * W + lane] = make_uint2(m.xB, dB + (e0 >> 16));
-                mb[2 * W + lane] = make_uint2(m.xC, dC + (e1 & 0xffffu));
-                mb[3 * W + lane] = make_uint2(m.xD, dD + (e1 >> 16));
-                mb[4 * W + lane] = make_uint2(m.yA, nxA + (e2 & 0xffffu));
-                mb[5 * W + lane] = make_uint2(m.yC, dC + nxC + (e2 >> 16));
-                mb[6 * W + lane] = make_uint2(m.zA, nxA + nyA + (e3 & 0xffffu));
-                mb[7 * W + lane] = make_uint2(m.zB, dB + cntB + (e3 >> 16));
-            }
-            __syncwarp();
-            Planes pl{};
-            if (VOL) {
-                const float* sk = slots + (size_t)(k % NS) * slab_floats;
-                pl.p1 = sk;
-                pl.p2 = hasZ ? slots + (size_t)((k + 1) % NS) * slab_floats : sk;
-                pl.p0 = k > 0 ? vol + ((long long)(k - 1) * g.ny + sl.jlo) * g.nx : sk;
-                pl.p3 = k + 2 < g.nz ? vol + ((long long)(k + 2) * g.ny + sl.jlo) * g.nx : pl.p2;
-                pl.jlo = sl.jlo;
-                pl.nx = g.nx;
-            }
-
-            if (MODE == kGenFE) {
-                // ---- vertices of grid row (j, k): x, y then z sections
-                const uint32_t nv = nxA + nyA + nzA;
-                const int ck = min(k, g.nz - 2), cj = min(j, g.ny - 2);
-                // word prefixes of the x, y and z sections in one word: 10 + 11 + 11 bits
-                const uint32_t P = (e0 & 0x3ffu) | ((e2 & 0x7ffu) << 10) | ((e3 & 0x7ffu) << 21);
-                for (uint32_t v0 = 0; v0 < nv; v0 += 32) {
-                    const uint32_t v = v0 + lane;
-                    const int axis = v < nxA ? 0 : (v < nxA + nyA ? 1 : 2);
-                    const uint32_t r = v - (axis == 0 ? 0u : (axis == 1 ? nxA : nxA + nyA));
-                    const int sh = axis == 0 ? 0 : (axis == 1 ? 10 : 21);
-                    const uint32_t fm = axis == 0 ? 0x3ffu : 0x7ffu;
-                    int lo = 0;
-#pragma unroll
-                    for (int step = 16; step > 0; step >>= 1) {
-                        const int mid = lo + step;
-                        const uint32_t pv = (__shfl_sync(0xffffffffu, P, mid & 31) >> sh) & fm;
-                        if (mid < W && pv <= r) lo = mid;
-                    }
-                    if (v < nv) {
-                        const uint2 e = mb[(axis == 0 ? 0 : (axis == 1 ? 4 : 6)) * W + lo];
-                        const int bit = (int)__fns(e.x, 0, (int)(v - e.y) + 1);
-                        const int i = 32 * lo + bit;
-                        float3 p, n;
-                        vertex_on_edge(pl, g, gs, iso, axis, i, j, 1, k, axis == 0 ? i : min(i, g.nx - 2),
-                                       axis == 1 ? j : cj, axis == 2 ? k : ck, p, n);
-                        store_vertex(points, normals, xsA + v, p, n);
-                    }
-                }
-            }
-            if (cellrow) {
-                // ---- active cells of cell row (j, k), compacted 32 at a time
-                uint32_t rem = in ? active_cells(rw, evalid) : 0u;
-                const uint32_t na = __popc(rem);
-                const uint32_t ia = warp_incl_scan(na, lane);
-                uint32_t rank = ia - na;
-                const uint32_t tot = __shfl_sync(0xffffffffu, ia, 31);
-                unsigned long long tcur = ts;  // FE / TRI: next triangle; MC: next vertex
-                for (uint32_t c0 = 0; c0 < tot; c0 += kGenCells) {
-                    while (rem != 0u && rank < c0 + kGenCells) {
-                        const int bit = __ffs(rem) - 1;
-                        cell[rank - c0] = (uint32_t)(32 * lane + bit) | ((uint32_t)cube_case(rw, bit) << 16);
-                        rem &= rem - 1u;
-                        ++rank;
-                    }
-                    __syncwarp();
-                    const uint32_t nc = min(tot - c0, (uint32_t)kGenCells);
-                    const bool live = (uint32_t)lane < nc;
-                    const uint32_t rec = live ? cell[lane] : 0u;
-                    const int cs = (int)(rec >> 16);
-                    if (MODE == kGenFE || MODE == kGenTri) {
-                        const uint32_t nt = live ? (uint32_t)iso_case_ntris(s_cases.tris[cs]) : 0u;
-                        const uint32_t it = warp_incl_scan(nt, lane);
-                        const uint32_t ntb = __shfl_sync(0xffffffffu, it, 31);
-                        for (uint32_t q = 0; q < nt; ++q) list[it - nt + q] = (unsigned char)(lane | (q << 5));
-                        __syncwarp();
-                        for (uint32_t tb = 0; tb < ntb; tb += 32) {
-                            const uint32_t t = tb + lane;
-                            if (t < ntb) {
-                                const uint32_t tr = list[t];
-                                const uint32_t cr = cell[tr & 31u];
-                                const int q = (int)(tr >> 5);
-                                const int ci = (int)(cr & 0xffffu);
-                                const uint64_t tl = s_cases.tris[cr >> 16];
-                                const int w = ci >> 5, bit = ci & 31;
-                                IndexT* o = tris + 3 * (tcur + t);
-#pragma unroll
-                                for (int c = 0; c < 3; ++c) {
-                                    const unsigned long long id =
-                                        xsA + fe_edge_rel(mb, W, iso_case_edge(tl, 3 * q + c), w, bit);
-                                    o[c] = MODE == kGenTri ? (IndexT)__ldg(fe2mc + id) : (IndexT)id;
-                                }
-                            }
-                        }
-                        tcur += ntb;
-                    } else {
-                        // ---- MC vertices owned by the batch's cells: cell order, then order of
-                        // first appearance in the cell's triangle list
-                        const int ci = (int)(rec & 0xffffu);
-                        const uint32_t own =
-                            live ? (mc_owned_edges(ci == 0, j == 0, k == 0) & s_cases.cut[cs]) : 0u;
-                        const uint32_t no = __popc(own);
-                        const uint32_t io = warp_incl_scan(no, lane);
-                        const uint32_t nob = __shfl_sync(0xffffffffu, io, 31);
-                        uint16_t* vl = reinterpret_cast<uint16_t*>(list);
-                        if (own) {
-                            const uint64_t ord = s_cases.order[cs];
-                            uint32_t o = io - no;
-                            for (int q = 0; q < iso_case_ntris(ord); ++q) {
-                                const int ed = iso_case_edge(ord, q);
-                                if ((own >> ed) & 1u) vl[o++] = (uint16_t)(lane | (ed << 5));
-                            }
-                        }
-                        __syncwarp();
-                        for (uint32_t vb = 0; vb < nob; vb += 32) {
-                            const uint32_t v = vb + lane;
-                            if (v < nob) {
-                                const uint32_t vr = vl[v];
-                                const uint32_t cr = cell[vr & 31u];
-                                const int e12 = (int)(vr >> 5);
-                                const int i = (int)(cr & 0xffffu);
-                                int dx, dy, dz, axis;
-                                cube_edge_geometry(e12, dx, dy, dz, axis);
-                                float3 p, n;
-                                vertex_on_edge(pl, g, gs, iso, axis, i + dx, j + dy, 1 + dz, k + dz, i, j, k, p, n);
-                                const unsigned long long id = tcur + v;
-                                store_vertex(points, normals, id, p, n);
-                                fe2mc[xsA + fe_edge_rel(mb, W, e12, i >> 5, i & 31)] = (uint32_t)id;
-                            }
-                        }
-                        tcur += nob;
-                    }
-                    __syncwarp();  // the next batch overwrites the lists
-                }
-            }
+        const bool cellrow = hasY && hasZ;
+        RowWords rw;
+        rw.a = wA;
+        rw.b = wB;
+        rw.c = hasZ ? wC : 0u;
+        rw.d = cellrow ? wD : 0u;
+        const uint32_t an = __shfl_down_sync(0xffffffffu, rw.a, 1);
+        const uint32_t bn = __shfl_down_sync(0xffffffffu, rw.b, 1);
+        const uint32_t cn = __shfl_down_sync(0xffffffffu, rw.c, 1);
+        const uint32_t dn = __shfl_down_sync(0xffffffffu, rw.d, 1);
+        rw.ash = (rw.a >> 1) | ((in1 ? an : 0u) << 31);
+        rw.bsh = (rw.b >> 1) | ((in1 ? bn : 0u) << 31);
+        rw.csh = (rw.c >> 1) | ((in1 ? cn : 0u) << 31);
+        rw.dsh = (rw.d >> 1) | ((in1 ? dn : 0u) << 31);
+        const CutMasks m = cut_masks(rw, evalid, pvalid, hasY, hasZ);
+        // popc prefixes, two 16-bit counts per scan
+        const uint32_t p0 = __popc(m.xA) | (__popc(m.xB) << 16);
+        const uint32_t p1 = __popc(m.xC) | (__popc(m.xD) << 16);
+        const uint32_t p2 = __popc(m.yA) | (__popc(m.yC) << 16);
+        const uint32_t p3 = __popc(m.zA) | (__popc(m.zB) << 16);
+        const uint32_t i0 = warp_incl_scan(p0, lane), i1 = warp_incl_scan(p1, lane);
+        const uint32_t i2 = warp_incl_scan(p2, lane), i3 = warp_incl_scan(p3, lane);
+        const uint32_t e0 = i0 - p0, e1 = i1 - p1, e2 = i2 - p2, e3 = i3 - p3;
+        const uint32_t t0 = __shfl_sync(0xffffffffu, i0, 31), t2 = __shfl_sync(0xffffffffu, i2, 31);
+        const uint32_t t1 = __shfl_sync(0xffffffffu, i1, 31), t3 = __shfl_sync(0xffffffffu, i3, 31);
+        const unsigned long long xsA = __shfl_sync(0xffffffffu, st, 0);
+        const uint32_t dB = (uint32_t)(__shfl_sync(0xffffffffu, st, 1) - xsA);
+        const uint32_t dC = (uint32_t)(__shfl_sync(0xffffffffu, st, 2) - xsA);
+        const uint32_t dD = (uint32_t)(__shfl_sync(0xffffffffu, st, 3) - xsA);
+        const unsigned long long ts = __shfl_sync(0xffffffffu, st, 4);
+        const uint32_t cntB = (uint32_t)__shfl_sync(0xffffffffu, st, 5);
+        const uint32_t nxA = t0 & 0xffffu, nyA = t2 & 0xffffu, nzA = t3 & 0xffffu, nxC = t1 & 0xffffu;
+        if (in) {  // first ids of the word's cut edges, relative to xsA
+            mb[0 * W + lane] = make_uint2(m.xA, e0 & 0xffffu);
+            mb[1 * W + lane] = make_uint2(m.xB, dB + (e0 >> 16));
+            mb[2 * W + lane] = make_uint2(m.xC, dC + (e1 & 0xffffu));
+            mb[3 * W + lane] = make_uint2(m.xD, dD + (e1 >> 16));
+            mb[4 * W + lane] = make_uint2(m.yA, nxA + (e2 & 0xffffu));
+            mb[5 * W + lane] = make_uint2(m.yC, dC + nxC + (e2 >> 16));
+            mb[6 * W + lane] = make_uint2(m.zA, nxA + nyA + (e3 & 0xffffu));
+            mb[7 * W + lane] = make_uint2(m.zB, dB + cntB + (e3 >> 16));
         }
         __syncwarp();
-        if (VOL && lane == 0) mbar_arrive(&empty[k % NS]);  // this warp is done with plane k
+        Planes pl{};
+        if (VOL) {  // planes k-1 .. k+2; those outside the grid alias plane k
+            pl.p1 = plane_ptr(k);
+            pl.p0 = k > 0 ? plane_ptr(k - 1) : pl.p1;
+            pl.p2 = hasZ ? plane_ptr(k + 1) : pl.p1;
+            pl.p3 = k + 2 < g.nz ? plane_ptr(k + 2) : pl.p1;
+            pl.jlo = jlo;
+            pl.nx = g.nx;
+        }
+
+        if (MODE == kGenFE) {
+            // ---- vertices of grid row (j, k): x, y then z sections
+            const uint32_t nv = nxA + nyA + nzA;
+            const int ck = min(k, g.nz - 2), cj = min(j, g.ny - 2);
+            // word prefixes of the x, y and z sections in one word: 10 + 11 + 11 bits
+            const uint32_t P = (e0 & 0x3ffu) | ((e2 & 0x7ffu) << 10) | ((e3 & 0x7ffu) << 21);
+            for (uint32_t v0 = 0; v0 < nv; v0 += 32) {
+                const uint32_t v = v0 + lane;
+                const int axis = v < nxA ? 0 : (v < nxA + nyA ? 1 : 2);
+                const uint32_t r = v - (axis == 0 ? 0u : (axis == 1 ? nxA : nxA + nyA));
+                const int sh = axis == 0 ? 0 : (axis == 1 ? 10 : 21);
+                const uint32_t fm = axis == 0 ? 0x3ffu : 0x7ffu;
+                int lo = 0;
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1) {
+                    const int mid = lo + step;
+                    const uint32_t pv = (__shfl_sync(0xffffffffu, P, mid & 31) >> sh) & fm;
+                    if (mid < W && pv <= r) lo = mid;
+                }
+                if (v < nv) {
+                    const uint2 e = mb[(axis == 0 ? 0 : (axis == 1 ? 4 : 6)) * W + lo];
+                    const int bit = (int)__fns(e.x, 0, (int)(v - e.y) + 1);
+                    const int i = 32 * lo + bit;
+                    float3 p, n;
+                    vertex_on_edge(pl, g, gs, iso, axis, i, j, 1, k, axis == 0 ? i : min(i, g.nx - 2),
+                                   axis == 1 ? j : cj, axis == 2 ? k : ck, p, n);
+                    store_vertex(points, normals, xsA + v, p, n);
+                }
+            }
+        }
+        if (cellrow) {
+            // ---- active cells of cell row (j, k), compacted 32 at a time
+            uint32_t rem = in ? active_cells(rw, evalid) : 0u;
+            const uint32_t na = __popc(rem);
+            const uint32_t ia = warp_incl_scan(na, lane);
+            uint32_t rank = ia - na;
+            const uint32_t tot = __shfl_sync(0xffffffffu, ia, 31);
+            unsigned long long tcur = ts;  // FE / TRI: next triangle; MC: next vertex
+            for (uint32_t c0 = 0; c0 < tot; c0 += kGenCells) {
+                while (rem != 0u && rank < c0 + kGenCells) {
+                    const int bit = __ffs(rem) - 1;
+                    cell[rank - c0] = (uint32_t)(32 * lane + bit) | ((uint32_t)cube_case(rw, bit) << 16);
+                    rem &= rem - 1u;
+                    ++rank;
+                }
+                __syncwarp();
+                const uint32_t nc = min(tot - c0, (uint32_t)kGenCells);
+                const bool live = (uint32_t)lane < nc;
+                const uint32_t rec = live ? cell[lane] : 0u;
+                const int cs = (int)(rec >> 16);
+                if (MODE == kGenFE || MODE == kGenTri) {
+                    const uint32_t nt = live ? (uint32_t)iso_case_ntris(s_tris[cs]) : 0u;
+                    const uint32_t it = warp_incl_scan(nt, lane);
+                    const uint32_t ntb = __shfl_sync(0xffffffffu, it, 31);
+                    for (uint32_t q = 0; q < nt; ++q) list[it - nt + q] = (unsigned char)(lane | (q << 5));
+                    __syncwarp();
+                    for (uint32_t tb = 0; tb < ntb; tb += 32) {
+                        const uint32_t t = tb + lane;
+                        if (t < ntb) {
+                            const uint32_t tr = list[t];
+                            const uint32_t cr = cell[tr & 31u];
+                            const int q = (int)(tr >> 5);
+                            const int ci = (int)(cr & 0xffffu);
+                            const uint64_t tl = s_tris[cr >> 16];
+                            const int w = ci >> 5, bit = ci & 31;
+                            IndexT* o = tris + 3 * (tcur + t);
+#pragma unroll
+                            for (int c = 0; c < 3; ++c) {
+                                const unsigned long long id =
+                                    xsA + fe_edge_rel(mb, W, iso_case_edge(tl, 3 * q + c), w, bit);
+                                o[c] = MODE == kGenTri ? (IndexT)__ldg(fe2mc + id) : (IndexT)id;
+                            }
+                        }
+                    }
+                    tcur += ntb;
+                } else {
+                    // ---- MC vertices owned by the batch's cells: cell order, then order of
+                    // first appearance in the cell's triangle list
+                    const int ci = (int)(rec & 0xffffu);
+                    const uint32_t own = live ? (mc_owned_edges(ci == 0, j == 0, k == 0) & s_cut[cs]) : 0u;
+                    const uint32_t no = __popc(own);
+                    const uint32_t io = warp_incl_scan(no, lane);
+                    const uint32_t nob = __shfl_sync(0xffffffffu, io, 31);
+                    uint16_t* vl = reinterpret_cast<uint16_t*>(list);
+                    if (own) {
+                        const uint64_t ord = s_order[cs];
+                        uint32_t o = io - no;
+                        for (int q = 0; q < iso_case_ntris(ord); ++q) {
+                            const int ed = iso_case_edge(ord, q);
+                            if ((own >> ed) & 1u) vl[o++] = (uint16_t)(lane | (ed << 5));
+                        }
+                    }
+                    __syncwarp();
+                    for (uint32_t vb = 0; vb < nob; vb += 32) {
+                        const uint32_t v = vb + lane;
+                        if (v < nob) {
+                            const uint32_t vr = vl[v];
+                            const uint32_t cr = cell[vr & 31u];
+                            const int e12 = (int)(vr >> 5);
+                            const int i = (int)(cr & 0xffffu);
+                            int dx, dy, dz, axis;
+                            cube_edge_geometry(e12, dx, dy, dz, axis);
+                            float3 p, n;
+                            vertex_on_edge(pl, g, gs, iso, axis, i + dx, j + dy, 1 + dz, k + dz, i, j, k, p, n);
+                            const unsigned long long id = tcur + v;
+                            store_vertex(points, normals, id, p, n);
+                            fe2mc[xsA + fe_edge_rel(mb, W, e12, i >> 5, i & 31)] = (uint32_t)id;
+                        }
+                    }
+                    tcur += nob;
+                }
+                __syncwarp();  // the next batch overwrites the lists
+            }
+        }
+        __syncwarp();  // the next step overwrites mb
         wA = wC;
         wB = wD;
         wC = nC;
         wD = nD;
         st = nst;
-    }
-    if (!alive && tid == 0) atomicOr(&totals[3], kStatusTimeout);
-    if (VOL && warp == 0) {  // copies still in flight must land before the CTA exits
-        for (int p = kb; p < kb + (int)issued; ++p) {
-            if (p >= ke || !alive) mbar_wait(&full[p % NS], ((p - kb) / NS) & 1);
-        }
     }
 }
 
@@ -535,11 +487,10 @@ void launch_gen_warps_impl(const float* vol, const Grid& g, float iso, const Cas
     const bool bulk = MODE != kGenTri && (g.nx % 4 == 0) && ((reinterpret_cast<uintptr_t>(vol) & 15) == 0);
     const unsigned blocks = (unsigned)(p.nyb * p.nkc);
     const int ws_bytes = (int)gen_warp_scratch_bytes(g.W, MODE);
-    const int slab = MODE == kGenTri ? 0 : p.slab_floats;
-    const size_t smem = (MODE == kGenTri ? 0 : gen_ring_bytes(slab)) + (size_t)kGenRows * ws_bytes;
+    const size_t smem = (size_t)kGenRows * ws_bytes;
     auto kern = bulk ? k_gen_warps<MODE, IndexT, true> : k_gen_warps<MODE, IndexT, false>;
     allow_smem(kern, smem);
-    kern<<<blocks, kThreads, smem, s>>>(vol, b.bits, g, make_grad_scale(g), iso, p.KC, p.nyb, slab, ws_bytes, cases,
+    kern<<<blocks, kThreads, smem, s>>>(vol, b.bits, g, make_grad_scale(g), iso, p.KC, p.nyb, ws_bytes, cases,
                                         b.rowcnt, rs, b.totals, capV, capT, points, normals, tris, b.fe2mc, reverse);
 }
 

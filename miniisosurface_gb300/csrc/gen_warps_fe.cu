@@ -4,23 +4,19 @@
 
 namespace iso {
 
-// Dynamic shared memory (slab ring + warp scratch); above kGenTwoPerSm only
-// one CTA fits per SM, above kGenMaxSmem (or rows wider than 32 words) the
-// row-wise kernels are used.
-constexpr size_t kGenTwoPerSm = 108 * 1024;
-constexpr size_t kGenMaxSmem = 200 * 1024;
-
+// Warp-per-row kernels take rows of up to 32 words (1024 points) whose cell
+// rows number their vertices in 32 bits relative to the row's first one;
+// wider grids use the row-wise kernels.
 GenPlan gen_plan(const Grid& g, int nsm)
 {
     GenPlan p;
     p.J = kGenRows;
     p.nyb = (g.ny + p.J - 1) / p.J;
-    p.slab_floats = (int)((((size_t)(p.J + 3) * g.nx) + 31) & ~(size_t)31);
-    p.smem = gen_ring_bytes(p.slab_floats) + (size_t)kGenRows * gen_warp_scratch_bytes(g.W, kGenMC);
-    // relative vertex ids of a cell row (up to two planes of vertices) in 32 bits
-    const bool rel32 = 6.0 * g.nx * g.ny < 4294967295.0;
-    p.fits = g.W <= 32 && p.smem <= kGenMaxSmem && rel32;
-    const long long resident = (long long)nsm * (p.smem <= kGenTwoPerSm ? 2 : 1);
+    p.smem = (size_t)kGenRows * gen_warp_scratch_bytes(g.W, kGenMC);
+    const bool rel32 = 6.0 * g.nx * g.ny < 4294967295.0;  // two planes of vertices
+    p.fits = g.W <= 32 && rel32;
+    // about 4 waves of resident CTAs, at least 4 planes per column
+    const long long resident = (long long)nsm * kGenCtasPerSm;
     int nkc = (int)((4 * resident + p.nyb - 1) / p.nyb);
     if (nkc < 1) nkc = 1;
     p.KC = (g.nz + nkc - 1) / nkc;

@@ -17,10 +17,7 @@ template <typename IndexT>
 void launch_mc_tri_warps(const Grid& g, const CaseTables* cases, const FeBuffers& b, const CountPlan& cp,
                          const GenPlan& p, long long capV, long long capT, IndexT* tris, cudaStream_t s)
 {
-    GenPlan q = p;
-    q.slab_floats = 0;
-    q.smem = 0;
-    launch_gen_warps_impl<kGenTri, IndexT>(nullptr, g, 0.f, cases, b, cp, q, capV, capT, nullptr, nullptr, tris, 0,
+    launch_gen_warps_impl<kGenTri, IndexT>(nullptr, g, 0.f, cases, b, cp, p, capV, capT, nullptr, nullptr, tris, 0,
                                            s);
 }
 

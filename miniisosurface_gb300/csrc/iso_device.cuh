@@ -441,6 +441,19 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsign
                  : "memory");
 }
 
+// L2 prefetch of [src, src + bytes) by the TMA engine; src 16-byte aligned,
+// bytes a multiple of 16.
+__device__ __forceinline__ void bulk_prefetch_l2(const void* src, unsigned bytes)
+{
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
+
+// L2 prefetch of the 128-byte line holding p.
+__device__ __forceinline__ void prefetch_l2_line(const void* p)
+{
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 __device__ __forceinline__ void cp_async4(void* dst, const void* src)
 {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");

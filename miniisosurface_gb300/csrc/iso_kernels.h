@@ -33,11 +33,10 @@ struct CountPlan {
 };
 
 // Work split of the warp-per-row generate kernels: blocks of J = 8 rows,
-// columns of KC planes, a ring of slabs of J+3 rows.
+// columns of KC planes.
 struct GenPlan {
     int J = 8, nyb = 1, KC = 1, nkc = 1;
-    int slab_floats = 0;
-    size_t smem = 0;
+    size_t smem = 0;  // per-warp scratch of the CTA
     bool fits = false;  // false: use the row-wise kernels
 };
 
