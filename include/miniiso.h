@@ -147,6 +147,29 @@ iso_status iso_extract_device(iso_ctx* ctx, iso_algorithm algo, const float* vol
 iso_status iso_extract_device_async(iso_ctx* ctx, iso_algorithm algo, const float* volume, const iso_grid* grid,
                                     float isoval, iso_mesh* out, int64_t* result_host, void* stream);
 
+/* z-slabs: the grid split along z into slabs of planes [k0, k1), for
+ * sharding over GPUs or streaming a volume that does not fit (no counterpart
+ * in the serial reference; marchingCubes/mpi/mpiutil.h:197-203 splits the
+ * MPI version the same way).  A slab owns the Flying Edges vertices of the
+ * grid rows of planes k0 .. k1-1, the cells between planes k0 and k1 (their
+ * triangles) and, for Marching Cubes, the vertices those cells own.
+ * `volume` (device memory) holds planes max(k0-1, 0) .. min(k1+1, nz-1) of
+ * the grid only; `grid` describes the whole volume.  Rows must be at most
+ * 1024 points long.
+ * iso_count_slab: the slab's vertex and triangle counts.
+ * iso_extract_slab: the slab's vertices and triangles, numbered exactly as in
+ * the whole-volume extraction: the slab's first vertex has id point_offset
+ * and its first triangle index tri_offset (the sums of the counts of the
+ * slabs below: an exclusive scan of iso_count_slab over the slabs); `out`
+ * receives the slab's part only (out->points row 0 is vertex point_offset).
+ * Concatenating the slabs' parts gives the whole extraction's mesh, bit for
+ * bit.  Both synchronise the stream. */
+iso_status iso_count_slab(iso_ctx* ctx, iso_algorithm algo, const float* volume, const iso_grid* grid, int64_t k0,
+                          int64_t k1, float isoval, int64_t* n_points, int64_t* n_tris, void* stream);
+iso_status iso_extract_slab(iso_ctx* ctx, iso_algorithm algo, const float* volume, const iso_grid* grid, int64_t k0,
+                            int64_t k1, float isoval, int64_t point_offset, int64_t tri_offset, iso_mesh* out,
+                            void* stream);
+
 /* Host in, host out: copies the volume to the device, extracts, and copies
  * the mesh back into the caller's host buffers (pinned buffers give the full
  * link bandwidth).  This is the whole reference call, util::Image3D in and

@@ -51,6 +51,10 @@ SIGNATURES = {
                                    C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.c_void_p]),
     "iso_count_device_noalloc": (C.c_int, [C.c_int, C.c_void_p, C.POINTER(IsoGrid), C.c_float, C.c_void_p,
                                            C.c_void_p]),
+    "iso_count_slab": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.POINTER(IsoGrid), C.c_int64, C.c_int64,
+                                 C.c_float, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.c_void_p]),
+    "iso_extract_slab": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.POINTER(IsoGrid), C.c_int64, C.c_int64,
+                                   C.c_float, C.c_int64, C.c_int64, C.POINTER(IsoMesh), C.c_void_p]),
     "iso_extract_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.POINTER(IsoGrid), C.c_float,
                                      C.POINTER(IsoMesh), C.c_void_p]),
     "iso_extract_device_async": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.POINTER(IsoGrid), C.c_float,

@@ -34,6 +34,7 @@ struct iso_ctx {
     long long d_cap_points = 0, d_cap_tris = 0;
     int d_index_bytes = 0;
     unsigned long long* h_totals = nullptr;  // pinned, 4 entries
+    unsigned long long* h_slab = nullptr;    // pinned, 9 entries (slab counts)
     int reverse = 1;  // pass 4 walks the planes backwards (the count pass leaves the last ones in L2)
     std::string last_error;
     // per-pass timing (iso_ctx_profile)
@@ -118,6 +119,9 @@ bool make_grid(const iso_grid* gr, Grid& g)
     g.W = (g.nx + 31) / 32;
     g.R = (long long)g.ny * g.nz;
     if ((long long)g.W * g.R > (1ll << 40)) return false;
+    g.kd = 0;
+    g.kr = 0;
+    g.ke = g.nz;
     for (int a = 0; a < 3; ++a) {
         g.sp[a] = gr->spacing[a];
         g.zp[a] = gr->origin[a];
@@ -326,9 +330,183 @@ iso_status finish_counts(iso_ctx* ctx, const iso_mesh* out, long long V, long lo
     return ISO_OK;
 }
 
+// ---------------------------------------------------------------------------
+// z-slabs [k0, k1) of a decomposition along z.  The window of a slab: the
+// volume pointer holds planes max(k0-1, 0) .. min(k1+1, nz-1); the scratch
+// rows are planes [kr, ke) with kr = k0 (FE) or max(k0-1, 0) (MC, whose
+// triangles at plane k0 reference vertices owned by cell row k0-1) and
+// ke = min(k1+1, nz) (rows of plane k1 number the vertices the slab's top
+// cells reference).
+// ---------------------------------------------------------------------------
+bool slab_grid(const iso_grid* gr, iso_algorithm algo, int64_t k0, int64_t k1, Grid& g)
+{
+    if (!make_grid(gr, g)) return false;
+    if (k0 < 0 || k1 <= k0 || k1 > g.nz) return false;
+    g.kd = (int)(k0 > 0 ? k0 - 1 : 0);
+    g.kr = algo == ISO_MARCHING_CUBES ? g.kd : (int)k0;
+    g.ke = (int)(k1 + 1 < g.nz ? k1 + 1 : g.nz);
+    g.R = (long long)g.ny * (g.ke - g.kr);
+    return true;
+}
+
+// Counts of the window (enqueued and read back): lo[a] / hi[a] = row starts
+// (vertices, triangles, MC vertices) at planes k0 and k1 (window totals for
+// k1 = nz).  The slab owns [lo, hi) of each.
+struct SlabCounts {
+    unsigned long long lo[3], hi[3], tot[3];
+};
+
+iso_status slab_count(iso_ctx* ctx, iso_algorithm algo, const float* vol, const Grid& g, int64_t k0, int64_t k1,
+                      float iso, const Plans& pl, FeBuffers& b, cudaStream_t s, SlabCounts& c)
+{
+    if (!ctx->h_slab) ISO_CUDA(ctx, cudaMallocHost(&ctx->h_slab, 9 * sizeof(unsigned long long)));
+    PassMarks pm(ctx, s);
+    enqueue_count(ctx, algo, vol, g, iso, pl, b, s, pm);
+    ISO_CUDA(ctx, cudaGetLastError());
+    ISO_CUDA(ctx, cudaMemsetAsync(b.totals + 3, 0, sizeof(unsigned long long), s));
+    unsigned long long* h = ctx->h_slab;
+    ISO_CUDA(ctx, cudaMemcpyAsync(h, b.totals, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    for (int a = 0; a < 3; ++a) {
+        const long long rlo = (long long)(k0 - g.kr) * g.ny, rhi = (long long)(k1 - g.kr) * g.ny;
+        if (rlo > 0) {
+            ISO_CUDA(ctx, cudaMemcpyAsync(h + 3 + a, b.starts + (long long)a * g.R + rlo, sizeof(unsigned long long),
+                                          cudaMemcpyDeviceToHost, s));
+        }
+        if (k1 < g.nz) {
+            ISO_CUDA(ctx, cudaMemcpyAsync(h + 6 + a, b.starts + (long long)a * g.R + rhi, sizeof(unsigned long long),
+                                          cudaMemcpyDeviceToHost, s));
+        }
+    }
+    ISO_CUDA(ctx, cudaStreamSynchronize(s));
+    for (int a = 0; a < 3; ++a) {
+        c.tot[a] = h[a];
+        c.lo[a] = k0 - g.kr > 0 ? h[3 + a] : 0;
+        c.hi[a] = k1 < g.nz ? h[6 + a] : h[a];
+    }
+    return ISO_OK;
+}
+
+iso_status slab_prepare(iso_ctx* ctx, iso_algorithm algo, const float* volume, const iso_grid* grid, int64_t k0,
+                        int64_t k1, Grid& g, Plans& pl, FeBuffers& b, cudaStream_t s)
+{
+    if (!ctx || !grid) return ISO_ERR_INVALID_ARG;
+    if (algo != ISO_FLYING_EDGES && algo != ISO_MARCHING_CUBES) return ISO_ERR_INVALID_ARG;
+    if (!slab_grid(grid, algo, k0, k1, g)) return ISO_ERR_INVALID_ARG;
+    if (empty_grid(g)) return ISO_OK;
+    if (!volume) return ISO_ERR_INVALID_ARG;
+    ISO_CUDA(ctx, cudaSetDevice(ctx->device));
+    pl = make_plans(ctx, g);
+    if (!pl.gp.fits) {
+        ctx->last_error = "slabs need rows of at most 1024 points";
+        return ISO_ERR_INVALID_ARG;
+    }
+    return ensure_scratch(ctx, g, pl.cp, b, s);
+}
+
 }  // namespace
 
 extern "C" {
+
+iso_status iso_count_slab(iso_ctx* ctx, iso_algorithm algo, const float* volume, const iso_grid* grid, int64_t k0,
+                          int64_t k1, float isoval, int64_t* n_points, int64_t* n_tris, void* stream)
+{
+    if (!n_points || !n_tris) return ISO_ERR_INVALID_ARG;
+    *n_points = *n_tris = 0;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    Grid g;
+    Plans pl;
+    FeBuffers b;
+    iso_status st = slab_prepare(ctx, algo, volume, grid, k0, k1, g, pl, b, s);
+    if (st != ISO_OK || empty_grid(g)) return st;
+    SlabCounts c;
+    st = slab_count(ctx, algo, volume, g, k0, k1, isoval, pl, b, s, c);
+    if (st != ISO_OK) return st;
+    const int av = algo == ISO_MARCHING_CUBES ? 2 : 0;
+    *n_points = (int64_t)(c.hi[av] - c.lo[av]);
+    *n_tris = (int64_t)(c.hi[1] - c.lo[1]);
+    return ISO_OK;
+}
+
+iso_status iso_extract_slab(iso_ctx* ctx, iso_algorithm algo, const float* volume, const iso_grid* grid, int64_t k0,
+                            int64_t k1, float isoval, int64_t point_offset, int64_t tri_offset, iso_mesh* out,
+                            void* stream)
+{
+    iso_status st = check_mesh(out);
+    if (st != ISO_OK) return st;
+    out->n_points = out->n_tris = 0;
+    if (point_offset < 0 || tri_offset < 0) return ISO_ERR_INVALID_ARG;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    Grid g;
+    Plans pl;
+    FeBuffers b;
+    st = slab_prepare(ctx, algo, volume, grid, k0, k1, g, pl, b, s);
+    if (st != ISO_OK || empty_grid(g)) return st;
+    SlabCounts c;
+    st = slab_count(ctx, algo, volume, g, k0, k1, isoval, pl, b, s, c);
+    if (st != ISO_OK) return st;
+    const bool mc = algo == ISO_MARCHING_CUBES;
+    const long long V = (long long)(c.hi[mc ? 2 : 0] - c.lo[mc ? 2 : 0]), T = (long long)(c.hi[1] - c.lo[1]);
+    out->n_points = V;
+    out->n_tris = T;
+    // the largest vertex id the slab's triangles reference
+    const long long top = point_offset + (mc ? V : (long long)c.tot[0]);
+    if (out->index_bytes == 4 && top > 0xffffffffll) {
+        ctx->last_error = "more than 2^32-1 vertices: use 64-bit indices";
+        return ISO_ERR_OVERFLOW;
+    }
+    if (V > out->cap_points || T > out->cap_tris) {
+        ctx->last_error = "output buffers too small";
+        return ISO_ERR_CAPACITY;
+    }
+    if (mc) {
+        st = ensure_fe2mc(ctx, (long long)c.tot[0], s);
+        if (st != ISO_OK) return st;
+        b.fe2mc = ctx->fe2mc;
+    }
+    iso::GenPlan gp = pl.gp;
+    gp.vbase = (unsigned long long)point_offset;
+    gp.tbase = (unsigned long long)tri_offset;
+    gp.add[0] = mc ? 0ull : (unsigned long long)point_offset - c.lo[0];
+    gp.add[1] = (unsigned long long)tri_offset - c.lo[1];
+    gp.add[2] = (unsigned long long)point_offset - c.lo[2];
+    const long long big = 1ll << 62;  // capacities were checked above
+    const bool i4 = out->index_bytes == 4;
+    PassMarks pm(ctx, s);
+    if (!mc) {
+        gp.kbeg = (int)k0;
+        gp.kend = (int)k1;
+        gp.kemit = (int)k0;
+        iso::gen_split(gp, ctx->nsm);
+        if (i4)
+            iso::launch_fe_gen_warps<uint32_t>(volume, g, isoval, ctx->d_cases, b, pl.cp, gp, big, big, out->points,
+                                               out->normals, static_cast<uint32_t*>(out->tris), ctx->reverse, s);
+        else
+            iso::launch_fe_gen_warps<uint64_t>(volume, g, isoval, ctx->d_cases, b, pl.cp, gp, big, big, out->points,
+                                               out->normals, static_cast<uint64_t*>(out->tris), ctx->reverse, s);
+        pm.mark(ISO_PASS_FE_GENERATE);
+    } else {
+        gp.kbeg = g.kr;  // cell row k0-1 maps the edges it owns on plane k0
+        gp.kend = (int)k1;
+        gp.kemit = (int)k0;
+        iso::gen_split(gp, ctx->nsm);
+        iso::launch_mc_gen_warps(volume, g, isoval, ctx->d_cases, b, pl.cp, gp, big, big, out->points, out->normals,
+                                 ctx->reverse, s);
+        pm.mark(ISO_PASS_MC_VERTICES);
+        gp.kbeg = (int)k0;
+        iso::gen_split(gp, ctx->nsm);
+        if (i4)
+            iso::launch_mc_tri_warps<uint32_t>(g, ctx->d_cases, b, pl.cp, gp, big, big,
+                                               static_cast<uint32_t*>(out->tris), s);
+        else
+            iso::launch_mc_tri_warps<uint64_t>(g, ctx->d_cases, b, pl.cp, gp, big, big,
+                                               static_cast<uint64_t*>(out->tris), s);
+        pm.mark(ISO_PASS_MC_TRIANGLES);
+    }
+    ISO_CUDA(ctx, cudaGetLastError());
+    ISO_CUDA(ctx, cudaStreamSynchronize(s));
+    return ISO_OK;
+}
+
 
 const char* iso_status_string(iso_status s)
 {
@@ -400,6 +578,7 @@ iso_status iso_ctx_destroy(iso_ctx* ctx)
     cudaFree(ctx->d_normals);
     cudaFree(ctx->d_tris);
     if (ctx->h_totals) cudaFreeHost(ctx->h_totals);
+    if (ctx->h_slab) cudaFreeHost(ctx->h_slab);
     for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
     delete ctx;
     return ISO_OK;

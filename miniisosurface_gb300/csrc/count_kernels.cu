@@ -166,11 +166,11 @@ __global__ void __launch_bounds__(kThreads) k_count_warps(const float* __restric
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int j = jb * kCountRows + warp;
     if (j >= g.ny) return;
-    const int kb = kc * KC, ke = min(kb + KC, g.nz);
+    const int kb = g.kr + kc * KC, ke = min(kb + KC, g.ke);
     const bool hasY = j < g.ny - 1;
     const int jy = hasY ? j + 1 : j;  // row B (a valid address even when B does not exist)
     const int nq = g.nx >> 2;
-    auto rowptr = [&](int k, int jj) { return vol + ((long long)k * g.ny + jj) * g.nx; };
+    auto rowptr = [&](int k, int jj) { return vol + ((long long)(k - g.kd) * g.ny + jj) * g.nx; };
 
     // words of rows A = (j,k), B = (j+1,k); Cw, Dw = the same rows at plane k+1
     uint32_t A[NW], B[NW], Cw[NW], Dw[NW];
@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(kThreads) k_count_warps(const float* __restric
             for (int q = 0; q < NW; ++q) Cw[q] = Dw[q] = 0u;
         }
         RowCounts rc;
-        const long long r = (long long)k * g.ny + j;
+        const long long r = (long long)(k - g.kr) * g.ny + j;
 #pragma unroll
         for (int q = 0; q < NW; ++q) {
             const int w = lane + 32 * q;
@@ -291,11 +291,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_count_pairs(const float* __rest
     const int j = jw + h;
     const bool row_ok = j < g.ny;
     const int jr = row_ok ? j : jw;  // a valid row address for a half without a row
-    const int kb = kc * KC, ke = min(kb + KC, g.nz);
+    const int kb = g.kr + kc * KC, ke = min(kb + KC, g.ke);
     const bool hasY = row_ok && j < g.ny - 1;
     const int jy = hasY ? j + 1 : jr;
     const int nq = g.nx >> 2;
-    auto rowptr = [&](int k, int jj) { return vol + ((long long)k * g.ny + jj) * g.nx; };
+    auto rowptr = [&](int k, int jj) { return vol + ((long long)(k - g.kd) * g.ny + jj) * g.nx; };
 
     uint32_t A, B, Cw, Dw;
     RowVals<U> pc, pd;
@@ -333,7 +333,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_count_pairs(const float* __rest
         rw.csh = (rw.c >> 1) | ((nxt ? cn : 0u) << 31);
         rw.dsh = (rw.d >> 1) | ((nxt ? dn : 0u) << 31);
         if (row_ok) count_word<MC>(rw, l16, g, j, k, hasY, hasZ, s_ntris, s_cut, rc);
-        const long long r = (long long)k * g.ny + j;
+        const long long r = (long long)(k - g.kr) * g.ny + j;
         if (row_ok && l16 < g.W) bits_out[r * g.W + l16] = rw.a;
         // both rows' totals at once: row h in bits 16h .. 16h+15 (each below 2^16)
         const int sh = 16 * h;
@@ -393,16 +393,16 @@ __global__ void __launch_bounds__(kThreads) k_count_wide(const float* __restrict
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int j = jb * kCountRows + warp;
     if (j >= g.ny) return;
-    const int kb = kc * KC, ke = min(kb + KC, g.nz);
+    const int kb = g.kr + kc * KC, ke = min(kb + KC, g.ke);
     const bool hasY = j < g.ny - 1;
     const int jy = hasY ? j + 1 : j;
     const int nchunks = (g.W + 31) / 32;
-    auto rowptr = [&](int k, int jj) { return vol + ((long long)k * g.ny + jj) * g.nx; };
+    auto rowptr = [&](int k, int jj) { return vol + ((long long)(k - g.kd) * g.ny + jj) * g.nx; };
     for (int k = kb; k < ke; ++k) {
         const bool hasZ = k + 1 < g.nz;
         const int kz = hasZ ? k + 1 : k;
         RowCounts rc;
-        const long long r = (long long)k * g.ny + j;
+        const long long r = (long long)(k - g.kr) * g.ny + j;
         for (int c = 0; c < nchunks; ++c) {
             RowWords rw;
             uint32_t na, nb, nc, nd;
@@ -565,13 +565,15 @@ CountPlan count_plan(const Grid& g, int nsm)
     p.vec_u = 1;
     while (p.vec_u * 128 < g.nx) p.vec_u <<= 1;  // float4 per lane for one row
     // ~8 CTAs per SM in total, at least 8 planes per column
+    const int nzw = g.ke - g.kr;  // planes of the window
     const long long target = (long long)nsm * 8;
     int nkc = (int)((target + p.nyb - 1) / p.nyb);
     if (nkc < 1) nkc = 1;
-    p.KC = (g.nz + nkc - 1) / nkc;
+    p.KC = (nzw + nkc - 1) / nkc;
     if (p.KC < 8) p.KC = 8;
-    if (p.KC > g.nz) p.KC = g.nz;
-    p.nkc = (g.nz + p.KC - 1) / p.KC;
+    if (p.KC > nzw) p.KC = nzw;
+    if (p.KC < 1) p.KC = 1;
+    p.nkc = (nzw + p.KC - 1) / p.KC;
     p.nseg = (int)((g.R + kSeg - 1) / kSeg);
     return p;
 }
@@ -644,6 +646,8 @@ RowStarts row_starts(const Grid& g, const CountPlan& p, const FeBuffers& b)
     rs.starts = b.starts;
     rs.R = g.R;
     rs.ny = g.ny;
+    rs.kr = g.kr;
+    rs.add[0] = rs.add[1] = rs.add[2] = 0;
     return rs;
 }
 

@@ -32,6 +32,7 @@
 //         (marchingCubes/serial/main.cpp:139-177), one per lane, and that map.
 #pragma once
 #include <cmath>
+#include <type_traits>
 
 #include "iso_device.cuh"
 #include "iso_kernels.h"
@@ -44,6 +45,7 @@ constexpr int kGenPrefetch = 3;   // planes of L2 prefetch ahead of the step
 constexpr int kGenCells = 32;  // cells per batch
 constexpr int kGenTris = 5 * kGenCells;    // triangles of a batch, at most
 constexpr int kGenOwned = 12 * kGenCells;  // MC vertices owned by a batch, at most
+constexpr int kGenVq = 64;                 // FE vertex queue per axis and warp (a ring of two batches)
 enum GenMode { kGenFE = 0, kGenMC = 1, kGenTri = 2 };
 
 // Per-warp scratch in shared memory:
@@ -52,10 +54,15 @@ enum GenMode { kGenFE = 0, kGenMC = 1, kGenTri = 2 };
 //   cell[32]   the batch's active cells: i | cube case << 16
 //   list[...]  FE / TRI: the batch's triangles, cell | triangle << 5 (u8);
 //              MC: the batch's owned vertices, cell | cube edge << 5 (u16)
+//   FE: vertex queues per axis (rings of kGenVq): ids (u64), then i | k << 10
+__host__ __device__ inline size_t gen_list_bytes(int mode)
+{
+    return mode == kGenMC ? (size_t)kGenOwned * 2 : (size_t)kGenTris;
+}
 __host__ __device__ inline size_t gen_warp_scratch_bytes(int W, int mode)
 {
-    const size_t list = mode == kGenMC ? (size_t)kGenOwned * 2 : (size_t)kGenTris;
-    return ((size_t)8 * W * 8 + kGenCells * 4 + list + 15) & ~(size_t)15;
+    const size_t vq = mode == kGenFE ? (size_t)3 * kGenVq * 12 : 0;
+    return ((size_t)8 * W * 8 + kGenCells * 4 + gen_list_bytes(mode) + vq + 15) & ~(size_t)15;
 }
 
 // Divisors of the gradient: the reference divides by the spacing (one-sided
@@ -164,6 +171,69 @@ __device__ __forceinline__ void vertex_on_edge(const Planes& pl, const Grid& g, 
     nrm.z = axis == 2 ? ga : (axis == 0 ? gc : gb);
 }
 
+// Gradient components at one point from its six neighbours (grad_component
+// of iso_device.cuh per axis).
+__device__ __forceinline__ float3 grad3(float xm, float xp, float ym, float yp, float zm, float zp, float here, int i,
+                                        int j, int kk, const Grid& g, const GradScale& gs)
+{
+    return make_float3(grad_axis(xm, here, xp, i, g.nx, 0, gs), grad_axis(ym, here, yp, j, g.ny, 1, gs),
+                       grad_axis(zm, here, zp, kk, g.nz, 2, gs));
+}
+
+// edge_vertex() of iso_device.cuh for a Flying Edges edge along the fixed
+// axis A from P0 = (i, j, kk), values read from the volume: planes kk-1 ..
+// kk+2 as lo, at, hi, hi2, each addressed from row jlo (planes outside the
+// grid alias a valid one and are not read).  The cube base is the edge's own
+// index along A and the clamped one (n-2) across, the cube that owns the
+// edge in Image3D::getPosCube terms.
+template <int A>
+__device__ __forceinline__ void vertex_axis(const float* lo, const float* at, const float* hi, const float* hi2,
+                                            int jlo, const Grid& g, const GradScale& gs, float iso, int i, int j,
+                                            int kk, float3& pos, float3& nrm)
+{
+    const int nx = g.nx;
+    const int o = (j - jlo) * nx + i;
+    const bool xl = i > 0, yl = j > 0, zl = kk > 0;
+    const bool xh = i < g.nx - 1, yh = j < g.ny - 1, zh = kk < g.nz - 1;
+    const float v0 = __ldg(at + o);
+    float v1;
+    float3 g0, g1;
+    if constexpr (A == 0) {
+        const int o1 = o + 1;
+        v1 = __ldg(at + o1);
+        g0 = grad3(xl ? __ldg(at + o - 1) : 0.f, v1, yl ? __ldg(at + o - nx) : 0.f, yh ? __ldg(at + o + nx) : 0.f,
+                   zl ? __ldg(lo + o) : 0.f, zh ? __ldg(hi + o) : 0.f, v0, i, j, kk, g, gs);
+        g1 = grad3(v0, i + 1 < g.nx - 1 ? __ldg(at + o1 + 1) : 0.f, yl ? __ldg(at + o1 - nx) : 0.f,
+                   yh ? __ldg(at + o1 + nx) : 0.f, zl ? __ldg(lo + o1) : 0.f, zh ? __ldg(hi + o1) : 0.f, v1, i + 1,
+                   j, kk, g, gs);
+    } else if constexpr (A == 1) {
+        const int o1 = o + nx;
+        v1 = __ldg(at + o1);
+        g0 = grad3(xl ? __ldg(at + o - 1) : 0.f, xh ? __ldg(at + o + 1) : 0.f, yl ? __ldg(at + o - nx) : 0.f, v1,
+                   zl ? __ldg(lo + o) : 0.f, zh ? __ldg(hi + o) : 0.f, v0, i, j, kk, g, gs);
+        g1 = grad3(xl ? __ldg(at + o1 - 1) : 0.f, xh ? __ldg(at + o1 + 1) : 0.f, v0,
+                   j + 1 < g.ny - 1 ? __ldg(at + o1 + nx) : 0.f, zl ? __ldg(lo + o1) : 0.f,
+                   zh ? __ldg(hi + o1) : 0.f, v1, i, j + 1, kk, g, gs);
+    } else {
+        v1 = __ldg(hi + o);
+        g0 = grad3(xl ? __ldg(at + o - 1) : 0.f, xh ? __ldg(at + o + 1) : 0.f, yl ? __ldg(at + o - nx) : 0.f,
+                   yh ? __ldg(at + o + nx) : 0.f, zl ? __ldg(lo + o) : 0.f, v1, v0, i, j, kk, g, gs);
+        g1 = grad3(xl ? __ldg(hi + o - 1) : 0.f, xh ? __ldg(hi + o + 1) : 0.f, yl ? __ldg(hi + o - nx) : 0.f,
+                   yh ? __ldg(hi + o + nx) : 0.f, v0, kk + 1 < g.nz - 1 ? __ldg(hi2 + o) : 0.f, v1, i, j, kk + 1, g,
+                   gs);
+    }
+    const float w = fdiv(fsub(iso, v0), fsub(v1, v0));
+    const int ci = A == 0 ? i : min(i, g.nx - 2), cj = A == 1 ? j : min(j, g.ny - 2);
+    const int ck = A == 2 ? kk : min(kk, g.nz - 2);
+    const int i1 = i + (A == 0), j1 = j + (A == 1), k1 = kk + (A == 2);
+    pos.x = lerp_ref(cube_coord(ci, i - ci, g.zp[0], g.sp[0]), cube_coord(ci, i1 - ci, g.zp[0], g.sp[0]), w);
+    pos.y = lerp_ref(cube_coord(cj, j - cj, g.zp[1], g.sp[1]), cube_coord(cj, j1 - cj, g.zp[1], g.sp[1]), w);
+    pos.z = lerp_ref(cube_coord(ck, kk - ck, g.zp[2], g.sp[2]), cube_coord(ck, k1 - ck, g.zp[2], g.sp[2]), w);
+    nrm.x = lerp_ref(g0.x, g1.x, w);
+    nrm.y = lerp_ref(g0.y, g1.y, w);
+    nrm.z = lerp_ref(g0.z, g1.z, w);
+}
+
 __device__ __forceinline__ void store_vertex(float* __restrict__ points, float* __restrict__ normals,
                                              unsigned long long id, const float3& p, const float3& n)
 {
@@ -202,7 +272,8 @@ __device__ __forceinline__ uint32_t fe_edge_rel(const uint2* mb, int W, int e, i
 template <int MODE, typename IndexT, bool BULK>
 __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
     const float* __restrict__ vol, const uint32_t* __restrict__ bits, Grid g, GradScale gs, float iso, int KC,
-    int nyb, int ws_bytes, const CaseTables* __restrict__ cases, const uint4* __restrict__ rowcnt, RowStarts rs,
+    int nyb, int kbeg, int kend, int kemit, unsigned long long vbase, unsigned long long tbase, int ws_bytes,
+    const CaseTables* __restrict__ cases, const uint4* __restrict__ rowcnt, RowStarts rs,
     unsigned long long* __restrict__ totals, long long capV, long long capT, float* __restrict__ points,
     float* __restrict__ normals, IndexT* __restrict__ tris, uint32_t* __restrict__ fe2mc, int reverse)
 {
@@ -217,6 +288,8 @@ __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
     uint2* mb = reinterpret_cast<uint2*>(ws);
     uint32_t* cell = reinterpret_cast<uint32_t*>(ws + (size_t)8 * W * 8);
     unsigned char* list = ws + (size_t)8 * W * 8 + kGenCells * 4;
+    unsigned long long* vq_id = reinterpret_cast<unsigned long long*>(list + gen_list_bytes(MODE));
+    uint32_t* vq_pos = reinterpret_cast<uint32_t*>(vq_id + 3 * kGenVq);
     for (int c = tid; c < 256; c += kThreads) {
         if (MODE == kGenMC) {
             s_order[c] = cases->order[c];
@@ -232,19 +305,20 @@ __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
     const int jb = blockIdx.x % nyb;
     const int kc = reverse ? nkc - 1 - (int)(blockIdx.x / nyb) : (int)(blockIdx.x / nyb);
     const int j0 = jb * kGenRows;
-    const int kb = kc * KC, ke = min(kb + KC, g.nz);
+    const int kb = kbeg + kc * KC, ke = min(kb + KC, kend);
     const int j = j0 + warp;
     if (j >= g.ny) return;
     const int jlo = j0 > 0 ? j0 - 1 : 0;  // planes are addressed from this row
     const long long plane = (long long)g.ny * g.nx;
-    auto plane_ptr = [&](int p) { return vol + (long long)p * plane + (long long)jlo * g.nx; };
+    auto plane_ptr = [&](int p) { return vol + (long long)(p - g.kd) * plane + (long long)jlo * g.nx; };
+    const int plast = min(g.ke, g.nz - 1);  // last plane held by vol
 
     // L2 prefetch (TMA bulk prefetch when rows are 16-byte aligned) of this
     // warp's rows j, j+1 of plane p, kGenPrefetch planes ahead of use.
     const bool hasY = j < g.ny - 1;
     auto prefetch_plane = [&](int p) {
-        if (!VOL || p >= g.nz) return;
-        const float* r0 = vol + (long long)p * plane + (long long)j * g.nx;
+        if (!VOL || p > plast || p < g.kd) return;
+        const float* r0 = vol + (long long)(p - g.kd) * plane + (long long)j * g.nx;
         const int nrows = hasY ? 2 : 1;
         if (BULK) {
             if (lane == 0) bulk_prefetch_l2(r0, (unsigned)(nrows * g.nx * 4));
@@ -252,9 +326,7 @@ __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
             for (int q = lane * 32; q < nrows * g.nx; q += 32 * 32) prefetch_l2_line(r0 + q);
         }
     };
-    for (int p = kb - 1; p < kb + kGenPrefetch; ++p) {
-        if (p >= 0) prefetch_plane(p);
-    }
+    for (int p = kb - 1; p < kb + kGenPrefetch; ++p) prefetch_plane(p);
 
     const bool in = lane < W, in1 = lane + 1 < W;
     const uint32_t evalid = validmask(lane, g.nx - 1);  // x-edges / cells: i <= nx-2
@@ -262,8 +334,8 @@ __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
 
     // Bit words of rows (j, p) and (j+1, p).
     auto load_words = [&](int p, uint32_t& wa, uint32_t& wb) {
-        const bool okp = p < g.nz;
-        const long long r = (long long)p * g.ny + j;
+        const bool okp = p < g.ke;  // rows of the window
+        const long long r = (long long)(p - g.kr) * g.ny + j;
         wa = (in && okp) ? __ldg(&bits[r * W + lane]) : 0u;
         wb = (in && okp && hasY) ? __ldg(&bits[(r + 1) * W + lane]) : 0u;
     };
@@ -273,12 +345,12 @@ __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
     // cuts of row B.
     auto load_starts = [&](int p) -> unsigned long long {
         const int dk = (lane >> 1) & 1, dj = lane & 1;
-        const bool hasZp = p + 1 < g.nz;
+        const bool hasZp = p + 1 < g.ke;
         bool ok = lane < 6;
         if (lane < 4) ok = ok && (dj == 0 || hasY) && (dk == 0 || hasZp);
         if (lane == 5) ok = ok && hasY;
         if (!ok) return 0ull;
-        const long long rA = (long long)p * g.ny + j;
+        const long long rA = (long long)(p - g.kr) * g.ny + j;
         if (lane == 5) {
             const uint2 c = __ldg(reinterpret_cast<const uint2*>(&rowcnt[rA + 1]));
             return (unsigned long long)c.x + c.y;
@@ -292,7 +364,65 @@ __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
     load_words(kb + 1, wC, wD);
     unsigned long long st = load_starts(kb);
 
-    for (int k = kb; k < ke; ++k) {
+    // FE vertex queues: ring heads and fill per axis (warp-uniform)
+    uint32_t vh0 = 0, vh1 = 0, vh2 = 0, vn0 = 0, vn1 = 0, vn2 = 0;
+    // (copied in and out by value: a reference would put them in local memory)
+    auto vq_get = [&](auto axis_tag, uint32_t& head, uint32_t& cnt) {
+        constexpr int A = decltype(axis_tag)::value;
+        if constexpr (A == 0) {
+            head = vh0;
+            cnt = vn0;
+        } else if constexpr (A == 1) {
+            head = vh1;
+            cnt = vn1;
+        } else {
+            head = vh2;
+            cnt = vn2;
+        }
+    };
+    auto vq_set = [&](auto axis_tag, uint32_t head, uint32_t cnt) {
+        constexpr int A = decltype(axis_tag)::value;
+        if constexpr (A == 0) {
+            vh0 = head;
+            vn0 = cnt;
+        } else if constexpr (A == 1) {
+            vh1 = head;
+            vn1 = cnt;
+        } else {
+            vh2 = head;
+            vn2 = cnt;
+        }
+    };
+    // Vertex batches of axis A from the queue: full ones, or all that is left
+    // at the end.  Each lane computes one vertex with the axis-A code.
+    auto drain = [&](auto axis_tag, bool all) {
+        constexpr int A = decltype(axis_tag)::value;
+        uint32_t head, cnt;
+        vq_get(axis_tag, head, cnt);
+        while (cnt >= 32u || (all && cnt > 0u)) {
+            const uint32_t nb = min(cnt, 32u);
+            if ((uint32_t)lane < nb) {
+                const uint32_t slot = A * kGenVq + ((head + lane) & (kGenVq - 1));
+                const uint32_t pos = vq_pos[slot];
+                const int i = (int)(pos & 1023u), kk = (int)(pos >> 10);
+                const float* at = plane_ptr(kk);
+                const float* lo = kk > 0 ? plane_ptr(kk - 1) : at;
+                const float* hi = kk + 1 < g.nz ? plane_ptr(kk + 1) : at;
+                const float* hi2 = kk + 2 < g.nz ? plane_ptr(kk + 2) : hi;
+                float3 p, n;
+                vertex_axis<A>(lo, at, hi, hi2, jlo, g, gs, iso, i, j, kk, p, n);
+                store_vertex(points, normals, vq_id[slot] - vbase, p, n);
+            }
+            head = (head + nb) & (kGenVq - 1);
+            cnt -= nb;
+        }
+        vq_set(axis_tag, head, cnt);
+    };
+
+    // One step past the column (fin): no row, the queued vertices are drained
+    // (one drain site per axis keeps the kernel's code small).
+    for (int k = kb; k <= ke; ++k) {
+        const bool fin = k == ke;
         const bool hasZ = k + 1 < g.nz;
         prefetch_plane(k + kGenPrefetch);
         // the next step's words and starts, in flight while this step runs
@@ -304,10 +434,10 @@ __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
         }
         const bool cellrow = hasY && hasZ;
         RowWords rw;
-        rw.a = wA;
-        rw.b = wB;
-        rw.c = hasZ ? wC : 0u;
-        rw.d = cellrow ? wD : 0u;
+        rw.a = fin ? 0u : wA;
+        rw.b = fin ? 0u : wB;
+        rw.c = hasZ && !fin ? wC : 0u;
+        rw.d = cellrow && !fin ? wD : 0u;
         const uint32_t an = __shfl_down_sync(0xffffffffu, rw.a, 1);
         const uint32_t bn = __shfl_down_sync(0xffffffffu, rw.b, 1);
         const uint32_t cn = __shfl_down_sync(0xffffffffu, rw.c, 1);
@@ -346,7 +476,7 @@ __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
         }
         __syncwarp();
         Planes pl{};
-        if (VOL) {  // planes k-1 .. k+2; those outside the grid alias plane k
+        if (MODE == kGenMC) {  // planes k-1 .. k+2; those outside the grid alias plane k
             pl.p1 = plane_ptr(k);
             pl.p0 = k > 0 ? plane_ptr(k - 1) : pl.p1;
             pl.p2 = hasZ ? plane_ptr(k + 1) : pl.p1;
@@ -358,10 +488,9 @@ __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
         if (MODE == kGenFE) {
             // ---- vertices of grid row (j, k): x, y then z sections
             const uint32_t nv = nxA + nyA + nzA;
-            const int ck = min(k, g.nz - 2), cj = min(j, g.ny - 2);
             // word prefixes of the x, y and z sections in one word: 10 + 11 + 11 bits
             const uint32_t P = (e0 & 0x3ffu) | ((e2 & 0x7ffu) << 10) | ((e3 & 0x7ffu) << 21);
-            for (uint32_t v0 = 0; v0 < nv; v0 += 32) {
+            for (uint32_t v0 = 0; v0 < nv || (fin && v0 == 0); v0 += 32) {
                 const uint32_t v = v0 + lane;
                 const int axis = v < nxA ? 0 : (v < nxA + nyA ? 1 : 2);
                 const uint32_t r = v - (axis == 0 ? 0u : (axis == 1 ? nxA : nxA + nyA));
@@ -374,15 +503,34 @@ __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
                     const uint32_t pv = (__shfl_sync(0xffffffffu, P, mid & 31) >> sh) & fm;
                     if (mid < W && pv <= r) lo = mid;
                 }
+                int i = 0;
                 if (v < nv) {
                     const uint2 e = mb[(axis == 0 ? 0 : (axis == 1 ? 4 : 6)) * W + lo];
-                    const int bit = (int)__fns(e.x, 0, (int)(v - e.y) + 1);
-                    const int i = 32 * lo + bit;
-                    float3 p, n;
-                    vertex_on_edge(pl, g, gs, iso, axis, i, j, 1, k, axis == 0 ? i : min(i, g.nx - 2),
-                                   axis == 1 ? j : cj, axis == 2 ? k : ck, p, n);
-                    store_vertex(points, normals, xsA + v, p, n);
+                    i = 32 * lo + (int)__fns(e.x, 0, (int)(v - e.y) + 1);
                 }
+                // append to the axis queues (each had < 32 entries: room for 32 more)
+                auto append = [&](auto axis_tag) {
+                    constexpr int a = decltype(axis_tag)::value;
+                    const bool mine = v < nv && axis == a;
+                    const uint32_t ball = __ballot_sync(0xffffffffu, mine);
+                    uint32_t head, cnt;
+                    vq_get(axis_tag, head, cnt);
+                    if (mine) {
+                        const uint32_t slot =
+                            a * kGenVq + ((head + cnt + __popc(ball & ((1u << lane) - 1u))) & (kGenVq - 1));
+                        vq_id[slot] = xsA + v;
+                        vq_pos[slot] = (uint32_t)i | ((uint32_t)k << 10);
+                    }
+                    vq_set(axis_tag, head, cnt + __popc(ball));
+                };
+                append(std::integral_constant<int, 0>());
+                append(std::integral_constant<int, 1>());
+                append(std::integral_constant<int, 2>());
+                __syncwarp();
+                drain(std::integral_constant<int, 0>(), fin);
+                drain(std::integral_constant<int, 1>(), fin);
+                drain(std::integral_constant<int, 2>(), fin);
+                __syncwarp();
             }
         }
         if (cellrow) {
@@ -420,7 +568,7 @@ __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
                             const int ci = (int)(cr & 0xffffu);
                             const uint64_t tl = s_tris[cr >> 16];
                             const int w = ci >> 5, bit = ci & 31;
-                            IndexT* o = tris + 3 * (tcur + t);
+                            IndexT* o = tris + 3 * (tcur + t - tbase);
 #pragma unroll
                             for (int c = 0; c < 3; ++c) {
                                 const unsigned long long id =
@@ -455,12 +603,14 @@ __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
                             const uint32_t cr = cell[vr & 31u];
                             const int e12 = (int)(vr >> 5);
                             const int i = (int)(cr & 0xffffu);
-                            int dx, dy, dz, axis;
-                            cube_edge_geometry(e12, dx, dy, dz, axis);
-                            float3 p, n;
-                            vertex_on_edge(pl, g, gs, iso, axis, i + dx, j + dy, 1 + dz, k + dz, i, j, k, p, n);
                             const unsigned long long id = tcur + v;
-                            store_vertex(points, normals, id, p, n);
+                            if (k >= kemit) {  // cell rows below kemit belong to the slab below: map only
+                                int dx, dy, dz, axis;
+                                cube_edge_geometry(e12, dx, dy, dz, axis);
+                                float3 p, n;
+                                vertex_on_edge(pl, g, gs, iso, axis, i + dx, j + dy, 1 + dz, k + dz, i, j, k, p, n);
+                                store_vertex(points, normals, id - vbase, p, n);
+                            }
                             fe2mc[xsA + fe_edge_rel(mb, W, e12, i >> 5, i & 31)] = (uint32_t)id;
                         }
                     }
@@ -483,15 +633,17 @@ void launch_gen_warps_impl(const float* vol, const Grid& g, float iso, const Cas
                            const CountPlan& cp, const GenPlan& p, long long capV, long long capT, float* points,
                            float* normals, IndexT* tris, int reverse, cudaStream_t s)
 {
-    const RowStarts rs = row_starts(g, cp, b);
+    RowStarts rs = row_starts(g, cp, b);
+    for (int a = 0; a < 3; ++a) rs.add[a] = p.add[a];
     const bool bulk = MODE != kGenTri && (g.nx % 4 == 0) && ((reinterpret_cast<uintptr_t>(vol) & 15) == 0);
     const unsigned blocks = (unsigned)(p.nyb * p.nkc);
     const int ws_bytes = (int)gen_warp_scratch_bytes(g.W, MODE);
     const size_t smem = (size_t)kGenRows * ws_bytes;
     auto kern = bulk ? k_gen_warps<MODE, IndexT, true> : k_gen_warps<MODE, IndexT, false>;
     allow_smem(kern, smem);
-    kern<<<blocks, kThreads, smem, s>>>(vol, b.bits, g, make_grad_scale(g), iso, p.KC, p.nyb, ws_bytes, cases,
-                                        b.rowcnt, rs, b.totals, capV, capT, points, normals, tris, b.fe2mc, reverse);
+    kern<<<blocks, kThreads, smem, s>>>(vol, b.bits, g, make_grad_scale(g), iso, p.KC, p.nyb, p.kbeg, p.kend, p.kemit,
+                                        p.vbase, p.tbase, ws_bytes, cases, b.rowcnt, rs, b.totals, capV, capT, points,
+                                        normals, tris, b.fe2mc, reverse);
 }
 
 }  // namespace iso

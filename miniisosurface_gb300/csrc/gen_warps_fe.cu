@@ -7,6 +7,21 @@ namespace iso {
 // Warp-per-row kernels take rows of up to 32 words (1024 points) whose cell
 // rows number their vertices in 32 bits relative to the row's first one;
 // wider grids use the row-wise kernels.
+// Columns of KC planes over [kbeg, kend): about 4 waves of resident CTAs,
+// at least 4 planes per column.
+void gen_split(GenPlan& p, int nsm)
+{
+    const int nzw = p.kend - p.kbeg;
+    const long long resident = (long long)nsm * kGenCtasPerSm;
+    int nkc = (int)((4 * resident + p.nyb - 1) / p.nyb);
+    if (nkc < 1) nkc = 1;
+    p.KC = (nzw + nkc - 1) / nkc;
+    if (p.KC < 4) p.KC = 4;
+    if (p.KC > nzw) p.KC = nzw;
+    if (p.KC < 1) p.KC = 1;
+    p.nkc = nzw > 0 ? (nzw + p.KC - 1) / p.KC : 0;
+}
+
 GenPlan gen_plan(const Grid& g, int nsm)
 {
     GenPlan p;
@@ -14,15 +29,11 @@ GenPlan gen_plan(const Grid& g, int nsm)
     p.nyb = (g.ny + p.J - 1) / p.J;
     p.smem = (size_t)kGenRows * gen_warp_scratch_bytes(g.W, kGenMC);
     const bool rel32 = 6.0 * g.nx * g.ny < 4294967295.0;  // two planes of vertices
-    p.fits = g.W <= 32 && rel32;
-    // about 4 waves of resident CTAs, at least 4 planes per column
-    const long long resident = (long long)nsm * kGenCtasPerSm;
-    int nkc = (int)((4 * resident + p.nyb - 1) / p.nyb);
-    if (nkc < 1) nkc = 1;
-    p.KC = (g.nz + nkc - 1) / nkc;
-    if (p.KC < 4) p.KC = 4;
-    if (p.KC > g.nz) p.KC = g.nz;
-    p.nkc = (g.nz + p.KC - 1) / p.KC;
+    p.fits = g.W <= 32 && rel32 && g.nz < (1 << 22);  // queued vertices pack i | k << 10
+    p.kbeg = g.kr;
+    p.kend = g.ke;
+    p.kemit = g.kr;
+    gen_split(p, nsm);
     return p;
 }
 

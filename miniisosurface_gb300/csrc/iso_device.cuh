@@ -29,8 +29,12 @@ constexpr int kThreads = 256;      // threads per CTA of the row kernels
 struct Grid {
     int nx, ny, nz;
     int W;                 // 32-bit words per bit row
-    long long R;           // grid rows = ny*nz
+    long long R;           // grid rows of the window = ny * (ke - kr)
     float sp[3], zp[3];
+    // z window (a slab of a decomposition; the whole grid by default): the
+    // volume pointer holds planes from kd on, the per-row scratch covers
+    // planes [kr, ke), row (j, k) at index (k - kr) * ny + j.
+    int kd, kr, ke;
 };
 
 // Per-case data derived from the packed triangle table when a context is
@@ -549,17 +553,20 @@ __device__ __forceinline__ void slab_copy(float* dst, const float* src, int nfl,
 
 // First vertex (comp 0), triangle (1) or MC vertex (2) of grid row r =
 // k*ny + j, from the scanned starts[3][R].
+// Window row r (see Grid); add[comp] shifts the window's numbering to the
+// whole volume's (slabs).
 struct RowStarts {
     const unsigned long long* starts;
     long long R;
-    int ny;
+    int ny, kr;
+    unsigned long long add[3];
     __device__ __forceinline__ unsigned long long get(long long r, int comp) const
     {
-        return __ldg(&starts[comp * R + r]);
+        return __ldg(&starts[comp * R + r]) + add[comp];
     }
     __device__ __forceinline__ unsigned long long get(int k, int j, int comp) const
     {
-        return get((long long)k * ny + j, comp);
+        return get((long long)(k - kr) * ny + j, comp);
     }
 };
 

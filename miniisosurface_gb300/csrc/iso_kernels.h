@@ -33,9 +33,14 @@ struct CountPlan {
 };
 
 // Work split of the warp-per-row generate kernels: blocks of J = 8 rows,
-// columns of KC planes.
+// columns of KC planes over planes [kbeg, kend).  For a slab: rows below
+// kemit only map (MC), ids are shifted by add[] and stored at id - vbase
+// (vertices) and t - tbase (triangles).
 struct GenPlan {
     int J = 8, nyb = 1, KC = 1, nkc = 1;
+    int kbeg = 0, kend = 0, kemit = 0;
+    unsigned long long vbase = 0, tbase = 0;
+    unsigned long long add[3] = {0, 0, 0};
     size_t smem = 0;  // per-warp scratch of the CTA
     bool fits = false;  // false: use the row-wise kernels
 };
@@ -51,6 +56,7 @@ inline void allow_smem(K kern, size_t dyn)
 }
 CountPlan count_plan(const Grid& g, int nsm);
 GenPlan gen_plan(const Grid& g, int nsm);
+void gen_split(GenPlan& p, int nsm);  // columns over [p.kbeg, p.kend)
 
 // passes 1-3
 void launch_count(const float* vol, const Grid& g, float iso, const CaseTables* cases, bool mc,

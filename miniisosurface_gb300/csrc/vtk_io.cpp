@@ -4,34 +4,63 @@
 //   writer: util::saveTriangleMesh (flyingEdges/util/SaveTriangleMesh.h:33-118),
 //           reproduced byte for byte (big-endian floats, POLYGONS records of
 //           four 8-byte big-endian words [3, a, b, c]).
+// Byte-order conversion runs on all host threads (OpenMP); the file is read
+// and written in one block each.
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
 #include <sstream>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/miniiso.h"
 
 namespace {
 
+// Byte order: the files are big-endian, the hosts (x86-64, Arm64) little-endian.
+inline uint16_t bswap(uint16_t v) { return __builtin_bswap16(v); }
+inline uint32_t bswap(uint32_t v) { return __builtin_bswap32(v); }
+inline uint64_t bswap(uint64_t v) { return __builtin_bswap64(v); }
+
 template <typename T>
 T from_big_endian(const unsigned char* p)
 {
-    unsigned char b[sizeof(T)];
-    for (size_t q = 0; q < sizeof(T); ++q) b[q] = p[sizeof(T) - 1 - q];
+    using U = typename std::conditional<sizeof(T) == 2, uint16_t,
+                                        typename std::conditional<sizeof(T) == 4, uint32_t, uint64_t>::type>::type;
+    U u;
+    std::memcpy(&u, p, sizeof(U));
+    u = bswap(u);
     T v;
-    std::memcpy(&v, b, sizeof(T));
+    std::memcpy(&v, &u, sizeof(T));
     return v;
 }
 
 template <typename T>
 void to_big_endian(T v, unsigned char* p)
 {
-    unsigned char b[sizeof(T)];
-    std::memcpy(b, &v, sizeof(T));
-    for (size_t q = 0; q < sizeof(T); ++q) p[q] = b[sizeof(T) - 1 - q];
+    using U = typename std::conditional<sizeof(T) == 2, uint16_t,
+                                        typename std::conditional<sizeof(T) == 4, uint32_t, uint64_t>::type>::type;
+    U u;
+    std::memcpy(&u, &v, sizeof(U));
+    u = bswap(u);
+    std::memcpy(p, &u, sizeof(U));
+}
+
+// Big-endian samples of type T -> float, on all host threads.
+template <typename T>
+void convert_samples(const unsigned char* raw, int64_t n, float* out)
+{
+#pragma omp parallel for schedule(static)
+    for (int64_t q = 0; q < n; ++q) out[q] = (float)from_big_endian<T>(raw + (size_t)q * sizeof(T));
+}
+
+// float[n] -> big-endian bytes, on all host threads.
+void floats_to_big_endian(const float* v, int64_t n, unsigned char* out)
+{
+#pragma omp parallel for schedule(static)
+    for (int64_t q = 0; q < n; ++q) to_big_endian<float>(v[q], out + (size_t)q * 4);
 }
 
 struct Header {
@@ -131,13 +160,19 @@ iso_status iso_vtk_read_image(const char* path, iso_grid* grid, float* data)
     if ((size_t)in.gcount() != raw.size()) return ISO_ERR_FORMAT;
     const unsigned char* p = raw.data();
     // "char" is read as a signed byte, as the reference does on its x86 hosts
-    for (int64_t q = 0; q < n; ++q, p += ts) {
-        if (h.type == "char") data[q] = (float)(int8_t)p[0];
-        else if (h.type == "short") data[q] = (float)from_big_endian<int16_t>(p);
-        else if (h.type == "unsigned_short") data[q] = (float)from_big_endian<uint16_t>(p);
-        else if (h.type == "int") data[q] = (float)from_big_endian<int32_t>(p);
-        else if (h.type == "float") data[q] = from_big_endian<float>(p);
-        else data[q] = (float)from_big_endian<double>(p);
+    if (h.type == "char") {
+#pragma omp parallel for schedule(static)
+        for (int64_t q = 0; q < n; ++q) data[q] = (float)(int8_t)p[q];
+    } else if (h.type == "short") {
+        convert_samples<int16_t>(p, n, data);
+    } else if (h.type == "unsigned_short") {
+        convert_samples<uint16_t>(p, n, data);
+    } else if (h.type == "int") {
+        convert_samples<int32_t>(p, n, data);
+    } else if (h.type == "float") {
+        convert_samples<float>(p, n, data);
+    } else {
+        convert_samples<double>(p, n, data);
     }
     return ISO_OK;
 }
@@ -155,10 +190,11 @@ iso_status iso_vtk_write_mesh(const char* path, const iso_mesh* mesh)
     out << "DATASET POLYDATA\n";
     out << "POINTS " << nv << " float\n";
     std::vector<unsigned char> buf((size_t)nv * 12);
-    for (int64_t q = 0; q < 3 * nv; ++q) to_big_endian<float>(mesh->points[q], &buf[(size_t)q * 4]);
+    floats_to_big_endian(mesh->points, 3 * nv, buf.data());
     out.write(reinterpret_cast<const char*>(buf.data()), (std::streamsize)buf.size());
     out << "\n";
     buf.assign((size_t)nt * 32, 0);
+#pragma omp parallel for schedule(static)
     for (int64_t t = 0; t < nt; ++t) {
         unsigned char* p = &buf[(size_t)t * 32];
         to_big_endian<uint64_t>(3, p);
@@ -172,7 +208,7 @@ iso_status iso_vtk_write_mesh(const char* path, const iso_mesh* mesh)
     out.write(reinterpret_cast<const char*>(buf.data()), (std::streamsize)buf.size());
     out << "\n";
     buf.resize((size_t)nv * 12);
-    for (int64_t q = 0; q < 3 * nv; ++q) to_big_endian<float>(mesh->normals[q], &buf[(size_t)q * 4]);
+    floats_to_big_endian(mesh->normals, 3 * nv, buf.data());
     out << "POINT_DATA " << nv << "\n";
     out << "NORMALS Normals float\n";
     out.write(reinterpret_cast<const char*>(buf.data()), (std::streamsize)buf.size());
@@ -203,7 +239,7 @@ iso_status iso_vtk_write_image(const char* path, const iso_grid* grid, const flo
     out << "SCALARS scalars float\n";
     out << "LOOKUP_TABLE default\n";
     std::vector<unsigned char> buf((size_t)n * 4);
-    for (int64_t q = 0; q < n; ++q) to_big_endian<float>(data[q], &buf[(size_t)q * 4]);
+    floats_to_big_endian(data, n, buf.data());
     out.write(reinterpret_cast<const char*>(buf.data()), (std::streamsize)buf.size());
     return out.good() ? ISO_OK : ISO_ERR_IO;
 }
