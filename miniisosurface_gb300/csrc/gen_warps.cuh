@@ -51,6 +51,7 @@ enum GenMode { kGenFE = 0, kGenMC = 1, kGenTri = 2 };
 // Per-warp scratch in shared memory:
 //   mb[8][W]   {cut mask, id of its first cut edge - the row's first vertex}
 //              per mask (xA xB xC xD yA yC zA zB) and word
+//   rwt[W][8]  the word's row words (a ash bsh b c csh dsh d: corners 0..7)
 //   cell[32]   the batch's active cells: i | cube case << 16
 //   list[...]  FE / TRI: the batch's triangles, cell | triangle << 5 (u8);
 //              MC: the batch's owned vertices, cell | cube edge << 5 (u16)
@@ -62,7 +63,7 @@ __host__ __device__ inline size_t gen_list_bytes(int mode)
 __host__ __device__ inline size_t gen_warp_scratch_bytes(int W, int mode)
 {
     const size_t vq = mode == kGenFE ? (size_t)3 * kGenVq * 12 : 0;
-    return ((size_t)8 * W * 8 + kGenCells * 4 + gen_list_bytes(mode) + vq + 15) & ~(size_t)15;
+    return ((size_t)8 * W * 8 + (size_t)8 * W * 4 + kGenCells * 4 + gen_list_bytes(mode) + vq + 15) & ~(size_t)15;
 }
 
 // Divisors of the gradient: the reference divides by the spacing (one-sided
@@ -286,8 +287,9 @@ __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
     const int W = g.W;
     unsigned char* ws = s_raw + (size_t)warp * ws_bytes;
     uint2* mb = reinterpret_cast<uint2*>(ws);
-    uint32_t* cell = reinterpret_cast<uint32_t*>(ws + (size_t)8 * W * 8);
-    unsigned char* list = ws + (size_t)8 * W * 8 + kGenCells * 4;
+    uint32_t* rwt = reinterpret_cast<uint32_t*>(ws + (size_t)8 * W * 8);
+    uint32_t* cell = rwt + 8 * W;
+    unsigned char* list = reinterpret_cast<unsigned char*>(cell + kGenCells);
     unsigned long long* vq_id = reinterpret_cast<unsigned long long*>(list + gen_list_bytes(MODE));
     uint32_t* vq_pos = reinterpret_cast<uint32_t*>(vq_id + 3 * kGenVq);
     for (int c = tid; c < 256; c += kThreads) {
@@ -473,6 +475,11 @@ __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
             mb[5 * W + lane] = make_uint2(m.yC, dC + nxC + (e2 >> 16));
             mb[6 * W + lane] = make_uint2(m.zA, nxA + nyA + (e3 & 0xffffu));
             mb[7 * W + lane] = make_uint2(m.zB, dB + cntB + (e3 >> 16));
+            if (cellrow) {  // corner order of the cube case: bit v = corner v
+                uint4* t = reinterpret_cast<uint4*>(rwt + 8 * lane);
+                t[0] = make_uint4(rw.a, rw.ash, rw.bsh, rw.b);
+                t[1] = make_uint4(rw.c, rw.csh, rw.dsh, rw.d);
+            }
         }
         __syncwarp();
         Planes pl{};
@@ -543,15 +550,26 @@ __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
             unsigned long long tcur = ts;  // FE / TRI: next triangle; MC: next vertex
             for (uint32_t c0 = 0; c0 < tot; c0 += kGenCells) {
                 while (rem != 0u && rank < c0 + kGenCells) {
-                    const int bit = __ffs(rem) - 1;
-                    cell[rank - c0] = (uint32_t)(32 * lane + bit) | ((uint32_t)cube_case(rw, bit) << 16);
+                    cell[rank - c0] = (uint32_t)(32 * lane + __ffs(rem) - 1);
                     rem &= rem - 1u;
                     ++rank;
                 }
                 __syncwarp();
                 const uint32_t nc = min(tot - c0, (uint32_t)kGenCells);
                 const bool live = (uint32_t)lane < nc;
-                const uint32_t rec = live ? cell[lane] : 0u;
+                uint32_t rec = 0u;
+                if (live) {  // the cell's cube case from its word's row words
+                    const uint32_t ci = cell[lane];
+                    const uint4* t = reinterpret_cast<const uint4*>(rwt + 8 * (ci >> 5));
+                    const uint4 lo4 = t[0], hi4 = t[1];
+                    const int b = (int)(ci & 31u);
+                    const uint32_t cs = ((lo4.x >> b) & 1u) | (((lo4.y >> b) & 1u) << 1) | (((lo4.z >> b) & 1u) << 2) |
+                                        (((lo4.w >> b) & 1u) << 3) | (((hi4.x >> b) & 1u) << 4) |
+                                        (((hi4.y >> b) & 1u) << 5) | (((hi4.z >> b) & 1u) << 6) |
+                                        (((hi4.w >> b) & 1u) << 7);
+                    rec = ci | (cs << 16);
+                    cell[lane] = rec;
+                }
                 const int cs = (int)(rec >> 16);
                 if (MODE == kGenFE || MODE == kGenTri) {
                     const uint32_t nt = live ? (uint32_t)iso_case_ntris(s_tris[cs]) : 0u;
