@@ -2,17 +2,20 @@
 // on sm_103a, with pass 1 (x-edge classification, trims) fused into pass 2
 // (cube cases, per-row counts):
 //
-//   k_count_warps  a CTA owns a block of 8 grid rows (one warp per row) and a
-//                  run of KC planes and marches along z.  Each warp classifies
-//                  its rows j and j+1 of plane k+1 straight from the volume
-//                  (loads for plane k+2 already in flight) into bit-per-point
-//                  words held one per lane -- the reference's edgeCases bytes
-//                  are never materialised -- and counts for grid row (j,k) its
-//                  cut x, y and z edges (the vertices it owns), the trims
-//                  xl/xr, the triangles of cell row (j,k) and, for Marching
-//                  Cubes, the vertices cell row (j,k) owns.  It writes the bit
-//                  words for pass 4.  No warp waits for another.  Rows of
-//                  up to 64 words; k_count_wide walks longer rows in chunks.
+//   k_count_pairs  (rows up to 512 points) a CTA owns a block of 16 grid rows
+//   k_count_warps  (up to 2048) / 8 rows (k_count_warps: a warp per row;
+//                  k_count_pairs: a half-warp per row) and a run of KC planes
+//                  and marches along z.  Each row's words of plane k+1 are
+//                  classified straight from the volume (float4 loads of plane
+//                  k+2 already in flight) into bit-per-point words held one
+//                  per lane -- the reference's edgeCases bytes are never
+//                  materialised -- and counted for grid row (j,k): its cut
+//                  x, y and z edges (the vertices it owns), the trims xl/xr,
+//                  the triangles of cell row (j,k) and, for Marching Cubes,
+//                  the vertices cell row (j,k) owns, all 32 cells of a word at
+//                  once (tris_of_word, mc_verts_of_word).  Writes the bit
+//                  words for pass 4.  No warp waits for another.
+//   k_count_wide   rows longer than 2048 points, walked in chunks.
 //   k_scan_*       exclusive scans of the per-row counts in (k, j) order, the
 //                  reference's row order: the first vertex / triangle / MC
 //                  vertex of every row (gridEdge xstart and triCounter after
@@ -102,7 +105,7 @@ struct RowCounts {
 // trim candidates, the triangles (and MC vertices) of its cells.
 template <bool MC>
 __device__ __forceinline__ void count_word(const RowWords& rw, int w, const Grid& g, int j, int k, bool hasY,
-                                           bool hasZ, const uint8_t* s_ntris, const uint16_t* s_cut, RowCounts& rc)
+                                           bool hasZ, RowCounts& rc)
 {
     const uint32_t evalid = validmask(w, g.nx - 1);  // x-edges / cells: i <= nx-2
     const uint32_t pvalid = validmask(w, g.nx);      // points: i <= nx-1
@@ -119,13 +122,10 @@ __device__ __forceinline__ void count_word(const RowWords& rw, int w, const Grid
         rc.first = min(rc.first, (uint32_t)(32 * w + __ffs(marked) - 1));
         rc.last = max(rc.last, (uint32_t)(32 * w + 32 - __clz(marked)));
     }
-    if (hasY && hasZ) {
-        for (uint32_t act = active_cells(rw, evalid); act; act &= act - 1) {
-            const int bit = __ffs(act) - 1;
-            const int c = cube_case(rw, bit);
-            rc.tc += s_ntris[c];
-            if (MC) rc.mc += __popc(mc_owned_edges(32 * w + bit == 0, j == 0, k == 0) & s_cut[c]);
-        }
+    if (hasY && hasZ) {  // all 32 cells at once (tris_of_word, mc_verts_of_word)
+        rc.tc += tris_of_word(rw.a, rw.ash, rw.bsh, rw.b, rw.c, rw.csh, rw.dsh, rw.d, evalid);
+        if (MC) rc.mc += mc_verts_of_word(rw.a, rw.ash, rw.bsh, rw.b, rw.c, rw.csh, rw.dsh, rw.d, evalid, j == 0, k == 0,
+                                          w == 0);
     }
 }
 
@@ -155,13 +155,7 @@ __global__ void __launch_bounds__(kThreads) k_count_warps(const float* __restric
                                                           uint4* __restrict__ rowcnt, uint2* __restrict__ trims,
                                                           uint32_t* __restrict__ mccnt, uint32_t* __restrict__ bits_out)
 {
-    __shared__ uint8_t s_ntris[256];
-    __shared__ uint16_t s_cut[256];
-    for (int c = threadIdx.x; c < 256; c += blockDim.x) {
-        s_ntris[c] = (uint8_t)iso_case_ntris(cases->tris[c]);
-        s_cut[c] = cases->cut[c];
-    }
-    __syncthreads();
+    (void)cases;  // the counts need no case table (tris_of_word, mc_verts_of_word)
     const int jb = blockIdx.x % nyb, kc = blockIdx.x / nyb;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int j = jb * kCountRows + warp;
@@ -220,7 +214,7 @@ __global__ void __launch_bounds__(kThreads) k_count_warps(const float* __restric
             rw.bsh = (rw.b >> 1) | (next_word<NW>(B, q, lane) << 31);
             rw.csh = (rw.c >> 1) | (next_word<NW>(Cw, q, lane) << 31);
             rw.dsh = (rw.d >> 1) | (next_word<NW>(Dw, q, lane) << 31);
-            count_word<MC>(rw, w, g, j, k, hasY, hasZ, s_ntris, s_cut, rc);
+            count_word<MC>(rw, w, g, j, k, hasY, hasZ, rc);
             if (w < g.W) bits_out[r * g.W + w] = rw.a;
         }
         finish_row<MC>(rc, lane, r, g, rowcnt, trims, mccnt);
@@ -277,13 +271,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_count_pairs(const float* __rest
                                                           uint4* __restrict__ rowcnt, uint2* __restrict__ trims,
                                                           uint32_t* __restrict__ mccnt, uint32_t* __restrict__ bits_out)
 {
-    __shared__ uint8_t s_ntris[256];
-    __shared__ uint16_t s_cut[256];
-    for (int c = threadIdx.x; c < 256; c += blockDim.x) {
-        s_ntris[c] = (uint8_t)iso_case_ntris(cases->tris[c]);
-        s_cut[c] = cases->cut[c];
-    }
-    __syncthreads();
+    (void)cases;  // the counts need no case table (tris_of_word, mc_verts_of_word)
     const int jb = blockIdx.x % nyb, kc = blockIdx.x / nyb;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, h = lane >> 4, l16 = lane & 15;
     const int jw = jb * kPairRows + 2 * warp;
@@ -332,7 +320,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_count_pairs(const float* __rest
         rw.bsh = (rw.b >> 1) | ((nxt ? bn : 0u) << 31);
         rw.csh = (rw.c >> 1) | ((nxt ? cn : 0u) << 31);
         rw.dsh = (rw.d >> 1) | ((nxt ? dn : 0u) << 31);
-        if (row_ok) count_word<MC>(rw, l16, g, j, k, hasY, hasZ, s_ntris, s_cut, rc);
+        if (row_ok) count_word<MC>(rw, l16, g, j, k, hasY, hasZ, rc);
         const long long r = (long long)(k - g.kr) * g.ny + j;
         if (row_ok && l16 < g.W) bits_out[r * g.W + l16] = rw.a;
         // both rows' totals at once: row h in bits 16h .. 16h+15 (each below 2^16)
@@ -382,13 +370,7 @@ __global__ void __launch_bounds__(kThreads) k_count_wide(const float* __restrict
                                                          uint4* __restrict__ rowcnt, uint2* __restrict__ trims,
                                                          uint32_t* __restrict__ mccnt, uint32_t* __restrict__ bits_out)
 {
-    __shared__ uint8_t s_ntris[256];
-    __shared__ uint16_t s_cut[256];
-    for (int c = threadIdx.x; c < 256; c += blockDim.x) {
-        s_ntris[c] = (uint8_t)iso_case_ntris(cases->tris[c]);
-        s_cut[c] = cases->cut[c];
-    }
-    __syncthreads();
+    (void)cases;  // the counts need no case table (tris_of_word, mc_verts_of_word)
     const int jb = blockIdx.x % nyb, kc = blockIdx.x / nyb;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int j = jb * kCountRows + warp;
@@ -417,7 +399,7 @@ __global__ void __launch_bounds__(kThreads) k_count_wide(const float* __restrict
             rw.csh = (rw.c >> 1) | ((lane < 31 ? dc : nc) << 31);
             rw.dsh = (rw.d >> 1) | ((lane < 31 ? dd : nd) << 31);
             const int w = 32 * c + lane;
-            count_word<MC>(rw, w, g, j, k, hasY, hasZ, s_ntris, s_cut, rc);
+            count_word<MC>(rw, w, g, j, k, hasY, hasZ, rc);
             if (w < g.W) bits_out[r * g.W + w] = rw.a;
         }
         finish_row<MC>(rc, lane, r, g, rowcnt, trims, mccnt);

@@ -1,31 +1,26 @@
 // Pass 4 on sm_103a (included by gen_warps_fe.cu and gen_warps_mc.cu).
 //
 // A CTA owns a block of J = 8 grid rows (j0 .. j0+7, one warp per row) and a
-// run of KC planes, and marches along z.  The warps never wait for one
-// another except through a ring of kGenSlots plane slabs in shared memory:
-//
-//   full[s]   the slab in slot s has landed (TMA bulk copy, or cp.async when
-//             rows are not 16-byte aligned), issued by warp 0 lane 0
-//   empty[s]  all 8 warps are done with the plane in slot s
-//
-// A slab holds rows j0-1 .. j0+J+1 of a plane (contiguous in memory), so a
-// warp finds every value it interpolates at planes k and k+1 in shared
-// memory; the gradient neighbours at planes k-1 and k+2 come from L2.
+// run of KC planes [kb, ke); each warp marches along z on its own (the only
+// CTA barrier stages the case tables).  Volume values are read through L1
+// from global memory; the count pass's bit rows say where the surface is.
 //
 // Per step a warp handles grid row (j, k) with one 32-bit word of the bit
-// mask written by the count pass per lane (the bit words and row starts of
-// the next step load while this one runs):
+// mask per lane (the bit words and row starts of the next step load while
+// this one runs):
 //   the 8 cut masks of the cell row and their popc prefixes (warp scans)
 //   give, per word, the id of each mask's first cut edge relative to the
-//   row's first vertex; the warp keeps them in shared memory (mb), so any
-//   lane numbers any edge of any cell with one 8-byte load and a popc;
-//   FE  : the row's vertices, one per lane (a shuffle binary search maps the
-//         lane's vertex rank to a word and __fns to a bit), written to
-//         consecutive ids;
+//   row's first vertex; the warp keeps them in shared memory (mb), with the
+//   row words (rwt), so that any lane numbers any edge of any cell with one
+//   8-byte load and a popc;
+//   FE  : the row's vertices, one per lane: a shuffle binary search maps the
+//         lane's vertex rank to a word and __fns to a bit; the vertex goes to
+//         its axis' queue (shared memory), and every full batch of 32 is
+//         computed by the axis' own code (no divergence by axis, full lanes);
 //   the active cells of the cell row are compacted, 32 at a time, into the
-//   warp's cell list (i, cube case), then
-//   FE, TRI: their triangles are listed as (cell, triangle) pairs and written
-//         one triangle per lane, consecutive lanes storing consecutive
+//   warp's cell list; each cell lane computes its cube case, then
+//   FE, TRI: the cells' triangles are listed as (cell, triangle) pairs and
+//         written one triangle per lane, consecutive lanes storing consecutive
 //         triangles (TRI, without volume, maps the corners through the
 //         Flying Edges -> MC index map);
 //   MC  : the vertices the cells own, in owner-cell / first-appearance order
@@ -41,7 +36,6 @@ namespace iso {
 
 constexpr int kGenRows = 8;       // grid rows per CTA, one per warp
 constexpr int kGenCtasPerSm = 3;  // resident CTAs per SM the kernel is built for
-constexpr int kGenPrefetch = 3;   // planes of L2 prefetch ahead of the step
 constexpr int kGenCells = 32;  // cells per batch
 constexpr int kGenTris = 5 * kGenCells;    // triangles of a batch, at most
 constexpr int kGenOwned = 12 * kGenCells;  // MC vertices owned by a batch, at most
@@ -270,7 +264,7 @@ __device__ __forceinline__ uint32_t fe_edge_rel(const uint2* mb, int W, int e, i
     return p.y + __popc(p.x & lowmask(bit + off));
 }
 
-template <int MODE, typename IndexT, bool BULK>
+template <int MODE, typename IndexT>
 __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
     const float* __restrict__ vol, const uint32_t* __restrict__ bits, Grid g, GradScale gs, float iso, int KC,
     int nyb, int kbeg, int kend, int kemit, unsigned long long vbase, unsigned long long tbase, int ws_bytes,
@@ -313,22 +307,8 @@ __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
     const int jlo = j0 > 0 ? j0 - 1 : 0;  // planes are addressed from this row
     const long long plane = (long long)g.ny * g.nx;
     auto plane_ptr = [&](int p) { return vol + (long long)(p - g.kd) * plane + (long long)jlo * g.nx; };
-    const int plast = min(g.ke, g.nz - 1);  // last plane held by vol
 
-    // L2 prefetch (TMA bulk prefetch when rows are 16-byte aligned) of this
-    // warp's rows j, j+1 of plane p, kGenPrefetch planes ahead of use.
     const bool hasY = j < g.ny - 1;
-    auto prefetch_plane = [&](int p) {
-        if (!VOL || p > plast || p < g.kd) return;
-        const float* r0 = vol + (long long)(p - g.kd) * plane + (long long)j * g.nx;
-        const int nrows = hasY ? 2 : 1;
-        if (BULK) {
-            if (lane == 0) bulk_prefetch_l2(r0, (unsigned)(nrows * g.nx * 4));
-        } else {
-            for (int q = lane * 32; q < nrows * g.nx; q += 32 * 32) prefetch_l2_line(r0 + q);
-        }
-    };
-    for (int p = kb - 1; p < kb + kGenPrefetch; ++p) prefetch_plane(p);
 
     const bool in = lane < W, in1 = lane + 1 < W;
     const uint32_t evalid = validmask(lane, g.nx - 1);  // x-edges / cells: i <= nx-2
@@ -426,7 +406,6 @@ __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
     for (int k = kb; k <= ke; ++k) {
         const bool fin = k == ke;
         const bool hasZ = k + 1 < g.nz;
-        prefetch_plane(k + kGenPrefetch);
         // the next step's words and starts, in flight while this step runs
         uint32_t nC = 0, nD = 0;
         unsigned long long nst = 0;
@@ -653,11 +632,10 @@ void launch_gen_warps_impl(const float* vol, const Grid& g, float iso, const Cas
 {
     RowStarts rs = row_starts(g, cp, b);
     for (int a = 0; a < 3; ++a) rs.add[a] = p.add[a];
-    const bool bulk = MODE != kGenTri && (g.nx % 4 == 0) && ((reinterpret_cast<uintptr_t>(vol) & 15) == 0);
     const unsigned blocks = (unsigned)(p.nyb * p.nkc);
     const int ws_bytes = (int)gen_warp_scratch_bytes(g.W, MODE);
     const size_t smem = (size_t)kGenRows * ws_bytes;
-    auto kern = bulk ? k_gen_warps<MODE, IndexT, true> : k_gen_warps<MODE, IndexT, false>;
+    auto kern = k_gen_warps<MODE, IndexT>;
     allow_smem(kern, smem);
     kern<<<blocks, kThreads, smem, s>>>(vol, b.bits, g, make_grad_scale(g), iso, p.KC, p.nyb, p.kbeg, p.kend, p.kemit,
                                         p.vbase, p.tbase, ws_bytes, cases, b.rowcnt, rs, b.totals, capV, capT, points,

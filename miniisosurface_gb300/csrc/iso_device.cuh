@@ -570,6 +570,71 @@ struct RowStarts {
     }
 };
 
+// Triangles of all cells of a word at once, without looking at the cases:
+// every polygon of a case spends its m cut edges on m-2 triangles, so
+// ntris = cut edges - 2 * polygons, and the polygons of a case are the
+// edge-connected components of its set corners, V - E + F (corners, cube
+// edges and faces inside the set), except when the two unset corners are
+// the ends of a body diagonal (cases 125, 190, 215, 235): the six set
+// corners form a ring that the faces miss, and the table makes two polygons
+// there.  The words are the corners 0..7 of the word's cells (cube_case).
+// Checked against numTris of all 256 cases (MarchingCubesTables.h:23).
+ISO_HD inline uint32_t popc32(uint32_t x)
+{
+#ifdef __CUDA_ARCH__
+    return (uint32_t)__popc(x);
+#else
+    return (uint32_t)__builtin_popcount(x);
+#endif
+}
+
+ISO_HD inline uint32_t tris_of_word(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t c4, uint32_t c5,
+                                    uint32_t c6, uint32_t c7, uint32_t cells)
+{
+    // cube edges (corner pairs) 0-1 1-2 3-2 0-3 4-5 5-6 7-6 4-7 0-4 1-5 3-7 2-6
+    const uint32_t e0a = c0 & c1, e1a = c1 & c2, e2a = c3 & c2, e3a = c0 & c3, e4a = c4 & c5, e5a = c5 & c6;
+    const uint32_t e6a = c7 & c6, e7a = c4 & c7, e8a = c0 & c4, e9a = c1 & c5, e10a = c3 & c7, e11a = c2 & c6;
+    const uint32_t cut = popc32((c0 ^ c1) & cells) + popc32((c1 ^ c2) & cells) + popc32((c3 ^ c2) & cells) +
+                         popc32((c0 ^ c3) & cells) + popc32((c4 ^ c5) & cells) + popc32((c5 ^ c6) & cells) +
+                         popc32((c7 ^ c6) & cells) + popc32((c4 ^ c7) & cells) + popc32((c0 ^ c4) & cells) +
+                         popc32((c1 ^ c5) & cells) + popc32((c3 ^ c7) & cells) + popc32((c2 ^ c6) & cells);
+    // only cells with a cut edge count (all-set cells have V - E + F = 1)
+    const uint32_t act = cells & ~((c0 & c1 & c2 & c3 & c4 & c5 & c6 & c7) | ~(c0 | c1 | c2 | c3 | c4 | c5 | c6 | c7));
+    const uint32_t verts = popc32(c0 & act) + popc32(c1 & act) + popc32(c2 & act) + popc32(c3 & act) +
+                           popc32(c4 & act) + popc32(c5 & act) + popc32(c6 & act) + popc32(c7 & act);
+    const uint32_t edges = popc32(e0a & act) + popc32(e1a & act) + popc32(e2a & act) + popc32(e3a & act) +
+                           popc32(e4a & act) + popc32(e5a & act) + popc32(e6a & act) + popc32(e7a & act) +
+                           popc32(e8a & act) + popc32(e9a & act) + popc32(e10a & act) + popc32(e11a & act);
+    // faces z- z+ y- y+ x- x+: 0123 4567 0154 3267 0374 1265
+    const uint32_t faces = popc32(e0a & e2a & act) + popc32(e4a & e6a & act) + popc32(e0a & e4a & act) +
+                           popc32(e2a & e6a & act) + popc32(e3a & e7a & act) + popc32(e1a & e5a & act);
+    // body diagonals 0-6 1-7 2-4 3-5 unset, the other six set
+    const uint32_t ring = (~(c0 | c6) & c1 & c2 & c3 & c4 & c5 & c7) | (~(c1 | c7) & c0 & c2 & c3 & c4 & c5 & c6) |
+                          (~(c2 | c4) & c0 & c1 & c3 & c5 & c6 & c7) | (~(c3 | c5) & c0 & c1 & c2 & c4 & c6 & c7);
+    const uint32_t polys = verts - edges + faces + 2u * popc32(ring & act);
+    return cut - 2u * polys;
+}
+
+// Marching Cubes vertices owned by the cells of a word (mc_owned_edges):
+// cut edges 5, 6, 11 of every cell; 1, 2 on plane k = 0; 4, 9 on row
+// j = 0; 0 on both; 7, 10 (3 with k = 0, 8 with j = 0) for the cell at i = 0,
+// bit 0 of word 0 (first0).
+ISO_HD inline uint32_t mc_verts_of_word(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t c4, uint32_t c5,
+                                        uint32_t c6, uint32_t c7, uint32_t cells, bool j0, bool k0, bool first0)
+{
+    uint32_t n = popc32((c5 ^ c6) & cells) + popc32((c7 ^ c6) & cells) + popc32((c2 ^ c6) & cells);
+    if (k0) n += popc32((c1 ^ c2) & cells) + popc32((c3 ^ c2) & cells);
+    if (j0) n += popc32((c4 ^ c5) & cells) + popc32((c1 ^ c5) & cells);
+    if (j0 && k0) n += popc32((c0 ^ c1) & cells);
+    if (first0) {
+        const uint32_t b0 = cells & 1u;
+        n += popc32((c4 ^ c7) & b0) + popc32((c3 ^ c7) & b0);
+        if (k0) n += popc32((c0 ^ c3) & b0);
+        if (j0) n += popc32((c0 ^ c4) & b0);
+    }
+    return n;
+}
+
 // Marching-cubes owned-edge mask of a cell (first-reference rule of
 // marchingCubes/serial/main.cpp:139-177): an edge belongs to the adjacent
 // cell with the smallest linear index.  Interior cells own e5, e6, e11.

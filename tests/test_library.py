@@ -126,3 +126,20 @@ def test_invalid_arguments_rejected_without_gpu_work(built):
     assert lib.iso_extract_device(None, 0, None, None, C.c_float(0), None, None) == _lib.ISO_ERR_INVALID_ARG
     d = (C.c_int64 * 3)(4, 4, 4)
     assert lib.iso_generate_value_noise(d, 0, 8, 1, None) == _lib.ISO_ERR_INVALID_ARG
+
+
+def test_bit_parallel_counts_match_case_tables(tmp_path):
+    """tris_of_word / mc_verts_of_word (iso_device.cuh) against numTris and the
+    MC owned-edge rule for every cube case and random words (host code)."""
+    import shutil
+    import subprocess
+    from pathlib import Path
+
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    root = Path(__file__).resolve().parents[1]
+    exe = tmp_path / "count_identities"
+    subprocess.run([nvcc, "-std=c++17", "-O1", "-I", str(root / "miniisosurface_gb300" / "csrc"), "-I",
+                    str(root / "include"), str(root / "tests" / "compat" / "count_identities.cu"), "-o", str(exe)],
+                   check=True, capture_output=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0 and out.stdout.strip() == "ok", out.stdout
