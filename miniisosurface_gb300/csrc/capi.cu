@@ -1,5 +1,6 @@
 // C ABI of the extractor: contexts, scratch, the extraction entry points and
 // the pass-by-pass Flying Edges object.  See include/miniiso.h.
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -35,7 +36,16 @@ struct iso_ctx {
     int d_index_bytes = 0;
     unsigned long long* h_totals = nullptr;  // pinned, 4 entries
     unsigned long long* h_slab = nullptr;    // pinned, 9 entries (slab counts)
+    // streamed host entry point: copy streams, events, two device staging meshes
+    cudaStream_t s_h2d = nullptr, s_d2h = nullptr;
+    std::vector<cudaEvent_t> sync_events;
+    float* st_points[2] = {nullptr, nullptr};
+    float* st_normals[2] = {nullptr, nullptr};
+    void* st_tris[2] = {nullptr, nullptr};
+    long long st_cap_points = 0, st_cap_tris = 0;
+    int st_index_bytes = 0;
     int reverse = 1;  // pass 4 walks the planes backwards (the count pass leaves the last ones in L2)
+    int stream_host = 1;  // iso_extract_host streams slabs (large grids)
     std::string last_error;
     // per-pass timing (iso_ctx_profile)
     bool profiling = false;
@@ -386,6 +396,56 @@ iso_status slab_count(iso_ctx* ctx, iso_algorithm algo, const float* vol, const 
     return ISO_OK;
 }
 
+// Pass 4 of slab [k0, k1) into the device mesh `out` (the slab's rows),
+// numbered from point_offset / tri_offset; enqueued on s.
+iso_status slab_generate(iso_ctx* ctx, iso_algorithm algo, const float* volume, const Grid& g, int64_t k0, int64_t k1,
+                         float isoval, const Plans& pl, const FeBuffers& b, const SlabCounts& c, int64_t point_offset,
+                         int64_t tri_offset, const iso_mesh* out, cudaStream_t s)
+{
+    const bool mc = algo == ISO_MARCHING_CUBES;
+    iso::GenPlan gp = pl.gp;
+    gp.vbase = (unsigned long long)point_offset;
+    gp.tbase = (unsigned long long)tri_offset;
+    gp.add[0] = mc ? 0ull : (unsigned long long)point_offset - c.lo[0];
+    gp.add[1] = (unsigned long long)tri_offset - c.lo[1];
+    gp.add[2] = (unsigned long long)point_offset - c.lo[2];
+    const long long big = 1ll << 62;  // capacities were checked above
+    const bool i4 = out->index_bytes == 4;
+    PassMarks pm(ctx, s);
+    if (!mc) {
+        gp.kbeg = (int)k0;
+        gp.kend = (int)k1;
+        gp.kemit = (int)k0;
+        iso::gen_split(gp, ctx->nsm);
+        if (i4)
+            iso::launch_fe_gen_warps<uint32_t>(volume, g, isoval, ctx->d_cases, b, pl.cp, gp, big, big, out->points,
+                                               out->normals, static_cast<uint32_t*>(out->tris), ctx->reverse, s);
+        else
+            iso::launch_fe_gen_warps<uint64_t>(volume, g, isoval, ctx->d_cases, b, pl.cp, gp, big, big, out->points,
+                                               out->normals, static_cast<uint64_t*>(out->tris), ctx->reverse, s);
+        pm.mark(ISO_PASS_FE_GENERATE);
+    } else {
+        gp.kbeg = g.kr;  // cell row k0-1 maps the edges it owns on plane k0
+        gp.kend = (int)k1;
+        gp.kemit = (int)k0;
+        iso::gen_split(gp, ctx->nsm);
+        iso::launch_mc_gen_warps(volume, g, isoval, ctx->d_cases, b, pl.cp, gp, big, big, out->points, out->normals,
+                                 ctx->reverse, s);
+        pm.mark(ISO_PASS_MC_VERTICES);
+        gp.kbeg = (int)k0;
+        iso::gen_split(gp, ctx->nsm);
+        if (i4)
+            iso::launch_mc_tri_warps<uint32_t>(g, ctx->d_cases, b, pl.cp, gp, big, big,
+                                               static_cast<uint32_t*>(out->tris), s);
+        else
+            iso::launch_mc_tri_warps<uint64_t>(g, ctx->d_cases, b, pl.cp, gp, big, big,
+                                               static_cast<uint64_t*>(out->tris), s);
+        pm.mark(ISO_PASS_MC_TRIANGLES);
+    }
+    ISO_CUDA(ctx, cudaGetLastError());
+    return ISO_OK;
+}
+
 iso_status slab_prepare(iso_ctx* ctx, iso_algorithm algo, const float* volume, const iso_grid* grid, int64_t k0,
                         int64_t k1, Grid& g, Plans& pl, FeBuffers& b, cudaStream_t s)
 {
@@ -401,6 +461,174 @@ iso_status slab_prepare(iso_ctx* ctx, iso_algorithm algo, const float* volume, c
         return ISO_ERR_INVALID_ARG;
     }
     return ensure_scratch(ctx, g, pl.cp, b, s);
+}
+
+// ---------------------------------------------------------------------------
+// Streamed host extraction: the volume goes to the device slab by slab on a
+// copy stream; each slab is counted as soon as its planes have landed,
+// generated with the offsets of the slabs before it into one of two device
+// staging meshes, and its part of the mesh goes back on a second copy stream
+// while the next slabs are copied and computed.  Host <-> device copies of
+// the whole volume and mesh overlap with each other and with the kernels.
+// ---------------------------------------------------------------------------
+constexpr int kStreamPlanes = 64;  // planes per slab of the streamed path
+
+cudaEvent_t sync_event(iso_ctx* ctx, size_t q)
+{
+    while (ctx->sync_events.size() <= q) {
+        cudaEvent_t e;
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return nullptr;
+        ctx->sync_events.push_back(e);
+    }
+    return ctx->sync_events[q];
+}
+
+// Staging meshes of at least (V, T); growing waits for the streams.
+iso_status ensure_stage(iso_ctx* ctx, long long V, long long T, int ib, cudaStream_t s)
+{
+    if (V <= ctx->st_cap_points && T <= ctx->st_cap_tris && ib == ctx->st_index_bytes) return ISO_OK;
+    ISO_CUDA(ctx, cudaStreamSynchronize(s));
+    ISO_CUDA(ctx, cudaStreamSynchronize(ctx->s_d2h));
+    const long long cv = std::max(V + V / 4 + 1024, ctx->st_cap_points);
+    const long long ct = std::max(T + T / 4 + 1024, ctx->st_index_bytes == ib ? ctx->st_cap_tris : 0ll);
+    for (int q = 0; q < 2; ++q) {
+        cudaFree(ctx->st_points[q]);
+        cudaFree(ctx->st_normals[q]);
+        cudaFree(ctx->st_tris[q]);
+        ctx->st_points[q] = ctx->st_normals[q] = nullptr;
+        ctx->st_tris[q] = nullptr;
+    }
+    ctx->st_cap_points = ctx->st_cap_tris = 0;
+    for (int q = 0; q < 2; ++q) {
+        ISO_CUDA(ctx, cudaMalloc(&ctx->st_points[q], (size_t)cv * 12));
+        ISO_CUDA(ctx, cudaMalloc(&ctx->st_normals[q], (size_t)cv * 12));
+        ISO_CUDA(ctx, cudaMalloc(&ctx->st_tris[q], (size_t)ct * 3 * ib));
+    }
+    ctx->st_cap_points = cv;
+    ctx->st_cap_tris = ct;
+    ctx->st_index_bytes = ib;
+    return ISO_OK;
+}
+
+bool stream_eligible(const iso_ctx* ctx, const Grid& g)
+{
+    return !empty_grid(g) && g.nz >= 2 * kStreamPlanes && iso::gen_plan(g, ctx->nsm).fits;
+}
+
+iso_status extract_host_streamed(iso_ctx* ctx, iso_algorithm algo, const float* volume, const iso_grid* grid,
+                                 const Grid& gfull, float isoval, iso_mesh* out, cudaStream_t s)
+{
+    if (!ctx->s_h2d) ISO_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->s_h2d, cudaStreamNonBlocking));
+    if (!ctx->s_d2h) ISO_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->s_d2h, cudaStreamNonBlocking));
+    const int nz = gfull.nz;
+    const size_t plane = (size_t)gfull.nx * gfull.ny;
+    const size_t vbytes = plane * nz * sizeof(float);
+    if (vbytes > ctx->d_volume_bytes) {
+        ISO_CUDA(ctx, cudaDeviceSynchronize());
+        cudaFree(ctx->d_volume);
+        ctx->d_volume = nullptr;
+        ctx->d_volume_bytes = 0;
+        ISO_CUDA(ctx, cudaMalloc(&ctx->d_volume, vbytes));
+        ctx->d_volume_bytes = vbytes;
+    }
+    const int nslab = (nz + kStreamPlanes - 1) / kStreamPlanes;
+    auto slab_k0 = [&](int q) { return (int)((long long)q * nz / nslab); };
+    // all volume copies up front, in order; event q: planes slab q reads have landed
+    ISO_CUDA(ctx, cudaStreamWaitEvent(ctx->s_h2d, [&] {
+                     cudaEvent_t e = sync_event(ctx, 0);
+                     cudaEventRecord(e, s);  // after the caller's earlier work on s
+                     return e;
+                 }(), 0));
+    int copied = 0;  // planes [0, copied) are enqueued
+    for (int q = 0; q < nslab; ++q) {
+        const int need = std::min(slab_k0(q + 1) + 2, nz);  // planes .. k1+1
+        if (need > copied) {
+            ISO_CUDA(ctx, cudaMemcpyAsync(ctx->d_volume + copied * plane, volume + copied * plane,
+                                          (size_t)(need - copied) * plane * sizeof(float), cudaMemcpyHostToDevice,
+                                          ctx->s_h2d));
+            copied = need;
+        }
+        cudaEvent_t e = sync_event(ctx, 1 + q);
+        if (!e) return ISO_ERR_CUDA;
+        ISO_CUDA(ctx, cudaEventRecord(e, ctx->s_h2d));
+    }
+    const bool mc = algo == ISO_MARCHING_CUBES;
+    long long V = 0, T = 0;
+    bool room = true;  // the caller's buffers hold everything so far
+    iso_status st = ISO_OK;
+    for (int q = 0; q < nslab && st == ISO_OK; ++q) {
+        const int k0 = slab_k0(q), k1 = slab_k0(q + 1);
+        Grid g;
+        Plans pl;
+        FeBuffers b;
+        if (!slab_grid(grid, algo, k0, k1, g)) return ISO_ERR_INVALID_ARG;
+        pl = make_plans(ctx, g);
+        ISO_CUDA(ctx, cudaStreamWaitEvent(s, sync_event(ctx, 1 + q), 0));
+        st = ensure_scratch(ctx, g, pl.cp, b, s);
+        if (st != ISO_OK) break;
+        const float* win = ctx->d_volume + (size_t)g.kd * plane;
+        SlabCounts c;
+        st = slab_count(ctx, algo, win, g, k0, k1, isoval, pl, b, s, c);  // waits for the counts
+        if (st != ISO_OK) break;
+        const long long Vq = (long long)(c.hi[mc ? 2 : 0] - c.lo[mc ? 2 : 0]), Tq = (long long)(c.hi[1] - c.lo[1]);
+        const long long top = V + (mc ? Vq : (long long)c.tot[0]);  // largest id the slab references
+        if (out->index_bytes == 4 && top > 0xffffffffll) {
+            ctx->last_error = "more than 2^32-1 vertices: use 64-bit indices";
+            st = ISO_ERR_OVERFLOW;
+            break;
+        }
+        if (V + Vq > out->cap_points || T + Tq > out->cap_tris) room = false;
+        if (room && (Vq > 0 || Tq > 0)) {
+            const int sb = q & 1;
+            st = ensure_stage(ctx, Vq, Tq, out->index_bytes, s);
+            if (st != ISO_OK) break;
+            if (q >= 2) ISO_CUDA(ctx, cudaStreamWaitEvent(s, sync_event(ctx, 1 + nslab + 2 + sb), 0));  // staging free
+            if (mc) {
+                st = ensure_fe2mc(ctx, (long long)c.tot[0], s);
+                if (st != ISO_OK) break;
+                b.fe2mc = ctx->fe2mc;
+            }
+            iso_mesh dm{};
+            dm.points = ctx->st_points[sb];
+            dm.normals = ctx->st_normals[sb];
+            dm.tris = ctx->st_tris[sb];
+            dm.index_bytes = out->index_bytes;
+            dm.cap_points = Vq;
+            dm.cap_tris = Tq;
+            st = slab_generate(ctx, algo, win, g, k0, k1, isoval, pl, b, c, V, T, &dm, s);
+            if (st != ISO_OK) break;
+            cudaEvent_t gen_done = sync_event(ctx, 1 + nslab + sb);
+            ISO_CUDA(ctx, cudaEventRecord(gen_done, s));
+            ISO_CUDA(ctx, cudaStreamWaitEvent(ctx->s_d2h, gen_done, 0));
+            if (Vq > 0) {
+                ISO_CUDA(ctx, cudaMemcpyAsync(out->points + 3 * V, dm.points, (size_t)Vq * 12, cudaMemcpyDeviceToHost,
+                                              ctx->s_d2h));
+                ISO_CUDA(ctx, cudaMemcpyAsync(out->normals + 3 * V, dm.normals, (size_t)Vq * 12,
+                                              cudaMemcpyDeviceToHost, ctx->s_d2h));
+            }
+            if (Tq > 0) {
+                char* dst = static_cast<char*>(out->tris) + (size_t)T * 3 * out->index_bytes;
+                ISO_CUDA(ctx, cudaMemcpyAsync(dst, dm.tris, (size_t)Tq * 3 * out->index_bytes, cudaMemcpyDeviceToHost,
+                                              ctx->s_d2h));
+            }
+            ISO_CUDA(ctx, cudaEventRecord(sync_event(ctx, 1 + nslab + 2 + sb), ctx->s_d2h));
+        }
+        V += Vq;
+        T += Tq;
+    }
+    // the mesh has landed when both copy streams and s are done
+    const iso_status sh = cudaStreamSynchronize(ctx->s_h2d) == cudaSuccess ? ISO_OK : ISO_ERR_CUDA;
+    const iso_status sd = cudaStreamSynchronize(ctx->s_d2h) == cudaSuccess ? ISO_OK : ISO_ERR_CUDA;
+    ISO_CUDA(ctx, cudaStreamSynchronize(s));
+    if (st != ISO_OK) return st;
+    if (sh != ISO_OK || sd != ISO_OK) return ISO_ERR_CUDA;
+    out->n_points = V;
+    out->n_tris = T;
+    if (!room) {
+        ctx->last_error = "output buffers too small";
+        return ISO_ERR_CAPACITY;
+    }
+    return ISO_OK;
 }
 
 }  // namespace
@@ -463,45 +691,8 @@ iso_status iso_extract_slab(iso_ctx* ctx, iso_algorithm algo, const float* volum
         if (st != ISO_OK) return st;
         b.fe2mc = ctx->fe2mc;
     }
-    iso::GenPlan gp = pl.gp;
-    gp.vbase = (unsigned long long)point_offset;
-    gp.tbase = (unsigned long long)tri_offset;
-    gp.add[0] = mc ? 0ull : (unsigned long long)point_offset - c.lo[0];
-    gp.add[1] = (unsigned long long)tri_offset - c.lo[1];
-    gp.add[2] = (unsigned long long)point_offset - c.lo[2];
-    const long long big = 1ll << 62;  // capacities were checked above
-    const bool i4 = out->index_bytes == 4;
-    PassMarks pm(ctx, s);
-    if (!mc) {
-        gp.kbeg = (int)k0;
-        gp.kend = (int)k1;
-        gp.kemit = (int)k0;
-        iso::gen_split(gp, ctx->nsm);
-        if (i4)
-            iso::launch_fe_gen_warps<uint32_t>(volume, g, isoval, ctx->d_cases, b, pl.cp, gp, big, big, out->points,
-                                               out->normals, static_cast<uint32_t*>(out->tris), ctx->reverse, s);
-        else
-            iso::launch_fe_gen_warps<uint64_t>(volume, g, isoval, ctx->d_cases, b, pl.cp, gp, big, big, out->points,
-                                               out->normals, static_cast<uint64_t*>(out->tris), ctx->reverse, s);
-        pm.mark(ISO_PASS_FE_GENERATE);
-    } else {
-        gp.kbeg = g.kr;  // cell row k0-1 maps the edges it owns on plane k0
-        gp.kend = (int)k1;
-        gp.kemit = (int)k0;
-        iso::gen_split(gp, ctx->nsm);
-        iso::launch_mc_gen_warps(volume, g, isoval, ctx->d_cases, b, pl.cp, gp, big, big, out->points, out->normals,
-                                 ctx->reverse, s);
-        pm.mark(ISO_PASS_MC_VERTICES);
-        gp.kbeg = (int)k0;
-        iso::gen_split(gp, ctx->nsm);
-        if (i4)
-            iso::launch_mc_tri_warps<uint32_t>(g, ctx->d_cases, b, pl.cp, gp, big, big,
-                                               static_cast<uint32_t*>(out->tris), s);
-        else
-            iso::launch_mc_tri_warps<uint64_t>(g, ctx->d_cases, b, pl.cp, gp, big, big,
-                                               static_cast<uint64_t*>(out->tris), s);
-        pm.mark(ISO_PASS_MC_TRIANGLES);
-    }
+    st = slab_generate(ctx, algo, volume, g, k0, k1, isoval, pl, b, c, point_offset, tri_offset, out, s);
+    if (st != ISO_OK) return st;
     ISO_CUDA(ctx, cudaGetLastError());
     ISO_CUDA(ctx, cudaStreamSynchronize(s));
     return ISO_OK;
@@ -579,6 +770,14 @@ iso_status iso_ctx_destroy(iso_ctx* ctx)
     cudaFree(ctx->d_tris);
     if (ctx->h_totals) cudaFreeHost(ctx->h_totals);
     if (ctx->h_slab) cudaFreeHost(ctx->h_slab);
+    for (int q = 0; q < 2; ++q) {
+        cudaFree(ctx->st_points[q]);
+        cudaFree(ctx->st_normals[q]);
+        cudaFree(ctx->st_tris[q]);
+    }
+    for (cudaEvent_t e : ctx->sync_events) cudaEventDestroy(e);
+    if (ctx->s_h2d) cudaStreamDestroy(ctx->s_h2d);
+    if (ctx->s_d2h) cudaStreamDestroy(ctx->s_d2h);
     for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
     delete ctx;
     return ISO_OK;
@@ -708,6 +907,7 @@ iso_status iso_extract_host(iso_ctx* ctx, iso_algorithm algo, const float* volum
     if (!volume) return ISO_ERR_INVALID_ARG;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     ISO_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (ctx->stream_host && stream_eligible(ctx, g)) return extract_host_streamed(ctx, algo, volume, grid, g, isoval, out, s);
     const size_t vbytes = (size_t)g.nx * g.ny * g.nz * sizeof(float);
     if (vbytes > ctx->d_volume_bytes) {
         ISO_CUDA(ctx, cudaStreamSynchronize(s));

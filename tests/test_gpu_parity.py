@@ -157,6 +157,20 @@ def test_host_entry_point(M):
     assert_same_mesh((m.points, m.normals, m.triangles), oracle_lib.mc(vol, 0.5, img.spacing, img.zeroPos))
 
 
+def test_host_entry_point_streamed(M):
+    """Grids of 128 planes and more take the streamed host path (slabs copied in,
+    counted, generated and copied back on overlapping streams)."""
+    cases = [((70, 45, 200), M.generate_value_noise((70, 45, 200), 3, 16, seed=6), 0.0, (1.0, 1.0, 1.0)),
+             ((64, 33, 130), M.generate_blobs((64, 33, 130), 7, seed=7), 0.45, (0.75, 1.5, 0.5))]
+    for dims, vol, iso, sp in cases:
+        img = M.Image3D.from_array(vol, sp, (2.0, -1.0, 0.25))
+        for algo, ref in ((M.FLYING_EDGES, oracle_lib.fe), (M.MARCHING_CUBES, oracle_lib.mc)):
+            want = ref(vol, iso, img.spacing, img.zeroPos)
+            for ib in (4, 8):
+                m = M.extract(img, iso, algo, index_bytes=ib)
+                assert_same_mesh((m.points, m.normals, m.triangles), want, "streamed %s ib %d" % (dims, ib))
+
+
 def test_fe_pass_by_pass_state(M):
     """gridEdges (xl, xr, xstart, ystart, zstart) and triCounter after pass 2
     and pass 3 equal the reference algorithm's state."""
