@@ -465,13 +465,17 @@ iso_status slab_prepare(iso_ctx* ctx, iso_algorithm algo, const float* volume, c
 
 // ---------------------------------------------------------------------------
 // Streamed host extraction: the volume goes to the device slab by slab on a
-// copy stream; each slab is counted as soon as its planes have landed,
-// generated with the offsets of the slabs before it into one of two device
-// staging meshes, and its part of the mesh goes back on a second copy stream
-// while the next slabs are copied and computed.  Host <-> device copies of
-// the whole volume and mesh overlap with each other and with the kernels.
+// copy stream, each slab's planes k0-1 .. k1+1 into one of kStreamWindows
+// device windows (so device memory does not grow with nz: volumes larger
+// than the device stream through); each slab is counted as soon as its
+// planes have landed, generated with the offsets of the slabs before it into
+// one of two device staging meshes, and its part of the mesh goes back on a
+// second copy stream while the next slabs are copied and computed.  Host <->
+// device copies of the volume and mesh overlap with each other and with the
+// kernels.
 // ---------------------------------------------------------------------------
 constexpr int kStreamPlanes = 64;  // planes per slab of the streamed path
+constexpr int kStreamWindows = 3;  // device windows of the volume
 
 cudaEvent_t sync_event(iso_ctx* ctx, size_t q)
 {
@@ -522,35 +526,41 @@ iso_status extract_host_streamed(iso_ctx* ctx, iso_algorithm algo, const float* 
     if (!ctx->s_d2h) ISO_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->s_d2h, cudaStreamNonBlocking));
     const int nz = gfull.nz;
     const size_t plane = (size_t)gfull.nx * gfull.ny;
-    const size_t vbytes = plane * nz * sizeof(float);
-    if (vbytes > ctx->d_volume_bytes) {
+    const int nslab = (nz + kStreamPlanes - 1) / kStreamPlanes;
+    auto slab_k0 = [&](int q) { return (int)((long long)q * nz / nslab); };
+    auto data_lo = [&](int q) { return std::max(slab_k0(q) - 1, 0); };
+    auto data_hi = [&](int q) { return std::min(slab_k0(q + 1) + 1, nz - 1); };  // inclusive
+    int wplanes = 0;
+    for (int q = 0; q < nslab; ++q) wplanes = std::max(wplanes, data_hi(q) - data_lo(q) + 1);
+    const size_t wbytes = (size_t)wplanes * plane * sizeof(float);
+    if (kStreamWindows * wbytes > ctx->d_volume_bytes) {
         ISO_CUDA(ctx, cudaDeviceSynchronize());
         cudaFree(ctx->d_volume);
         ctx->d_volume = nullptr;
         ctx->d_volume_bytes = 0;
-        ISO_CUDA(ctx, cudaMalloc(&ctx->d_volume, vbytes));
-        ctx->d_volume_bytes = vbytes;
+        ISO_CUDA(ctx, cudaMalloc(&ctx->d_volume, kStreamWindows * wbytes));
+        ctx->d_volume_bytes = kStreamWindows * wbytes;
     }
-    const int nslab = (nz + kStreamPlanes - 1) / kStreamPlanes;
-    auto slab_k0 = [&](int q) { return (int)((long long)q * nz / nslab); };
-    // all volume copies up front, in order; event q: planes slab q reads have landed
-    ISO_CUDA(ctx, cudaStreamWaitEvent(ctx->s_h2d, [&] {
-                     cudaEvent_t e = sync_event(ctx, 0);
-                     cudaEventRecord(e, s);  // after the caller's earlier work on s
-                     return e;
-                 }(), 0));
-    int copied = 0;  // planes [0, copied) are enqueued
-    for (int q = 0; q < nslab; ++q) {
-        const int need = std::min(slab_k0(q + 1) + 2, nz);  // planes .. k1+1
-        if (need > copied) {
-            ISO_CUDA(ctx, cudaMemcpyAsync(ctx->d_volume + copied * plane, volume + copied * plane,
-                                          (size_t)(need - copied) * plane * sizeof(float), cudaMemcpyHostToDevice,
-                                          ctx->s_h2d));
-            copied = need;
-        }
-        cudaEvent_t e = sync_event(ctx, 1 + q);
-        if (!e) return ISO_ERR_CUDA;
-        ISO_CUDA(ctx, cudaEventRecord(e, ctx->s_h2d));
+    auto window = [&](int q) { return ctx->d_volume + (size_t)(q % kStreamWindows) * wplanes * plane; };
+    // events: 1 + q the planes of slab q have landed; 1 + nslab + w window w is
+    // free again; 1 + nslab + kStreamWindows + sb slab generated into
+    // staging sb; 1 + nslab + kStreamWindows + 2 + sb staging sb copied out
+    const size_t ev_win = 1 + nslab, ev_gen = ev_win + kStreamWindows, ev_out = ev_gen + 2;
+    if (!sync_event(ctx, ev_out + 1)) return ISO_ERR_CUDA;
+    ISO_CUDA(ctx, cudaEventRecord(sync_event(ctx, 0), s));  // after the caller's earlier work on s
+    ISO_CUDA(ctx, cudaStreamWaitEvent(ctx->s_h2d, sync_event(ctx, 0), 0));
+    auto copy_in = [&](int q) -> iso_status {
+        if (q >= kStreamWindows)  // the window's previous slab is generated
+            ISO_CUDA(ctx, cudaStreamWaitEvent(ctx->s_h2d, sync_event(ctx, ev_win + q % kStreamWindows), 0));
+        const int lo = data_lo(q), hi = data_hi(q);
+        ISO_CUDA(ctx, cudaMemcpyAsync(window(q), volume + (size_t)lo * plane, (size_t)(hi - lo + 1) * plane * sizeof(float),
+                                      cudaMemcpyHostToDevice, ctx->s_h2d));
+        ISO_CUDA(ctx, cudaEventRecord(sync_event(ctx, 1 + q), ctx->s_h2d));
+        return ISO_OK;
+    };
+    for (int q = 0; q < std::min(nslab, kStreamWindows); ++q) {
+        const iso_status c = copy_in(q);
+        if (c != ISO_OK) return c;
     }
     const bool mc = algo == ISO_MARCHING_CUBES;
     long long V = 0, T = 0;
@@ -566,7 +576,7 @@ iso_status extract_host_streamed(iso_ctx* ctx, iso_algorithm algo, const float* 
         ISO_CUDA(ctx, cudaStreamWaitEvent(s, sync_event(ctx, 1 + q), 0));
         st = ensure_scratch(ctx, g, pl.cp, b, s);
         if (st != ISO_OK) break;
-        const float* win = ctx->d_volume + (size_t)g.kd * plane;
+        const float* win = window(q);  // holds planes g.kd = data_lo(q) ..
         SlabCounts c;
         st = slab_count(ctx, algo, win, g, k0, k1, isoval, pl, b, s, c);  // waits for the counts
         if (st != ISO_OK) break;
@@ -582,7 +592,7 @@ iso_status extract_host_streamed(iso_ctx* ctx, iso_algorithm algo, const float* 
             const int sb = q & 1;
             st = ensure_stage(ctx, Vq, Tq, out->index_bytes, s);
             if (st != ISO_OK) break;
-            if (q >= 2) ISO_CUDA(ctx, cudaStreamWaitEvent(s, sync_event(ctx, 1 + nslab + 2 + sb), 0));  // staging free
+            if (q >= 2) ISO_CUDA(ctx, cudaStreamWaitEvent(s, sync_event(ctx, ev_out + sb), 0));  // staging free
             if (mc) {
                 st = ensure_fe2mc(ctx, (long long)c.tot[0], s);
                 if (st != ISO_OK) break;
@@ -597,7 +607,7 @@ iso_status extract_host_streamed(iso_ctx* ctx, iso_algorithm algo, const float* 
             dm.cap_tris = Tq;
             st = slab_generate(ctx, algo, win, g, k0, k1, isoval, pl, b, c, V, T, &dm, s);
             if (st != ISO_OK) break;
-            cudaEvent_t gen_done = sync_event(ctx, 1 + nslab + sb);
+            cudaEvent_t gen_done = sync_event(ctx, ev_gen + sb);
             ISO_CUDA(ctx, cudaEventRecord(gen_done, s));
             ISO_CUDA(ctx, cudaStreamWaitEvent(ctx->s_d2h, gen_done, 0));
             if (Vq > 0) {
@@ -611,10 +621,16 @@ iso_status extract_host_streamed(iso_ctx* ctx, iso_algorithm algo, const float* 
                 ISO_CUDA(ctx, cudaMemcpyAsync(dst, dm.tris, (size_t)Tq * 3 * out->index_bytes, cudaMemcpyDeviceToHost,
                                               ctx->s_d2h));
             }
-            ISO_CUDA(ctx, cudaEventRecord(sync_event(ctx, 1 + nslab + 2 + sb), ctx->s_d2h));
+            ISO_CUDA(ctx, cudaEventRecord(sync_event(ctx, ev_out + sb), ctx->s_d2h));
         }
         V += Vq;
         T += Tq;
+        // window q % kStreamWindows is free once slab q's kernels are done: the next slab for it
+        ISO_CUDA(ctx, cudaEventRecord(sync_event(ctx, ev_win + q % kStreamWindows), s));
+        if (q + kStreamWindows < nslab) {
+            st = copy_in(q + kStreamWindows);
+            if (st != ISO_OK) break;
+        }
     }
     // the mesh has landed when both copy streams and s are done
     const iso_status sh = cudaStreamSynchronize(ctx->s_h2d) == cudaSuccess ? ISO_OK : ISO_ERR_CUDA;

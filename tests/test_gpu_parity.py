@@ -158,10 +158,12 @@ def test_host_entry_point(M):
 
 
 def test_host_entry_point_streamed(M):
-    """Grids of 128 planes and more take the streamed host path (slabs copied in,
-    counted, generated and copied back on overlapping streams)."""
+    """Grids of 128 planes and more take the streamed host path (slabs copied into
+    three device windows, counted, generated and copied back on overlapping
+    streams); 450 planes reuse every window twice."""
     cases = [((70, 45, 200), M.generate_value_noise((70, 45, 200), 3, 16, seed=6), 0.0, (1.0, 1.0, 1.0)),
-             ((64, 33, 130), M.generate_blobs((64, 33, 130), 7, seed=7), 0.45, (0.75, 1.5, 0.5))]
+             ((64, 33, 130), M.generate_blobs((64, 33, 130), 7, seed=7), 0.45, (0.75, 1.5, 0.5)),
+             ((40, 30, 450), M.generate_value_noise((40, 30, 450), 3, 8, seed=9), 0.1, (1.0, 0.5, 1.0))]
     for dims, vol, iso, sp in cases:
         img = M.Image3D.from_array(vol, sp, (2.0, -1.0, 0.25))
         for algo, ref in ((M.FLYING_EDGES, oracle_lib.fe), (M.MARCHING_CUBES, oracle_lib.mc)):
