@@ -48,7 +48,11 @@ typedef enum iso_status {
 
 typedef enum iso_algorithm {
     ISO_FLYING_EDGES = 0,    /* vertex order of flyingEdges/serial */
-    ISO_MARCHING_CUBES = 1   /* vertex order of marchingCubes/serial */
+    ISO_MARCHING_CUBES = 1,  /* vertex order of marchingCubes/serial */
+    ISO_MC_DUPFREE = 2       /* Marching Cubes with the vertices in global-edge-index order, the order
+                                util::duplicateRemover gives marchingCubes/openmpDupFree
+                                (marchingCubes/util/DuplicateRemover.h:38-103); rows of at most
+                                1024 points, whole-volume entry points only */
 } iso_algorithm;
 
 /* Geometry of a structured-points volume (Image3D's dims, spacing, zeroPos). */

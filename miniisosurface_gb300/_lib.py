@@ -25,6 +25,7 @@ PASS_NAMES = ("classify", "count", "scan", "fe_generate", "mc_vertices", "mc_tri
 
 ISO_FLYING_EDGES = 0
 ISO_MARCHING_CUBES = 1
+ISO_MC_DUPFREE = 2
 
 
 class IsoGrid(C.Structure):

@@ -24,6 +24,7 @@ from ._lib import IsoGrid, IsoMesh, check, load
 
 FLYING_EDGES = _lib.ISO_FLYING_EDGES
 MARCHING_CUBES = _lib.ISO_MARCHING_CUBES
+MC_DUPFREE = _lib.ISO_MC_DUPFREE  # MC, vertices in global-edge-index order (marchingCubes/openmpDupFree)
 
 
 class file_not_found(FileNotFoundError):
@@ -39,6 +40,8 @@ def _algo(a):
         return FLYING_EDGES
     if a in (MARCHING_CUBES, "mc", "marching_cubes", "MarchingCubes"):
         return MARCHING_CUBES
+    if a in (MC_DUPFREE, "mc_dupfree", "dupfree"):
+        return MC_DUPFREE
     raise ValueError("unknown algorithm %r" % (a,))
 
 

@@ -118,6 +118,11 @@ void build_case_tables(CaseTables& t)
     }
 }
 
+bool valid_algo(iso_algorithm a)
+{
+    return a == ISO_FLYING_EDGES || a == ISO_MARCHING_CUBES || a == ISO_MC_DUPFREE;
+}
+
 bool make_grid(const iso_grid* gr, Grid& g)
 {
     for (int a = 0; a < 3; ++a) {
@@ -144,8 +149,8 @@ bool empty_grid(const Grid& g) { return g.nx < 2 || g.ny < 2 || g.nz < 2; }
 size_t scratch_size(const Grid& g, const iso::CountPlan& cp)
 {
     const size_t R = (size_t)g.R;
-    return align256(R * 16) + align256(R * 8) + align256(R * 4) + align256(3 * R * 8) +
-           align256(3 * (size_t)cp.nseg * 8) + align256(4 * 8) + align256(R * (size_t)g.W * 4);
+    return align256(R * 16) + align256(R * 8) + align256(R * 4) + align256(4 * R * 8) +
+           align256(4 * (size_t)cp.nseg * 8) + align256(8 * 8) + align256(R * (size_t)g.W * 4);
 }
 
 void carve(void* base, const Grid& g, const iso::CountPlan& cp, FeBuffers& b)
@@ -155,9 +160,9 @@ void carve(void* base, const Grid& g, const iso::CountPlan& cp, FeBuffers& b)
     b.rowcnt = reinterpret_cast<uint4*>(p); p += align256(R * 16);
     b.trims = reinterpret_cast<uint2*>(p); p += align256(R * 8);
     b.mccnt = reinterpret_cast<uint32_t*>(p); p += align256(R * 4);
-    b.starts = reinterpret_cast<unsigned long long*>(p); p += align256(3 * R * 8);
-    b.part = reinterpret_cast<unsigned long long*>(p); p += align256(3 * (size_t)cp.nseg * 8);
-    b.totals = reinterpret_cast<unsigned long long*>(p); p += align256(4 * 8);
+    b.starts = reinterpret_cast<unsigned long long*>(p); p += align256(4 * R * 8);
+    b.part = reinterpret_cast<unsigned long long*>(p); p += align256(4 * (size_t)cp.nseg * 8);
+    b.totals = reinterpret_cast<unsigned long long*>(p); p += align256(8 * 8);
     b.bits = reinterpret_cast<uint32_t*>(p);
 }
 
@@ -264,7 +269,7 @@ void enqueue_count(iso_ctx* ctx, iso_algorithm algo, const float* vol, const Gri
     const bool mc = algo == ISO_MARCHING_CUBES;
     iso::launch_count(vol, g, iso, ctx->d_cases, mc, pl.cp, b, s);
     pm.mark(ISO_PASS_COUNT);
-    iso::launch_scan(g, pl.cp, mc, b, s);
+    iso::launch_scan(g, pl.cp, algo == ISO_MC_DUPFREE ? iso::kScanDup : (mc ? iso::kScanMC : iso::kScanFE), b, s);
     pm.mark(ISO_PASS_SCAN);
 }
 
@@ -292,6 +297,14 @@ void enqueue_generate(iso_ctx* ctx, iso_algorithm algo, const float* vol, const 
                                                   static_cast<uint64_t*>(out->tris), ctx->nsm, s);
         }
         pm.mark(ISO_PASS_FE_GENERATE);
+    } else if (algo == ISO_MC_DUPFREE) {  // vertices and triangles in one pass (make_plans checked fits)
+        if (i4)
+            iso::launch_dup_gen_warps<uint32_t>(vol, g, iso, ctx->d_cases, b, pl.cp, pl.gp, capV, capT, out->points,
+                                                out->normals, static_cast<uint32_t*>(out->tris), ctx->reverse, s);
+        else
+            iso::launch_dup_gen_warps<uint64_t>(vol, g, iso, ctx->d_cases, b, pl.cp, pl.gp, capV, capT, out->points,
+                                                out->normals, static_cast<uint64_t*>(out->tris), ctx->reverse, s);
+        pm.mark(ISO_PASS_MC_VERTICES);
     } else {
         const long long capM = capV < 0xffffffffll ? capV : 0xffffffffll;  // fe2mc holds 32-bit ids
         if (pl.gp.fits)
@@ -450,7 +463,7 @@ iso_status slab_prepare(iso_ctx* ctx, iso_algorithm algo, const float* volume, c
                         int64_t k1, Grid& g, Plans& pl, FeBuffers& b, cudaStream_t s)
 {
     if (!ctx || !grid) return ISO_ERR_INVALID_ARG;
-    if (algo != ISO_FLYING_EDGES && algo != ISO_MARCHING_CUBES) return ISO_ERR_INVALID_ARG;
+    if (algo != ISO_FLYING_EDGES && algo != ISO_MARCHING_CUBES) return ISO_ERR_INVALID_ARG;  // no Dup slabs
     if (!slab_grid(grid, algo, k0, k1, g)) return ISO_ERR_INVALID_ARG;
     if (empty_grid(g)) return ISO_OK;
     if (!volume) return ISO_ERR_INVALID_ARG;
@@ -514,9 +527,9 @@ iso_status ensure_stage(iso_ctx* ctx, long long V, long long T, int ib, cudaStre
     return ISO_OK;
 }
 
-bool stream_eligible(const iso_ctx* ctx, const Grid& g)
+bool stream_eligible(const iso_ctx* ctx, iso_algorithm algo, const Grid& g)
 {
-    return !empty_grid(g) && g.nz >= 2 * kStreamPlanes && iso::gen_plan(g, ctx->nsm).fits;
+    return algo != ISO_MC_DUPFREE && !empty_grid(g) && g.nz >= 2 * kStreamPlanes && iso::gen_plan(g, ctx->nsm).fits;
 }
 
 iso_status extract_host_streamed(iso_ctx* ctx, iso_algorithm algo, const float* volume, const iso_grid* grid,
@@ -841,7 +854,7 @@ iso_status iso_count_device(iso_ctx* ctx, iso_algorithm algo, const float* volum
                             float isoval, int64_t* n_points, int64_t* n_tris, void* stream)
 {
     if (!ctx || !grid || !n_points || !n_tris) return ISO_ERR_INVALID_ARG;
-    if (algo != ISO_FLYING_EDGES && algo != ISO_MARCHING_CUBES) return ISO_ERR_INVALID_ARG;
+    if (!valid_algo(algo)) return ISO_ERR_INVALID_ARG;
     Grid g;
     if (!make_grid(grid, g)) return ISO_ERR_INVALID_ARG;
     *n_points = 0;
@@ -868,7 +881,7 @@ iso_status iso_extract_device_async(iso_ctx* ctx, iso_algorithm algo, const floa
                                     float isoval, iso_mesh* out, int64_t* result_host, void* stream)
 {
     if (!ctx || !grid || !result_host) return ISO_ERR_INVALID_ARG;
-    if (algo != ISO_FLYING_EDGES && algo != ISO_MARCHING_CUBES) return ISO_ERR_INVALID_ARG;
+    if (!valid_algo(algo)) return ISO_ERR_INVALID_ARG;
     iso_status st = check_mesh(out);
     if (st != ISO_OK) return st;
     Grid g;
@@ -879,6 +892,10 @@ iso_status iso_extract_device_async(iso_ctx* ctx, iso_algorithm algo, const floa
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     ISO_CUDA(ctx, cudaSetDevice(ctx->device));
     const Plans pl = make_plans(ctx, g);
+    if (algo == ISO_MC_DUPFREE && !pl.gp.fits) {
+        ctx->last_error = "the duplicate-free order needs rows of at most 1024 points";
+        return ISO_ERR_INVALID_ARG;
+    }
     FeBuffers b;
     st = ensure_scratch(ctx, g, pl.cp, b, s);
     if (st != ISO_OK) return st;
@@ -913,7 +930,7 @@ iso_status iso_extract_host(iso_ctx* ctx, iso_algorithm algo, const float* volum
                             float isoval, iso_mesh* out, void* stream)
 {
     if (!ctx || !grid) return ISO_ERR_INVALID_ARG;
-    if (algo != ISO_FLYING_EDGES && algo != ISO_MARCHING_CUBES) return ISO_ERR_INVALID_ARG;
+    if (!valid_algo(algo)) return ISO_ERR_INVALID_ARG;
     iso_status st = check_mesh(out);
     if (st != ISO_OK) return st;
     Grid g;
@@ -923,7 +940,7 @@ iso_status iso_extract_host(iso_ctx* ctx, iso_algorithm algo, const float* volum
     if (!volume) return ISO_ERR_INVALID_ARG;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     ISO_CUDA(ctx, cudaSetDevice(ctx->device));
-    if (ctx->stream_host && stream_eligible(ctx, g)) return extract_host_streamed(ctx, algo, volume, grid, g, isoval, out, s);
+    if (ctx->stream_host && stream_eligible(ctx, algo, g)) return extract_host_streamed(ctx, algo, volume, grid, g, isoval, out, s);
     const size_t vbytes = (size_t)g.nx * g.ny * g.nz * sizeof(float);
     if (vbytes > ctx->d_volume_bytes) {
         ISO_CUDA(ctx, cudaStreamSynchronize(s));
@@ -935,6 +952,10 @@ iso_status iso_extract_host(iso_ctx* ctx, iso_algorithm algo, const float* volum
     }
     ISO_CUDA(ctx, cudaMemcpyAsync(ctx->d_volume, volume, vbytes, cudaMemcpyHostToDevice, s));
     const Plans pl = make_plans(ctx, g);
+    if (algo == ISO_MC_DUPFREE && !pl.gp.fits) {
+        ctx->last_error = "the duplicate-free order needs rows of at most 1024 points";
+        return ISO_ERR_INVALID_ARG;
+    }
     FeBuffers b;
     st = ensure_scratch(ctx, g, pl.cp, b, s);
     if (st != ISO_OK) return st;
@@ -1049,7 +1070,7 @@ iso_status iso_fe_pass3(iso_fe* fe)
     iso_ctx* ctx = fe->ctx;
     ISO_CUDA(ctx, cudaSetDevice(ctx->device));
     const Plans pl = make_plans(ctx, fe->g);
-    iso::launch_scan(fe->g, pl.cp, false, fe->buf, 0);
+    iso::launch_scan(fe->g, pl.cp, iso::kScanFE, fe->buf, 0);
     ISO_CUDA(ctx, cudaGetLastError());
     unsigned long long tot[4];
     ISO_CUDA(ctx, cudaMemcpy(tot, fe->buf.totals, sizeof(tot), cudaMemcpyDeviceToHost));

@@ -417,59 +417,78 @@ __global__ void __launch_bounds__(kThreads) k_count_wide(const float* __restrict
 constexpr int kScanPer = 8;
 constexpr int kSeg = kThreads * kScanPer;
 
-template <bool MC>
+// Scan modes: the components scanned per row.
+//   kScanFE   0: vertices (x+y+z cuts)  1: triangles
+//   kScanMC   0: vertices  1: triangles  2: MC vertices
+//   kScanDup  0: x cuts  1: triangles  2: y cuts  3: z cuts (the blocks of the
+//             global-edge-index order; totals[4], totals[5] = all x, all y cuts)
+template <int SM>
+struct ScanComps {
+    static constexpr int n = SM == kScanDup ? 4 : 3;
+};
+
+template <int SM>
 __device__ __forceinline__ void load_counts(const uint4* __restrict__ rowcnt, const uint32_t* __restrict__ mccnt,
-                                            long long R, long long b, uint32_t (&v)[3][kScanPer],
-                                            unsigned long long (&s)[3])
+                                            long long R, long long b, uint32_t (&v)[4][kScanPer],
+                                            unsigned long long (&s)[4])
 {
-    s[0] = s[1] = s[2] = 0;
+    s[0] = s[1] = s[2] = s[3] = 0;
 #pragma unroll
     for (int q = 0; q < kScanPer; ++q) {
         const bool ok = b + q < R;
         const uint4 c = ok ? __ldg(&rowcnt[b + q]) : make_uint4(0, 0, 0, 0);
-        v[0][q] = c.x + c.y + c.z;
+        if (SM == kScanDup) {
+            v[0][q] = c.x;
+            v[2][q] = c.y;
+            v[3][q] = c.z;
+        } else {
+            v[0][q] = c.x + c.y + c.z;
+            v[2][q] = (SM == kScanMC && ok) ? __ldg(&mccnt[b + q]) : 0u;
+            v[3][q] = 0u;
+        }
         v[1][q] = c.w;
-        v[2][q] = (MC && ok) ? __ldg(&mccnt[b + q]) : 0u;
 #pragma unroll
-        for (int a = 0; a < 3; ++a) s[a] += v[a][q];
+        for (int a = 0; a < 4; ++a) s[a] += v[a][q];
     }
 }
 
-template <bool MC>
+template <int SM>
 __global__ void __launch_bounds__(kThreads) k_scan_partial(const uint4* __restrict__ rowcnt,
                                                            const uint32_t* __restrict__ mccnt, long long R,
                                                            unsigned long long* __restrict__ part, int nseg)
 {
-    __shared__ unsigned long long s_w[3][kThreads / 32];
+    constexpr int NC = ScanComps<SM>::n;
+    __shared__ unsigned long long s_w[NC][kThreads / 32];
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    uint32_t v[3][kScanPer];
-    unsigned long long s[3];
-    load_counts<MC>(rowcnt, mccnt, R, (long long)blockIdx.x * kSeg + (long long)t * kScanPer, v, s);
+    uint32_t v[4][kScanPer];
+    unsigned long long s[4];
+    load_counts<SM>(rowcnt, mccnt, R, (long long)blockIdx.x * kSeg + (long long)t * kScanPer, v, s);
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
+    for (int a = 0; a < NC; ++a) {
 #pragma unroll
         for (int d = 16; d > 0; d >>= 1) s[a] += __shfl_xor_sync(0xffffffffu, s[a], d);
         if (lane == 0) s_w[a][warp] = s[a];
     }
     __syncthreads();
-    if (t < 3) {
+    if (t < NC) {
         unsigned long long tot = 0;
         for (int w = 0; w < kThreads / 32; ++w) tot += s_w[t][w];
         part[t * nseg + blockIdx.x] = tot;
     }
 }
 
-template <bool MC>
+template <int SM>
 __global__ void __launch_bounds__(kThreads) k_scan_final(const uint4* __restrict__ rowcnt,
                                                          const uint32_t* __restrict__ mccnt, long long R,
                                                          const unsigned long long* __restrict__ part, int nseg,
                                                          unsigned long long* __restrict__ starts,
                                                          unsigned long long* __restrict__ totals)
 {
-    __shared__ unsigned long long s_w[3][kThreads / 32];
-    __shared__ unsigned long long s_base[3];
+    constexpr int NC = ScanComps<SM>::n;
+    __shared__ unsigned long long s_w[NC][kThreads / 32];
+    __shared__ unsigned long long s_base[NC], s_tot[NC];
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    if (t < 3) {
+    if (t < NC) {
         unsigned long long b = 0, tot = 0;
         for (int q = 0; q < nseg; ++q) {
             const unsigned long long x = part[t * nseg + q];
@@ -477,14 +496,14 @@ __global__ void __launch_bounds__(kThreads) k_scan_final(const uint4* __restrict
             tot += x;
         }
         s_base[t] = b;
-        if (blockIdx.x == 0) totals[t] = tot;
+        s_tot[t] = tot;
     }
     const long long b = (long long)blockIdx.x * kSeg + (long long)t * kScanPer;
-    uint32_t v[3][kScanPer];
-    unsigned long long s[3], inc[3];
-    load_counts<MC>(rowcnt, mccnt, R, b, v, s);
+    uint32_t v[4][kScanPer];
+    unsigned long long s[4], inc[4];
+    load_counts<SM>(rowcnt, mccnt, R, b, v, s);
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
+    for (int a = 0; a < NC; ++a) {
         inc[a] = s[a];
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
@@ -494,8 +513,20 @@ __global__ void __launch_bounds__(kThreads) k_scan_final(const uint4* __restrict
         if (lane == 31) s_w[a][warp] = inc[a];
     }
     __syncthreads();
+    if (blockIdx.x == 0 && t == 0) {
+        if (SM == kScanDup) {
+            totals[0] = s_tot[0] + s_tot[2] + s_tot[3];
+            totals[1] = s_tot[1];
+            totals[2] = 0;
+            totals[4] = s_tot[0];
+            totals[5] = s_tot[2];
+        } else {
+            for (int a = 0; a < 3; ++a) totals[a] = s_tot[a];
+        }
+    }
 #pragma unroll
-    for (int a = 0; a < (MC ? 3 : 2); ++a) {
+    for (int a = 0; a < NC; ++a) {
+        if (SM == kScanFE && a == 2) continue;
         unsigned long long run = s_base[a] + inc[a] - s[a];
         for (int w = 0; w < warp; ++w) run += s_w[a][w];
 #pragma unroll
@@ -610,15 +641,19 @@ void launch_count(const float* vol, const Grid& g, float iso, const CaseTables* 
     else count_launch<false>(p, vol, g, iso, cases, b, s);
 }
 
-void launch_scan(const Grid& g, const CountPlan& p, bool mc, FeBuffers& b, cudaStream_t s)
+void launch_scan(const Grid& g, const CountPlan& p, int mode, FeBuffers& b, cudaStream_t s)
 {
-    if (mc) {
-        k_scan_partial<true><<<p.nseg, kThreads, 0, s>>>(b.rowcnt, b.mccnt, g.R, b.part, p.nseg);
-        k_scan_final<true><<<p.nseg, kThreads, 0, s>>>(b.rowcnt, b.mccnt, g.R, b.part, p.nseg, b.starts, b.totals);
+#define ISO_SCAN(SM)                                                                                            \
+    k_scan_partial<SM><<<p.nseg, kThreads, 0, s>>>(b.rowcnt, b.mccnt, g.R, b.part, p.nseg);                      \
+    k_scan_final<SM><<<p.nseg, kThreads, 0, s>>>(b.rowcnt, b.mccnt, g.R, b.part, p.nseg, b.starts, b.totals)
+    if (mode == kScanMC) {
+        ISO_SCAN(kScanMC);
+    } else if (mode == kScanDup) {
+        ISO_SCAN(kScanDup);
     } else {
-        k_scan_partial<false><<<p.nseg, kThreads, 0, s>>>(b.rowcnt, b.mccnt, g.R, b.part, p.nseg);
-        k_scan_final<false><<<p.nseg, kThreads, 0, s>>>(b.rowcnt, b.mccnt, g.R, b.part, p.nseg, b.starts, b.totals);
+        ISO_SCAN(kScanFE);
     }
+#undef ISO_SCAN
 }
 
 RowStarts row_starts(const Grid& g, const CountPlan& p, const FeBuffers& b)
@@ -629,7 +664,7 @@ RowStarts row_starts(const Grid& g, const CountPlan& p, const FeBuffers& b)
     rs.R = g.R;
     rs.ny = g.ny;
     rs.kr = g.kr;
-    rs.add[0] = rs.add[1] = rs.add[2] = 0;
+    rs.add[0] = rs.add[1] = rs.add[2] = rs.add[3] = 0;
     return rs;
 }
 

@@ -40,7 +40,7 @@ constexpr int kGenCells = 32;  // cells per batch
 constexpr int kGenTris = 5 * kGenCells;    // triangles of a batch, at most
 constexpr int kGenOwned = 12 * kGenCells;  // MC vertices owned by a batch, at most
 constexpr int kGenVq = 64;                 // FE vertex queue per axis and warp (a ring of two batches)
-enum GenMode { kGenFE = 0, kGenMC = 1, kGenTri = 2 };
+enum GenMode { kGenFE = 0, kGenMC = 1, kGenTri = 2, kGenDup = 3 };
 
 // Per-warp scratch in shared memory:
 //   mb[8][W]   {cut mask, id of its first cut edge - the row's first vertex}
@@ -52,12 +52,16 @@ enum GenMode { kGenFE = 0, kGenMC = 1, kGenTri = 2 };
 //   FE: vertex queues per axis (rings of kGenVq): ids (u64), then i | k << 10
 __host__ __device__ inline size_t gen_list_bytes(int mode)
 {
-    return mode == kGenMC ? (size_t)kGenOwned * 2 : (size_t)kGenTris;
+    return mode == kGenMC || mode == kGenDup ? (size_t)kGenOwned * 2 : (size_t)kGenTris;
 }
+//   Dup: db[8][W] the global-edge-index order id of each mask's first cut
+//        edge, after the list
 __host__ __device__ inline size_t gen_warp_scratch_bytes(int W, int mode)
 {
     const size_t vq = mode == kGenFE ? (size_t)3 * kGenVq * 12 : 0;
-    return ((size_t)8 * W * 8 + (size_t)8 * W * 4 + kGenCells * 4 + gen_list_bytes(mode) + vq + 15) & ~(size_t)15;
+    const size_t db = mode == kGenDup ? (size_t)8 * W * 8 : 0;
+    return ((size_t)8 * W * 8 + (size_t)8 * W * 4 + kGenCells * 4 + gen_list_bytes(mode) + vq + db + 15) &
+           ~(size_t)15;
 }
 
 // Divisors of the gradient: the reference divides by the spacing (one-sided
@@ -264,6 +268,17 @@ __device__ __forceinline__ uint32_t fe_edge_rel(const uint2* mb, int W, int e, i
     return p.y + __popc(p.x & lowmask(bit + off));
 }
 
+// Id in the global-edge-index order (x block, y block, z block) of cube edge
+// e of the cell at bit `bit` of word w: util::duplicateRemover's order
+// (marchingCubes/util/DuplicateRemover.h:38-103).
+__device__ __forceinline__ unsigned long long dup_edge_id(const uint2* mb, const unsigned long long* db, int W, int e,
+                                                          int w, int bit)
+{
+    const int sel = (int)((0x776653524140ull >> (4 * e)) & 7u);
+    const int off = (0xA22 >> e) & 1;
+    return db[sel * W + w] + __popc(mb[sel * W + w].x & lowmask(bit + off));
+}
+
 template <int MODE, typename IndexT>
 __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
     const float* __restrict__ vol, const uint32_t* __restrict__ bits, Grid g, GradScale gs, float iso, int KC,
@@ -274,9 +289,10 @@ __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
 {
     constexpr bool VOL = MODE != kGenTri;
     extern __shared__ __align__(16) unsigned char s_raw[];
+    constexpr bool OWNED = MODE == kGenMC || MODE == kGenDup;  // vertices computed by their owner cell
     __shared__ uint64_t s_tris[MODE == kGenMC ? 1 : 256];
-    __shared__ uint64_t s_order[MODE == kGenMC ? 256 : 1];
-    __shared__ uint16_t s_cut[MODE == kGenMC ? 256 : 1];
+    __shared__ uint64_t s_order[OWNED ? 256 : 1];
+    __shared__ uint16_t s_cut[OWNED ? 256 : 1];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int W = g.W;
     unsigned char* ws = s_raw + (size_t)warp * ws_bytes;
@@ -286,13 +302,13 @@ __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
     unsigned char* list = reinterpret_cast<unsigned char*>(cell + kGenCells);
     unsigned long long* vq_id = reinterpret_cast<unsigned long long*>(list + gen_list_bytes(MODE));
     uint32_t* vq_pos = reinterpret_cast<uint32_t*>(vq_id + 3 * kGenVq);
+    unsigned long long* db = reinterpret_cast<unsigned long long*>(list + gen_list_bytes(MODE));  // Dup
     for (int c = tid; c < 256; c += kThreads) {
-        if (MODE == kGenMC) {
+        if (OWNED) {
             s_order[c] = cases->order[c];
             s_cut[c] = cases->cut[c];
-        } else {
-            s_tris[c] = cases->tris[c];
         }
+        if (MODE != kGenMC) s_tris[c] = cases->tris[c];
     }
     __syncthreads();  // the only CTA barrier: from here on every warp runs alone
     if ((long long)totals[0] > capV || (long long)totals[1] > capT) return;  // caller grows buffers
@@ -325,7 +341,36 @@ __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
     // A = (j,p), B = (j+1,p), C = (j,p+1), D = (j+1,p+1); lane 4 the first
     // triangle (FE, TRI) or MC vertex (MC) of cell row A; lane 5 the x + y
     // cuts of row B.
+    // Dup instead: lanes 0..3 the first x cut of rows A..D, lane 4 the first
+    // triangle of cell row A, lanes 5, 6 the first y cut of rows A, C, lanes
+    // 7, 8 the first z cut of rows A, B (each block's own numbering).
+    auto load_starts_dup = [&](int p) -> unsigned long long {
+        const long long rA = (long long)(p - g.kr) * g.ny + j;
+        const bool hasZp = p + 1 < g.ke;
+        // (row offset dk * ny + dj, component, exists)
+        int dk = 0, dj = 0, comp = 0;
+        bool ok = true;
+        if (lane < 4) {
+            dk = (lane >> 1) & 1;
+            dj = lane & 1;
+            ok = (dj == 0 || hasY) && (dk == 0 || hasZp);
+        } else if (lane == 4) {
+            comp = 1;
+        } else if (lane <= 6) {
+            comp = 2;
+            dk = lane - 5;
+            ok = dk == 0 || hasZp;
+        } else if (lane <= 8) {
+            comp = 3;
+            dj = lane - 7;
+            ok = dj == 0 || hasY;
+        } else {
+            ok = false;
+        }
+        return ok ? rs.get(rA + (long long)dk * g.ny + dj, comp) : 0ull;
+    };
     auto load_starts = [&](int p) -> unsigned long long {
+        if (MODE == kGenDup) return load_starts_dup(p);
         const int dk = (lane >> 1) & 1, dj = lane & 1;
         const bool hasZp = p + 1 < g.ke;
         bool ok = lane < 6;
@@ -341,6 +386,8 @@ __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
         return rs.get(r, lane < 4 ? 0 : (MODE == kGenMC ? 2 : 1));
     };
 
+    const unsigned long long dupY = MODE == kGenDup ? totals[4] : 0ull;  // all x cuts
+    const unsigned long long dupZ = MODE == kGenDup ? totals[4] + totals[5] : 0ull;  // all x and y cuts
     uint32_t wA = 0, wB = 0, wC = 0, wD = 0;
     load_words(kb, wA, wB);
     load_words(kb + 1, wC, wD);
@@ -445,6 +492,11 @@ __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
         const unsigned long long ts = __shfl_sync(0xffffffffu, st, 4);
         const uint32_t cntB = (uint32_t)__shfl_sync(0xffffffffu, st, 5);
         const uint32_t nxA = t0 & 0xffffu, nyA = t2 & 0xffffu, nzA = t3 & 0xffffu, nxC = t1 & 0xffffu;
+        unsigned long long dxB[8];  // Dup: block starts of the 8 masks' rows (x A B C D, y A C, z A B)
+        if (MODE == kGenDup) {
+#pragma unroll
+            for (int q = 0; q < 8; ++q) dxB[q] = __shfl_sync(0xffffffffu, st, q < 4 ? q : q + 1);
+        }
         if (in) {  // first ids of the word's cut edges, relative to xsA
             mb[0 * W + lane] = make_uint2(m.xA, e0 & 0xffffu);
             mb[1 * W + lane] = make_uint2(m.xB, dB + (e0 >> 16));
@@ -454,6 +506,16 @@ __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
             mb[5 * W + lane] = make_uint2(m.yC, dC + nxC + (e2 >> 16));
             mb[6 * W + lane] = make_uint2(m.zA, nxA + nyA + (e3 & 0xffffu));
             mb[7 * W + lane] = make_uint2(m.zB, dB + cntB + (e3 >> 16));
+            if (MODE == kGenDup) {  // ids in the global-edge-index order: x block, y block, z block
+                db[0 * W + lane] = dxB[0] + (e0 & 0xffffu);
+                db[1 * W + lane] = dxB[1] + (e0 >> 16);
+                db[2 * W + lane] = dxB[2] + (e1 & 0xffffu);
+                db[3 * W + lane] = dxB[3] + (e1 >> 16);
+                db[4 * W + lane] = dupY + dxB[4] + (e2 & 0xffffu);
+                db[5 * W + lane] = dupY + dxB[5] + (e2 >> 16);
+                db[6 * W + lane] = dupZ + dxB[6] + (e3 & 0xffffu);
+                db[7 * W + lane] = dupZ + dxB[7] + (e3 >> 16);
+            }
             if (cellrow) {  // corner order of the cube case: bit v = corner v
                 uint4* t = reinterpret_cast<uint4*>(rwt + 8 * lane);
                 t[0] = make_uint4(rw.a, rw.ash, rw.bsh, rw.b);
@@ -462,7 +524,7 @@ __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
         }
         __syncwarp();
         Planes pl{};
-        if (MODE == kGenMC) {  // planes k-1 .. k+2; those outside the grid alias plane k
+        if (OWNED) {  // planes k-1 .. k+2; those outside the grid alias plane k
             pl.p1 = plane_ptr(k);
             pl.p0 = k > 0 ? plane_ptr(k - 1) : pl.p1;
             pl.p2 = hasZ ? plane_ptr(k + 1) : pl.p1;
@@ -526,7 +588,8 @@ __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
             const uint32_t ia = warp_incl_scan(na, lane);
             uint32_t rank = ia - na;
             const uint32_t tot = __shfl_sync(0xffffffffu, ia, 31);
-            unsigned long long tcur = ts;  // FE / TRI: next triangle; MC: next vertex
+            unsigned long long tcur = ts;  // FE / TRI / Dup: next triangle
+            unsigned long long mcur = ts;  // MC: next vertex
             for (uint32_t c0 = 0; c0 < tot; c0 += kGenCells) {
                 while (rem != 0u && rank < c0 + kGenCells) {
                     cell[rank - c0] = (uint32_t)(32 * lane + __ffs(rem) - 1);
@@ -550,7 +613,7 @@ __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
                     cell[lane] = rec;
                 }
                 const int cs = (int)(rec >> 16);
-                if (MODE == kGenFE || MODE == kGenTri) {
+                if (MODE != kGenMC) {
                     const uint32_t nt = live ? (uint32_t)iso_case_ntris(s_tris[cs]) : 0u;
                     const uint32_t it = warp_incl_scan(nt, lane);
                     const uint32_t ntb = __shfl_sync(0xffffffffu, it, 31);
@@ -568,14 +631,20 @@ __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
                             IndexT* o = tris + 3 * (tcur + t - tbase);
 #pragma unroll
                             for (int c = 0; c < 3; ++c) {
-                                const unsigned long long id =
-                                    xsA + fe_edge_rel(mb, W, iso_case_edge(tl, 3 * q + c), w, bit);
-                                o[c] = MODE == kGenTri ? (IndexT)__ldg(fe2mc + id) : (IndexT)id;
+                                const int e = iso_case_edge(tl, 3 * q + c);
+                                if (MODE == kGenDup) {
+                                    o[c] = (IndexT)dup_edge_id(mb, db, W, e, w, bit);
+                                } else {
+                                    const unsigned long long id = xsA + fe_edge_rel(mb, W, e, w, bit);
+                                    o[c] = MODE == kGenTri ? (IndexT)__ldg(fe2mc + id) : (IndexT)id;
+                                }
                             }
                         }
                     }
                     tcur += ntb;
-                } else {
+                }
+                if (MODE == kGenDup) __syncwarp();  // the vertex list below reuses the triangle list
+                if (OWNED) {
                     // ---- MC vertices owned by the batch's cells: cell order, then order of
                     // first appearance in the cell's triangle list
                     const int ci = (int)(rec & 0xffffu);
@@ -600,7 +669,9 @@ __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
                             const uint32_t cr = cell[vr & 31u];
                             const int e12 = (int)(vr >> 5);
                             const int i = (int)(cr & 0xffffu);
-                            const unsigned long long id = tcur + v;
+                            // MC: owner order; Dup: the edge's place in the global-edge-index order
+                            const unsigned long long id =
+                                MODE == kGenDup ? dup_edge_id(mb, db, W, e12, i >> 5, i & 31) : mcur + v;
                             if (k >= kemit) {  // cell rows below kemit belong to the slab below: map only
                                 int dx, dy, dz, axis;
                                 cube_edge_geometry(e12, dx, dy, dz, axis);
@@ -608,10 +679,10 @@ __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
                                 vertex_on_edge(pl, g, gs, iso, axis, i + dx, j + dy, 1 + dz, k + dz, i, j, k, p, n);
                                 store_vertex(points, normals, id - vbase, p, n);
                             }
-                            fe2mc[xsA + fe_edge_rel(mb, W, e12, i >> 5, i & 31)] = (uint32_t)id;
+                            if (MODE == kGenMC) fe2mc[xsA + fe_edge_rel(mb, W, e12, i >> 5, i & 31)] = (uint32_t)id;
                         }
                     }
-                    tcur += nob;
+                    mcur += nob;
                 }
                 __syncwarp();  // the next batch overwrites the lists
             }

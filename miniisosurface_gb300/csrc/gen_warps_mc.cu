@@ -1,6 +1,6 @@
 // Marching Cubes pass 4 (warp-per-row kernels of gen_warps.cuh): vertices in
 // owner order with the Flying Edges -> MC index map, then the triangles with
-// their corners mapped.
+// their corners mapped; and the duplicate-free order in one pass.
 #include "gen_warps.cuh"
 
 namespace iso {
@@ -21,6 +21,21 @@ void launch_mc_tri_warps(const Grid& g, const CaseTables* cases, const FeBuffers
                                            s);
 }
 
+template <typename IndexT>
+void launch_dup_gen_warps(const float* vol, const Grid& g, float iso, const CaseTables* cases, const FeBuffers& b,
+                          const CountPlan& cp, const GenPlan& p, long long capV, long long capT, float* points,
+                          float* normals, IndexT* tris, int reverse, cudaStream_t s)
+{
+    launch_gen_warps_impl<kGenDup, IndexT>(vol, g, iso, cases, b, cp, p, capV, capT, points, normals, tris, reverse,
+                                           s);
+}
+
+template void launch_dup_gen_warps<uint32_t>(const float*, const Grid&, float, const CaseTables*, const FeBuffers&,
+                                             const CountPlan&, const GenPlan&, long long, long long, float*, float*,
+                                             uint32_t*, int, cudaStream_t);
+template void launch_dup_gen_warps<uint64_t>(const float*, const Grid&, float, const CaseTables*, const FeBuffers&,
+                                             const CountPlan&, const GenPlan&, long long, long long, float*, float*,
+                                             uint64_t*, int, cudaStream_t);
 template void launch_mc_tri_warps<uint32_t>(const Grid&, const CaseTables*, const FeBuffers&, const CountPlan&,
                                             const GenPlan&, long long, long long, uint32_t*, cudaStream_t);
 template void launch_mc_tri_warps<uint64_t>(const Grid&, const CaseTables*, const FeBuffers&, const CountPlan&,

@@ -559,7 +559,7 @@ struct RowStarts {
     const unsigned long long* starts;
     long long R;
     int ny, kr;
-    unsigned long long add[3];
+    unsigned long long add[4];
     __device__ __forceinline__ unsigned long long get(long long r, int comp) const
     {
         return __ldg(&starts[comp * R + r]) + add[comp];

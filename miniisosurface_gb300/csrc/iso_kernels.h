@@ -16,9 +16,9 @@ struct FeBuffers {
     uint4* rowcnt = nullptr;               // R      x/y/z cuts, triangles
     uint2* trims = nullptr;                // R      xl, xr (pass 1 trims)
     uint32_t* mccnt = nullptr;             // R      MC vertices per cell row
-    unsigned long long* starts = nullptr;  // 3*R    first vertex, triangle, MC vertex of each row
-    unsigned long long* part = nullptr;    // 3*nseg scan segment totals
-    unsigned long long* totals = nullptr;  // 4      vertices, triangles, mc vertices, status
+    unsigned long long* starts = nullptr;  // 4*R    per row: first vertex, triangle, MC vertex (or y, z cuts)
+    unsigned long long* part = nullptr;    // 4*nseg scan segment totals
+    unsigned long long* totals = nullptr;  // 8      vertices, triangles, mc vertices, status, x cuts, y cuts
     uint32_t* bits = nullptr;              // R*W    bit rows (row-wise kernels only)
     uint32_t* fe2mc = nullptr;             // >= V   FE vertex index -> MC index
 };
@@ -40,7 +40,7 @@ struct GenPlan {
     int J = 8, nyb = 1, KC = 1, nkc = 1;
     int kbeg = 0, kend = 0, kemit = 0;
     unsigned long long vbase = 0, tbase = 0;
-    unsigned long long add[3] = {0, 0, 0};
+    unsigned long long add[4] = {0, 0, 0, 0};
     size_t smem = 0;  // per-warp scratch of the CTA
     bool fits = false;  // false: use the row-wise kernels
 };
@@ -61,7 +61,8 @@ void gen_split(GenPlan& p, int nsm);  // columns over [p.kbeg, p.kend)
 // passes 1-3
 void launch_count(const float* vol, const Grid& g, float iso, const CaseTables* cases, bool mc,
                   const CountPlan& p, FeBuffers& b, cudaStream_t s);
-void launch_scan(const Grid& g, const CountPlan& p, bool mc, FeBuffers& b, cudaStream_t s);
+enum ScanMode { kScanFE = 0, kScanMC = 1, kScanDup = 2 };
+void launch_scan(const Grid& g, const CountPlan& p, int mode, FeBuffers& b, cudaStream_t s);
 void launch_grid_edges(const Grid& g, const CountPlan& p, const FeBuffers& b, int scanned, unsigned long long* ge,
                        unsigned long long* tri_counter, cudaStream_t s);
 // Row-start accessor of a counted extraction.
@@ -75,6 +76,11 @@ void launch_fe_gen_warps(const float* vol, const Grid& g, float iso, const CaseT
 void launch_mc_gen_warps(const float* vol, const Grid& g, float iso, const CaseTables* cases, const FeBuffers& b,
                          const CountPlan& cp, const GenPlan& p, long long capV, long long capT, float* points,
                          float* normals, int reverse, cudaStream_t s);
+// pass 4 of the global-edge-index (duplicate-free) Marching Cubes order
+template <typename IndexT>
+void launch_dup_gen_warps(const float* vol, const Grid& g, float iso, const CaseTables* cases, const FeBuffers& b,
+                          const CountPlan& cp, const GenPlan& p, long long capV, long long capT, float* points,
+                          float* normals, IndexT* tris, int reverse, cudaStream_t s);
 template <typename IndexT>
 void launch_mc_tri_warps(const Grid& g, const CaseTables* cases, const FeBuffers& b, const CountPlan& cp,
                          const GenPlan& p, long long capV, long long capT, IndexT* tris, cudaStream_t s);

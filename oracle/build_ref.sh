@@ -8,6 +8,7 @@
 #   flyingEdgesOpenMP  flyingEdges/openmp/{main,FlyingEdgesAlgorithm}.cpp
 #   mcSerial           marchingCubes/serial/main.cpp
 #   mcOpenMP           marchingCubes/openmp/main.cpp
+#   mcOpenMPDupFree    marchingCubes/openmpDupFree/main.cpp
 #   SameContentsCheck  utilities/tests/SameContentsCheck.cpp
 #
 # The reference's CMake files are not used (they need CMake >= 2.8 policies
@@ -26,6 +27,7 @@ $CXX $FLAGS -o "$OUT/flyingEdgesSerial" "$REF/flyingEdges/serial/main.cpp" "$REF
 $CXX $FLAGS -fopenmp -o "$OUT/flyingEdgesOpenMP" "$REF/flyingEdges/openmp/main.cpp" "$REF/flyingEdges/openmp/FlyingEdgesAlgorithm.cpp" $FE_UTIL &
 $CXX $FLAGS -o "$OUT/mcSerial" "$REF/marchingCubes/serial/main.cpp" $MC_UTIL &
 $CXX $FLAGS -fopenmp -o "$OUT/mcOpenMP" "$REF/marchingCubes/openmp/main.cpp" $MC_UTIL &
+$CXX $FLAGS -fopenmp -o "$OUT/mcOpenMPDupFree" "$REF/marchingCubes/openmpDupFree/main.cpp" $MC_UTIL &
 $CXX $FLAGS -o "$OUT/SameContentsCheck" "$REF/utilities/tests/SameContentsCheck.cpp" -I"$REF/marchingCubes/util" &
 wait
 ls "$OUT"

@@ -208,3 +208,53 @@ int oracle_mc_run(const float* data, const size_t dims[3], const float spacing[3
 }
 
 double oracle_mc_last_wall_seconds(void) { return g_mc_wall; }
+
+/* util::duplicateRemover (marchingCubes/util/DuplicateRemover.h:38-103) for a
+ * mesh made by one section: the vertices sorted by global edge index (each
+ * edge appears once), triangles renumbered.  This is what
+ * marchingCubes/openmpDupFree returns with one thread. */
+typedef struct {
+    size_t gid, idx;
+} gid_pair;
+
+static int cmp_gid(const void* a, const void* b)
+{
+    const size_t x = ((const gid_pair*)a)->gid, y = ((const gid_pair*)b)->gid;
+    return x < y ? -1 : (x > y ? 1 : 0);
+}
+
+int oracle_mc_dupfree_run(const float* data, const size_t dims[3], const float spacing[3], const float origin[3],
+                          float isoval, oracle_mesh* out)
+{
+    int st = oracle_mc_run(data, dims, spacing, origin, isoval, out);
+    if (st != 0 || out->n_points == 0) return st;
+    const size_t n = out->n_points;
+    gid_pair* pr = (gid_pair*)malloc(n * sizeof(gid_pair));
+    size_t* newidx = (size_t*)malloc(n * sizeof(size_t));
+    float* pts = (float*)malloc(3 * n * sizeof(float));
+    float* nrm = (float*)malloc(3 * n * sizeof(float));
+    size_t* eov = (size_t*)malloc(n * sizeof(size_t));
+    if (!pr || !newidx || !pts || !nrm || !eov) return 1;
+    for (size_t i = 0; i < n; ++i) {
+        pr[i].gid = out->edge_of_vertex[i];
+        pr[i].idx = i;
+    }
+    qsort(pr, n, sizeof(gid_pair), cmp_gid);
+    for (size_t r = 0; r < n; ++r) {
+        const size_t o = pr[r].idx;
+        newidx[o] = r;
+        memcpy(pts + 3 * r, out->points + 3 * o, 3 * sizeof(float));
+        memcpy(nrm + 3 * r, out->normals + 3 * o, 3 * sizeof(float));
+        eov[r] = pr[r].gid;
+    }
+    for (size_t t = 0; t < 3 * out->n_tris; ++t) out->tris[t] = newidx[out->tris[t]];
+    free(out->points);
+    free(out->normals);
+    free(out->edge_of_vertex);
+    out->points = pts;
+    out->normals = nrm;
+    out->edge_of_vertex = eov;
+    free(pr);
+    free(newidx);
+    return 0;
+}

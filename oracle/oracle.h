@@ -63,6 +63,12 @@ int oracle_fe_run(const float* data, const size_t dims[3], const float spacing[3
 int oracle_mc_run(const float* data, const size_t dims[3], const float spacing[3],
                   const float origin[3], float isoval, oracle_mesh* out);
 
+/* The same mesh with its vertices in global-edge-index order
+ * (util::duplicateRemover, marchingCubes/util/DuplicateRemover.h:38-103):
+ * marchingCubes/openmpDupFree's output with one thread. */
+int oracle_mc_dupfree_run(const float* data, const size_t dims[3], const float spacing[3],
+                          const float origin[3], float isoval, oracle_mesh* out);
+
 void oracle_mesh_free(oracle_mesh* m);
 
 /* Seconds of wall time of the last oracle_fe_run / oracle_mc_run call

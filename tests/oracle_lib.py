@@ -40,6 +40,7 @@ def lib():
         f3 = C.c_float * 3
         L.oracle_fe_run.argtypes = [C.c_void_p, sz3, f3, f3, C.c_float, C.c_int, C.POINTER(OracleMesh)]
         L.oracle_mc_run.argtypes = [C.c_void_p, sz3, f3, f3, C.c_float, C.POINTER(OracleMesh)]
+        L.oracle_mc_dupfree_run.argtypes = [C.c_void_p, sz3, f3, f3, C.c_float, C.POINTER(OracleMesh)]
         L.oracle_mesh_free.argtypes = [C.POINTER(OracleMesh)]
         L.oracle_fe_create.restype = C.c_void_p
         L.oracle_fe_create.argtypes = [C.c_void_p, sz3, f3, f3, C.c_float, C.c_int]
@@ -103,6 +104,21 @@ def mc(vol, iso, spacing=(1, 1, 1), origin=(0, 0, 0)):
                 np.zeros(0, np.uint64))
     m = OracleMesh()
     L.oracle_mc_run(vol.ctypes.data, dims, sp, org, C.c_float(iso), C.byref(m))
+    try:
+        return _mesh_to_numpy(m)
+    finally:
+        L.oracle_mesh_free(C.byref(m))
+
+
+def mc_dupfree(vol, iso, spacing=(1, 1, 1), origin=(0, 0, 0)):
+    """Oracle MC with vertices in global-edge-index order (marchingCubes/openmpDupFree, one thread)."""
+    L = lib()
+    vol, dims, sp, org = _args(vol, spacing, origin)
+    if any(d < 2 for d in vol.shape):
+        return (np.zeros((0, 3), np.float32), np.zeros((0, 3), np.float32), np.zeros((0, 3), np.uint64),
+                np.zeros(0, np.uint64))
+    m = OracleMesh()
+    L.oracle_mc_dupfree_run(vol.ctypes.data, dims, sp, org, C.c_float(iso), C.byref(m))
     try:
         return _mesh_to_numpy(m)
     finally:

@@ -173,6 +173,28 @@ def test_host_entry_point_streamed(M):
                 assert_same_mesh((m.points, m.normals, m.triangles), want, "streamed %s ib %d" % (dims, ib))
 
 
+def test_mc_dupfree_matches_oracle(M):
+    """ISO_MC_DUPFREE: the serial MC mesh with vertices in global-edge-index
+    order (marchingCubes/openmpDupFree with one section), bit for bit."""
+    import torch
+
+    cases = [((128, 128, 128), M.generate_blobs((128, 128, 128), 8, seed=0), 0.5, (1, 1, 1), (0, 0, 0)),
+             ((61, 37, 29), M.generate_value_noise((61, 37, 29), 3, 8, seed=2), 0.05, (0.3, 1.7, 0.9), (3, -2, 1)),
+             ((33, 2, 2), np.random.default_rng(4).standard_normal((2, 2, 33)).astype(np.float32), 0.0, (1, 1, 1),
+              (0, 0, 0)),
+             ((1000, 5, 4), M.generate_value_noise((1000, 5, 4), 4, 16, seed=3), 0.0, (1, 1, 1), (0, 0, 0))]
+    for dims, vol, iso, sp, org in cases:
+        want = oracle_lib.mc_dupfree(vol, iso, sp, org)
+        for ib in (4, 8):
+            got = gpu_extract(M, vol, iso, M.MC_DUPFREE, sp, org, index_bytes=ib)
+            assert_same_mesh(got, want, "dupfree %s" % (dims,))
+        img = M.Image3D.from_array(vol, sp, org)
+        m = M.extract(img, iso, M.MC_DUPFREE)
+        assert_same_mesh((m.points, m.normals, m.triangles), want, "dupfree host %s" % (dims,))
+        flat = torch.from_numpy(np.ascontiguousarray(vol).reshape(-1)).cuda()
+        assert M.count_device(flat, dims, iso, M.MC_DUPFREE) == (len(want[0]), len(want[2]))
+
+
 def test_fe_pass_by_pass_state(M):
     """gridEdges (xl, xr, xstart, ystart, zstart) and triCounter after pass 2
     and pass 3 equal the reference algorithm's state."""

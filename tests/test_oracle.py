@@ -105,6 +105,44 @@ def test_oracle_vs_reference_programs(built, seed):
         assert np.array_equal(rn.view(np.uint32), n.view(np.uint32)), prog
 
 
+def _ulps(a, b):
+    ia = a.view(np.int32).astype(np.int64)
+    ib = b.view(np.int32).astype(np.int64)
+    ia = np.where(ia < 0, np.int64(-2**31) - ia, ia)
+    ib = np.where(ib < 0, np.int64(-2**31) - ib, ib)
+    return np.abs(ia - ib)
+
+
+@pytest.mark.skipif(not oracle_lib.ref_available("mcOpenMPDupFree"), reason="reference programs not built here")
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_dupfree_oracle_vs_reference_program(built, seed):
+    """marchingCubes/openmpDupFree: with one thread (one section) its mesh is
+    the oracle's global-edge-index order bit for bit; with four sections the
+    vertices are the same in the same order, a seam vertex computed by the
+    cell on either side of the seam (positions within 2 ulp, normals equal),
+    and the triangles the same set."""
+    import miniisosurface_gb300 as M
+
+    rng = np.random.default_rng(100 + seed)
+    dims = tuple(int(x) for x in rng.integers(8, 40, 3))
+    vol = M.generate_value_noise(dims, 4, 8, seed=seed)
+    iso = float(rng.uniform(-0.3, 0.3))
+    sp = tuple(float(np.float32(x)) for x in rng.uniform(0.1, 3, 3))
+    org = tuple(float(np.float32(x)) for x in rng.uniform(-10, 10, 3))
+    p, n, t, eov = oracle_lib.mc_dupfree(vol, iso, sp, org)
+    assert np.all(np.diff(eov.astype(np.int64)) > 0)  # strictly increasing global edge index
+    rp, rn, rt, _, _ = oracle_lib.run_ref("mcOpenMPDupFree", vol, iso, sp, org, threads=1)
+    assert np.array_equal(rt, t)
+    assert np.array_equal(rp.view(np.uint32), p.view(np.uint32))
+    assert np.array_equal(rn.view(np.uint32), n.view(np.uint32))
+    rp4, rn4, rt4, _, _ = oracle_lib.run_ref("mcOpenMPDupFree", vol, iso, sp, org, threads=4)
+    assert rp4.shape == p.shape
+    assert _ulps(rp4, p).max() <= 2
+    assert np.array_equal(rn4.view(np.uint32), n.view(np.uint32))
+    key = lambda a: a[np.lexsort(a.T[::-1])]
+    assert np.array_equal(key(rt4), key(t.astype(rt4.dtype)))
+
+
 @needs_ref
 def test_product_image_writer_readable_by_reference(built, tmp_path):
     """A volume written by iso_vtk_write_image loads in the reference loader."""
