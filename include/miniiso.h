@@ -56,6 +56,18 @@ typedef enum iso_algorithm {
 } iso_algorithm;
 
 /* Geometry of a structured-points volume (Image3D's dims, spacing, zeroPos). */
+/* Sample types of a volume: the VTK scalar types the reference reads
+ * (flyingEdges/util/ConvertBuffer.h:45-72, TypeInfo.h) plus unsigned char. */
+typedef enum iso_dtype {
+    ISO_FLOAT32 = 0, /* float */
+    ISO_INT8 = 1,    /* char (signed, as the reference's x86 hosts read it) */
+    ISO_UINT8 = 2,   /* unsigned_char */
+    ISO_INT16 = 3,   /* short */
+    ISO_UINT16 = 4,  /* unsigned_short */
+    ISO_INT32 = 5,   /* int */
+    ISO_FLOAT64 = 6  /* double */
+} iso_dtype;
+
 typedef struct iso_grid {
     int64_t dims[3];
     float spacing[3];
@@ -173,6 +185,17 @@ iso_status iso_count_slab(iso_ctx* ctx, iso_algorithm algo, const float* volume,
 iso_status iso_extract_slab(iso_ctx* ctx, iso_algorithm algo, const float* volume, const iso_grid* grid, int64_t k0,
                             int64_t k1, float isoval, int64_t point_offset, int64_t tri_offset, iso_mesh* out,
                             void* stream);
+
+/* Typed volumes: samples of `dtype`, converted to float32 on the device with
+ * the reference's C cast to scalar_t (ConvertBuffer.h:45-72), then extracted
+ * as float32 -- the same mesh as converting on the host first.  The narrow
+ * types cross the host -> device link in 1/4 (8-bit) or 1/2 (16-bit) of the
+ * bytes.  volume is a device pointer (_device_typed) or a host pointer
+ * (_host_typed); otherwise as iso_extract_device / iso_extract_host. */
+iso_status iso_extract_device_typed(iso_ctx* ctx, iso_algorithm algo, const void* volume, iso_dtype dtype,
+                                    const iso_grid* grid, float isoval, iso_mesh* out, void* stream);
+iso_status iso_extract_host_typed(iso_ctx* ctx, iso_algorithm algo, const void* volume, iso_dtype dtype,
+                                  const iso_grid* grid, float isoval, iso_mesh* out, void* stream);
 
 /* Host in, host out: copies the volume to the device, extracts, and copies
  * the mesh back into the caller's host buffers (pinned buffers give the full

@@ -27,6 +27,9 @@ ISO_FLYING_EDGES = 0
 ISO_MARCHING_CUBES = 1
 ISO_MC_DUPFREE = 2
 
+# iso_dtype
+ISO_FLOAT32, ISO_INT8, ISO_UINT8, ISO_INT16, ISO_UINT16, ISO_INT32, ISO_FLOAT64 = range(7)
+
 
 class IsoGrid(C.Structure):
     _fields_ = [("dims", C.c_int64 * 3), ("spacing", C.c_float * 3), ("origin", C.c_float * 3)]
@@ -56,6 +59,10 @@ SIGNATURES = {
                                  C.c_float, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.c_void_p]),
     "iso_extract_slab": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.POINTER(IsoGrid), C.c_int64, C.c_int64,
                                    C.c_float, C.c_int64, C.c_int64, C.POINTER(IsoMesh), C.c_void_p]),
+    "iso_extract_device_typed": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.POINTER(IsoGrid), C.c_float,
+                                           C.POINTER(IsoMesh), C.c_void_p]),
+    "iso_extract_host_typed": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.POINTER(IsoGrid), C.c_float,
+                                         C.POINTER(IsoMesh), C.c_void_p]),
     "iso_extract_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.POINTER(IsoGrid), C.c_float,
                                      C.POINTER(IsoMesh), C.c_void_p]),
     "iso_extract_device_async": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.POINTER(IsoGrid), C.c_float,

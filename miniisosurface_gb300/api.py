@@ -54,6 +54,18 @@ def _ptr(x):
     return x.ctypes.data
 
 
+_DTYPES = {"float32": _lib.ISO_FLOAT32, "int8": _lib.ISO_INT8, "uint8": _lib.ISO_UINT8, "int16": _lib.ISO_INT16,
+           "uint16": _lib.ISO_UINT16, "int32": _lib.ISO_INT32, "float64": _lib.ISO_FLOAT64}
+
+
+def _dtype_code(dtype):
+    """iso_dtype of a numpy or torch dtype (the VTK scalar types the reference reads, plus uint8)."""
+    name = str(dtype).replace("torch.", "")
+    if name not in _DTYPES:
+        raise ValueError("unsupported sample type %s" % (dtype,))
+    return _DTYPES[name]
+
+
 def make_grid(dims, spacing=(1.0, 1.0, 1.0), origin=(0.0, 0.0, 0.0)):
     g = IsoGrid()
     for a in range(3):
@@ -188,6 +200,30 @@ def extract(image, isoval, algorithm=FLYING_EDGES, index_bytes=8, ctx=None):
     raise RuntimeError("output size changed between two extractions of the same volume")
 
 
+def extract_typed(volume, isoval, algorithm=FLYING_EDGES, spacing=(1, 1, 1), origin=(0, 0, 0), index_bytes=8,
+                  ctx=None):
+    """Host array of any supported sample type ([k][j][i]) in, TriangleMesh out:
+    the samples cross to the device as they are and become float32 there
+    (iso_extract_host_typed); the mesh equals extracting volume.astype(float32)."""
+    lib = load()
+    ctx = ctx or default_context()
+    algo = _algo(algorithm)
+    vol = np.ascontiguousarray(volume)
+    dcode = _dtype_code(vol.dtype)
+    g = make_grid((vol.shape[2], vol.shape[1], vol.shape[0]), spacing, origin)
+    nv, nt = 0, 0
+    for _ in range(2):
+        m, pts, nrm, tri = _host_mesh_buffers(nv, nt, index_bytes)
+        st = lib.iso_extract_host_typed(ctx.handle, algo, _ptr(vol), dcode, C.byref(g), C.c_float(isoval), C.byref(m),
+                                        None)
+        if st == _lib.ISO_ERR_CAPACITY:
+            nv, nt = m.n_points, m.n_tris
+            continue
+        check(st, ctx.handle)
+        return TriangleMesh(pts[: m.n_points], nrm[: m.n_points], tri[: m.n_tris])
+    raise RuntimeError("output size changed between two extractions of the same volume")
+
+
 def MarchingCubes(image, isoval, ctx=None):
     """marchingCubes/serial/main.cpp:42-192: mesh with MC vertex numbering."""
     return extract(image, isoval, MARCHING_CUBES, 8, ctx)
@@ -284,15 +320,20 @@ def extract_device(volume, dims, isoval, algorithm=FLYING_EDGES, spacing=(1, 1, 
     ctx = ctx or default_context(volume.device.index or 0)
     algo = _algo(algorithm)
     g = make_grid(dims, spacing, origin)
-    if not volume.is_cuda or volume.dtype != torch.float32 or not volume.is_contiguous():
-        raise ValueError("volume must be a contiguous float32 CUDA tensor")
+    if not volume.is_cuda or not volume.is_contiguous():
+        raise ValueError("volume must be a contiguous CUDA tensor")
+    dcode = _dtype_code(volume.dtype)  # narrow types are converted to float32 on the device
     s = stream if stream is not None else torch.cuda.current_stream(volume.device).cuda_stream
     if out is None:
         out = DeviceMesh(0, 0, index_bytes, volume.device)
     for _ in range(2):
         m = out.descriptor()
-        st = lib.iso_extract_device(ctx.handle, algo, _ptr(volume), C.byref(g), C.c_float(isoval), C.byref(m),
-                                    C.c_void_p(s))
+        if dcode == _lib.ISO_FLOAT32:
+            st = lib.iso_extract_device(ctx.handle, algo, _ptr(volume), C.byref(g), C.c_float(isoval), C.byref(m),
+                                        C.c_void_p(s))
+        else:
+            st = lib.iso_extract_device_typed(ctx.handle, algo, _ptr(volume), dcode, C.byref(g), C.c_float(isoval),
+                                              C.byref(m), C.c_void_p(s))
         if st == _lib.ISO_ERR_CAPACITY:
             out = DeviceMesh(m.n_points, m.n_tris, out.index_bytes, volume.device)
             continue

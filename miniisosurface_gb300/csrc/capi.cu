@@ -36,6 +36,8 @@ struct iso_ctx {
     int d_index_bytes = 0;
     unsigned long long* h_totals = nullptr;  // pinned, 4 entries
     unsigned long long* h_slab = nullptr;    // pinned, 9 entries (slab counts)
+    void* d_typed = nullptr;                 // typed volume samples before conversion
+    size_t d_typed_bytes = 0;
     // streamed host entry point: copy streams, events, two device staging meshes
     cudaStream_t s_h2d = nullptr, s_d2h = nullptr;
     std::vector<cudaEvent_t> sync_events;
@@ -182,6 +184,19 @@ iso_status ensure_scratch(iso_ctx* ctx, const Grid& g, const iso::CountPlan& cp,
     }
     carve(ctx->scratch, g, cp, b);
     b.fe2mc = ctx->fe2mc;
+    return ISO_OK;
+}
+
+// Device buffer for typed samples before their conversion to float.
+iso_status ensure_typed(iso_ctx* ctx, size_t bytes, cudaStream_t s)
+{
+    if (bytes <= ctx->d_typed_bytes) return ISO_OK;
+    ISO_CUDA(ctx, cudaStreamSynchronize(s));
+    cudaFree(ctx->d_typed);
+    ctx->d_typed = nullptr;
+    ctx->d_typed_bytes = 0;
+    ISO_CUDA(ctx, cudaMalloc(&ctx->d_typed, bytes));
+    ctx->d_typed_bytes = bytes;
     return ISO_OK;
 }
 
@@ -532,8 +547,8 @@ bool stream_eligible(const iso_ctx* ctx, iso_algorithm algo, const Grid& g)
     return algo != ISO_MC_DUPFREE && !empty_grid(g) && g.nz >= 2 * kStreamPlanes && iso::gen_plan(g, ctx->nsm).fits;
 }
 
-iso_status extract_host_streamed(iso_ctx* ctx, iso_algorithm algo, const float* volume, const iso_grid* grid,
-                                 const Grid& gfull, float isoval, iso_mesh* out, cudaStream_t s)
+iso_status extract_host_streamed(iso_ctx* ctx, iso_algorithm algo, const void* volume, int dtype,
+                                 const iso_grid* grid, const Grid& gfull, float isoval, iso_mesh* out, cudaStream_t s)
 {
     if (!ctx->s_h2d) ISO_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->s_h2d, cudaStreamNonBlocking));
     if (!ctx->s_d2h) ISO_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->s_d2h, cudaStreamNonBlocking));
@@ -555,6 +570,17 @@ iso_status extract_host_streamed(iso_ctx* ctx, iso_algorithm algo, const float* 
         ctx->d_volume_bytes = kStreamWindows * wbytes;
     }
     auto window = [&](int q) { return ctx->d_volume + (size_t)(q % kStreamWindows) * wplanes * plane; };
+    // typed samples land in their own windows and are converted into the float ones
+    const size_t elem = iso::dtype_bytes(dtype);
+    const bool typed = dtype != ISO_FLOAT32;
+    if (typed) {
+        const iso_status ts = ensure_typed(ctx, kStreamWindows * (size_t)wplanes * plane * elem, s);
+        if (ts != ISO_OK) return ts;
+    }
+    auto typed_window = [&](int q) {
+        return static_cast<char*>(ctx->d_typed) + (size_t)(q % kStreamWindows) * wplanes * plane * elem;
+    };
+    const char* src = static_cast<const char*>(volume);
     // events: 1 + q the planes of slab q have landed; 1 + nslab + w window w is
     // free again; 1 + nslab + kStreamWindows + sb slab generated into
     // staging sb; 1 + nslab + kStreamWindows + 2 + sb staging sb copied out
@@ -566,7 +592,8 @@ iso_status extract_host_streamed(iso_ctx* ctx, iso_algorithm algo, const float* 
         if (q >= kStreamWindows)  // the window's previous slab is generated
             ISO_CUDA(ctx, cudaStreamWaitEvent(ctx->s_h2d, sync_event(ctx, ev_win + q % kStreamWindows), 0));
         const int lo = data_lo(q), hi = data_hi(q);
-        ISO_CUDA(ctx, cudaMemcpyAsync(window(q), volume + (size_t)lo * plane, (size_t)(hi - lo + 1) * plane * sizeof(float),
+        ISO_CUDA(ctx, cudaMemcpyAsync(typed ? static_cast<void*>(typed_window(q)) : static_cast<void*>(window(q)),
+                                      src + (size_t)lo * plane * elem, (size_t)(hi - lo + 1) * plane * elem,
                                       cudaMemcpyHostToDevice, ctx->s_h2d));
         ISO_CUDA(ctx, cudaEventRecord(sync_event(ctx, 1 + q), ctx->s_h2d));
         return ISO_OK;
@@ -587,6 +614,9 @@ iso_status extract_host_streamed(iso_ctx* ctx, iso_algorithm algo, const float* 
         if (!slab_grid(grid, algo, k0, k1, g)) return ISO_ERR_INVALID_ARG;
         pl = make_plans(ctx, g);
         ISO_CUDA(ctx, cudaStreamWaitEvent(s, sync_event(ctx, 1 + q), 0));
+        if (typed)
+            iso::launch_to_float(typed_window(q), dtype, window(q),
+                                 (long long)(data_hi(q) - data_lo(q) + 1) * (long long)plane, ctx->nsm, s);
         st = ensure_scratch(ctx, g, pl.cp, b, s);
         if (st != ISO_OK) break;
         const float* win = window(q);  // holds planes g.kd = data_lo(q) ..
@@ -799,6 +829,7 @@ iso_status iso_ctx_destroy(iso_ctx* ctx)
     cudaFree(ctx->d_tris);
     if (ctx->h_totals) cudaFreeHost(ctx->h_totals);
     if (ctx->h_slab) cudaFreeHost(ctx->h_slab);
+    cudaFree(ctx->d_typed);
     for (int q = 0; q < 2; ++q) {
         cudaFree(ctx->st_points[q]);
         cudaFree(ctx->st_normals[q]);
@@ -926,11 +957,11 @@ iso_status iso_extract_device(iso_ctx* ctx, iso_algorithm algo, const float* vol
     return finish_counts(ctx, out, res[0], res[1], res[3], &out->n_points, &out->n_tris);
 }
 
-iso_status iso_extract_host(iso_ctx* ctx, iso_algorithm algo, const float* volume, const iso_grid* grid,
-                            float isoval, iso_mesh* out, void* stream)
+static iso_status extract_host_impl(iso_ctx* ctx, iso_algorithm algo, const void* volume, int dtype,
+                                    const iso_grid* grid, float isoval, iso_mesh* out, void* stream)
 {
     if (!ctx || !grid) return ISO_ERR_INVALID_ARG;
-    if (!valid_algo(algo)) return ISO_ERR_INVALID_ARG;
+    if (!valid_algo(algo) || iso::dtype_bytes(dtype) == 0) return ISO_ERR_INVALID_ARG;
     iso_status st = check_mesh(out);
     if (st != ISO_OK) return st;
     Grid g;
@@ -940,7 +971,8 @@ iso_status iso_extract_host(iso_ctx* ctx, iso_algorithm algo, const float* volum
     if (!volume) return ISO_ERR_INVALID_ARG;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     ISO_CUDA(ctx, cudaSetDevice(ctx->device));
-    if (ctx->stream_host && stream_eligible(ctx, algo, g)) return extract_host_streamed(ctx, algo, volume, grid, g, isoval, out, s);
+    if (ctx->stream_host && stream_eligible(ctx, algo, g))
+        return extract_host_streamed(ctx, algo, volume, dtype, grid, g, isoval, out, s);
     const size_t vbytes = (size_t)g.nx * g.ny * g.nz * sizeof(float);
     if (vbytes > ctx->d_volume_bytes) {
         ISO_CUDA(ctx, cudaStreamSynchronize(s));
@@ -950,7 +982,16 @@ iso_status iso_extract_host(iso_ctx* ctx, iso_algorithm algo, const float* volum
         ISO_CUDA(ctx, cudaMalloc(&ctx->d_volume, vbytes));
         ctx->d_volume_bytes = vbytes;
     }
-    ISO_CUDA(ctx, cudaMemcpyAsync(ctx->d_volume, volume, vbytes, cudaMemcpyHostToDevice, s));
+    if (dtype == ISO_FLOAT32) {
+        ISO_CUDA(ctx, cudaMemcpyAsync(ctx->d_volume, volume, vbytes, cudaMemcpyHostToDevice, s));
+    } else {  // narrow samples over the link, float on the device
+        const long long n = (long long)g.nx * g.ny * g.nz;
+        iso_status ts = ensure_typed(ctx, (size_t)n * iso::dtype_bytes(dtype), s);
+        if (ts != ISO_OK) return ts;
+        ISO_CUDA(ctx, cudaMemcpyAsync(ctx->d_typed, volume, (size_t)n * iso::dtype_bytes(dtype), cudaMemcpyHostToDevice,
+                                      s));
+        iso::launch_to_float(ctx->d_typed, dtype, ctx->d_volume, n, ctx->nsm, s);
+    }
     const Plans pl = make_plans(ctx, g);
     if (algo == ISO_MC_DUPFREE && !pl.gp.fits) {
         ctx->last_error = "the duplicate-free order needs rows of at most 1024 points";
@@ -1007,6 +1048,43 @@ iso_status iso_extract_host(iso_ctx* ctx, iso_algorithm algo, const float* volum
     ISO_CUDA(ctx, cudaMemcpyAsync(ctx->h_totals, b.totals, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
     ISO_CUDA(ctx, cudaStreamSynchronize(s));
     return finish_counts(ctx, out, V, T, (long long)ctx->h_totals[3], &out->n_points, &out->n_tris);
+}
+
+iso_status iso_extract_host(iso_ctx* ctx, iso_algorithm algo, const float* volume, const iso_grid* grid,
+                            float isoval, iso_mesh* out, void* stream)
+{
+    return extract_host_impl(ctx, algo, volume, ISO_FLOAT32, grid, isoval, out, stream);
+}
+
+iso_status iso_extract_host_typed(iso_ctx* ctx, iso_algorithm algo, const void* volume, iso_dtype dtype,
+                                  const iso_grid* grid, float isoval, iso_mesh* out, void* stream)
+{
+    return extract_host_impl(ctx, algo, volume, dtype, grid, isoval, out, stream);
+}
+
+iso_status iso_extract_device_typed(iso_ctx* ctx, iso_algorithm algo, const void* volume, iso_dtype dtype,
+                                    const iso_grid* grid, float isoval, iso_mesh* out, void* stream)
+{
+    if (!ctx || !grid || iso::dtype_bytes(dtype) == 0) return ISO_ERR_INVALID_ARG;
+    if (dtype == ISO_FLOAT32) return iso_extract_device(ctx, algo, static_cast<const float*>(volume), grid, isoval,
+                                                        out, stream);
+    Grid g;
+    if (!make_grid(grid, g)) return ISO_ERR_INVALID_ARG;
+    if (empty_grid(g) || !volume) return iso_extract_device(ctx, algo, nullptr, grid, isoval, out, stream);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    ISO_CUDA(ctx, cudaSetDevice(ctx->device));
+    const long long n = (long long)g.nx * g.ny * g.nz;
+    if ((size_t)n * 4 > ctx->d_volume_bytes) {
+        ISO_CUDA(ctx, cudaStreamSynchronize(s));
+        cudaFree(ctx->d_volume);
+        ctx->d_volume = nullptr;
+        ctx->d_volume_bytes = 0;
+        ISO_CUDA(ctx, cudaMalloc(&ctx->d_volume, (size_t)n * 4));
+        ctx->d_volume_bytes = (size_t)n * 4;
+    }
+    iso::launch_to_float(volume, dtype, ctx->d_volume, n, ctx->nsm, s);
+    ISO_CUDA(ctx, cudaGetLastError());
+    return iso_extract_device(ctx, algo, ctx->d_volume, grid, isoval, out, stream);
 }
 
 // ---------------------------------------------------------------------------

@@ -47,6 +47,11 @@ struct GenPlan {
 
 int lanes_per_row(int W);
 
+// typed volumes (convert.cu): bytes per sample of an iso_dtype (0: unknown);
+// n samples converted to float
+size_t dtype_bytes(int dtype);
+void launch_to_float(const void* in, int dtype, float* out, long long n, int nsm, cudaStream_t s);
+
 // Opt a kernel into `dyn` bytes of dynamic shared memory (needed once the
 // dynamic plus static shared memory passes the 48 KB default).
 template <typename K>

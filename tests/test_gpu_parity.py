@@ -195,6 +195,37 @@ def test_mc_dupfree_matches_oracle(M):
         assert M.count_device(flat, dims, iso, M.MC_DUPFREE) == (len(want[0]), len(want[2]))
 
 
+@pytest.mark.parametrize("dtype", ["int8", "uint8", "int16", "uint16", "int32", "float64"])
+def test_typed_volumes(M, dtype):
+    """Volumes of the reference's other sample types: converted to float32 on
+    the device (host and device entry points, streamed and not), the same mesh
+    as the oracle on volume.astype(float32)."""
+    import torch
+
+    rng = np.random.default_rng(len(dtype))
+    info = np.iinfo(dtype) if dtype not in ("float64",) else None
+    for dims in ((45, 33, 28), (40, 30, 200)):
+        noise = M.generate_value_noise(dims, 3, 8, seed=5)
+        if info is not None:
+            lo, hi = int(info.min), int(info.max)
+            scaled = np.round((noise.astype(np.float64) + 1.5) / 3.0 * (hi - lo) + lo)
+            vol = np.clip(scaled.astype(np.int64), lo, hi).astype(dtype)
+            iso = float(np.float32((lo + hi) / 2 + 0.5))
+        else:
+            vol = (noise.astype(np.float64) * 1.000000123)
+            iso = 0.01
+        ref_vol = vol.astype(np.float32)
+        for algo, ref in ((M.FLYING_EDGES, oracle_lib.fe), (M.MARCHING_CUBES, oracle_lib.mc)):
+            want = ref(ref_vol, iso)
+            m = M.extract_typed(vol, iso, algo)
+            assert_same_mesh((m.points, m.normals, m.triangles), want, "host %s %s" % (dtype, dims))
+            dev = torch.from_numpy(np.ascontiguousarray(vol).reshape(-1)).cuda()
+            mesh = M.extract_device(dev, dims, iso, algo)
+            got = (mesh.points[:mesh.n_points].cpu().numpy(), mesh.normals[:mesh.n_points].cpu().numpy(),
+                   mesh.tris[:mesh.n_tris].cpu().numpy().astype(np.uint64))
+            assert_same_mesh(got, want, "device %s %s" % (dtype, dims))
+
+
 def test_fe_pass_by_pass_state(M):
     """gridEdges (xl, xr, xstart, ystart, zstart) and triCounter after pass 2
     and pass 3 equal the reference algorithm's state."""
