@@ -35,7 +35,9 @@ struct iso_ctx {
     long long d_cap_points = 0, d_cap_tris = 0;
     int d_index_bytes = 0;
     unsigned long long* h_totals = nullptr;  // pinned, 4 entries
-    unsigned long long* h_slab = nullptr;    // pinned, 9 entries (slab counts)
+    unsigned long long* h_slab = nullptr;    // pinned, 2 x 9 entries (slab counts)
+    void* scratch_b = nullptr;               // second scratch set (streamed path: the next slab's counts)
+    size_t scratch_b_bytes = 0;
     void* d_typed = nullptr;                 // typed volume samples before conversion
     size_t d_typed_bytes = 0;
     // streamed host entry point: copy streams, events, two device staging meshes
@@ -197,6 +199,27 @@ iso_status ensure_typed(iso_ctx* ctx, size_t bytes, cudaStream_t s)
     ctx->d_typed_bytes = 0;
     ISO_CUDA(ctx, cudaMalloc(&ctx->d_typed, bytes));
     ctx->d_typed_bytes = bytes;
+    return ISO_OK;
+}
+
+// The second scratch set (the streamed path counts slab q+1 while slab q
+// is generated from the first).
+iso_status ensure_scratch_b(iso_ctx* ctx, const Grid& g, const iso::CountPlan& cp, FeBuffers& b, cudaStream_t s)
+{
+    const size_t need = scratch_size(g, cp);
+    if (need > ctx->scratch_b_bytes) {
+        if (ctx->scratch_b) {
+            ISO_CUDA(ctx, cudaStreamSynchronize(s));
+            cudaFree(ctx->scratch_b);
+            ctx->scratch_b = nullptr;
+            ctx->scratch_b_bytes = 0;
+        }
+        const size_t alloc = need + need / 4;
+        ISO_CUDA(ctx, cudaMalloc(&ctx->scratch_b, alloc));
+        ctx->scratch_b_bytes = alloc;
+    }
+    carve(ctx->scratch_b, g, cp, b);
+    b.fe2mc = ctx->fe2mc;
     return ISO_OK;
 }
 
@@ -394,15 +417,15 @@ struct SlabCounts {
     unsigned long long lo[3], hi[3], tot[3];
 };
 
-iso_status slab_count(iso_ctx* ctx, iso_algorithm algo, const float* vol, const Grid& g, int64_t k0, int64_t k1,
-                      float iso, const Plans& pl, FeBuffers& b, cudaStream_t s, SlabCounts& c)
+// Enqueues the count of the window and the copies of its totals and row
+// starts into h[0..8] (pinned).
+iso_status slab_count_enqueue(iso_ctx* ctx, iso_algorithm algo, const float* vol, const Grid& g, int64_t k0,
+                              int64_t k1, float iso, const Plans& pl, FeBuffers& b, cudaStream_t s,
+                              unsigned long long* h)
 {
-    if (!ctx->h_slab) ISO_CUDA(ctx, cudaMallocHost(&ctx->h_slab, 9 * sizeof(unsigned long long)));
     PassMarks pm(ctx, s);
     enqueue_count(ctx, algo, vol, g, iso, pl, b, s, pm);
     ISO_CUDA(ctx, cudaGetLastError());
-    ISO_CUDA(ctx, cudaMemsetAsync(b.totals + 3, 0, sizeof(unsigned long long), s));
-    unsigned long long* h = ctx->h_slab;
     ISO_CUDA(ctx, cudaMemcpyAsync(h, b.totals, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
     for (int a = 0; a < 3; ++a) {
         const long long rlo = (long long)(k0 - g.kr) * g.ny, rhi = (long long)(k1 - g.kr) * g.ny;
@@ -415,12 +438,27 @@ iso_status slab_count(iso_ctx* ctx, iso_algorithm algo, const float* vol, const 
                                           cudaMemcpyDeviceToHost, s));
         }
     }
-    ISO_CUDA(ctx, cudaStreamSynchronize(s));
+    return ISO_OK;
+}
+
+// The counts copied by slab_count_enqueue, once they have landed.
+void slab_count_read(const Grid& g, int64_t k0, int64_t k1, const unsigned long long* h, SlabCounts& c)
+{
     for (int a = 0; a < 3; ++a) {
         c.tot[a] = h[a];
         c.lo[a] = k0 - g.kr > 0 ? h[3 + a] : 0;
         c.hi[a] = k1 < g.nz ? h[6 + a] : h[a];
     }
+}
+
+iso_status slab_count(iso_ctx* ctx, iso_algorithm algo, const float* vol, const Grid& g, int64_t k0, int64_t k1,
+                      float iso, const Plans& pl, FeBuffers& b, cudaStream_t s, SlabCounts& c)
+{
+    if (!ctx->h_slab) ISO_CUDA(ctx, cudaMallocHost(&ctx->h_slab, 18 * sizeof(unsigned long long)));
+    const iso_status st = slab_count_enqueue(ctx, algo, vol, g, k0, k1, iso, pl, b, s, ctx->h_slab);
+    if (st != ISO_OK) return st;
+    ISO_CUDA(ctx, cudaStreamSynchronize(s));
+    slab_count_read(g, k0, k1, ctx->h_slab, c);
     return ISO_OK;
 }
 
@@ -606,23 +644,52 @@ iso_status extract_host_streamed(iso_ctx* ctx, iso_algorithm algo, const void* v
     long long V = 0, T = 0;
     bool room = true;  // the caller's buffers hold everything so far
     iso_status st = ISO_OK;
-    for (int q = 0; q < nslab && st == ISO_OK; ++q) {
-        const int k0 = slab_k0(q), k1 = slab_k0(q + 1);
+    // Slab q+1 is counted (into the other scratch set) before slab q is
+    // generated, so the host reads counts that have already landed and the
+    // kernels run back to back.
+    if (!ctx->h_slab) ISO_CUDA(ctx, cudaMallocHost(&ctx->h_slab, 18 * sizeof(unsigned long long)));
+    struct SlabRun {
         Grid g;
         Plans pl;
         FeBuffers b;
-        if (!slab_grid(grid, algo, k0, k1, g)) return ISO_ERR_INVALID_ARG;
-        pl = make_plans(ctx, g);
+        int k0, k1;
+    } run[2];
+    const size_t ev_cnt = ev_out + 2;  // 2 events: counts of slab q landed in h_slab + 9 * (q & 1)
+    auto start_count = [&](int q) -> iso_status {
+        SlabRun& r = run[q & 1];
+        r.k0 = slab_k0(q);
+        r.k1 = slab_k0(q + 1);
+        if (!slab_grid(grid, algo, r.k0, r.k1, r.g)) return ISO_ERR_INVALID_ARG;
+        r.pl = make_plans(ctx, r.g);
         ISO_CUDA(ctx, cudaStreamWaitEvent(s, sync_event(ctx, 1 + q), 0));
         if (typed)
             iso::launch_to_float(typed_window(q), dtype, window(q),
                                  (long long)(data_hi(q) - data_lo(q) + 1) * (long long)plane, ctx->nsm, s);
-        st = ensure_scratch(ctx, g, pl.cp, b, s);
-        if (st != ISO_OK) break;
+        iso_status e =
+            (q & 1) ? ensure_scratch_b(ctx, r.g, r.pl.cp, r.b, s) : ensure_scratch(ctx, r.g, r.pl.cp, r.b, s);
+        if (e != ISO_OK) return e;
+        e = slab_count_enqueue(ctx, algo, window(q), r.g, r.k0, r.k1, isoval, r.pl, r.b, s,
+                               ctx->h_slab + 9 * (q & 1));
+        if (e != ISO_OK) return e;
+        ISO_CUDA(ctx, cudaEventRecord(sync_event(ctx, ev_cnt + (q & 1)), s));
+        return ISO_OK;
+    };
+    if (!sync_event(ctx, ev_cnt + 1)) return ISO_ERR_CUDA;
+    st = start_count(0);
+    for (int q = 0; q < nslab && st == ISO_OK; ++q) {
+        if (q + 1 < nslab) {
+            st = start_count(q + 1);
+            if (st != ISO_OK) break;
+        }
+        SlabRun& r = run[q & 1];
+        const int k0 = r.k0, k1 = r.k1;
+        const Grid& g = r.g;
+        const Plans& pl = r.pl;
+        FeBuffers& b = r.b;
         const float* win = window(q);  // holds planes g.kd = data_lo(q) ..
+        ISO_CUDA(ctx, cudaEventSynchronize(sync_event(ctx, ev_cnt + (q & 1))));
         SlabCounts c;
-        st = slab_count(ctx, algo, win, g, k0, k1, isoval, pl, b, s, c);  // waits for the counts
-        if (st != ISO_OK) break;
+        slab_count_read(g, k0, k1, ctx->h_slab + 9 * (q & 1), c);
         const long long Vq = (long long)(c.hi[mc ? 2 : 0] - c.lo[mc ? 2 : 0]), Tq = (long long)(c.hi[1] - c.lo[1]);
         const long long top = V + (mc ? Vq : (long long)c.tot[0]);  // largest id the slab references
         if (out->index_bytes == 4 && top > 0xffffffffll) {
@@ -830,6 +897,7 @@ iso_status iso_ctx_destroy(iso_ctx* ctx)
     if (ctx->h_totals) cudaFreeHost(ctx->h_totals);
     if (ctx->h_slab) cudaFreeHost(ctx->h_slab);
     cudaFree(ctx->d_typed);
+    cudaFree(ctx->scratch_b);
     for (int q = 0; q < 2; ++q) {
         cudaFree(ctx->st_points[q]);
         cudaFree(ctx->st_normals[q]);
