@@ -2,14 +2,15 @@
 // on sm_103a, with pass 1 (x-edge classification, trims) fused into pass 2
 // (cube cases, per-row counts):
 //
-//   k_count_pairs  (rows up to 512 points) a CTA owns a block of 16 grid rows
-//   k_count_warps  (up to 2048) / 8 rows (k_count_warps: a warp per row;
-//                  k_count_pairs: a half-warp per row) and a run of KC planes
-//                  and marches along z.  Each row's words of plane k+1 are
-//                  classified straight from the volume (float4 loads of plane
-//                  k+2 already in flight) into bit-per-point words held one
-//                  per lane -- the reference's edgeCases bytes are never
-//                  materialised -- and counted for grid row (j,k): its cut
+//   k_count_tma    (rows up to 512 points, 16-byte aligned) a CTA owns a block
+//   k_count_warps  (up to 2048) of 16 grid rows (k_count_tma: a half-warp per
+//                  row) / 8 rows (k_count_warps: a warp per row) and a run of
+//                  KC planes and marches along z.  Each row's words of plane
+//                  k+1 are classified straight from the volume (plane k+2
+//                  already in flight: a TMA bulk copy into the warp's shared
+//                  buffer, or float4 loads into registers) into bit-per-point
+//                  words held one per lane -- the reference's edgeCases bytes
+//                  are never materialised -- and counted for grid row (j,k): its cut
 //                  x, y and z edges (the vertices it owns), the trims xl/xr,
 //                  the triangles of cell row (j,k) and, for Marching Cubes,
 //                  the vertices cell row (j,k) owns, all 32 cells of a word at
@@ -228,18 +229,8 @@ __global__ void __launch_bounds__(kThreads) k_count_warps(const float* __restric
 
 // Rows of up to 16 words (nx <= 512): two rows per warp, one per half-warp
 // (lanes 16h .. 16h+15 hold words 0..15 of row j0 + 2*warp + h), so no lane
-// idles on words past the row.  The same counts as k_count_warps.
+// idles on words past the row.
 constexpr int kPairRows = 2 * kCountRows;  // grid rows per CTA
-
-template <int U>
-__device__ __forceinline__ void load_half_vec4(const float* __restrict__ row, int nq, int l16, bool ok, RowVals<U>& r)
-{
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-        const int q = l16 + 16 * u;
-        r.v[u] = (ok && q < nq) ? __ldg(reinterpret_cast<const float4*>(row) + q) : make_float4(0.f, 0.f, 0.f, 0.f);
-    }
-}
 
 // Bit words of the half-warp's row: word w in lane 16h + w.
 template <int U>
@@ -265,48 +256,89 @@ __device__ __forceinline__ uint32_t words_half(const RowVals<U>& r, int nq, int 
     return out;
 }
 
-template <bool MC, int U>
-__global__ void __launch_bounds__(kThreads, 2) k_count_pairs(const float* __restrict__ vol, Grid g, float iso, int KC,
-                                                          int nyb, const CaseTables* __restrict__ cases,
-                                                          uint4* __restrict__ rowcnt, uint2* __restrict__ trims,
-                                                          uint32_t* __restrict__ mccnt, uint32_t* __restrict__ bits_out)
+// Rows of up to 16 words (nx <= 512), 16-byte aligned, two per warp: the
+// counts of k_count_warps, with the volume brought in by the TMA bulk engine.  A warp's
+// two grid rows jw, jw+1 read rows jw .. jw+2 of every plane (A and B of both
+// half-warps), which lie next to each other in memory: one cp.async.bulk per
+// plane fills the warp's buffer of kTmaRows rows and completes on the warp's
+// mbarrier.  The words of plane k+1 are taken from the buffer before the copy
+// of plane k+2 is issued into it, so the copy runs while step k is counted;
+// no register holds raw values across a step.
+constexpr int kTmaRows = 3;
+
+template <int U>
+__device__ __forceinline__ uint32_t words_from_buffer(const float* row, int nq, int lane, bool ok, float iso)
 {
-    (void)cases;  // the counts need no case table (tris_of_word, mc_verts_of_word)
+    const int l16 = lane & 15;
+    RowVals<U> r;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const int q = l16 + 16 * u;
+        r.v[u] = (ok && q < nq) ? reinterpret_cast<const float4*>(row)[q] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    return words_half<U>(r, nq, lane, iso);
+}
+
+template <bool MC, int U>
+__global__ void __launch_bounds__(kThreads, 4) k_count_tma(const float* __restrict__ vol, Grid g, float iso, int KC,
+                                                        int nyb, uint4* __restrict__ rowcnt,
+                                                        uint2* __restrict__ trims, uint32_t* __restrict__ mccnt,
+                                                        uint32_t* __restrict__ bits_out,
+                                                        unsigned long long* __restrict__ status)
+{
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    __shared__ uint64_t s_bar[kCountRows];
     const int jb = blockIdx.x % nyb, kc = blockIdx.x / nyb;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, h = lane >> 4, l16 = lane & 15;
     const int jw = jb * kPairRows + 2 * warp;
     if (jw >= g.ny) return;  // both halves past the grid
+    float* buf = reinterpret_cast<float*>(s_raw) + (size_t)warp * kTmaRows * g.nx;
+    uint64_t* bar = &s_bar[warp];
+    if (lane == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+    }
+    __syncwarp();
     const int j = jw + h;
     const bool row_ok = j < g.ny;
-    const int jr = row_ok ? j : jw;  // a valid row address for a half without a row
     const int kb = g.kr + kc * KC, ke = min(kb + KC, g.ke);
     const bool hasY = row_ok && j < g.ny - 1;
-    const int jy = hasY ? j + 1 : jr;
     const int nq = g.nx >> 2;
-    auto rowptr = [&](int k, int jj) { return vol + ((long long)(k - g.kd) * g.ny + jj) * g.nx; };
+    const unsigned bytes = (unsigned)(min(kTmaRows, g.ny - jw) * g.nx * 4);
 
-    uint32_t A, B, Cw, Dw;
-    RowVals<U> pc, pd;
-    {
-        RowVals<U> ra, rbv;
-        load_half_vec4<U>(rowptr(kb, jr), nq, l16, row_ok, ra);
-        load_half_vec4<U>(rowptr(kb, jy), nq, l16, hasY, rbv);
-        if (kb + 1 < g.nz) {
-            load_half_vec4<U>(rowptr(kb + 1, jr), nq, l16, row_ok, pc);
-            load_half_vec4<U>(rowptr(kb + 1, jy), nq, l16, hasY, pd);
+    // plane p -> buffer (lane 0); earlier reads of the buffer are ordered
+    // before the engine's writes by the caller's __syncwarp and the fence
+    auto issue = [&](int p) {
+        if (lane == 0) {
+            fence_proxy_async();
+            mbar_arrive_expect_tx(bar, bytes);
+            bulk_copy_g2s(buf, vol + ((long long)(p - g.kd) * g.ny + jw) * g.nx, bytes, bar);
         }
-        A = words_half<U>(ra, nq, lane, iso);
-        B = words_half<U>(rbv, nq, lane, iso);
-    }
-    for (int k = kb; k < ke; ++k) {
+    };
+    unsigned phase = 0;
+    // words of rows A = buffer row h and B = buffer row h+1 of the plane in the buffer
+    auto take = [&](uint32_t& wa, uint32_t& wb) -> bool {
+        const bool done = mbar_wait(bar, phase);
+        if (!__all_sync(0xffffffffu, done)) return false;
+        phase ^= 1u;
+        wa = words_from_buffer<U>(buf + h * g.nx, nq, lane, row_ok, iso);
+        wb = words_from_buffer<U>(buf + (h + 1) * g.nx, nq, lane, hasY, iso);
+        __syncwarp();  // every lane has read the buffer before it is refilled
+        return true;
+    };
+
+    uint32_t A = 0, B = 0, Cw = 0, Dw = 0;
+    bool ok = true;
+    issue(kb);
+    ok = take(A, B);
+    if (ok && kb + 1 < g.nz) issue(kb + 1);
+    for (int k = kb; ok && k < ke; ++k) {
         const bool hasZ = k + 1 < g.nz;
-        Cw = words_half<U>(pc, nq, lane, iso);
-        Dw = words_half<U>(pd, nq, lane, iso);
-        if (k + 2 < g.nz && k + 1 < ke) {
-            load_half_vec4<U>(rowptr(k + 2, jr), nq, l16, row_ok, pc);
-            load_half_vec4<U>(rowptr(k + 2, jy), nq, l16, hasY, pd);
+        Cw = Dw = 0u;
+        if (hasZ) {  // plane k+1 was issued one step earlier
+            if (!(ok = take(Cw, Dw))) break;
+            if (k + 2 < g.nz && k + 1 < ke) issue(k + 2);
         }
-        if (!hasZ) Cw = Dw = 0u;
         RowCounts rc;
         RowWords rw;
         rw.a = A;
@@ -343,6 +375,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_count_pairs(const float* __rest
         }
         A = Cw;
         B = Dw;
+    }
+    if (!ok) {  // a copy did not complete in time: report it, and let the copy land before the CTA ends
+        if (lane == 0) atomicOr(status, kStatusTimeout);
+        mbar_wait(bar, phase);
     }
 }
 
@@ -597,18 +633,23 @@ static void count_launch(const CountPlan& p, const float* vol, const Grid& g, fl
 {
     const unsigned blocks = (unsigned)(p.nyb * p.nkc);
     const bool vec4 = g.W <= 64 && (g.nx % 4 == 0) && ((reinterpret_cast<uintptr_t>(vol) & 15) == 0);
-    if (vec4 && g.W <= 16) {  // two rows per warp
+    if (vec4 && g.W <= 16) {  // two rows per warp, planes through the TMA engine
         const int nyb2 = (g.ny + kPairRows - 1) / kPairRows;
         const unsigned blocks2 = (unsigned)(nyb2 * p.nkc);
         const int nq = g.nx >> 2;
-#define ISO_PAIRS(UU)                                                                                          \
-    k_count_pairs<MC, UU><<<blocks2, kThreads, 0, s>>>(vol, g, iso, p.KC, nyb2, cases, b.rowcnt, b.trims, b.mccnt, \
-                                                       b.bits)
-        if (nq <= 16) ISO_PAIRS(1);
-        else if (nq <= 32) ISO_PAIRS(2);
-        else if (nq <= 64) ISO_PAIRS(4);
-        else ISO_PAIRS(8);
-#undef ISO_PAIRS
+        const size_t smem = (size_t)kCountRows * kTmaRows * g.nx * sizeof(float);
+#define ISO_TMA(UU)                                                                                            \
+    {                                                                                                          \
+        auto kern = k_count_tma<MC, UU>;                                                                      \
+        allow_smem(kern, smem);                                                                                \
+        kern<<<blocks2, kThreads, smem, s>>>(vol, g, iso, p.KC, nyb2, b.rowcnt, b.trims, b.mccnt, b.bits,       \
+                                             b.totals + 3);                                                    \
+    }
+        if (nq <= 16) ISO_TMA(1)
+        else if (nq <= 32) ISO_TMA(2)
+        else if (nq <= 64) ISO_TMA(4)
+        else ISO_TMA(8)
+#undef ISO_TMA
         return;
     }
 #define ISO_COUNT(VEC, UU, NWW)                                                                                \
