@@ -6,7 +6,9 @@ One step = one full extraction (passes 1-4) of the volume.
             iso_extract_device_async, K steps between two CUDA events)
   e2e       Mcells/s through the host entry point (iso_extract_host): pinned
             host volume copied in, mesh copied back to pinned host buffers,
-            every step
+            every step; e2e.link gives this machine's host link rates (copy
+            engines, pinned memory, measured after the timed regions) and the
+            shortest time the step's copies could take on them
   roofline  the dominant kernel (largest summed time), timed with CUDA events
             recorded between kernels on the extraction stream during the
             timed region; algorithmic bytes per launch:
@@ -159,6 +161,51 @@ def _ref_program_seconds(prog, vol, cores, steps, warmup):
             if i >= warmup:
                 times.append(float(m.group(1)))
         return sum(times)
+
+
+def link_rates(dev, nbytes=256 << 20, reps=3):
+    """Host link rates of this machine with pinned memory and the copy engines,
+    in bytes/s: host -> device alone, device -> host alone, both at once."""
+    import torch
+
+    h_in = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    h_out = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    d_a = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    d_b = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    s_in, s_out = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+
+    def h2d():
+        with torch.cuda.stream(s_in):
+            d_a.copy_(h_in, non_blocking=True)
+
+    def d2h():
+        with torch.cuda.stream(s_out):
+            h_out.copy_(d_b, non_blocking=True)
+
+    def both():
+        h2d()
+        d2h()
+
+    def seconds(fn):
+        fn()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize(dev)
+        return (time.perf_counter() - t0) / reps
+
+    t_in, t_out, t_both = seconds(h2d), seconds(d2h), seconds(both)
+    return nbytes / t_in, nbytes / t_out, 2 * nbytes / t_both
+
+
+def link_floor(rates, h2d_bytes, d2h_bytes, ms_per_step):
+    """The shortest time a step's copies can take on this link, and the share
+    of the measured step it is."""
+    r_in, r_out, r_both = rates
+    floor_s = max(h2d_bytes / r_in, d2h_bytes / r_out, (h2d_bytes + d2h_bytes) / r_both)
+    return {"h2d_GBps": r_in / 1e9, "d2h_GBps": r_out / 1e9, "both_GBps": r_both / 1e9,
+            "floor_ms_per_step": 1e3 * floor_s, "frac_of_floor": 1e3 * floor_s / ms_per_step}
 
 
 def run_reference(args, rank):
@@ -327,6 +374,7 @@ def main():
     torch.cuda.synchronize()
     e2e16_s = time.perf_counter() - t0
     clk = clocks.stop()
+    rates = link_rates(dev)
 
     # max over ranks
     times = torch.tensor([ms, e2e_s], dtype=torch.float64, device=dev)
@@ -367,11 +415,13 @@ def main():
                          "frac": B_total / (ms / args.steps / 1e3) / 1e9 / peak,
                          "per_pass": per, "event_overhead_ms_per_step": (ms - prof_ms) / args.steps},
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": 4 * N,
-                    "d2h_bytes_per_step": 24 * V + 12 * T, "ms_per_step": 1e3 * e2e_s / args.e2e_steps},
+                    "d2h_bytes_per_step": 24 * V + 12 * T, "ms_per_step": 1e3 * e2e_s / args.e2e_steps,
+                    "link": link_floor(rates, 4 * N, 24 * V + 12 * T, 1e3 * e2e_s / args.e2e_steps)},
             "e2e_typed": {"dtype": "int16", "field": "the same noise x 8192, rounded", "value":
                           C_cells * args.e2e_steps * world / e2e16_s / 1e6, "unit": METRIC,
                           "h2d_bytes_per_step": 2 * N, "d2h_bytes_per_step": 24 * V16 + 12 * T16,
-                          "ms_per_step": 1e3 * e2e16_s / args.e2e_steps},
+                          "ms_per_step": 1e3 * e2e16_s / args.e2e_steps,
+                          "link": link_floor(rates, 2 * N, 24 * V16 + 12 * T16, 1e3 * e2e16_s / args.e2e_steps)},
             # count + scan + row starts + generate per step (scan/row starts share one mark)
             "gpu_launches": int(sum(n_pass[p] for p in range(6)) + n_pass[2]),
             "clocks": clk,

@@ -232,28 +232,37 @@ __global__ void __launch_bounds__(kThreads) k_count_warps(const float* __restric
 // idles on words past the row.
 constexpr int kPairRows = 2 * kCountRows;  // grid rows per CTA
 
-// Bit words of the half-warp's row: word w in lane 16h + w.
-template <int U>
-__device__ __forceinline__ uint32_t words_half(const RowVals<U>& r, int nq, int lane, float iso)
+// All ones when v >= iso, else zero (false for NaN; -0 >= +0), one ALU op.
+__device__ __forceinline__ uint32_t ge_mask(float v, float iso)
 {
-    const int l16 = lane & 15;
-    uint32_t out = 0u;
+    uint32_t d;
+    asm("set.ge.u32.f32 %0, %1, %2;" : "=r"(d) : "f"(v), "f"(iso));
+    return d;
+}
+
+// Word l16 (points 32*l16 .. 32*l16+31) of a row of nq float4 in shared
+// memory, built by one lane alone: at step u it reads float4 (u + l16) & 7 of
+// its word into bits 4u .. 4u+3 (eight consecutive lanes read eight different
+// bank groups), and the word is rotated into place at the end.  FULL: the
+// row has all 16 words (nx = 512).
+template <bool FULL>
+__device__ __forceinline__ uint32_t row_word(const float* row, int nq, int l16, float iso)
+{
+    const float4* r4 = reinterpret_cast<const float4*>(row) + 8 * l16;
+    const int nv = FULL ? 8 : nq - 8 * l16;  // float4 of the word inside the row
+    uint32_t w = 0u;
 #pragma unroll
-    for (int u = 0; u < U; ++u) {
-        const int f = l16 + 16 * u;
-        const float4 v = r.v[u];
-        const uint32_t nib = f < nq ? ((uint32_t)(v.x >= iso) | ((uint32_t)(v.y >= iso) << 1) |
-                                       ((uint32_t)(v.z >= iso) << 2) | ((uint32_t)(v.w >= iso) << 3))
-                                    : 0u;
-        uint32_t word = nib << (4 * (lane & 7));
-        word |= __shfl_xor_sync(0xffffffffu, word, 1);
-        word |= __shfl_xor_sync(0xffffffffu, word, 2);
-        word |= __shfl_xor_sync(0xffffffffu, word, 4);
-        // lanes 16h + 8g .. +7 hold word 2u + g of row h; lane 16h + w wants word w
-        const uint32_t x = __shfl_sync(0xffffffffu, word, (lane & 16) | ((lane & 1) << 3));
-        if (u == (l16 >> 1)) out = x;
+    for (int u = 0; u < 8; ++u) {
+        const int q = (u + l16) & 7;
+        if (FULL || q < nv) {
+            const float4 v = r4[q];
+            w |= ge_mask(v.x, iso) & (1u << (4 * u));
+            w |= ge_mask(v.y, iso) & (2u << (4 * u));
+            w |= ge_mask(v.z, iso) & (4u << (4 * u));
+            w |= ge_mask(v.w, iso) & (8u << (4 * u));
+        }
     }
-    return out;
+    return __funnelshift_l(w, w, 4 * (l16 & 7));
 }
 
 // Rows of up to 16 words (nx <= 512), 16-byte aligned, two per warp: the
@@ -266,20 +275,7 @@ __device__ __forceinline__ uint32_t words_half(const RowVals<U>& r, int nq, int 
 // no register holds raw values across a step.
 constexpr int kTmaRows = 3;
 
-template <int U>
-__device__ __forceinline__ uint32_t words_from_buffer(const float* row, int nq, int lane, bool ok, float iso)
-{
-    const int l16 = lane & 15;
-    RowVals<U> r;
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-        const int q = l16 + 16 * u;
-        r.v[u] = (ok && q < nq) ? reinterpret_cast<const float4*>(row)[q] : make_float4(0.f, 0.f, 0.f, 0.f);
-    }
-    return words_half<U>(r, nq, lane, iso);
-}
-
-template <bool MC, int U>
+template <bool MC, bool FULL>
 __global__ void __launch_bounds__(kThreads, 4) k_count_tma(const float* __restrict__ vol, Grid g, float iso, int KC,
                                                         int nyb, uint4* __restrict__ rowcnt,
                                                         uint2* __restrict__ trims, uint32_t* __restrict__ mccnt,
@@ -321,8 +317,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_count_tma(const float* __restri
         const bool done = mbar_wait(bar, phase);
         if (!__all_sync(0xffffffffu, done)) return false;
         phase ^= 1u;
-        wa = words_from_buffer<U>(buf + h * g.nx, nq, lane, row_ok, iso);
-        wb = words_from_buffer<U>(buf + (h + 1) * g.nx, nq, lane, hasY, iso);
+        wa = row_ok ? row_word<FULL>(buf + h * g.nx, nq, l16, iso) : 0u;
+        wb = hasY ? row_word<FULL>(buf + (h + 1) * g.nx, nq, l16, iso) : 0u;
         __syncwarp();  // every lane has read the buffer before it is refilled
         return true;
     };
@@ -638,17 +634,15 @@ static void count_launch(const CountPlan& p, const float* vol, const Grid& g, fl
         const unsigned blocks2 = (unsigned)(nyb2 * p.nkc);
         const int nq = g.nx >> 2;
         const size_t smem = (size_t)kCountRows * kTmaRows * g.nx * sizeof(float);
-#define ISO_TMA(UU)                                                                                            \
+#define ISO_TMA(FULL)                                                                                          \
     {                                                                                                          \
-        auto kern = k_count_tma<MC, UU>;                                                                      \
+        auto kern = k_count_tma<MC, FULL>;                                                                    \
         allow_smem(kern, smem);                                                                                \
         kern<<<blocks2, kThreads, smem, s>>>(vol, g, iso, p.KC, nyb2, b.rowcnt, b.trims, b.mccnt, b.bits,       \
                                              b.totals + 3);                                                    \
     }
-        if (nq <= 16) ISO_TMA(1)
-        else if (nq <= 32) ISO_TMA(2)
-        else if (nq <= 64) ISO_TMA(4)
-        else ISO_TMA(8)
+        if (nq == 128) ISO_TMA(true)
+        else ISO_TMA(false)
 #undef ISO_TMA
         return;
     }

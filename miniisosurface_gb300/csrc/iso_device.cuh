@@ -570,15 +570,6 @@ struct RowStarts {
     }
 };
 
-// Triangles of all cells of a word at once, without looking at the cases:
-// every polygon of a case spends its m cut edges on m-2 triangles, so
-// ntris = cut edges - 2 * polygons, and the polygons of a case are the
-// edge-connected components of its set corners, V - E + F (corners, cube
-// edges and faces inside the set), except when the two unset corners are
-// the ends of a body diagonal (cases 125, 190, 215, 235): the six set
-// corners form a ring that the faces miss, and the table makes two polygons
-// there.  The words are the corners 0..7 of the word's cells (cube_case).
-// Checked against numTris of all 256 cases (MarchingCubesTables.h:23).
 ISO_HD inline uint32_t popc32(uint32_t x)
 {
 #ifdef __CUDA_ARCH__
@@ -588,31 +579,41 @@ ISO_HD inline uint32_t popc32(uint32_t x)
 #endif
 }
 
+// Triangles of all cells of a word at once, without looking at the cases:
+// every polygon of a case spends its m cut edges on m-2 triangles, so
+// ntris = cut edges - 2 * polygons, and the polygons of a case are the
+// edge-connected components of its set corners, V - E + F (corners, cube
+// edges and faces inside the set), except when the two unset corners are
+// the ends of a body diagonal (cases 125, 190, 215, 235): the six set
+// corners form a ring that the faces miss, and the table makes two polygons
+// there.  A cell has 3V - 2E cut edges (every corner ends three edges; an
+// edge between two set corners is not cut), so ntris = V - 2F - 4 * rings
+// for a cell with a cut edge; an all-set cell gives 8 - 12 = -4 and is added
+// back, an empty one gives 0.  The words are the corners 0..7 of the word's
+// cells (cube_case).  Checked against numTris of all 256 cases
+// (MarchingCubesTables.h:23).
 ISO_HD inline uint32_t tris_of_word(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t c4, uint32_t c5,
                                     uint32_t c6, uint32_t c7, uint32_t cells)
 {
-    // cube edges (corner pairs) 0-1 1-2 3-2 0-3 4-5 5-6 7-6 4-7 0-4 1-5 3-7 2-6
-    const uint32_t e0a = c0 & c1, e1a = c1 & c2, e2a = c3 & c2, e3a = c0 & c3, e4a = c4 & c5, e5a = c5 & c6;
-    const uint32_t e6a = c7 & c6, e7a = c4 & c7, e8a = c0 & c4, e9a = c1 & c5, e10a = c3 & c7, e11a = c2 & c6;
-    const uint32_t cut = popc32((c0 ^ c1) & cells) + popc32((c1 ^ c2) & cells) + popc32((c3 ^ c2) & cells) +
-                         popc32((c0 ^ c3) & cells) + popc32((c4 ^ c5) & cells) + popc32((c5 ^ c6) & cells) +
-                         popc32((c7 ^ c6) & cells) + popc32((c4 ^ c7) & cells) + popc32((c0 ^ c4) & cells) +
-                         popc32((c1 ^ c5) & cells) + popc32((c3 ^ c7) & cells) + popc32((c2 ^ c6) & cells);
-    // only cells with a cut edge count (all-set cells have V - E + F = 1)
-    const uint32_t act = cells & ~((c0 & c1 & c2 & c3 & c4 & c5 & c6 & c7) | ~(c0 | c1 | c2 | c3 | c4 | c5 | c6 | c7));
-    const uint32_t verts = popc32(c0 & act) + popc32(c1 & act) + popc32(c2 & act) + popc32(c3 & act) +
-                           popc32(c4 & act) + popc32(c5 & act) + popc32(c6 & act) + popc32(c7 & act);
-    const uint32_t edges = popc32(e0a & act) + popc32(e1a & act) + popc32(e2a & act) + popc32(e3a & act) +
-                           popc32(e4a & act) + popc32(e5a & act) + popc32(e6a & act) + popc32(e7a & act) +
-                           popc32(e8a & act) + popc32(e9a & act) + popc32(e10a & act) + popc32(e11a & act);
+    c0 &= cells;
+    c1 &= cells;
+    c2 &= cells;
+    c3 &= cells;
+    c4 &= cells;
+    c5 &= cells;
+    c6 &= cells;
+    c7 &= cells;
+    const uint32_t verts = popc32(c0) + popc32(c1) + popc32(c2) + popc32(c3) + popc32(c4) + popc32(c5) +
+                           popc32(c6) + popc32(c7);
+    const uint32_t e01 = c0 & c1, e32 = c3 & c2, e45 = c4 & c5, e76 = c7 & c6;
     // faces z- z+ y- y+ x- x+: 0123 4567 0154 3267 0374 1265
-    const uint32_t faces = popc32(e0a & e2a & act) + popc32(e4a & e6a & act) + popc32(e0a & e4a & act) +
-                           popc32(e2a & e6a & act) + popc32(e3a & e7a & act) + popc32(e1a & e5a & act);
+    const uint32_t faces = popc32(e01 & e32) + popc32(e45 & e76) + popc32(e01 & e45) + popc32(e32 & e76) +
+                           popc32(c0 & c3 & c7 & c4) + popc32(c1 & c2 & c6 & c5);
+    const uint32_t all = e01 & e32 & e45 & e76;
     // body diagonals 0-6 1-7 2-4 3-5 unset, the other six set
     const uint32_t ring = (~(c0 | c6) & c1 & c2 & c3 & c4 & c5 & c7) | (~(c1 | c7) & c0 & c2 & c3 & c4 & c5 & c6) |
                           (~(c2 | c4) & c0 & c1 & c3 & c5 & c6 & c7) | (~(c3 | c5) & c0 & c1 & c2 & c4 & c6 & c7);
-    const uint32_t polys = verts - edges + faces + 2u * popc32(ring & act);
-    return cut - 2u * polys;
+    return verts - 2u * faces - 4u * popc32(ring) + 4u * popc32(all);
 }
 
 // Marching Cubes vertices owned by the cells of a word (mc_owned_edges):
