@@ -35,13 +35,14 @@ struct iso_ctx {
     long long d_cap_points = 0, d_cap_tris = 0;
     int d_index_bytes = 0;
     unsigned long long* h_totals = nullptr;  // pinned, 4 entries
-    unsigned long long* h_slab = nullptr;    // pinned, 2 x 9 entries (slab counts)
+    unsigned long long* h_slab = nullptr;    // pinned and mapped, 2 x 9 entries (slab counts)
+    unsigned long long* h_slab_dev = nullptr;  // its device address (written by k_slab_readback)
     void* scratch_b = nullptr;               // second scratch set (streamed path: the next slab's counts)
     size_t scratch_b_bytes = 0;
     void* d_typed = nullptr;                 // typed volume samples before conversion
     size_t d_typed_bytes = 0;
     // streamed host entry point: copy streams, events, two device staging meshes
-    cudaStream_t s_h2d = nullptr, s_d2h = nullptr;
+    cudaStream_t s_h2d = nullptr, s_d2h = nullptr, s_cnt = nullptr;  // copies in / out, slab counts
     std::vector<cudaEvent_t> sync_events;
     float* st_points[2] = {nullptr, nullptr};
     float* st_normals[2] = {nullptr, nullptr};
@@ -419,6 +420,15 @@ struct SlabCounts {
 
 // Enqueues the count of the window and the copies of its totals and row
 // starts into h[0..8] (pinned).
+// The slab-count read-back buffer: pinned host memory that kernels write.
+iso_status ensure_h_slab(iso_ctx* ctx)
+{
+    if (ctx->h_slab) return ISO_OK;
+    ISO_CUDA(ctx, cudaHostAlloc(&ctx->h_slab, 18 * sizeof(unsigned long long), cudaHostAllocMapped));
+    ISO_CUDA(ctx, cudaHostGetDevicePointer(reinterpret_cast<void**>(&ctx->h_slab_dev), ctx->h_slab, 0));
+    return ISO_OK;
+}
+
 iso_status slab_count_enqueue(iso_ctx* ctx, iso_algorithm algo, const float* vol, const Grid& g, int64_t k0,
                               int64_t k1, float iso, const Plans& pl, FeBuffers& b, cudaStream_t s,
                               unsigned long long* h)
@@ -426,18 +436,10 @@ iso_status slab_count_enqueue(iso_ctx* ctx, iso_algorithm algo, const float* vol
     PassMarks pm(ctx, s);
     enqueue_count(ctx, algo, vol, g, iso, pl, b, s, pm);
     ISO_CUDA(ctx, cudaGetLastError());
-    ISO_CUDA(ctx, cudaMemcpyAsync(h, b.totals, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
-    for (int a = 0; a < 3; ++a) {
-        const long long rlo = (long long)(k0 - g.kr) * g.ny, rhi = (long long)(k1 - g.kr) * g.ny;
-        if (rlo > 0) {
-            ISO_CUDA(ctx, cudaMemcpyAsync(h + 3 + a, b.starts + (long long)a * g.R + rlo, sizeof(unsigned long long),
-                                          cudaMemcpyDeviceToHost, s));
-        }
-        if (k1 < g.nz) {
-            ISO_CUDA(ctx, cudaMemcpyAsync(h + 6 + a, b.starts + (long long)a * g.R + rhi, sizeof(unsigned long long),
-                                          cudaMemcpyDeviceToHost, s));
-        }
-    }
+    // h lies in ctx->h_slab; the kernel writes it through the device address
+    const long long rlo = (long long)(k0 - g.kr) * g.ny, rhi = (long long)(k1 - g.kr) * g.ny;
+    iso::launch_slab_readback(b, g, rlo, rhi, rlo > 0, k1 < g.nz, ctx->h_slab_dev + (h - ctx->h_slab), s);
+    ISO_CUDA(ctx, cudaGetLastError());
     return ISO_OK;
 }
 
@@ -454,8 +456,9 @@ void slab_count_read(const Grid& g, int64_t k0, int64_t k1, const unsigned long 
 iso_status slab_count(iso_ctx* ctx, iso_algorithm algo, const float* vol, const Grid& g, int64_t k0, int64_t k1,
                       float iso, const Plans& pl, FeBuffers& b, cudaStream_t s, SlabCounts& c)
 {
-    if (!ctx->h_slab) ISO_CUDA(ctx, cudaMallocHost(&ctx->h_slab, 18 * sizeof(unsigned long long)));
-    const iso_status st = slab_count_enqueue(ctx, algo, vol, g, k0, k1, iso, pl, b, s, ctx->h_slab);
+    iso_status st = ensure_h_slab(ctx);
+    if (st != ISO_OK) return st;
+    st = slab_count_enqueue(ctx, algo, vol, g, k0, k1, iso, pl, b, s, ctx->h_slab);
     if (st != ISO_OK) return st;
     ISO_CUDA(ctx, cudaStreamSynchronize(s));
     slab_count_read(g, k0, k1, ctx->h_slab, c);
@@ -590,6 +593,7 @@ iso_status extract_host_streamed(iso_ctx* ctx, iso_algorithm algo, const void* v
 {
     if (!ctx->s_h2d) ISO_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->s_h2d, cudaStreamNonBlocking));
     if (!ctx->s_d2h) ISO_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->s_d2h, cudaStreamNonBlocking));
+    if (!ctx->s_cnt) ISO_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->s_cnt, cudaStreamNonBlocking));
     const int nz = gfull.nz;
     const size_t plane = (size_t)gfull.nx * gfull.ny;
     const int nslab = (nz + kStreamPlanes - 1) / kStreamPlanes;
@@ -618,14 +622,39 @@ iso_status extract_host_streamed(iso_ctx* ctx, iso_algorithm algo, const void* v
     auto typed_window = [&](int q) {
         return static_cast<char*>(ctx->d_typed) + (size_t)(q % kStreamWindows) * wplanes * plane * elem;
     };
+    {
+        const iso_status e = ensure_h_slab(ctx);
+        if (e != ISO_OK) return e;
+    }
+    {  // both scratch sets sized for the largest slab up front: none is reallocated while a stream uses it
+        size_t best = 0;
+        int qb = 0;
+        for (int q = 0; q < nslab; ++q) {
+            Grid gq;
+            if (!slab_grid(grid, algo, slab_k0(q), slab_k0(q + 1), gq)) return ISO_ERR_INVALID_ARG;
+            const size_t need = scratch_size(gq, make_plans(ctx, gq).cp);
+            if (need > best) {
+                best = need;
+                qb = q;
+            }
+        }
+        Grid gq;
+        if (!slab_grid(grid, algo, slab_k0(qb), slab_k0(qb + 1), gq)) return ISO_ERR_INVALID_ARG;
+        const Plans pq = make_plans(ctx, gq);
+        FeBuffers unused;
+        iso_status e = ensure_scratch(ctx, gq, pq.cp, unused, s);
+        if (e == ISO_OK) e = ensure_scratch_b(ctx, gq, pq.cp, unused, s);
+        if (e != ISO_OK) return e;
+    }
     const char* src = static_cast<const char*>(volume);
     // events: 1 + q the planes of slab q have landed; 1 + nslab + w window w is
     // free again; 1 + nslab + kStreamWindows + sb slab generated into
     // staging sb; 1 + nslab + kStreamWindows + 2 + sb staging sb copied out
     const size_t ev_win = 1 + nslab, ev_gen = ev_win + kStreamWindows, ev_out = ev_gen + 2;
-    if (!sync_event(ctx, ev_out + 1)) return ISO_ERR_CUDA;
+    if (!sync_event(ctx, ev_out + 5)) return ISO_ERR_CUDA;  // with the count and scratch events below
     ISO_CUDA(ctx, cudaEventRecord(sync_event(ctx, 0), s));  // after the caller's earlier work on s
     ISO_CUDA(ctx, cudaStreamWaitEvent(ctx->s_h2d, sync_event(ctx, 0), 0));
+    ISO_CUDA(ctx, cudaStreamWaitEvent(ctx->s_cnt, sync_event(ctx, 0), 0));
     auto copy_in = [&](int q) -> iso_status {
         if (q >= kStreamWindows)  // the window's previous slab is generated
             ISO_CUDA(ctx, cudaStreamWaitEvent(ctx->s_h2d, sync_event(ctx, ev_win + q % kStreamWindows), 0));
@@ -644,10 +673,10 @@ iso_status extract_host_streamed(iso_ctx* ctx, iso_algorithm algo, const void* v
     long long V = 0, T = 0;
     bool room = true;  // the caller's buffers hold everything so far
     iso_status st = ISO_OK;
-    // Slab q+1 is counted (into the other scratch set) before slab q is
-    // generated, so the host reads counts that have already landed and the
-    // kernels run back to back.
-    if (!ctx->h_slab) ISO_CUDA(ctx, cudaMallocHost(&ctx->h_slab, 18 * sizeof(unsigned long long)));
+    // Slab q+1 is counted (into the other scratch set, on the count stream)
+    // while slab q is generated, so the host reads counts that have already
+    // landed and the generate pass of slab q never waits for the volume of
+    // slab q+1.
     struct SlabRun {
         Grid g;
         Plans pl;
@@ -655,26 +684,28 @@ iso_status extract_host_streamed(iso_ctx* ctx, iso_algorithm algo, const void* v
         int k0, k1;
     } run[2];
     const size_t ev_cnt = ev_out + 2;  // 2 events: counts of slab q landed in h_slab + 9 * (q & 1)
+    const size_t ev_scr = ev_cnt + 2;  // 2 events: slab q generated, scratch set q & 1 free again
     auto start_count = [&](int q) -> iso_status {
         SlabRun& r = run[q & 1];
         r.k0 = slab_k0(q);
         r.k1 = slab_k0(q + 1);
         if (!slab_grid(grid, algo, r.k0, r.k1, r.g)) return ISO_ERR_INVALID_ARG;
         r.pl = make_plans(ctx, r.g);
-        ISO_CUDA(ctx, cudaStreamWaitEvent(s, sync_event(ctx, 1 + q), 0));
+        cudaStream_t sc = ctx->s_cnt;
+        ISO_CUDA(ctx, cudaStreamWaitEvent(sc, sync_event(ctx, 1 + q), 0));
+        if (q >= 2) ISO_CUDA(ctx, cudaStreamWaitEvent(sc, sync_event(ctx, ev_scr + (q & 1)), 0));
         if (typed)
             iso::launch_to_float(typed_window(q), dtype, window(q),
-                                 (long long)(data_hi(q) - data_lo(q) + 1) * (long long)plane, ctx->nsm, s);
+                                 (long long)(data_hi(q) - data_lo(q) + 1) * (long long)plane, ctx->nsm, sc);
         iso_status e =
-            (q & 1) ? ensure_scratch_b(ctx, r.g, r.pl.cp, r.b, s) : ensure_scratch(ctx, r.g, r.pl.cp, r.b, s);
+            (q & 1) ? ensure_scratch_b(ctx, r.g, r.pl.cp, r.b, sc) : ensure_scratch(ctx, r.g, r.pl.cp, r.b, sc);
         if (e != ISO_OK) return e;
-        e = slab_count_enqueue(ctx, algo, window(q), r.g, r.k0, r.k1, isoval, r.pl, r.b, s,
+        e = slab_count_enqueue(ctx, algo, window(q), r.g, r.k0, r.k1, isoval, r.pl, r.b, sc,
                                ctx->h_slab + 9 * (q & 1));
         if (e != ISO_OK) return e;
-        ISO_CUDA(ctx, cudaEventRecord(sync_event(ctx, ev_cnt + (q & 1)), s));
+        ISO_CUDA(ctx, cudaEventRecord(sync_event(ctx, ev_cnt + (q & 1)), sc));
         return ISO_OK;
     };
-    if (!sync_event(ctx, ev_cnt + 1)) return ISO_ERR_CUDA;
     st = start_count(0);
     for (int q = 0; q < nslab && st == ISO_OK; ++q) {
         if (q + 1 < nslab) {
@@ -688,6 +719,7 @@ iso_status extract_host_streamed(iso_ctx* ctx, iso_algorithm algo, const void* v
         FeBuffers& b = r.b;
         const float* win = window(q);  // holds planes g.kd = data_lo(q) ..
         ISO_CUDA(ctx, cudaEventSynchronize(sync_event(ctx, ev_cnt + (q & 1))));
+        ISO_CUDA(ctx, cudaStreamWaitEvent(s, sync_event(ctx, ev_cnt + (q & 1)), 0));
         SlabCounts c;
         slab_count_read(g, k0, k1, ctx->h_slab + 9 * (q & 1), c);
         const long long Vq = (long long)(c.hi[mc ? 2 : 0] - c.lo[mc ? 2 : 0]), Tq = (long long)(c.hi[1] - c.lo[1]);
@@ -735,19 +767,21 @@ iso_status extract_host_streamed(iso_ctx* ctx, iso_algorithm algo, const void* v
         }
         V += Vq;
         T += Tq;
-        // window q % kStreamWindows is free once slab q's kernels are done: the next slab for it
+        // window q % kStreamWindows and scratch set q & 1 are free once slab q's kernels are done
         ISO_CUDA(ctx, cudaEventRecord(sync_event(ctx, ev_win + q % kStreamWindows), s));
+        ISO_CUDA(ctx, cudaEventRecord(sync_event(ctx, ev_scr + (q & 1)), s));
         if (q + kStreamWindows < nslab) {
             st = copy_in(q + kStreamWindows);
             if (st != ISO_OK) break;
         }
     }
-    // the mesh has landed when both copy streams and s are done
+    // the mesh has landed when the copy streams, the count stream and s are done
     const iso_status sh = cudaStreamSynchronize(ctx->s_h2d) == cudaSuccess ? ISO_OK : ISO_ERR_CUDA;
     const iso_status sd = cudaStreamSynchronize(ctx->s_d2h) == cudaSuccess ? ISO_OK : ISO_ERR_CUDA;
+    const iso_status sk = cudaStreamSynchronize(ctx->s_cnt) == cudaSuccess ? ISO_OK : ISO_ERR_CUDA;
     ISO_CUDA(ctx, cudaStreamSynchronize(s));
     if (st != ISO_OK) return st;
-    if (sh != ISO_OK || sd != ISO_OK) return ISO_ERR_CUDA;
+    if (sh != ISO_OK || sd != ISO_OK || sk != ISO_OK) return ISO_ERR_CUDA;
     out->n_points = V;
     out->n_tris = T;
     if (!room) {
@@ -906,6 +940,7 @@ iso_status iso_ctx_destroy(iso_ctx* ctx)
     for (cudaEvent_t e : ctx->sync_events) cudaEventDestroy(e);
     if (ctx->s_h2d) cudaStreamDestroy(ctx->s_h2d);
     if (ctx->s_d2h) cudaStreamDestroy(ctx->s_d2h);
+    if (ctx->s_cnt) cudaStreamDestroy(ctx->s_cnt);
     for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
     delete ctx;
     return ISO_OK;

@@ -703,6 +703,29 @@ RowStarts row_starts(const Grid& g, const CountPlan& p, const FeBuffers& b)
     return rs;
 }
 
+// A slab's counts for the host, written by one warp straight into mapped
+// pinned host memory (no copy engine: the read-back does not queue behind
+// bulk copies of other streams): out[a] the totals, out[3 + a] the start of
+// row rlo and out[6 + a] that of row rhi, for a = vertices, triangles, MC
+// vertices.
+__global__ void k_slab_readback(const unsigned long long* __restrict__ totals,
+                                const unsigned long long* __restrict__ starts, long long R, long long rlo,
+                                long long rhi, int has_lo, int has_hi, unsigned long long* out)
+{
+    const int a = threadIdx.x;
+    if (a < 3) {
+        out[a] = totals[a];
+        if (has_lo) out[3 + a] = starts[a * R + rlo];
+        if (has_hi) out[6 + a] = starts[a * R + rhi];
+    }
+}
+
+void launch_slab_readback(const FeBuffers& b, const Grid& g, long long rlo, long long rhi, bool has_lo, bool has_hi,
+                          unsigned long long* out, cudaStream_t s)
+{
+    k_slab_readback<<<1, 32, 0, s>>>(b.totals, b.starts, g.R, rlo, rhi, has_lo ? 1 : 0, has_hi ? 1 : 0, out);
+}
+
 void launch_grid_edges(const Grid& g, const CountPlan& p, const FeBuffers& b, int scanned, unsigned long long* ge,
                        unsigned long long* tri_counter, cudaStream_t s)
 {

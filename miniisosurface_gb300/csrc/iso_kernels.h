@@ -68,6 +68,9 @@ void launch_count(const float* vol, const Grid& g, float iso, const CaseTables* 
                   const CountPlan& p, FeBuffers& b, cudaStream_t s);
 enum ScanMode { kScanFE = 0, kScanMC = 1, kScanDup = 2 };
 void launch_scan(const Grid& g, const CountPlan& p, int mode, FeBuffers& b, cudaStream_t s);
+// totals and the starts of rows rlo / rhi into out[0..8] (device-visible host memory)
+void launch_slab_readback(const FeBuffers& b, const Grid& g, long long rlo, long long rhi, bool has_lo, bool has_hi,
+                          unsigned long long* out, cudaStream_t s);
 void launch_grid_edges(const Grid& g, const CountPlan& p, const FeBuffers& b, int scanned, unsigned long long* ge,
                        unsigned long long* tri_counter, cudaStream_t s);
 // Row-start accessor of a counted extraction.
