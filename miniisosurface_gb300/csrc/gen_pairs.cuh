@@ -1,0 +1,376 @@
+// Flying Edges pass 4 (FlyingEdgesAlgorithm.cpp:271-500) for rows of up to
+// 16 words (nx <= 512), two grid rows per warp (included by gen_warps_fe.cu).
+//
+// Lanes 16h .. 16h+15 hold words 0..15 of grid row j = jw + h.  Rows (jw, k)
+// and (jw+1, k) are neighbours in the output order (rows in (k, j) order, the
+// reference's), so the step's vertices are one list -- those of row jw, then
+// those of row jw+1, numbered from the first vertex of row jw -- and so are
+// its triangles -- cell row jw, then jw+1, from the first triangle of cell row
+// jw.  Each step runs the phases of k_gen_warps once for both rows: the cut
+// masks, their 16-lane prefix scans and the edge-id tables (one per row), one
+// joint compaction of the active cells and one joint triangle list, so that
+// the fixed work of a step is shared by two rows and the batches fill from
+// both.
+//
+// The vertices are not computed here: each lane writes, for every cut edge its
+// word owns, a record (i, axis, j, k) into the first 8 bytes of the vertex's
+// own 12-byte slot of the points buffer, and k_fe_vertices -- one thread per
+// vertex, many warps per SM to cover the latency of the volume gathers --
+// turns each record into the vertex's position and normal in place.
+#pragma once
+#include "gen_warps.cuh"
+
+namespace iso {
+
+constexpr int kGenPairRows = 2 * kGenRows;  // grid rows per CTA
+constexpr int kGenPairCtasPerSm = 4;        // resident CTAs per SM the kernel is built for
+
+// Per-warp scratch: mb[2][8][W] uint2, rwt[2][W][8], cell[32], the batch's
+// triangle list (u8).
+__host__ __device__ inline size_t gen_pair_scratch_bytes(int W)
+{
+    return ((size_t)2 * 8 * W * 8 + (size_t)2 * 8 * W * 4 + kGenCells * 4 + kGenTris + 15) & ~(size_t)15;
+}
+
+// Vertex record in the first 8 bytes of a vertex's points slot: word 0 =
+// i | axis << 10 | (j & 0xfffff) << 12, word 1 = j >> 20 | k << 8 (i < 1024,
+// j < 2^28, k < 2^24).
+__device__ __forceinline__ void put_vertex_record(float* points, unsigned long long idx, uint32_t i, uint32_t axis,
+                                                  uint32_t j, uint32_t k)
+{
+    uint32_t* r = reinterpret_cast<uint32_t*>(points) + 3 * idx;
+    r[0] = i | (axis << 10) | ((j & 0xfffffu) << 12);
+    r[1] = (j >> 20) | (k << 8);
+}
+
+// edge_vertex() of iso_device.cuh for the Flying Edges edge from P0 =
+// (i, j, kk) along axis a, with the operations of vertex_axis<a> on the same
+// operands (so bit-identical to it), written once for all three axes with the
+// axis as data: a warp of consecutive vertex ids mixes axes without diverging.
+__device__ __forceinline__ void vertex_any_axis(const float* __restrict__ vol, const Grid& g, const GradScale& gs,
+                                                float iso, int a, int i, int j, int kk, float3& pos, float3& nrm)
+{
+    const long long sy = g.nx, sz = (long long)g.nx * g.ny;
+    const float* p0 = vol + ((long long)(kk - g.kd) * g.ny + j) * g.nx + i;
+    const float* p1 = p0 + (a == 0 ? 1 : (a == 1 ? sy : sz));
+    const int i1 = i + (a == 0), j1 = j + (a == 1), k1 = kk + (a == 2);
+    const float v0 = __ldg(p0), v1 = __ldg(p1);
+    // neighbours of P0 and P1 = P0 + e_a; the edge's own values stand in along a
+    const float xm0 = i > 0 ? __ldg(p0 - 1) : 0.f;
+    const float xp0 = a == 0 ? v1 : (i < g.nx - 1 ? __ldg(p0 + 1) : 0.f);
+    const float ym0 = j > 0 ? __ldg(p0 - sy) : 0.f;
+    const float yp0 = a == 1 ? v1 : (j < g.ny - 1 ? __ldg(p0 + sy) : 0.f);
+    const float zm0 = kk > 0 ? __ldg(p0 - sz) : 0.f;
+    const float zp0 = a == 2 ? v1 : (kk < g.nz - 1 ? __ldg(p0 + sz) : 0.f);
+    const float xm1 = a == 0 ? v0 : (i1 > 0 ? __ldg(p1 - 1) : 0.f);
+    const float xp1 = i1 < g.nx - 1 ? __ldg(p1 + 1) : 0.f;
+    const float ym1 = a == 1 ? v0 : (j1 > 0 ? __ldg(p1 - sy) : 0.f);
+    const float yp1 = j1 < g.ny - 1 ? __ldg(p1 + sy) : 0.f;
+    const float zm1 = a == 2 ? v0 : (k1 > 0 ? __ldg(p1 - sz) : 0.f);
+    const float zp1 = k1 < g.nz - 1 ? __ldg(p1 + sz) : 0.f;
+    const float3 g0 = grad3(xm0, xp0, ym0, yp0, zm0, zp0, v0, i, j, kk, g, gs);
+    const float3 g1 = grad3(xm1, xp1, ym1, yp1, zm1, zp1, v1, i1, j1, k1, g, gs);
+    const float w = fdiv(fsub(iso, v0), fsub(v1, v0));
+    const int ci = a == 0 ? i : min(i, g.nx - 2), cj = a == 1 ? j : min(j, g.ny - 2);
+    const int ck = a == 2 ? kk : min(kk, g.nz - 2);
+    pos.x = lerp_ref(cube_coord(ci, i - ci, g.zp[0], g.sp[0]), cube_coord(ci, i1 - ci, g.zp[0], g.sp[0]), w);
+    pos.y = lerp_ref(cube_coord(cj, j - cj, g.zp[1], g.sp[1]), cube_coord(cj, j1 - cj, g.zp[1], g.sp[1]), w);
+    pos.z = lerp_ref(cube_coord(ck, kk - ck, g.zp[2], g.sp[2]), cube_coord(ck, k1 - ck, g.zp[2], g.sp[2]), w);
+    nrm.x = lerp_ref(g0.x, g1.x, w);
+    nrm.y = lerp_ref(g0.y, g1.y, w);
+    nrm.z = lerp_ref(g0.z, g1.z, w);
+}
+
+// The vertices of the rows of planes [kbeg, kend), one thread each, from the
+// records k_gen_pairs left in their points slots (slot v = vertex vbase + v).
+__global__ void __launch_bounds__(kThreads) k_fe_vertices(const float* __restrict__ vol, Grid g, GradScale gs,
+                                                          float iso, int kbeg, int kend,
+                                                          const unsigned long long* __restrict__ starts,
+                                                          const unsigned long long* __restrict__ totals,
+                                                          long long capV, long long capT, float* __restrict__ points,
+                                                          float* __restrict__ normals)
+{
+    if ((long long)totals[0] > capV || (long long)totals[1] > capT) return;  // k_gen_pairs wrote nothing
+    auto first = [&](int p) { return p < g.ke ? starts[(long long)(p - g.kr) * g.ny] : totals[0]; };
+    const unsigned long long n = first(kend) - first(kbeg);
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    for (unsigned long long v = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride) {
+        const uint2 r = make_uint2(reinterpret_cast<const uint32_t*>(points)[3 * v],
+                                   reinterpret_cast<const uint32_t*>(points)[3 * v + 1]);
+        const int i = (int)(r.x & 1023u), a = (int)((r.x >> 10) & 3u);
+        const int j = (int)((r.x >> 12) | ((r.y & 0xffu) << 20)), kk = (int)(r.y >> 8);
+        // every slot holds a record of the launch's rows; anything else is left alone, never read through
+        if (a > 2 || i + (a == 0) >= g.nx || j + (a == 1) >= g.ny || kk < kbeg || kk >= kend ||
+            kk + (a == 2) >= g.nz)
+            continue;
+        float3 p, nm;
+        vertex_any_axis(vol, g, gs, iso, a, i, j, kk, p, nm);
+        store_vertex(points, normals, v, p, nm);
+    }
+}
+
+// Inclusive scan within each 16-lane half of the warp.
+__device__ __forceinline__ uint32_t half_incl_scan(uint32_t v, int l16)
+{
+#pragma unroll
+    for (int d = 1; d < 16; d <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, v, d, 16);
+        if (l16 >= d) v += t;
+    }
+    return v;
+}
+
+template <typename IndexT>
+__global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
+    const float* __restrict__ vol, const uint32_t* __restrict__ bits, Grid g, GradScale gs, float iso, int KC,
+    int nyb, int kbeg, int kend, unsigned long long vbase, unsigned long long tbase, int ws_bytes,
+    const CaseTables* __restrict__ cases, const uint4* __restrict__ rowcnt, RowStarts rs,
+    const unsigned long long* __restrict__ totals, long long capV, long long capT, float* __restrict__ points,
+    float* __restrict__ normals, IndexT* __restrict__ tris, int reverse)
+{
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    __shared__ uint64_t s_tris[256];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, h = lane >> 4, l16 = lane & 15;
+    const int W = g.W;
+    unsigned char* ws = s_raw + (size_t)warp * ws_bytes;
+    uint2* mb = reinterpret_cast<uint2*>(ws);                                  // [2][8][W]
+    uint32_t* rwt = reinterpret_cast<uint32_t*>(ws + (size_t)2 * 8 * W * 8);  // [2][W][8]
+    uint32_t* cell = rwt + 2 * 8 * W;
+    unsigned char* list = reinterpret_cast<unsigned char*>(cell + kGenCells);
+    for (int c = tid; c < 256; c += kThreads) s_tris[c] = cases->tris[c];
+    __syncthreads();  // the only CTA barrier: from here on every warp runs alone
+    if ((long long)totals[0] > capV || (long long)totals[1] > capT) return;  // caller grows buffers
+
+    const int nkc = gridDim.x / nyb;
+    const int jb = blockIdx.x % nyb;
+    const int kc = reverse ? nkc - 1 - (int)(blockIdx.x / nyb) : (int)(blockIdx.x / nyb);
+    const int j0 = jb * kGenPairRows;
+    const int kb = kbeg + kc * KC, ke = min(kb + KC, kend);
+    const int jw = j0 + 2 * warp;
+    if (jw >= g.ny) return;
+    const int j = jw + h;
+    const bool row_ok = j < g.ny;
+    const int jlo = j0 > 0 ? j0 - 1 : 0;  // planes are addressed from this row
+    const long long plane = (long long)g.ny * g.nx;
+    auto plane_ptr = [&](int p) { return vol + (long long)(p - g.kd) * plane + (long long)jlo * g.nx; };
+
+    const bool hasY = row_ok && j < g.ny - 1;
+    const bool in = row_ok && l16 < W, in1 = l16 + 1 < W;
+    const uint32_t evalid = validmask(l16, g.nx - 1);  // x-edges / cells: i <= nx-2
+    const uint32_t pvalid = validmask(l16, g.nx);      // points: i <= nx-1
+    uint2* mbh = mb + h * 8 * W;
+    uint32_t* rwth = rwt + h * 8 * W;
+
+    // Bit words of rows (j, p) and (j+1, p).
+    auto load_words = [&](int p, uint32_t& wa, uint32_t& wb) {
+        const bool okp = p < g.ke;  // rows of the window
+        const long long r = (long long)(p - g.kr) * g.ny + j;
+        wa = (in && okp) ? __ldg(&bits[r * W + l16]) : 0u;
+        wb = (in && okp && hasY) ? __ldg(&bits[(r + 1) * W + l16]) : 0u;
+    };
+    // Row starts of step p, lanes 0..5 of each half for its row: the first
+    // vertex of rows A = (j,p), B = (j+1,p), C = (j,p+1), D = (j+1,p+1), the
+    // first triangle of cell row A, the x + y cuts of row B.
+    auto load_starts = [&](int p) -> unsigned long long {
+        const int dk = (l16 >> 1) & 1, dj = l16 & 1;
+        const bool hasZp = p + 1 < g.ke;
+        bool ok = row_ok && l16 < 6;
+        if (l16 < 4) ok = ok && (dj == 0 || hasY) && (dk == 0 || hasZp);
+        if (l16 == 5) ok = ok && hasY;
+        if (!ok) return 0ull;
+        const long long rA = (long long)(p - g.kr) * g.ny + j;
+        if (l16 == 5) {
+            const uint2 c = __ldg(reinterpret_cast<const uint2*>(&rowcnt[rA + 1]));
+            return (unsigned long long)c.x + c.y;
+        }
+        const long long r = l16 < 4 ? rA + (long long)dk * g.ny + dj : rA;
+        return rs.get(r, l16 < 4 ? 0 : 1);
+    };
+
+    uint32_t wA = 0, wB = 0, wC = 0, wD = 0;
+    load_words(kb, wA, wB);
+    load_words(kb + 1, wC, wD);
+    unsigned long long st = load_starts(kb);
+
+    for (int k = kb; k < ke; ++k) {
+        const bool hasZ = k + 1 < g.nz;
+        // the next step's words and starts, in flight while this step runs
+        uint32_t nC = 0, nD = 0;
+        unsigned long long nst = 0;
+        if (k + 1 < ke) {
+            load_words(k + 2, nC, nD);
+            nst = load_starts(k + 1);
+        }
+        const bool cellrow = hasY && hasZ;
+        RowWords rw;
+        rw.a = wA;
+        rw.b = wB;
+        rw.c = hasZ ? wC : 0u;
+        rw.d = cellrow ? wD : 0u;
+        const uint32_t an = __shfl_down_sync(0xffffffffu, rw.a, 1, 16);
+        const uint32_t bn = __shfl_down_sync(0xffffffffu, rw.b, 1, 16);
+        const uint32_t cn = __shfl_down_sync(0xffffffffu, rw.c, 1, 16);
+        const uint32_t dn = __shfl_down_sync(0xffffffffu, rw.d, 1, 16);
+        rw.ash = (rw.a >> 1) | ((in1 ? an : 0u) << 31);
+        rw.bsh = (rw.b >> 1) | ((in1 ? bn : 0u) << 31);
+        rw.csh = (rw.c >> 1) | ((in1 ? cn : 0u) << 31);
+        rw.dsh = (rw.d >> 1) | ((in1 ? dn : 0u) << 31);
+        const CutMasks m = cut_masks(rw, evalid, pvalid, hasY, hasZ);
+        // popc prefixes within each half, two 16-bit counts per scan
+        const uint32_t p0 = __popc(m.xA) | (__popc(m.xB) << 16);
+        const uint32_t p1 = __popc(m.xC) | (__popc(m.xD) << 16);
+        const uint32_t p2 = __popc(m.yA) | (__popc(m.yC) << 16);
+        const uint32_t p3 = __popc(m.zA) | (__popc(m.zB) << 16);
+        const uint32_t i0 = half_incl_scan(p0, l16), i1 = half_incl_scan(p1, l16);
+        const uint32_t i2 = half_incl_scan(p2, l16), i3 = half_incl_scan(p3, l16);
+        const uint32_t e0 = i0 - p0, e1 = i1 - p1, e2 = i2 - p2, e3 = i3 - p3;
+        const uint32_t t0 = __shfl_sync(0xffffffffu, i0, 15, 16), t2 = __shfl_sync(0xffffffffu, i2, 15, 16);
+        const uint32_t t1 = __shfl_sync(0xffffffffu, i1, 15, 16), t3 = __shfl_sync(0xffffffffu, i3, 15, 16);
+        const unsigned long long xsA = __shfl_sync(0xffffffffu, st, 0, 16);  // this half's row
+        const unsigned long long xs0 = __shfl_sync(0xffffffffu, st, 0);      // row jw: the step's numbering
+        const uint32_t dB = (uint32_t)(__shfl_sync(0xffffffffu, st, 1, 16) - xsA);
+        const uint32_t dC = (uint32_t)(__shfl_sync(0xffffffffu, st, 2, 16) - xsA);
+        const uint32_t dD = (uint32_t)(__shfl_sync(0xffffffffu, st, 3, 16) - xsA);
+        const uint32_t cntB = (uint32_t)__shfl_sync(0xffffffffu, st, 5, 16);
+        const unsigned long long ts0 = __shfl_sync(0xffffffffu, st, 4);  // first triangle of cell row jw
+        const uint32_t nxA = t0 & 0xffffu, nyA = t2 & 0xffffu, nxC = t1 & 0xffffu;
+        const uint32_t off = (uint32_t)(xsA - xs0);  // 0, or the vertices of row jw
+        if (in) {  // first ids of the word's cut edges, relative to xs0
+            mbh[0 * W + l16] = make_uint2(m.xA, off + (e0 & 0xffffu));
+            mbh[1 * W + l16] = make_uint2(m.xB, off + dB + (e0 >> 16));
+            mbh[2 * W + l16] = make_uint2(m.xC, off + dC + (e1 & 0xffffu));
+            mbh[3 * W + l16] = make_uint2(m.xD, off + dD + (e1 >> 16));
+            mbh[4 * W + l16] = make_uint2(m.yA, off + nxA + (e2 & 0xffffu));
+            mbh[5 * W + l16] = make_uint2(m.yC, off + dC + nxC + (e2 >> 16));
+            mbh[6 * W + l16] = make_uint2(m.zA, off + nxA + nyA + (e3 & 0xffffu));
+            mbh[7 * W + l16] = make_uint2(m.zB, off + dB + cntB + (e3 >> 16));
+            if (cellrow) {  // corner order of the cube case: bit v = corner v
+                uint4* t = reinterpret_cast<uint4*>(rwth + 8 * l16);
+                t[0] = make_uint4(rw.a, rw.ash, rw.bsh, rw.b);
+                t[1] = make_uint4(rw.c, rw.csh, rw.dsh, rw.d);
+            }
+        }
+        __syncwarp();
+
+        // ---- vertex records of grid row (j, k): the x, y, z cuts its word owns
+        if (in) {
+            auto records = [&](uint32_t mk, uint32_t first, uint32_t axis) {
+                unsigned long long idx = xs0 + first - vbase;
+                while (mk != 0u) {
+                    put_vertex_record(points, idx, (uint32_t)(32 * l16 + __ffs(mk) - 1), axis, (uint32_t)j,
+                                      (uint32_t)k);
+                    mk &= mk - 1u;
+                    ++idx;
+                }
+            };
+            records(m.xA, off + (e0 & 0xffffu), 0u);
+            records(m.yA, off + nxA + (e2 & 0xffffu), 1u);
+            records(m.zA, off + nxA + nyA + (e3 & 0xffffu), 2u);
+        }
+
+        // ---- active cells of cell rows (jw, k) and (jw+1, k), compacted 32 at a time
+        uint32_t rem = (in && cellrow) ? active_cells(rw, evalid) : 0u;
+        const uint32_t na = __popc(rem);
+        const uint32_t ia = warp_incl_scan(na, lane);  // the cells of row jw come first
+        uint32_t rank = ia - na;
+        const uint32_t tot = __shfl_sync(0xffffffffu, ia, 31);
+        unsigned long long tcur = ts0;
+        for (uint32_t c0 = 0; c0 < tot; c0 += kGenCells) {
+            while (rem != 0u && rank < c0 + kGenCells) {
+                cell[rank - c0] = (uint32_t)(32 * l16 + __ffs(rem) - 1) | ((uint32_t)h << 9);
+                rem &= rem - 1u;
+                ++rank;
+            }
+            __syncwarp();
+            const uint32_t nc = min(tot - c0, (uint32_t)kGenCells);
+            const bool live = (uint32_t)lane < nc;
+            uint32_t rec = 0u;
+            if (live) {  // the cell's cube case from its word's row words
+                const uint32_t ch = cell[lane];
+                const uint32_t ci = ch & 511u;
+                const uint4* t = reinterpret_cast<const uint4*>(rwt + (ch >> 9) * 8 * W + 8 * (ci >> 5));
+                const uint4 lo4 = t[0], hi4 = t[1];
+                const int b = (int)(ci & 31u);
+                const uint32_t cs = ((lo4.x >> b) & 1u) | (((lo4.y >> b) & 1u) << 1) | (((lo4.z >> b) & 1u) << 2) |
+                                    (((lo4.w >> b) & 1u) << 3) | (((hi4.x >> b) & 1u) << 4) |
+                                    (((hi4.y >> b) & 1u) << 5) | (((hi4.z >> b) & 1u) << 6) |
+                                    (((hi4.w >> b) & 1u) << 7);
+                rec = ch | (cs << 16);
+                cell[lane] = rec;
+            }
+            const int cs = (int)(rec >> 16);
+            const uint32_t nt = live ? (uint32_t)iso_case_ntris(s_tris[cs]) : 0u;
+            const uint32_t it = warp_incl_scan(nt, lane);
+            const uint32_t ntb = __shfl_sync(0xffffffffu, it, 31);
+            for (uint32_t q = 0; q < nt; ++q) list[it - nt + q] = (unsigned char)(lane | (q << 5));
+            __syncwarp();
+            for (uint32_t tb = 0; tb < ntb; tb += 32) {
+                const uint32_t t = tb + lane;
+                if (t < ntb) {
+                    const uint32_t tr = list[t];
+                    const uint32_t cr = cell[tr & 31u];
+                    const int q = (int)(tr >> 5);
+                    const int ci = (int)(cr & 511u);
+                    const uint2* mbc = mb + ((cr >> 9) & 1u) * 8 * W;
+                    const uint64_t tl = s_tris[cr >> 16];
+                    const int w = ci >> 5, bit = ci & 31;
+                    IndexT* o = tris + 3 * (tcur + t - tbase);
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        const int e = iso_case_edge(tl, 3 * q + c);
+                        o[c] = (IndexT)(xs0 + fe_edge_rel(mbc, W, e, w, bit));
+                    }
+                }
+            }
+            tcur += ntb;
+            __syncwarp();  // the next batch overwrites the lists
+        }
+        __syncwarp();  // the next step overwrites mb
+        wA = wC;
+        wB = wD;
+        wC = nC;
+        wD = nD;
+        st = nst;
+    }
+}
+
+// Columns of KC planes over [p.kbeg, p.kend) for blocks of kGenPairRows
+// rows: about two waves of resident CTAs, at least 4 planes per column.
+inline void gen_pairs_split(GenPlan& p, const Grid& g, int nsm)
+{
+    p.nyb = (g.ny + kGenPairRows - 1) / kGenPairRows;
+    const int nzw = p.kend - p.kbeg;
+    const long long resident = (long long)nsm * kGenPairCtasPerSm;
+    int nkc = (int)((2 * resident + p.nyb - 1) / p.nyb);
+    if (nkc < 1) nkc = 1;
+    p.KC = (nzw + nkc - 1) / nkc;
+    if (p.KC < 4) p.KC = 4;
+    if (p.KC > nzw) p.KC = nzw;
+    if (p.KC < 1) p.KC = 1;
+    p.nkc = nzw > 0 ? (nzw + p.KC - 1) / p.KC : 0;
+}
+
+template <typename IndexT>
+void launch_gen_pairs_impl(const float* vol, const Grid& g, float iso, const CaseTables* cases, const FeBuffers& b,
+                           const CountPlan& cp, const GenPlan& plan, int nsm, long long capV, long long capT,
+                           float* points, float* normals, IndexT* tris, int reverse, cudaStream_t s)
+{
+    GenPlan p = plan;
+    gen_pairs_split(p, g, nsm);
+    if (p.nkc == 0) return;
+    RowStarts rs = row_starts(g, cp, b);
+    for (int a = 0; a < 3; ++a) rs.add[a] = p.add[a];
+    const unsigned blocks = (unsigned)(p.nyb * p.nkc);
+    const int ws_bytes = (int)gen_pair_scratch_bytes(g.W);
+    const size_t smem = (size_t)kGenRows * ws_bytes;
+    auto kern = k_gen_pairs<IndexT>;
+    allow_smem(kern, smem);
+    const GradScale gs = make_grad_scale(g);
+    kern<<<blocks, kThreads, smem, s>>>(vol, b.bits, g, gs, iso, p.KC, p.nyb, p.kbeg, p.kend, p.vbase, p.tbase,
+                                        ws_bytes, cases, b.rowcnt, rs, b.totals, capV, capT, points, normals, tris,
+                                        reverse);
+    k_fe_vertices<<<(unsigned)nsm * 8, kThreads, 0, s>>>(vol, g, gs, iso, p.kbeg, p.kend, b.starts, b.totals, capV,
+                                                         capT, points, normals);
+}
+
+}  // namespace iso

@@ -1,5 +1,7 @@
-// Flying Edges pass 4 (warp-per-row kernel of gen_warps.cuh) and the plan of
-// the warp-per-row kernels.
+// Flying Edges pass 4 (two rows per warp, gen_pairs.cuh, for rows of up to 16
+// words; else one row per warp, gen_warps.cuh) and the plan of the
+// warp-per-row kernels.
+#include "gen_pairs.cuh"
 #include "gen_warps.cuh"
 
 namespace iso {
@@ -11,6 +13,7 @@ namespace iso {
 // at least 4 planes per column.
 void gen_split(GenPlan& p, int nsm)
 {
+    p.nsm = nsm;
     const int nzw = p.kend - p.kbeg;
     const long long resident = (long long)nsm * kGenCtasPerSm;
     int nkc = (int)((4 * resident + p.nyb - 1) / p.nyb);
@@ -42,8 +45,12 @@ void launch_fe_gen_warps(const float* vol, const Grid& g, float iso, const CaseT
                          const CountPlan& cp, const GenPlan& p, long long capV, long long capT, float* points,
                          float* normals, IndexT* tris, int reverse, cudaStream_t s)
 {
-    launch_gen_warps_impl<kGenFE, IndexT>(vol, g, iso, cases, b, cp, p, capV, capT, points, normals, tris, reverse,
-                                          s);
+    if (g.W <= 16 && p.nsm > 0)  // two rows per warp
+        launch_gen_pairs_impl<IndexT>(vol, g, iso, cases, b, cp, p, p.nsm, capV, capT, points, normals, tris,
+                                      reverse, s);
+    else
+        launch_gen_warps_impl<kGenFE, IndexT>(vol, g, iso, cases, b, cp, p, capV, capT, points, normals, tris,
+                                              reverse, s);
 }
 
 template void launch_fe_gen_warps<uint32_t>(const float*, const Grid&, float, const CaseTables*, const FeBuffers&,

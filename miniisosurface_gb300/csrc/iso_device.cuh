@@ -562,7 +562,9 @@ struct RowStarts {
     unsigned long long add[4];
     __device__ __forceinline__ unsigned long long get(long long r, int comp) const
     {
-        return __ldg(&starts[comp * R + r]) + add[comp];
+        // selects, not add[comp]: a kernel parameter array indexed at run time is copied to local memory
+        const unsigned long long a = comp == 0 ? add[0] : (comp == 1 ? add[1] : (comp == 2 ? add[2] : add[3]));
+        return __ldg(&starts[comp * R + r]) + a;
     }
     __device__ __forceinline__ unsigned long long get(int k, int j, int comp) const
     {

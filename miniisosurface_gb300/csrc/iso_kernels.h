@@ -42,6 +42,7 @@ struct GenPlan {
     unsigned long long vbase = 0, tbase = 0;
     unsigned long long add[4] = {0, 0, 0, 0};
     size_t smem = 0;  // per-warp scratch of the CTA
+    int nsm = 0;      // SMs of the device the plan is for
     bool fits = false;  // false: use the row-wise kernels
 };
 
