@@ -83,20 +83,31 @@ __device__ __forceinline__ void vertex_any_axis(const float* __restrict__ vol, c
 
 // The vertices of the rows of planes [kbeg, kend), one thread each, from the
 // records k_gen_pairs left in their points slots (slot v = vertex vbase + v).
-__global__ void __launch_bounds__(kThreads) k_fe_vertices(const float* __restrict__ vol, Grid g, GradScale gs,
-                                                          float iso, int kbeg, int kend,
-                                                          const unsigned long long* __restrict__ starts,
-                                                          const unsigned long long* __restrict__ totals,
-                                                          long long capV, long long capT, float* __restrict__ points,
-                                                          float* __restrict__ normals)
+// One wave of kFeVertexCtasPerSm CTAs per SM walks the slots with a stride;
+// each thread loads the record of its next slot before it works on the
+// current one, so the record's trip to memory overlaps the volume gathers.
+constexpr int kFeVertexCtasPerSm = 6;
+
+__device__ __forceinline__ uint2 vertex_record(const float* points, unsigned long long v)
+{
+    const uint32_t* r = reinterpret_cast<const uint32_t*>(points) + 3 * v;
+    return make_uint2(r[0], r[1]);
+}
+
+__global__ void __launch_bounds__(kThreads, kFeVertexCtasPerSm)
+    k_fe_vertices(const float* __restrict__ vol, Grid g, GradScale gs, float iso, int kbeg, int kend,
+                  const unsigned long long* __restrict__ starts, const unsigned long long* __restrict__ totals,
+                  long long capV, long long capT, float* __restrict__ points, float* __restrict__ normals)
 {
     if ((long long)totals[0] > capV || (long long)totals[1] > capT) return;  // k_gen_pairs wrote nothing
     auto first = [&](int p) { return p < g.ke ? starts[(long long)(p - g.kr) * g.ny] : totals[0]; };
     const unsigned long long n = first(kend) - first(kbeg);
     const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
-    for (unsigned long long v = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride) {
-        const uint2 r = make_uint2(reinterpret_cast<const uint32_t*>(points)[3 * v],
-                                   reinterpret_cast<const uint32_t*>(points)[3 * v + 1]);
+    unsigned long long v = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    uint2 next = v < n ? vertex_record(points, v) : make_uint2(0u, 0u);
+    for (; v < n; v += stride) {
+        const uint2 r = next;
+        if (v + stride < n) next = vertex_record(points, v + stride);  // this thread's next slot
         const int i = (int)(r.x & 1023u), a = (int)((r.x >> 10) & 3u);
         const int j = (int)((r.x >> 12) | ((r.y & 0xffu) << 20)), kk = (int)(r.y >> 8);
         // every slot holds a record of the launch's rows; anything else is left alone, never read through
@@ -120,13 +131,17 @@ __device__ __forceinline__ uint32_t half_incl_scan(uint32_t v, int l16)
     return v;
 }
 
+// One wave of CTAs; every warp takes work items -- a row pair and a run of KC
+// planes -- from the counter `work` until none is left, so no warp waits for
+// another and no CTA stays resident for its slowest warp.  Item q is row pair
+// q % npairs of plane run q / npairs (runs walked backwards when `reverse`).
 template <typename IndexT>
 __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
-    const float* __restrict__ vol, const uint32_t* __restrict__ bits, Grid g, GradScale gs, float iso, int KC,
-    int nyb, int kbeg, int kend, unsigned long long vbase, unsigned long long tbase, int ws_bytes,
-    const CaseTables* __restrict__ cases, const uint4* __restrict__ rowcnt, RowStarts rs,
-    const unsigned long long* __restrict__ totals, long long capV, long long capT, float* __restrict__ points,
-    float* __restrict__ normals, IndexT* __restrict__ tris, int reverse)
+    const uint32_t* __restrict__ bits, Grid g, int KC, int npairs, int nkc, int kbeg, int kend,
+    unsigned long long vbase, unsigned long long tbase, int ws_bytes, const CaseTables* __restrict__ cases,
+    const uint4* __restrict__ rowcnt, RowStarts rs, const unsigned long long* __restrict__ totals,
+    unsigned int* __restrict__ work, long long capV, long long capT, float* __restrict__ points,
+    IndexT* __restrict__ tris, int reverse)
 {
     extern __shared__ __align__(16) unsigned char s_raw[];
     __shared__ uint64_t s_tris[256];
@@ -141,236 +156,232 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
     __syncthreads();  // the only CTA barrier: from here on every warp runs alone
     if ((long long)totals[0] > capV || (long long)totals[1] > capT) return;  // caller grows buffers
 
-    const int nkc = gridDim.x / nyb;
-    const int jb = blockIdx.x % nyb;
-    const int kc = reverse ? nkc - 1 - (int)(blockIdx.x / nyb) : (int)(blockIdx.x / nyb);
-    const int j0 = jb * kGenPairRows;
-    const int kb = kbeg + kc * KC, ke = min(kb + KC, kend);
-    const int jw = j0 + 2 * warp;
-    if (jw >= g.ny) return;
-    const int j = jw + h;
-    const bool row_ok = j < g.ny;
-    const int jlo = j0 > 0 ? j0 - 1 : 0;  // planes are addressed from this row
-    const long long plane = (long long)g.ny * g.nx;
-    auto plane_ptr = [&](int p) { return vol + (long long)(p - g.kd) * plane + (long long)jlo * g.nx; };
-
-    const bool hasY = row_ok && j < g.ny - 1;
-    const bool in = row_ok && l16 < W, in1 = l16 + 1 < W;
+    const bool in1 = l16 + 1 < W;
     const uint32_t evalid = validmask(l16, g.nx - 1);  // x-edges / cells: i <= nx-2
     const uint32_t pvalid = validmask(l16, g.nx);      // points: i <= nx-1
     uint2* mbh = mb + h * 8 * W;
     uint32_t* rwth = rwt + h * 8 * W;
+    const uint32_t nitems = (uint32_t)npairs * (uint32_t)nkc;
+    for (;;) {
+        uint32_t item = 0u;
+        if (lane == 0) item = atomicAdd(work, 1u);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= nitems) break;
+        const int col = (int)(item / (uint32_t)npairs);
+        const int kc = reverse ? nkc - 1 - col : col;
+        const int jw = 2 * (int)(item % (uint32_t)npairs);
+        const int kb = kbeg + kc * KC, ke = min(kb + KC, kend);
+        const int j = jw + h;
+        const bool row_ok = j < g.ny;
+        const bool hasY = row_ok && j < g.ny - 1;
+        const bool in = row_ok && l16 < W;
 
-    // Bit words of rows (j, p) and (j+1, p).
-    auto load_words = [&](int p, uint32_t& wa, uint32_t& wb) {
-        const bool okp = p < g.ke;  // rows of the window
-        const long long r = (long long)(p - g.kr) * g.ny + j;
-        wa = (in && okp) ? __ldg(&bits[r * W + l16]) : 0u;
-        wb = (in && okp && hasY) ? __ldg(&bits[(r + 1) * W + l16]) : 0u;
-    };
-    // Row starts of step p, lanes 0..5 of each half for its row: the first
-    // vertex of rows A = (j,p), B = (j+1,p), C = (j,p+1), D = (j+1,p+1), the
-    // first triangle of cell row A, the x + y cuts of row B.
-    auto load_starts = [&](int p) -> unsigned long long {
-        const int dk = (l16 >> 1) & 1, dj = l16 & 1;
-        const bool hasZp = p + 1 < g.ke;
-        bool ok = row_ok && l16 < 6;
-        if (l16 < 4) ok = ok && (dj == 0 || hasY) && (dk == 0 || hasZp);
-        if (l16 == 5) ok = ok && hasY;
-        if (!ok) return 0ull;
-        const long long rA = (long long)(p - g.kr) * g.ny + j;
-        if (l16 == 5) {
-            const uint2 c = __ldg(reinterpret_cast<const uint2*>(&rowcnt[rA + 1]));
-            return (unsigned long long)c.x + c.y;
-        }
-        const long long r = l16 < 4 ? rA + (long long)dk * g.ny + dj : rA;
-        return rs.get(r, l16 < 4 ? 0 : 1);
-    };
-
-    uint32_t wA = 0, wB = 0, wC = 0, wD = 0;
-    load_words(kb, wA, wB);
-    load_words(kb + 1, wC, wD);
-    unsigned long long st = load_starts(kb);
-
-    for (int k = kb; k < ke; ++k) {
-        const bool hasZ = k + 1 < g.nz;
-        // the next step's words and starts, in flight while this step runs
-        uint32_t nC = 0, nD = 0;
-        unsigned long long nst = 0;
-        if (k + 1 < ke) {
-            load_words(k + 2, nC, nD);
-            nst = load_starts(k + 1);
-        }
-        const bool cellrow = hasY && hasZ;
-        RowWords rw;
-        rw.a = wA;
-        rw.b = wB;
-        rw.c = hasZ ? wC : 0u;
-        rw.d = cellrow ? wD : 0u;
-        const uint32_t an = __shfl_down_sync(0xffffffffu, rw.a, 1, 16);
-        const uint32_t bn = __shfl_down_sync(0xffffffffu, rw.b, 1, 16);
-        const uint32_t cn = __shfl_down_sync(0xffffffffu, rw.c, 1, 16);
-        const uint32_t dn = __shfl_down_sync(0xffffffffu, rw.d, 1, 16);
-        rw.ash = (rw.a >> 1) | ((in1 ? an : 0u) << 31);
-        rw.bsh = (rw.b >> 1) | ((in1 ? bn : 0u) << 31);
-        rw.csh = (rw.c >> 1) | ((in1 ? cn : 0u) << 31);
-        rw.dsh = (rw.d >> 1) | ((in1 ? dn : 0u) << 31);
-        const CutMasks m = cut_masks(rw, evalid, pvalid, hasY, hasZ);
-        // popc prefixes within each half, two 16-bit counts per scan
-        const uint32_t p0 = __popc(m.xA) | (__popc(m.xB) << 16);
-        const uint32_t p1 = __popc(m.xC) | (__popc(m.xD) << 16);
-        const uint32_t p2 = __popc(m.yA) | (__popc(m.yC) << 16);
-        const uint32_t p3 = __popc(m.zA) | (__popc(m.zB) << 16);
-        const uint32_t i0 = half_incl_scan(p0, l16), i1 = half_incl_scan(p1, l16);
-        const uint32_t i2 = half_incl_scan(p2, l16), i3 = half_incl_scan(p3, l16);
-        const uint32_t e0 = i0 - p0, e1 = i1 - p1, e2 = i2 - p2, e3 = i3 - p3;
-        const uint32_t t0 = __shfl_sync(0xffffffffu, i0, 15, 16), t2 = __shfl_sync(0xffffffffu, i2, 15, 16);
-        const uint32_t t1 = __shfl_sync(0xffffffffu, i1, 15, 16), t3 = __shfl_sync(0xffffffffu, i3, 15, 16);
-        const unsigned long long xsA = __shfl_sync(0xffffffffu, st, 0, 16);  // this half's row
-        const unsigned long long xs0 = __shfl_sync(0xffffffffu, st, 0);      // row jw: the step's numbering
-        const uint32_t dB = (uint32_t)(__shfl_sync(0xffffffffu, st, 1, 16) - xsA);
-        const uint32_t dC = (uint32_t)(__shfl_sync(0xffffffffu, st, 2, 16) - xsA);
-        const uint32_t dD = (uint32_t)(__shfl_sync(0xffffffffu, st, 3, 16) - xsA);
-        const uint32_t cntB = (uint32_t)__shfl_sync(0xffffffffu, st, 5, 16);
-        const unsigned long long ts0 = __shfl_sync(0xffffffffu, st, 4);  // first triangle of cell row jw
-        const uint32_t nxA = t0 & 0xffffu, nyA = t2 & 0xffffu, nxC = t1 & 0xffffu;
-        const uint32_t off = (uint32_t)(xsA - xs0);  // 0, or the vertices of row jw
-        if (in) {  // first ids of the word's cut edges, relative to xs0
-            mbh[0 * W + l16] = make_uint2(m.xA, off + (e0 & 0xffffu));
-            mbh[1 * W + l16] = make_uint2(m.xB, off + dB + (e0 >> 16));
-            mbh[2 * W + l16] = make_uint2(m.xC, off + dC + (e1 & 0xffffu));
-            mbh[3 * W + l16] = make_uint2(m.xD, off + dD + (e1 >> 16));
-            mbh[4 * W + l16] = make_uint2(m.yA, off + nxA + (e2 & 0xffffu));
-            mbh[5 * W + l16] = make_uint2(m.yC, off + dC + nxC + (e2 >> 16));
-            mbh[6 * W + l16] = make_uint2(m.zA, off + nxA + nyA + (e3 & 0xffffu));
-            mbh[7 * W + l16] = make_uint2(m.zB, off + dB + cntB + (e3 >> 16));
-            if (cellrow) {  // corner order of the cube case: bit v = corner v
-                uint4* t = reinterpret_cast<uint4*>(rwth + 8 * l16);
-                t[0] = make_uint4(rw.a, rw.ash, rw.bsh, rw.b);
-                t[1] = make_uint4(rw.c, rw.csh, rw.dsh, rw.d);
+        // Bit words of rows (j, p) and (j+1, p).
+        auto load_words = [&](int p, uint32_t& wa, uint32_t& wb) {
+            const bool okp = p < g.ke;  // rows of the window
+            const long long r = (long long)(p - g.kr) * g.ny + j;
+            wa = (in && okp) ? __ldg(&bits[r * W + l16]) : 0u;
+            wb = (in && okp && hasY) ? __ldg(&bits[(r + 1) * W + l16]) : 0u;
+        };
+        // Row starts of step p, lanes 0..5 of each half for its row: the first
+        // vertex of rows A = (j,p), B = (j+1,p), C = (j,p+1), D = (j+1,p+1), the
+        // first triangle of cell row A, the x + y cuts of row B.
+        auto load_starts = [&](int p) -> unsigned long long {
+            const int dk = (l16 >> 1) & 1, dj = l16 & 1;
+            const bool hasZp = p + 1 < g.ke;
+            bool ok = row_ok && l16 < 6;
+            if (l16 < 4) ok = ok && (dj == 0 || hasY) && (dk == 0 || hasZp);
+            if (l16 == 5) ok = ok && hasY;
+            if (!ok) return 0ull;
+            const long long rA = (long long)(p - g.kr) * g.ny + j;
+            if (l16 == 5) {
+                const uint2 c = __ldg(reinterpret_cast<const uint2*>(&rowcnt[rA + 1]));
+                return (unsigned long long)c.x + c.y;
             }
-        }
-        __syncwarp();
+            const long long r = l16 < 4 ? rA + (long long)dk * g.ny + dj : rA;
+            return rs.get(r, l16 < 4 ? 0 : 1);
+        };
 
-        // ---- vertex records of grid row (j, k): the x, y, z cuts its word owns
-        if (in) {
-            auto records = [&](uint32_t mk, uint32_t first, uint32_t axis) {
-                unsigned long long idx = xs0 + first - vbase;
-                while (mk != 0u) {
-                    put_vertex_record(points, idx, (uint32_t)(32 * l16 + __ffs(mk) - 1), axis, (uint32_t)j,
-                                      (uint32_t)k);
-                    mk &= mk - 1u;
-                    ++idx;
+        uint32_t wA = 0, wB = 0, wC = 0, wD = 0;
+        load_words(kb, wA, wB);
+        load_words(kb + 1, wC, wD);
+        unsigned long long st = load_starts(kb);
+
+        for (int k = kb; k < ke; ++k) {
+            const bool hasZ = k + 1 < g.nz;
+            // the next step's words and starts, in flight while this step runs
+            uint32_t nC = 0, nD = 0;
+            unsigned long long nst = 0;
+            if (k + 1 < ke) {
+                load_words(k + 2, nC, nD);
+                nst = load_starts(k + 1);
+            }
+            const bool cellrow = hasY && hasZ;
+            RowWords rw;
+            rw.a = wA;
+            rw.b = wB;
+            rw.c = hasZ ? wC : 0u;
+            rw.d = cellrow ? wD : 0u;
+            const uint32_t an = __shfl_down_sync(0xffffffffu, rw.a, 1, 16);
+            const uint32_t bn = __shfl_down_sync(0xffffffffu, rw.b, 1, 16);
+            const uint32_t cn = __shfl_down_sync(0xffffffffu, rw.c, 1, 16);
+            const uint32_t dn = __shfl_down_sync(0xffffffffu, rw.d, 1, 16);
+            rw.ash = (rw.a >> 1) | ((in1 ? an : 0u) << 31);
+            rw.bsh = (rw.b >> 1) | ((in1 ? bn : 0u) << 31);
+            rw.csh = (rw.c >> 1) | ((in1 ? cn : 0u) << 31);
+            rw.dsh = (rw.d >> 1) | ((in1 ? dn : 0u) << 31);
+            const CutMasks m = cut_masks(rw, evalid, pvalid, hasY, hasZ);
+            // popc prefixes within each half, two 16-bit counts per scan
+            const uint32_t p0 = __popc(m.xA) | (__popc(m.xB) << 16);
+            const uint32_t p1 = __popc(m.xC) | (__popc(m.xD) << 16);
+            const uint32_t p2 = __popc(m.yA) | (__popc(m.yC) << 16);
+            const uint32_t p3 = __popc(m.zA) | (__popc(m.zB) << 16);
+            const uint32_t i0 = half_incl_scan(p0, l16), i1 = half_incl_scan(p1, l16);
+            const uint32_t i2 = half_incl_scan(p2, l16), i3 = half_incl_scan(p3, l16);
+            const uint32_t e0 = i0 - p0, e1 = i1 - p1, e2 = i2 - p2, e3 = i3 - p3;
+            const uint32_t t0 = __shfl_sync(0xffffffffu, i0, 15, 16), t2 = __shfl_sync(0xffffffffu, i2, 15, 16);
+            const uint32_t t1 = __shfl_sync(0xffffffffu, i1, 15, 16), t3 = __shfl_sync(0xffffffffu, i3, 15, 16);
+            const unsigned long long xsA = __shfl_sync(0xffffffffu, st, 0, 16);  // this half's row
+            const unsigned long long xs0 = __shfl_sync(0xffffffffu, st, 0);      // row jw: the step's numbering
+            const uint32_t dB = (uint32_t)(__shfl_sync(0xffffffffu, st, 1, 16) - xsA);
+            const uint32_t dC = (uint32_t)(__shfl_sync(0xffffffffu, st, 2, 16) - xsA);
+            const uint32_t dD = (uint32_t)(__shfl_sync(0xffffffffu, st, 3, 16) - xsA);
+            const uint32_t cntB = (uint32_t)__shfl_sync(0xffffffffu, st, 5, 16);
+            const unsigned long long ts0 = __shfl_sync(0xffffffffu, st, 4);  // first triangle of cell row jw
+            const uint32_t nxA = t0 & 0xffffu, nyA = t2 & 0xffffu, nxC = t1 & 0xffffu;
+            const uint32_t off = (uint32_t)(xsA - xs0);  // 0, or the vertices of row jw
+            if (in) {  // first ids of the word's cut edges, relative to xs0
+                mbh[0 * W + l16] = make_uint2(m.xA, off + (e0 & 0xffffu));
+                mbh[1 * W + l16] = make_uint2(m.xB, off + dB + (e0 >> 16));
+                mbh[2 * W + l16] = make_uint2(m.xC, off + dC + (e1 & 0xffffu));
+                mbh[3 * W + l16] = make_uint2(m.xD, off + dD + (e1 >> 16));
+                mbh[4 * W + l16] = make_uint2(m.yA, off + nxA + (e2 & 0xffffu));
+                mbh[5 * W + l16] = make_uint2(m.yC, off + dC + nxC + (e2 >> 16));
+                mbh[6 * W + l16] = make_uint2(m.zA, off + nxA + nyA + (e3 & 0xffffu));
+                mbh[7 * W + l16] = make_uint2(m.zB, off + dB + cntB + (e3 >> 16));
+                if (cellrow) {  // corner order of the cube case: bit v = corner v
+                    uint4* t = reinterpret_cast<uint4*>(rwth + 8 * l16);
+                    t[0] = make_uint4(rw.a, rw.ash, rw.bsh, rw.b);
+                    t[1] = make_uint4(rw.c, rw.csh, rw.dsh, rw.d);
                 }
-            };
-            records(m.xA, off + (e0 & 0xffffu), 0u);
-            records(m.yA, off + nxA + (e2 & 0xffffu), 1u);
-            records(m.zA, off + nxA + nyA + (e3 & 0xffffu), 2u);
-        }
+            }
+            __syncwarp();
 
-        // ---- active cells of cell rows (jw, k) and (jw+1, k), compacted 32 at a time
-        uint32_t rem = (in && cellrow) ? active_cells(rw, evalid) : 0u;
-        const uint32_t na = __popc(rem);
-        const uint32_t ia = warp_incl_scan(na, lane);  // the cells of row jw come first
-        uint32_t rank = ia - na;
-        const uint32_t tot = __shfl_sync(0xffffffffu, ia, 31);
-        unsigned long long tcur = ts0;
-        for (uint32_t c0 = 0; c0 < tot; c0 += kGenCells) {
-            while (rem != 0u && rank < c0 + kGenCells) {
-                cell[rank - c0] = (uint32_t)(32 * l16 + __ffs(rem) - 1) | ((uint32_t)h << 9);
-                rem &= rem - 1u;
-                ++rank;
+            // ---- vertex records of grid row (j, k): the x, y, z cuts its word owns
+            if (in) {
+                auto records = [&](uint32_t mk, uint32_t first, uint32_t axis) {
+                    unsigned long long idx = xs0 + first - vbase;
+                    while (mk != 0u) {
+                        put_vertex_record(points, idx, (uint32_t)(32 * l16 + __ffs(mk) - 1), axis, (uint32_t)j,
+                                          (uint32_t)k);
+                        mk &= mk - 1u;
+                        ++idx;
+                    }
+                };
+                records(m.xA, off + (e0 & 0xffffu), 0u);
+                records(m.yA, off + nxA + (e2 & 0xffffu), 1u);
+                records(m.zA, off + nxA + nyA + (e3 & 0xffffu), 2u);
             }
-            __syncwarp();
-            const uint32_t nc = min(tot - c0, (uint32_t)kGenCells);
-            const bool live = (uint32_t)lane < nc;
-            uint32_t rec = 0u;
-            if (live) {  // the cell's cube case from its word's row words
-                const uint32_t ch = cell[lane];
-                const uint32_t ci = ch & 511u;
-                const uint4* t = reinterpret_cast<const uint4*>(rwt + (ch >> 9) * 8 * W + 8 * (ci >> 5));
-                const uint4 lo4 = t[0], hi4 = t[1];
-                const int b = (int)(ci & 31u);
-                const uint32_t cs = ((lo4.x >> b) & 1u) | (((lo4.y >> b) & 1u) << 1) | (((lo4.z >> b) & 1u) << 2) |
-                                    (((lo4.w >> b) & 1u) << 3) | (((hi4.x >> b) & 1u) << 4) |
-                                    (((hi4.y >> b) & 1u) << 5) | (((hi4.z >> b) & 1u) << 6) |
-                                    (((hi4.w >> b) & 1u) << 7);
-                rec = ch | (cs << 16);
-                cell[lane] = rec;
-            }
-            const int cs = (int)(rec >> 16);
-            const uint32_t nt = live ? (uint32_t)iso_case_ntris(s_tris[cs]) : 0u;
-            const uint32_t it = warp_incl_scan(nt, lane);
-            const uint32_t ntb = __shfl_sync(0xffffffffu, it, 31);
-            for (uint32_t q = 0; q < nt; ++q) list[it - nt + q] = (unsigned char)(lane | (q << 5));
-            __syncwarp();
-            for (uint32_t tb = 0; tb < ntb; tb += 32) {
-                const uint32_t t = tb + lane;
-                if (t < ntb) {
-                    const uint32_t tr = list[t];
-                    const uint32_t cr = cell[tr & 31u];
-                    const int q = (int)(tr >> 5);
-                    const int ci = (int)(cr & 511u);
-                    const uint2* mbc = mb + ((cr >> 9) & 1u) * 8 * W;
-                    const uint64_t tl = s_tris[cr >> 16];
-                    const int w = ci >> 5, bit = ci & 31;
-                    IndexT* o = tris + 3 * (tcur + t - tbase);
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) {
-                        const int e = iso_case_edge(tl, 3 * q + c);
-                        o[c] = (IndexT)(xs0 + fe_edge_rel(mbc, W, e, w, bit));
+
+            // ---- active cells of cell rows (jw, k) and (jw+1, k), compacted 32 at a time
+            uint32_t rem = (in && cellrow) ? active_cells(rw, evalid) : 0u;
+            const uint32_t na = __popc(rem);
+            const uint32_t ia = warp_incl_scan(na, lane);  // the cells of row jw come first
+            uint32_t rank = ia - na;
+            const uint32_t tot = __shfl_sync(0xffffffffu, ia, 31);
+            unsigned long long tcur = ts0;
+            for (uint32_t c0 = 0; c0 < tot; c0 += kGenCells) {
+                while (rem != 0u && rank < c0 + kGenCells) {
+                    cell[rank - c0] = (uint32_t)(32 * l16 + __ffs(rem) - 1) | ((uint32_t)h << 9);
+                    rem &= rem - 1u;
+                    ++rank;
+                }
+                __syncwarp();
+                const uint32_t nc = min(tot - c0, (uint32_t)kGenCells);
+                const bool live = (uint32_t)lane < nc;
+                uint32_t rec = 0u;
+                if (live) {  // the cell's cube case from its word's row words
+                    const uint32_t ch = cell[lane];
+                    const uint32_t ci = ch & 511u;
+                    const uint4* t = reinterpret_cast<const uint4*>(rwt + (ch >> 9) * 8 * W + 8 * (ci >> 5));
+                    const uint4 lo4 = t[0], hi4 = t[1];
+                    const int b = (int)(ci & 31u);
+                    const uint32_t cs = ((lo4.x >> b) & 1u) | (((lo4.y >> b) & 1u) << 1) | (((lo4.z >> b) & 1u) << 2) |
+                                        (((lo4.w >> b) & 1u) << 3) | (((hi4.x >> b) & 1u) << 4) |
+                                        (((hi4.y >> b) & 1u) << 5) | (((hi4.z >> b) & 1u) << 6) |
+                                        (((hi4.w >> b) & 1u) << 7);
+                    rec = ch | (cs << 16);
+                    cell[lane] = rec;
+                }
+                const int cs = (int)(rec >> 16);
+                const uint32_t nt = live ? (uint32_t)iso_case_ntris(s_tris[cs]) : 0u;
+                const uint32_t it = warp_incl_scan(nt, lane);
+                const uint32_t ntb = __shfl_sync(0xffffffffu, it, 31);
+                for (uint32_t q = 0; q < nt; ++q) list[it - nt + q] = (unsigned char)(lane | (q << 5));
+                __syncwarp();
+                for (uint32_t tb = 0; tb < ntb; tb += 32) {
+                    const uint32_t t = tb + lane;
+                    if (t < ntb) {
+                        const uint32_t tr = list[t];
+                        const uint32_t cr = cell[tr & 31u];
+                        const int q = (int)(tr >> 5);
+                        const int ci = (int)(cr & 511u);
+                        const uint2* mbc = mb + ((cr >> 9) & 1u) * 8 * W;
+                        const uint64_t tl = s_tris[cr >> 16];
+                        const int w = ci >> 5, bit = ci & 31;
+                        IndexT* o = tris + 3 * (tcur + t - tbase);
+    #pragma unroll
+                        for (int c = 0; c < 3; ++c) {
+                            const int e = iso_case_edge(tl, 3 * q + c);
+                            o[c] = (IndexT)(xs0 + fe_edge_rel(mbc, W, e, w, bit));
+                        }
                     }
                 }
+                tcur += ntb;
+                __syncwarp();  // the next batch overwrites the lists
             }
-            tcur += ntb;
-            __syncwarp();  // the next batch overwrites the lists
+            __syncwarp();  // the next step overwrites mb
+            wA = wC;
+            wB = wD;
+            wC = nC;
+            wD = nD;
+            st = nst;
         }
-        __syncwarp();  // the next step overwrites mb
-        wA = wC;
-        wB = wD;
-        wC = nC;
-        wD = nD;
-        st = nst;
     }
-}
-
-// Columns of KC planes over [p.kbeg, p.kend) for blocks of kGenPairRows
-// rows: about two waves of resident CTAs, at least 4 planes per column.
-inline void gen_pairs_split(GenPlan& p, const Grid& g, int nsm)
-{
-    p.nyb = (g.ny + kGenPairRows - 1) / kGenPairRows;
-    const int nzw = p.kend - p.kbeg;
-    const long long resident = (long long)nsm * kGenPairCtasPerSm;
-    int nkc = (int)((2 * resident + p.nyb - 1) / p.nyb);
-    if (nkc < 1) nkc = 1;
-    p.KC = (nzw + nkc - 1) / nkc;
-    if (p.KC < 4) p.KC = 4;
-    if (p.KC > nzw) p.KC = nzw;
-    if (p.KC < 1) p.KC = 1;
-    p.nkc = nzw > 0 ? (nzw + p.KC - 1) / p.KC : 0;
 }
 
 template <typename IndexT>
 void launch_gen_pairs_impl(const float* vol, const Grid& g, float iso, const CaseTables* cases, const FeBuffers& b,
-                           const CountPlan& cp, const GenPlan& plan, int nsm, long long capV, long long capT,
+                           const CountPlan& cp, const GenPlan& p, int nsm, long long capV, long long capT,
                            float* points, float* normals, IndexT* tris, int reverse, cudaStream_t s)
 {
-    GenPlan p = plan;
-    gen_pairs_split(p, g, nsm);
-    if (p.nkc == 0) return;
+    const int nzw = p.kend - p.kbeg;
+    if (nzw <= 0) return;
+    // items of KC planes: about four per warp of one wave, at least 4 planes
+    const long long npairs = (g.ny + 1) / 2;
+    const long long warps = (long long)nsm * kGenPairCtasPerSm * kGenRows;
+    long long KC = (npairs * nzw + 4 * warps - 1) / (4 * warps);
+    if (KC < 4) KC = 4;
+    while (npairs * ((nzw + KC - 1) / KC) >= (1ll << 31)) KC *= 2;  // item numbers stay below 2^31
+    if (KC > nzw) KC = nzw;
+    const int nkc = (int)((nzw + KC - 1) / KC);
+    const long long nitems = npairs * nkc;
+    long long blocks = (nitems + kGenRows - 1) / kGenRows;
+    if (blocks > (long long)nsm * kGenPairCtasPerSm) blocks = (long long)nsm * kGenPairCtasPerSm;
     RowStarts rs = row_starts(g, cp, b);
     for (int a = 0; a < 3; ++a) rs.add[a] = p.add[a];
-    const unsigned blocks = (unsigned)(p.nyb * p.nkc);
+    unsigned int* work = reinterpret_cast<unsigned int*>(b.totals + 7);
+    cudaMemsetAsync(work, 0, sizeof(unsigned int), s);
     const int ws_bytes = (int)gen_pair_scratch_bytes(g.W);
     const size_t smem = (size_t)kGenRows * ws_bytes;
     auto kern = k_gen_pairs<IndexT>;
     allow_smem(kern, smem);
-    const GradScale gs = make_grad_scale(g);
-    kern<<<blocks, kThreads, smem, s>>>(vol, b.bits, g, gs, iso, p.KC, p.nyb, p.kbeg, p.kend, p.vbase, p.tbase,
-                                        ws_bytes, cases, b.rowcnt, rs, b.totals, capV, capT, points, normals, tris,
-                                        reverse);
-    k_fe_vertices<<<(unsigned)nsm * 8, kThreads, 0, s>>>(vol, g, gs, iso, p.kbeg, p.kend, b.starts, b.totals, capV,
-                                                         capT, points, normals);
+    kern<<<(unsigned)blocks, kThreads, smem, s>>>(b.bits, g, (int)KC, (int)npairs, nkc, p.kbeg, p.kend, p.vbase,
+                                                  p.tbase, ws_bytes, cases, b.rowcnt, rs, b.totals, work, capV, capT,
+                                                  points, tris, reverse);
+    k_fe_vertices<<<(unsigned)nsm * kFeVertexCtasPerSm, kThreads, 0, s>>>(vol, g, make_grad_scale(g), iso, p.kbeg,
+                                                                          p.kend, b.starts, b.totals, capV, capT,
+                                                                          points, normals);
 }
 
 }  // namespace iso

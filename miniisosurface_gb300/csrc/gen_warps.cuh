@@ -287,7 +287,6 @@ __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
     unsigned long long* __restrict__ totals, long long capV, long long capT, float* __restrict__ points,
     float* __restrict__ normals, IndexT* __restrict__ tris, uint32_t* __restrict__ fe2mc, int reverse)
 {
-    constexpr bool VOL = MODE != kGenTri;
     extern __shared__ __align__(16) unsigned char s_raw[];
     constexpr bool OWNED = MODE == kGenMC || MODE == kGenDup;  // vertices computed by their owner cell
     __shared__ uint64_t s_tris[MODE == kGenMC ? 1 : 256];
