@@ -13,7 +13,10 @@ One step = one full extraction (passes 1-4) of the volume.
             recorded between kernels on the extraction stream during the
             timed region; algorithmic bytes per launch:
               count          4 N                 (volume read; passes 1+2 fused)
-              fe_generate    4 N + 24 V + 12 T   (volume read, points+normals, uint32 triangles)
+              fe_generate    12 T                (uint32 triangles; with fe_vertices)
+                             4 N + 24 V + 12 T   (volume read, points+normals, triangles; alone)
+              fe_vertices    4 N + 24 V          (pass-4 volume read, points+normals)
+            intermediates (bit rows, counts, vertex records) count nothing;
             the whole extraction is B = 8 N + 24 V + 12 T
   cpu_baseline  the oracle port of the reference's OpenMP Flying Edges on
             all host cores, full volume, repeated for a bounded time.
@@ -316,8 +319,9 @@ def main():
     if dist:
         dist.barrier()
     lib.iso_ctx_profile(ctx.handle, 0)
-    ms_pass = (C.c_double * 6)()
-    n_pass = (C.c_int64 * 6)()
+    npass = len(_lib.PASS_NAMES)
+    ms_pass = (C.c_double * npass)()
+    n_pass = (C.c_int64 * npass)()
     _lib.check(lib.iso_ctx_profile_read(ctx.handle, ms_pass, n_pass), ctx.handle)
     ms = e0.elapsed_time(e1)
 
@@ -391,8 +395,10 @@ def main():
         names = _lib.PASS_NAMES
         per = {names[p]: {"ms_total": ms_pass[p], "launches": int(n_pass[p]),
                           "us_per_launch": 1e3 * ms_pass[p] / n_pass[p] if n_pass[p] else None}
-               for p in range(6) if n_pass[p]}
-        alg_bytes = {"classify": 4 * N, "count": 4 * N, "scan": 0, "fe_generate": 4 * N + 24 * V + 12 * T,
+               for p in range(npass) if n_pass[p]}
+        split = "fe_vertices" in per  # pass 4 as generate (triangles, vertex records) + vertices
+        alg_bytes = {"classify": 4 * N, "count": 4 * N, "scan": 0,
+                     "fe_generate": 12 * T if split else 4 * N + 24 * V + 12 * T, "fe_vertices": 4 * N + 24 * V,
                      "mc_vertices": 4 * N + 24 * V, "mc_triangles": 12 * T}
         dom = max(per, key=lambda k: per[k]["ms_total"])
         dom_s = per[dom]["us_per_launch"] * 1e-6
@@ -423,7 +429,7 @@ def main():
                           "ms_per_step": 1e3 * e2e16_s / args.e2e_steps,
                           "link": link_floor(rates, 2 * N, 24 * V16 + 12 * T16, 1e3 * e2e16_s / args.e2e_steps)},
             # count + scan + row starts + generate per step (scan/row starts share one mark)
-            "gpu_launches": int(sum(n_pass[p] for p in range(6)) + n_pass[2]),
+            "gpu_launches": int(sum(n_pass[p] for p in range(npass)) + n_pass[2]),
             "clocks": clk,
         }
         if not args.no_cpu_baseline:

@@ -115,7 +115,8 @@ enum {
     ISO_PASS_FE_GENERATE = 3,  /* pass 4, Flying Edges */
     ISO_PASS_MC_VERTICES = 4,  /* pass 4, Marching Cubes vertices */
     ISO_PASS_MC_TRIANGLES = 5, /* pass 4, Marching Cubes triangles */
-    ISO_NUM_PASSES = 6
+    ISO_PASS_FE_VERTICES = 6,  /* pass 4, Flying Edges vertices (rows of up to 512 points) */
+    ISO_NUM_PASSES = 7
 };
 iso_status iso_ctx_profile(iso_ctx* ctx, int enable);
 iso_status iso_ctx_profile_read(iso_ctx* ctx, double* ms, int64_t* launches);

@@ -327,6 +327,10 @@ void enqueue_generate(iso_ctx* ctx, iso_algorithm algo, const float* vol, const 
             else
                 iso::launch_fe_gen_warps<uint64_t>(vol, g, iso, ctx->d_cases, b, pl.cp, pl.gp, capV, capT, out->points,
                                                    out->normals, static_cast<uint64_t*>(out->tris), ctx->reverse, s);
+            pm.mark(ISO_PASS_FE_GENERATE);
+            if (iso::launch_fe_vertices(vol, g, iso, b, pl.gp, capV, capT, out->points, out->normals, s))
+                pm.mark(ISO_PASS_FE_VERTICES);
+            return;
         } else {
             if (i4)
                 iso::launch_fe_gen_rows<uint32_t>(vol, g, iso, ctx->d_cases, b, pl.cp, capV, capT, out->points, out->normals,
@@ -493,6 +497,8 @@ iso_status slab_generate(iso_ctx* ctx, iso_algorithm algo, const float* volume, 
             iso::launch_fe_gen_warps<uint64_t>(volume, g, isoval, ctx->d_cases, b, pl.cp, gp, big, big, out->points,
                                                out->normals, static_cast<uint64_t*>(out->tris), ctx->reverse, s);
         pm.mark(ISO_PASS_FE_GENERATE);
+        if (iso::launch_fe_vertices(volume, g, isoval, b, gp, big, big, out->points, out->normals, s))
+            pm.mark(ISO_PASS_FE_VERTICES);
     } else {
         gp.kbeg = g.kr;  // cell row k0-1 maps the edges it owns on plane k0
         gp.kend = (int)k1;

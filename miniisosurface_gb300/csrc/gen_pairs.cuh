@@ -379,6 +379,13 @@ void launch_gen_pairs_impl(const float* vol, const Grid& g, float iso, const Cas
     kern<<<(unsigned)blocks, kThreads, smem, s>>>(b.bits, g, (int)KC, (int)npairs, nkc, p.kbeg, p.kend, p.vbase,
                                                   p.tbase, ws_bytes, cases, b.rowcnt, rs, b.totals, work, capV, capT,
                                                   points, tris, reverse);
+}
+
+inline void launch_fe_vertices_impl(const float* vol, const Grid& g, float iso, const FeBuffers& b, const GenPlan& p,
+                                    int nsm, long long capV, long long capT, float* points, float* normals,
+                                    cudaStream_t s)
+{
+    if (p.kend <= p.kbeg) return;
     k_fe_vertices<<<(unsigned)nsm * kFeVertexCtasPerSm, kThreads, 0, s>>>(vol, g, make_grad_scale(g), iso, p.kbeg,
                                                                           p.kend, b.starts, b.totals, capV, capT,
                                                                           points, normals);

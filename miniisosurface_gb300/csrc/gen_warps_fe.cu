@@ -40,17 +40,31 @@ GenPlan gen_plan(const Grid& g, int nsm)
     return p;
 }
 
+// Grids whose pass 4 runs as k_gen_pairs + k_fe_vertices.
+static bool fe_writes_records(const Grid& g, const GenPlan& p)
+{
+    return g.W <= 16 && p.nsm > 0;
+}
+
 template <typename IndexT>
 void launch_fe_gen_warps(const float* vol, const Grid& g, float iso, const CaseTables* cases, const FeBuffers& b,
                          const CountPlan& cp, const GenPlan& p, long long capV, long long capT, float* points,
                          float* normals, IndexT* tris, int reverse, cudaStream_t s)
 {
-    if (g.W <= 16 && p.nsm > 0)  // two rows per warp
+    if (fe_writes_records(g, p))  // two rows per warp
         launch_gen_pairs_impl<IndexT>(vol, g, iso, cases, b, cp, p, p.nsm, capV, capT, points, normals, tris,
                                       reverse, s);
     else
         launch_gen_warps_impl<kGenFE, IndexT>(vol, g, iso, cases, b, cp, p, capV, capT, points, normals, tris,
                                               reverse, s);
+}
+
+bool launch_fe_vertices(const float* vol, const Grid& g, float iso, const FeBuffers& b, const GenPlan& p,
+                        long long capV, long long capT, float* points, float* normals, cudaStream_t s)
+{
+    if (!fe_writes_records(g, p)) return false;
+    launch_fe_vertices_impl(vol, g, iso, b, p, p.nsm, capV, capT, points, normals, s);
+    return true;
 }
 
 template void launch_fe_gen_warps<uint32_t>(const float*, const Grid&, float, const CaseTables*, const FeBuffers&,

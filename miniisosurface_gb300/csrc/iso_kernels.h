@@ -77,11 +77,15 @@ void launch_grid_edges(const Grid& g, const CountPlan& p, const FeBuffers& b, in
 // Row-start accessor of a counted extraction.
 RowStarts row_starts(const Grid& g, const CountPlan& p, const FeBuffers& b);
 
-// pass 4, warp per row (volume slabs staged in shared memory)
+// pass 4, Flying Edges: rows of up to 16 words two per warp, writing vertex
+// records that launch_fe_vertices turns into vertices (it returns false, and
+// launches nothing, for the grids whose generate pass computes them itself)
 template <typename IndexT>
 void launch_fe_gen_warps(const float* vol, const Grid& g, float iso, const CaseTables* cases, const FeBuffers& b,
                          const CountPlan& cp, const GenPlan& p, long long capV, long long capT, float* points,
                          float* normals, IndexT* tris, int reverse, cudaStream_t s);
+bool launch_fe_vertices(const float* vol, const Grid& g, float iso, const FeBuffers& b, const GenPlan& p,
+                        long long capV, long long capT, float* points, float* normals, cudaStream_t s);
 void launch_mc_gen_warps(const float* vol, const Grid& g, float iso, const CaseTables* cases, const FeBuffers& b,
                          const CountPlan& cp, const GenPlan& p, long long capV, long long capT, float* points,
                          float* normals, int reverse, cudaStream_t s);
