@@ -144,7 +144,9 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
     IndexT* __restrict__ tris, int reverse)
 {
     extern __shared__ __align__(16) unsigned char s_raw[];
-    __shared__ uint64_t s_tris[256];
+    // per case: each triangle corner as the nibble (edge-id table row | point offset << 3) of fe_edge_rel,
+    // the triangle count in bits 60..63 (the packed triangle list with edges replaced)
+    __shared__ uint64_t s_tri[256];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, h = lane >> 4, l16 = lane & 15;
     const int W = g.W;
     unsigned char* ws = s_raw + (size_t)warp * ws_bytes;
@@ -152,7 +154,16 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
     uint32_t* rwt = reinterpret_cast<uint32_t*>(ws + (size_t)2 * 8 * W * 8);  // [2][W][8]
     uint32_t* cell = rwt + 2 * 8 * W;
     unsigned char* list = reinterpret_cast<unsigned char*>(cell + kGenCells);
-    for (int c = tid; c < 256; c += kThreads) s_tris[c] = cases->tris[c];
+    for (int c = tid; c < 256; c += kThreads) {
+        const uint64_t w = cases->tris[c];
+        uint64_t x = w & (0xfull << 60);
+        for (int q = 0; q < 15; ++q) {
+            const int e = (int)((w >> (4 * q)) & 15u);
+            const uint64_t nib = e < 12 ? (((0x776653524140ull >> (4 * e)) & 7u) | (((0xA22u >> e) & 1u) << 3)) : 0u;
+            x |= nib << (4 * q);
+        }
+        s_tri[c] = x;
+    }
     __syncthreads();  // the only CTA barrier: from here on every warp runs alone
     if ((long long)totals[0] > capV || (long long)totals[1] > capT) return;  // caller grows buffers
 
@@ -314,7 +325,7 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
                     cell[lane] = rec;
                 }
                 const int cs = (int)(rec >> 16);
-                const uint32_t nt = live ? (uint32_t)iso_case_ntris(s_tris[cs]) : 0u;
+                const uint32_t nt = live ? (uint32_t)iso_case_ntris(s_tri[cs]) : 0u;
                 const uint32_t it = warp_incl_scan(nt, lane);
                 const uint32_t ntb = __shfl_sync(0xffffffffu, it, 31);
                 for (uint32_t q = 0; q < nt; ++q) list[it - nt + q] = (unsigned char)(lane | (q << 5));
@@ -326,14 +337,21 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
                         const uint32_t cr = cell[tr & 31u];
                         const int q = (int)(tr >> 5);
                         const int ci = (int)(cr & 511u);
-                        const uint2* mbc = mb + ((cr >> 9) & 1u) * 8 * W;
-                        const uint64_t tl = s_tris[cr >> 16];
-                        const int w = ci >> 5, bit = ci & 31;
+                        const uint2* mbc = mb + ((cr >> 9) & 1u) * 8 * W + (ci >> 5);
+                        const uint32_t corners = (uint32_t)(s_tri[cr >> 16] >> (12 * q)) & 0xfffu;
+                        const int bit = ci & 31;
                         IndexT* o = tris + 3 * (tcur + t - tbase);
-    #pragma unroll
-                        for (int c = 0; c < 3; ++c) {
-                            const int e = iso_case_edge(tl, 3 * q + c);
-                            o[c] = (IndexT)(xs0 + fe_edge_rel(mbc, W, e, w, bit));
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) {  // fe_edge_rel with its table row and offset precomputed
+                            const uint32_t nib = (corners >> (4 * c)) & 15u;
+                            const uint2 pm = mbc[(nib & 7u) * W];
+                            // popc of the mask's bits below bit + offset (the funnel shift clamps at 32)
+                            const int pos = bit + (int)(nib >> 3);
+                            const uint32_t rel = pm.y + __popc(__funnelshift_lc(0u, pm.x, 32 - pos));
+                            if constexpr (sizeof(IndexT) == 4)
+                                o[c] = (IndexT)((uint32_t)xs0 + rel);  // 32-bit ids: V < 2^32
+                            else
+                                o[c] = (IndexT)(xs0 + rel);
                         }
                     }
                 }
