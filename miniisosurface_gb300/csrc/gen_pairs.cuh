@@ -295,24 +295,29 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
             }
 
             // ---- active cells of cell rows (jw, k) and (jw+1, k), compacted 32 at a time
-            uint32_t rem = (in && cellrow) ? active_cells(rw, evalid) : 0u;
-            const uint32_t na = __popc(rem);
+            const uint32_t act = (in && cellrow) ? active_cells(rw, evalid) : 0u;
+            const uint32_t na = __popc(act);
             const uint32_t ia = warp_incl_scan(na, lane);  // the cells of row jw come first
-            uint32_t rank = ia - na;
             const uint32_t tot = __shfl_sync(0xffffffffu, ia, 31);
             unsigned long long tcur = ts0;
             for (uint32_t c0 = 0; c0 < tot; c0 += kGenCells) {
-                while (rem != 0u && rank < c0 + kGenCells) {
-                    cell[rank - c0] = (uint32_t)(32 * l16 + __ffs(rem) - 1) | ((uint32_t)h << 9);
-                    rem &= rem - 1u;
-                    ++rank;
+                // lane L takes active cell c0 + L: the first lane whose inclusive count passes it
+                // (a shuffle binary search over the lanes), then the bit by __fns
+                const uint32_t target = c0 + (uint32_t)lane;
+                int src = 0;
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1) {
+                    const uint32_t before = __shfl_sync(0xffffffffu, ia, (src + step - 1) & 31);
+                    if (before <= target) src += step;
                 }
-                __syncwarp();
+                const uint32_t srcact = __shfl_sync(0xffffffffu, act, src);
+                const uint32_t srcexc = __shfl_sync(0xffffffffu, ia - na, src);
                 const uint32_t nc = min(tot - c0, (uint32_t)kGenCells);
                 const bool live = (uint32_t)lane < nc;
                 uint32_t rec = 0u;
                 if (live) {  // the cell's cube case from its word's row words
-                    const uint32_t ch = cell[lane];
+                    const uint32_t ch = (uint32_t)(32 * (src & 15) + (int)__fns(srcact, 0, (int)(target - srcexc) + 1)) |
+                                        ((uint32_t)(src >> 4) << 9);
                     const uint32_t ci = ch & 511u;
                     const uint4* t = reinterpret_cast<const uint4*>(rwt + (ch >> 9) * 8 * W + 8 * (ci >> 5));
                     const uint4 lo4 = t[0], hi4 = t[1];
