@@ -1234,7 +1234,9 @@ iso_status iso_fe_pass1(iso_fe* fe)
     ISO_CUDA(ctx, cudaMalloc(&fe->scratch, scratch_size(g, pl.cp)));
     carve(fe->scratch, g, pl.cp, fe->buf);
     ISO_CUDA(ctx, cudaMemcpy(fe->d_volume, fe->host_volume, vbytes, cudaMemcpyHostToDevice));
-    iso::launch_count(fe->d_volume, g, fe->isoval, ctx->d_cases, false, pl.cp, fe->buf, 0);
+    iso::CountPlan cp = pl.cp;
+    cp.trims = true;  // the gridEdge records carry them
+    iso::launch_count(fe->d_volume, g, fe->isoval, ctx->d_cases, false, cp, fe->buf, 0);
     ISO_CUDA(ctx, cudaGetLastError());
     ISO_CUDA(ctx, cudaDeviceSynchronize());
     return ISO_OK;

@@ -104,9 +104,11 @@ struct RowCounts {
 
 // Counts of word w of grid row (j,k): cut x / y / z edges the row owns, the
 // trim candidates, the triangles (and MC vertices) of its cells.
+// trims: whether the row trims are wanted (only the pass-by-pass interface
+// reads them; an extraction skips them).
 template <bool MC>
 __device__ __forceinline__ void count_word(const RowWords& rw, int w, const Grid& g, int j, int k, bool hasY,
-                                           bool hasZ, RowCounts& rc)
+                                           bool hasZ, bool trims, RowCounts& rc)
 {
     const uint32_t evalid = validmask(w, g.nx - 1);  // x-edges / cells: i <= nx-2
     const uint32_t pvalid = validmask(w, g.nx);      // points: i <= nx-1
@@ -118,7 +120,7 @@ __device__ __forceinline__ void count_word(const RowWords& rw, int w, const Grid
     rc.zc += __popc(zm);
     // isCutEdge (FlyingEdgesAlgorithm.cpp:515-554): edge i is marked when
     // it is cut or the y / z edge at its left point is.
-    const uint32_t marked = xm | ((ym | zm) & evalid);
+    const uint32_t marked = trims ? (xm | ((ym | zm) & evalid)) : 0u;
     if (marked) {
         rc.first = min(rc.first, (uint32_t)(32 * w + __ffs(marked) - 1));
         rc.last = max(rc.last, (uint32_t)(32 * w + 32 - __clz(marked)));
@@ -141,11 +143,13 @@ __device__ __forceinline__ void finish_row(RowCounts& rc, int lane, long long r,
     rc.zc = __reduce_add_sync(0xffffffffu, rc.zc);
     rc.tc = __reduce_add_sync(0xffffffffu, rc.tc);
     if (MC) rc.mc = __reduce_add_sync(0xffffffffu, rc.mc);
-    rc.first = __reduce_min_sync(0xffffffffu, rc.first);
-    rc.last = __reduce_max_sync(0xffffffffu, rc.last);
+    if (trims) {
+        rc.first = __reduce_min_sync(0xffffffffu, rc.first);
+        rc.last = __reduce_max_sync(0xffffffffu, rc.last);
+    }
     if (lane == 0) {
         rowcnt[r] = make_uint4(rc.xc, rc.yc, rc.zc, rc.tc);
-        trims[r] = make_uint2(rc.first == 0xffffffffu ? (uint32_t)g.nx : rc.first, rc.last);
+        if (trims) trims[r] = make_uint2(rc.first == 0xffffffffu ? (uint32_t)g.nx : rc.first, rc.last);
         if (MC) mccnt[r] = rc.mc;
     }
 }
@@ -215,7 +219,7 @@ __global__ void __launch_bounds__(kThreads) k_count_warps(const float* __restric
             rw.bsh = (rw.b >> 1) | (next_word<NW>(B, q, lane) << 31);
             rw.csh = (rw.c >> 1) | (next_word<NW>(Cw, q, lane) << 31);
             rw.dsh = (rw.d >> 1) | (next_word<NW>(Dw, q, lane) << 31);
-            count_word<MC>(rw, w, g, j, k, hasY, hasZ, rc);
+            count_word<MC>(rw, w, g, j, k, hasY, hasZ, trims != nullptr, rc);
             if (w < g.W) bits_out[r * g.W + w] = rw.a;
         }
         finish_row<MC>(rc, lane, r, g, rowcnt, trims, mccnt);
@@ -348,7 +352,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_count_tma(const float* __restri
         rw.bsh = (rw.b >> 1) | ((nxt ? bn : 0u) << 31);
         rw.csh = (rw.c >> 1) | ((nxt ? cn : 0u) << 31);
         rw.dsh = (rw.d >> 1) | ((nxt ? dn : 0u) << 31);
-        if (row_ok) count_word<MC>(rw, l16, g, j, k, hasY, hasZ, rc);
+        if (row_ok) count_word<MC>(rw, l16, g, j, k, hasY, hasZ, trims != nullptr, rc);
         const long long r = (long long)(k - g.kr) * g.ny + j;
         if (row_ok && l16 < g.W) bits_out[r * g.W + l16] = rw.a;
         // both rows' totals at once: row h in bits 16h .. 16h+15 (each below 2^16)
@@ -358,15 +362,18 @@ __global__ void __launch_bounds__(kThreads, 4) k_count_tma(const float* __restri
         const uint32_t sz = __reduce_add_sync(0xffffffffu, rc.zc << sh);
         const uint32_t st = __reduce_add_sync(0xffffffffu, rc.tc << sh);
         const uint32_t sm = MC ? __reduce_add_sync(0xffffffffu, rc.mc << sh) : 0u;
-        const uint32_t f0 = __reduce_min_sync(0xffffffffu, h ? 0xffffffffu : rc.first);
-        const uint32_t f1 = __reduce_min_sync(0xffffffffu, h ? rc.first : 0xffffffffu);
-        const uint32_t x0 = __reduce_max_sync(0xffffffffu, h ? 0u : rc.last);
-        const uint32_t x1 = __reduce_max_sync(0xffffffffu, h ? rc.last : 0u);
+        uint32_t f0 = 0u, f1 = 0u, x0 = 0u, x1 = 0u;
+        if (trims) {
+            f0 = __reduce_min_sync(0xffffffffu, h ? 0xffffffffu : rc.first);
+            f1 = __reduce_min_sync(0xffffffffu, h ? rc.first : 0xffffffffu);
+            x0 = __reduce_max_sync(0xffffffffu, h ? 0u : rc.last);
+            x1 = __reduce_max_sync(0xffffffffu, h ? rc.last : 0u);
+        }
         if (row_ok && l16 == 0) {
             const uint32_t first = h ? f1 : f0, last = h ? x1 : x0;
             rowcnt[r] = make_uint4((sx >> sh) & 0xffffu, (sy >> sh) & 0xffffu, (sz >> sh) & 0xffffu,
                                    (st >> sh) & 0xffffu);
-            trims[r] = make_uint2(first == 0xffffffffu ? (uint32_t)g.nx : first, last);
+            if (trims) trims[r] = make_uint2(first == 0xffffffffu ? (uint32_t)g.nx : first, last);
             if (MC) mccnt[r] = (sm >> sh) & 0xffffu;
         }
         A = Cw;
@@ -431,7 +438,7 @@ __global__ void __launch_bounds__(kThreads) k_count_wide(const float* __restrict
             rw.csh = (rw.c >> 1) | ((lane < 31 ? dc : nc) << 31);
             rw.dsh = (rw.d >> 1) | ((lane < 31 ? dd : nd) << 31);
             const int w = 32 * c + lane;
-            count_word<MC>(rw, w, g, j, k, hasY, hasZ, rc);
+            count_word<MC>(rw, w, g, j, k, hasY, hasZ, trims != nullptr, rc);
             if (w < g.W) bits_out[r * g.W + w] = rw.a;
         }
         finish_row<MC>(rc, lane, r, g, rowcnt, trims, mccnt);
@@ -629,6 +636,7 @@ static void count_launch(const CountPlan& p, const float* vol, const Grid& g, fl
 {
     const unsigned blocks = (unsigned)(p.nyb * p.nkc);
     const bool vec4 = g.W <= 64 && (g.nx % 4 == 0) && ((reinterpret_cast<uintptr_t>(vol) & 15) == 0);
+    uint2* trims = p.trims ? b.trims : nullptr;  // the kernels skip the trims when null
     if (vec4 && g.W <= 16) {  // two rows per warp, planes through the TMA engine
         const int nyb2 = (g.ny + kPairRows - 1) / kPairRows;
         const unsigned blocks2 = (unsigned)(nyb2 * p.nkc);
@@ -638,7 +646,7 @@ static void count_launch(const CountPlan& p, const float* vol, const Grid& g, fl
     {                                                                                                          \
         auto kern = k_count_tma<MC, FULL>;                                                                    \
         allow_smem(kern, smem);                                                                                \
-        kern<<<blocks2, kThreads, smem, s>>>(vol, g, iso, p.KC, nyb2, b.rowcnt, b.trims, b.mccnt, b.bits,       \
+        kern<<<blocks2, kThreads, smem, s>>>(vol, g, iso, p.KC, nyb2, b.rowcnt, trims, b.mccnt, b.bits,         \
                                              b.totals + 3);                                                    \
     }
         if (nq == 128) ISO_TMA(true)
@@ -648,7 +656,7 @@ static void count_launch(const CountPlan& p, const float* vol, const Grid& g, fl
     }
 #define ISO_COUNT(VEC, UU, NWW)                                                                                \
     k_count_warps<MC, VEC, UU, NWW><<<blocks, kThreads, 0, s>>>(vol, g, iso, p.KC, p.nyb, cases, b.rowcnt,     \
-                                                                b.trims, b.mccnt, b.bits)
+                                                                trims, b.mccnt, b.bits)
     if (vec4) {
         switch (p.vec_u) {
             case 1: ISO_COUNT(true, 1, 1); break;
@@ -662,7 +670,7 @@ static void count_launch(const CountPlan& p, const float* vol, const Grid& g, fl
     } else if (g.W <= 64) {
         ISO_COUNT(false, 1, 2);
     } else {
-        k_count_wide<MC><<<blocks, kThreads, 0, s>>>(vol, g, iso, p.KC, p.nyb, cases, b.rowcnt, b.trims, b.mccnt,
+        k_count_wide<MC><<<blocks, kThreads, 0, s>>>(vol, g, iso, p.KC, p.nyb, cases, b.rowcnt, trims, b.mccnt,
                                                      b.bits);
     }
 #undef ISO_COUNT

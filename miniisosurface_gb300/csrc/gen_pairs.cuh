@@ -165,7 +165,10 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
         s_tri[c] = x;
     }
     __syncthreads();  // the only CTA barrier: from here on every warp runs alone
-    if ((long long)totals[0] > capV || (long long)totals[1] > capT) return;  // caller grows buffers
+    // Caller grows buffers.  Past this check every record slot and triangle index written below lies
+    // under the totals, because the count pass derives the counts and starts from the same bit words
+    // with the same masks (cut_masks, tris_of_word); the writes are not checked one by one.
+    if ((long long)totals[0] > capV || (long long)totals[1] > capT) return;
 
     const bool in1 = l16 + 1 < W;
     const uint32_t evalid = validmask(l16, g.nx - 1);  // x-edges / cells: i <= nx-2

@@ -30,6 +30,7 @@ struct CountPlan {
     int J = 8, nyb = 1, KC = 1, nkc = 1;
     int vec_u = 1;  // float4 loads per lane for one row (rows up to 64 words)
     int nseg = 1;
+    bool trims = false;  // write the row trims (only the pass-by-pass interface reads them)
 };
 
 // Work split of the warp-per-row generate kernels: blocks of J = 8 rows,
