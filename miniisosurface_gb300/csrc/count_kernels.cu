@@ -527,15 +527,22 @@ __global__ void __launch_bounds__(kThreads) k_scan_final(const uint4* __restrict
     __shared__ unsigned long long s_w[NC][kThreads / 32];
     __shared__ unsigned long long s_base[NC], s_tot[NC];
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    if (t < NC) {
+    if (warp < NC) {  // warp a: the segments before this one and all of them, for component a
         unsigned long long b = 0, tot = 0;
-        for (int q = 0; q < nseg; ++q) {
-            const unsigned long long x = part[t * nseg + q];
+        for (int q = lane; q < nseg; q += 32) {
+            const unsigned long long x = part[warp * nseg + q];
             if (q < (int)blockIdx.x) b += x;
             tot += x;
         }
-        s_base[t] = b;
-        s_tot[t] = tot;
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) {
+            b += __shfl_xor_sync(0xffffffffu, b, d);
+            tot += __shfl_xor_sync(0xffffffffu, tot, d);
+        }
+        if (lane == 0) {
+            s_base[warp] = b;
+            s_tot[warp] = tot;
+        }
     }
     const long long b = (long long)blockIdx.x * kSeg + (long long)t * kScanPer;
     uint32_t v[4][kScanPer];
