@@ -3,8 +3,8 @@
 // (cube cases, per-row counts):
 //
 //   k_count_tma    (rows up to 512 points, 16-byte aligned) a CTA owns a block
-//   k_count_warps  (up to 2048) of 16 grid rows (k_count_tma: a half-warp per
-//                  row) / 8 rows (k_count_warps: a warp per row) and a run of
+//   k_count_warps  (up to 2048) of 16 or 32 grid rows (k_count_tma: a half- or
+//                  quarter-warp per row) / 8 rows (k_count_warps: a warp per row) and a run of
 //                  KC planes and marches along z.  Each row's words of plane
 //                  k+1 are classified straight from the volume (plane k+2
 //                  already in flight: a TMA bulk copy into the warp's shared
@@ -231,11 +231,6 @@ __global__ void __launch_bounds__(kThreads) k_count_warps(const float* __restric
     }
 }
 
-// Rows of up to 16 words (nx <= 512): two rows per warp, one per half-warp
-// (lanes 16h .. 16h+15 hold words 0..15 of row j0 + 2*warp + h), so no lane
-// idles on words past the row.
-constexpr int kPairRows = 2 * kCountRows;  // grid rows per CTA
-
 // All ones when v >= iso, else zero (false for NaN; -0 >= +0), one ALU op.
 __device__ __forceinline__ uint32_t ge_mask(float v, float iso)
 {
@@ -269,30 +264,34 @@ __device__ __forceinline__ uint32_t row_word(const float* row, int nq, int l16, 
     return __funnelshift_l(w, w, 4 * (l16 & 7));
 }
 
-// Rows of up to 16 words (nx <= 512), 16-byte aligned, two per warp: the
-// counts of k_count_warps, with the volume brought in by the TMA bulk engine.  A warp's
-// two grid rows jw, jw+1 read rows jw .. jw+2 of every plane (A and B of both
-// half-warps), which lie next to each other in memory: one cp.async.bulk per
-// plane fills the warp's buffer of kTmaRows rows and completes on the warp's
-// mbarrier.  The words of plane k+1 are taken from the buffer before the copy
-// of plane k+2 is issued into it, so the copy runs while step k is counted;
-// no register holds raw values across a step.
-constexpr int kTmaRows = 3;
-
-template <bool MC, bool FULL>
+// Rows of up to 16 words (nx <= 512), 16-byte aligned, several per warp so
+// that no lane idles on words past a short row: the counts of k_count_warps,
+// with the volume brought in by the TMA bulk engine.  A warp's grid rows
+// jw .. jw+RPW-1 read rows jw .. jw+RPW of every plane (A and B of each
+// row's lanes), which lie next to each other in memory: one cp.async.bulk per
+// plane fills the warp's buffer and completes on the warp's mbarrier.  The
+// words of plane k+1 are taken from the buffer before the copy of plane k+2
+// is issued into it, so the copy runs while step k is counted; no register
+// holds raw values across a step.
+// RPW grid rows per warp (2: rows of up to 16 words, 4: up to 8), LPR =
+// 32 / RPW lanes per row; a warp's rows jw .. jw+RPW-1 read rows jw .. jw+RPW
+// of every plane, RPW + 1 rows of its buffer.  FULL: every lane's word is
+// inside the row (nx = 32 * LPR).
+template <bool MC, bool FULL, int RPW>
 __global__ void __launch_bounds__(kThreads, 4) k_count_tma(const float* __restrict__ vol, Grid g, float iso, int KC,
                                                         int nyb, uint4* __restrict__ rowcnt,
                                                         uint2* __restrict__ trims, uint32_t* __restrict__ mccnt,
                                                         uint32_t* __restrict__ bits_out,
                                                         unsigned long long* __restrict__ status)
 {
+    constexpr int LPR = 32 / RPW, NBUF = RPW + 1;
     extern __shared__ __align__(16) unsigned char s_raw[];
     __shared__ uint64_t s_bar[kCountRows];
     const int jb = blockIdx.x % nyb, kc = blockIdx.x / nyb;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, h = lane >> 4, l16 = lane & 15;
-    const int jw = jb * kPairRows + 2 * warp;
-    if (jw >= g.ny) return;  // both halves past the grid
-    float* buf = reinterpret_cast<float*>(s_raw) + (size_t)warp * kTmaRows * g.nx;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, h = lane / LPR, lw = lane % LPR;
+    const int jw = jb * kCountRows * RPW + RPW * warp;
+    if (jw >= g.ny) return;  // all the warp's rows past the grid
+    float* buf = reinterpret_cast<float*>(s_raw) + (size_t)warp * NBUF * g.nx;
     uint64_t* bar = &s_bar[warp];
     if (lane == 0) {
         mbar_init(bar, 1);
@@ -304,7 +303,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_count_tma(const float* __restri
     const int kb = g.kr + kc * KC, ke = min(kb + KC, g.ke);
     const bool hasY = row_ok && j < g.ny - 1;
     const int nq = g.nx >> 2;
-    const unsigned bytes = (unsigned)(min(kTmaRows, g.ny - jw) * g.nx * 4);
+    const unsigned bytes = (unsigned)(min(NBUF, g.ny - jw) * g.nx * 4);
 
     // plane p -> buffer (lane 0); earlier reads of the buffer are ordered
     // before the engine's writes by the caller's __syncwarp and the fence
@@ -321,10 +320,17 @@ __global__ void __launch_bounds__(kThreads, 4) k_count_tma(const float* __restri
         const bool done = mbar_wait(bar, phase);
         if (!__all_sync(0xffffffffu, done)) return false;
         phase ^= 1u;
-        wa = row_ok ? row_word<FULL>(buf + h * g.nx, nq, l16, iso) : 0u;
-        wb = hasY ? row_word<FULL>(buf + (h + 1) * g.nx, nq, l16, iso) : 0u;
+        wa = row_ok ? row_word<FULL>(buf + h * g.nx, nq, lw, iso) : 0u;
+        wb = hasY ? row_word<FULL>(buf + (h + 1) * g.nx, nq, lw, iso) : 0u;
         __syncwarp();  // every lane has read the buffer before it is refilled
         return true;
+    };
+    // per-row totals: rows 0,1 (and 2,3) of the warp in the two 16-bit halves of one reduction
+    auto row_sum = [&](uint32_t v) -> uint32_t {
+        const int sh = 16 * (h & 1);
+        const uint32_t lo = __reduce_add_sync(0xffffffffu, h < 2 ? v << sh : 0u);
+        const uint32_t hi = RPW > 2 ? __reduce_add_sync(0xffffffffu, h >= 2 ? v << sh : 0u) : 0u;
+        return ((h < 2 ? lo : hi) >> sh) & 0xffffu;
     };
 
     uint32_t A = 0, B = 0, Cw = 0, Dw = 0;
@@ -345,36 +351,36 @@ __global__ void __launch_bounds__(kThreads, 4) k_count_tma(const float* __restri
         rw.b = B;
         rw.c = Cw;
         rw.d = Dw;
-        const uint32_t an = __shfl_down_sync(0xffffffffu, rw.a, 1, 16), bn = __shfl_down_sync(0xffffffffu, rw.b, 1, 16);
-        const uint32_t cn = __shfl_down_sync(0xffffffffu, rw.c, 1, 16), dn = __shfl_down_sync(0xffffffffu, rw.d, 1, 16);
-        const bool nxt = l16 < 15;
+        const uint32_t an = __shfl_down_sync(0xffffffffu, rw.a, 1, LPR);
+        const uint32_t bn = __shfl_down_sync(0xffffffffu, rw.b, 1, LPR);
+        const uint32_t cn = __shfl_down_sync(0xffffffffu, rw.c, 1, LPR);
+        const uint32_t dn = __shfl_down_sync(0xffffffffu, rw.d, 1, LPR);
+        const bool nxt = lw < LPR - 1;
         rw.ash = (rw.a >> 1) | ((nxt ? an : 0u) << 31);
         rw.bsh = (rw.b >> 1) | ((nxt ? bn : 0u) << 31);
         rw.csh = (rw.c >> 1) | ((nxt ? cn : 0u) << 31);
         rw.dsh = (rw.d >> 1) | ((nxt ? dn : 0u) << 31);
-        if (row_ok) count_word<MC>(rw, l16, g, j, k, hasY, hasZ, trims != nullptr, rc);
+        if (row_ok) count_word<MC>(rw, lw, g, j, k, hasY, hasZ, trims != nullptr, rc);
         const long long r = (long long)(k - g.kr) * g.ny + j;
-        if (row_ok && l16 < g.W) bits_out[r * g.W + l16] = rw.a;
-        // both rows' totals at once: row h in bits 16h .. 16h+15 (each below 2^16)
-        const int sh = 16 * h;
-        const uint32_t sx = __reduce_add_sync(0xffffffffu, rc.xc << sh);
-        const uint32_t sy = __reduce_add_sync(0xffffffffu, rc.yc << sh);
-        const uint32_t sz = __reduce_add_sync(0xffffffffu, rc.zc << sh);
-        const uint32_t st = __reduce_add_sync(0xffffffffu, rc.tc << sh);
-        const uint32_t sm = MC ? __reduce_add_sync(0xffffffffu, rc.mc << sh) : 0u;
-        uint32_t f0 = 0u, f1 = 0u, x0 = 0u, x1 = 0u;
-        if (trims) {
-            f0 = __reduce_min_sync(0xffffffffu, h ? 0xffffffffu : rc.first);
-            f1 = __reduce_min_sync(0xffffffffu, h ? rc.first : 0xffffffffu);
-            x0 = __reduce_max_sync(0xffffffffu, h ? 0u : rc.last);
-            x1 = __reduce_max_sync(0xffffffffu, h ? rc.last : 0u);
+        if (row_ok && lw < g.W) bits_out[r * g.W + lw] = rw.a;
+        const uint32_t sx = row_sum(rc.xc), sy = row_sum(rc.yc), sz = row_sum(rc.zc), st = row_sum(rc.tc);
+        const uint32_t sm = MC ? row_sum(rc.mc) : 0u;
+        uint32_t first = 0u, last = 0u;
+        if (trims) {  // each row's own minimum and maximum, the other rows contributing the identity
+#pragma unroll
+            for (int q = 0; q < RPW; ++q) {
+                const uint32_t f = __reduce_min_sync(0xffffffffu, h == q ? rc.first : 0xffffffffu);
+                const uint32_t x = __reduce_max_sync(0xffffffffu, h == q ? rc.last : 0u);
+                if (h == q) {
+                    first = f;
+                    last = x;
+                }
+            }
         }
-        if (row_ok && l16 == 0) {
-            const uint32_t first = h ? f1 : f0, last = h ? x1 : x0;
-            rowcnt[r] = make_uint4((sx >> sh) & 0xffffu, (sy >> sh) & 0xffffu, (sz >> sh) & 0xffffu,
-                                   (st >> sh) & 0xffffu);
+        if (row_ok && lw == 0) {
+            rowcnt[r] = make_uint4(sx, sy, sz, st);
             if (trims) trims[r] = make_uint2(first == 0xffffffffu ? (uint32_t)g.nx : first, last);
-            if (MC) mccnt[r] = (sm >> sh) & 0xffffu;
+            if (MC) mccnt[r] = sm;
         }
         A = Cw;
         B = Dw;
@@ -644,20 +650,27 @@ static void count_launch(const CountPlan& p, const float* vol, const Grid& g, fl
     const unsigned blocks = (unsigned)(p.nyb * p.nkc);
     const bool vec4 = g.W <= 64 && (g.nx % 4 == 0) && ((reinterpret_cast<uintptr_t>(vol) & 15) == 0);
     uint2* trims = p.trims ? b.trims : nullptr;  // the kernels skip the trims when null
-    if (vec4 && g.W <= 16) {  // two rows per warp, planes through the TMA engine
-        const int nyb2 = (g.ny + kPairRows - 1) / kPairRows;
+    if (vec4 && g.W <= 16) {  // 4 rows per warp up to 8 words, else 2; planes through the TMA engine
+        const int rpw = g.W <= 8 ? 4 : 2;
+        const int rows = kCountRows * rpw;
+        const int nyb2 = (g.ny + rows - 1) / rows;
         const unsigned blocks2 = (unsigned)(nyb2 * p.nkc);
         const int nq = g.nx >> 2;
-        const size_t smem = (size_t)kCountRows * kTmaRows * g.nx * sizeof(float);
-#define ISO_TMA(FULL)                                                                                          \
+        const size_t smem = (size_t)kCountRows * (rpw + 1) * g.nx * sizeof(float);
+#define ISO_TMA(FULL, RPW)                                                                                     \
     {                                                                                                          \
-        auto kern = k_count_tma<MC, FULL>;                                                                    \
+        auto kern = k_count_tma<MC, FULL, RPW>;                                                               \
         allow_smem(kern, smem);                                                                                \
         kern<<<blocks2, kThreads, smem, s>>>(vol, g, iso, p.KC, nyb2, b.rowcnt, trims, b.mccnt, b.bits,         \
                                              b.totals + 3);                                                    \
     }
-        if (nq == 128) ISO_TMA(true)
-        else ISO_TMA(false)
+        if (rpw == 4) {
+            if (nq == 64) ISO_TMA(true, 4)
+            else ISO_TMA(false, 4)
+        } else {
+            if (nq == 128) ISO_TMA(true, 2)
+            else ISO_TMA(false, 2)
+        }
 #undef ISO_TMA
         return;
     }

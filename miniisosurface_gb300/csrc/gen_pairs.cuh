@@ -1,16 +1,21 @@
 // Flying Edges pass 4 (FlyingEdgesAlgorithm.cpp:271-500) for rows of up to
-// 16 words (nx <= 512), two grid rows per warp (included by gen_warps_fe.cu).
+// 16 words (nx <= 512), several grid rows per warp (included by
+// gen_warps_fe.cu): two for rows of 9-16 words, four for rows of up to 8, so
+// that no lane idles on words past a short row.
 //
-// Lanes 16h .. 16h+15 hold words 0..15 of grid row j = jw + h.  Rows (jw, k)
-// and (jw+1, k) are neighbours in the output order (rows in (k, j) order, the
-// reference's), so the step's vertices are one list -- those of row jw, then
-// those of row jw+1, numbered from the first vertex of row jw -- and so are
-// its triangles -- cell row jw, then jw+1, from the first triangle of cell row
-// jw.  Each step runs the phases of k_gen_warps once for both rows: the cut
-// masks, their 16-lane prefix scans and the edge-id tables (one per row), one
-// joint compaction of the active cells and one joint triangle list, so that
-// the fixed work of a step is shared by two rows and the batches fill from
-// both.
+// Lanes LPR*h .. LPR*h + LPR-1 (LPR = 32 / rows per warp) hold the words of
+// grid row j = jw + h.  Rows (jw, k), (jw+1, k), ... are neighbours in the
+// output order (rows in (k, j) order, the reference's), so the step's vertices
+// are one list -- those of row jw, then jw+1, ..., numbered from the first
+// vertex of row jw -- and so are its triangles -- cell row jw, then jw+1, ...,
+// from the first triangle of cell row jw.  Each step runs the phases of
+// k_gen_warps once for all the warp's rows: the cut masks, their per-row
+// prefix scans and the edge-id tables (one per row), then the active cells of
+// the rows 32 at a time and their triangles 32 at a time, so that the fixed
+// work of a step is shared and the batches fill from all rows.  Each cell lane
+// finds its cell by a shuffle binary search over the lanes' running counts:
+// no per-lane loop, which diverges where the active cells cluster along the
+// surface.
 //
 // The vertices are not computed here: each lane writes, for every cut edge its
 // word owns, a record (i, axis, j, k) into the first 8 bytes of the vertex's
@@ -22,14 +27,13 @@
 
 namespace iso {
 
-constexpr int kGenPairRows = 2 * kGenRows;  // grid rows per CTA
 constexpr int kGenPairCtasPerSm = 4;        // resident CTAs per SM the kernel is built for
 
-// Per-warp scratch: mb[2][8][W] uint2, rwt[2][W][8], cell[32], the batch's
-// triangle list (u8).
-__host__ __device__ inline size_t gen_pair_scratch_bytes(int W)
+// Per-warp scratch: mb[RPW][8][W] uint2, rwt[RPW][W][8], cell[32], the
+// batch's triangle list (u8).
+__host__ __device__ inline size_t gen_pair_scratch_bytes(int W, int RPW)
 {
-    return ((size_t)2 * 8 * W * 8 + (size_t)2 * 8 * W * 4 + kGenCells * 4 + kGenTris + 15) & ~(size_t)15;
+    return ((size_t)RPW * 8 * W * 8 + (size_t)RPW * 8 * W * 4 + kGenCells * 4 + kGenTris + 15) & ~(size_t)15;
 }
 
 // Vertex record in the first 8 bytes of a vertex's points slot: word 0 =
@@ -120,24 +124,15 @@ __global__ void __launch_bounds__(kThreads, kFeVertexCtasPerSm)
     }
 }
 
-// Inclusive scan within each 16-lane half of the warp.
-__device__ __forceinline__ uint32_t half_incl_scan(uint32_t v, int l16)
-{
-#pragma unroll
-    for (int d = 1; d < 16; d <<= 1) {
-        const uint32_t t = __shfl_up_sync(0xffffffffu, v, d, 16);
-        if (l16 >= d) v += t;
-    }
-    return v;
-}
-
-// One wave of CTAs; every warp takes work items -- a row pair and a run of KC
-// planes -- from the counter `work` until none is left, so no warp waits for
-// another and no CTA stays resident for its slowest warp.  Item q is row pair
-// q % npairs of plane run q / npairs (runs walked backwards when `reverse`).
-template <typename IndexT>
+// One wave of CTAs; every warp takes work items -- a group of RPW rows and a
+// run of KC planes -- from the counter `work` until none is left, so no warp
+// waits for another and no CTA stays resident for its slowest warp.  Item q is
+// row group q % ngroups of plane run q / ngroups (runs walked backwards when
+// `reverse`).  RPW = 2 for rows of up to 16 words, 4 for up to 8: lanes
+// LPR*h .. LPR*h + LPR-1 hold the words of row jw + h.
+template <typename IndexT, int RPW>
 __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
-    const uint32_t* __restrict__ bits, Grid g, int KC, int npairs, int nkc, int kbeg, int kend,
+    const uint32_t* __restrict__ bits, Grid g, int KC, int ngroups, int nkc, int kbeg, int kend,
     unsigned long long vbase, unsigned long long tbase, int ws_bytes, const CaseTables* __restrict__ cases,
     const uint4* __restrict__ rowcnt, RowStarts rs, const unsigned long long* __restrict__ totals,
     unsigned int* __restrict__ work, long long capV, long long capT, float* __restrict__ points,
@@ -147,12 +142,13 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
     // per case: each triangle corner as the nibble (edge-id table row | point offset << 3) of fe_edge_rel,
     // the triangle count in bits 60..63 (the packed triangle list with edges replaced)
     __shared__ uint64_t s_tri[256];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, h = lane >> 4, l16 = lane & 15;
+    constexpr int LPR = 32 / RPW;  // lanes per row
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, h = lane / LPR, lw = lane % LPR;
     const int W = g.W;
     unsigned char* ws = s_raw + (size_t)warp * ws_bytes;
-    uint2* mb = reinterpret_cast<uint2*>(ws);                                  // [2][8][W]
-    uint32_t* rwt = reinterpret_cast<uint32_t*>(ws + (size_t)2 * 8 * W * 8);  // [2][W][8]
-    uint32_t* cell = rwt + 2 * 8 * W;
+    uint2* mb = reinterpret_cast<uint2*>(ws);                                    // [RPW][8][W]
+    uint32_t* rwt = reinterpret_cast<uint32_t*>(ws + (size_t)RPW * 8 * W * 8);  // [RPW][W][8]
+    uint32_t* cell = rwt + RPW * 8 * W;
     unsigned char* list = reinterpret_cast<unsigned char*>(cell + kGenCells);
     for (int c = tid; c < 256; c += kThreads) {
         const uint64_t w = cases->tris[c];
@@ -170,50 +166,50 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
     // with the same masks (cut_masks, tris_of_word); the writes are not checked one by one.
     if ((long long)totals[0] > capV || (long long)totals[1] > capT) return;
 
-    const bool in1 = l16 + 1 < W;
-    const uint32_t evalid = validmask(l16, g.nx - 1);  // x-edges / cells: i <= nx-2
-    const uint32_t pvalid = validmask(l16, g.nx);      // points: i <= nx-1
+    const bool in1 = lw + 1 < W;
+    const uint32_t evalid = validmask(lw, g.nx - 1);  // x-edges / cells: i <= nx-2
+    const uint32_t pvalid = validmask(lw, g.nx);      // points: i <= nx-1
     uint2* mbh = mb + h * 8 * W;
     uint32_t* rwth = rwt + h * 8 * W;
-    const uint32_t nitems = (uint32_t)npairs * (uint32_t)nkc;
+    const uint32_t nitems = (uint32_t)ngroups * (uint32_t)nkc;
     for (;;) {
         uint32_t item = 0u;
         if (lane == 0) item = atomicAdd(work, 1u);
         item = __shfl_sync(0xffffffffu, item, 0);
         if (item >= nitems) break;
-        const int col = (int)(item / (uint32_t)npairs);
+        const int col = (int)(item / (uint32_t)ngroups);
         const int kc = reverse ? nkc - 1 - col : col;
-        const int jw = 2 * (int)(item % (uint32_t)npairs);
+        const int jw = RPW * (int)(item % (uint32_t)ngroups);
         const int kb = kbeg + kc * KC, ke = min(kb + KC, kend);
         const int j = jw + h;
         const bool row_ok = j < g.ny;
         const bool hasY = row_ok && j < g.ny - 1;
-        const bool in = row_ok && l16 < W;
+        const bool in = row_ok && lw < W;
 
         // Bit words of rows (j, p) and (j+1, p).
         auto load_words = [&](int p, uint32_t& wa, uint32_t& wb) {
             const bool okp = p < g.ke;  // rows of the window
             const long long r = (long long)(p - g.kr) * g.ny + j;
-            wa = (in && okp) ? __ldg(&bits[r * W + l16]) : 0u;
-            wb = (in && okp && hasY) ? __ldg(&bits[(r + 1) * W + l16]) : 0u;
+            wa = (in && okp) ? __ldg(&bits[r * W + lw]) : 0u;
+            wb = (in && okp && hasY) ? __ldg(&bits[(r + 1) * W + lw]) : 0u;
         };
-        // Row starts of step p, lanes 0..5 of each half for its row: the first
+        // Row starts of step p, lanes 0..5 of each row's lanes: the first
         // vertex of rows A = (j,p), B = (j+1,p), C = (j,p+1), D = (j+1,p+1), the
         // first triangle of cell row A, the x + y cuts of row B.
         auto load_starts = [&](int p) -> unsigned long long {
-            const int dk = (l16 >> 1) & 1, dj = l16 & 1;
+            const int dk = (lw >> 1) & 1, dj = lw & 1;
             const bool hasZp = p + 1 < g.ke;
-            bool ok = row_ok && l16 < 6;
-            if (l16 < 4) ok = ok && (dj == 0 || hasY) && (dk == 0 || hasZp);
-            if (l16 == 5) ok = ok && hasY;
+            bool ok = row_ok && lw < 6;
+            if (lw < 4) ok = ok && (dj == 0 || hasY) && (dk == 0 || hasZp);
+            if (lw == 5) ok = ok && hasY;
             if (!ok) return 0ull;
             const long long rA = (long long)(p - g.kr) * g.ny + j;
-            if (l16 == 5) {
+            if (lw == 5) {
                 const uint2 c = __ldg(reinterpret_cast<const uint2*>(&rowcnt[rA + 1]));
                 return (unsigned long long)c.x + c.y;
             }
-            const long long r = l16 < 4 ? rA + (long long)dk * g.ny + dj : rA;
-            return rs.get(r, l16 < 4 ? 0 : 1);
+            const long long r = lw < 4 ? rA + (long long)dk * g.ny + dj : rA;
+            return rs.get(r, lw < 4 ? 0 : 1);
         };
 
         uint32_t wA = 0, wB = 0, wC = 0, wD = 0;
@@ -236,45 +232,49 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
             rw.b = wB;
             rw.c = hasZ ? wC : 0u;
             rw.d = cellrow ? wD : 0u;
-            const uint32_t an = __shfl_down_sync(0xffffffffu, rw.a, 1, 16);
-            const uint32_t bn = __shfl_down_sync(0xffffffffu, rw.b, 1, 16);
-            const uint32_t cn = __shfl_down_sync(0xffffffffu, rw.c, 1, 16);
-            const uint32_t dn = __shfl_down_sync(0xffffffffu, rw.d, 1, 16);
+            const uint32_t an = __shfl_down_sync(0xffffffffu, rw.a, 1, LPR);
+            const uint32_t bn = __shfl_down_sync(0xffffffffu, rw.b, 1, LPR);
+            const uint32_t cn = __shfl_down_sync(0xffffffffu, rw.c, 1, LPR);
+            const uint32_t dn = __shfl_down_sync(0xffffffffu, rw.d, 1, LPR);
             rw.ash = (rw.a >> 1) | ((in1 ? an : 0u) << 31);
             rw.bsh = (rw.b >> 1) | ((in1 ? bn : 0u) << 31);
             rw.csh = (rw.c >> 1) | ((in1 ? cn : 0u) << 31);
             rw.dsh = (rw.d >> 1) | ((in1 ? dn : 0u) << 31);
             const CutMasks m = cut_masks(rw, evalid, pvalid, hasY, hasZ);
-            // popc prefixes within each half, two 16-bit counts per scan
+            // popc prefixes within each row's lanes, two 16-bit counts per scan
             const uint32_t p0 = __popc(m.xA) | (__popc(m.xB) << 16);
             const uint32_t p1 = __popc(m.xC) | (__popc(m.xD) << 16);
             const uint32_t p2 = __popc(m.yA) | (__popc(m.yC) << 16);
             const uint32_t p3 = __popc(m.zA) | (__popc(m.zB) << 16);
-            const uint32_t i0 = half_incl_scan(p0, l16), i1 = half_incl_scan(p1, l16);
-            const uint32_t i2 = half_incl_scan(p2, l16), i3 = half_incl_scan(p3, l16);
+            const uint32_t i0 = group_incl_scan<LPR>(p0, lw, 0xffffffffu);
+            const uint32_t i1 = group_incl_scan<LPR>(p1, lw, 0xffffffffu);
+            const uint32_t i2 = group_incl_scan<LPR>(p2, lw, 0xffffffffu);
+            const uint32_t i3 = group_incl_scan<LPR>(p3, lw, 0xffffffffu);
             const uint32_t e0 = i0 - p0, e1 = i1 - p1, e2 = i2 - p2, e3 = i3 - p3;
-            const uint32_t t0 = __shfl_sync(0xffffffffu, i0, 15, 16), t2 = __shfl_sync(0xffffffffu, i2, 15, 16);
-            const uint32_t t1 = __shfl_sync(0xffffffffu, i1, 15, 16), t3 = __shfl_sync(0xffffffffu, i3, 15, 16);
-            const unsigned long long xsA = __shfl_sync(0xffffffffu, st, 0, 16);  // this half's row
+            const uint32_t t0 = __shfl_sync(0xffffffffu, i0, LPR - 1, LPR);
+            const uint32_t t1 = __shfl_sync(0xffffffffu, i1, LPR - 1, LPR);
+            const uint32_t t2 = __shfl_sync(0xffffffffu, i2, LPR - 1, LPR);
+            const uint32_t t3 = __shfl_sync(0xffffffffu, i3, LPR - 1, LPR);
+            const unsigned long long xsA = __shfl_sync(0xffffffffu, st, 0, LPR);  // this lane's row
             const unsigned long long xs0 = __shfl_sync(0xffffffffu, st, 0);      // row jw: the step's numbering
-            const uint32_t dB = (uint32_t)(__shfl_sync(0xffffffffu, st, 1, 16) - xsA);
-            const uint32_t dC = (uint32_t)(__shfl_sync(0xffffffffu, st, 2, 16) - xsA);
-            const uint32_t dD = (uint32_t)(__shfl_sync(0xffffffffu, st, 3, 16) - xsA);
-            const uint32_t cntB = (uint32_t)__shfl_sync(0xffffffffu, st, 5, 16);
+            const uint32_t dB = (uint32_t)(__shfl_sync(0xffffffffu, st, 1, LPR) - xsA);
+            const uint32_t dC = (uint32_t)(__shfl_sync(0xffffffffu, st, 2, LPR) - xsA);
+            const uint32_t dD = (uint32_t)(__shfl_sync(0xffffffffu, st, 3, LPR) - xsA);
+            const uint32_t cntB = (uint32_t)__shfl_sync(0xffffffffu, st, 5, LPR);
             const unsigned long long ts0 = __shfl_sync(0xffffffffu, st, 4);  // first triangle of cell row jw
             const uint32_t nxA = t0 & 0xffffu, nyA = t2 & 0xffffu, nxC = t1 & 0xffffu;
-            const uint32_t off = (uint32_t)(xsA - xs0);  // 0, or the vertices of row jw
+            const uint32_t off = (uint32_t)(xsA - xs0);  // the vertices of rows jw .. j-1
             if (in) {  // first ids of the word's cut edges, relative to xs0
-                mbh[0 * W + l16] = make_uint2(m.xA, off + (e0 & 0xffffu));
-                mbh[1 * W + l16] = make_uint2(m.xB, off + dB + (e0 >> 16));
-                mbh[2 * W + l16] = make_uint2(m.xC, off + dC + (e1 & 0xffffu));
-                mbh[3 * W + l16] = make_uint2(m.xD, off + dD + (e1 >> 16));
-                mbh[4 * W + l16] = make_uint2(m.yA, off + nxA + (e2 & 0xffffu));
-                mbh[5 * W + l16] = make_uint2(m.yC, off + dC + nxC + (e2 >> 16));
-                mbh[6 * W + l16] = make_uint2(m.zA, off + nxA + nyA + (e3 & 0xffffu));
-                mbh[7 * W + l16] = make_uint2(m.zB, off + dB + cntB + (e3 >> 16));
+                mbh[0 * W + lw] = make_uint2(m.xA, off + (e0 & 0xffffu));
+                mbh[1 * W + lw] = make_uint2(m.xB, off + dB + (e0 >> 16));
+                mbh[2 * W + lw] = make_uint2(m.xC, off + dC + (e1 & 0xffffu));
+                mbh[3 * W + lw] = make_uint2(m.xD, off + dD + (e1 >> 16));
+                mbh[4 * W + lw] = make_uint2(m.yA, off + nxA + (e2 & 0xffffu));
+                mbh[5 * W + lw] = make_uint2(m.yC, off + dC + nxC + (e2 >> 16));
+                mbh[6 * W + lw] = make_uint2(m.zA, off + nxA + nyA + (e3 & 0xffffu));
+                mbh[7 * W + lw] = make_uint2(m.zB, off + dB + cntB + (e3 >> 16));
                 if (cellrow) {  // corner order of the cube case: bit v = corner v
-                    uint4* t = reinterpret_cast<uint4*>(rwth + 8 * l16);
+                    uint4* t = reinterpret_cast<uint4*>(rwth + 8 * lw);
                     t[0] = make_uint4(rw.a, rw.ash, rw.bsh, rw.b);
                     t[1] = make_uint4(rw.c, rw.csh, rw.dsh, rw.d);
                 }
@@ -286,7 +286,7 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
                 auto records = [&](uint32_t mk, uint32_t first, uint32_t axis) {
                     unsigned long long idx = xs0 + first - vbase;
                     while (mk != 0u) {
-                        put_vertex_record(points, idx, (uint32_t)(32 * l16 + __ffs(mk) - 1), axis, (uint32_t)j,
+                        put_vertex_record(points, idx, (uint32_t)(32 * lw + __ffs(mk) - 1), axis, (uint32_t)j,
                                           (uint32_t)k);
                         mk &= mk - 1u;
                         ++idx;
@@ -297,7 +297,7 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
                 records(m.zA, off + nxA + nyA + (e3 & 0xffffu), 2u);
             }
 
-            // ---- active cells of cell rows (jw, k) and (jw+1, k), compacted 32 at a time
+            // ---- active cells of cell rows (jw, k) .. (jw+RPW-1, k), 32 at a time
             const uint32_t act = (in && cellrow) ? active_cells(rw, evalid) : 0u;
             const uint32_t na = __popc(act);
             const uint32_t ia = warp_incl_scan(na, lane);  // the cells of row jw come first
@@ -319,8 +319,9 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
                 const bool live = (uint32_t)lane < nc;
                 uint32_t rec = 0u;
                 if (live) {  // the cell's cube case from its word's row words
-                    const uint32_t ch = (uint32_t)(32 * (src & 15) + (int)__fns(srcact, 0, (int)(target - srcexc) + 1)) |
-                                        ((uint32_t)(src >> 4) << 9);
+                    const uint32_t ch =
+                        (uint32_t)(32 * (src % LPR) + (int)__fns(srcact, 0, (int)(target - srcexc) + 1)) |
+                        ((uint32_t)(src / LPR) << 9);  // i | row << 9
                     const uint32_t ci = ch & 511u;
                     const uint4* t = reinterpret_cast<const uint4*>(rwt + (ch >> 9) * 8 * W + 8 * (ci >> 5));
                     const uint4 lo4 = t[0], hi4 = t[1];
@@ -345,7 +346,7 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
                         const uint32_t cr = cell[tr & 31u];
                         const int q = (int)(tr >> 5);
                         const int ci = (int)(cr & 511u);
-                        const uint2* mbc = mb + ((cr >> 9) & 1u) * 8 * W + (ci >> 5);
+                        const uint2* mbc = mb + ((cr >> 9) & 3u) * 8 * W + (ci >> 5);
                         const uint32_t corners = (uint32_t)(s_tri[cr >> 16] >> (12 * q)) & 0xfffu;
                         const int bit = ci & 31;
                         IndexT* o = tris + 3 * (tcur + t - tbase);
@@ -384,7 +385,8 @@ void launch_gen_pairs_impl(const float* vol, const Grid& g, float iso, const Cas
     const int nzw = p.kend - p.kbeg;
     if (nzw <= 0) return;
     // items of KC planes: about four per warp of one wave, at least 4 planes
-    const long long npairs = (g.ny + 1) / 2;
+    const int rpw = g.W <= 8 ? 4 : 2;
+    const long long npairs = (g.ny + rpw - 1) / rpw;  // row groups
     const long long warps = (long long)nsm * kGenPairCtasPerSm * kGenRows;
     long long KC = (npairs * nzw + 4 * warps - 1) / (4 * warps);
     if (KC < 4) KC = 4;
@@ -398,9 +400,9 @@ void launch_gen_pairs_impl(const float* vol, const Grid& g, float iso, const Cas
     for (int a = 0; a < 3; ++a) rs.add[a] = p.add[a];
     unsigned int* work = reinterpret_cast<unsigned int*>(b.totals + 7);
     cudaMemsetAsync(work, 0, sizeof(unsigned int), s);
-    const int ws_bytes = (int)gen_pair_scratch_bytes(g.W);
+    const int ws_bytes = (int)gen_pair_scratch_bytes(g.W, rpw);
     const size_t smem = (size_t)kGenRows * ws_bytes;
-    auto kern = k_gen_pairs<IndexT>;
+    auto kern = rpw == 4 ? k_gen_pairs<IndexT, 4> : k_gen_pairs<IndexT, 2>;
     allow_smem(kern, smem);
     kern<<<(unsigned)blocks, kThreads, smem, s>>>(b.bits, g, (int)KC, (int)npairs, nkc, p.kbeg, p.kend, p.vbase,
                                                   p.tbase, ws_bytes, cases, b.rowcnt, rs, b.totals, work, capV, capT,

@@ -1,4 +1,4 @@
-// Flying Edges pass 4 (two rows per warp, gen_pairs.cuh, for rows of up to 16
+// Flying Edges pass 4 (two or four rows per warp, gen_pairs.cuh, for rows of up to 16
 // words; else one row per warp, gen_warps.cuh) and the plan of the
 // warp-per-row kernels.
 #include "gen_pairs.cuh"
@@ -51,7 +51,7 @@ void launch_fe_gen_warps(const float* vol, const Grid& g, float iso, const CaseT
                          const CountPlan& cp, const GenPlan& p, long long capV, long long capT, float* points,
                          float* normals, IndexT* tris, int reverse, cudaStream_t s)
 {
-    if (fe_writes_records(g, p))  // two rows per warp
+    if (fe_writes_records(g, p))  // several rows per warp
         launch_gen_pairs_impl<IndexT>(vol, g, iso, cases, b, cp, p, p.nsm, capV, capT, points, normals, tris,
                                       reverse, s);
     else

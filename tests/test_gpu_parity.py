@@ -100,6 +100,19 @@ def test_wide_rows_multi_chunk(M):
     both(M, vol, -0.05)
 
 
+@pytest.mark.parametrize("nx", [252, 256, 260, 508, 512])
+def test_row_width_boundaries(M, nx):
+    """Rows at the edges of the kernel choices: up to 8 words the count and
+    generate kernels put four rows in a warp (256 points: every lane's word
+    full), from 9 to 16 words two (512: full); 13 rows leave the last group
+    of rows short."""
+    vol = M.generate_value_noise((nx, 13, 11), 3, 16, seed=nx)
+    both(M, vol, 0.0)
+    rng = np.random.default_rng(nx)
+    vol = rng.standard_normal((9, 13, nx)).astype(np.float32)
+    both(M, vol, 0.2, (0.5, 1.5, 0.75), (1.0, -2.0, 0.5))
+
+
 @pytest.mark.parametrize("dims", [(2, 2, 2), (2, 9, 5), (3, 2, 7), (33, 2, 2), (5, 6, 2), (31, 32, 33), (32, 17, 9),
                                   (65, 3, 4), (97, 11, 13)])
 def test_random_small(M, dims):
