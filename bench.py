@@ -13,10 +13,12 @@ One step = one full extraction (passes 1-4) of the volume.
             recorded between kernels on the extraction stream during the
             timed region; algorithmic bytes per launch:
               count          4 N                 (volume read; passes 1+2 fused)
-              fe_generate    12 T                (uint32 triangles; with fe_vertices)
+              fe_generate    12 T                (uint32 triangles; with `vertices`)
                              4 N + 24 V + 12 T   (volume read, points+normals, triangles; alone)
-              fe_vertices    4 N + 24 V          (pass-4 volume read, points+normals)
-            intermediates (bit rows, counts, vertex records) count nothing;
+              mc_vertices    0                   (vertex records, FE -> MC map; with `vertices`)
+              mc_triangles   12 T
+              vertices       4 N + 24 V          (pass-4 volume read, points+normals)
+            intermediates (bit rows, counts, vertex records, maps) count nothing;
             the whole extraction is B = 8 N + 24 V + 12 T
   cpu_baseline  the oracle port of the reference's OpenMP Flying Edges on
             all host cores, full volume, repeated for a bounded time.
@@ -396,10 +398,10 @@ def main():
         per = {names[p]: {"ms_total": ms_pass[p], "launches": int(n_pass[p]),
                           "us_per_launch": 1e3 * ms_pass[p] / n_pass[p] if n_pass[p] else None}
                for p in range(npass) if n_pass[p]}
-        split = "fe_vertices" in per  # pass 4 as generate (triangles, vertex records) + vertices
+        split = "vertices" in per  # pass 4 as generate (triangles, vertex records) + vertices
         alg_bytes = {"classify": 4 * N, "count": 4 * N, "scan": 0,
-                     "fe_generate": 12 * T if split else 4 * N + 24 * V + 12 * T, "fe_vertices": 4 * N + 24 * V,
-                     "mc_vertices": 4 * N + 24 * V, "mc_triangles": 12 * T}
+                     "fe_generate": 12 * T if split else 4 * N + 24 * V + 12 * T, "vertices": 4 * N + 24 * V,
+                     "mc_vertices": 0 if split else 4 * N + 24 * V, "mc_triangles": 12 * T}
         dom = max(per, key=lambda k: per[k]["ms_total"])
         dom_s = per[dom]["us_per_launch"] * 1e-6
         achieved = alg_bytes[dom] / dom_s / 1e9

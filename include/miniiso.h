@@ -115,7 +115,7 @@ enum {
     ISO_PASS_FE_GENERATE = 3,  /* pass 4, Flying Edges */
     ISO_PASS_MC_VERTICES = 4,  /* pass 4, Marching Cubes vertices */
     ISO_PASS_MC_TRIANGLES = 5, /* pass 4, Marching Cubes triangles */
-    ISO_PASS_FE_VERTICES = 6,  /* pass 4, Flying Edges vertices (rows of up to 512 points) */
+    ISO_PASS_VERTICES = 6,     /* pass 4, vertex points and normals from the generate pass's records */
     ISO_NUM_PASSES = 7
 };
 iso_status iso_ctx_profile(iso_ctx* ctx, int enable);

@@ -21,7 +21,7 @@ ISO_ERR_STATE = 9
 ISO_ERR_TOO_LARGE = 10
 ISO_NOALLOC_MAX_ROWS = 1 << 20
 
-PASS_NAMES = ("classify", "count", "scan", "fe_generate", "mc_vertices", "mc_triangles", "fe_vertices")
+PASS_NAMES = ("classify", "count", "scan", "fe_generate", "mc_vertices", "mc_triangles", "vertices")
 
 ISO_FLYING_EDGES = 0
 ISO_MARCHING_CUBES = 1

@@ -329,7 +329,7 @@ void enqueue_generate(iso_ctx* ctx, iso_algorithm algo, const float* vol, const 
                                                    out->normals, static_cast<uint64_t*>(out->tris), ctx->reverse, s);
             pm.mark(ISO_PASS_FE_GENERATE);
             if (iso::launch_fe_vertices(vol, g, iso, b, pl.gp, capV, capT, out->points, out->normals, s))
-                pm.mark(ISO_PASS_FE_VERTICES);
+                pm.mark(ISO_PASS_VERTICES);
             return;
         } else {
             if (i4)
@@ -357,6 +357,8 @@ void enqueue_generate(iso_ctx* ctx, iso_algorithm algo, const float* vol, const 
             iso::launch_mc_vertices_rows(vol, g, iso, ctx->d_cases, b, pl.cp, capM, capT, out->points, out->normals,
                                          ctx->nsm, s);
         pm.mark(ISO_PASS_MC_VERTICES);
+        if (pl.gp.fits && iso::launch_mc_vertices(vol, g, iso, b, pl.gp, capM, capT, out->points, out->normals, s))
+            pm.mark(ISO_PASS_VERTICES);
         if (pl.gp.fits) {
             if (i4)
                 iso::launch_mc_tri_warps<uint32_t>(g, ctx->d_cases, b, pl.cp, pl.gp, capM, capT,
@@ -498,7 +500,7 @@ iso_status slab_generate(iso_ctx* ctx, iso_algorithm algo, const float* volume, 
                                                out->normals, static_cast<uint64_t*>(out->tris), ctx->reverse, s);
         pm.mark(ISO_PASS_FE_GENERATE);
         if (iso::launch_fe_vertices(volume, g, isoval, b, gp, big, big, out->points, out->normals, s))
-            pm.mark(ISO_PASS_FE_VERTICES);
+            pm.mark(ISO_PASS_VERTICES);
     } else {
         gp.kbeg = g.kr;  // cell row k0-1 maps the edges it owns on plane k0
         gp.kend = (int)k1;
@@ -507,6 +509,8 @@ iso_status slab_generate(iso_ctx* ctx, iso_algorithm algo, const float* volume, 
         iso::launch_mc_gen_warps(volume, g, isoval, ctx->d_cases, b, pl.cp, gp, big, big, out->points, out->normals,
                                  ctx->reverse, s);
         pm.mark(ISO_PASS_MC_VERTICES);
+        if (iso::launch_mc_vertices(volume, g, isoval, b, gp, big, big, out->points, out->normals, s))
+            pm.mark(ISO_PASS_VERTICES);
         gp.kbeg = (int)k0;
         iso::gen_split(gp, ctx->nsm);
         if (i4)

@@ -19,11 +19,12 @@
 //
 // The vertices are not computed here: each lane writes, for every cut edge its
 // word owns, a record (i, axis, j, k) into the first 8 bytes of the vertex's
-// own 12-byte slot of the points buffer, and k_fe_vertices -- one thread per
+// own 12-byte slot of the points buffer, and k_vertices -- one thread per
 // vertex, many warps per SM to cover the latency of the volume gathers --
 // turns each record into the vertex's position and normal in place.
 #pragma once
 #include "gen_warps.cuh"
+#include "vertices.cuh"
 
 namespace iso {
 
@@ -34,94 +35,6 @@ constexpr int kGenPairCtasPerSm = 4;        // resident CTAs per SM the kernel i
 __host__ __device__ inline size_t gen_pair_scratch_bytes(int W, int RPW)
 {
     return ((size_t)RPW * 8 * W * 8 + (size_t)RPW * 8 * W * 4 + kGenCells * 4 + kGenTris + 15) & ~(size_t)15;
-}
-
-// Vertex record in the first 8 bytes of a vertex's points slot: word 0 =
-// i | axis << 10 | (j & 0xfffff) << 12, word 1 = j >> 20 | k << 8 (i < 1024,
-// j < 2^28, k < 2^24).
-__device__ __forceinline__ void put_vertex_record(float* points, unsigned long long idx, uint32_t i, uint32_t axis,
-                                                  uint32_t j, uint32_t k)
-{
-    uint32_t* r = reinterpret_cast<uint32_t*>(points) + 3 * idx;
-    r[0] = i | (axis << 10) | ((j & 0xfffffu) << 12);
-    r[1] = (j >> 20) | (k << 8);
-}
-
-// edge_vertex() of iso_device.cuh for the Flying Edges edge from P0 =
-// (i, j, kk) along axis a, with the operations of vertex_axis<a> on the same
-// operands (so bit-identical to it), written once for all three axes with the
-// axis as data: a warp of consecutive vertex ids mixes axes without diverging.
-__device__ __forceinline__ void vertex_any_axis(const float* __restrict__ vol, const Grid& g, const GradScale& gs,
-                                                float iso, int a, int i, int j, int kk, float3& pos, float3& nrm)
-{
-    const long long sy = g.nx, sz = (long long)g.nx * g.ny;
-    const float* p0 = vol + ((long long)(kk - g.kd) * g.ny + j) * g.nx + i;
-    const float* p1 = p0 + (a == 0 ? 1 : (a == 1 ? sy : sz));
-    const int i1 = i + (a == 0), j1 = j + (a == 1), k1 = kk + (a == 2);
-    const float v0 = __ldg(p0), v1 = __ldg(p1);
-    // neighbours of P0 and P1 = P0 + e_a; the edge's own values stand in along a
-    const float xm0 = i > 0 ? __ldg(p0 - 1) : 0.f;
-    const float xp0 = a == 0 ? v1 : (i < g.nx - 1 ? __ldg(p0 + 1) : 0.f);
-    const float ym0 = j > 0 ? __ldg(p0 - sy) : 0.f;
-    const float yp0 = a == 1 ? v1 : (j < g.ny - 1 ? __ldg(p0 + sy) : 0.f);
-    const float zm0 = kk > 0 ? __ldg(p0 - sz) : 0.f;
-    const float zp0 = a == 2 ? v1 : (kk < g.nz - 1 ? __ldg(p0 + sz) : 0.f);
-    const float xm1 = a == 0 ? v0 : (i1 > 0 ? __ldg(p1 - 1) : 0.f);
-    const float xp1 = i1 < g.nx - 1 ? __ldg(p1 + 1) : 0.f;
-    const float ym1 = a == 1 ? v0 : (j1 > 0 ? __ldg(p1 - sy) : 0.f);
-    const float yp1 = j1 < g.ny - 1 ? __ldg(p1 + sy) : 0.f;
-    const float zm1 = a == 2 ? v0 : (k1 > 0 ? __ldg(p1 - sz) : 0.f);
-    const float zp1 = k1 < g.nz - 1 ? __ldg(p1 + sz) : 0.f;
-    const float3 g0 = grad3(xm0, xp0, ym0, yp0, zm0, zp0, v0, i, j, kk, g, gs);
-    const float3 g1 = grad3(xm1, xp1, ym1, yp1, zm1, zp1, v1, i1, j1, k1, g, gs);
-    const float w = fdiv(fsub(iso, v0), fsub(v1, v0));
-    const int ci = a == 0 ? i : min(i, g.nx - 2), cj = a == 1 ? j : min(j, g.ny - 2);
-    const int ck = a == 2 ? kk : min(kk, g.nz - 2);
-    pos.x = lerp_ref(cube_coord(ci, i - ci, g.zp[0], g.sp[0]), cube_coord(ci, i1 - ci, g.zp[0], g.sp[0]), w);
-    pos.y = lerp_ref(cube_coord(cj, j - cj, g.zp[1], g.sp[1]), cube_coord(cj, j1 - cj, g.zp[1], g.sp[1]), w);
-    pos.z = lerp_ref(cube_coord(ck, kk - ck, g.zp[2], g.sp[2]), cube_coord(ck, k1 - ck, g.zp[2], g.sp[2]), w);
-    nrm.x = lerp_ref(g0.x, g1.x, w);
-    nrm.y = lerp_ref(g0.y, g1.y, w);
-    nrm.z = lerp_ref(g0.z, g1.z, w);
-}
-
-// The vertices of the rows of planes [kbeg, kend), one thread each, from the
-// records k_gen_pairs left in their points slots (slot v = vertex vbase + v).
-// One wave of kFeVertexCtasPerSm CTAs per SM walks the slots with a stride;
-// each thread loads the record of its next slot before it works on the
-// current one, so the record's trip to memory overlaps the volume gathers.
-constexpr int kFeVertexCtasPerSm = 6;
-
-__device__ __forceinline__ uint2 vertex_record(const float* points, unsigned long long v)
-{
-    const uint32_t* r = reinterpret_cast<const uint32_t*>(points) + 3 * v;
-    return make_uint2(r[0], r[1]);
-}
-
-__global__ void __launch_bounds__(kThreads, kFeVertexCtasPerSm)
-    k_fe_vertices(const float* __restrict__ vol, Grid g, GradScale gs, float iso, int kbeg, int kend,
-                  const unsigned long long* __restrict__ starts, const unsigned long long* __restrict__ totals,
-                  long long capV, long long capT, float* __restrict__ points, float* __restrict__ normals)
-{
-    if ((long long)totals[0] > capV || (long long)totals[1] > capT) return;  // k_gen_pairs wrote nothing
-    auto first = [&](int p) { return p < g.ke ? starts[(long long)(p - g.kr) * g.ny] : totals[0]; };
-    const unsigned long long n = first(kend) - first(kbeg);
-    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
-    unsigned long long v = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
-    uint2 next = v < n ? vertex_record(points, v) : make_uint2(0u, 0u);
-    for (; v < n; v += stride) {
-        const uint2 r = next;
-        if (v + stride < n) next = vertex_record(points, v + stride);  // this thread's next slot
-        const int i = (int)(r.x & 1023u), a = (int)((r.x >> 10) & 3u);
-        const int j = (int)((r.x >> 12) | ((r.y & 0xffu) << 20)), kk = (int)(r.y >> 8);
-        // every slot holds a record of the launch's rows; anything else is left alone, never read through
-        if (a > 2 || i + (a == 0) >= g.nx || j + (a == 1) >= g.ny || kk < kbeg || kk >= kend ||
-            kk + (a == 2) >= g.nz)
-            continue;
-        float3 p, nm;
-        vertex_any_axis(vol, g, gs, iso, a, i, j, kk, p, nm);
-        store_vertex(points, normals, v, p, nm);
-    }
 }
 
 // One wave of CTAs; every warp takes work items -- a group of RPW rows and a
@@ -407,16 +320,6 @@ void launch_gen_pairs_impl(const float* vol, const Grid& g, float iso, const Cas
     kern<<<(unsigned)blocks, kThreads, smem, s>>>(b.bits, g, (int)KC, (int)npairs, nkc, p.kbeg, p.kend, p.vbase,
                                                   p.tbase, ws_bytes, cases, b.rowcnt, rs, b.totals, work, capV, capT,
                                                   points, tris, reverse);
-}
-
-inline void launch_fe_vertices_impl(const float* vol, const Grid& g, float iso, const FeBuffers& b, const GenPlan& p,
-                                    int nsm, long long capV, long long capT, float* points, float* normals,
-                                    cudaStream_t s)
-{
-    if (p.kend <= p.kbeg) return;
-    k_fe_vertices<<<(unsigned)nsm * kFeVertexCtasPerSm, kThreads, 0, s>>>(vol, g, make_grad_scale(g), iso, p.kbeg,
-                                                                          p.kend, b.starts, b.totals, capV, capT,
-                                                                          points, normals);
 }
 
 }  // namespace iso

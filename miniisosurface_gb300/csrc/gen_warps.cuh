@@ -244,6 +244,19 @@ __device__ __forceinline__ void store_vertex(float* __restrict__ points, float* 
     normals[3 * id + 2] = n.z;
 }
 
+// Marching Cubes vertex record in the first 8 bytes of the vertex's points
+// slot: the edge's lower point (i, j, k), its axis and the offset d (bit 0 x,
+// 1 y, 2 z) of that point from the owner cell, whose cube places the vertex:
+// word 0 = i | axis << 10 | d << 12 | (j & 0x1ffff) << 15, word 1 = j >> 17 |
+// k << 10 (i < 1024, j < 2^27, k < 2^22).
+__device__ __forceinline__ void put_mc_record(float* points, unsigned long long idx, uint32_t i, uint32_t axis,
+                                              uint32_t d, uint32_t j, uint32_t k)
+{
+    uint32_t* r = reinterpret_cast<uint32_t*>(points) + 3 * idx;
+    r[0] = i | (axis << 10) | (d << 12) | ((j & 0x1ffffu) << 15);
+    r[1] = (j >> 17) | (k << 10);
+}
+
 // Inclusive warp scan.
 __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v, int lane)
 {
@@ -674,9 +687,16 @@ __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
                             if (k >= kemit) {  // cell rows below kemit belong to the slab below: map only
                                 int dx, dy, dz, axis;
                                 cube_edge_geometry(e12, dx, dy, dz, axis);
-                                float3 p, n;
-                                vertex_on_edge(pl, g, gs, iso, axis, i + dx, j + dy, 1 + dz, k + dz, i, j, k, p, n);
-                                store_vertex(points, normals, id - vbase, p, n);
+                                if (MODE == kGenMC) {  // k_vertices<true> computes it from the record
+                                    put_mc_record(points, id - vbase, (uint32_t)(i + dx), (uint32_t)axis,
+                                                  (uint32_t)(dx | (dy << 1) | (dz << 2)), (uint32_t)(j + dy),
+                                                  (uint32_t)(k + dz));
+                                } else {
+                                    float3 p, n;
+                                    vertex_on_edge(pl, g, gs, iso, axis, i + dx, j + dy, 1 + dz, k + dz, i, j, k, p,
+                                                   n);
+                                    store_vertex(points, normals, id - vbase, p, n);
+                                }
                             }
                             if (MODE == kGenMC) fe2mc[xsA + fe_edge_rel(mb, W, e12, i >> 5, i & 31)] = (uint32_t)id;
                         }

@@ -32,7 +32,8 @@ GenPlan gen_plan(const Grid& g, int nsm)
     p.nyb = (g.ny + p.J - 1) / p.J;
     p.smem = (size_t)kGenRows * gen_warp_scratch_bytes(g.W, kGenMC);
     const bool rel32 = 6.0 * g.nx * g.ny < 4294967295.0;  // two planes of vertices
-    p.fits = g.W <= 32 && rel32 && g.nz < (1 << 22);  // queued vertices pack i | k << 10
+    // vertex records pack i < 2^10, j < 2^27, k < 2^22
+    p.fits = g.W <= 32 && rel32 && g.ny < (1 << 27) && g.nz < (1 << 22);
     p.kbeg = g.kr;
     p.kend = g.ke;
     p.kemit = g.kr;
@@ -40,7 +41,7 @@ GenPlan gen_plan(const Grid& g, int nsm)
     return p;
 }
 
-// Grids whose pass 4 runs as k_gen_pairs + k_fe_vertices.
+// Grids whose pass 4 runs as k_gen_pairs + k_vertices.
 static bool fe_writes_records(const Grid& g, const GenPlan& p)
 {
     return g.W <= 16 && p.nsm > 0;
@@ -63,7 +64,7 @@ bool launch_fe_vertices(const float* vol, const Grid& g, float iso, const FeBuff
                         long long capV, long long capT, float* points, float* normals, cudaStream_t s)
 {
     if (!fe_writes_records(g, p)) return false;
-    launch_fe_vertices_impl(vol, g, iso, b, p, p.nsm, capV, capT, points, normals, s);
+    launch_vertices_impl<false>(vol, g, iso, b, p.kbeg, p.kend, p.nsm, capV, capT, points, normals, s);
     return true;
 }
 

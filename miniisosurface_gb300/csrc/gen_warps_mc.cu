@@ -1,7 +1,9 @@
-// Marching Cubes pass 4 (warp-per-row kernels of gen_warps.cuh): vertices in
-// owner order with the Flying Edges -> MC index map, then the triangles with
-// their corners mapped; and the duplicate-free order in one pass.
+// Marching Cubes pass 4 (warp-per-row kernels of gen_warps.cuh): vertex records
+// in owner order with the Flying Edges -> MC index map, the vertices from the
+// records (vertices.cuh), then the triangles with their corners mapped; and
+// the duplicate-free order in one pass.
 #include "gen_warps.cuh"
+#include "vertices.cuh"
 
 namespace iso {
 
@@ -11,6 +13,14 @@ void launch_mc_gen_warps(const float* vol, const Grid& g, float iso, const CaseT
 {
     launch_gen_warps_impl<kGenMC, uint32_t>(vol, g, iso, cases, b, cp, p, capV, capT, points, normals, nullptr,
                                             reverse, s);
+}
+
+bool launch_mc_vertices(const float* vol, const Grid& g, float iso, const FeBuffers& b, const GenPlan& p,
+                        long long capV, long long capT, float* points, float* normals, cudaStream_t s)
+{
+    if (p.nsm <= 0) return false;
+    launch_vertices_impl<true>(vol, g, iso, b, p.kemit, p.kend, p.nsm, capV, capT, points, normals, s);
+    return true;
 }
 
 template <typename IndexT>

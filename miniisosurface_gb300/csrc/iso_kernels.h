@@ -87,6 +87,10 @@ void launch_fe_gen_warps(const float* vol, const Grid& g, float iso, const CaseT
                          float* normals, IndexT* tris, int reverse, cudaStream_t s);
 bool launch_fe_vertices(const float* vol, const Grid& g, float iso, const FeBuffers& b, const GenPlan& p,
                         long long capV, long long capT, float* points, float* normals, cudaStream_t s);
+// Marching Cubes vertices from the records launch_mc_gen_warps wrote (false:
+// nothing launched, the plan cannot run it)
+bool launch_mc_vertices(const float* vol, const Grid& g, float iso, const FeBuffers& b, const GenPlan& p,
+                        long long capV, long long capT, float* points, float* normals, cudaStream_t s);
 void launch_mc_gen_warps(const float* vol, const Grid& g, float iso, const CaseTables* cases, const FeBuffers& b,
                          const CountPlan& cp, const GenPlan& p, long long capV, long long capT, float* points,
                          float* normals, int reverse, cudaStream_t s);
