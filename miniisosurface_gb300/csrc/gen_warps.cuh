@@ -295,9 +295,10 @@ __device__ __forceinline__ unsigned long long dup_edge_id(const uint2* mb, const
 template <int MODE, typename IndexT>
 __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
     const float* __restrict__ vol, const uint32_t* __restrict__ bits, Grid g, GradScale gs, float iso, int KC,
-    int nyb, int kbeg, int kend, int kemit, unsigned long long vbase, unsigned long long tbase, int ws_bytes,
+    int nkc, int kbeg, int kend, int kemit, unsigned long long vbase, unsigned long long tbase, int ws_bytes,
     const CaseTables* __restrict__ cases, const uint4* __restrict__ rowcnt, RowStarts rs,
-    unsigned long long* __restrict__ totals, long long capV, long long capT, float* __restrict__ points,
+    unsigned long long* __restrict__ totals, unsigned int* __restrict__ work, long long capV, long long capT,
+    float* __restrict__ points,
     float* __restrict__ normals, IndexT* __restrict__ tris, uint32_t* __restrict__ fe2mc, int reverse)
 {
     extern __shared__ __align__(16) unsigned char s_raw[];
@@ -325,394 +326,406 @@ __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
     __syncthreads();  // the only CTA barrier: from here on every warp runs alone
     if ((long long)totals[0] > capV || (long long)totals[1] > capT) return;  // caller grows buffers
 
-    const int nkc = gridDim.x / nyb;
-    const int jb = blockIdx.x % nyb;
-    const int kc = reverse ? nkc - 1 - (int)(blockIdx.x / nyb) : (int)(blockIdx.x / nyb);
-    const int j0 = jb * kGenRows;
-    const int kb = kbeg + kc * KC, ke = min(kb + KC, kend);
-    const int j = j0 + warp;
-    if (j >= g.ny) return;
-    const int jlo = j0 > 0 ? j0 - 1 : 0;  // planes are addressed from this row
-    const long long plane = (long long)g.ny * g.nx;
-    auto plane_ptr = [&](int p) { return vol + (long long)(p - g.kd) * plane + (long long)jlo * g.nx; };
+    // work items: grid row j and a run of KC planes, taken from the counter `work`
+    // (one wave of CTAs; no warp waits for another, no CTA stays for its slowest warp)
+    const uint32_t nitems = (uint32_t)g.ny * (uint32_t)nkc;
+    for (;;) {
+        uint32_t item = 0u;
+        if (lane == 0) item = atomicAdd(work, 1u);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= nitems) break;
+        const int col = (int)(item / (uint32_t)g.ny);
+        const int kc = reverse ? nkc - 1 - col : col;
+        const int kb = kbeg + kc * KC, ke = min(kb + KC, kend);
+        const int j = (int)(item % (uint32_t)g.ny);
+        const int jlo = j > 0 ? j - 1 : 0;  // planes are addressed from this row
+        const long long plane = (long long)g.ny * g.nx;
+        auto plane_ptr = [&](int p) { return vol + (long long)(p - g.kd) * plane + (long long)jlo * g.nx; };
 
-    const bool hasY = j < g.ny - 1;
+        const bool hasY = j < g.ny - 1;
 
-    const bool in = lane < W, in1 = lane + 1 < W;
-    const uint32_t evalid = validmask(lane, g.nx - 1);  // x-edges / cells: i <= nx-2
-    const uint32_t pvalid = validmask(lane, g.nx);      // points: i <= nx-1
+        const bool in = lane < W, in1 = lane + 1 < W;
+        const uint32_t evalid = validmask(lane, g.nx - 1);  // x-edges / cells: i <= nx-2
+        const uint32_t pvalid = validmask(lane, g.nx);      // points: i <= nx-1
 
-    // Bit words of rows (j, p) and (j+1, p).
-    auto load_words = [&](int p, uint32_t& wa, uint32_t& wb) {
-        const bool okp = p < g.ke;  // rows of the window
-        const long long r = (long long)(p - g.kr) * g.ny + j;
-        wa = (in && okp) ? __ldg(&bits[r * W + lane]) : 0u;
-        wb = (in && okp && hasY) ? __ldg(&bits[(r + 1) * W + lane]) : 0u;
-    };
-    // Row starts of step p, one per lane: lanes 0..3 the first vertex of rows
-    // A = (j,p), B = (j+1,p), C = (j,p+1), D = (j+1,p+1); lane 4 the first
-    // triangle (FE, TRI) or MC vertex (MC) of cell row A; lane 5 the x + y
-    // cuts of row B.
-    // Dup instead: lanes 0..3 the first x cut of rows A..D, lane 4 the first
-    // triangle of cell row A, lanes 5, 6 the first y cut of rows A, C, lanes
-    // 7, 8 the first z cut of rows A, B (each block's own numbering).
-    auto load_starts_dup = [&](int p) -> unsigned long long {
-        const long long rA = (long long)(p - g.kr) * g.ny + j;
-        const bool hasZp = p + 1 < g.ke;
-        // (row offset dk * ny + dj, component, exists)
-        int dk = 0, dj = 0, comp = 0;
-        bool ok = true;
-        if (lane < 4) {
-            dk = (lane >> 1) & 1;
-            dj = lane & 1;
-            ok = (dj == 0 || hasY) && (dk == 0 || hasZp);
-        } else if (lane == 4) {
-            comp = 1;
-        } else if (lane <= 6) {
-            comp = 2;
-            dk = lane - 5;
-            ok = dk == 0 || hasZp;
-        } else if (lane <= 8) {
-            comp = 3;
-            dj = lane - 7;
-            ok = dj == 0 || hasY;
-        } else {
-            ok = false;
-        }
-        return ok ? rs.get(rA + (long long)dk * g.ny + dj, comp) : 0ull;
-    };
-    auto load_starts = [&](int p) -> unsigned long long {
-        if (MODE == kGenDup) return load_starts_dup(p);
-        const int dk = (lane >> 1) & 1, dj = lane & 1;
-        const bool hasZp = p + 1 < g.ke;
-        bool ok = lane < 6;
-        if (lane < 4) ok = ok && (dj == 0 || hasY) && (dk == 0 || hasZp);
-        if (lane == 5) ok = ok && hasY;
-        if (!ok) return 0ull;
-        const long long rA = (long long)(p - g.kr) * g.ny + j;
-        if (lane == 5) {
-            const uint2 c = __ldg(reinterpret_cast<const uint2*>(&rowcnt[rA + 1]));
-            return (unsigned long long)c.x + c.y;
-        }
-        const long long r = lane < 4 ? rA + (long long)dk * g.ny + dj : rA;
-        return rs.get(r, lane < 4 ? 0 : (MODE == kGenMC ? 2 : 1));
-    };
-
-    const unsigned long long dupY = MODE == kGenDup ? totals[4] : 0ull;  // all x cuts
-    const unsigned long long dupZ = MODE == kGenDup ? totals[4] + totals[5] : 0ull;  // all x and y cuts
-    uint32_t wA = 0, wB = 0, wC = 0, wD = 0;
-    load_words(kb, wA, wB);
-    load_words(kb + 1, wC, wD);
-    unsigned long long st = load_starts(kb);
-
-    // FE vertex queues: ring heads and fill per axis (warp-uniform)
-    uint32_t vh0 = 0, vh1 = 0, vh2 = 0, vn0 = 0, vn1 = 0, vn2 = 0;
-    // (copied in and out by value: a reference would put them in local memory)
-    auto vq_get = [&](auto axis_tag, uint32_t& head, uint32_t& cnt) {
-        constexpr int A = decltype(axis_tag)::value;
-        if constexpr (A == 0) {
-            head = vh0;
-            cnt = vn0;
-        } else if constexpr (A == 1) {
-            head = vh1;
-            cnt = vn1;
-        } else {
-            head = vh2;
-            cnt = vn2;
-        }
-    };
-    auto vq_set = [&](auto axis_tag, uint32_t head, uint32_t cnt) {
-        constexpr int A = decltype(axis_tag)::value;
-        if constexpr (A == 0) {
-            vh0 = head;
-            vn0 = cnt;
-        } else if constexpr (A == 1) {
-            vh1 = head;
-            vn1 = cnt;
-        } else {
-            vh2 = head;
-            vn2 = cnt;
-        }
-    };
-    // Vertex batches of axis A from the queue: full ones, or all that is left
-    // at the end.  Each lane computes one vertex with the axis-A code.
-    auto drain = [&](auto axis_tag, bool all) {
-        constexpr int A = decltype(axis_tag)::value;
-        uint32_t head, cnt;
-        vq_get(axis_tag, head, cnt);
-        while (cnt >= 32u || (all && cnt > 0u)) {
-            const uint32_t nb = min(cnt, 32u);
-            if ((uint32_t)lane < nb) {
-                const uint32_t slot = A * kGenVq + ((head + lane) & (kGenVq - 1));
-                const uint32_t pos = vq_pos[slot];
-                const int i = (int)(pos & 1023u), kk = (int)(pos >> 10);
-                const float* at = plane_ptr(kk);
-                const float* lo = kk > 0 ? plane_ptr(kk - 1) : at;
-                const float* hi = kk + 1 < g.nz ? plane_ptr(kk + 1) : at;
-                const float* hi2 = kk + 2 < g.nz ? plane_ptr(kk + 2) : hi;
-                float3 p, n;
-                vertex_axis<A>(lo, at, hi, hi2, jlo, g, gs, iso, i, j, kk, p, n);
-                store_vertex(points, normals, vq_id[slot] - vbase, p, n);
+        // Bit words of rows (j, p) and (j+1, p).
+        auto load_words = [&](int p, uint32_t& wa, uint32_t& wb) {
+            const bool okp = p < g.ke;  // rows of the window
+            const long long r = (long long)(p - g.kr) * g.ny + j;
+            wa = (in && okp) ? __ldg(&bits[r * W + lane]) : 0u;
+            wb = (in && okp && hasY) ? __ldg(&bits[(r + 1) * W + lane]) : 0u;
+        };
+        // Row starts of step p, one per lane: lanes 0..3 the first vertex of rows
+        // A = (j,p), B = (j+1,p), C = (j,p+1), D = (j+1,p+1); lane 4 the first
+        // triangle (FE, TRI) or MC vertex (MC) of cell row A; lane 5 the x + y
+        // cuts of row B.
+        // Dup instead: lanes 0..3 the first x cut of rows A..D, lane 4 the first
+        // triangle of cell row A, lanes 5, 6 the first y cut of rows A, C, lanes
+        // 7, 8 the first z cut of rows A, B (each block's own numbering).
+        auto load_starts_dup = [&](int p) -> unsigned long long {
+            const long long rA = (long long)(p - g.kr) * g.ny + j;
+            const bool hasZp = p + 1 < g.ke;
+            // (row offset dk * ny + dj, component, exists)
+            int dk = 0, dj = 0, comp = 0;
+            bool ok = true;
+            if (lane < 4) {
+                dk = (lane >> 1) & 1;
+                dj = lane & 1;
+                ok = (dj == 0 || hasY) && (dk == 0 || hasZp);
+            } else if (lane == 4) {
+                comp = 1;
+            } else if (lane <= 6) {
+                comp = 2;
+                dk = lane - 5;
+                ok = dk == 0 || hasZp;
+            } else if (lane <= 8) {
+                comp = 3;
+                dj = lane - 7;
+                ok = dj == 0 || hasY;
+            } else {
+                ok = false;
             }
-            head = (head + nb) & (kGenVq - 1);
-            cnt -= nb;
-        }
-        vq_set(axis_tag, head, cnt);
-    };
-
-    // One step past the column (fin): no row, the queued vertices are drained
-    // (one drain site per axis keeps the kernel's code small).
-    for (int k = kb; k <= ke; ++k) {
-        const bool fin = k == ke;
-        const bool hasZ = k + 1 < g.nz;
-        // the next step's words and starts, in flight while this step runs
-        uint32_t nC = 0, nD = 0;
-        unsigned long long nst = 0;
-        if (k + 1 < ke) {
-            load_words(k + 2, nC, nD);
-            nst = load_starts(k + 1);
-        }
-        const bool cellrow = hasY && hasZ;
-        RowWords rw;
-        rw.a = fin ? 0u : wA;
-        rw.b = fin ? 0u : wB;
-        rw.c = hasZ && !fin ? wC : 0u;
-        rw.d = cellrow && !fin ? wD : 0u;
-        const uint32_t an = __shfl_down_sync(0xffffffffu, rw.a, 1);
-        const uint32_t bn = __shfl_down_sync(0xffffffffu, rw.b, 1);
-        const uint32_t cn = __shfl_down_sync(0xffffffffu, rw.c, 1);
-        const uint32_t dn = __shfl_down_sync(0xffffffffu, rw.d, 1);
-        rw.ash = (rw.a >> 1) | ((in1 ? an : 0u) << 31);
-        rw.bsh = (rw.b >> 1) | ((in1 ? bn : 0u) << 31);
-        rw.csh = (rw.c >> 1) | ((in1 ? cn : 0u) << 31);
-        rw.dsh = (rw.d >> 1) | ((in1 ? dn : 0u) << 31);
-        const CutMasks m = cut_masks(rw, evalid, pvalid, hasY, hasZ);
-        // popc prefixes, two 16-bit counts per scan
-        const uint32_t p0 = __popc(m.xA) | (__popc(m.xB) << 16);
-        const uint32_t p1 = __popc(m.xC) | (__popc(m.xD) << 16);
-        const uint32_t p2 = __popc(m.yA) | (__popc(m.yC) << 16);
-        const uint32_t p3 = __popc(m.zA) | (__popc(m.zB) << 16);
-        const uint32_t i0 = warp_incl_scan(p0, lane), i1 = warp_incl_scan(p1, lane);
-        const uint32_t i2 = warp_incl_scan(p2, lane), i3 = warp_incl_scan(p3, lane);
-        const uint32_t e0 = i0 - p0, e1 = i1 - p1, e2 = i2 - p2, e3 = i3 - p3;
-        const uint32_t t0 = __shfl_sync(0xffffffffu, i0, 31), t2 = __shfl_sync(0xffffffffu, i2, 31);
-        const uint32_t t1 = __shfl_sync(0xffffffffu, i1, 31), t3 = __shfl_sync(0xffffffffu, i3, 31);
-        const unsigned long long xsA = __shfl_sync(0xffffffffu, st, 0);
-        const uint32_t dB = (uint32_t)(__shfl_sync(0xffffffffu, st, 1) - xsA);
-        const uint32_t dC = (uint32_t)(__shfl_sync(0xffffffffu, st, 2) - xsA);
-        const uint32_t dD = (uint32_t)(__shfl_sync(0xffffffffu, st, 3) - xsA);
-        const unsigned long long ts = __shfl_sync(0xffffffffu, st, 4);
-        const uint32_t cntB = (uint32_t)__shfl_sync(0xffffffffu, st, 5);
-        const uint32_t nxA = t0 & 0xffffu, nyA = t2 & 0xffffu, nzA = t3 & 0xffffu, nxC = t1 & 0xffffu;
-        unsigned long long dxB[8];  // Dup: block starts of the 8 masks' rows (x A B C D, y A C, z A B)
-        if (MODE == kGenDup) {
-#pragma unroll
-            for (int q = 0; q < 8; ++q) dxB[q] = __shfl_sync(0xffffffffu, st, q < 4 ? q : q + 1);
-        }
-        if (in) {  // first ids of the word's cut edges, relative to xsA
-            mb[0 * W + lane] = make_uint2(m.xA, e0 & 0xffffu);
-            mb[1 * W + lane] = make_uint2(m.xB, dB + (e0 >> 16));
-            mb[2 * W + lane] = make_uint2(m.xC, dC + (e1 & 0xffffu));
-            mb[3 * W + lane] = make_uint2(m.xD, dD + (e1 >> 16));
-            mb[4 * W + lane] = make_uint2(m.yA, nxA + (e2 & 0xffffu));
-            mb[5 * W + lane] = make_uint2(m.yC, dC + nxC + (e2 >> 16));
-            mb[6 * W + lane] = make_uint2(m.zA, nxA + nyA + (e3 & 0xffffu));
-            mb[7 * W + lane] = make_uint2(m.zB, dB + cntB + (e3 >> 16));
-            if (MODE == kGenDup) {  // ids in the global-edge-index order: x block, y block, z block
-                db[0 * W + lane] = dxB[0] + (e0 & 0xffffu);
-                db[1 * W + lane] = dxB[1] + (e0 >> 16);
-                db[2 * W + lane] = dxB[2] + (e1 & 0xffffu);
-                db[3 * W + lane] = dxB[3] + (e1 >> 16);
-                db[4 * W + lane] = dupY + dxB[4] + (e2 & 0xffffu);
-                db[5 * W + lane] = dupY + dxB[5] + (e2 >> 16);
-                db[6 * W + lane] = dupZ + dxB[6] + (e3 & 0xffffu);
-                db[7 * W + lane] = dupZ + dxB[7] + (e3 >> 16);
+            return ok ? rs.get(rA + (long long)dk * g.ny + dj, comp) : 0ull;
+        };
+        auto load_starts = [&](int p) -> unsigned long long {
+            if (MODE == kGenDup) return load_starts_dup(p);
+            const int dk = (lane >> 1) & 1, dj = lane & 1;
+            const bool hasZp = p + 1 < g.ke;
+            bool ok = lane < 6;
+            if (lane < 4) ok = ok && (dj == 0 || hasY) && (dk == 0 || hasZp);
+            if (lane == 5) ok = ok && hasY;
+            if (!ok) return 0ull;
+            const long long rA = (long long)(p - g.kr) * g.ny + j;
+            if (lane == 5) {
+                const uint2 c = __ldg(reinterpret_cast<const uint2*>(&rowcnt[rA + 1]));
+                return (unsigned long long)c.x + c.y;
             }
-            if (cellrow) {  // corner order of the cube case: bit v = corner v
-                uint4* t = reinterpret_cast<uint4*>(rwt + 8 * lane);
-                t[0] = make_uint4(rw.a, rw.ash, rw.bsh, rw.b);
-                t[1] = make_uint4(rw.c, rw.csh, rw.dsh, rw.d);
-            }
-        }
-        __syncwarp();
-        Planes pl{};
-        if (OWNED) {  // planes k-1 .. k+2; those outside the grid alias plane k
-            pl.p1 = plane_ptr(k);
-            pl.p0 = k > 0 ? plane_ptr(k - 1) : pl.p1;
-            pl.p2 = hasZ ? plane_ptr(k + 1) : pl.p1;
-            pl.p3 = k + 2 < g.nz ? plane_ptr(k + 2) : pl.p1;
-            pl.jlo = jlo;
-            pl.nx = g.nx;
-        }
+            const long long r = lane < 4 ? rA + (long long)dk * g.ny + dj : rA;
+            return rs.get(r, lane < 4 ? 0 : (MODE == kGenMC ? 2 : 1));
+        };
 
-        if (MODE == kGenFE) {
-            // ---- vertices of grid row (j, k): x, y then z sections
-            const uint32_t nv = nxA + nyA + nzA;
-            // word prefixes of the x, y and z sections in one word: 10 + 11 + 11 bits
-            const uint32_t P = (e0 & 0x3ffu) | ((e2 & 0x7ffu) << 10) | ((e3 & 0x7ffu) << 21);
-            for (uint32_t v0 = 0; v0 < nv || (fin && v0 == 0); v0 += 32) {
-                const uint32_t v = v0 + lane;
-                const int axis = v < nxA ? 0 : (v < nxA + nyA ? 1 : 2);
-                const uint32_t r = v - (axis == 0 ? 0u : (axis == 1 ? nxA : nxA + nyA));
-                const int sh = axis == 0 ? 0 : (axis == 1 ? 10 : 21);
-                const uint32_t fm = axis == 0 ? 0x3ffu : 0x7ffu;
-                int lo = 0;
-#pragma unroll
-                for (int step = 16; step > 0; step >>= 1) {
-                    const int mid = lo + step;
-                    const uint32_t pv = (__shfl_sync(0xffffffffu, P, mid & 31) >> sh) & fm;
-                    if (mid < W && pv <= r) lo = mid;
+        const unsigned long long dupY = MODE == kGenDup ? totals[4] : 0ull;  // all x cuts
+        const unsigned long long dupZ = MODE == kGenDup ? totals[4] + totals[5] : 0ull;  // all x and y cuts
+        uint32_t wA = 0, wB = 0, wC = 0, wD = 0;
+        load_words(kb, wA, wB);
+        load_words(kb + 1, wC, wD);
+        unsigned long long st = load_starts(kb);
+
+        // FE vertex queues: ring heads and fill per axis (warp-uniform)
+        uint32_t vh0 = 0, vh1 = 0, vh2 = 0, vn0 = 0, vn1 = 0, vn2 = 0;
+        // (copied in and out by value: a reference would put them in local memory)
+        auto vq_get = [&](auto axis_tag, uint32_t& head, uint32_t& cnt) {
+            constexpr int A = decltype(axis_tag)::value;
+            if constexpr (A == 0) {
+                head = vh0;
+                cnt = vn0;
+            } else if constexpr (A == 1) {
+                head = vh1;
+                cnt = vn1;
+            } else {
+                head = vh2;
+                cnt = vn2;
+            }
+        };
+        auto vq_set = [&](auto axis_tag, uint32_t head, uint32_t cnt) {
+            constexpr int A = decltype(axis_tag)::value;
+            if constexpr (A == 0) {
+                vh0 = head;
+                vn0 = cnt;
+            } else if constexpr (A == 1) {
+                vh1 = head;
+                vn1 = cnt;
+            } else {
+                vh2 = head;
+                vn2 = cnt;
+            }
+        };
+        // Vertex batches of axis A from the queue: full ones, or all that is left
+        // at the end.  Each lane computes one vertex with the axis-A code.
+        auto drain = [&](auto axis_tag, bool all) {
+            constexpr int A = decltype(axis_tag)::value;
+            uint32_t head, cnt;
+            vq_get(axis_tag, head, cnt);
+            while (cnt >= 32u || (all && cnt > 0u)) {
+                const uint32_t nb = min(cnt, 32u);
+                if ((uint32_t)lane < nb) {
+                    const uint32_t slot = A * kGenVq + ((head + lane) & (kGenVq - 1));
+                    const uint32_t pos = vq_pos[slot];
+                    const int i = (int)(pos & 1023u), kk = (int)(pos >> 10);
+                    const float* at = plane_ptr(kk);
+                    const float* lo = kk > 0 ? plane_ptr(kk - 1) : at;
+                    const float* hi = kk + 1 < g.nz ? plane_ptr(kk + 1) : at;
+                    const float* hi2 = kk + 2 < g.nz ? plane_ptr(kk + 2) : hi;
+                    float3 p, n;
+                    vertex_axis<A>(lo, at, hi, hi2, jlo, g, gs, iso, i, j, kk, p, n);
+                    store_vertex(points, normals, vq_id[slot] - vbase, p, n);
                 }
-                int i = 0;
-                if (v < nv) {
-                    const uint2 e = mb[(axis == 0 ? 0 : (axis == 1 ? 4 : 6)) * W + lo];
-                    i = 32 * lo + (int)__fns(e.x, 0, (int)(v - e.y) + 1);
+                head = (head + nb) & (kGenVq - 1);
+                cnt -= nb;
+            }
+            vq_set(axis_tag, head, cnt);
+        };
+
+        // One step past the column (fin): no row, the queued vertices are drained
+        // (one drain site per axis keeps the kernel's code small).
+        for (int k = kb; k <= ke; ++k) {
+            const bool fin = k == ke;
+            const bool hasZ = k + 1 < g.nz;
+            // the next step's words and starts, in flight while this step runs
+            uint32_t nC = 0, nD = 0;
+            unsigned long long nst = 0;
+            if (k + 1 < ke) {
+                load_words(k + 2, nC, nD);
+                nst = load_starts(k + 1);
+            }
+            const bool cellrow = hasY && hasZ;
+            RowWords rw;
+            rw.a = fin ? 0u : wA;
+            rw.b = fin ? 0u : wB;
+            rw.c = hasZ && !fin ? wC : 0u;
+            rw.d = cellrow && !fin ? wD : 0u;
+            const uint32_t an = __shfl_down_sync(0xffffffffu, rw.a, 1);
+            const uint32_t bn = __shfl_down_sync(0xffffffffu, rw.b, 1);
+            const uint32_t cn = __shfl_down_sync(0xffffffffu, rw.c, 1);
+            const uint32_t dn = __shfl_down_sync(0xffffffffu, rw.d, 1);
+            rw.ash = (rw.a >> 1) | ((in1 ? an : 0u) << 31);
+            rw.bsh = (rw.b >> 1) | ((in1 ? bn : 0u) << 31);
+            rw.csh = (rw.c >> 1) | ((in1 ? cn : 0u) << 31);
+            rw.dsh = (rw.d >> 1) | ((in1 ? dn : 0u) << 31);
+            const CutMasks m = cut_masks(rw, evalid, pvalid, hasY, hasZ);
+            // popc prefixes, two 16-bit counts per scan
+            const uint32_t p0 = __popc(m.xA) | (__popc(m.xB) << 16);
+            const uint32_t p1 = __popc(m.xC) | (__popc(m.xD) << 16);
+            const uint32_t p2 = __popc(m.yA) | (__popc(m.yC) << 16);
+            const uint32_t p3 = __popc(m.zA) | (__popc(m.zB) << 16);
+            const uint32_t i0 = warp_incl_scan(p0, lane), i1 = warp_incl_scan(p1, lane);
+            const uint32_t i2 = warp_incl_scan(p2, lane), i3 = warp_incl_scan(p3, lane);
+            const uint32_t e0 = i0 - p0, e1 = i1 - p1, e2 = i2 - p2, e3 = i3 - p3;
+            const uint32_t t0 = __shfl_sync(0xffffffffu, i0, 31), t2 = __shfl_sync(0xffffffffu, i2, 31);
+            const uint32_t t1 = __shfl_sync(0xffffffffu, i1, 31), t3 = __shfl_sync(0xffffffffu, i3, 31);
+            const unsigned long long xsA = __shfl_sync(0xffffffffu, st, 0);
+            const uint32_t dB = (uint32_t)(__shfl_sync(0xffffffffu, st, 1) - xsA);
+            const uint32_t dC = (uint32_t)(__shfl_sync(0xffffffffu, st, 2) - xsA);
+            const uint32_t dD = (uint32_t)(__shfl_sync(0xffffffffu, st, 3) - xsA);
+            const unsigned long long ts = __shfl_sync(0xffffffffu, st, 4);
+            const uint32_t cntB = (uint32_t)__shfl_sync(0xffffffffu, st, 5);
+            const uint32_t nxA = t0 & 0xffffu, nyA = t2 & 0xffffu, nzA = t3 & 0xffffu, nxC = t1 & 0xffffu;
+            unsigned long long dxB[8];  // Dup: block starts of the 8 masks' rows (x A B C D, y A C, z A B)
+            if (MODE == kGenDup) {
+#pragma unroll
+                for (int q = 0; q < 8; ++q) dxB[q] = __shfl_sync(0xffffffffu, st, q < 4 ? q : q + 1);
+            }
+            if (in) {  // first ids of the word's cut edges, relative to xsA
+                mb[0 * W + lane] = make_uint2(m.xA, e0 & 0xffffu);
+                mb[1 * W + lane] = make_uint2(m.xB, dB + (e0 >> 16));
+                mb[2 * W + lane] = make_uint2(m.xC, dC + (e1 & 0xffffu));
+                mb[3 * W + lane] = make_uint2(m.xD, dD + (e1 >> 16));
+                mb[4 * W + lane] = make_uint2(m.yA, nxA + (e2 & 0xffffu));
+                mb[5 * W + lane] = make_uint2(m.yC, dC + nxC + (e2 >> 16));
+                mb[6 * W + lane] = make_uint2(m.zA, nxA + nyA + (e3 & 0xffffu));
+                mb[7 * W + lane] = make_uint2(m.zB, dB + cntB + (e3 >> 16));
+                if (MODE == kGenDup) {  // ids in the global-edge-index order: x block, y block, z block
+                    db[0 * W + lane] = dxB[0] + (e0 & 0xffffu);
+                    db[1 * W + lane] = dxB[1] + (e0 >> 16);
+                    db[2 * W + lane] = dxB[2] + (e1 & 0xffffu);
+                    db[3 * W + lane] = dxB[3] + (e1 >> 16);
+                    db[4 * W + lane] = dupY + dxB[4] + (e2 & 0xffffu);
+                    db[5 * W + lane] = dupY + dxB[5] + (e2 >> 16);
+                    db[6 * W + lane] = dupZ + dxB[6] + (e3 & 0xffffu);
+                    db[7 * W + lane] = dupZ + dxB[7] + (e3 >> 16);
                 }
-                // append to the axis queues (each had < 32 entries: room for 32 more)
-                auto append = [&](auto axis_tag) {
-                    constexpr int a = decltype(axis_tag)::value;
-                    const bool mine = v < nv && axis == a;
-                    const uint32_t ball = __ballot_sync(0xffffffffu, mine);
-                    uint32_t head, cnt;
-                    vq_get(axis_tag, head, cnt);
-                    if (mine) {
-                        const uint32_t slot =
-                            a * kGenVq + ((head + cnt + __popc(ball & ((1u << lane) - 1u))) & (kGenVq - 1));
-                        vq_id[slot] = xsA + v;
-                        vq_pos[slot] = (uint32_t)i | ((uint32_t)k << 10);
+                if (cellrow) {  // corner order of the cube case: bit v = corner v
+                    uint4* t = reinterpret_cast<uint4*>(rwt + 8 * lane);
+                    t[0] = make_uint4(rw.a, rw.ash, rw.bsh, rw.b);
+                    t[1] = make_uint4(rw.c, rw.csh, rw.dsh, rw.d);
+                }
+            }
+            __syncwarp();
+            Planes pl{};
+            if (OWNED) {  // planes k-1 .. k+2; those outside the grid alias plane k
+                pl.p1 = plane_ptr(k);
+                pl.p0 = k > 0 ? plane_ptr(k - 1) : pl.p1;
+                pl.p2 = hasZ ? plane_ptr(k + 1) : pl.p1;
+                pl.p3 = k + 2 < g.nz ? plane_ptr(k + 2) : pl.p1;
+                pl.jlo = jlo;
+                pl.nx = g.nx;
+            }
+
+            if (MODE == kGenFE) {
+                // ---- vertices of grid row (j, k): x, y then z sections
+                const uint32_t nv = nxA + nyA + nzA;
+                // word prefixes of the x, y and z sections in one word: 10 + 11 + 11 bits
+                const uint32_t P = (e0 & 0x3ffu) | ((e2 & 0x7ffu) << 10) | ((e3 & 0x7ffu) << 21);
+                for (uint32_t v0 = 0; v0 < nv || (fin && v0 == 0); v0 += 32) {
+                    const uint32_t v = v0 + lane;
+                    const int axis = v < nxA ? 0 : (v < nxA + nyA ? 1 : 2);
+                    const uint32_t r = v - (axis == 0 ? 0u : (axis == 1 ? nxA : nxA + nyA));
+                    const int sh = axis == 0 ? 0 : (axis == 1 ? 10 : 21);
+                    const uint32_t fm = axis == 0 ? 0x3ffu : 0x7ffu;
+                    int lo = 0;
+#pragma unroll
+                    for (int step = 16; step > 0; step >>= 1) {
+                        const int mid = lo + step;
+                        const uint32_t pv = (__shfl_sync(0xffffffffu, P, mid & 31) >> sh) & fm;
+                        if (mid < W && pv <= r) lo = mid;
                     }
-                    vq_set(axis_tag, head, cnt + __popc(ball));
-                };
-                append(std::integral_constant<int, 0>());
-                append(std::integral_constant<int, 1>());
-                append(std::integral_constant<int, 2>());
-                __syncwarp();
-                drain(std::integral_constant<int, 0>(), fin);
-                drain(std::integral_constant<int, 1>(), fin);
-                drain(std::integral_constant<int, 2>(), fin);
-                __syncwarp();
-            }
-        }
-        if (cellrow) {
-            // ---- active cells of cell row (j, k), compacted 32 at a time
-            uint32_t rem = in ? active_cells(rw, evalid) : 0u;
-            const uint32_t na = __popc(rem);
-            const uint32_t ia = warp_incl_scan(na, lane);
-            uint32_t rank = ia - na;
-            const uint32_t tot = __shfl_sync(0xffffffffu, ia, 31);
-            unsigned long long tcur = ts;  // FE / TRI / Dup: next triangle
-            unsigned long long mcur = ts;  // MC: next vertex
-            for (uint32_t c0 = 0; c0 < tot; c0 += kGenCells) {
-                while (rem != 0u && rank < c0 + kGenCells) {
-                    cell[rank - c0] = (uint32_t)(32 * lane + __ffs(rem) - 1);
-                    rem &= rem - 1u;
-                    ++rank;
-                }
-                __syncwarp();
-                const uint32_t nc = min(tot - c0, (uint32_t)kGenCells);
-                const bool live = (uint32_t)lane < nc;
-                uint32_t rec = 0u;
-                if (live) {  // the cell's cube case from its word's row words
-                    const uint32_t ci = cell[lane];
-                    const uint4* t = reinterpret_cast<const uint4*>(rwt + 8 * (ci >> 5));
-                    const uint4 lo4 = t[0], hi4 = t[1];
-                    const int b = (int)(ci & 31u);
-                    const uint32_t cs = ((lo4.x >> b) & 1u) | (((lo4.y >> b) & 1u) << 1) | (((lo4.z >> b) & 1u) << 2) |
-                                        (((lo4.w >> b) & 1u) << 3) | (((hi4.x >> b) & 1u) << 4) |
-                                        (((hi4.y >> b) & 1u) << 5) | (((hi4.z >> b) & 1u) << 6) |
-                                        (((hi4.w >> b) & 1u) << 7);
-                    rec = ci | (cs << 16);
-                    cell[lane] = rec;
-                }
-                const int cs = (int)(rec >> 16);
-                if (MODE != kGenMC) {
-                    const uint32_t nt = live ? (uint32_t)iso_case_ntris(s_tris[cs]) : 0u;
-                    const uint32_t it = warp_incl_scan(nt, lane);
-                    const uint32_t ntb = __shfl_sync(0xffffffffu, it, 31);
-                    for (uint32_t q = 0; q < nt; ++q) list[it - nt + q] = (unsigned char)(lane | (q << 5));
+                    int i = 0;
+                    if (v < nv) {
+                        const uint2 e = mb[(axis == 0 ? 0 : (axis == 1 ? 4 : 6)) * W + lo];
+                        i = 32 * lo + (int)__fns(e.x, 0, (int)(v - e.y) + 1);
+                    }
+                    // append to the axis queues (each had < 32 entries: room for 32 more)
+                    auto append = [&](auto axis_tag) {
+                        constexpr int a = decltype(axis_tag)::value;
+                        const bool mine = v < nv && axis == a;
+                        const uint32_t ball = __ballot_sync(0xffffffffu, mine);
+                        uint32_t head, cnt;
+                        vq_get(axis_tag, head, cnt);
+                        if (mine) {
+                            const uint32_t slot =
+                                a * kGenVq + ((head + cnt + __popc(ball & ((1u << lane) - 1u))) & (kGenVq - 1));
+                            vq_id[slot] = xsA + v;
+                            vq_pos[slot] = (uint32_t)i | ((uint32_t)k << 10);
+                        }
+                        vq_set(axis_tag, head, cnt + __popc(ball));
+                    };
+                    append(std::integral_constant<int, 0>());
+                    append(std::integral_constant<int, 1>());
+                    append(std::integral_constant<int, 2>());
                     __syncwarp();
-                    for (uint32_t tb = 0; tb < ntb; tb += 32) {
-                        const uint32_t t = tb + lane;
-                        if (t < ntb) {
-                            const uint32_t tr = list[t];
-                            const uint32_t cr = cell[tr & 31u];
-                            const int q = (int)(tr >> 5);
-                            const int ci = (int)(cr & 0xffffu);
-                            const uint64_t tl = s_tris[cr >> 16];
-                            const int w = ci >> 5, bit = ci & 31;
-                            IndexT* o = tris + 3 * (tcur + t - tbase);
+                    drain(std::integral_constant<int, 0>(), fin);
+                    drain(std::integral_constant<int, 1>(), fin);
+                    drain(std::integral_constant<int, 2>(), fin);
+                    __syncwarp();
+                }
+            }
+            if (cellrow) {
+                // ---- active cells of cell row (j, k), 32 at a time
+                const uint32_t act = in ? active_cells(rw, evalid) : 0u;
+                const uint32_t na = __popc(act);
+                const uint32_t ia = warp_incl_scan(na, lane);
+                const uint32_t tot = __shfl_sync(0xffffffffu, ia, 31);
+                unsigned long long tcur = ts;  // FE / TRI / Dup: next triangle
+                unsigned long long mcur = ts;  // MC: next vertex
+                for (uint32_t c0 = 0; c0 < tot; c0 += kGenCells) {
+                    // lane L takes active cell c0 + L: the first lane whose inclusive count passes it (a
+                    // shuffle binary search over the lanes), then the bit by __fns -- no per-lane loop,
+                    // which diverges where the active cells cluster along the surface
+                    const uint32_t target = c0 + (uint32_t)lane;
+                    int src = 0;
 #pragma unroll
-                            for (int c = 0; c < 3; ++c) {
-                                const int e = iso_case_edge(tl, 3 * q + c);
-                                if (MODE == kGenDup) {
-                                    o[c] = (IndexT)dup_edge_id(mb, db, W, e, w, bit);
-                                } else {
-                                    const unsigned long long id = xsA + fe_edge_rel(mb, W, e, w, bit);
-                                    o[c] = MODE == kGenTri ? (IndexT)__ldg(fe2mc + id) : (IndexT)id;
+                    for (int step = 16; step > 0; step >>= 1) {
+                        const uint32_t before = __shfl_sync(0xffffffffu, ia, (src + step - 1) & 31);
+                        if (before <= target) src += step;
+                    }
+                    const uint32_t srcact = __shfl_sync(0xffffffffu, act, src);
+                    const uint32_t srcexc = __shfl_sync(0xffffffffu, ia - na, src);
+                    const uint32_t nc = min(tot - c0, (uint32_t)kGenCells);
+                    const bool live = (uint32_t)lane < nc;
+                    uint32_t rec = 0u;
+                    if (live) {  // the cell's cube case from its word's row words
+                        const uint32_t ci = (uint32_t)(32 * src + (int)__fns(srcact, 0, (int)(target - srcexc) + 1));
+                        const uint4* t = reinterpret_cast<const uint4*>(rwt + 8 * (ci >> 5));
+                        const uint4 lo4 = t[0], hi4 = t[1];
+                        const int b = (int)(ci & 31u);
+                        const uint32_t cs = ((lo4.x >> b) & 1u) | (((lo4.y >> b) & 1u) << 1) |
+                                            (((lo4.z >> b) & 1u) << 2) | (((lo4.w >> b) & 1u) << 3) |
+                                            (((hi4.x >> b) & 1u) << 4) |
+                                            (((hi4.y >> b) & 1u) << 5) | (((hi4.z >> b) & 1u) << 6) |
+                                            (((hi4.w >> b) & 1u) << 7);
+                        rec = ci | (cs << 16);
+                        cell[lane] = rec;
+                    }
+                    const int cs = (int)(rec >> 16);
+                    if (MODE != kGenMC) {
+                        const uint32_t nt = live ? (uint32_t)iso_case_ntris(s_tris[cs]) : 0u;
+                        const uint32_t it = warp_incl_scan(nt, lane);
+                        const uint32_t ntb = __shfl_sync(0xffffffffu, it, 31);
+                        for (uint32_t q = 0; q < nt; ++q) list[it - nt + q] = (unsigned char)(lane | (q << 5));
+                        __syncwarp();
+                        for (uint32_t tb = 0; tb < ntb; tb += 32) {
+                            const uint32_t t = tb + lane;
+                            if (t < ntb) {
+                                const uint32_t tr = list[t];
+                                const uint32_t cr = cell[tr & 31u];
+                                const int q = (int)(tr >> 5);
+                                const int ci = (int)(cr & 0xffffu);
+                                const uint64_t tl = s_tris[cr >> 16];
+                                const int w = ci >> 5, bit = ci & 31;
+                                IndexT* o = tris + 3 * (tcur + t - tbase);
+#pragma unroll
+                                for (int c = 0; c < 3; ++c) {
+                                    const int e = iso_case_edge(tl, 3 * q + c);
+                                    if (MODE == kGenDup) {
+                                        o[c] = (IndexT)dup_edge_id(mb, db, W, e, w, bit);
+                                    } else {
+                                        const unsigned long long id = xsA + fe_edge_rel(mb, W, e, w, bit);
+                                        o[c] = MODE == kGenTri ? (IndexT)__ldg(fe2mc + id) : (IndexT)id;
+                                    }
                                 }
                             }
                         }
+                        tcur += ntb;
                     }
-                    tcur += ntb;
-                }
-                if (MODE == kGenDup) __syncwarp();  // the vertex list below reuses the triangle list
-                if (OWNED) {
-                    // ---- MC vertices owned by the batch's cells: cell order, then order of
-                    // first appearance in the cell's triangle list
-                    const int ci = (int)(rec & 0xffffu);
-                    const uint32_t own = live ? (mc_owned_edges(ci == 0, j == 0, k == 0) & s_cut[cs]) : 0u;
-                    const uint32_t no = __popc(own);
-                    const uint32_t io = warp_incl_scan(no, lane);
-                    const uint32_t nob = __shfl_sync(0xffffffffu, io, 31);
-                    uint16_t* vl = reinterpret_cast<uint16_t*>(list);
-                    if (own) {
-                        const uint64_t ord = s_order[cs];
-                        uint32_t o = io - no;
-                        for (int q = 0; q < iso_case_ntris(ord); ++q) {
-                            const int ed = iso_case_edge(ord, q);
-                            if ((own >> ed) & 1u) vl[o++] = (uint16_t)(lane | (ed << 5));
-                        }
-                    }
-                    __syncwarp();
-                    for (uint32_t vb = 0; vb < nob; vb += 32) {
-                        const uint32_t v = vb + lane;
-                        if (v < nob) {
-                            const uint32_t vr = vl[v];
-                            const uint32_t cr = cell[vr & 31u];
-                            const int e12 = (int)(vr >> 5);
-                            const int i = (int)(cr & 0xffffu);
-                            // MC: owner order; Dup: the edge's place in the global-edge-index order
-                            const unsigned long long id =
-                                MODE == kGenDup ? dup_edge_id(mb, db, W, e12, i >> 5, i & 31) : mcur + v;
-                            if (k >= kemit) {  // cell rows below kemit belong to the slab below: map only
-                                int dx, dy, dz, axis;
-                                cube_edge_geometry(e12, dx, dy, dz, axis);
-                                if (MODE == kGenMC) {  // k_vertices<true> computes it from the record
-                                    put_mc_record(points, id - vbase, (uint32_t)(i + dx), (uint32_t)axis,
-                                                  (uint32_t)(dx | (dy << 1) | (dz << 2)), (uint32_t)(j + dy),
-                                                  (uint32_t)(k + dz));
-                                } else {
-                                    float3 p, n;
-                                    vertex_on_edge(pl, g, gs, iso, axis, i + dx, j + dy, 1 + dz, k + dz, i, j, k, p,
-                                                   n);
-                                    store_vertex(points, normals, id - vbase, p, n);
-                                }
+                    if (MODE == kGenDup) __syncwarp();  // the vertex list below reuses the triangle list
+                    if (OWNED) {
+                        // ---- MC vertices owned by the batch's cells: cell order, then order of
+                        // first appearance in the cell's triangle list
+                        const int ci = (int)(rec & 0xffffu);
+                        const uint32_t own = live ? (mc_owned_edges(ci == 0, j == 0, k == 0) & s_cut[cs]) : 0u;
+                        const uint32_t no = __popc(own);
+                        const uint32_t io = warp_incl_scan(no, lane);
+                        const uint32_t nob = __shfl_sync(0xffffffffu, io, 31);
+                        uint16_t* vl = reinterpret_cast<uint16_t*>(list);
+                        if (own) {
+                            const uint64_t ord = s_order[cs];
+                            uint32_t o = io - no;
+                            for (int q = 0; q < iso_case_ntris(ord); ++q) {
+                                const int ed = iso_case_edge(ord, q);
+                                if ((own >> ed) & 1u) vl[o++] = (uint16_t)(lane | (ed << 5));
                             }
-                            if (MODE == kGenMC) fe2mc[xsA + fe_edge_rel(mb, W, e12, i >> 5, i & 31)] = (uint32_t)id;
                         }
+                        __syncwarp();
+                        for (uint32_t vb = 0; vb < nob; vb += 32) {
+                            const uint32_t v = vb + lane;
+                            if (v < nob) {
+                                const uint32_t vr = vl[v];
+                                const uint32_t cr = cell[vr & 31u];
+                                const int e12 = (int)(vr >> 5);
+                                const int i = (int)(cr & 0xffffu);
+                                // MC: owner order; Dup: the edge's place in the global-edge-index order
+                                const unsigned long long id =
+                                    MODE == kGenDup ? dup_edge_id(mb, db, W, e12, i >> 5, i & 31) : mcur + v;
+                                if (k >= kemit) {  // cell rows below kemit belong to the slab below: map only
+                                    int dx, dy, dz, axis;
+                                    cube_edge_geometry(e12, dx, dy, dz, axis);
+                                    if (MODE == kGenMC) {  // k_vertices<true> computes it from the record
+                                        put_mc_record(points, id - vbase, (uint32_t)(i + dx), (uint32_t)axis,
+                                                      (uint32_t)(dx | (dy << 1) | (dz << 2)), (uint32_t)(j + dy),
+                                                      (uint32_t)(k + dz));
+                                    } else {
+                                        float3 p, n;
+                                        vertex_on_edge(pl, g, gs, iso, axis, i + dx, j + dy, 1 + dz, k + dz, i, j, k, p,
+                                                       n);
+                                        store_vertex(points, normals, id - vbase, p, n);
+                                    }
+                                }
+                                if (MODE == kGenMC) fe2mc[xsA + fe_edge_rel(mb, W, e12, i >> 5, i & 31)] = (uint32_t)id;
+                            }
+                        }
+                        mcur += nob;
                     }
-                    mcur += nob;
+                    __syncwarp();  // the next batch overwrites the lists
                 }
-                __syncwarp();  // the next batch overwrites the lists
             }
+            __syncwarp();  // the next step overwrites mb
+            wA = wC;
+            wB = wD;
+            wC = nC;
+            wD = nD;
+            st = nst;
         }
-        __syncwarp();  // the next step overwrites mb
-        wA = wC;
-        wB = wD;
-        wC = nC;
-        wD = nD;
-        st = nst;
-    }
+    }  // work items
 }
 
 template <int MODE, typename IndexT>
@@ -720,16 +733,30 @@ void launch_gen_warps_impl(const float* vol, const Grid& g, float iso, const Cas
                            const CountPlan& cp, const GenPlan& p, long long capV, long long capT, float* points,
                            float* normals, IndexT* tris, int reverse, cudaStream_t s)
 {
+    const int nzw = p.kend - p.kbeg;
+    if (nzw <= 0) return;
+    // items of KC planes: about four per warp of one wave, at least 4 planes
+    const long long warps = (long long)p.nsm * kGenCtasPerSm * kGenRows;
+    long long KC = ((long long)g.ny * nzw + 4 * warps - 1) / (4 * warps);
+    if (KC < 4) KC = 4;
+    while ((long long)g.ny * ((nzw + KC - 1) / KC) >= (1ll << 31)) KC *= 2;  // item numbers stay below 2^31
+    if (KC > nzw) KC = nzw;
+    const int nkc = (int)((nzw + KC - 1) / KC);
+    const long long nitems = (long long)g.ny * nkc;
+    long long blocks = (nitems + kGenRows - 1) / kGenRows;
+    if (blocks > (long long)p.nsm * kGenCtasPerSm) blocks = (long long)p.nsm * kGenCtasPerSm;
     RowStarts rs = row_starts(g, cp, b);
     for (int a = 0; a < 3; ++a) rs.add[a] = p.add[a];
-    const unsigned blocks = (unsigned)(p.nyb * p.nkc);
+    unsigned int* work = reinterpret_cast<unsigned int*>(b.totals + 7);
+    cudaMemsetAsync(work, 0, sizeof(unsigned int), s);
     const int ws_bytes = (int)gen_warp_scratch_bytes(g.W, MODE);
     const size_t smem = (size_t)kGenRows * ws_bytes;
     auto kern = k_gen_warps<MODE, IndexT>;
     allow_smem(kern, smem);
-    kern<<<blocks, kThreads, smem, s>>>(vol, b.bits, g, make_grad_scale(g), iso, p.KC, p.nyb, p.kbeg, p.kend, p.kemit,
-                                        p.vbase, p.tbase, ws_bytes, cases, b.rowcnt, rs, b.totals, capV, capT, points,
-                                        normals, tris, b.fe2mc, reverse);
+    kern<<<(unsigned)blocks, kThreads, smem, s>>>(vol, b.bits, g, make_grad_scale(g), iso, (int)KC, nkc, p.kbeg,
+                                                  p.kend, p.kemit, p.vbase, p.tbase, ws_bytes, cases, b.rowcnt, rs,
+                                                  b.totals, work, capV, capT, points, normals, tris, b.fe2mc,
+                                                  reverse);
 }
 
 }  // namespace iso

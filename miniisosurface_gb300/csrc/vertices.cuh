@@ -64,10 +64,11 @@ __device__ __forceinline__ void vertex_any_axis(const float* __restrict__ vol, c
     nrm.z = lerp_ref(g0.z, g1.z, w);
 }
 
-// One wave of kVertexCtasPerSm CTAs per SM walks the slots with a stride; each
-// thread loads the record of its next slot before it works on the current one,
-// so the record's trip to memory overlaps the volume gathers.
-constexpr int kVertexCtasPerSm = 6;
+// One wave of vertex_ctas_per_sm(MC) CTAs per SM walks the slots with a
+// stride; each thread loads the record of its next slot before it works on the
+// current one, so the record's trip to memory overlaps the volume gathers.
+// (The Marching Cubes record takes a few more registers to decode: 5 CTAs.)
+__host__ __device__ constexpr int vertex_ctas_per_sm(bool mc) { return mc ? 5 : 6; }
 
 __device__ __forceinline__ uint2 vertex_record(const float* points, unsigned long long v)
 {
@@ -80,7 +81,7 @@ __device__ __forceinline__ uint2 vertex_record(const float* points, unsigned lon
 // thread each, slot v = vertex vbase + v.  The capacity test is the generate
 // kernels': when it fails they wrote no record and nothing is read here.
 template <bool MC>
-__global__ void __launch_bounds__(kThreads, kVertexCtasPerSm)
+__global__ void __launch_bounds__(kThreads, vertex_ctas_per_sm(MC))
     k_vertices(const float* __restrict__ vol, Grid g, GradScale gs, float iso, int kbeg, int kend,
                const unsigned long long* __restrict__ starts, const unsigned long long* __restrict__ totals,
                long long capV, long long capT, float* __restrict__ points, float* __restrict__ normals)
@@ -128,9 +129,9 @@ inline void launch_vertices_impl(const float* vol, const Grid& g, float iso, con
                                  cudaStream_t s)
 {
     if (k1 <= k0) return;
-    k_vertices<MC><<<(unsigned)nsm * kVertexCtasPerSm, kThreads, 0, s>>>(vol, g, make_grad_scale(g), iso, k0, k1,
-                                                                         b.starts, b.totals, capV, capT, points,
-                                                                         normals);
+    const unsigned blocks = (unsigned)nsm * vertex_ctas_per_sm(MC);
+    k_vertices<MC><<<blocks, kThreads, 0, s>>>(vol, g, make_grad_scale(g), iso, k0, k1, b.starts, b.totals, capV,
+                                               capT, points, normals);
 }
 
 }  // namespace iso
