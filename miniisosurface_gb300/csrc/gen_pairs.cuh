@@ -31,10 +31,11 @@ namespace iso {
 constexpr int kGenPairCtasPerSm = 4;        // resident CTAs per SM the kernel is built for
 
 // Per-warp scratch: mb[RPW][8][W] uint2, rwt[RPW][W][8], cell[32], the
-// batch's triangle list (u8).
-__host__ __device__ inline size_t gen_pair_scratch_bytes(int W, int RPW)
+// batch's list (gen_list_bytes: triangles, or Marching Cubes owned vertices).
+__host__ __device__ inline size_t gen_pair_scratch_bytes(int W, int RPW, int mode)
 {
-    return ((size_t)RPW * 8 * W * 8 + (size_t)RPW * 8 * W * 4 + kGenCells * 4 + kGenTris + 15) & ~(size_t)15;
+    return ((size_t)RPW * 8 * W * 8 + (size_t)RPW * 8 * W * 4 + kGenCells * 4 + gen_list_bytes(mode) + 15) &
+           ~(size_t)15;
 }
 
 // One wave of CTAs; every warp takes work items -- a group of RPW rows and a
@@ -43,18 +44,25 @@ __host__ __device__ inline size_t gen_pair_scratch_bytes(int W, int RPW)
 // row group q % ngroups of plane run q / ngroups (runs walked backwards when
 // `reverse`).  RPW = 2 for rows of up to 16 words, 4 for up to 8: lanes
 // LPR*h .. LPR*h + LPR-1 hold the words of row jw + h.
-template <typename IndexT, int RPW>
+// MODE kGenFE: Flying Edges vertex records and triangles.  kGenMC: the
+// Marching Cubes vertices the cells own (marchingCubes/serial/main.cpp:
+// 139-177: cell order, then first appearance in the cell's triangle list)
+// get their ids, records for the rows from kemit on, and the FE -> MC map
+// entry of their edge.  kGenTri: the triangles, corners mapped through it.
+template <typename IndexT, int RPW, int MODE>
 __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
     const uint32_t* __restrict__ bits, Grid g, int KC, int ngroups, int nkc, int kbeg, int kend,
-    unsigned long long vbase, unsigned long long tbase, int ws_bytes, const CaseTables* __restrict__ cases,
-    const uint4* __restrict__ rowcnt, RowStarts rs, const unsigned long long* __restrict__ totals,
-    unsigned int* __restrict__ work, long long capV, long long capT, float* __restrict__ points,
-    IndexT* __restrict__ tris, int reverse)
+    int kemit, unsigned long long vbase, unsigned long long tbase, int ws_bytes,
+    const CaseTables* __restrict__ cases, const uint4* __restrict__ rowcnt, RowStarts rs,
+    const unsigned long long* __restrict__ totals, unsigned int* __restrict__ work, long long capV, long long capT,
+    float* __restrict__ points, IndexT* __restrict__ tris, uint32_t* __restrict__ fe2mc, int reverse)
 {
     extern __shared__ __align__(16) unsigned char s_raw[];
     // per case: each triangle corner as the nibble (edge-id table row | point offset << 3) of fe_edge_rel,
     // the triangle count in bits 60..63 (the packed triangle list with edges replaced)
-    __shared__ uint64_t s_tri[256];
+    __shared__ uint64_t s_tri[MODE == kGenMC ? 1 : 256];
+    __shared__ uint64_t s_order[MODE == kGenMC ? 256 : 1];  // kGenMC: first-appearance order, cut edges
+    __shared__ uint16_t s_cut[MODE == kGenMC ? 256 : 1];
     constexpr int LPR = 32 / RPW;  // lanes per row
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, h = lane / LPR, lw = lane % LPR;
     const int W = g.W;
@@ -64,6 +72,11 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
     uint32_t* cell = rwt + RPW * 8 * W;
     unsigned char* list = reinterpret_cast<unsigned char*>(cell + kGenCells);
     for (int c = tid; c < 256; c += kThreads) {
+        if (MODE == kGenMC) {
+            s_order[c] = cases->order[c];
+            s_cut[c] = cases->cut[c];
+            continue;
+        }
         const uint64_t w = cases->tris[c];
         uint64_t x = w & (0xfull << 60);
         for (int q = 0; q < 15; ++q) {
@@ -122,7 +135,7 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
                 return (unsigned long long)c.x + c.y;
             }
             const long long r = lw < 4 ? rA + (long long)dk * g.ny + dj : rA;
-            return rs.get(r, lw < 4 ? 0 : 1);
+            return rs.get(r, lw < 4 ? 0 : (MODE == kGenMC ? 2 : 1));
         };
 
         uint32_t wA = 0, wB = 0, wC = 0, wD = 0;
@@ -174,7 +187,8 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
             const uint32_t dC = (uint32_t)(__shfl_sync(0xffffffffu, st, 2, LPR) - xsA);
             const uint32_t dD = (uint32_t)(__shfl_sync(0xffffffffu, st, 3, LPR) - xsA);
             const uint32_t cntB = (uint32_t)__shfl_sync(0xffffffffu, st, 5, LPR);
-            const unsigned long long ts0 = __shfl_sync(0xffffffffu, st, 4);  // first triangle of cell row jw
+            // first triangle (kGenMC: first owned MC vertex) of cell row jw
+            const unsigned long long ts0 = __shfl_sync(0xffffffffu, st, 4);
             const uint32_t nxA = t0 & 0xffffu, nyA = t2 & 0xffffu, nxC = t1 & 0xffffu;
             const uint32_t off = (uint32_t)(xsA - xs0);  // the vertices of rows jw .. j-1
             if (in) {  // first ids of the word's cut edges, relative to xs0
@@ -195,7 +209,7 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
             __syncwarp();
 
             // ---- vertex records of grid row (j, k): the x, y, z cuts its word owns
-            if (in) {
+            if (MODE == kGenFE && in) {
                 auto records = [&](uint32_t mk, uint32_t first, uint32_t axis) {
                     unsigned long long idx = xs0 + first - vbase;
                     while (mk != 0u) {
@@ -247,37 +261,80 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
                     cell[lane] = rec;
                 }
                 const int cs = (int)(rec >> 16);
-                const uint32_t nt = live ? (uint32_t)iso_case_ntris(s_tri[cs]) : 0u;
-                const uint32_t it = warp_incl_scan(nt, lane);
-                const uint32_t ntb = __shfl_sync(0xffffffffu, it, 31);
-                for (uint32_t q = 0; q < nt; ++q) list[it - nt + q] = (unsigned char)(lane | (q << 5));
-                __syncwarp();
-                for (uint32_t tb = 0; tb < ntb; tb += 32) {
-                    const uint32_t t = tb + lane;
-                    if (t < ntb) {
-                        const uint32_t tr = list[t];
-                        const uint32_t cr = cell[tr & 31u];
-                        const int q = (int)(tr >> 5);
-                        const int ci = (int)(cr & 511u);
-                        const uint2* mbc = mb + ((cr >> 9) & 3u) * 8 * W + (ci >> 5);
-                        const uint32_t corners = (uint32_t)(s_tri[cr >> 16] >> (12 * q)) & 0xfffu;
-                        const int bit = ci & 31;
-                        IndexT* o = tris + 3 * (tcur + t - tbase);
+                if (MODE != kGenMC) {
+                    const uint32_t nt = live ? (uint32_t)iso_case_ntris(s_tri[cs]) : 0u;
+                    const uint32_t it = warp_incl_scan(nt, lane);
+                    const uint32_t ntb = __shfl_sync(0xffffffffu, it, 31);
+                    for (uint32_t q = 0; q < nt; ++q) list[it - nt + q] = (unsigned char)(lane | (q << 5));
+                    __syncwarp();
+                    for (uint32_t tb = 0; tb < ntb; tb += 32) {
+                        const uint32_t t = tb + lane;
+                        if (t < ntb) {
+                            const uint32_t tr = list[t];
+                            const uint32_t cr = cell[tr & 31u];
+                            const int q = (int)(tr >> 5);
+                            const int ci = (int)(cr & 511u);
+                            const uint2* mbc = mb + ((cr >> 9) & 3u) * 8 * W + (ci >> 5);
+                            const uint32_t corners = (uint32_t)(s_tri[cr >> 16] >> (12 * q)) & 0xfffu;
+                            const int bit = ci & 31;
+                            IndexT* o = tris + 3 * (tcur + t - tbase);
 #pragma unroll
-                        for (int c = 0; c < 3; ++c) {  // fe_edge_rel with its table row and offset precomputed
-                            const uint32_t nib = (corners >> (4 * c)) & 15u;
-                            const uint2 pm = mbc[(nib & 7u) * W];
-                            // popc of the mask's bits below bit + offset (the funnel shift clamps at 32)
-                            const int pos = bit + (int)(nib >> 3);
-                            const uint32_t rel = pm.y + __popc(__funnelshift_lc(0u, pm.x, 32 - pos));
-                            if constexpr (sizeof(IndexT) == 4)
-                                o[c] = (IndexT)((uint32_t)xs0 + rel);  // 32-bit ids: V < 2^32
-                            else
-                                o[c] = (IndexT)(xs0 + rel);
+                            for (int c = 0; c < 3; ++c) {  // fe_edge_rel with its table row and offset precomputed
+                                const uint32_t nib = (corners >> (4 * c)) & 15u;
+                                const uint2 pm = mbc[(nib & 7u) * W];
+                                // popc of the mask's bits below bit + offset (the funnel shift clamps at 32)
+                                const int pos = bit + (int)(nib >> 3);
+                                const uint32_t rel = pm.y + __popc(__funnelshift_lc(0u, pm.x, 32 - pos));
+                                if (MODE == kGenTri)  // the corner's MC id through the FE -> MC map
+                                    o[c] = (IndexT)__ldg(fe2mc + (xs0 + rel));
+                                else if constexpr (sizeof(IndexT) == 4)
+                                    o[c] = (IndexT)((uint32_t)xs0 + rel);  // 32-bit ids: V < 2^32
+                                else
+                                    o[c] = (IndexT)(xs0 + rel);
+                            }
                         }
                     }
+                    tcur += ntb;
                 }
-                tcur += ntb;
+                if (MODE == kGenMC) {
+                    // ---- the MC vertices the batch's cells own: cell order, then order of first appearance in
+                    // the cell's triangle list (marchingCubes/serial/main.cpp:139-177)
+                    const int cci = (int)(rec & 511u), cj = jw + (int)((rec >> 9) & 3u);
+                    const uint32_t own = live ? (mc_owned_edges(cci == 0, cj == 0, k == 0) & s_cut[cs]) : 0u;
+                    const uint32_t no = __popc(own);
+                    const uint32_t io = warp_incl_scan(no, lane);
+                    const uint32_t nob = __shfl_sync(0xffffffffu, io, 31);
+                    uint16_t* vl = reinterpret_cast<uint16_t*>(list);
+                    if (own) {
+                        const uint64_t ord = s_order[cs];
+                        uint32_t o = io - no;
+                        for (int q = 0; q < iso_case_ntris(ord); ++q) {
+                            const int ed = iso_case_edge(ord, q);
+                            if ((own >> ed) & 1u) vl[o++] = (uint16_t)(lane | (ed << 5));
+                        }
+                    }
+                    __syncwarp();
+                    for (uint32_t vb = 0; vb < nob; vb += 32) {
+                        const uint32_t v = vb + lane;
+                        if (v < nob) {
+                            const uint32_t vr = vl[v];
+                            const uint32_t cr = cell[vr & 31u];
+                            const int e12 = (int)(vr >> 5);
+                            const int i = (int)(cr & 511u), jc = jw + (int)((cr >> 9) & 3u);
+                            const unsigned long long id = tcur + v;
+                            if (k >= kemit) {  // cell rows below kemit belong to the slab below: map only
+                                int dx, dy, dz, axis;
+                                cube_edge_geometry(e12, dx, dy, dz, axis);
+                                put_mc_record(points, id - vbase, (uint32_t)(i + dx), (uint32_t)axis,
+                                              (uint32_t)(dx | (dy << 1) | (dz << 2)), (uint32_t)(jc + dy),
+                                              (uint32_t)(k + dz));
+                            }
+                            const uint2* mbc = mb + ((cr >> 9) & 3u) * 8 * W;
+                            fe2mc[xs0 + fe_edge_rel(mbc, W, e12, i >> 5, i & 31)] = (uint32_t)id;
+                        }
+                    }
+                    tcur += nob;
+                }
                 __syncwarp();  // the next batch overwrites the lists
             }
             __syncwarp();  // the next step overwrites mb
@@ -290,10 +347,12 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
     }
 }
 
-template <typename IndexT>
-void launch_gen_pairs_impl(const float* vol, const Grid& g, float iso, const CaseTables* cases, const FeBuffers& b,
-                           const CountPlan& cp, const GenPlan& p, int nsm, long long capV, long long capT,
-                           float* points, float* normals, IndexT* tris, int reverse, cudaStream_t s)
+// Rows of up to 16 words (gen_plan's fits, and W <= 16) in MODE over the
+// plan's planes [kbeg, kend).
+template <typename IndexT, int MODE>
+void launch_gen_pairs_impl(const Grid& g, const CaseTables* cases, const FeBuffers& b, const CountPlan& cp,
+                           const GenPlan& p, int nsm, long long capV, long long capT, float* points, IndexT* tris,
+                           int reverse, cudaStream_t s)
 {
     const int nzw = p.kend - p.kbeg;
     if (nzw <= 0) return;
@@ -313,13 +372,13 @@ void launch_gen_pairs_impl(const float* vol, const Grid& g, float iso, const Cas
     for (int a = 0; a < 3; ++a) rs.add[a] = p.add[a];
     unsigned int* work = reinterpret_cast<unsigned int*>(b.totals + 7);
     cudaMemsetAsync(work, 0, sizeof(unsigned int), s);
-    const int ws_bytes = (int)gen_pair_scratch_bytes(g.W, rpw);
+    const int ws_bytes = (int)gen_pair_scratch_bytes(g.W, rpw, MODE);
     const size_t smem = (size_t)kGenRows * ws_bytes;
-    auto kern = rpw == 4 ? k_gen_pairs<IndexT, 4> : k_gen_pairs<IndexT, 2>;
+    auto kern = rpw == 4 ? k_gen_pairs<IndexT, 4, MODE> : k_gen_pairs<IndexT, 2, MODE>;
     allow_smem(kern, smem);
-    kern<<<(unsigned)blocks, kThreads, smem, s>>>(b.bits, g, (int)KC, (int)npairs, nkc, p.kbeg, p.kend, p.vbase,
-                                                  p.tbase, ws_bytes, cases, b.rowcnt, rs, b.totals, work, capV, capT,
-                                                  points, tris, reverse);
+    kern<<<(unsigned)blocks, kThreads, smem, s>>>(b.bits, g, (int)KC, (int)npairs, nkc, p.kbeg, p.kend, p.kemit,
+                                                  p.vbase, p.tbase, ws_bytes, cases, b.rowcnt, rs, b.totals, work,
+                                                  capV, capT, points, tris, b.fe2mc, reverse);
 }
 
 }  // namespace iso

@@ -53,8 +53,7 @@ void launch_fe_gen_warps(const float* vol, const Grid& g, float iso, const CaseT
                          float* normals, IndexT* tris, int reverse, cudaStream_t s)
 {
     if (fe_writes_records(g, p))  // several rows per warp
-        launch_gen_pairs_impl<IndexT>(vol, g, iso, cases, b, cp, p, p.nsm, capV, capT, points, normals, tris,
-                                      reverse, s);
+        launch_gen_pairs_impl<IndexT, kGenFE>(g, cases, b, cp, p, p.nsm, capV, capT, points, tris, reverse, s);
     else
         launch_gen_warps_impl<kGenFE, IndexT>(vol, g, iso, cases, b, cp, p, capV, capT, points, normals, tris,
                                               reverse, s);

@@ -1,7 +1,9 @@
-// Marching Cubes pass 4 (warp-per-row kernels of gen_warps.cuh): vertex records
+// Marching Cubes pass 4 (the kernels of gen_pairs.cuh for rows of up to 16
+// words, else the warp-per-row kernels of gen_warps.cuh): vertex records
 // in owner order with the Flying Edges -> MC index map, the vertices from the
 // records (vertices.cuh), then the triangles with their corners mapped; and
 // the duplicate-free order in one pass.
+#include "gen_pairs.cuh"
 #include "gen_warps.cuh"
 #include "vertices.cuh"
 
@@ -11,8 +13,11 @@ void launch_mc_gen_warps(const float* vol, const Grid& g, float iso, const CaseT
                          const CountPlan& cp, const GenPlan& p, long long capV, long long capT, float* points,
                          float* normals, int reverse, cudaStream_t s)
 {
-    launch_gen_warps_impl<kGenMC, uint32_t>(vol, g, iso, cases, b, cp, p, capV, capT, points, normals, nullptr,
-                                            reverse, s);
+    if (g.W <= 16 && p.nsm > 0)  // several rows per warp
+        launch_gen_pairs_impl<uint32_t, kGenMC>(g, cases, b, cp, p, p.nsm, capV, capT, points, nullptr, reverse, s);
+    else
+        launch_gen_warps_impl<kGenMC, uint32_t>(vol, g, iso, cases, b, cp, p, capV, capT, points, normals, nullptr,
+                                                reverse, s);
 }
 
 bool launch_mc_vertices(const float* vol, const Grid& g, float iso, const FeBuffers& b, const GenPlan& p,
@@ -27,8 +32,11 @@ template <typename IndexT>
 void launch_mc_tri_warps(const Grid& g, const CaseTables* cases, const FeBuffers& b, const CountPlan& cp,
                          const GenPlan& p, long long capV, long long capT, IndexT* tris, cudaStream_t s)
 {
-    launch_gen_warps_impl<kGenTri, IndexT>(nullptr, g, 0.f, cases, b, cp, p, capV, capT, nullptr, nullptr, tris, 0,
-                                           s);
+    if (g.W <= 16 && p.nsm > 0)  // several rows per warp
+        launch_gen_pairs_impl<IndexT, kGenTri>(g, cases, b, cp, p, p.nsm, capV, capT, nullptr, tris, 0, s);
+    else
+        launch_gen_warps_impl<kGenTri, IndexT>(nullptr, g, 0.f, cases, b, cp, p, capV, capT, nullptr, nullptr, tris,
+                                               0, s);
 }
 
 template <typename IndexT>
