@@ -348,6 +348,8 @@ void enqueue_generate(iso_ctx* ctx, iso_algorithm algo, const float* vol, const 
             iso::launch_dup_gen_warps<uint64_t>(vol, g, iso, ctx->d_cases, b, pl.cp, pl.gp, capV, capT, out->points,
                                                 out->normals, static_cast<uint64_t*>(out->tris), ctx->reverse, s);
         pm.mark(ISO_PASS_MC_VERTICES);
+        if (iso::launch_dup_vertices(vol, g, iso, b, pl.gp, capV, capT, out->points, out->normals, s))
+            pm.mark(ISO_PASS_VERTICES);
     } else {
         const long long capM = capV < 0xffffffffll ? capV : 0xffffffffll;  // fe2mc holds 32-bit ids
         if (pl.gp.fits)

@@ -1,9 +1,12 @@
-// Pass 4 on sm_103a (included by gen_warps_fe.cu and gen_warps_mc.cu).
+// Pass 4 on sm_103a, one grid row per warp (included by gen_warps_fe.cu,
+// gen_pairs.cuh and gen_warps_mc.cu): rows of 17-32 words, and the
+// duplicate-free Marching Cubes order; rows of up to 16 words run on the
+// multi-row kernel of gen_pairs.cuh, which reuses the helpers here.
 //
-// A CTA owns a block of J = 8 grid rows (j0 .. j0+7, one warp per row) and a
-// run of KC planes [kb, ke); each warp marches along z on its own (the only
-// CTA barrier stages the case tables).  Volume values are read through L1
-// from global memory; the count pass's bit rows say where the surface is.
+// One wave of CTAs of 8 warps; every warp takes (grid row j, run of KC planes)
+// work items from a counter and marches along z on its own (the only CTA
+// barrier stages the case tables).  The count pass's bit rows say where the
+// surface is.
 //
 // Per step a warp handles grid row (j, k) with one 32-bit word of the bit
 // mask per lane (the bit words and row starts of the next step load while
@@ -16,15 +19,19 @@
 //   FE  : the row's vertices, one per lane: a shuffle binary search maps the
 //         lane's vertex rank to a word and __fns to a bit; the vertex goes to
 //         its axis' queue (shared memory), and every full batch of 32 is
-//         computed by the axis' own code (no divergence by axis, full lanes);
-//   the active cells of the cell row are compacted, 32 at a time, into the
-//   warp's cell list; each cell lane computes its cube case, then
+//         computed by the axis' own code from the volume (no divergence by
+//         axis, full lanes);
+//   the active cells of the cell row, 32 at a time: each cell lane finds its
+//   cell by a shuffle binary search over the lanes' counts and computes its
+//   cube case, then
 //   FE, TRI: the cells' triangles are listed as (cell, triangle) pairs and
 //         written one triangle per lane, consecutive lanes storing consecutive
 //         triangles (TRI, without volume, maps the corners through the
 //         Flying Edges -> MC index map);
-//   MC  : the vertices the cells own, in owner-cell / first-appearance order
-//         (marchingCubes/serial/main.cpp:139-177), one per lane, and that map.
+//   MC, Dup: the vertices the cells own, in owner-cell / first-appearance
+//         order (marchingCubes/serial/main.cpp:139-177), one per lane: their
+//         ids (owner order, or the global-edge-index order for Dup) and a
+//         record each for k_vertices (vertices.cuh); MC also the map.
 #pragma once
 #include <cmath>
 #include <type_traits>
@@ -105,69 +112,6 @@ __device__ __forceinline__ float grad_axis(float prev, float here, float next, i
     }
     const float sp = a == 0 ? gs.sp[0] : (a == 1 ? gs.sp[1] : gs.sp[2]);
     return fdiv(num, one ? sp : fmul(2.0f, sp));
-}
-
-// The four planes around step k (index dp = plane - k + 1: k-1, k, k+1,
-// k+2), each addressed from row jlo: the staged planes in shared memory, the
-// others in global memory.  Planes outside the grid alias a valid one and
-// are never read.
-struct Planes {
-    const float* p0;
-    const float* p1;
-    const float* p2;
-    const float* p3;
-    int jlo, nx;
-    __device__ __forceinline__ float operator()(int i, int j, int dp) const
-    {
-        const float* b = dp == 0 ? p0 : (dp == 1 ? p1 : (dp == 2 ? p2 : p3));
-        return b[(j - jlo) * nx + i];
-    }
-};
-
-// edge_vertex() of iso_device.cuh through the planes: the vertex on the edge
-// from P0 = (i, j, plane kk = k + dp - 1) along `axis`, computed by the cube
-// with base (ci, cj, ck).  The gradients are evaluated in the frame
-// (a, b, c) = (axis, axis+1, axis+2), so lanes with different axes run the
-// same instructions; the two endpoints share the edge's own values.
-__device__ __forceinline__ void vertex_on_edge(const Planes& pl, const Grid& g, const GradScale& gs, float iso,
-                                               int axis, int i, int j, int dp, int kk, int ci, int cj, int ck,
-                                               float3& pos, float3& nrm)
-{
-    const int ex = axis == 0, ey = axis == 1, ez = axis == 2;
-    const int bx = axis == 2, by = axis == 0, bz = axis == 1;  // b = axis+1
-    const int cx = axis == 1, cy = axis == 2, cz = axis == 0;  // c = axis+2
-    const int ab = axis == 2 ? 0 : axis + 1, ac = axis == 0 ? 2 : axis - 1;
-    const int i1 = i + ex, j1 = j + ey, dp1 = dp + ez, kk1 = kk + ez;
-    const int pa = axis == 0 ? i : (axis == 1 ? j : kk);
-    const int pb = axis == 0 ? j : (axis == 1 ? kk : i);
-    const int pc = axis == 0 ? kk : (axis == 1 ? i : j);
-    const int na = axis == 0 ? g.nx : (axis == 1 ? g.ny : g.nz);
-    const int nb = axis == 0 ? g.ny : (axis == 1 ? g.nz : g.nx);
-    const int nc = axis == 0 ? g.nz : (axis == 1 ? g.nx : g.ny);
-    const float v0 = pl(i, j, dp);
-    const float v1 = pl(i1, j1, dp1);
-    const float am = pa > 0 ? pl(i - ex, j - ey, dp - ez) : 0.f;
-    const float ap = pa + 1 < na - 1 ? pl(i1 + ex, j1 + ey, dp1 + ez) : 0.f;
-    const bool blo = pb > 0, bhi = pb < nb - 1, clo = pc > 0, chi = pc < nc - 1;
-    const float b0m = blo ? pl(i - bx, j - by, dp - bz) : 0.f;
-    const float b0p = bhi ? pl(i + bx, j + by, dp + bz) : 0.f;
-    const float c0m = clo ? pl(i - cx, j - cy, dp - cz) : 0.f;
-    const float c0p = chi ? pl(i + cx, j + cy, dp + cz) : 0.f;
-    const float b1m = blo ? pl(i1 - bx, j1 - by, dp1 - bz) : 0.f;
-    const float b1p = bhi ? pl(i1 + bx, j1 + by, dp1 + bz) : 0.f;
-    const float c1m = clo ? pl(i1 - cx, j1 - cy, dp1 - cz) : 0.f;
-    const float c1p = chi ? pl(i1 + cx, j1 + cy, dp1 + cz) : 0.f;
-    const float w = fdiv(fsub(iso, v0), fsub(v1, v0));
-    pos.x = lerp_ref(cube_coord(ci, i - ci, g.zp[0], g.sp[0]), cube_coord(ci, i1 - ci, g.zp[0], g.sp[0]), w);
-    pos.y = lerp_ref(cube_coord(cj, j - cj, g.zp[1], g.sp[1]), cube_coord(cj, j1 - cj, g.zp[1], g.sp[1]), w);
-    pos.z = lerp_ref(cube_coord(ck, kk - ck, g.zp[2], g.sp[2]), cube_coord(ck, kk1 - ck, g.zp[2], g.sp[2]), w);
-    const float ga =
-        lerp_ref(grad_axis(am, v0, v1, pa, na, axis, gs), grad_axis(v0, v1, ap, pa + 1, na, axis, gs), w);
-    const float gb = lerp_ref(grad_axis(b0m, v0, b0p, pb, nb, ab, gs), grad_axis(b1m, v1, b1p, pb, nb, ab, gs), w);
-    const float gc = lerp_ref(grad_axis(c0m, v0, c0p, pc, nc, ac, gs), grad_axis(c1m, v1, c1p, pc, nc, ac, gs), w);
-    nrm.x = axis == 0 ? ga : (axis == 1 ? gc : gb);
-    nrm.y = axis == 1 ? ga : (axis == 2 ? gc : gb);
-    nrm.z = axis == 2 ? ga : (axis == 0 ? gc : gb);
 }
 
 // Gradient components at one point from its six neighbours (grad_component
@@ -541,16 +485,6 @@ __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
                 }
             }
             __syncwarp();
-            Planes pl{};
-            if (OWNED) {  // planes k-1 .. k+2; those outside the grid alias plane k
-                pl.p1 = plane_ptr(k);
-                pl.p0 = k > 0 ? plane_ptr(k - 1) : pl.p1;
-                pl.p2 = hasZ ? plane_ptr(k + 1) : pl.p1;
-                pl.p3 = k + 2 < g.nz ? plane_ptr(k + 2) : pl.p1;
-                pl.jlo = jlo;
-                pl.nx = g.nx;
-            }
-
             if (MODE == kGenFE) {
                 // ---- vertices of grid row (j, k): x, y then z sections
                 const uint32_t nv = nxA + nyA + nzA;
@@ -699,16 +633,10 @@ __global__ void __launch_bounds__(kThreads, kGenCtasPerSm) k_gen_warps(
                                 if (k >= kemit) {  // cell rows below kemit belong to the slab below: map only
                                     int dx, dy, dz, axis;
                                     cube_edge_geometry(e12, dx, dy, dz, axis);
-                                    if (MODE == kGenMC) {  // k_vertices<true> computes it from the record
-                                        put_mc_record(points, id - vbase, (uint32_t)(i + dx), (uint32_t)axis,
-                                                      (uint32_t)(dx | (dy << 1) | (dz << 2)), (uint32_t)(j + dy),
-                                                      (uint32_t)(k + dz));
-                                    } else {
-                                        float3 p, n;
-                                        vertex_on_edge(pl, g, gs, iso, axis, i + dx, j + dy, 1 + dz, k + dz, i, j, k, p,
-                                                       n);
-                                        store_vertex(points, normals, id - vbase, p, n);
-                                    }
+                                    // the record kernel (k_vertices) computes the vertex from its record
+                                    put_mc_record(points, id - vbase, (uint32_t)(i + dx), (uint32_t)axis,
+                                                  (uint32_t)(dx | (dy << 1) | (dz << 2)), (uint32_t)(j + dy),
+                                                  (uint32_t)(k + dz));
                                 }
                                 if (MODE == kGenMC) fe2mc[xsA + fe_edge_rel(mb, W, e12, i >> 5, i & 31)] = (uint32_t)id;
                             }

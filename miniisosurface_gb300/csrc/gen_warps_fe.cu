@@ -63,7 +63,7 @@ bool launch_fe_vertices(const float* vol, const Grid& g, float iso, const FeBuff
                         long long capV, long long capT, float* points, float* normals, cudaStream_t s)
 {
     if (!fe_writes_records(g, p)) return false;
-    launch_vertices_impl<false>(vol, g, iso, b, p.kbeg, p.kend, p.nsm, capV, capT, points, normals, s);
+    launch_vertices_impl<false, 0>(vol, g, iso, b, p.kbeg, p.kend, p.nsm, capV, capT, points, normals, s);
     return true;
 }
 

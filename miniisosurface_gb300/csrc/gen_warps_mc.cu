@@ -24,7 +24,15 @@ bool launch_mc_vertices(const float* vol, const Grid& g, float iso, const FeBuff
                         long long capV, long long capT, float* points, float* normals, cudaStream_t s)
 {
     if (p.nsm <= 0) return false;
-    launch_vertices_impl<true>(vol, g, iso, b, p.kemit, p.kend, p.nsm, capV, capT, points, normals, s);
+    launch_vertices_impl<true, 2>(vol, g, iso, b, p.kemit, p.kend, p.nsm, capV, capT, points, normals, s);
+    return true;
+}
+
+bool launch_dup_vertices(const float* vol, const Grid& g, float iso, const FeBuffers& b, const GenPlan& p,
+                         long long capV, long long capT, float* points, float* normals, cudaStream_t s)
+{
+    if (p.nsm <= 0) return false;
+    launch_vertices_impl<true, 0>(vol, g, iso, b, g.kr, g.ke, p.nsm, capV, capT, points, normals, s);
     return true;
 }
 

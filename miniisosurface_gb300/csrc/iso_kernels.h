@@ -91,6 +91,9 @@ bool launch_fe_vertices(const float* vol, const Grid& g, float iso, const FeBuff
 // nothing launched, the plan cannot run it)
 bool launch_mc_vertices(const float* vol, const Grid& g, float iso, const FeBuffers& b, const GenPlan& p,
                         long long capV, long long capT, float* points, float* normals, cudaStream_t s);
+// The duplicate-free order's vertices from the records launch_dup_gen_warps wrote (whole grids)
+bool launch_dup_vertices(const float* vol, const Grid& g, float iso, const FeBuffers& b, const GenPlan& p,
+                         long long capV, long long capT, float* points, float* normals, cudaStream_t s);
 void launch_mc_gen_warps(const float* vol, const Grid& g, float iso, const CaseTables* cases, const FeBuffers& b,
                          const CountPlan& cp, const GenPlan& p, long long capV, long long capT, float* points,
                          float* normals, int reverse, cudaStream_t s);

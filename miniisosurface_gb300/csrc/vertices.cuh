@@ -26,11 +26,12 @@ __device__ __forceinline__ void put_vertex_record(float* points, unsigned long l
 }
 
 // edge_vertex() of iso_device.cuh for the edge from P0 = (i, j, kk) along
-// axis a, placed by the cube with base (ci, cj, ck), with the operations of
-// vertex_axis<a> (Flying Edges) and vertex_on_edge (Marching Cubes) on the
-// same operands, so bit-identical to them; written once for all three axes
-// with the axis as data: a warp of consecutive vertex ids mixes axes without
-// diverging.
+// axis a, placed by the cube with base (ci, cj, ck): the gradients at both
+// ends from their six neighbours (grad_axis per axis, the edge's own values
+// along a) and the position from the cube's corner coordinates, with the
+// operations of vertex_axis<a> on the same operands, so bit-identical to it
+// and to edge_vertex; written once for all three axes with the axis as data: a
+// warp of consecutive vertex ids mixes axes without diverging.
 __device__ __forceinline__ void vertex_any_axis(const float* __restrict__ vol, const Grid& g, const GradScale& gs,
                                                 float iso, int a, int i, int j, int kk, int ci, int cj, int ck,
                                                 float3& pos, float3& nrm)
@@ -77,18 +78,19 @@ __device__ __forceinline__ uint2 vertex_record(const float* points, unsigned lon
 }
 
 // The vertices owned by the rows of planes [kbeg, kend) -- Flying Edges: grid
-// rows (starts component 0); Marching Cubes: cell rows (component 2) -- one
-// thread each, slot v = vertex vbase + v.  The capacity test is the generate
-// kernels': when it fails they wrote no record and nothing is read here.
-template <bool MC>
+// rows (starts component COMP = 0); Marching Cubes: cell rows (COMP = 2; the
+// duplicate-free order, whole grids only, counts all of them with COMP = 0)
+// -- one thread each, slot v = vertex vbase + v.  MC: the records carry the
+// owner cell.  The capacity test is the generate kernels': when it fails they
+// wrote no record and nothing is read here.
+template <bool MC, int COMP>
 __global__ void __launch_bounds__(kThreads, vertex_ctas_per_sm(MC))
     k_vertices(const float* __restrict__ vol, Grid g, GradScale gs, float iso, int kbeg, int kend,
                const unsigned long long* __restrict__ starts, const unsigned long long* __restrict__ totals,
                long long capV, long long capT, float* __restrict__ points, float* __restrict__ normals)
 {
     if ((long long)totals[0] > capV || (long long)totals[1] > capT) return;
-    constexpr int comp = MC ? 2 : 0;
-    auto first = [&](int p) { return p < g.ke ? starts[comp * g.R + (long long)(p - g.kr) * g.ny] : totals[comp]; };
+    auto first = [&](int p) { return p < g.ke ? starts[COMP * g.R + (long long)(p - g.kr) * g.ny] : totals[COMP]; };
     const unsigned long long n = first(kend) - first(kbeg);
     const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
     unsigned long long v = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -123,14 +125,14 @@ __global__ void __launch_bounds__(kThreads, vertex_ctas_per_sm(MC))
 }
 
 // Vertices of the rows of planes [k0, k1) from their records.
-template <bool MC>
+template <bool MC, int COMP>
 inline void launch_vertices_impl(const float* vol, const Grid& g, float iso, const FeBuffers& b, int k0, int k1,
                                  int nsm, long long capV, long long capT, float* points, float* normals,
                                  cudaStream_t s)
 {
     if (k1 <= k0) return;
     const unsigned blocks = (unsigned)nsm * vertex_ctas_per_sm(MC);
-    k_vertices<MC><<<blocks, kThreads, 0, s>>>(vol, g, make_grad_scale(g), iso, k0, k1, b.starts, b.totals, capV,
+    k_vertices<MC, COMP><<<blocks, kThreads, 0, s>>>(vol, g, make_grad_scale(g), iso, k0, k1, b.starts, b.totals, capV,
                                                capT, points, normals);
 }
 
