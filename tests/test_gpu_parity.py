@@ -100,6 +100,23 @@ def test_wide_rows_multi_chunk(M):
     both(M, vol, -0.05)
 
 
+@pytest.mark.parametrize("dims", [(600, 9, 7), (1000, 7, 6), (1024, 5, 5)])
+def test_rows_of_17_to_32_words(M, dims):
+    """Rows of 545-1024 points: one grid row per warp in pass 4 (Flying Edges
+    vertices through the per-axis queues), the multi-word count kernels."""
+    vol = M.generate_value_noise(dims, 4, 16, seed=sum(dims))
+    both(M, vol, 0.0)
+
+
+@pytest.mark.parametrize("dims", [(8, 6, 1500), (20, 3, 4000)])
+def test_tall_grids(M, dims):
+    """Thousands of planes: many plane runs of work items, plane numbers well
+    past the first bytes of the vertex records."""
+    rng = np.random.default_rng(dims[2])
+    vol = rng.standard_normal(dims[::-1]).astype(np.float32)
+    both(M, vol, 0.1, (1.0, 0.5, 0.25), (0.0, 1.0, -3.0))
+
+
 @pytest.mark.parametrize("nx", [252, 256, 260, 508, 512])
 def test_row_width_boundaries(M, nx):
     """Rows at the edges of the kernel choices: up to 8 words the count and
