@@ -239,20 +239,21 @@ __device__ __forceinline__ uint32_t ge_mask(float v, float iso)
     return d;
 }
 
-// Word l16 (points 32*l16 .. 32*l16+31) of a row of nq float4 in shared
-// memory, built by one lane alone: at step u it reads float4 (u + l16) & 7 of
-// its word into bits 4u .. 4u+3 (eight consecutive lanes read eight different
-// bank groups), and the word is rotated into place at the end.  FULL: the
-// row has all 16 words (nx = 512).
+// Word wd (points 32*wd .. 32*wd+31) of a row of nq float4 in shared
+// memory, built by one lane alone: at step u it reads float4 (u + rot) & 7 of
+// its word into bits 4u .. 4u+3 (rot = the lane's place in its group of eight,
+// so eight consecutive lanes read eight different bank groups), and the word
+// is rotated into place at the end.  FULL: every lane's word lies inside the
+// row.
 template <bool FULL>
-__device__ __forceinline__ uint32_t row_word(const float* row, int nq, int l16, float iso)
+__device__ __forceinline__ uint32_t row_word(const float* row, int nq, int wd, int rot, float iso)
 {
-    const float4* r4 = reinterpret_cast<const float4*>(row) + 8 * l16;
-    const int nv = FULL ? 8 : nq - 8 * l16;  // float4 of the word inside the row
+    const float4* r4 = reinterpret_cast<const float4*>(row) + 8 * wd;
+    const int nv = FULL ? 8 : nq - 8 * wd;  // float4 of the word inside the row
     uint32_t w = 0u;
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
-        const int q = (u + l16) & 7;
+        const int q = (u + rot) & 7;
         if (FULL || q < nv) {
             const float4 v = r4[q];
             w |= ge_mask(v.x, iso) & (1u << (4 * u));
@@ -261,7 +262,7 @@ __device__ __forceinline__ uint32_t row_word(const float* row, int nq, int l16, 
             w |= ge_mask(v.w, iso) & (8u << (4 * u));
         }
     }
-    return __funnelshift_l(w, w, 4 * (l16 & 7));
+    return __funnelshift_l(w, w, 4 * rot);
 }
 
 // Rows of up to 16 words (nx <= 512), 16-byte aligned, several per warp so
@@ -273,7 +274,7 @@ __device__ __forceinline__ uint32_t row_word(const float* row, int nq, int l16, 
 // words of plane k+1 are taken from the buffer before the copy of plane k+2
 // is issued into it, so the copy runs while step k is counted; no register
 // holds raw values across a step.
-// RPW grid rows per warp (2: rows of up to 16 words, 4: up to 8), LPR =
+// RPW grid rows per warp (2: rows of up to 16 words, 4: up to 8, 8: up to 4), LPR =
 // 32 / RPW lanes per row; a warp's rows jw .. jw+RPW-1 read rows jw .. jw+RPW
 // of every plane, RPW + 1 rows of its buffer.  FULL: every lane's word is
 // inside the row (nx = 32 * LPR).
@@ -320,17 +321,21 @@ __global__ void __launch_bounds__(kThreads, 4) k_count_tma(const float* __restri
         const bool done = mbar_wait(bar, phase);
         if (!__all_sync(0xffffffffu, done)) return false;
         phase ^= 1u;
-        wa = row_ok ? row_word<FULL>(buf + h * g.nx, nq, lw, iso) : 0u;
-        wb = hasY ? row_word<FULL>(buf + (h + 1) * g.nx, nq, lw, iso) : 0u;
+        wa = row_ok ? row_word<FULL>(buf + h * g.nx, nq, lw, lane & 7, iso) : 0u;
+        wb = hasY ? row_word<FULL>(buf + (h + 1) * g.nx, nq, lw, lane & 7, iso) : 0u;
         __syncwarp();  // every lane has read the buffer before it is refilled
         return true;
     };
-    // per-row totals: rows 0,1 (and 2,3) of the warp in the two 16-bit halves of one reduction
+    // per-row totals: rows 2p, 2p+1 of the warp in the two 16-bit halves of reduction p
     auto row_sum = [&](uint32_t v) -> uint32_t {
         const int sh = 16 * (h & 1);
-        const uint32_t lo = __reduce_add_sync(0xffffffffu, h < 2 ? v << sh : 0u);
-        const uint32_t hi = RPW > 2 ? __reduce_add_sync(0xffffffffu, h >= 2 ? v << sh : 0u) : 0u;
-        return ((h < 2 ? lo : hi) >> sh) & 0xffffu;
+        uint32_t mine = 0u;
+#pragma unroll
+        for (int p = 0; p < RPW / 2; ++p) {
+            const uint32_t s = __reduce_add_sync(0xffffffffu, (h >> 1) == p ? v << sh : 0u);
+            if ((h >> 1) == p) mine = s;
+        }
+        return (mine >> sh) & 0xffffu;
     };
 
     uint32_t A = 0, B = 0, Cw = 0, Dw = 0;
@@ -650,8 +655,8 @@ static void count_launch(const CountPlan& p, const float* vol, const Grid& g, fl
     const unsigned blocks = (unsigned)(p.nyb * p.nkc);
     const bool vec4 = g.W <= 64 && (g.nx % 4 == 0) && ((reinterpret_cast<uintptr_t>(vol) & 15) == 0);
     uint2* trims = p.trims ? b.trims : nullptr;  // the kernels skip the trims when null
-    if (vec4 && g.W <= 16) {  // 4 rows per warp up to 8 words, else 2; planes through the TMA engine
-        const int rpw = g.W <= 8 ? 4 : 2;
+    if (vec4 && g.W <= 16) {  // 8 rows per warp up to 4 words, 4 up to 8, else 2; planes through TMA
+        const int rpw = g.W <= 4 ? 8 : (g.W <= 8 ? 4 : 2);
         const int rows = kCountRows * rpw;
         const int nyb2 = (g.ny + rows - 1) / rows;
         const unsigned blocks2 = (unsigned)(nyb2 * p.nkc);
@@ -664,7 +669,10 @@ static void count_launch(const CountPlan& p, const float* vol, const Grid& g, fl
         kern<<<blocks2, kThreads, smem, s>>>(vol, g, iso, p.KC, nyb2, b.rowcnt, trims, b.mccnt, b.bits,         \
                                              b.totals + 3);                                                    \
     }
-        if (rpw == 4) {
+        if (rpw == 8) {
+            if (nq == 32) ISO_TMA(true, 8)
+            else ISO_TMA(false, 8)
+        } else if (rpw == 4) {
             if (nq == 64) ISO_TMA(true, 4)
             else ISO_TMA(false, 4)
         } else {

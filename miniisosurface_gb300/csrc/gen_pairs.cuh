@@ -1,7 +1,8 @@
 // Flying Edges pass 4 (FlyingEdgesAlgorithm.cpp:271-500) for rows of up to
 // 16 words (nx <= 512), several grid rows per warp (included by
-// gen_warps_fe.cu): two for rows of 9-16 words, four for rows of up to 8, so
-// that no lane idles on words past a short row.
+// gen_warps_fe.cu and gen_warps_mc.cu): two for rows of 9-16 words, four for
+// rows of 5-8, eight for rows of up to 4, so that no lane idles on words past
+// a short row.
 //
 // Lanes LPR*h .. LPR*h + LPR-1 (LPR = 32 / rows per warp) hold the words of
 // grid row j = jw + h.  Rows (jw, k), (jw+1, k), ... are neighbours in the
@@ -42,7 +43,7 @@ __host__ __device__ inline size_t gen_pair_scratch_bytes(int W, int RPW, int mod
 // run of KC planes -- from the counter `work` until none is left, so no warp
 // waits for another and no CTA stays resident for its slowest warp.  Item q is
 // row group q % ngroups of plane run q / ngroups (runs walked backwards when
-// `reverse`).  RPW = 2 for rows of up to 16 words, 4 for up to 8: lanes
+// `reverse`).  RPW = 2 for rows of up to 16 words, 4 for up to 8, 8 for up to 4: lanes
 // LPR*h .. LPR*h + LPR-1 hold the words of row jw + h.
 // MODE kGenFE: Flying Edges vertex records and triangles.  kGenMC: the
 // Marching Cubes vertices the cells own (marchingCubes/serial/main.cpp:
@@ -119,38 +120,38 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
             wa = (in && okp) ? __ldg(&bits[r * W + lw]) : 0u;
             wb = (in && okp && hasY) ? __ldg(&bits[(r + 1) * W + lw]) : 0u;
         };
-        // Row starts of step p, lanes 0..5 of each row's lanes: the first
-        // vertex of rows A = (j,p), B = (j+1,p), C = (j,p+1), D = (j+1,p+1), the
-        // first triangle of cell row A, the x + y cuts of row B.
-        auto load_starts = [&](int p) -> unsigned long long {
+        // Row starts of step p, in lanes 0..3 of each row's lanes: s1 = the
+        // first vertex of rows A = (j,p), B = (j+1,p), C = (j,p+1), D = (j+1,p+1);
+        // s2 = the first triangle (kGenMC: owned MC vertex) of cell row A (lane 0)
+        // and the x + y cuts of row B (lane 1).
+        auto load_starts = [&](int p, unsigned long long& s1, unsigned long long& s2) {
             const int dk = (lw >> 1) & 1, dj = lw & 1;
             const bool hasZp = p + 1 < g.ke;
-            bool ok = row_ok && lw < 6;
-            if (lw < 4) ok = ok && (dj == 0 || hasY) && (dk == 0 || hasZp);
-            if (lw == 5) ok = ok && hasY;
-            if (!ok) return 0ull;
             const long long rA = (long long)(p - g.kr) * g.ny + j;
-            if (lw == 5) {
+            s1 = s2 = 0ull;
+            if (row_ok && lw < 4 && (dj == 0 || hasY) && (dk == 0 || hasZp))
+                s1 = rs.get(rA + (long long)dk * g.ny + dj, 0);
+            if (row_ok && lw == 0) s2 = rs.get(rA, MODE == kGenMC ? 2 : 1);
+            if (row_ok && lw == 1 && hasY) {
                 const uint2 c = __ldg(reinterpret_cast<const uint2*>(&rowcnt[rA + 1]));
-                return (unsigned long long)c.x + c.y;
+                s2 = (unsigned long long)c.x + c.y;
             }
-            const long long r = lw < 4 ? rA + (long long)dk * g.ny + dj : rA;
-            return rs.get(r, lw < 4 ? 0 : (MODE == kGenMC ? 2 : 1));
         };
 
         uint32_t wA = 0, wB = 0, wC = 0, wD = 0;
         load_words(kb, wA, wB);
         load_words(kb + 1, wC, wD);
-        unsigned long long st = load_starts(kb);
+        unsigned long long st, st2;
+        load_starts(kb, st, st2);
 
         for (int k = kb; k < ke; ++k) {
             const bool hasZ = k + 1 < g.nz;
             // the next step's words and starts, in flight while this step runs
             uint32_t nC = 0, nD = 0;
-            unsigned long long nst = 0;
+            unsigned long long nst = 0, nst2 = 0;
             if (k + 1 < ke) {
                 load_words(k + 2, nC, nD);
-                nst = load_starts(k + 1);
+                load_starts(k + 1, nst, nst2);
             }
             const bool cellrow = hasY && hasZ;
             RowWords rw;
@@ -186,9 +187,9 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
             const uint32_t dB = (uint32_t)(__shfl_sync(0xffffffffu, st, 1, LPR) - xsA);
             const uint32_t dC = (uint32_t)(__shfl_sync(0xffffffffu, st, 2, LPR) - xsA);
             const uint32_t dD = (uint32_t)(__shfl_sync(0xffffffffu, st, 3, LPR) - xsA);
-            const uint32_t cntB = (uint32_t)__shfl_sync(0xffffffffu, st, 5, LPR);
+            const uint32_t cntB = (uint32_t)__shfl_sync(0xffffffffu, st2, 1, LPR);
             // first triangle (kGenMC: first owned MC vertex) of cell row jw
-            const unsigned long long ts0 = __shfl_sync(0xffffffffu, st, 4);
+            const unsigned long long ts0 = __shfl_sync(0xffffffffu, st2, 0);
             const uint32_t nxA = t0 & 0xffffu, nyA = t2 & 0xffffu, nxC = t1 & 0xffffu;
             const uint32_t off = (uint32_t)(xsA - xs0);  // the vertices of rows jw .. j-1
             if (in) {  // first ids of the word's cut edges, relative to xs0
@@ -274,7 +275,7 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
                             const uint32_t cr = cell[tr & 31u];
                             const int q = (int)(tr >> 5);
                             const int ci = (int)(cr & 511u);
-                            const uint2* mbc = mb + ((cr >> 9) & 3u) * 8 * W + (ci >> 5);
+                            const uint2* mbc = mb + ((cr >> 9) & 7u) * 8 * W + (ci >> 5);
                             const uint32_t corners = (uint32_t)(s_tri[cr >> 16] >> (12 * q)) & 0xfffu;
                             const int bit = ci & 31;
                             IndexT* o = tris + 3 * (tcur + t - tbase);
@@ -299,7 +300,7 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
                 if (MODE == kGenMC) {
                     // ---- the MC vertices the batch's cells own: cell order, then order of first appearance in
                     // the cell's triangle list (marchingCubes/serial/main.cpp:139-177)
-                    const int cci = (int)(rec & 511u), cj = jw + (int)((rec >> 9) & 3u);
+                    const int cci = (int)(rec & 511u), cj = jw + (int)((rec >> 9) & 7u);
                     const uint32_t own = live ? (mc_owned_edges(cci == 0, cj == 0, k == 0) & s_cut[cs]) : 0u;
                     const uint32_t no = __popc(own);
                     const uint32_t io = warp_incl_scan(no, lane);
@@ -320,7 +321,7 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
                             const uint32_t vr = vl[v];
                             const uint32_t cr = cell[vr & 31u];
                             const int e12 = (int)(vr >> 5);
-                            const int i = (int)(cr & 511u), jc = jw + (int)((cr >> 9) & 3u);
+                            const int i = (int)(cr & 511u), jc = jw + (int)((cr >> 9) & 7u);
                             const unsigned long long id = tcur + v;
                             if (k >= kemit) {  // cell rows below kemit belong to the slab below: map only
                                 int dx, dy, dz, axis;
@@ -329,7 +330,7 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
                                               (uint32_t)(dx | (dy << 1) | (dz << 2)), (uint32_t)(jc + dy),
                                               (uint32_t)(k + dz));
                             }
-                            const uint2* mbc = mb + ((cr >> 9) & 3u) * 8 * W;
+                            const uint2* mbc = mb + ((cr >> 9) & 7u) * 8 * W;
                             fe2mc[xs0 + fe_edge_rel(mbc, W, e12, i >> 5, i & 31)] = (uint32_t)id;
                         }
                     }
@@ -343,6 +344,7 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
             wC = nC;
             wD = nD;
             st = nst;
+            st2 = nst2;
         }
     }
 }
@@ -357,7 +359,7 @@ void launch_gen_pairs_impl(const Grid& g, const CaseTables* cases, const FeBuffe
     const int nzw = p.kend - p.kbeg;
     if (nzw <= 0) return;
     // items of KC planes: about four per warp of one wave, at least 4 planes
-    const int rpw = g.W <= 8 ? 4 : 2;
+    const int rpw = g.W <= 4 ? 8 : (g.W <= 8 ? 4 : 2);
     const long long npairs = (g.ny + rpw - 1) / rpw;  // row groups
     const long long warps = (long long)nsm * kGenPairCtasPerSm * kGenRows;
     long long KC = (npairs * nzw + 4 * warps - 1) / (4 * warps);
@@ -374,7 +376,8 @@ void launch_gen_pairs_impl(const Grid& g, const CaseTables* cases, const FeBuffe
     cudaMemsetAsync(work, 0, sizeof(unsigned int), s);
     const int ws_bytes = (int)gen_pair_scratch_bytes(g.W, rpw, MODE);
     const size_t smem = (size_t)kGenRows * ws_bytes;
-    auto kern = rpw == 4 ? k_gen_pairs<IndexT, 4, MODE> : k_gen_pairs<IndexT, 2, MODE>;
+    auto kern = rpw == 8 ? k_gen_pairs<IndexT, 8, MODE>
+                         : (rpw == 4 ? k_gen_pairs<IndexT, 4, MODE> : k_gen_pairs<IndexT, 2, MODE>);
     allow_smem(kern, smem);
     kern<<<(unsigned)blocks, kThreads, smem, s>>>(b.bits, g, (int)KC, (int)npairs, nkc, p.kbeg, p.kend, p.kemit,
                                                   p.vbase, p.tbase, ws_bytes, cases, b.rowcnt, rs, b.totals, work,
