@@ -265,7 +265,55 @@ __device__ __forceinline__ uint32_t row_word(const float* row, int nq, int wd, i
     return __funnelshift_l(w, w, 4 * rot);
 }
 
-// Rows of up to 16 words (nx <= 512), 16-byte aligned, several per warp so
+// Word wd of a row that starts o floats into a 16-byte aligned buffer and is
+// npts points long, for rows at any offset: the 8 float4 from the one that
+// holds the word's first point (rotated over the lanes as in row_word), the 4
+// points after them from the next lane's word of the same row (lane wd + 1
+// builds its own first float4 from them) or, for the last lane of the row's
+// group (last), by one more load; the 36 bits shifted down by o & 3.  Every
+// lane of the warp calls it (the shuffle); only float4 that hold points of the
+// row are read.
+__device__ __forceinline__ uint32_t row_word_shift(const float* buf, int o, int npts, int wd, int rot, bool last,
+                                                   float iso)
+{
+    const int base = o + 32 * wd, b4 = base >> 2, sh = base & 3;
+    const int nvq = ((o + npts + 3) >> 2) - b4;  // float4 from b4 on that hold points of the row
+    const float4* r4 = reinterpret_cast<const float4*>(buf) + b4;
+    uint32_t w = 0u;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+        const int q = (u + rot) & 7;
+        if (q < nvq) {
+            const float4 v = r4[q];
+            w |= ge_mask(v.x, iso) & (1u << (4 * u));
+            w |= ge_mask(v.y, iso) & (2u << (4 * u));
+            w |= ge_mask(v.z, iso) & (4u << (4 * u));
+            w |= ge_mask(v.w, iso) & (8u << (4 * u));
+        }
+    }
+    w = __funnelshift_l(w, w, 4 * rot);
+    uint32_t hi = __shfl_down_sync(0xffffffffu, w, 1);
+    if (last) {
+        hi = 0u;
+        if (nvq > 8) {
+            const float4 v = r4[8];
+            hi = (ge_mask(v.x, iso) & 1u) | (ge_mask(v.y, iso) & 2u) | (ge_mask(v.z, iso) & 4u) |
+                 (ge_mask(v.w, iso) & 8u);
+        }
+    }
+    const uint32_t r = __funnelshift_r(w, hi, sh);
+    const int nv = npts - 32 * wd;  // points of the word inside the row
+    return nv >= 32 ? r : (nv > 0 ? r & ((1u << nv) - 1u) : 0u);
+}
+
+// Floats of a warp's buffer in k_count_tma: RPW + 1 rows (plus up to 3 points
+// of lead-in and padding to 16 bytes when the rows are not 16-byte aligned).
+__host__ __device__ inline int count_buffer_floats(int nx, int rpw, bool aligned)
+{
+    return aligned ? (rpw + 1) * nx : (((rpw + 1) * nx + 3) + 3) & ~3;
+}
+
+// Rows of up to 16 words (nx <= 512), several per warp so
 // that no lane idles on words past a short row: the counts of k_count_warps,
 // with the volume brought in by the TMA bulk engine.  A warp's grid rows
 // jw .. jw+RPW-1 read rows jw .. jw+RPW of every plane (A and B of each
@@ -273,12 +321,17 @@ __device__ __forceinline__ uint32_t row_word(const float* row, int nq, int wd, i
 // plane fills the warp's buffer and completes on the warp's mbarrier.  The
 // words of plane k+1 are taken from the buffer before the copy of plane k+2
 // is issued into it, so the copy runs while step k is counted; no register
-// holds raw values across a step.
+// holds raw values across a step.  Rows whose length is not a multiple of 4
+// points (ALIGNED false; the volume itself 16-byte aligned): the copy runs
+// from the rows' first point rounded down to 16 bytes to their last rounded
+// down, the last few points come by plain loads, and row_word_shift builds
+// the words at the rows' offsets in the buffer.
 // RPW grid rows per warp (2: rows of up to 16 words, 4: up to 8, 8: up to 4), LPR =
 // 32 / RPW lanes per row; a warp's rows jw .. jw+RPW-1 read rows jw .. jw+RPW
 // of every plane, RPW + 1 rows of its buffer.  FULL: every lane's word is
 // inside the row (nx = 32 * LPR).
-template <bool MC, bool FULL, int RPW>
+
+template <bool MC, bool FULL, int RPW, bool ALIGNED>
 __global__ void __launch_bounds__(kThreads, 4) k_count_tma(const float* __restrict__ vol, Grid g, float iso, int KC,
                                                         int nyb, uint4* __restrict__ rowcnt,
                                                         uint2* __restrict__ trims, uint32_t* __restrict__ mccnt,
@@ -292,7 +345,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_count_tma(const float* __restri
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, h = lane / LPR, lw = lane % LPR;
     const int jw = jb * kCountRows * RPW + RPW * warp;
     if (jw >= g.ny) return;  // all the warp's rows past the grid
-    float* buf = reinterpret_cast<float*>(s_raw) + (size_t)warp * NBUF * g.nx;
+    float* buf = reinterpret_cast<float*>(s_raw) + (size_t)warp * count_buffer_floats(g.nx, RPW, ALIGNED);
     uint64_t* bar = &s_bar[warp];
     if (lane == 0) {
         mbar_init(bar, 1);
@@ -304,25 +357,56 @@ __global__ void __launch_bounds__(kThreads, 4) k_count_tma(const float* __restri
     const int kb = g.kr + kc * KC, ke = min(kb + KC, g.ke);
     const bool hasY = row_ok && j < g.ny - 1;
     const int nq = g.nx >> 2;
-    const unsigned bytes = (unsigned)(min(NBUF, g.ny - jw) * g.nx * 4);
+    const int nrows = min(NBUF, g.ny - jw);
+    const unsigned bytes = (unsigned)(nrows * g.nx * 4);
+    int lead = 0;      // points of the buffer before the warp's first row (ALIGNED false)
+    int tail_at = -1;  // this lane's place in the buffer for one of the rows' last points, or -1
+    float tail_v = 0.f;
 
-    // plane p -> buffer (lane 0); earlier reads of the buffer are ordered
-    // before the engine's writes by the caller's __syncwarp and the fence
+    // plane p -> buffer (lane 0 issues the copy); earlier reads of the buffer
+    // are ordered before the engine's writes by the caller's __syncwarp and
+    // the fence
     auto issue = [&](int p) {
-        if (lane == 0) {
-            fence_proxy_async();
-            mbar_arrive_expect_tx(bar, bytes);
-            bulk_copy_g2s(buf, vol + ((long long)(p - g.kd) * g.ny + jw) * g.nx, bytes, bar);
+        const long long s0 = ((long long)(p - g.kd) * g.ny + jw) * g.nx;
+        if (ALIGNED) {
+            if (lane == 0) {
+                fence_proxy_async();
+                mbar_arrive_expect_tx(bar, bytes);
+                bulk_copy_g2s(buf, vol + s0, bytes, bar);
+            }
+        } else {  // [a0, e0) by the engine, [max(e0, s0), e) by plain loads; all inside the volume
+            const long long a0 = s0 & ~3ll, e = s0 + (long long)nrows * g.nx, e0 = e & ~3ll;
+            const unsigned nb = e0 > a0 ? (unsigned)((e0 - a0) * 4) : 0u;
+            lead = (int)(s0 - a0);
+            if (lane == 0) {
+                fence_proxy_async();
+                mbar_arrive_expect_tx(bar, nb);
+                if (nb) bulk_copy_g2s(buf, vol + a0, nb, bar);
+            }
+            // loaded now, stored by take(): the warp does not wait here for the load
+            const long long lo = e0 > s0 ? e0 : s0;
+            tail_at = lane < (int)(e - lo) ? (int)(lo - a0) + lane : -1;
+            if (tail_at >= 0) tail_v = __ldg(vol + lo + lane);
         }
     };
     unsigned phase = 0;
     // words of rows A = buffer row h and B = buffer row h+1 of the plane in the buffer
     auto take = [&](uint32_t& wa, uint32_t& wb) -> bool {
+        if (!ALIGNED && tail_at >= 0) buf[tail_at] = tail_v;
+        __syncwarp();  // the plain loads of the buffer's last points are visible
         const bool done = mbar_wait(bar, phase);
         if (!__all_sync(0xffffffffu, done)) return false;
         phase ^= 1u;
-        wa = row_ok ? row_word<FULL>(buf + h * g.nx, nq, lw, lane & 7, iso) : 0u;
-        wb = hasY ? row_word<FULL>(buf + (h + 1) * g.nx, nq, lw, lane & 7, iso) : 0u;
+        if (ALIGNED) {
+            wa = row_ok ? row_word<FULL>(buf + h * g.nx, nq, lw, lane & 7, iso) : 0u;
+            wb = hasY ? row_word<FULL>(buf + (h + 1) * g.nx, nq, lw, lane & 7, iso) : 0u;
+        } else {
+            // every lane builds both words (the shuffles); rows past the grid read stale buffer rows
+            wa = row_word_shift(buf, lead + h * g.nx, g.nx, lw, lane & 7, lw == LPR - 1, iso);
+            wb = row_word_shift(buf, lead + (h + 1) * g.nx, g.nx, lw, lane & 7, lw == LPR - 1, iso);
+            wa = row_ok ? wa : 0u;
+            wb = hasY ? wb : 0u;
+        }
         __syncwarp();  // every lane has read the buffer before it is refilled
         return true;
     };
@@ -655,29 +739,35 @@ static void count_launch(const CountPlan& p, const float* vol, const Grid& g, fl
     const unsigned blocks = (unsigned)(p.nyb * p.nkc);
     const bool vec4 = g.W <= 64 && (g.nx % 4 == 0) && ((reinterpret_cast<uintptr_t>(vol) & 15) == 0);
     uint2* trims = p.trims ? b.trims : nullptr;  // the kernels skip the trims when null
-    if (vec4 && g.W <= 16) {  // 8 rows per warp up to 4 words, 4 up to 8, else 2; planes through TMA
+    const bool base16 = (reinterpret_cast<uintptr_t>(vol) & 15) == 0;
+    if (base16 && g.W <= 16) {  // 8 rows per warp up to 4 words, 4 up to 8, else 2; planes through TMA
         const int rpw = g.W <= 4 ? 8 : (g.W <= 8 ? 4 : 2);
+        const bool aligned = g.nx % 4 == 0;
         const int rows = kCountRows * rpw;
         const int nyb2 = (g.ny + rows - 1) / rows;
         const unsigned blocks2 = (unsigned)(nyb2 * p.nkc);
         const int nq = g.nx >> 2;
-        const size_t smem = (size_t)kCountRows * (rpw + 1) * g.nx * sizeof(float);
-#define ISO_TMA(FULL, RPW)                                                                                     \
+        const size_t smem = (size_t)kCountRows * count_buffer_floats(g.nx, rpw, aligned) * sizeof(float);
+#define ISO_TMA(FULL, RPW, AL)                                                                                 \
     {                                                                                                          \
-        auto kern = k_count_tma<MC, FULL, RPW>;                                                               \
+        auto kern = k_count_tma<MC, FULL, RPW, AL>;                                                           \
         allow_smem(kern, smem);                                                                                \
         kern<<<blocks2, kThreads, smem, s>>>(vol, g, iso, p.KC, nyb2, b.rowcnt, trims, b.mccnt, b.bits,         \
                                              b.totals + 3);                                                    \
     }
-        if (rpw == 8) {
-            if (nq == 32) ISO_TMA(true, 8)
-            else ISO_TMA(false, 8)
+        if (!aligned) {
+            if (rpw == 8) ISO_TMA(false, 8, false)
+            else if (rpw == 4) ISO_TMA(false, 4, false)
+            else ISO_TMA(false, 2, false)
+        } else if (rpw == 8) {
+            if (nq == 32) ISO_TMA(true, 8, true)
+            else ISO_TMA(false, 8, true)
         } else if (rpw == 4) {
-            if (nq == 64) ISO_TMA(true, 4)
-            else ISO_TMA(false, 4)
+            if (nq == 64) ISO_TMA(true, 4, true)
+            else ISO_TMA(false, 4, true)
         } else {
-            if (nq == 128) ISO_TMA(true, 2)
-            else ISO_TMA(false, 2)
+            if (nq == 128) ISO_TMA(true, 2, true)
+            else ISO_TMA(false, 2, true)
         }
 #undef ISO_TMA
         return;

@@ -117,12 +117,14 @@ def test_tall_grids(M, dims):
     both(M, vol, 0.1, (1.0, 0.5, 0.25), (0.0, 1.0, -3.0))
 
 
-@pytest.mark.parametrize("nx", [124, 128, 132, 252, 256, 260, 508, 512])
+@pytest.mark.parametrize("nx", [124, 127, 128, 129, 132, 251, 252, 255, 256, 257, 260, 506, 508, 511, 512])
 def test_row_width_boundaries(M, nx):
     """Rows at the edges of the kernel choices: up to 4 words the count and
     generate kernels put eight rows in a warp (128 points: every lane's word
     full), up to 8 words four (256: full), from 9 to 16 words two (512:
-    full); 13 rows leave the last group of rows short."""
+    full); 13 rows leave the last group of rows short.  Widths that are not a
+    multiple of 4 points put the rows of a plane at every offset from a
+    16-byte boundary in the count kernel's plane copies."""
     vol = M.generate_value_noise((nx, 13, 11), 3, 16, seed=nx)
     both(M, vol, 0.0)
     rng = np.random.default_rng(nx)
