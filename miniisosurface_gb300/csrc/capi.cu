@@ -556,6 +556,7 @@ iso_status slab_prepare(iso_ctx* ctx, iso_algorithm algo, const float* volume, c
 // kernels.
 // ---------------------------------------------------------------------------
 constexpr int kStreamPlanes = 64;  // planes per slab of the streamed path
+constexpr int kTailPlanes = 16;    // the smallest slabs, at the end of the volume
 constexpr int kStreamWindows = 3;  // device windows of the volume
 
 cudaEvent_t sync_event(iso_ctx* ctx, size_t q)
@@ -608,8 +609,25 @@ iso_status extract_host_streamed(iso_ctx* ctx, iso_algorithm algo, const void* v
     if (!ctx->s_cnt) ISO_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->s_cnt, cudaStreamNonBlocking));
     const int nz = gfull.nz;
     const size_t plane = (size_t)gfull.nx * gfull.ny;
-    const int nslab = (nz + kStreamPlanes - 1) / kStreamPlanes;
-    auto slab_k0 = [&](int q) { return (int)((long long)q * nz / nslab); };
+    // Slabs of at most kStreamPlanes planes; the last kStreamPlanes planes go
+    // as slabs of halving size (1/2, 1/4, ... down to kTailPlanes, that one
+    // twice), so that little is left to count, generate and copy back once
+    // the last planes have landed.
+    std::vector<int> kb;  // slab q = planes kb[q] .. kb[q + 1] - 1
+    {
+        const int body = nz - kStreamPlanes;  // >= kStreamPlanes (stream_eligible)
+        const int nb = (body + kStreamPlanes - 1) / kStreamPlanes;
+        for (int q = 0; q < nb; ++q) kb.push_back((int)((long long)q * body / nb));
+        int at = body;
+        for (int part = kStreamPlanes / 2; part >= kTailPlanes; part /= 2) {
+            kb.push_back(at);
+            at += part;
+        }
+        kb.push_back(at);
+        kb.push_back(nz);
+    }
+    const int nslab = (int)kb.size() - 1;
+    auto slab_k0 = [&](int q) { return kb[q]; };
     auto data_lo = [&](int q) { return std::max(slab_k0(q) - 1, 0); };
     auto data_hi = [&](int q) { return std::min(slab_k0(q + 1) + 1, nz - 1); };  // inclusive
     int wplanes = 0;
@@ -667,13 +685,25 @@ iso_status extract_host_streamed(iso_ctx* ctx, iso_algorithm algo, const void* v
     ISO_CUDA(ctx, cudaEventRecord(sync_event(ctx, 0), s));  // after the caller's earlier work on s
     ISO_CUDA(ctx, cudaStreamWaitEvent(ctx->s_h2d, sync_event(ctx, 0), 0));
     ISO_CUDA(ctx, cudaStreamWaitEvent(ctx->s_cnt, sync_event(ctx, 0), 0));
+    // the window slab q's samples land in (typed: converted from there)
+    auto landing = [&](int q) -> char* {
+        return typed ? typed_window(q) : reinterpret_cast<char*>(window(q));
+    };
     auto copy_in = [&](int q) -> iso_status {
         if (q >= kStreamWindows)  // the window's previous slab is generated
             ISO_CUDA(ctx, cudaStreamWaitEvent(ctx->s_h2d, sync_event(ctx, ev_win + q % kStreamWindows), 0));
         const int lo = data_lo(q), hi = data_hi(q);
-        ISO_CUDA(ctx, cudaMemcpyAsync(typed ? static_cast<void*>(typed_window(q)) : static_cast<void*>(window(q)),
-                                      src + (size_t)lo * plane * elem, (size_t)(hi - lo + 1) * plane * elem,
-                                      cudaMemcpyHostToDevice, ctx->s_h2d));
+        // the planes slab q shares with slab q-1 (k0-1 .. k0+1) come from its
+        // window, which is refilled only after this copy on the same stream
+        const int shared = q > 0 ? std::min(data_hi(q - 1), hi) - lo + 1 : 0;
+        if (shared > 0)
+            ISO_CUDA(ctx, cudaMemcpyAsync(landing(q), landing(q - 1) + (size_t)(lo - data_lo(q - 1)) * plane * elem,
+                                          (size_t)shared * plane * elem, cudaMemcpyDeviceToDevice, ctx->s_h2d));
+        const int from = lo + std::max(shared, 0);
+        if (from <= hi)
+            ISO_CUDA(ctx, cudaMemcpyAsync(landing(q) + (size_t)(from - lo) * plane * elem,
+                                          src + (size_t)from * plane * elem, (size_t)(hi - from + 1) * plane * elem,
+                                          cudaMemcpyHostToDevice, ctx->s_h2d));
         ISO_CUDA(ctx, cudaEventRecord(sync_event(ctx, 1 + q), ctx->s_h2d));
         return ISO_OK;
     };

@@ -205,6 +205,42 @@ def test_host_entry_point_streamed(M):
                 assert_same_mesh((m.points, m.normals, m.triangles), want, "streamed %s ib %d" % (dims, ib))
 
 
+def test_host_entry_point_streamed_pinned(M):
+    """Streamed host path into pinned output buffers (the bench's end-to-end
+    case), each slab's part of the mesh at its offset in them; buffers that
+    start 4 bytes past a 16-byte boundary too."""
+    import torch
+    from miniisosurface_gb300 import _lib
+
+    lib = _lib.load()
+    ctx = M.Context(0)
+    dims = (70, 45, 200)
+    vol = M.generate_value_noise(dims, 3, 16, seed=6)
+    img = M.Image3D.from_array(vol, (1.0, 0.5, 1.0), (2.0, -1.0, 0.25))
+    g = img.grid()
+    for algo, ref in ((M.FLYING_EDGES, oracle_lib.fe), (M.MARCHING_CUBES, oracle_lib.mc)):
+        want = ref(vol, 0.0, img.spacing, img.zeroPos)
+        V, T = want[0].shape[0], want[2].shape[0]
+        for ib, shift in ((4, 0), (8, 0), (4, 1), (8, 1)):
+            it = torch.int32 if ib == 4 else torch.int64
+            # shift words of padding at the front of each buffer
+            hp = torch.zeros(3 * V + shift, dtype=torch.float32).pin_memory()
+            hn = torch.zeros(3 * V + shift, dtype=torch.float32).pin_memory()
+            ht = torch.zeros(3 * T * ib // 4 + shift, dtype=torch.int32).pin_memory()
+            m = _lib.IsoMesh()
+            m.points, m.normals = hp.data_ptr() + 4 * shift, hn.data_ptr() + 4 * shift
+            m.tris = ht.data_ptr() + 4 * shift
+            m.index_bytes, m.cap_points, m.cap_tris = ib, V, T
+            st = lib.iso_extract_host(ctx.handle, M.api._algo(algo), img.data.ctypes.data, C.byref(g), C.c_float(0.0),
+                                      C.byref(m), None)
+            _lib.check(st, ctx.handle)
+            assert (m.n_points, m.n_tris) == (V, T)
+            p = hp.numpy()[shift:].reshape(V, 3)
+            n = hn.numpy()[shift:].reshape(V, 3)
+            tr = ht.numpy()[shift:].view(np.int32 if ib == 4 else np.int64).reshape(T, 3).astype(np.uint64)
+            assert_same_mesh((p, n, tr), want, "pinned algo %s ib %d shift %d" % (algo, ib, shift))
+
+
 def test_mc_dupfree_matches_oracle(M):
     """ISO_MC_DUPFREE: the serial MC mesh with vertices in global-edge-index
     order (marchingCubes/openmpDupFree with one section), bit for bit."""
