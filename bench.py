@@ -24,6 +24,15 @@ One step = one full extraction (passes 1-4) of the volume.
   pipeline  the whole extraction: B = 8 N + 24 V + 12 T over the step
   cpu_baseline  the oracle port of the reference's OpenMP Flying Edges on
             all host cores, full volume, repeated for a bounded time.
+  batched   64 volumes with per-axis dimensions uniform in [32, 320] (half
+            Gaussian blobs, half value noise), each with 1-4 isovalues uniform
+            in its field's [5th, 95th] percentile: Flying Edges over all
+            (volume, isovalue) requests, volumes resident on the device.
+            plain = one iso_extract_device call per request (the drop-in
+            call, which synchronises); plain_async = the same calls queued on
+            one stream without synchronising; batched = iso_extract_batch
+            (lanes picked by its autotuner, graph replayed).  Outputs are
+            compared request by request (identical).
 
 --impl reference runs that CPU implementation alone, rank 0 only.
 Under torchrun (N > 1) every rank extracts its own replica (no collective in
@@ -61,6 +70,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batched-reps", type=int, default=5)
     return ap.parse_args()
 
 
@@ -213,6 +224,102 @@ def link_floor(rates, h2d_bytes, d2h_bytes, ms_per_step):
     floor_s = max(h2d_bytes / r_in, d2h_bytes / r_out, (h2d_bytes + d2h_bytes) / r_both)
     return {"h2d_GBps": r_in / 1e9, "d2h_GBps": r_out / 1e9, "both_GBps": r_both / 1e9,
             "floor_ms_per_step": 1e3 * floor_s, "frac_of_floor": 1e3 * floor_s / ms_per_step}
+
+
+def batch_workload(M, seed=2, nvol=64):
+    """(volumes, requests): 64 volumes, per-axis dims uniform in [32, 320],
+    even ones Gaussian blobs and odd ones value noise (the single-volume
+    generators), each with 1-4 isovalues uniform in [p5, p95] of its field."""
+    rng = np.random.default_rng(seed)
+    vols, reqs = [], []
+    for v in range(nvol):
+        dims = tuple(int(d) for d in rng.integers(32, 321, size=3))
+        if v % 2 == 0:
+            vol = M.generate_blobs(dims, 8, seed=1000 + v)
+        else:
+            vol = M.generate_value_noise(dims, 4, 64, seed=1000 + v)
+        lo, hi = np.percentile(vol[:: max(1, vol.shape[0] // 16)], [5, 95])
+        vols.append((dims, vol))
+        for _ in range(int(rng.integers(1, 5))):
+            reqs.append((v, float(np.float32(rng.uniform(lo, hi)))))
+    return vols, reqs
+
+
+def batched_leg(M, lib, dev, reps):
+    """Batched vs plain per-request extraction of the batch workload (see the module notes)."""
+    import torch
+    from miniisosurface_gb300 import _lib
+    vols, reqs = batch_workload(M)
+    dvols = [torch.from_numpy(np.ascontiguousarray(v).reshape(-1)).to(dev) for _, v in vols]
+    ctx = M.Context(dev.index or 0)
+    requests = [M.Request(dvols[v], vols[v][0], iso, M.FLYING_EDGES) for v, iso in reqs]
+    cells = sum((d[0] - 1) * (d[1] - 1) * (d[2] - 1) for d in (vols[v][0] for v, _ in reqs))
+    sizes = [M.count_device(r.volume, r.dims, r.isoval, ctx=ctx) for r in requests]
+    plain_m = [M.DeviceMesh(nv, nt, 4, dev) for nv, nt in sizes]
+    batch_m = [M.DeviceMesh(nv, nt, 4, dev) for nv, nt in sizes]
+    descs = [m.descriptor() for m in plain_m]
+    grids = [M.make_grid(r.dims) for r in requests]
+    stream = torch.cuda.current_stream(dev)
+    sh = C.c_void_p(stream.cuda_stream)
+    res = torch.zeros((len(requests), 4), dtype=torch.int64).pin_memory()
+
+    def plain():
+        for r, g, d in zip(requests, grids, descs):
+            st = lib.iso_extract_device(ctx.handle, 0, r.volume.data_ptr(), C.byref(g), C.c_float(r.isoval),
+                                        C.byref(d), sh)
+            if st != 0:
+                _lib.check(st, ctx.handle)
+
+    def plain_async():
+        for i, (r, g, d) in enumerate(zip(requests, grids, descs)):
+            st = lib.iso_extract_device_async(ctx.handle, 0, r.volume.data_ptr(), C.byref(g), C.c_float(r.isoval),
+                                              C.byref(d), C.c_void_p(res.data_ptr() + 32 * i), sh)
+            if st != 0:
+                _lib.check(st, ctx.handle)
+        stream.synchronize()
+
+    batch = M.Batch(requests, batch_m)
+
+    def batched():
+        codes = batch.run(ctx)
+        if any(c != 0 for c in codes):
+            raise RuntimeError("batch request failed: %s" % codes)
+
+    def seconds(fn):
+        fn()
+        torch.cuda.synchronize()
+        best = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            best.append(time.perf_counter() - t0)
+        return statistics.median(best)
+
+    M.set_batch_lanes(0, ctx)
+    batched()  # the autotuner's first batch
+    lanes = M.batch_lanes(ctx)
+    t_batch = seconds(batched)
+    t_plain = seconds(plain)
+    t_async = seconds(plain_async)
+    same = True
+    for a, b in zip(plain_m, batch_m):
+        same &= bool(torch.equal(a.points[: b.n_points], b.points[: b.n_points]))
+        same &= bool(torch.equal(a.normals[: b.n_points], b.normals[: b.n_points]))
+        same &= bool(torch.equal(a.tris[: b.n_tris], b.tris[: b.n_tris]))
+    same &= all((b.n_points, b.n_tris) == s for b, s in zip(batch_m, sizes))
+    mc = lambda s: cells / s / 1e6
+    return {
+        "workload": "64 volumes, dims uniform in [32, 320] per axis, half blobs / half value noise, "
+                    "1-4 isovalues each in [p5, p95]; flying edges, uint32 indices, volumes resident",
+        "volumes": len(vols), "requests": len(requests), "cells": cells,
+        "vertices": int(sum(s[0] for s in sizes)), "triangles": int(sum(s[1] for s in sizes)),
+        "plain": {"ms": 1e3 * t_plain, "value": mc(t_plain), "unit": METRIC},
+        "plain_async": {"ms": 1e3 * t_async, "value": mc(t_async), "unit": METRIC},
+        "batched": {"ms": 1e3 * t_batch, "value": mc(t_batch), "unit": METRIC, "lanes": lanes},
+        "speedup_vs_plain": t_plain / t_batch, "speedup_vs_plain_async": t_async / t_batch,
+        "identical_output": same,
+    }
 
 
 def run_reference(args, rank):
@@ -443,6 +550,8 @@ def main():
             "gpu_launches": int(sum(n_pass[p] for p in range(npass)) + n_pass[2]),
             "clocks": clk,
         }
+        if not args.no_batched:
+            line["batched"] = batched_leg(M, lib, dev, args.batched_reps)
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(vol_host, args.cpu_seconds)
         print(json.dumps(line), flush=True)

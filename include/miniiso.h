@@ -164,6 +164,39 @@ iso_status iso_extract_device(iso_ctx* ctx, iso_algorithm algo, const float* vol
 iso_status iso_extract_device_async(iso_ctx* ctx, iso_algorithm algo, const float* volume, const iso_grid* grid,
                                     float isoval, iso_mesh* out, int64_t* result_host, void* stream);
 
+/* Batched extraction (no counterpart in the reference, which extracts one
+ * volume per call).  n requests -- each a volume in device memory with its
+ * own grid, isovalue and algorithm (an iso_algorithm value) -- into n
+ * device meshes out[0..n); each mesh is exactly what iso_extract_device
+ * gives for its request.  The requests are spread over lanes (streams with
+ * their own scratch, largest requests first) and the whole batch is captured
+ * once as a CUDA graph, launched on `stream`: no host round trip between
+ * requests, and a repeated call with the same requests and meshes only
+ * relaunches the graph (a changed batch is captured again and the graph
+ * updated in place).  Capacities are checked on the device: a request whose
+ * mesh is too small writes nothing and gets ISO_ERR_CAPACITY with the sizes
+ * it needs in out[r].n_points / n_tris, as from iso_extract_device.
+ * status (n entries, may be NULL) receives each request's status; the call
+ * returns ISO_OK when every request succeeded, else the first failing
+ * request's status.  Synchronises the stream.  Calls on one context must not
+ * overlap, and none may run while a stream is being captured. */
+typedef struct iso_request {
+    const float* volume;
+    iso_grid grid;
+    float isoval;
+    int32_t algorithm;
+} iso_request;
+iso_status iso_extract_batch(iso_ctx* ctx, int64_t n, const iso_request* req, iso_mesh* out, iso_status* status,
+                             void* stream);
+
+/* Lanes of iso_extract_batch: a fixed count (1..64), or 0 (the default): the
+ * autotuner times the context's next batch at 1, 2, 4, 8, 16 and 32 lanes
+ * (each run writes the same meshes) and keeps the fastest count for that batch and
+ * the ones after it.  iso_batch_lanes returns the count in use (0 before the
+ * autotuner has run). */
+iso_status iso_batch_set_lanes(iso_ctx* ctx, int lanes);
+int iso_batch_lanes(const iso_ctx* ctx);
+
 /* z-slabs: the grid split along z into slabs of planes [k0, k1), for
  * sharding over GPUs or streaming a volume that does not fit (no counterpart
  * in the serial reference; marchingCubes/mpi/mpiutil.h:197-203 splits the

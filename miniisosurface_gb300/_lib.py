@@ -41,6 +41,10 @@ class IsoMesh(C.Structure):
                 ("n_points", C.c_int64), ("n_tris", C.c_int64)]
 
 
+class IsoRequest(C.Structure):
+    _fields_ = [("volume", C.c_void_p), ("grid", IsoGrid), ("isoval", C.c_float), ("algorithm", C.c_int32)]
+
+
 # name -> (restype, argtypes); mirrors include/miniiso.h
 SIGNATURES = {
     "iso_status_string": (C.c_char_p, [C.c_int]),
@@ -69,6 +73,10 @@ SIGNATURES = {
                                            C.POINTER(IsoMesh), C.c_void_p, C.c_void_p]),
     "iso_extract_host": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.POINTER(IsoGrid), C.c_float,
                                    C.POINTER(IsoMesh), C.c_void_p]),
+    "iso_extract_batch": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(IsoRequest), C.POINTER(IsoMesh),
+                                    C.POINTER(C.c_int), C.c_void_p]),
+    "iso_batch_set_lanes": (C.c_int, [C.c_void_p, C.c_int]),
+    "iso_batch_lanes": (C.c_int, [C.c_void_p]),
     "iso_fe_create": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(IsoGrid), C.c_float, C.POINTER(C.c_void_p)]),
     "iso_fe_pass1": (C.c_int, [C.c_void_p]),
     "iso_fe_pass2": (C.c_int, [C.c_void_p]),

@@ -343,6 +343,93 @@ def extract_device(volume, dims, isoval, algorithm=FLYING_EDGES, spacing=(1, 1, 
     raise RuntimeError("output size changed between two extractions of the same volume")
 
 
+class Request:
+    """One extraction of a batch: a contiguous CUDA float32 volume (x fastest)
+    with its grid, isovalue and algorithm."""
+
+    def __init__(self, volume, dims, isoval, algorithm=FLYING_EDGES, spacing=(1, 1, 1), origin=(0, 0, 0)):
+        if not volume.is_cuda or not volume.is_contiguous() or str(volume.dtype) != "torch.float32":
+            raise ValueError("a batch volume must be a contiguous CUDA float32 tensor")
+        self.volume = volume
+        self.dims = tuple(int(d) for d in dims)
+        self.isoval = float(isoval)
+        self.algorithm = algorithm
+        self.spacing = spacing
+        self.origin = origin
+
+    def descriptor(self):
+        r = _lib.IsoRequest()
+        r.volume = _ptr(self.volume)
+        r.grid = make_grid(self.dims, self.spacing, self.origin)
+        r.isoval = self.isoval
+        r.algorithm = _algo(self.algorithm)
+        return r
+
+
+class Batch:
+    """Requests and their meshes as the C arrays of iso_extract_batch, built
+    once: running the same Batch again relaunches the captured graph."""
+
+    def __init__(self, requests, meshes):
+        self.requests = list(requests)
+        self.meshes = list(meshes)
+        n = len(self.requests)
+        self.req = (_lib.IsoRequest * max(n, 1))(*[r.descriptor() for r in self.requests])
+        self.out = (IsoMesh * max(n, 1))(*[m.descriptor() for m in self.meshes])
+        self.status = (C.c_int * max(n, 1))()
+
+    def run(self, ctx=None, stream=None):
+        """One iso_extract_batch call; returns the per-request statuses."""
+        import torch
+        lib = load()
+        ctx = ctx or default_context()
+        s = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        n = len(self.requests)
+        st = lib.iso_extract_batch(ctx.handle, n, self.req, self.out, self.status, C.c_void_p(s))
+        for i, m in enumerate(self.meshes):
+            m.n_points, m.n_tris = self.out[i].n_points, self.out[i].n_tris
+        codes = [self.status[i] for i in range(n)]
+        if st not in (_lib.ISO_OK, _lib.ISO_ERR_CAPACITY) or any(
+                c not in (_lib.ISO_OK, _lib.ISO_ERR_CAPACITY) for c in codes):
+            check(st if st != _lib.ISO_OK else next(c for c in codes if c != _lib.ISO_OK), ctx.handle)
+        return codes
+
+
+def extract_batch(requests, meshes=None, index_bytes=4, ctx=None, stream=None):
+    """Batched extraction (iso_extract_batch): a list of Request in, a list
+    of DeviceMesh out, each what extract_device gives for its request.
+
+    Meshes too small for their request (or none given) come back with the
+    sizes needed from the first batch run; they are re-allocated at exactly
+    that size and those requests run again as one more batch.
+    """
+    requests = list(requests)
+    if meshes is None:
+        meshes = [DeviceMesh(0, 0, index_bytes, r.volume.device) for r in requests]
+    meshes = list(meshes)
+    codes = Batch(requests, meshes).run(ctx, stream)
+    redo = [i for i, c in enumerate(codes) if c == _lib.ISO_ERR_CAPACITY]
+    if redo:
+        for i in redo:
+            meshes[i] = DeviceMesh(meshes[i].n_points, meshes[i].n_tris, meshes[i].index_bytes,
+                                   requests[i].volume.device)
+        codes = Batch([requests[i] for i in redo], [meshes[i] for i in redo]).run(ctx, stream)
+        if any(c != _lib.ISO_OK for c in codes):
+            raise RuntimeError("output size changed between two extractions of the same volume")
+    return meshes
+
+
+def set_batch_lanes(lanes, ctx=None):
+    """Lanes of the batched path (0: the autotuner picks them on the next batch)."""
+    ctx = ctx or default_context()
+    check(load().iso_batch_set_lanes(ctx.handle, int(lanes)), ctx.handle)
+
+
+def batch_lanes(ctx=None):
+    ctx = ctx or default_context()
+    return int(load().iso_batch_lanes(ctx.handle))
+
+
 def count_device(volume, dims, isoval, algorithm=FLYING_EDGES, ctx=None, stream=None):
     """Passes 1-3 only: exact (n_points, n_tris) of a device-resident volume."""
     import torch

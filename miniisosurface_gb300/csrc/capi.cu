@@ -49,6 +49,19 @@ struct iso_ctx {
     void* st_tris[2] = {nullptr, nullptr};
     long long st_cap_points = 0, st_cap_tris = 0;
     int st_index_bytes = 0;
+    // batched entry point (iso_extract_batch): lanes, their scratch, the captured graph
+    int batch_lanes = 0;        // set by iso_batch_set_lanes; 0: the autotuner's choice
+    int batch_tuned = 0;        // lanes the autotuner picked (0: not yet tuned)
+    cudaStream_t s_capture = nullptr;
+    std::vector<cudaStream_t> lane_streams;
+    std::vector<cudaEvent_t> lane_join;
+    cudaEvent_t batch_fork = nullptr, batch_t0 = nullptr, batch_t1 = nullptr;
+    void* batch_arena = nullptr;
+    size_t batch_arena_bytes = 0;
+    unsigned long long* h_batch = nullptr;  // pinned: 8 counters per request
+    size_t h_batch_n = 0;
+    cudaGraphExec_t batch_exec = nullptr;
+    std::vector<unsigned char> batch_key;  // what the graph in batch_exec was captured for
     int reverse = 1;  // pass 4 walks the planes backwards (the count pass leaves the last ones in L2)
     int stream_host = 1;  // iso_extract_host streams slabs (large grids)
     std::string last_error;
@@ -833,6 +846,218 @@ iso_status extract_host_streamed(iso_ctx* ctx, iso_algorithm algo, const void* v
     return ISO_OK;
 }
 
+
+// ---------------------------------------------------------------------------
+// Batched extraction.  The requests are spread over L lanes (streams, each
+// with its own scratch and, for Marching Cubes, its own FE -> MC map), the
+// largest requests first, each to the lane with the fewest cells so far; a
+// lane runs its requests one after the other (count, scan, generate,
+// vertices), the lanes run side by side.  The whole batch is captured once
+// as a CUDA graph: its 8-counter block per request (totals, device status,
+// work counter) lives in the batch arena, so the counts stay on the device
+// and the generate kernels check the capacities there; one copy at the end
+// brings every request's counters back.
+// ---------------------------------------------------------------------------
+struct BatchItem {
+    Grid g;
+    Plans pl;
+    int lane = 0;
+};
+
+constexpr int kMaxLanes = 64;
+constexpr int kTuneLanes[] = {1, 2, 4, 8, 16, 32};
+
+// Lane of every request with work and the arena layout: counters of all n
+// requests, then per lane its scratch and FE -> MC map.
+struct BatchLayout {
+    int lanes = 1;
+    std::vector<size_t> scratch_at, scratch_bytes, map_at;
+    size_t bytes = 0;
+};
+
+BatchLayout plan_batch(const iso_request* req, const iso_mesh* out, int64_t n, std::vector<BatchItem>& items,
+                       const std::vector<int>& run, int lanes)
+{
+    BatchLayout lay;
+    lay.lanes = lanes;
+    std::vector<int> order(run);
+    auto cells = [&](int r) { return (double)(items[r].g.nx - 1) * (items[r].g.ny - 1) * (items[r].g.nz - 1); };
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cells(a) > cells(b); });
+    std::vector<double> load(lanes, 0.0);
+    std::vector<size_t> scratch(lanes, 0), map(lanes, 0);
+    for (int r : order) {
+        const int l = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        items[r].lane = l;
+        load[l] += cells(r);
+        scratch[l] = std::max(scratch[l], scratch_size(items[r].g, items[r].pl.cp));
+        if (req[r].algorithm == ISO_MARCHING_CUBES) {
+            const long long capV = vertex_limit(&out[r], out[r].cap_points);
+            const long long capM = capV < 0xffffffffll ? capV : 0xffffffffll;
+            map[l] = std::max(map[l], (size_t)(capM + 1024) * 4);
+        }
+    }
+    size_t at = align256((size_t)n * 8 * sizeof(unsigned long long));
+    for (int l = 0; l < lanes; ++l) {
+        lay.scratch_at.push_back(at);
+        lay.scratch_bytes.push_back(scratch[l]);
+        at += align256(scratch[l]);
+        lay.map_at.push_back(at);
+        at += align256(map[l]);
+    }
+    lay.bytes = at;
+    return lay;
+}
+
+iso_status ensure_batch(iso_ctx* ctx, const BatchLayout& lay, int64_t n, cudaStream_t s)
+{
+    if (lay.bytes > ctx->batch_arena_bytes) {
+        ISO_CUDA(ctx, cudaStreamSynchronize(s));
+        ISO_CUDA(ctx, cudaDeviceSynchronize());
+        cudaFree(ctx->batch_arena);
+        ctx->batch_arena = nullptr;
+        ctx->batch_arena_bytes = 0;
+        ISO_CUDA(ctx, cudaMalloc(&ctx->batch_arena, lay.bytes));
+        ctx->batch_arena_bytes = lay.bytes;
+    }
+    if ((size_t)n > ctx->h_batch_n) {
+        ISO_CUDA(ctx, cudaStreamSynchronize(s));
+        if (ctx->h_batch) cudaFreeHost(ctx->h_batch);
+        ctx->h_batch = nullptr;
+        ctx->h_batch_n = 0;
+        ISO_CUDA(ctx, cudaHostAlloc(&ctx->h_batch, (size_t)n * 8 * sizeof(unsigned long long), cudaHostAllocDefault));
+        ctx->h_batch_n = (size_t)n;
+    }
+    if (!ctx->s_capture) ISO_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->s_capture, cudaStreamNonBlocking));
+    for (cudaEvent_t* e : {&ctx->batch_fork, &ctx->batch_t0, &ctx->batch_t1})
+        if (!*e) ISO_CUDA(ctx, cudaEventCreateWithFlags(e, e == &ctx->batch_fork ? cudaEventDisableTiming : 0));
+    while ((int)ctx->lane_streams.size() < lay.lanes) {
+        cudaStream_t q;
+        cudaEvent_t e;
+        ISO_CUDA(ctx, cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking));
+        ctx->lane_streams.push_back(q);
+        ISO_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        ctx->lane_join.push_back(e);
+    }
+    return ISO_OK;
+}
+
+// What a captured graph depends on: lanes, buffers, requests and meshes.
+std::vector<unsigned char> batch_key(const iso_ctx* ctx, int lanes, const iso_request* req, const iso_mesh* out,
+                                     int64_t n)
+{
+    std::vector<unsigned char> k;
+    auto put = [&](const void* p, size_t len) {
+        const unsigned char* c = static_cast<const unsigned char*>(p);
+        k.insert(k.end(), c, c + len);
+    };
+    put(&lanes, sizeof lanes);
+    put(&ctx->reverse, sizeof ctx->reverse);
+    put(&ctx->batch_arena, sizeof ctx->batch_arena);
+    put(&ctx->h_batch, sizeof ctx->h_batch);
+    put(&n, sizeof n);
+    put(req, (size_t)n * sizeof(iso_request));
+    for (int64_t r = 0; r < n; ++r) {
+        put(&out[r].points, sizeof out[r].points);
+        put(&out[r].normals, sizeof out[r].normals);
+        put(&out[r].tris, sizeof out[r].tris);
+        put(&out[r].index_bytes, sizeof out[r].index_bytes);
+        put(&out[r].cap_points, sizeof out[r].cap_points);
+        put(&out[r].cap_tris, sizeof out[r].cap_tris);
+    }
+    return k;
+}
+
+// Capture the batch on the lanes and make ctx->batch_exec run it (updating
+// the executable graph in place when the topology allows).
+iso_status capture_batch(iso_ctx* ctx, const iso_request* req, const iso_mesh* out, int64_t n,
+                         std::vector<BatchItem>& items, const std::vector<int>& run, const BatchLayout& lay)
+{
+    char* arena = static_cast<char*>(ctx->batch_arena);
+    unsigned long long* counters = reinterpret_cast<unsigned long long*>(arena);
+    cudaStream_t sc = ctx->s_capture;
+    const bool prof = ctx->profiling;
+    ctx->profiling = false;  // no timing events inside the graph
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(sc, cudaStreamCaptureModeRelaxed);
+    if (e == cudaSuccess) {
+        cudaEventRecord(ctx->batch_fork, sc);
+        for (int l = 0; l < lay.lanes; ++l) cudaStreamWaitEvent(ctx->lane_streams[l], ctx->batch_fork, 0);
+        for (int r : run) {
+            BatchItem& it = items[r];
+            cudaStream_t ls = ctx->lane_streams[it.lane];
+            FeBuffers b;
+            carve(arena + lay.scratch_at[it.lane], it.g, it.pl.cp, b);
+            b.totals = counters + 8 * r;
+            b.fe2mc = reinterpret_cast<uint32_t*>(arena + lay.map_at[it.lane]);
+            PassMarks pm(ctx, ls);
+            const iso_algorithm algo = static_cast<iso_algorithm>(req[r].algorithm);
+            enqueue_count(ctx, algo, req[r].volume, it.g, req[r].isoval, it.pl, b, ls, pm);
+            enqueue_generate(ctx, algo, req[r].volume, it.g, req[r].isoval, it.pl, b, &out[r], ls, pm);
+        }
+        for (int l = 0; l < lay.lanes; ++l) {
+            cudaEventRecord(ctx->lane_join[l], ctx->lane_streams[l]);
+            cudaStreamWaitEvent(sc, ctx->lane_join[l], 0);
+        }
+        cudaMemcpyAsync(ctx->h_batch, counters, (size_t)n * 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                        sc);
+        e = cudaStreamEndCapture(sc, &graph);
+    }
+    ctx->profiling = prof;
+    if (e != cudaSuccess || !graph) {
+        cudaGetLastError();
+        if (graph) cudaGraphDestroy(graph);
+        ctx->batch_key.clear();
+        ctx->last_error = std::string("capturing the batch failed: ") + cudaGetErrorString(e);
+        return ISO_ERR_CUDA;
+    }
+    if (ctx->batch_exec) {
+        cudaGraphExecUpdateResultInfo info;
+        if (cudaGraphExecUpdate(ctx->batch_exec, graph, &info) != cudaSuccess) {
+            cudaGetLastError();
+            cudaGraphExecDestroy(ctx->batch_exec);
+            ctx->batch_exec = nullptr;
+        }
+    }
+    if (!ctx->batch_exec) e = cudaGraphInstantiate(&ctx->batch_exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        ctx->batch_exec = nullptr;
+        ctx->batch_key.clear();
+        return cuda_fail(ctx, e, "cudaGraphInstantiate");
+    }
+    return ISO_OK;
+}
+
+// Prepare (lanes, buffers, graph) for `lanes` lanes; nothing runs.
+iso_status prepare_batch(iso_ctx* ctx, const iso_request* req, const iso_mesh* out, int64_t n,
+                         std::vector<BatchItem>& items, const std::vector<int>& run, int lanes, cudaStream_t s)
+{
+    const BatchLayout lay = plan_batch(req, out, n, items, run, lanes);
+    iso_status st = ensure_batch(ctx, lay, n, s);
+    if (st != ISO_OK) return st;
+    std::vector<unsigned char> key = batch_key(ctx, lanes, req, out, n);
+    if (ctx->batch_exec && key == ctx->batch_key) return ISO_OK;
+    st = capture_batch(ctx, req, out, n, items, run, lay);
+    if (st == ISO_OK) ctx->batch_key.swap(key);
+    return st;
+}
+
+// Milliseconds of one run of the prepared batch (the best of two after one warm-up run).
+iso_status time_batch(iso_ctx* ctx, cudaStream_t s, float& best)
+{
+    best = 1e30f;
+    for (int rep = 0; rep < 3; ++rep) {
+        ISO_CUDA(ctx, cudaEventRecord(ctx->batch_t0, s));
+        ISO_CUDA(ctx, cudaGraphLaunch(ctx->batch_exec, s));
+        ISO_CUDA(ctx, cudaEventRecord(ctx->batch_t1, s));
+        ISO_CUDA(ctx, cudaEventSynchronize(ctx->batch_t1));
+        float ms = 0.f;
+        ISO_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->batch_t0, ctx->batch_t1));
+        if (rep > 0) best = std::min(best, ms);
+    }
+    return ISO_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -984,6 +1209,14 @@ iso_status iso_ctx_destroy(iso_ctx* ctx)
     if (ctx->s_d2h) cudaStreamDestroy(ctx->s_d2h);
     if (ctx->s_cnt) cudaStreamDestroy(ctx->s_cnt);
     for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
+    if (ctx->batch_exec) cudaGraphExecDestroy(ctx->batch_exec);
+    for (cudaStream_t q : ctx->lane_streams) cudaStreamDestroy(q);
+    for (cudaEvent_t e : ctx->lane_join) cudaEventDestroy(e);
+    for (cudaEvent_t e : {ctx->batch_fork, ctx->batch_t0, ctx->batch_t1})
+        if (e) cudaEventDestroy(e);
+    if (ctx->s_capture) cudaStreamDestroy(ctx->s_capture);
+    cudaFree(ctx->batch_arena);
+    if (ctx->h_batch) cudaFreeHost(ctx->h_batch);
     delete ctx;
     return ISO_OK;
 }
@@ -1086,6 +1319,91 @@ iso_status iso_extract_device_async(iso_ctx* ctx, iso_algorithm algo, const floa
     ISO_CUDA(ctx, cudaGetLastError());
     ISO_CUDA(ctx, cudaMemcpyAsync(result_host, b.totals, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
     return ISO_OK;
+}
+
+iso_status iso_extract_batch(iso_ctx* ctx, int64_t n, const iso_request* req, iso_mesh* out, iso_status* status,
+                             void* stream)
+{
+    if (!ctx || n < 0 || (n > 0 && (!req || !out))) return ISO_ERR_INVALID_ARG;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    ISO_CUDA(ctx, cudaSetDevice(ctx->device));
+    std::vector<iso_status> st((size_t)n, ISO_OK);
+    std::vector<BatchItem> items((size_t)n);
+    std::vector<int> run;  // requests with work
+    for (int64_t r = 0; r < n; ++r) {
+        if (check_mesh(&out[r]) != ISO_OK) {
+            st[r] = ISO_ERR_INVALID_ARG;
+            continue;
+        }
+        out[r].n_points = out[r].n_tris = 0;
+        Grid g;
+        if (!valid_algo(static_cast<iso_algorithm>(req[r].algorithm)) || !make_grid(&req[r].grid, g)) {
+            st[r] = ISO_ERR_INVALID_ARG;
+            continue;
+        }
+        if (empty_grid(g)) continue;
+        if (!req[r].volume) {
+            st[r] = ISO_ERR_INVALID_ARG;
+            continue;
+        }
+        items[r].g = g;
+        items[r].pl = make_plans(ctx, g);
+        if (req[r].algorithm == ISO_MC_DUPFREE && !items[r].pl.gp.fits) {
+            ctx->last_error = "the duplicate-free order needs rows of at most 1024 points";
+            st[r] = ISO_ERR_INVALID_ARG;
+            continue;
+        }
+        run.push_back((int)r);
+    }
+    iso_status rc = ISO_OK;
+    if (!run.empty()) {
+        int lanes = ctx->batch_lanes > 0 ? ctx->batch_lanes : ctx->batch_tuned;
+        if (lanes <= 0) {  // autotuner: time the batch at each lane count, keep the fastest
+            float best = 1e30f;
+            for (int L : kTuneLanes) {
+                if (L > 1 && L > (int)run.size()) break;
+                rc = prepare_batch(ctx, req, out, n, items, run, L, s);
+                if (rc != ISO_OK) return rc;
+                float ms;
+                rc = time_batch(ctx, s, ms);
+                if (rc != ISO_OK) return rc;
+                if (ms < best) {
+                    best = ms;
+                    lanes = L;
+                }
+            }
+            ctx->batch_tuned = lanes;
+        }
+        lanes = std::min(lanes, std::max(1, (int)run.size()));
+        rc = prepare_batch(ctx, req, out, n, items, run, lanes, s);
+        if (rc != ISO_OK) return rc;
+        ISO_CUDA(ctx, cudaGraphLaunch(ctx->batch_exec, s));
+        ISO_CUDA(ctx, cudaStreamSynchronize(s));
+        for (int r : run) {
+            const unsigned long long* c = ctx->h_batch + 8 * (size_t)r;
+            st[r] = finish_counts(ctx, &out[r], (long long)c[0], (long long)c[1], (long long)c[3], &out[r].n_points,
+                                  &out[r].n_tris);
+        }
+    }
+    for (int64_t r = 0; r < n; ++r) {
+        if (status) status[r] = st[r];
+        if (rc == ISO_OK && st[r] != ISO_OK) rc = st[r];
+    }
+    return rc;
+}
+
+iso_status iso_batch_set_lanes(iso_ctx* ctx, int lanes)
+{
+    if (!ctx || lanes < 0 || lanes > kMaxLanes) return ISO_ERR_INVALID_ARG;
+    ctx->batch_lanes = lanes;
+    if (lanes == 0) ctx->batch_tuned = 0;  // tune again on the next batch
+    return ISO_OK;
+}
+
+int iso_batch_lanes(const iso_ctx* ctx)
+{
+    if (!ctx) return 0;
+    return ctx->batch_lanes > 0 ? ctx->batch_lanes : ctx->batch_tuned;
 }
 
 iso_status iso_extract_device(iso_ctx* ctx, iso_algorithm algo, const float* volume, const iso_grid* grid,

@@ -130,8 +130,10 @@ inline void launch_vertices_impl(const float* vol, const Grid& g, float iso, con
                                  int nsm, long long capV, long long capT, float* points, float* normals,
                                  cudaStream_t s)
 {
-    if (k1 <= k0) return;
-    const unsigned blocks = (unsigned)nsm * vertex_ctas_per_sm(MC);
+    if (k1 <= k0 || capV <= 0) return;
+    // one wave, or fewer CTAs when the mesh cannot hold that many vertices (small grids in a batch)
+    const long long wave = (long long)nsm * vertex_ctas_per_sm(MC);
+    const unsigned blocks = (unsigned)std::min(wave, (capV + kThreads - 1) / kThreads);
     k_vertices<MC, COMP><<<blocks, kThreads, 0, s>>>(vol, g, make_grad_scale(g), iso, k0, k1, b.starts, b.totals, capV,
                                                capT, points, normals);
 }
