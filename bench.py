@@ -33,6 +33,14 @@ One step = one full extraction (passes 1-4) of the volume.
             one stream without synchronising; batched = iso_extract_batch
             (lanes picked by its autotuner, graph replayed).  Outputs are
             compared request by request (identical).
+  served    a pool of 8 resident volumes with side lengths log-uniform in
+            [64, 768] per axis (blobs / noise); requests (volume, isovalue in
+            its [p5, p95], Flying Edges) arrive as a Poisson stream at 0.5,
+            1 and 2 times the plain loop's saturated rate.  served = the
+            serving loop (two slots, continuous batching, exact-count
+            admission under a 120 GB budget); plain = one request at a time
+            (iso_count_device, allocate, iso_extract_device).  p50/p99
+            latency and throughput of both; outputs compared at one rate.
 
 --impl reference runs that CPU implementation alone, rank 0 only.
 Under torchrun (N > 1) every rank extracts its own replica (no collective in
@@ -72,6 +80,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batched-reps", type=int, default=5)
+    ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--served-requests", type=int, default=160)
     return ap.parse_args()
 
 
@@ -322,6 +332,54 @@ def batched_leg(M, lib, dev, reps):
     }
 
 
+def served_leg(M, dev, nreq, seed=4, npool=8):
+    """Serving loop vs the plain loop under Poisson arrivals (see the module notes)."""
+    import torch
+    from miniisosurface_gb300 import serve
+    rng = np.random.default_rng(seed)
+    pool = []
+    for v in range(npool):
+        dims = tuple(int(round(x)) for x in np.exp(rng.uniform(np.log(64), np.log(768), size=3)))
+        vol = M.generate_blobs(dims, 8, seed=2000 + v) if v % 2 == 0 else \
+            M.generate_value_noise(dims, 4, 64, seed=2000 + v)
+        lo, hi = np.percentile(vol[:: max(1, vol.shape[0] // 16)], [5, 95])
+        pool.append((torch.from_numpy(np.ascontiguousarray(vol).reshape(-1)).to(dev), dims, lo, hi))
+        del vol
+    volumes = [(v, d) for v, d, _, _ in pool]
+    picks = [(int(rng.integers(npool)),) for _ in range(nreq)]
+    picks = [(vi, float(np.float32(rng.uniform(pool[vi][2], pool[vi][3])))) for (vi,) in picks]
+    cells = [int(np.prod([d - 1 for d in pool[vi][1]])) for vi, _ in picks]
+    reqs_at = lambda times: [(float(t), vi, iso, M.FLYING_EDGES) for t, (vi, iso) in zip(times, picks)]
+    server = serve.Server(volumes, slots=2, max_batch=32, budget_bytes=120 << 30, lanes=8, device=dev.index or 0)
+    serve.run_plain(volumes, reqs_at(np.zeros(nreq))[:8], device=dev.index or 0)  # warm-up
+    server.run(reqs_at(np.zeros(nreq))[:16])
+    sat = serve.summary(serve.run_plain(volumes, reqs_at(np.zeros(nreq)), device=dev.index or 0), cells)
+    sat_served = serve.summary(server.run(reqs_at(np.zeros(nreq))), cells)
+    out = {"pool": [list(d) for _, d, _, _ in pool], "requests": nreq, "mean_cells": float(np.mean(cells)),
+           "saturated": {"plain": sat, "served": sat_served,
+                         "speedup": sat_served["requests_per_s"] / sat["requests_per_s"]},
+           "rates": []}
+    identical = None
+    for f in (0.5, 1.0, 2.0):
+        rate = f * sat["requests_per_s"]
+        times = serve.poisson_arrivals(nreq, rate, seed=seed + int(10 * f))
+        keep = identical is None
+        p = serve.run_plain(volumes, reqs_at(times), device=dev.index or 0, keep_meshes=keep)
+        s = server.run(reqs_at(times), keep_meshes=keep)
+        if keep:
+            identical = all(
+                (a.n_points, a.n_tris) == (b.n_points, b.n_tris) and
+                torch.equal(a.mesh.points[: a.n_points], b.mesh.points[: b.n_points]) and
+                torch.equal(a.mesh.normals[: a.n_points], b.mesh.normals[: b.n_points]) and
+                torch.equal(a.mesh.tris[: a.n_tris], b.mesh.tris[: b.n_tris]) for a, b in zip(p, s))
+            for r in p + s:
+                r.mesh = None
+        out["rates"].append({"rate_per_s": rate, "x_plain_capacity": f, "plain": serve.summary(p, cells),
+                             "served": serve.summary(s, cells)})
+    out["identical_output"] = identical
+    return out
+
+
 def run_reference(args, rank):
     if rank != 0:
         return
@@ -552,6 +610,8 @@ def main():
         }
         if not args.no_batched:
             line["batched"] = batched_leg(M, lib, dev, args.batched_reps)
+        if not args.no_served:
+            line["served"] = served_leg(M, dev, args.served_requests)
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(vol_host, args.cpu_seconds)
         print(json.dumps(line), flush=True)

@@ -189,8 +189,15 @@ typedef struct iso_request {
 iso_status iso_extract_batch(iso_ctx* ctx, int64_t n, const iso_request* req, iso_mesh* out, iso_status* status,
                              void* stream);
 
-/* Lanes of iso_extract_batch: a fixed count (1..64), or 0 (the default): the
- * autotuner times the context's next batch at 1, 2, 4, 8, 16 and 32 lanes
+/* Counts only (passes 1-3) of a batch of requests, the same lanes and graph
+ * as iso_extract_batch without the generate passes: n_points[r] / n_tris[r]
+ * receive what iso_count_device returns for request r, for all requests with
+ * one synchronisation (sizing meshes, admitting requests by output bytes). */
+iso_status iso_count_batch(iso_ctx* ctx, int64_t n, const iso_request* req, int64_t* n_points, int64_t* n_tris,
+                           iso_status* status, void* stream);
+
+/* Lanes of iso_extract_batch / iso_count_batch: a fixed count (1..64), or 0
+ * (the default): the autotuner times the context's next batch at 1, 2, 4, 8, 16 and 32 lanes
  * (each run writes the same meshes) and keeps the fastest count for that batch and
  * the ones after it.  iso_batch_lanes returns the count in use (0 before the
  * autotuner has run). */

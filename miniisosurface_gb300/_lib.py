@@ -75,6 +75,8 @@ SIGNATURES = {
                                    C.POINTER(IsoMesh), C.c_void_p]),
     "iso_extract_batch": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(IsoRequest), C.POINTER(IsoMesh),
                                     C.POINTER(C.c_int), C.c_void_p]),
+    "iso_count_batch": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(IsoRequest), C.POINTER(C.c_int64),
+                                  C.POINTER(C.c_int64), C.POINTER(C.c_int), C.c_void_p]),
     "iso_batch_set_lanes": (C.c_int, [C.c_void_p, C.c_int]),
     "iso_batch_lanes": (C.c_int, [C.c_void_p]),
     "iso_fe_create": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(IsoGrid), C.c_float, C.POINTER(C.c_void_p)]),

@@ -60,8 +60,9 @@ struct iso_ctx {
     size_t batch_arena_bytes = 0;
     unsigned long long* h_batch = nullptr;  // pinned: 8 counters per request
     size_t h_batch_n = 0;
-    cudaGraphExec_t batch_exec = nullptr;
-    std::vector<unsigned char> batch_key;  // what the graph in batch_exec was captured for
+    // executable graphs of iso_extract_batch [0] and iso_count_batch [1], and what each was captured for
+    cudaGraphExec_t batch_exec[2] = {nullptr, nullptr};
+    std::vector<unsigned char> batch_key[2];
     int reverse = 1;  // pass 4 walks the planes backwards (the count pass leaves the last ones in L2)
     int stream_host = 1;  // iso_extract_host streams slabs (large grids)
     std::string last_error;
@@ -890,7 +891,7 @@ BatchLayout plan_batch(const iso_request* req, const iso_mesh* out, int64_t n, s
         items[r].lane = l;
         load[l] += cells(r);
         scratch[l] = std::max(scratch[l], scratch_size(items[r].g, items[r].pl.cp));
-        if (req[r].algorithm == ISO_MARCHING_CUBES) {
+        if (out && req[r].algorithm == ISO_MARCHING_CUBES) {
             const long long capV = vertex_limit(&out[r], out[r].cap_points);
             const long long capM = capV < 0xffffffffll ? capV : 0xffffffffll;
             map[l] = std::max(map[l], (size_t)(capM + 1024) * 4);
@@ -950,13 +951,15 @@ std::vector<unsigned char> batch_key(const iso_ctx* ctx, int lanes, const iso_re
         const unsigned char* c = static_cast<const unsigned char*>(p);
         k.insert(k.end(), c, c + len);
     };
+    const unsigned char count_only = out ? 0 : 1;
+    put(&count_only, 1);
     put(&lanes, sizeof lanes);
     put(&ctx->reverse, sizeof ctx->reverse);
     put(&ctx->batch_arena, sizeof ctx->batch_arena);
     put(&ctx->h_batch, sizeof ctx->h_batch);
     put(&n, sizeof n);
     put(req, (size_t)n * sizeof(iso_request));
-    for (int64_t r = 0; r < n; ++r) {
+    for (int64_t r = 0; out && r < n; ++r) {
         put(&out[r].points, sizeof out[r].points);
         put(&out[r].normals, sizeof out[r].normals);
         put(&out[r].tris, sizeof out[r].tris);
@@ -968,13 +971,16 @@ std::vector<unsigned char> batch_key(const iso_ctx* ctx, int lanes, const iso_re
 }
 
 // Capture the batch on the lanes and make ctx->batch_exec run it (updating
-// the executable graph in place when the topology allows).
+// the executable graph in place when the topology allows).  out == nullptr:
+// passes 1-3 only (iso_count_batch).
 iso_status capture_batch(iso_ctx* ctx, const iso_request* req, const iso_mesh* out, int64_t n,
                          std::vector<BatchItem>& items, const std::vector<int>& run, const BatchLayout& lay)
 {
     char* arena = static_cast<char*>(ctx->batch_arena);
     unsigned long long* counters = reinterpret_cast<unsigned long long*>(arena);
     cudaStream_t sc = ctx->s_capture;
+    const int slot = out ? 0 : 1;
+    cudaGraphExec_t& exec = ctx->batch_exec[slot];
     const bool prof = ctx->profiling;
     ctx->profiling = false;  // no timing events inside the graph
     cudaGraph_t graph = nullptr;
@@ -992,7 +998,7 @@ iso_status capture_batch(iso_ctx* ctx, const iso_request* req, const iso_mesh* o
             PassMarks pm(ctx, ls);
             const iso_algorithm algo = static_cast<iso_algorithm>(req[r].algorithm);
             enqueue_count(ctx, algo, req[r].volume, it.g, req[r].isoval, it.pl, b, ls, pm);
-            enqueue_generate(ctx, algo, req[r].volume, it.g, req[r].isoval, it.pl, b, &out[r], ls, pm);
+            if (out) enqueue_generate(ctx, algo, req[r].volume, it.g, req[r].isoval, it.pl, b, &out[r], ls, pm);
         }
         for (int l = 0; l < lay.lanes; ++l) {
             cudaEventRecord(ctx->lane_join[l], ctx->lane_streams[l]);
@@ -1006,23 +1012,23 @@ iso_status capture_batch(iso_ctx* ctx, const iso_request* req, const iso_mesh* o
     if (e != cudaSuccess || !graph) {
         cudaGetLastError();
         if (graph) cudaGraphDestroy(graph);
-        ctx->batch_key.clear();
+        ctx->batch_key[slot].clear();
         ctx->last_error = std::string("capturing the batch failed: ") + cudaGetErrorString(e);
         return ISO_ERR_CUDA;
     }
-    if (ctx->batch_exec) {
+    if (exec) {
         cudaGraphExecUpdateResultInfo info;
-        if (cudaGraphExecUpdate(ctx->batch_exec, graph, &info) != cudaSuccess) {
+        if (cudaGraphExecUpdate(exec, graph, &info) != cudaSuccess) {
             cudaGetLastError();
-            cudaGraphExecDestroy(ctx->batch_exec);
-            ctx->batch_exec = nullptr;
+            cudaGraphExecDestroy(exec);
+            exec = nullptr;
         }
     }
-    if (!ctx->batch_exec) e = cudaGraphInstantiate(&ctx->batch_exec, graph, 0);
+    if (!exec) e = cudaGraphInstantiate(&exec, graph, 0);
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) {
-        ctx->batch_exec = nullptr;
-        ctx->batch_key.clear();
+        exec = nullptr;
+        ctx->batch_key[slot].clear();
         return cuda_fail(ctx, e, "cudaGraphInstantiate");
     }
     return ISO_OK;
@@ -1036,19 +1042,20 @@ iso_status prepare_batch(iso_ctx* ctx, const iso_request* req, const iso_mesh* o
     iso_status st = ensure_batch(ctx, lay, n, s);
     if (st != ISO_OK) return st;
     std::vector<unsigned char> key = batch_key(ctx, lanes, req, out, n);
-    if (ctx->batch_exec && key == ctx->batch_key) return ISO_OK;
+    const int slot = out ? 0 : 1;
+    if (ctx->batch_exec[slot] && key == ctx->batch_key[slot]) return ISO_OK;
     st = capture_batch(ctx, req, out, n, items, run, lay);
-    if (st == ISO_OK) ctx->batch_key.swap(key);
+    if (st == ISO_OK) ctx->batch_key[slot].swap(key);
     return st;
 }
 
 // Milliseconds of one run of the prepared batch (the best of two after one warm-up run).
-iso_status time_batch(iso_ctx* ctx, cudaStream_t s, float& best)
+iso_status time_batch(iso_ctx* ctx, cudaGraphExec_t exec, cudaStream_t s, float& best)
 {
     best = 1e30f;
     for (int rep = 0; rep < 3; ++rep) {
         ISO_CUDA(ctx, cudaEventRecord(ctx->batch_t0, s));
-        ISO_CUDA(ctx, cudaGraphLaunch(ctx->batch_exec, s));
+        ISO_CUDA(ctx, cudaGraphLaunch(exec, s));
         ISO_CUDA(ctx, cudaEventRecord(ctx->batch_t1, s));
         ISO_CUDA(ctx, cudaEventSynchronize(ctx->batch_t1));
         float ms = 0.f;
@@ -1209,7 +1216,8 @@ iso_status iso_ctx_destroy(iso_ctx* ctx)
     if (ctx->s_d2h) cudaStreamDestroy(ctx->s_d2h);
     if (ctx->s_cnt) cudaStreamDestroy(ctx->s_cnt);
     for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
-    if (ctx->batch_exec) cudaGraphExecDestroy(ctx->batch_exec);
+    for (cudaGraphExec_t x : ctx->batch_exec)
+        if (x) cudaGraphExecDestroy(x);
     for (cudaStream_t q : ctx->lane_streams) cudaStreamDestroy(q);
     for (cudaEvent_t e : ctx->lane_join) cudaEventDestroy(e);
     for (cudaEvent_t e : {ctx->batch_fork, ctx->batch_t0, ctx->batch_t1})
@@ -1321,21 +1329,29 @@ iso_status iso_extract_device_async(iso_ctx* ctx, iso_algorithm algo, const floa
     return ISO_OK;
 }
 
-iso_status iso_extract_batch(iso_ctx* ctx, int64_t n, const iso_request* req, iso_mesh* out, iso_status* status,
-                             void* stream)
+}  // extern "C"
+
+namespace {
+
+// iso_extract_batch (out != nullptr) and iso_count_batch (out == nullptr, the
+// counts into nV / nT): validate, tune the lanes if asked, run the graph.
+iso_status run_batch(iso_ctx* ctx, int64_t n, const iso_request* req, iso_mesh* out, int64_t* nV, int64_t* nT,
+                     iso_status* status, cudaStream_t s)
 {
-    if (!ctx || n < 0 || (n > 0 && (!req || !out))) return ISO_ERR_INVALID_ARG;
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
     ISO_CUDA(ctx, cudaSetDevice(ctx->device));
     std::vector<iso_status> st((size_t)n, ISO_OK);
     std::vector<BatchItem> items((size_t)n);
     std::vector<int> run;  // requests with work
     for (int64_t r = 0; r < n; ++r) {
-        if (check_mesh(&out[r]) != ISO_OK) {
-            st[r] = ISO_ERR_INVALID_ARG;
-            continue;
+        if (out) {
+            if (check_mesh(&out[r]) != ISO_OK) {
+                st[r] = ISO_ERR_INVALID_ARG;
+                continue;
+            }
+            out[r].n_points = out[r].n_tris = 0;
+        } else {
+            nV[r] = nT[r] = 0;
         }
-        out[r].n_points = out[r].n_tris = 0;
         Grid g;
         if (!valid_algo(static_cast<iso_algorithm>(req[r].algorithm)) || !make_grid(&req[r].grid, g)) {
             st[r] = ISO_ERR_INVALID_ARG;
@@ -1348,7 +1364,7 @@ iso_status iso_extract_batch(iso_ctx* ctx, int64_t n, const iso_request* req, is
         }
         items[r].g = g;
         items[r].pl = make_plans(ctx, g);
-        if (req[r].algorithm == ISO_MC_DUPFREE && !items[r].pl.gp.fits) {
+        if (out && req[r].algorithm == ISO_MC_DUPFREE && !items[r].pl.gp.fits) {
             ctx->last_error = "the duplicate-free order needs rows of at most 1024 points";
             st[r] = ISO_ERR_INVALID_ARG;
             continue;
@@ -1365,7 +1381,7 @@ iso_status iso_extract_batch(iso_ctx* ctx, int64_t n, const iso_request* req, is
                 rc = prepare_batch(ctx, req, out, n, items, run, L, s);
                 if (rc != ISO_OK) return rc;
                 float ms;
-                rc = time_batch(ctx, s, ms);
+                rc = time_batch(ctx, ctx->batch_exec[out ? 0 : 1], s, ms);
                 if (rc != ISO_OK) return rc;
                 if (ms < best) {
                     best = ms;
@@ -1377,12 +1393,16 @@ iso_status iso_extract_batch(iso_ctx* ctx, int64_t n, const iso_request* req, is
         lanes = std::min(lanes, std::max(1, (int)run.size()));
         rc = prepare_batch(ctx, req, out, n, items, run, lanes, s);
         if (rc != ISO_OK) return rc;
-        ISO_CUDA(ctx, cudaGraphLaunch(ctx->batch_exec, s));
+        ISO_CUDA(ctx, cudaGraphLaunch(ctx->batch_exec[out ? 0 : 1], s));
         ISO_CUDA(ctx, cudaStreamSynchronize(s));
         for (int r : run) {
             const unsigned long long* c = ctx->h_batch + 8 * (size_t)r;
-            st[r] = finish_counts(ctx, &out[r], (long long)c[0], (long long)c[1], (long long)c[3], &out[r].n_points,
-                                  &out[r].n_tris);
+            if (out) {
+                st[r] = finish_counts(ctx, &out[r], (long long)c[0], (long long)c[1], (long long)c[3],
+                                      &out[r].n_points, &out[r].n_tris);
+            } else {
+                st[r] = finish_counts(ctx, nullptr, (long long)c[0], (long long)c[1], (long long)c[3], &nV[r], &nT[r]);
+            }
         }
     }
     for (int64_t r = 0; r < n; ++r) {
@@ -1390,6 +1410,24 @@ iso_status iso_extract_batch(iso_ctx* ctx, int64_t n, const iso_request* req, is
         if (rc == ISO_OK && st[r] != ISO_OK) rc = st[r];
     }
     return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+iso_status iso_extract_batch(iso_ctx* ctx, int64_t n, const iso_request* req, iso_mesh* out, iso_status* status,
+                             void* stream)
+{
+    if (!ctx || n < 0 || (n > 0 && (!req || !out))) return ISO_ERR_INVALID_ARG;
+    return run_batch(ctx, n, req, out, nullptr, nullptr, status, static_cast<cudaStream_t>(stream));
+}
+
+iso_status iso_count_batch(iso_ctx* ctx, int64_t n, const iso_request* req, int64_t* n_points, int64_t* n_tris,
+                           iso_status* status, void* stream)
+{
+    if (!ctx || n < 0 || (n > 0 && (!req || !n_points || !n_tris))) return ISO_ERR_INVALID_ARG;
+    return run_batch(ctx, n, req, nullptr, n_points, n_tris, status, static_cast<cudaStream_t>(stream));
 }
 
 iso_status iso_batch_set_lanes(iso_ctx* ctx, int lanes)

@@ -1,0 +1,239 @@
+"""Serving loop over the batched entry points (no counterpart in the reference,
+which extracts one volume per program run).
+
+Requests for (resident volume, isovalue) pairs arrive over time.  Worker
+slots -- each a context and a CUDA stream driven by its own host thread --
+take every request that is waiting when they become free, count them in one
+batch (iso_count_batch), admit them in arrival order while their meshes fit
+the device-memory budget beside the meshes of the other slots' batches, and
+extract the admitted ones in one batch (iso_extract_batch) into meshes of
+exactly the counted size.  Requests that arrive while other slots' batches
+are on the GPU are taken by the next free slot, so the batches of different
+slots overlap on the device (continuous batching); a request that does not
+fit waits at the head of the queue until memory frees up.
+
+`run_plain` is the loop to compare with: one request at a time, in arrival
+order, iso_count_device then iso_extract_device.
+"""
+import collections
+import ctypes as C
+import threading
+import time
+
+import numpy as np
+
+from . import _lib
+from .api import Batch, Context, DeviceMesh, Request, make_grid
+from ._lib import check, load
+
+
+def mesh_bytes(n_points, n_tris, index_bytes=4):
+    """Device bytes of a mesh: float3 points and normals, 3 indices per triangle."""
+    return 24 * int(n_points) + 3 * index_bytes * int(n_tris)
+
+
+def admit(sizes, in_use, budget, index_bytes=4):
+    """How many of the waiting requests (their (n_points, n_tris) in arrival
+    order) a slot admits: the longest prefix whose meshes fit beside `in_use`
+    bytes under `budget`.  Returns (count, bytes).  A request larger than the
+    whole budget is admitted alone once nothing else holds memory, so that it
+    fails loudly instead of waiting forever."""
+    total = 0
+    count = 0
+    for nv, nt in sizes:
+        b = mesh_bytes(nv, nt, index_bytes)
+        if in_use + total + b > budget:
+            if count == 0 and in_use == 0:
+                return 1, b
+            break
+        total += b
+        count += 1
+    return count, total
+
+
+def poisson_arrivals(n, rate, seed=0):
+    """n arrival times (seconds from the first) of a Poisson process of `rate` per second."""
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, n)
+    gaps[0] = 0.0
+    return np.cumsum(gaps)
+
+
+class Result:
+    __slots__ = ("index", "arrival", "done", "n_points", "n_tris", "mesh", "slot", "batch")
+
+    def __init__(self, index, arrival):
+        self.index = index
+        self.arrival = arrival
+        self.done = None
+        self.n_points = self.n_tris = 0
+        self.mesh = None
+        self.slot = -1
+        self.batch = -1
+
+    @property
+    def latency(self):
+        return self.done - self.arrival
+
+
+def _request(volumes, vi, iso, algo):
+    vol, dims = volumes[vi]
+    return Request(vol, dims, iso, algo)
+
+
+class Server:
+    """Continuous batching over `slots` worker slots.
+
+    volumes: list of (contiguous CUDA float32 tensor, dims) kept resident.
+    budget_bytes: device memory the meshes in flight may hold.
+    lanes: lanes of each slot's batches (0 leaves them to the autotuner).
+    """
+
+    def __init__(self, volumes, slots=2, max_batch=64, budget_bytes=120 << 30, lanes=8, device=0,
+                 index_bytes=4):
+        self.volumes = volumes
+        self.slots = slots
+        self.max_batch = max_batch
+        self.budget = budget_bytes
+        self.lanes = lanes
+        self.device = device
+        self.index_bytes = index_bytes
+        self.contexts = [Context(device) for _ in range(slots)]
+        for c in self.contexts:
+            check(load().iso_batch_set_lanes(c.handle, int(lanes)), c.handle)
+
+    def run(self, requests, keep_meshes=False):
+        """Serve `requests` = [(arrival seconds, volume index, isovalue, algorithm)] in real time.
+        Returns one Result per request (latency = completion - arrival, seconds)."""
+        import torch
+
+        lib = load()
+        order = sorted(range(len(requests)), key=lambda i: requests[i][0])
+        results = [None] * len(requests)
+        queue = collections.deque()
+        cond = threading.Condition()
+        state = {"fed": False, "in_use": 0, "error": None, "batches": 0}
+        t0 = time.perf_counter() + 0.002
+
+        def worker(slot):
+            ctx = self.contexts[slot]
+            stream = torch.cuda.Stream(self.device)
+            try:
+                while True:
+                    with cond:
+                        while not queue and not (state["fed"] or state["error"]):
+                            cond.wait()
+                        if state["error"] or (not queue and state["fed"]):
+                            return
+                        take = [queue.popleft() for _ in range(min(len(queue), self.max_batch))]
+                    reqs = [_request(self.volumes, *requests[i][1:]) for i in take]
+                    n = len(reqs)
+                    arr = (_lib.IsoRequest * n)(*[r.descriptor() for r in reqs])
+                    nv, nt = (C.c_int64 * n)(), (C.c_int64 * n)()
+                    st = (C.c_int * n)()
+                    check(lib.iso_count_batch(ctx.handle, n, arr, nv, nt, st, C.c_void_p(stream.cuda_stream)),
+                          ctx.handle)
+                    sizes = [(nv[i], nt[i]) for i in range(n)]
+                    with cond:
+                        while True:
+                            k, nbytes = admit(sizes, state["in_use"], self.budget, self.index_bytes)
+                            if k > 0 or state["error"]:
+                                break
+                            cond.wait()  # another slot's meshes are holding the memory
+                        if k == 0:
+                            return
+                        state["in_use"] += nbytes
+                        for i in reversed(take[k:]):  # the rest goes back to the head of the queue
+                            queue.appendleft(i)
+                        batch_no = state["batches"]
+                        state["batches"] += 1
+                        cond.notify_all()
+                    with torch.cuda.stream(stream):
+                        meshes = [DeviceMesh(v, t, self.index_bytes, torch.device("cuda", self.device))
+                                  for v, t in sizes[:k]]
+                    codes = Batch(reqs[:k], meshes).run(ctx, stream.cuda_stream)
+                    done = time.perf_counter() - t0
+                    if any(c != 0 for c in codes):
+                        raise RuntimeError("batch request failed: %s" % codes)
+                    for i, m in zip(take[:k], meshes):
+                        r = results[i]
+                        r.done = done
+                        r.n_points, r.n_tris = m.n_points, m.n_tris
+                        r.mesh = m if keep_meshes else None
+                        r.slot, r.batch = slot, batch_no
+                    del meshes
+                    with cond:
+                        state["in_use"] -= nbytes
+                        cond.notify_all()
+            except BaseException as e:  # surfaced by run()
+                with cond:
+                    state["error"] = e
+                    cond.notify_all()
+
+        threads = [threading.Thread(target=worker, args=(s,), daemon=True) for s in range(self.slots)]
+        for th in threads:
+            th.start()
+        for i in order:
+            arrival = requests[i][0]
+            results[i] = Result(i, arrival)
+            wait = t0 + arrival - time.perf_counter()
+            if wait > 0:
+                time.sleep(wait)
+            with cond:
+                if state["error"]:
+                    break
+                queue.append(i)
+                cond.notify_all()
+        with cond:
+            state["fed"] = True
+            cond.notify_all()
+        for th in threads:
+            th.join()
+        if state["error"]:
+            raise state["error"]
+        return results
+
+
+def run_plain(volumes, requests, device=0, index_bytes=4, keep_meshes=False):
+    """One request at a time in arrival order: iso_count_device, allocate the
+    mesh at that size, iso_extract_device.  Same Result records as Server.run."""
+    import torch
+
+    lib = load()
+    ctx = Context(device)
+    stream = torch.cuda.current_stream(device)
+    sh = C.c_void_p(stream.cuda_stream)
+    order = sorted(range(len(requests)), key=lambda i: requests[i][0])
+    results = [None] * len(requests)
+    t0 = time.perf_counter() + 0.002
+    for i in order:
+        arrival, vi, iso, algo = requests[i]
+        r = Result(i, arrival)
+        results[i] = r
+        wait = t0 + arrival - time.perf_counter()
+        if wait > 0:
+            time.sleep(wait)
+        req = _request(volumes, vi, iso, algo)
+        g = make_grid(req.dims, req.spacing, req.origin)
+        nv, nt = C.c_int64(), C.c_int64()
+        a = req.descriptor().algorithm
+        check(lib.iso_count_device(ctx.handle, a, req.volume.data_ptr(), C.byref(g), C.c_float(iso),
+                                   C.byref(nv), C.byref(nt), sh), ctx.handle)
+        m = DeviceMesh(nv.value, nt.value, index_bytes, torch.device("cuda", device))
+        d = m.descriptor()
+        check(lib.iso_extract_device(ctx.handle, a, req.volume.data_ptr(), C.byref(g), C.c_float(iso), C.byref(d),
+                                     sh), ctx.handle)
+        m.n_points, m.n_tris = d.n_points, d.n_tris
+        r.done = time.perf_counter() - t0
+        r.n_points, r.n_tris = m.n_points, m.n_tris
+        r.mesh = m if keep_meshes else None
+    return results
+
+
+def summary(results, cells):
+    """p50 / p99 latency (ms) and throughput of a run; cells[i] = cells of request i."""
+    lat = np.array([r.latency for r in results]) * 1e3
+    span = max(r.done for r in results) - min(r.arrival for r in results)
+    return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "mean_ms": float(lat.mean()), "requests_per_s": len(results) / span,
+            "Mcells_per_s": float(sum(cells)) / span / 1e6}
