@@ -196,6 +196,45 @@ iso_status iso_extract_batch(iso_ctx* ctx, int64_t n, const iso_request* req, is
 iso_status iso_count_batch(iso_ctx* ctx, int64_t n, const iso_request* req, int64_t* n_points, int64_t* n_tris,
                            iso_status* status, void* stream);
 
+/* Learned output-size predictor (no counterpart in the reference): a small
+ * network that predicts how many triangles an isovalue gives in each block of
+ * 16^3 cells, from statistics of the block's samples.  Blocks are numbered
+ * (bz * nby + by) * nbx + bx with nbx = ceil((nx - 1) / 16) and so on.
+ *   iso_block_count     blocks of a grid.
+ *   iso_block_stats     per block (ISO_MLP_IN floats): min, max and a 32-bin
+ *                       histogram of its 17^3 point values over [min, max]
+ *                       (fractions of its points); independent of the
+ *                       isovalue, so computed once per resident volume.
+ *   iso_block_tris      exact triangles of every block at isoval (the count
+ *                       pass's bit rows, summed per block): the training
+ *                       labels and the reference the predictor is judged by.
+ *   iso_mlp_forward     the network (ISO_MLP_IN -> 64 -> 64 -> 1, ReLU,
+ *                       float32, ISO_MLP_PARAMS parameters) on n samples:
+ *                       inputs of sample i are (min - iso[i]) / (max - min),
+ *                       (max - iso[i]) / (max - min) and the 32 fractions of
+ *                       stats row i; y[i] predicts the block's triangles
+ *                       (the package trains it on triangles / 256).  It is
+ *                       meant for blocks with min < iso <= max (the others
+ *                       have no triangles).
+ *   iso_mlp_gradient    gradient of (1/n) sum (y - target)^2 with respect to
+ *                       the parameters (grads, ISO_MLP_PARAMS floats) and the
+ *                       loss, for the same inputs.
+ *   iso_mlp_adam        one Adam step (step counts from 1).
+ * All pointers are device memory; the calls enqueue on `stream`. */
+#define ISO_BLOCK 16
+#define ISO_MLP_IN 34
+#define ISO_MLP_HIDDEN 64
+#define ISO_MLP_PARAMS (ISO_MLP_IN * ISO_MLP_HIDDEN + ISO_MLP_HIDDEN + ISO_MLP_HIDDEN * ISO_MLP_HIDDEN + 2 * ISO_MLP_HIDDEN + 1)
+int64_t iso_block_count(const iso_grid* grid);
+iso_status iso_block_stats(const float* volume, const iso_grid* grid, float* stats, void* stream);
+iso_status iso_block_tris(iso_ctx* ctx, const float* volume, const iso_grid* grid, float isoval, int32_t* counts,
+                          void* stream);
+iso_status iso_mlp_forward(const float* params, const float* stats, const float* isovals, int64_t n, float* y,
+                           void* stream);
+iso_status iso_mlp_gradient(const float* params, const float* stats, const float* isovals, const float* target,
+                            int64_t n, float* grads, float* loss, void* stream);
+iso_status iso_mlp_adam(float* params, float* m, float* v, const float* grads, int64_t step, float lr, void* stream);
+
 /* Lanes of iso_extract_batch / iso_count_batch: a fixed count (1..64), or 0
  * (the default): the autotuner times the context's next batch at 1, 2, 4, 8, 16 and 32 lanes
  * (each run writes the same meshes) and keeps the fastest count for that batch and

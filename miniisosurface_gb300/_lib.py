@@ -78,6 +78,13 @@ SIGNATURES = {
     "iso_count_batch": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(IsoRequest), C.POINTER(C.c_int64),
                                   C.POINTER(C.c_int64), C.POINTER(C.c_int), C.c_void_p]),
     "iso_batch_set_lanes": (C.c_int, [C.c_void_p, C.c_int]),
+    "iso_block_count": (C.c_int64, [C.POINTER(IsoGrid)]),
+    "iso_block_stats": (C.c_int, [C.c_void_p, C.POINTER(IsoGrid), C.c_void_p, C.c_void_p]),
+    "iso_block_tris": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(IsoGrid), C.c_float, C.c_void_p, C.c_void_p]),
+    "iso_mlp_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
+    "iso_mlp_gradient": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p,
+                                   C.c_void_p, C.c_void_p]),
+    "iso_mlp_adam": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_float, C.c_void_p]),
     "iso_batch_lanes": (C.c_int, [C.c_void_p]),
     "iso_fe_create": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(IsoGrid), C.c_float, C.POINTER(C.c_void_p)]),
     "iso_fe_pass1": (C.c_int, [C.c_void_p]),

@@ -1430,6 +1430,27 @@ iso_status iso_count_batch(iso_ctx* ctx, int64_t n, const iso_request* req, int6
     return run_batch(ctx, n, req, nullptr, n_points, n_tris, status, static_cast<cudaStream_t>(stream));
 }
 
+iso_status iso_block_tris(iso_ctx* ctx, const float* volume, const iso_grid* grid, float isoval, int32_t* counts,
+                          void* stream)
+{
+    if (!ctx || !grid) return ISO_ERR_INVALID_ARG;
+    Grid g;
+    if (!make_grid(grid, g)) return ISO_ERR_INVALID_ARG;
+    if (empty_grid(g)) return ISO_OK;
+    if (!volume || !counts) return ISO_ERR_INVALID_ARG;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    ISO_CUDA(ctx, cudaSetDevice(ctx->device));
+    const Plans pl = make_plans(ctx, g);
+    FeBuffers b;
+    iso_status st = ensure_scratch(ctx, g, pl.cp, b, s);
+    if (st != ISO_OK) return st;
+    iso::launch_count(volume, g, isoval, ctx->d_cases, false, pl.cp, b, s);  // bit rows of the whole grid
+    ISO_CUDA(ctx, cudaMemsetAsync(counts, 0, sizeof(int32_t) * (size_t)iso::block_count(g), s));
+    iso::launch_block_tris(g, b.bits, counts, s);
+    ISO_CUDA(ctx, cudaGetLastError());
+    return ISO_OK;
+}
+
 iso_status iso_batch_set_lanes(iso_ctx* ctx, int lanes)
 {
     if (!ctx || lanes < 0 || lanes > kMaxLanes) return ISO_ERR_INVALID_ARG;

@@ -73,6 +73,10 @@ void launch_scan(const Grid& g, const CountPlan& p, int mode, FeBuffers& b, cuda
 // totals and the starts of rows rlo / rhi into out[0..8] (device-visible host memory)
 void launch_slab_readback(const FeBuffers& b, const Grid& g, long long rlo, long long rhi, bool has_lo, bool has_hi,
                           unsigned long long* out, cudaStream_t s);
+// learned output-size predictor (predictor.cu): 16^3-cell blocks
+long long block_count(const Grid& g);
+void launch_block_tris(const Grid& g, const uint32_t* bits, int* counts, cudaStream_t s);
+
 void launch_grid_edges(const Grid& g, const CountPlan& p, const FeBuffers& b, int scanned, unsigned long long* ge,
                        unsigned long long* tri_counter, cudaStream_t s);
 // Row-start accessor of a counted extraction.

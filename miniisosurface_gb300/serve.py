@@ -7,7 +7,10 @@ take every request that is waiting when they become free, count them in one
 batch (iso_count_batch), admit them in arrival order while their meshes fit
 the device-memory budget beside the meshes of the other slots' batches, and
 extract the admitted ones in one batch (iso_extract_batch) into meshes of
-exactly the counted size.  Requests that arrive while other slots' batches
+exactly the counted size.  With a predictor (predictor.Predictor) the count
+batch is skipped: the network sizes every mesh from the resident volumes'
+block statistics in one launch, and a request whose mesh was too small goes
+back to the head of the queue with the exact sizes the extraction reported.  Requests that arrive while other slots' batches
 are on the GPU are taken by the next free slot, so the batches of different
 slots overlap on the device (continuous batching); a request that does not
 fit waits at the head of the queue until memory frees up.
@@ -90,7 +93,7 @@ class Server:
     """
 
     def __init__(self, volumes, slots=2, max_batch=64, budget_bytes=120 << 30, lanes=8, device=0,
-                 index_bytes=4):
+                 index_bytes=4, predictor=None):
         self.volumes = volumes
         self.slots = slots
         self.max_batch = max_batch
@@ -99,6 +102,11 @@ class Server:
         self.device = device
         self.index_bytes = index_bytes
         self.contexts = [Context(device) for _ in range(slots)]
+        self.predictor = predictor
+        self.stats = None
+        if predictor is not None:
+            from .predictor import block_stats
+            self.stats = [block_stats(v, d) for v, d in volumes]
         for c in self.contexts:
             check(load().iso_batch_set_lanes(c.handle, int(lanes)), c.handle)
 
@@ -112,7 +120,8 @@ class Server:
         results = [None] * len(requests)
         queue = collections.deque()
         cond = threading.Condition()
-        state = {"fed": False, "in_use": 0, "error": None, "batches": 0}
+        state = {"fed": False, "in_use": 0, "error": None, "batches": 0, "fallbacks": 0}
+        exact = {}  # request -> exact (n_points, n_tris) after a mesh came out too small
         t0 = time.perf_counter() + 0.002
 
         def worker(slot):
@@ -128,12 +137,19 @@ class Server:
                         take = [queue.popleft() for _ in range(min(len(queue), self.max_batch))]
                     reqs = [_request(self.volumes, *requests[i][1:]) for i in take]
                     n = len(reqs)
-                    arr = (_lib.IsoRequest * n)(*[r.descriptor() for r in reqs])
-                    nv, nt = (C.c_int64 * n)(), (C.c_int64 * n)()
-                    st = (C.c_int * n)()
-                    check(lib.iso_count_batch(ctx.handle, n, arr, nv, nt, st, C.c_void_p(stream.cuda_stream)),
-                          ctx.handle)
-                    sizes = [(nv[i], nt[i]) for i in range(n)]
+                    if self.predictor is not None:
+                        guess = [i for i in take if i not in exact]
+                        caps = self.predictor.capacities(
+                            [(self.stats[requests[i][1]], requests[i][2]) for i in guess], stream.cuda_stream)
+                        pred = dict(zip(guess, caps))
+                        sizes = [exact[i] if i in exact else pred[i] for i in take]
+                    else:
+                        arr = (_lib.IsoRequest * n)(*[r.descriptor() for r in reqs])
+                        nv, nt = (C.c_int64 * n)(), (C.c_int64 * n)()
+                        st = (C.c_int * n)()
+                        check(lib.iso_count_batch(ctx.handle, n, arr, nv, nt, st, C.c_void_p(stream.cuda_stream)),
+                              ctx.handle)
+                        sizes = [(nv[i], nt[i]) for i in range(n)]
                     with cond:
                         while True:
                             k, nbytes = admit(sizes, state["in_use"], self.budget, self.index_bytes)
@@ -153,9 +169,20 @@ class Server:
                                   for v, t in sizes[:k]]
                     codes = Batch(reqs[:k], meshes).run(ctx, stream.cuda_stream)
                     done = time.perf_counter() - t0
-                    if any(c != 0 for c in codes):
+                    redo = [i for i, c in zip(take[:k], codes) if c == _lib.ISO_ERR_CAPACITY]
+                    if any(c not in (0, _lib.ISO_ERR_CAPACITY) for c in codes) or (redo and self.predictor is None):
                         raise RuntimeError("batch request failed: %s" % codes)
-                    for i, m in zip(take[:k], meshes):
+                    if redo:  # predicted too small: back to the head of the queue with the exact sizes
+                        with cond:
+                            for i, m, c in reversed(list(zip(take[:k], meshes, codes))):
+                                if c == _lib.ISO_ERR_CAPACITY:
+                                    exact[i] = (m.n_points, m.n_tris)
+                                    queue.appendleft(i)
+                            state["fallbacks"] += len(redo)
+                            cond.notify_all()
+                    for i, m, c in zip(take[:k], meshes, codes):
+                        if c != 0:
+                            continue
                         r = results[i]
                         r.done = done
                         r.n_points, r.n_tris = m.n_points, m.n_tris
@@ -191,6 +218,7 @@ class Server:
             th.join()
         if state["error"]:
             raise state["error"]
+        self.last_fallbacks = state["fallbacks"]
         return results
 
 

@@ -448,3 +448,22 @@ void oracle_mesh_free(oracle_mesh* m)
     free(m->points); free(m->normals); free(m->tris); free(m->edge_of_vertex);
     memset(m, 0, sizeof(*m));
 }
+
+void oracle_block_tris(const float* data, const size_t dims[3], float iso, int block, int* counts)
+{
+    const size_t nx = dims[0], ny = dims[1], nz = dims[2];
+    if (nx < 2 || ny < 2 || nz < 2) return;
+    const size_t nbx = (nx - 2) / block + 1, nby = (ny - 2) / block + 1, nbz = (nz - 2) / block + 1;
+    memset(counts, 0, sizeof(int) * nbx * nby * nbz);
+    /* corner v: (i + dx[v], j + dy[v], k + dz[v]) */
+    static const int dx[8] = {0, 1, 1, 0, 0, 1, 1, 0}, dy[8] = {0, 0, 1, 1, 0, 0, 1, 1}, dz[8] = {0, 0, 0, 0, 1, 1, 1, 1};
+    for (size_t k = 0; k + 1 < nz; ++k)
+        for (size_t j = 0; j + 1 < ny; ++j)
+            for (size_t i = 0; i + 1 < nx; ++i) {
+                int c = 0;
+                for (int v = 0; v < 8; ++v)
+                    if (data[((k + dz[v]) * ny + (j + dy[v])) * nx + (i + dx[v])] >= iso) c |= 1 << v;
+                const int n = case_ntris(c);
+                if (n) counts[((k / block) * nby + j / block) * nbx + i / block] += n;
+            }
+}

@@ -71,6 +71,15 @@ int oracle_mc_dupfree_run(const float* data, const size_t dims[3], const float s
 
 void oracle_mesh_free(oracle_mesh* m);
 
+/* Triangles per block of `block`^3 cells at isovalue iso: each cell's case
+ * from its eight corners (v0..v7 of Image3D::getValsCube,
+ * flyingEdges/util/Image3D.cpp:26-43; corner bit set when value >= iso, the
+ * test of calcCaseEdge, FlyingEdgesAlgorithm.cpp:31-45) and that case's
+ * triangle count (numTris, flyingEdges/util/MarchingCubesTables.h:23),
+ * summed over the block's cells.  counts has nbx*nby*nbz entries, block
+ * (bx, by, bz) at (bz*nby + by)*nbx + bx, nb = ceil((n-1)/block). */
+void oracle_block_tris(const float* data, const size_t dims[3], float iso, int block, int* counts);
+
 /* Seconds of wall time of the last oracle_fe_run / oracle_mc_run call
  * (extraction only, like the reference's "Total Program WALL Time"). */
 double oracle_last_wall_seconds(void);

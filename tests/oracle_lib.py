@@ -49,6 +49,7 @@ def lib():
         L.oracle_fe_grid_edges.argtypes = [C.c_void_p, C.c_void_p]
         L.oracle_fe_tri_counter.argtypes = [C.c_void_p, C.c_void_p]
         L.oracle_fe_take.argtypes = [C.c_void_p, C.POINTER(OracleMesh)]
+        L.oracle_block_tris.argtypes = [C.c_void_p, sz3, C.c_float, C.c_int, C.c_void_p]
         L.oracle_last_wall_seconds.restype = C.c_double
         L.oracle_mc_last_wall_seconds.restype = C.c_double
         _LIB = L
@@ -86,6 +87,18 @@ def fe(vol, iso, spacing=(1, 1, 1), origin=(0, 0, 0), nthreads=1):
         return _mesh_to_numpy(m)
     finally:
         L.oracle_mesh_free(C.byref(m))
+
+
+def block_tris(vol, iso, block=16):
+    """Triangles per block of block^3 cells (oracle_block_tris)."""
+    vol = np.ascontiguousarray(vol, dtype=np.float32)
+    nz, ny, nx = vol.shape
+    nb = [max(0, (n - 2) // block + 1) if n >= 2 else 0 for n in (nx, ny, nz)]
+    out = np.zeros(nb[0] * nb[1] * nb[2], dtype=np.int32)
+    if out.size:
+        dims = (C.c_size_t * 3)(nx, ny, nz)
+        lib().oracle_block_tris(vol.ctypes.data, dims, C.c_float(iso), block, out.ctypes.data)
+    return out
 
 
 def fe_wall_seconds():
