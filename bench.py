@@ -39,8 +39,10 @@ One step = one full extraction (passes 1-4) of the volume.
             1 and 2 times the plain loop's saturated rate.  served = the
             serving loop (two slots, continuous batching, exact-count
             admission under a 120 GB budget); plain = one request at a time
-            (iso_count_device, allocate, iso_extract_device).  p50/p99
-            latency and throughput of both; outputs compared at one rate.
+            (iso_count_device, allocate, iso_extract_device); served_predicted
+            = the serving loop sizing meshes with the trained output-size
+            network instead of the count batch (fallbacks counted).  p50/p99
+            latency and throughput of each; outputs compared at one rate.
 
 --impl reference runs that CPU implementation alone, rank 0 only.
 Under torchrun (N > 1) every rank extracts its own replica (no collective in
@@ -350,15 +352,29 @@ def served_leg(M, dev, nreq, seed=4, npool=8):
     picks = [(vi, float(np.float32(rng.uniform(pool[vi][2], pool[vi][3])))) for (vi,) in picks]
     cells = [int(np.prod([d - 1 for d in pool[vi][1]])) for vi, _ in picks]
     reqs_at = lambda times: [(float(t), vi, iso, M.FLYING_EDGES) for t, (vi, iso) in zip(times, picks)]
+    from miniisosurface_gb300 import predictor as P
     server = serve.Server(volumes, slots=2, max_batch=32, budget_bytes=120 << 30, lanes=8, device=dev.index or 0)
+    server_p = serve.Server(volumes, slots=2, max_batch=32, budget_bytes=120 << 30, lanes=8, device=dev.index or 0,
+                            predictor=P.Predictor.load(device=dev)) if P.WEIGHTS.exists() else None
     serve.run_plain(volumes, reqs_at(np.zeros(nreq))[:8], device=dev.index or 0)  # warm-up
     server.run(reqs_at(np.zeros(nreq))[:16])
+    if server_p:
+        server_p.run(reqs_at(np.zeros(nreq))[:16])
+
+    def served_p(times, keep=False):
+        res = server_p.run(reqs_at(times), keep_meshes=keep)
+        return res, dict(serve.summary(res, cells), fallbacks=server_p.last_fallbacks)
+
     sat = serve.summary(serve.run_plain(volumes, reqs_at(np.zeros(nreq)), device=dev.index or 0), cells)
     sat_served = serve.summary(server.run(reqs_at(np.zeros(nreq))), cells)
     out = {"pool": [list(d) for _, d, _, _ in pool], "requests": nreq, "mean_cells": float(np.mean(cells)),
            "saturated": {"plain": sat, "served": sat_served,
                          "speedup": sat_served["requests_per_s"] / sat["requests_per_s"]},
            "rates": []}
+    if server_p:
+        _, sat_p = served_p(np.zeros(nreq))
+        out["saturated"]["served_predicted"] = sat_p
+        out["saturated"]["speedup_predicted"] = sat_p["requests_per_s"] / sat["requests_per_s"]
     identical = None
     for f in (0.5, 1.0, 2.0):
         rate = f * sat["requests_per_s"]
@@ -366,16 +382,20 @@ def served_leg(M, dev, nreq, seed=4, npool=8):
         keep = identical is None
         p = serve.run_plain(volumes, reqs_at(times), device=dev.index or 0, keep_meshes=keep)
         s = server.run(reqs_at(times), keep_meshes=keep)
+        sp, sp_sum = served_p(times, keep) if server_p else ([], None)
         if keep:
-            identical = all(
-                (a.n_points, a.n_tris) == (b.n_points, b.n_tris) and
-                torch.equal(a.mesh.points[: a.n_points], b.mesh.points[: b.n_points]) and
-                torch.equal(a.mesh.normals[: a.n_points], b.mesh.normals[: b.n_points]) and
-                torch.equal(a.mesh.tris[: a.n_tris], b.mesh.tris[: b.n_tris]) for a, b in zip(p, s))
-            for r in p + s:
+            same = lambda a, b: ((a.n_points, a.n_tris) == (b.n_points, b.n_tris) and
+                                 torch.equal(a.mesh.points[: a.n_points], b.mesh.points[: b.n_points]) and
+                                 torch.equal(a.mesh.normals[: a.n_points], b.mesh.normals[: b.n_points]) and
+                                 torch.equal(a.mesh.tris[: a.n_tris], b.mesh.tris[: b.n_tris]))
+            identical = all(same(a, b) for a, b in zip(p, s)) and all(same(a, b) for a, b in zip(p, sp))
+            for r in p + s + sp:
                 r.mesh = None
-        out["rates"].append({"rate_per_s": rate, "x_plain_capacity": f, "plain": serve.summary(p, cells),
-                             "served": serve.summary(s, cells)})
+        entry = {"rate_per_s": rate, "x_plain_capacity": f, "plain": serve.summary(p, cells),
+                 "served": serve.summary(s, cells)}
+        if sp_sum:
+            entry["served_predicted"] = sp_sum
+        out["rates"].append(entry)
     out["identical_output"] = identical
     return out
 

@@ -220,6 +220,14 @@ iso_status iso_count_batch(iso_ctx* ctx, int64_t n, const iso_request* req, int6
  *                       the parameters (grads, ISO_MLP_PARAMS floats) and the
  *                       loss, for the same inputs.
  *   iso_mlp_adam        one Adam step (step counts from 1).
+ *   iso_mlp_predict     for each of n_sets (block statistics, isovalue)
+ *                       sets -- a volume's iso_block_stats and one isovalue
+ *                       -- totals[s] = the sum of max(y, 0) over the set's
+ *                       blocks with min < iso <= max: the predicted
+ *                       triangles of a whole extraction (in the units the
+ *                       network was trained on), all sets in one launch per
+ *                       128 sets; totals (n_sets floats, device) is zeroed
+ *                       first; `sets` is a host array.
  * All pointers are device memory; the calls enqueue on `stream`. */
 #define ISO_BLOCK 16
 #define ISO_MLP_IN 34
@@ -234,6 +242,13 @@ iso_status iso_mlp_forward(const float* params, const float* stats, const float*
 iso_status iso_mlp_gradient(const float* params, const float* stats, const float* isovals, const float* target,
                             int64_t n, float* grads, float* loss, void* stream);
 iso_status iso_mlp_adam(float* params, float* m, float* v, const float* grads, int64_t step, float lr, void* stream);
+typedef struct iso_block_set {
+    const float* stats; /* n_blocks x ISO_MLP_IN, device */
+    int64_t n_blocks;
+    float isoval;
+} iso_block_set;
+iso_status iso_mlp_predict(const float* params, int64_t n_sets, const iso_block_set* sets, float* totals,
+                           void* stream);
 
 /* Lanes of iso_extract_batch / iso_count_batch: a fixed count (1..64), or 0
  * (the default): the autotuner times the context's next batch at 1, 2, 4, 8, 16 and 32 lanes
@@ -241,6 +256,14 @@ iso_status iso_mlp_adam(float* params, float* m, float* v, const float* grads, i
  * the ones after it.  iso_batch_lanes returns the count in use (0 before the
  * autotuner has run). */
 iso_status iso_batch_set_lanes(iso_ctx* ctx, int lanes);
+/* Whether the context's batches are captured as CUDA graphs (1, the default:
+ * a repeated batch only relaunches its graph) or their lanes are launched
+ * directly each call (0: no capture, for batches that change every call, as
+ * in a serving loop; the lanes default to 8, or the autotuner's count once it
+ * has run).  While a batch is being captured, no other thread may free device
+ * memory or synchronise the device: that would invalidate the capture (the
+ * library's own calls take turns with captures). */
+iso_status iso_batch_set_graph(iso_ctx* ctx, int enable);
 int iso_batch_lanes(const iso_ctx* ctx);
 
 /* z-slabs: the grid split along z into slabs of planes [k0, k1), for

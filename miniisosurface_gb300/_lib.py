@@ -41,6 +41,10 @@ class IsoMesh(C.Structure):
                 ("n_points", C.c_int64), ("n_tris", C.c_int64)]
 
 
+class IsoBlockSet(C.Structure):
+    _fields_ = [("stats", C.c_void_p), ("n_blocks", C.c_int64), ("isoval", C.c_float)]
+
+
 class IsoRequest(C.Structure):
     _fields_ = [("volume", C.c_void_p), ("grid", IsoGrid), ("isoval", C.c_float), ("algorithm", C.c_int32)]
 
@@ -78,6 +82,7 @@ SIGNATURES = {
     "iso_count_batch": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(IsoRequest), C.POINTER(C.c_int64),
                                   C.POINTER(C.c_int64), C.POINTER(C.c_int), C.c_void_p]),
     "iso_batch_set_lanes": (C.c_int, [C.c_void_p, C.c_int]),
+    "iso_batch_set_graph": (C.c_int, [C.c_void_p, C.c_int]),
     "iso_block_count": (C.c_int64, [C.POINTER(IsoGrid)]),
     "iso_block_stats": (C.c_int, [C.c_void_p, C.POINTER(IsoGrid), C.c_void_p, C.c_void_p]),
     "iso_block_tris": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(IsoGrid), C.c_float, C.c_void_p, C.c_void_p]),
@@ -85,6 +90,7 @@ SIGNATURES = {
     "iso_mlp_gradient": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p,
                                    C.c_void_p, C.c_void_p]),
     "iso_mlp_adam": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_float, C.c_void_p]),
+    "iso_mlp_predict": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(IsoBlockSet), C.c_void_p, C.c_void_p]),
     "iso_batch_lanes": (C.c_int, [C.c_void_p]),
     "iso_fe_create": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(IsoGrid), C.c_float, C.POINTER(C.c_void_p)]),
     "iso_fe_pass1": (C.c_int, [C.c_void_p]),

@@ -425,6 +425,12 @@ def set_batch_lanes(lanes, ctx=None):
     check(load().iso_batch_set_lanes(ctx.handle, int(lanes)), ctx.handle)
 
 
+def set_batch_graph(enable, ctx=None):
+    """Capture batches as CUDA graphs (default) or launch their lanes directly."""
+    ctx = ctx or default_context()
+    check(load().iso_batch_set_graph(ctx.handle, 1 if enable else 0), ctx.handle)
+
+
 def batch_lanes(ctx=None):
     ctx = ctx or default_context()
     return int(load().iso_batch_lanes(ctx.handle))

@@ -52,6 +52,7 @@ struct iso_ctx {
     // batched entry point (iso_extract_batch): lanes, their scratch, the captured graph
     int batch_lanes = 0;        // set by iso_batch_set_lanes; 0: the autotuner's choice
     int batch_tuned = 0;        // lanes the autotuner picked (0: not yet tuned)
+    int batch_graph = 1;        // capture batches as CUDA graphs (0: launch the lanes directly)
     cudaStream_t s_capture = nullptr;
     std::vector<cudaStream_t> lane_streams;
     std::vector<cudaEvent_t> lane_join;
@@ -909,11 +910,17 @@ BatchLayout plan_batch(const iso_request* req, const iso_mesh* out, int64_t n, s
     return lay;
 }
 
+// Captures and the batch buffers' allocations of all contexts take turns: a
+// free (which synchronises the device) in one thread would invalidate a
+// capture running in another.
+std::mutex g_batch_mutex;
+
+// Batch buffers (the caller holds g_batch_mutex).  Only this context's work on
+// s uses them: the graphs and the lanes join back into s.
 iso_status ensure_batch(iso_ctx* ctx, const BatchLayout& lay, int64_t n, cudaStream_t s)
 {
     if (lay.bytes > ctx->batch_arena_bytes) {
         ISO_CUDA(ctx, cudaStreamSynchronize(s));
-        ISO_CUDA(ctx, cudaDeviceSynchronize());
         cudaFree(ctx->batch_arena);
         ctx->batch_arena = nullptr;
         ctx->batch_arena_bytes = 0;
@@ -970,45 +977,53 @@ std::vector<unsigned char> batch_key(const iso_ctx* ctx, int lanes, const iso_re
     return k;
 }
 
+// The batch's work from `origin`: fork to the lanes, each lane's requests in
+// turn, join, the counters' copy to the host; all on origin's side of the join.
+void enqueue_batch(iso_ctx* ctx, const iso_request* req, const iso_mesh* out, int64_t n, std::vector<BatchItem>& items,
+                   const std::vector<int>& run, const BatchLayout& lay, cudaStream_t origin)
+{
+    char* arena = static_cast<char*>(ctx->batch_arena);
+    unsigned long long* counters = reinterpret_cast<unsigned long long*>(arena);
+    const bool prof = ctx->profiling;
+    ctx->profiling = false;  // no timing events between the lanes' kernels
+    cudaEventRecord(ctx->batch_fork, origin);
+    for (int l = 0; l < lay.lanes; ++l) cudaStreamWaitEvent(ctx->lane_streams[l], ctx->batch_fork, 0);
+    for (int r : run) {
+        BatchItem& it = items[r];
+        cudaStream_t ls = ctx->lane_streams[it.lane];
+        FeBuffers b;
+        carve(arena + lay.scratch_at[it.lane], it.g, it.pl.cp, b);
+        b.totals = counters + 8 * r;
+        b.fe2mc = reinterpret_cast<uint32_t*>(arena + lay.map_at[it.lane]);
+        PassMarks pm(ctx, ls);
+        const iso_algorithm algo = static_cast<iso_algorithm>(req[r].algorithm);
+        enqueue_count(ctx, algo, req[r].volume, it.g, req[r].isoval, it.pl, b, ls, pm);
+        if (out) enqueue_generate(ctx, algo, req[r].volume, it.g, req[r].isoval, it.pl, b, &out[r], ls, pm);
+    }
+    for (int l = 0; l < lay.lanes; ++l) {
+        cudaEventRecord(ctx->lane_join[l], ctx->lane_streams[l]);
+        cudaStreamWaitEvent(origin, ctx->lane_join[l], 0);
+    }
+    cudaMemcpyAsync(ctx->h_batch, counters, (size_t)n * 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                    origin);
+    ctx->profiling = prof;
+}
+
 // Capture the batch on the lanes and make ctx->batch_exec run it (updating
 // the executable graph in place when the topology allows).  out == nullptr:
 // passes 1-3 only (iso_count_batch).
 iso_status capture_batch(iso_ctx* ctx, const iso_request* req, const iso_mesh* out, int64_t n,
                          std::vector<BatchItem>& items, const std::vector<int>& run, const BatchLayout& lay)
 {
-    char* arena = static_cast<char*>(ctx->batch_arena);
-    unsigned long long* counters = reinterpret_cast<unsigned long long*>(arena);
     cudaStream_t sc = ctx->s_capture;
     const int slot = out ? 0 : 1;
     cudaGraphExec_t& exec = ctx->batch_exec[slot];
-    const bool prof = ctx->profiling;
-    ctx->profiling = false;  // no timing events inside the graph
     cudaGraph_t graph = nullptr;
     cudaError_t e = cudaStreamBeginCapture(sc, cudaStreamCaptureModeRelaxed);
     if (e == cudaSuccess) {
-        cudaEventRecord(ctx->batch_fork, sc);
-        for (int l = 0; l < lay.lanes; ++l) cudaStreamWaitEvent(ctx->lane_streams[l], ctx->batch_fork, 0);
-        for (int r : run) {
-            BatchItem& it = items[r];
-            cudaStream_t ls = ctx->lane_streams[it.lane];
-            FeBuffers b;
-            carve(arena + lay.scratch_at[it.lane], it.g, it.pl.cp, b);
-            b.totals = counters + 8 * r;
-            b.fe2mc = reinterpret_cast<uint32_t*>(arena + lay.map_at[it.lane]);
-            PassMarks pm(ctx, ls);
-            const iso_algorithm algo = static_cast<iso_algorithm>(req[r].algorithm);
-            enqueue_count(ctx, algo, req[r].volume, it.g, req[r].isoval, it.pl, b, ls, pm);
-            if (out) enqueue_generate(ctx, algo, req[r].volume, it.g, req[r].isoval, it.pl, b, &out[r], ls, pm);
-        }
-        for (int l = 0; l < lay.lanes; ++l) {
-            cudaEventRecord(ctx->lane_join[l], ctx->lane_streams[l]);
-            cudaStreamWaitEvent(sc, ctx->lane_join[l], 0);
-        }
-        cudaMemcpyAsync(ctx->h_batch, counters, (size_t)n * 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
-                        sc);
+        enqueue_batch(ctx, req, out, n, items, run, lay, sc);
         e = cudaStreamEndCapture(sc, &graph);
     }
-    ctx->profiling = prof;
     if (e != cudaSuccess || !graph) {
         cudaGetLastError();
         if (graph) cudaGraphDestroy(graph);
@@ -1039,6 +1054,7 @@ iso_status prepare_batch(iso_ctx* ctx, const iso_request* req, const iso_mesh* o
                          std::vector<BatchItem>& items, const std::vector<int>& run, int lanes, cudaStream_t s)
 {
     const BatchLayout lay = plan_batch(req, out, n, items, run, lanes);
+    std::lock_guard<std::mutex> lock(g_batch_mutex);
     iso_status st = ensure_batch(ctx, lay, n, s);
     if (st != ISO_OK) return st;
     std::vector<unsigned char> key = batch_key(ctx, lanes, req, out, n);
@@ -1372,7 +1388,19 @@ iso_status run_batch(iso_ctx* ctx, int64_t n, const iso_request* req, iso_mesh* 
         run.push_back((int)r);
     }
     iso_status rc = ISO_OK;
-    if (!run.empty()) {
+    if (!run.empty() && !ctx->batch_graph) {  // the lanes launched directly, no graph
+        int lanes = ctx->batch_lanes > 0 ? ctx->batch_lanes : (ctx->batch_tuned > 0 ? ctx->batch_tuned : 8);
+        lanes = std::min(lanes, std::max(1, (int)run.size()));
+        const BatchLayout lay = plan_batch(req, out, n, items, run, lanes);
+        {
+            std::lock_guard<std::mutex> lock(g_batch_mutex);
+            rc = ensure_batch(ctx, lay, n, s);
+        }
+        if (rc != ISO_OK) return rc;
+        enqueue_batch(ctx, req, out, n, items, run, lay, s);
+        ISO_CUDA(ctx, cudaGetLastError());
+        ISO_CUDA(ctx, cudaStreamSynchronize(s));
+    } else if (!run.empty()) {
         int lanes = ctx->batch_lanes > 0 ? ctx->batch_lanes : ctx->batch_tuned;
         if (lanes <= 0) {  // autotuner: time the batch at each lane count, keep the fastest
             float best = 1e30f;
@@ -1395,6 +1423,8 @@ iso_status run_batch(iso_ctx* ctx, int64_t n, const iso_request* req, iso_mesh* 
         if (rc != ISO_OK) return rc;
         ISO_CUDA(ctx, cudaGraphLaunch(ctx->batch_exec[out ? 0 : 1], s));
         ISO_CUDA(ctx, cudaStreamSynchronize(s));
+    }
+    if (!run.empty()) {
         for (int r : run) {
             const unsigned long long* c = ctx->h_batch + 8 * (size_t)r;
             if (out) {
@@ -1456,6 +1486,13 @@ iso_status iso_batch_set_lanes(iso_ctx* ctx, int lanes)
     if (!ctx || lanes < 0 || lanes > kMaxLanes) return ISO_ERR_INVALID_ARG;
     ctx->batch_lanes = lanes;
     if (lanes == 0) ctx->batch_tuned = 0;  // tune again on the next batch
+    return ISO_OK;
+}
+
+iso_status iso_batch_set_graph(iso_ctx* ctx, int enable)
+{
+    if (!ctx) return ISO_ERR_INVALID_ARG;
+    ctx->batch_graph = enable ? 1 : 0;
     return ISO_OK;
 }
 

@@ -219,6 +219,66 @@ __global__ void __launch_bounds__(256) k_mlp_forward(const float* __restrict__ p
     }
 }
 
+// Prediction for many (block statistics, isovalue) sets in one launch: the
+// samples are the sets' blocks one after another; a block counts when
+// min < iso <= max, and max(y, 0) of those is added to its set's total.
+constexpr int kMaxSets = 128;
+struct PredictSets {
+    int n;
+    long long start[kMaxSets + 1];  // first sample of each set; start[n] = all samples
+    const float* stats[kMaxSets];
+    float iso[kMaxSets];
+};
+
+__global__ void __launch_bounds__(256) k_mlp_predict(const float* __restrict__ params, PredictSets sets,
+                                                     float* __restrict__ totals)
+{
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    MlpSmem& s = *reinterpret_cast<MlpSmem*>(s_raw);
+    __shared__ int s_set[kTile];
+    load_params(s, params);
+    __syncthreads();
+    const long long n = sets.start[sets.n];
+    for (long long base = (long long)blockIdx.x * kTile; base < n; base += (long long)gridDim.x * kTile) {
+        if (threadIdx.x < kTile) {  // the set of sample base + t (-1: past the end or an inactive block)
+            const long long q = base + threadIdx.x;
+            int set = -1;
+            if (q < n) {
+                int lo = 0, hi = sets.n - 1;  // last set with start <= q
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (sets.start[mid] <= q) lo = mid;
+                    else hi = mid - 1;
+                }
+                const float* st = sets.stats[lo] + (q - sets.start[lo]) * kIn;
+                if (st[0] < sets.iso[lo] && st[1] >= sets.iso[lo]) set = lo;
+            }
+            s_set[threadIdx.x] = set;
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < kTile * kIn; i += blockDim.x) {
+            const int r = i / kIn, c = i % kIn;
+            const int set = s_set[r];
+            float v = 0.f;
+            if (set >= 0) {
+                const float* st = sets.stats[set] + (base + r - sets.start[set]) * kIn;
+                if (c < 2) {
+                    const float range = st[1] - st[0];
+                    v = range > 0.f ? (st[c] - sets.iso[set]) / range : 0.f;
+                } else {
+                    v = st[c];
+                }
+            }
+            s.x[r * kXPad + c] = v;
+        }
+        __syncthreads();
+        forward_tile(s);
+        if (threadIdx.x < kTile && s_set[threadIdx.x] >= 0)
+            atomicAdd(&totals[s_set[threadIdx.x]], fmaxf(s.y[threadIdx.x], 0.f));
+        __syncthreads();
+    }
+}
+
 // Gradient of the mean squared error (1/n) sum (y - target)^2 with respect
 // to every parameter, added into grads (zeroed by the caller); the loss
 // into *loss.
@@ -412,6 +472,36 @@ iso_status iso_mlp_forward(const float* params, const float* stats, const float*
     iso::k_mlp_forward<<<iso::mlp_blocks(n, iso::device_sms()), 256, smem, static_cast<cudaStream_t>(stream)>>>(
         params, stats, isovals, n, y);
     return launch_status(cudaGetLastError());
+}
+
+iso_status iso_mlp_predict(const float* params, int64_t n_sets, const iso_block_set* sets, float* totals,
+                           void* stream)
+{
+    if (n_sets < 0 || (n_sets > 0 && (!params || !sets || !totals))) return ISO_ERR_INVALID_ARG;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (n_sets == 0) return ISO_OK;
+    if (cudaMemsetAsync(totals, 0, sizeof(float) * (size_t)n_sets, s) != cudaSuccess) return ISO_ERR_CUDA;
+    const size_t smem = iso::mlp_smem();
+    cudaFuncSetAttribute(iso::k_mlp_predict, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const int nsm = iso::device_sms();
+    for (int64_t s0 = 0; s0 < n_sets; s0 += iso::kMaxSets) {  // kMaxSets sets per launch
+        iso::PredictSets ps{};
+        ps.n = (int)std::min<int64_t>(iso::kMaxSets, n_sets - s0);
+        long long at = 0;
+        for (int q = 0; q < ps.n; ++q) {
+            const iso_block_set& b = sets[s0 + q];
+            if (b.n_blocks < 0 || (b.n_blocks > 0 && !b.stats)) return ISO_ERR_INVALID_ARG;
+            ps.start[q] = at;
+            ps.stats[q] = b.stats;
+            ps.iso[q] = b.isoval;
+            at += b.n_blocks;
+        }
+        ps.start[ps.n] = at;
+        if (at == 0) continue;
+        iso::k_mlp_predict<<<iso::mlp_blocks(at, nsm), 256, smem, s>>>(params, ps, totals + s0);
+        if (cudaGetLastError() != cudaSuccess) return ISO_ERR_CUDA;
+    }
+    return ISO_OK;
 }
 
 iso_status iso_mlp_gradient(const float* params, const float* stats, const float* isovals, const float* target,

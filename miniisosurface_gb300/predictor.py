@@ -148,22 +148,22 @@ class Predictor:
         self.slack = slack
 
     def predict(self, items, stream=None):
-        """Predicted triangles of each (stats, iso) in one network launch."""
+        """Predicted triangles of each (stats, iso): one iso_mlp_predict launch
+        (per 128 items) on `stream` (a CUDA stream handle; default: the current
+        stream) and one copy of the totals back."""
         import torch
-        rows, isos, seg = [], [], []
-        for q, (st, iso) in enumerate(items):
-            act = (st[:, 0] < iso) & (st[:, 1] >= iso)
-            a = st[act]
-            rows.append(a)
-            isos.append(torch.full((a.shape[0],), float(iso), dtype=torch.float32, device=st.device))
-            seg.append(torch.full((a.shape[0],), q, dtype=torch.int64, device=st.device))
         if not items:
             return []
-        x = torch.cat(rows).contiguous()
-        y = mlp_forward(self.params, x, torch.cat(isos).contiguous(), stream)
-        tot = torch.zeros(len(items), dtype=torch.float64, device=x.device)
-        tot.index_add_(0, torch.cat(seg), torch.clamp(y, min=0).double() * LABEL_SCALE)
-        return tot.cpu().tolist()
+        sets = (_lib.IsoBlockSet * len(items))()
+        for q, (st, iso) in enumerate(items):
+            sets[q].stats, sets[q].n_blocks, sets[q].isoval = _ptr(st), st.shape[0], float(iso)
+        totals = torch.empty(len(items), dtype=torch.float32, device=self.params.device)
+        strm = torch.cuda.ExternalStream(stream) if stream is not None else \
+            torch.cuda.current_stream(self.params.device)
+        check(load().iso_mlp_predict(_ptr(self.params), len(items), sets, _ptr(totals), C.c_void_p(strm.cuda_stream)))
+        with torch.cuda.stream(strm):
+            host = totals.cpu()  # copied on strm, which it waits for
+        return [float(t) * LABEL_SCALE for t in host.tolist()]
 
     def capacities(self, items, stream=None):
         """(cap_points, cap_tris) of each (stats, iso)."""
@@ -249,7 +249,7 @@ def main(argv=None):
     ap.add_argument("--volumes", type=int, default=500)
     ap.add_argument("--isos", type=int, default=40)
     ap.add_argument("--eval-volumes", type=int, default=50)
-    ap.add_argument("--epochs", type=int, default=6)
+    ap.add_argument("--epochs", type=int, default=30)
     ap.add_argument("--out", default=str(WEIGHTS))
     args = ap.parse_args(argv)
     dev = torch.device("cuda", 0)

@@ -105,10 +105,13 @@ class Server:
         self.predictor = predictor
         self.stats = None
         if predictor is not None:
+            import torch
             from .predictor import block_stats
             self.stats = [block_stats(v, d) for v, d in volumes]
-        for c in self.contexts:
+            torch.cuda.synchronize(device)  # the slots read them from their own streams
+        for c in self.contexts:  # every batch differs: lanes launched directly, no graph capture
             check(load().iso_batch_set_lanes(c.handle, int(lanes)), c.handle)
+            check(load().iso_batch_set_graph(c.handle, 0), c.handle)
 
     def run(self, requests, keep_meshes=False):
         """Serve `requests` = [(arrival seconds, volume index, isovalue, algorithm)] in real time.

@@ -94,8 +94,9 @@ def test_batch_matches_plain_and_oracle(M):
 def test_lanes_and_autotuner_agree(M):
     reqs, _ = mixed_requests(M)
     want = None
-    for lanes in (1, 4, 0):
+    for lanes, graph in ((1, True), (4, True), (0, True), (3, False), (1, False)):
         M.set_batch_lanes(lanes)
+        M.set_batch_graph(graph)
         got = [as_np(m) for m in M.extract_batch([r for r, _ in reqs], [M.DeviceMesh(0, 0, ib) for _, ib in reqs])]
         if lanes == 0:
             assert M.batch_lanes() in (1, 2, 4, 8, 16, 32)
@@ -103,7 +104,8 @@ def test_lanes_and_autotuner_agree(M):
             want = got
         else:
             for i, (a, b) in enumerate(zip(got, want)):
-                same(a, b, "lanes %d request %d" % (lanes, i))
+                same(a, b, "lanes %d graph %s request %d" % (lanes, graph, i))
+    M.set_batch_graph(True)
     M.set_batch_lanes(0)
 
 

@@ -137,3 +137,22 @@ def test_served_with_predictor_equals_alone(M, trained):
             assert bool((r.mesh.points[: r.n_points] == alone.points[: alone.n_points]).all())
             assert bool((r.mesh.normals[: r.n_points] == alone.normals[: alone.n_points]).all())
             assert bool((r.mesh.tris[: r.n_tris] == alone.tris[: alone.n_tris]).all())
+
+
+def test_fused_prediction_matches_per_block_forward(M, trained):
+    """iso_mlp_predict over several (statistics, isovalue) sets in one launch equals the
+    per-block network summed over each set's active blocks."""
+    import torch
+    P, pred, _ = trained
+    items = []
+    for i, (dims, kind, _) in enumerate(CASES[:4]):
+        st = P.block_stats(dev(volume(M, dims, kind, 40 + i)), dims)
+        for iso in (0.0, 0.2, 0.45):
+            items.append((st, iso))
+    got = pred.predict(items)
+    for (st, iso), g in zip(items, got):
+        act = (st[:, 0] < iso) & (st[:, 1] >= iso)
+        y = P.mlp_forward(pred.params, st[act].contiguous(),
+                          torch.full((int(act.sum()),), iso, dtype=torch.float32, device=st.device))
+        want = float(torch.clamp(y, min=0).sum()) * P.LABEL_SCALE
+        assert abs(g - want) <= 1e-4 * max(want, 1.0), (g, want)
