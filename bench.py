@@ -31,7 +31,7 @@ One step = one full extraction (passes 1-4) of the volume.
             plain = one iso_extract_device call per request (the drop-in
             call, which synchronises); plain_async = the same calls queued on
             one stream without synchronising; batched = iso_extract_batch
-            (lanes picked by its autotuner, graph replayed).  Outputs are
+            (lanes and work split picked by its autotuner, graph replayed).  Outputs are
             compared request by request (identical).
   served    a pool of 8 resident volumes with side lengths log-uniform in
             [64, 768] per axis (blobs / noise); requests (volume, isovalue in
@@ -310,7 +310,7 @@ def batched_leg(M, lib, dev, reps):
 
     M.set_batch_lanes(0, ctx)
     batched()  # the autotuner's first batch
-    lanes = M.batch_lanes(ctx)
+    lanes, split = M.batch_lanes(ctx), M.batch_split(ctx)
     t_batch = seconds(batched)
     t_plain = seconds(plain)
     t_async = seconds(plain_async)
@@ -328,7 +328,8 @@ def batched_leg(M, lib, dev, reps):
         "vertices": int(sum(s[0] for s in sizes)), "triangles": int(sum(s[1] for s in sizes)),
         "plain": {"ms": 1e3 * t_plain, "value": mc(t_plain), "unit": METRIC},
         "plain_async": {"ms": 1e3 * t_async, "value": mc(t_async), "unit": METRIC},
-        "batched": {"ms": 1e3 * t_batch, "value": mc(t_batch), "unit": METRIC, "lanes": lanes},
+        "batched": {"ms": 1e3 * t_batch, "value": mc(t_batch), "unit": METRIC, "lanes": lanes,
+                    "split": split},
         "speedup_vs_plain": t_plain / t_batch, "speedup_vs_plain_async": t_async / t_batch,
         "identical_output": same,
     }

@@ -251,11 +251,16 @@ iso_status iso_mlp_predict(const float* params, int64_t n_sets, const iso_block_
                            void* stream);
 
 /* Lanes of iso_extract_batch / iso_count_batch: a fixed count (1..64), or 0
- * (the default): the autotuner times the context's next batch at 1, 2, 4, 8, 16 and 32 lanes
- * (each run writes the same meshes) and keeps the fastest count for that batch and
- * the ones after it.  iso_batch_lanes returns the count in use (0 before the
- * autotuner has run). */
+ * (the default).  Work split: a request's count and generate passes size
+ * their grids and work items for nsm / share SMs (1..64; the lanes share the
+ * GPU), or 0 (the default).  Whatever is 0 the autotuner picks: it times the
+ * context's next batch at 1, 2, 4, ..., 64 lanes and shares 1, 2, 4, 8 (at
+ * most the lanes; each run writes the same meshes) and keeps the fastest for
+ * that batch and the ones after it.  iso_batch_lanes / iso_batch_split
+ * return the values in use (0 before the autotuner has run). */
 iso_status iso_batch_set_lanes(iso_ctx* ctx, int lanes);
+iso_status iso_batch_set_split(iso_ctx* ctx, int share);
+int iso_batch_split(const iso_ctx* ctx);
 /* Whether the context's batches are captured as CUDA graphs (1, the default:
  * a repeated batch only relaunches its graph) or their lanes are launched
  * directly each call (0: no capture, for batches that change every call, as

@@ -436,6 +436,17 @@ def batch_lanes(ctx=None):
     return int(load().iso_batch_lanes(ctx.handle))
 
 
+def set_batch_split(share, ctx=None):
+    """Work split of the batched path: plans sized for nsm / share SMs (0: the autotuner picks it)."""
+    ctx = ctx or default_context()
+    check(load().iso_batch_set_split(ctx.handle, int(share)), ctx.handle)
+
+
+def batch_split(ctx=None):
+    ctx = ctx or default_context()
+    return int(load().iso_batch_split(ctx.handle))
+
+
 def count_device(volume, dims, isoval, algorithm=FLYING_EDGES, ctx=None, stream=None):
     """Passes 1-3 only: exact (n_points, n_tris) of a device-resident volume."""
     import torch

@@ -53,6 +53,8 @@ struct iso_ctx {
     int batch_lanes = 0;        // set by iso_batch_set_lanes; 0: the autotuner's choice
     int batch_tuned = 0;        // lanes the autotuner picked (0: not yet tuned)
     int batch_graph = 1;        // capture batches as CUDA graphs (0: launch the lanes directly)
+    int batch_share = 0;        // set by iso_batch_set_split: a request's plans assume nsm / share SMs; 0: tuned
+    int batch_tuned_share = 0;  // the autotuner's share (0: not yet tuned)
     cudaStream_t s_capture = nullptr;
     std::vector<cudaStream_t> lane_streams;
     std::vector<cudaEvent_t> lane_join;
@@ -308,11 +310,12 @@ struct Plans {
     iso::GenPlan gp;
 };
 
-Plans make_plans(const iso_ctx* ctx, const Grid& g)
+Plans make_plans(const iso_ctx* ctx, const Grid& g, int nsm = 0)
 {
     Plans p;
-    p.cp = iso::count_plan(g, ctx->nsm);
-    p.gp = iso::gen_plan(g, ctx->nsm);
+    const int n = nsm > 0 ? nsm : ctx->nsm;
+    p.cp = iso::count_plan(g, n);
+    p.gp = iso::gen_plan(g, n);
     return p;
 }
 
@@ -867,7 +870,16 @@ struct BatchItem {
 };
 
 constexpr int kMaxLanes = 64;
-constexpr int kTuneLanes[] = {1, 2, 4, 8, 16, 32};
+constexpr int kTuneLanes[] = {1, 2, 4, 8, 16, 32, 64};
+// work splits: a request's count and generate plans size their grids and work
+// items for nsm / share SMs (several lanes share the GPU)
+constexpr int kTuneShares[] = {1, 2, 4, 8};
+
+void replan(iso_ctx* ctx, std::vector<BatchItem>& items, const std::vector<int>& run, int share)
+{
+    const int nsm = std::max(1, ctx->nsm / std::max(1, share));
+    for (int r : run) items[r].pl = make_plans(ctx, items[r].g, nsm);
+}
 
 // Lane of every request with work and the arena layout: counters of all n
 // requests, then per lane its scratch and FE -> MC map.
@@ -950,8 +962,8 @@ iso_status ensure_batch(iso_ctx* ctx, const BatchLayout& lay, int64_t n, cudaStr
 }
 
 // What a captured graph depends on: lanes, buffers, requests and meshes.
-std::vector<unsigned char> batch_key(const iso_ctx* ctx, int lanes, const iso_request* req, const iso_mesh* out,
-                                     int64_t n)
+std::vector<unsigned char> batch_key(const iso_ctx* ctx, int lanes, int share, const iso_request* req,
+                                     const iso_mesh* out, int64_t n)
 {
     std::vector<unsigned char> k;
     auto put = [&](const void* p, size_t len) {
@@ -961,6 +973,7 @@ std::vector<unsigned char> batch_key(const iso_ctx* ctx, int lanes, const iso_re
     const unsigned char count_only = out ? 0 : 1;
     put(&count_only, 1);
     put(&lanes, sizeof lanes);
+    put(&share, sizeof share);
     put(&ctx->reverse, sizeof ctx->reverse);
     put(&ctx->batch_arena, sizeof ctx->batch_arena);
     put(&ctx->h_batch, sizeof ctx->h_batch);
@@ -1051,13 +1064,15 @@ iso_status capture_batch(iso_ctx* ctx, const iso_request* req, const iso_mesh* o
 
 // Prepare (lanes, buffers, graph) for `lanes` lanes; nothing runs.
 iso_status prepare_batch(iso_ctx* ctx, const iso_request* req, const iso_mesh* out, int64_t n,
-                         std::vector<BatchItem>& items, const std::vector<int>& run, int lanes, cudaStream_t s)
+                         std::vector<BatchItem>& items, const std::vector<int>& run, int lanes, int share,
+                         cudaStream_t s)
 {
+    replan(ctx, items, run, share);
     const BatchLayout lay = plan_batch(req, out, n, items, run, lanes);
     std::lock_guard<std::mutex> lock(g_batch_mutex);
     iso_status st = ensure_batch(ctx, lay, n, s);
     if (st != ISO_OK) return st;
-    std::vector<unsigned char> key = batch_key(ctx, lanes, req, out, n);
+    std::vector<unsigned char> key = batch_key(ctx, lanes, share, req, out, n);
     const int slot = out ? 0 : 1;
     if (ctx->batch_exec[slot] && key == ctx->batch_key[slot]) return ISO_OK;
     st = capture_batch(ctx, req, out, n, items, run, lay);
@@ -1390,7 +1405,9 @@ iso_status run_batch(iso_ctx* ctx, int64_t n, const iso_request* req, iso_mesh* 
     iso_status rc = ISO_OK;
     if (!run.empty() && !ctx->batch_graph) {  // the lanes launched directly, no graph
         int lanes = ctx->batch_lanes > 0 ? ctx->batch_lanes : (ctx->batch_tuned > 0 ? ctx->batch_tuned : 8);
+        const int share = ctx->batch_share > 0 ? ctx->batch_share : std::max(1, ctx->batch_tuned_share);
         lanes = std::min(lanes, std::max(1, (int)run.size()));
+        replan(ctx, items, run, share);
         const BatchLayout lay = plan_batch(req, out, n, items, run, lanes);
         {
             std::lock_guard<std::mutex> lock(g_batch_mutex);
@@ -1402,24 +1419,35 @@ iso_status run_batch(iso_ctx* ctx, int64_t n, const iso_request* req, iso_mesh* 
         ISO_CUDA(ctx, cudaStreamSynchronize(s));
     } else if (!run.empty()) {
         int lanes = ctx->batch_lanes > 0 ? ctx->batch_lanes : ctx->batch_tuned;
-        if (lanes <= 0) {  // autotuner: time the batch at each lane count, keep the fastest
+        int share = ctx->batch_share > 0 ? ctx->batch_share : ctx->batch_tuned_share;
+        if (lanes <= 0 || share <= 0) {  // autotuner: time the batch at each (lanes, split), keep the fastest
             float best = 1e30f;
+            int best_l = 1, best_s = 1;
             for (int L : kTuneLanes) {
+                if (lanes > 0 && L != lanes) continue;
                 if (L > 1 && L > (int)run.size()) break;
-                rc = prepare_batch(ctx, req, out, n, items, run, L, s);
-                if (rc != ISO_OK) return rc;
-                float ms;
-                rc = time_batch(ctx, ctx->batch_exec[out ? 0 : 1], s, ms);
-                if (rc != ISO_OK) return rc;
-                if (ms < best) {
-                    best = ms;
-                    lanes = L;
+                for (int S : kTuneShares) {
+                    if (share > 0 && S != share) continue;
+                    if (S > L) break;  // a request never has fewer SMs than nsm / lanes
+                    rc = prepare_batch(ctx, req, out, n, items, run, L, S, s);
+                    if (rc != ISO_OK) return rc;
+                    float ms;
+                    rc = time_batch(ctx, ctx->batch_exec[out ? 0 : 1], s, ms);
+                    if (rc != ISO_OK) return rc;
+                    if (ms < best) {
+                        best = ms;
+                        best_l = L;
+                        best_s = S;
+                    }
                 }
             }
-            ctx->batch_tuned = lanes;
+            lanes = best_l;
+            share = best_s;
+            if (ctx->batch_lanes <= 0) ctx->batch_tuned = lanes;
+            if (ctx->batch_share <= 0) ctx->batch_tuned_share = share;
         }
         lanes = std::min(lanes, std::max(1, (int)run.size()));
-        rc = prepare_batch(ctx, req, out, n, items, run, lanes, s);
+        rc = prepare_batch(ctx, req, out, n, items, run, lanes, share, s);
         if (rc != ISO_OK) return rc;
         ISO_CUDA(ctx, cudaGraphLaunch(ctx->batch_exec[out ? 0 : 1], s));
         ISO_CUDA(ctx, cudaStreamSynchronize(s));
@@ -1485,8 +1513,25 @@ iso_status iso_batch_set_lanes(iso_ctx* ctx, int lanes)
 {
     if (!ctx || lanes < 0 || lanes > kMaxLanes) return ISO_ERR_INVALID_ARG;
     ctx->batch_lanes = lanes;
-    if (lanes == 0) ctx->batch_tuned = 0;  // tune again on the next batch
+    if (lanes == 0) {  // tune again on the next batch, the split too
+        ctx->batch_tuned = 0;
+        ctx->batch_tuned_share = 0;
+    }
     return ISO_OK;
+}
+
+iso_status iso_batch_set_split(iso_ctx* ctx, int share)
+{
+    if (!ctx || share < 0 || share > 64) return ISO_ERR_INVALID_ARG;
+    ctx->batch_share = share;
+    if (share == 0) ctx->batch_tuned_share = 0;  // tune again on the next batch
+    return ISO_OK;
+}
+
+int iso_batch_split(const iso_ctx* ctx)
+{
+    if (!ctx) return 0;
+    return ctx->batch_share > 0 ? ctx->batch_share : ctx->batch_tuned_share;
 }
 
 iso_status iso_batch_set_graph(iso_ctx* ctx, int enable)

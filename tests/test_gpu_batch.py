@@ -94,19 +94,23 @@ def test_batch_matches_plain_and_oracle(M):
 def test_lanes_and_autotuner_agree(M):
     reqs, _ = mixed_requests(M)
     want = None
-    for lanes, graph in ((1, True), (4, True), (0, True), (3, False), (1, False)):
+    for lanes, graph, share in ((1, True, 1), (4, True, 4), (0, True, 0), (3, False, 2), (1, False, 1),
+                                (5, True, 8)):
         M.set_batch_lanes(lanes)
+        M.set_batch_split(share)
         M.set_batch_graph(graph)
         got = [as_np(m) for m in M.extract_batch([r for r, _ in reqs], [M.DeviceMesh(0, 0, ib) for _, ib in reqs])]
         if lanes == 0:
-            assert M.batch_lanes() in (1, 2, 4, 8, 16, 32)
+            assert M.batch_lanes() in (1, 2, 4, 8, 16, 32, 64)
+            assert M.batch_split() in (1, 2, 4, 8) and M.batch_split() <= M.batch_lanes()
         if want is None:
             want = got
         else:
             for i, (a, b) in enumerate(zip(got, want)):
-                same(a, b, "lanes %d graph %s request %d" % (lanes, graph, i))
+                same(a, b, "lanes %d graph %s split %d request %d" % (lanes, graph, share, i))
     M.set_batch_graph(True)
     M.set_batch_lanes(0)
+    M.set_batch_split(0)
 
 
 def test_capacity_per_request(M):
