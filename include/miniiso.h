@@ -164,6 +164,17 @@ iso_status iso_extract_device(iso_ctx* ctx, iso_algorithm algo, const float* vol
 iso_status iso_extract_device_async(iso_ctx* ctx, iso_algorithm algo, const float* volume, const iso_grid* grid,
                                     float isoval, iso_mesh* out, int64_t* result_host, void* stream);
 
+/* Graph mode of iso_extract_device / iso_extract_device_async (no
+ * counterpart in the reference; off by default): the first call captures its
+ * kernels and the copy of the counts to result_host as a CUDA graph, and
+ * later calls with the same arguments (volume, grid, isovalue, mesh,
+ * result_host) relaunch it -- no per-kernel launch overhead between the
+ * passes; a call with other arguments captures again (updating the graph in
+ * place where possible).  result_host must be pinned for the graph path;
+ * while per-pass profiling (iso_ctx_profile) is on, calls take the stream
+ * path.  The same capture rules as iso_extract_batch apply. */
+iso_status iso_ctx_set_graph(iso_ctx* ctx, int enable);
+
 /* Batched extraction (no counterpart in the reference, which extracts one
  * volume per call).  n requests -- each a volume in device memory with its
  * own grid, isovalue and algorithm (an iso_algorithm value) -- into n

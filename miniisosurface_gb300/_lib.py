@@ -83,6 +83,7 @@ SIGNATURES = {
                                   C.POINTER(C.c_int64), C.POINTER(C.c_int), C.c_void_p]),
     "iso_batch_set_lanes": (C.c_int, [C.c_void_p, C.c_int]),
     "iso_batch_set_graph": (C.c_int, [C.c_void_p, C.c_int]),
+    "iso_ctx_set_graph": (C.c_int, [C.c_void_p, C.c_int]),
     "iso_batch_set_split": (C.c_int, [C.c_void_p, C.c_int]),
     "iso_batch_split": (C.c_int, [C.c_void_p]),
     "iso_block_count": (C.c_int64, [C.POINTER(IsoGrid)]),

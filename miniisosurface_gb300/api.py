@@ -425,6 +425,13 @@ def set_batch_lanes(lanes, ctx=None):
     check(load().iso_batch_set_lanes(ctx.handle, int(lanes)), ctx.handle)
 
 
+def set_graph(enable, ctx=None):
+    """Graph mode of the one-shot device extraction (iso_ctx_set_graph): repeated calls relaunch a
+    captured CUDA graph."""
+    ctx = ctx or default_context()
+    check(load().iso_ctx_set_graph(ctx.handle, 1 if enable else 0), ctx.handle)
+
+
 def set_batch_graph(enable, ctx=None):
     """Capture batches as CUDA graphs (default) or launch their lanes directly."""
     ctx = ctx or default_context()

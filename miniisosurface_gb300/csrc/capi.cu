@@ -53,6 +53,10 @@ struct iso_ctx {
     int batch_lanes = 0;        // set by iso_batch_set_lanes; 0: the autotuner's choice
     int batch_tuned = 0;        // lanes the autotuner picked (0: not yet tuned)
     int batch_graph = 1;        // capture batches as CUDA graphs (0: launch the lanes directly)
+    // iso_extract_device_async as a replayed CUDA graph (iso_ctx_set_graph)
+    int one_graph = 0;
+    cudaGraphExec_t one_exec = nullptr;
+    std::vector<unsigned char> one_key;
     int batch_share = 0;        // set by iso_batch_set_split: a request's plans assume nsm / share SMs; 0: tuned
     int batch_tuned_share = 0;  // the autotuner's share (0: not yet tuned)
     cudaStream_t s_capture = nullptr;
@@ -1096,6 +1100,85 @@ iso_status time_batch(iso_ctx* ctx, cudaGraphExec_t exec, cudaStream_t s, float&
     return ISO_OK;
 }
 
+// iso_extract_device_async as a CUDA graph: the passes and the counters'
+// copy to result_host captured once, relaunched while the call's arguments,
+// the context's buffers and result_host stay the same (result_host must be
+// pinned: a pageable one takes the stream path).
+iso_status extract_graph(iso_ctx* ctx, iso_algorithm algo, const float* volume, const Grid& g, const iso_grid* grid,
+                         float isoval, const Plans& pl, FeBuffers& b, const iso_mesh* out, int64_t* result_host,
+                         cudaStream_t s)
+{
+    cudaPointerAttributes attr{};
+    if (cudaPointerGetAttributes(&attr, result_host) != cudaSuccess || attr.type != cudaMemoryTypeHost) {
+        cudaGetLastError();
+        PassMarks pm(ctx, s);
+        enqueue_count(ctx, algo, volume, g, isoval, pl, b, s, pm);
+        enqueue_generate(ctx, algo, volume, g, isoval, pl, b, out, s, pm);
+        ISO_CUDA(ctx, cudaGetLastError());
+        ISO_CUDA(ctx,
+                 cudaMemcpyAsync(result_host, b.totals, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+        return ISO_OK;
+    }
+    std::vector<unsigned char> key;
+    auto put = [&](const void* p, size_t len) {
+        const unsigned char* c = static_cast<const unsigned char*>(p);
+        key.insert(key.end(), c, c + len);
+    };
+    put(&algo, sizeof algo);
+    put(&volume, sizeof volume);
+    put(grid, sizeof *grid);
+    put(&isoval, sizeof isoval);
+    put(&out->points, sizeof out->points);
+    put(&out->normals, sizeof out->normals);
+    put(&out->tris, sizeof out->tris);
+    put(&out->index_bytes, sizeof out->index_bytes);
+    put(&out->cap_points, sizeof out->cap_points);
+    put(&out->cap_tris, sizeof out->cap_tris);
+    put(&result_host, sizeof result_host);
+    put(&ctx->scratch, sizeof ctx->scratch);
+    put(&ctx->fe2mc, sizeof ctx->fe2mc);
+    put(&ctx->reverse, sizeof ctx->reverse);
+    if (!ctx->one_exec || key != ctx->one_key) {
+        std::lock_guard<std::mutex> lock(g_batch_mutex);
+        if (!ctx->s_capture) ISO_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->s_capture, cudaStreamNonBlocking));
+        cudaStream_t sc = ctx->s_capture;
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(sc, cudaStreamCaptureModeRelaxed);
+        if (e == cudaSuccess) {
+            PassMarks pm(ctx, sc);
+            enqueue_count(ctx, algo, volume, g, isoval, pl, b, sc, pm);
+            enqueue_generate(ctx, algo, volume, g, isoval, pl, b, out, sc, pm);
+            cudaMemcpyAsync(result_host, b.totals, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, sc);
+            e = cudaStreamEndCapture(sc, &graph);
+        }
+        if (e != cudaSuccess || !graph) {
+            cudaGetLastError();
+            if (graph) cudaGraphDestroy(graph);
+            ctx->one_key.clear();
+            ctx->last_error = std::string("capturing the extraction failed: ") + cudaGetErrorString(e);
+            return ISO_ERR_CUDA;
+        }
+        if (ctx->one_exec) {
+            cudaGraphExecUpdateResultInfo info;
+            if (cudaGraphExecUpdate(ctx->one_exec, graph, &info) != cudaSuccess) {
+                cudaGetLastError();
+                cudaGraphExecDestroy(ctx->one_exec);
+                ctx->one_exec = nullptr;
+            }
+        }
+        if (!ctx->one_exec) e = cudaGraphInstantiate(&ctx->one_exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            ctx->one_exec = nullptr;
+            ctx->one_key.clear();
+            return cuda_fail(ctx, e, "cudaGraphInstantiate");
+        }
+        ctx->one_key.swap(key);
+    }
+    ISO_CUDA(ctx, cudaGraphLaunch(ctx->one_exec, s));
+    return ISO_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1249,6 +1332,7 @@ iso_status iso_ctx_destroy(iso_ctx* ctx)
     for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
     for (cudaGraphExec_t x : ctx->batch_exec)
         if (x) cudaGraphExecDestroy(x);
+    if (ctx->one_exec) cudaGraphExecDestroy(ctx->one_exec);
     for (cudaStream_t q : ctx->lane_streams) cudaStreamDestroy(q);
     for (cudaEvent_t e : ctx->lane_join) cudaEventDestroy(e);
     for (cudaEvent_t e : {ctx->batch_fork, ctx->batch_t0, ctx->batch_t1})
@@ -1352,11 +1436,25 @@ iso_status iso_extract_device_async(iso_ctx* ctx, iso_algorithm algo, const floa
         if (st != ISO_OK) return st;
         b.fe2mc = ctx->fe2mc;
     }
+    if (ctx->one_graph && !ctx->profiling) return extract_graph(ctx, algo, volume, g, grid, isoval, pl, b, out,
+                                                                result_host, s);
     PassMarks pm(ctx, s);
     enqueue_count(ctx, algo, volume, g, isoval, pl, b, s, pm);
     enqueue_generate(ctx, algo, volume, g, isoval, pl, b, out, s, pm);
     ISO_CUDA(ctx, cudaGetLastError());
     ISO_CUDA(ctx, cudaMemcpyAsync(result_host, b.totals, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    return ISO_OK;
+}
+
+iso_status iso_ctx_set_graph(iso_ctx* ctx, int enable)
+{
+    if (!ctx) return ISO_ERR_INVALID_ARG;
+    ctx->one_graph = enable ? 1 : 0;
+    if (!enable && ctx->one_exec) {
+        cudaGraphExecDestroy(ctx->one_exec);
+        ctx->one_exec = nullptr;
+        ctx->one_key.clear();
+    }
     return ISO_OK;
 }
 

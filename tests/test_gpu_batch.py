@@ -151,3 +151,26 @@ def test_replay_and_update(M):
     for i in range(1, len(rs)):
         same(as_np(meshes2[i]), first[i], "updated batch request %d" % i)
     M.set_batch_lanes(0)
+
+
+def test_one_shot_graph_mode(M):
+    """iso_ctx_set_graph: repeated device extractions relaunch a captured graph; a changed isovalue, mesh or
+    algorithm captures again; every mesh equals the stream path's."""
+    import torch
+    reqs, _ = mixed_requests(M)
+    ctx = M.Context(0)
+    picks = [reqs[i] for i in (0, 1, 3, 9, 11)]
+    want = [plain(M, r, ib) for r, ib in picks]
+    M.set_graph(True, ctx)
+    try:
+        for rep in range(3):
+            for (r, ib), w in zip(picks, want):
+                m = M.DeviceMesh(len(w[0]), len(w[2]), ib)
+                for _ in range(2):  # the second call relaunches the graph of the first
+                    m.points.fill_(3.0)
+                    got = M.extract_device(r.volume, r.dims, r.isoval, r.algorithm, r.spacing, r.origin, out=m,
+                                           index_bytes=ib, ctx=ctx)
+                    torch.cuda.synchronize()
+                    same(as_np(got), w, "graph mode %s rep %d" % (r.dims, rep))
+    finally:
+        M.set_graph(False, ctx)
