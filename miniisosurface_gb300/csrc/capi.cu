@@ -374,6 +374,23 @@ void enqueue_generate(iso_ctx* ctx, iso_algorithm algo, const float* vol, const 
             pm.mark(ISO_PASS_VERTICES);
     } else {
         const long long capM = capV < 0xffffffffll ? capV : 0xffffffffll;  // fe2mc holds 32-bit ids
+        if (pl.gp.fits && iso::mc_fused(g, pl.gp)) {  // owned vertices + FE-id triangles, vertices, remap
+            if (i4)
+                iso::launch_mc_gen_tris<uint32_t>(g, ctx->d_cases, b, pl.cp, pl.gp, capM, capT, out->points,
+                                                  static_cast<uint32_t*>(out->tris), ctx->reverse, s);
+            else
+                iso::launch_mc_gen_tris<uint64_t>(g, ctx->d_cases, b, pl.cp, pl.gp, capM, capT, out->points,
+                                                  static_cast<uint64_t*>(out->tris), ctx->reverse, s);
+            pm.mark(ISO_PASS_MC_VERTICES);
+            if (iso::launch_mc_vertices(vol, g, iso, b, pl.gp, capM, capT, out->points, out->normals, s))
+                pm.mark(ISO_PASS_VERTICES);
+            if (i4)
+                iso::launch_mc_remap<uint32_t>(b, pl.gp, capM, capT, static_cast<uint32_t*>(out->tris), s);
+            else
+                iso::launch_mc_remap<uint64_t>(b, pl.gp, capM, capT, static_cast<uint64_t*>(out->tris), s);
+            pm.mark(ISO_PASS_MC_TRIANGLES);
+            return;
+        }
         if (pl.gp.fits)
             iso::launch_mc_gen_warps(vol, g, iso, ctx->d_cases, b, pl.cp, pl.gp, capM, capT, out->points, out->normals,
                                      ctx->reverse, s);

@@ -62,8 +62,9 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
     // per case: each triangle corner as the nibble (edge-id table row | point offset << 3) of fe_edge_rel,
     // the triangle count in bits 60..63 (the packed triangle list with edges replaced)
     __shared__ uint64_t s_tri[MODE == kGenMC ? 1 : 256];
-    __shared__ uint64_t s_order[MODE == kGenMC ? 256 : 1];  // kGenMC: first-appearance order, cut edges
-    __shared__ uint16_t s_cut[MODE == kGenMC ? 256 : 1];
+    constexpr bool OWNS = MODE == kGenMC || MODE == kGenMCT;  // numbers the MC vertices its cells own
+    __shared__ uint64_t s_order[OWNS ? 256 : 1];  // first-appearance order, cut edges
+    __shared__ uint16_t s_cut[OWNS ? 256 : 1];
     constexpr int LPR = 32 / RPW;  // lanes per row
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, h = lane / LPR, lw = lane % LPR;
     const int W = g.W;
@@ -73,10 +74,10 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
     uint32_t* cell = rwt + RPW * 8 * W;
     unsigned char* list = reinterpret_cast<unsigned char*>(cell + kGenCells);
     for (int c = tid; c < 256; c += kThreads) {
-        if (MODE == kGenMC) {
+        if (OWNS) {
             s_order[c] = cases->order[c];
             s_cut[c] = cases->cut[c];
-            continue;
+            if (MODE == kGenMC) continue;
         }
         const uint64_t w = cases->tris[c];
         uint64_t x = w & (0xfull << 60);
@@ -131,7 +132,8 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
             s1 = s2 = 0ull;
             if (row_ok && lw < 4 && (dj == 0 || hasY) && (dk == 0 || hasZp))
                 s1 = rs.get(rA + (long long)dk * g.ny + dj, 0);
-            if (row_ok && lw == 0) s2 = rs.get(rA, MODE == kGenMC ? 2 : 1);
+            if (row_ok && lw == 0) s2 = rs.get(rA, OWNS ? 2 : 1);
+            if (MODE == kGenMCT && row_ok && lw == 2) s2 = rs.get(rA, 1);  // first triangle of cell row A
             if (row_ok && lw == 1 && hasY) {
                 const uint2 c = __ldg(reinterpret_cast<const uint2*>(&rowcnt[rA + 1]));
                 s2 = (unsigned long long)c.x + c.y;
@@ -190,6 +192,8 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
             const uint32_t cntB = (uint32_t)__shfl_sync(0xffffffffu, st2, 1, LPR);
             // first triangle (kGenMC: first owned MC vertex) of cell row jw
             const unsigned long long ts0 = __shfl_sync(0xffffffffu, st2, 0);
+            // kGenMCT: first triangle of cell row jw (ts0 numbers the owned MC vertices)
+            const unsigned long long tt0 = MODE == kGenMCT ? __shfl_sync(0xffffffffu, st2, 2) : 0ull;
             const uint32_t nxA = t0 & 0xffffu, nyA = t2 & 0xffffu, nxC = t1 & 0xffffu;
             const uint32_t off = (uint32_t)(xsA - xs0);  // the vertices of rows jw .. j-1
             if (in) {  // first ids of the word's cut edges, relative to xs0
@@ -231,6 +235,7 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
             const uint32_t ia = warp_incl_scan(na, lane);  // the cells of row jw come first
             const uint32_t tot = __shfl_sync(0xffffffffu, ia, 31);
             unsigned long long tcur = ts0;
+            unsigned long long ttri = tt0;
             for (uint32_t c0 = 0; c0 < tot; c0 += kGenCells) {
                 // lane L takes active cell c0 + L: the first lane whose inclusive count passes it
                 // (a shuffle binary search over the lanes), then the bit by __fns
@@ -262,7 +267,10 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
                     cell[lane] = rec;
                 }
                 const int cs = (int)(rec >> 16);
-                if (MODE != kGenMC) {
+                // triangles: kGenFE / kGenMCT with the corners' FE ids, kGenTri mapped to MC ids; kGenMCT
+                // only for the cell rows it emits (the rows below kemit belong to the slab below)
+                if (MODE == kGenFE || MODE == kGenTri || (MODE == kGenMCT && k >= kemit)) {
+                    unsigned long long& tc = MODE == kGenMCT ? ttri : tcur;
                     const uint32_t nt = live ? (uint32_t)iso_case_ntris(s_tri[cs]) : 0u;
                     const uint32_t it = warp_incl_scan(nt, lane);
                     const uint32_t ntb = __shfl_sync(0xffffffffu, it, 31);
@@ -278,7 +286,7 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
                             const uint2* mbc = mb + ((cr >> 9) & 7u) * 8 * W + (ci >> 5);
                             const uint32_t corners = (uint32_t)(s_tri[cr >> 16] >> (12 * q)) & 0xfffu;
                             const int bit = ci & 31;
-                            IndexT* o = tris + 3 * (tcur + t - tbase);
+                            IndexT* o = tris + 3 * (tc + t - tbase);
 #pragma unroll
                             for (int c = 0; c < 3; ++c) {  // fe_edge_rel with its table row and offset precomputed
                                 const uint32_t nib = (corners >> (4 * c)) & 15u;
@@ -295,9 +303,10 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
                             }
                         }
                     }
-                    tcur += ntb;
+                    tc += ntb;
                 }
-                if (MODE == kGenMC) {
+                if (OWNS) {
+                    if (MODE == kGenMCT) __syncwarp();  // the triangle list is read before the vertex list reuses it
                     // ---- the MC vertices the batch's cells own: cell order, then order of first appearance in
                     // the cell's triangle list (marchingCubes/serial/main.cpp:139-177)
                     const int cci = (int)(rec & 511u), cj = jw + (int)((rec >> 9) & 7u);

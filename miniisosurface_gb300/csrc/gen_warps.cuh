@@ -47,7 +47,7 @@ constexpr int kGenCells = 32;  // cells per batch
 constexpr int kGenTris = 5 * kGenCells;    // triangles of a batch, at most
 constexpr int kGenOwned = 12 * kGenCells;  // MC vertices owned by a batch, at most
 constexpr int kGenVq = 64;                 // FE vertex queue per axis and warp (a ring of two batches)
-enum GenMode { kGenFE = 0, kGenMC = 1, kGenTri = 2, kGenDup = 3 };
+enum GenMode { kGenFE = 0, kGenMC = 1, kGenTri = 2, kGenDup = 3, kGenMCT = 4 };
 
 // Per-warp scratch in shared memory:
 //   mb[8][W]   {cut mask, id of its first cut edge - the row's first vertex}
@@ -59,7 +59,7 @@ enum GenMode { kGenFE = 0, kGenMC = 1, kGenTri = 2, kGenDup = 3 };
 //   FE: vertex queues per axis (rings of kGenVq): ids (u64), then i | k << 10
 __host__ __device__ inline size_t gen_list_bytes(int mode)
 {
-    return mode == kGenMC || mode == kGenDup ? (size_t)kGenOwned * 2 : (size_t)kGenTris;
+    return mode == kGenMC || mode == kGenDup || mode == kGenMCT ? (size_t)kGenOwned * 2 : (size_t)kGenTris;
 }
 //   Dup: db[8][W] the global-edge-index order id of each mask's first cut
 //        edge, after the list

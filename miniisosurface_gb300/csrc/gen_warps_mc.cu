@@ -36,6 +36,85 @@ bool launch_dup_vertices(const float* vol, const Grid& g, float iso, const FeBuf
     return true;
 }
 
+// Marching Cubes over rows of up to 16 words in two passes instead of
+// three: the owned vertices (records, FE -> MC map) and the triangles with
+// the corners' Flying Edges ids in one generate pass, then k_mc_remap
+// replaces every index by its MC id once the map is complete.
+bool mc_fused(const Grid& g, const GenPlan& p) { return g.W <= 16 && p.nsm > 0 && p.kemit == g.kr; }
+
+template <typename IndexT>
+void launch_mc_gen_tris(const Grid& g, const CaseTables* cases, const FeBuffers& b, const CountPlan& cp,
+                        const GenPlan& p, long long capV, long long capT, float* points, IndexT* tris, int reverse,
+                        cudaStream_t s)
+{
+    launch_gen_pairs_impl<IndexT, kGenMCT>(g, cases, b, cp, p, p.nsm, capV, capT, points, tris, reverse, s);
+}
+
+// tris[i] = fe2mc[tris[i]] for the 3 T indices (T from the totals); nothing
+// when the mesh did not fit.  VEC (tris 16-byte aligned): four indices per
+// thread and step, one 16-byte load and store around four independent
+// gathers; the last n % 4 one by one.
+template <typename IndexT, bool VEC>
+__global__ void k_mc_remap(IndexT* __restrict__ tris, const uint32_t* __restrict__ fe2mc,
+                           const unsigned long long* __restrict__ totals, long long capV, long long capT)
+{
+    if ((long long)totals[0] > capV || (long long)totals[1] > capT) return;
+    const unsigned long long n = 3ull * totals[1];
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    const unsigned long long t0 = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long done = 0;
+    if (VEC) {
+        const unsigned long long n4 = n / 4;
+        for (unsigned long long q = t0; q < n4; q += stride) {
+            IndexT v[4];
+            if (sizeof(IndexT) == 4) {
+                const uint4 a = reinterpret_cast<const uint4*>(tris)[q];
+                v[0] = (IndexT)a.x, v[1] = (IndexT)a.y, v[2] = (IndexT)a.z, v[3] = (IndexT)a.w;
+            } else {
+                const ulonglong2 a = reinterpret_cast<const ulonglong2*>(tris)[2 * q];
+                const ulonglong2 b = reinterpret_cast<const ulonglong2*>(tris)[2 * q + 1];
+                v[0] = (IndexT)a.x, v[1] = (IndexT)a.y, v[2] = (IndexT)b.x, v[3] = (IndexT)b.y;
+            }
+            uint32_t m[4];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) m[c] = __ldg(fe2mc + (unsigned long long)v[c]);
+            if (sizeof(IndexT) == 4) {
+                reinterpret_cast<uint4*>(tris)[q] = make_uint4(m[0], m[1], m[2], m[3]);
+            } else {
+                reinterpret_cast<ulonglong2*>(tris)[2 * q] = make_ulonglong2(m[0], m[1]);
+                reinterpret_cast<ulonglong2*>(tris)[2 * q + 1] = make_ulonglong2(m[2], m[3]);
+            }
+        }
+        done = 4 * n4;
+    }
+    for (unsigned long long i = done + t0; i < n; i += stride)
+        tris[i] = (IndexT)__ldg(fe2mc + (unsigned long long)tris[i]);
+}
+
+template <typename IndexT>
+void launch_mc_remap(const FeBuffers& b, const GenPlan& p, long long capV, long long capT, IndexT* tris,
+                     cudaStream_t s)
+{
+    const long long wave = (long long)p.nsm * 8;
+    const long long need = (3 * capT / 4 + kThreads - 1) / kThreads;
+    const unsigned blocks = (unsigned)std::max(1ll, std::min(wave, need));
+    if ((reinterpret_cast<uintptr_t>(tris) & 15) == 0)
+        k_mc_remap<IndexT, true><<<blocks, kThreads, 0, s>>>(tris, b.fe2mc, b.totals, capV, capT);
+    else
+        k_mc_remap<IndexT, false><<<blocks, kThreads, 0, s>>>(tris, b.fe2mc, b.totals, capV, capT);
+}
+
+template void launch_mc_gen_tris<uint32_t>(const Grid&, const CaseTables*, const FeBuffers&, const CountPlan&,
+                                           const GenPlan&, long long, long long, float*, uint32_t*, int,
+                                           cudaStream_t);
+template void launch_mc_gen_tris<uint64_t>(const Grid&, const CaseTables*, const FeBuffers&, const CountPlan&,
+                                           const GenPlan&, long long, long long, float*, uint64_t*, int,
+                                           cudaStream_t);
+template void launch_mc_remap<uint32_t>(const FeBuffers&, const GenPlan&, long long, long long, uint32_t*,
+                                        cudaStream_t);
+template void launch_mc_remap<uint64_t>(const FeBuffers&, const GenPlan&, long long, long long, uint64_t*,
+                                        cudaStream_t);
+
 template <typename IndexT>
 void launch_mc_tri_warps(const Grid& g, const CaseTables* cases, const FeBuffers& b, const CountPlan& cp,
                          const GenPlan& p, long long capV, long long capT, IndexT* tris, cudaStream_t s)

@@ -73,6 +73,17 @@ void launch_scan(const Grid& g, const CountPlan& p, int mode, FeBuffers& b, cuda
 // totals and the starts of rows rlo / rhi into out[0..8] (device-visible host memory)
 void launch_slab_readback(const FeBuffers& b, const Grid& g, long long rlo, long long rhi, bool has_lo, bool has_hi,
                           unsigned long long* out, cudaStream_t s);
+// Marching Cubes in two passes (rows of up to 16 words, whole windows): owned
+// vertices and FE-id triangles together, then the triangles' ids remapped
+bool mc_fused(const Grid& g, const GenPlan& p);
+template <typename IndexT>
+void launch_mc_gen_tris(const Grid& g, const CaseTables* cases, const FeBuffers& b, const CountPlan& cp,
+                        const GenPlan& p, long long capV, long long capT, float* points, IndexT* tris, int reverse,
+                        cudaStream_t s);
+template <typename IndexT>
+void launch_mc_remap(const FeBuffers& b, const GenPlan& p, long long capV, long long capT, IndexT* tris,
+                     cudaStream_t s);
+
 // learned output-size predictor (predictor.cu): 16^3-cell blocks
 long long block_count(const Grid& g);
 void launch_block_tris(const Grid& g, const uint32_t* bits, int* counts, cudaStream_t s);

@@ -399,3 +399,22 @@ def test_noise_512_bitexact(M):
     got = gpu_extract(M, vol, 0.0, M.MARCHING_CUBES)
     ref = oracle_lib.mc(vol, 0.0)
     assert_same_mesh(got, ref, "MC 512")
+
+
+def test_mc_triangles_into_unaligned_buffer(M):
+    """Marching Cubes over rows of up to 16 words writes FE-id triangles and remaps them in place: a triangle
+    buffer 4 bytes past a 16-byte boundary takes the remap's one-by-one path, with the same mesh."""
+    import torch
+    vol = M.generate_value_noise((61, 47, 35), 4, 16, seed=5)
+    ref = oracle_lib.mc(vol, 0.0)
+    V, T = ref[0].shape[0], ref[2].shape[0]
+    dv = torch.from_numpy(vol.reshape(-1)).cuda()
+    for ib, dt in ((4, torch.int32), (8, torch.int64)):
+        m = M.DeviceMesh(V, T, ib)
+        buf = torch.empty(3 * T + 1, dtype=dt, device="cuda")
+        m.tris = buf[1:].view(T, 3)
+        got = M.extract_device(dv, (61, 47, 35), 0.0, M.MARCHING_CUBES, out=m, index_bytes=ib)
+        torch.cuda.synchronize()
+        assert got is m
+        assert_same_mesh((m.points[:V].cpu().numpy(), m.normals[:V].cpu().numpy(),
+                          m.tris[:T].cpu().numpy().astype(np.uint64)), ref, "MC unaligned tris ib %d" % ib)
