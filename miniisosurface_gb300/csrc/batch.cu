@@ -1,0 +1,536 @@
+// C ABI of the batched extraction and of graph mode (iso_extract_batch,
+// iso_count_batch, iso_batch_*, iso_ctx_set_graph) and the exact per-block
+// triangle counts of the output-size network (iso_block_tris).
+#include "capi_internal.h"
+
+using namespace capi;
+
+namespace capi {
+
+// ---------------------------------------------------------------------------
+// Batched extraction.  The requests are spread over L lanes (streams, each
+// with its own scratch and, for Marching Cubes, its own FE -> MC map), the
+// largest requests first, each to the lane with the fewest cells so far; a
+// lane runs its requests one after the other (count, scan, generate,
+// vertices), the lanes run side by side.  The whole batch is captured once
+// as a CUDA graph: its 8-counter block per request (totals, device status,
+// work counter) lives in the batch arena, so the counts stay on the device
+// and the generate kernels check the capacities there; one copy at the end
+// brings every request's counters back.
+// ---------------------------------------------------------------------------
+struct BatchItem {
+    Grid g;
+    Plans pl;
+    int lane = 0;
+};
+
+constexpr int kMaxLanes = 64;
+constexpr int kTuneLanes[] = {1, 2, 4, 8, 16, 32, 64};
+// work splits: a request's count and generate plans size their grids and work
+// items for nsm / share SMs (several lanes share the GPU)
+constexpr int kTuneShares[] = {1, 2, 4, 8};
+
+void replan(iso_ctx* ctx, std::vector<BatchItem>& items, const std::vector<int>& run, int share)
+{
+    const int nsm = std::max(1, ctx->nsm / std::max(1, share));
+    for (int r : run) items[r].pl = make_plans(ctx, items[r].g, nsm);
+}
+
+// Lane of every request with work and the arena layout: counters of all n
+// requests, then per lane its scratch and FE -> MC map.
+struct BatchLayout {
+    int lanes = 1;
+    std::vector<size_t> scratch_at, scratch_bytes, map_at;
+    size_t bytes = 0;
+};
+
+BatchLayout plan_batch(const iso_request* req, const iso_mesh* out, int64_t n, std::vector<BatchItem>& items,
+                       const std::vector<int>& run, int lanes)
+{
+    BatchLayout lay;
+    lay.lanes = lanes;
+    std::vector<int> order(run);
+    auto cells = [&](int r) { return (double)(items[r].g.nx - 1) * (items[r].g.ny - 1) * (items[r].g.nz - 1); };
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cells(a) > cells(b); });
+    std::vector<double> load(lanes, 0.0);
+    std::vector<size_t> scratch(lanes, 0), map(lanes, 0);
+    for (int r : order) {
+        const int l = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        items[r].lane = l;
+        load[l] += cells(r);
+        scratch[l] = std::max(scratch[l], scratch_size(items[r].g, items[r].pl.cp));
+        if (out && req[r].algorithm == ISO_MARCHING_CUBES) {
+            const long long capV = vertex_limit(&out[r], out[r].cap_points);
+            const long long capM = capV < 0xffffffffll ? capV : 0xffffffffll;
+            map[l] = std::max(map[l], (size_t)(capM + 1024) * 4);
+        }
+    }
+    size_t at = align256((size_t)n * 8 * sizeof(unsigned long long));
+    for (int l = 0; l < lanes; ++l) {
+        lay.scratch_at.push_back(at);
+        lay.scratch_bytes.push_back(scratch[l]);
+        at += align256(scratch[l]);
+        lay.map_at.push_back(at);
+        at += align256(map[l]);
+    }
+    lay.bytes = at;
+    return lay;
+}
+
+// Captures and the batch buffers' allocations of all contexts take turns: a
+// free (which synchronises the device) in one thread would invalidate a
+// capture running in another.
+std::mutex g_batch_mutex;
+
+// Batch buffers (the caller holds g_batch_mutex).  Only this context's work on
+// s uses them: the graphs and the lanes join back into s.
+iso_status ensure_batch(iso_ctx* ctx, const BatchLayout& lay, int64_t n, cudaStream_t s)
+{
+    if (lay.bytes > ctx->batch_arena_bytes) {
+        ISO_CUDA(ctx, cudaStreamSynchronize(s));
+        cudaFree(ctx->batch_arena);
+        ctx->batch_arena = nullptr;
+        ctx->batch_arena_bytes = 0;
+        ISO_CUDA(ctx, cudaMalloc(&ctx->batch_arena, lay.bytes));
+        ctx->batch_arena_bytes = lay.bytes;
+    }
+    if ((size_t)n > ctx->h_batch_n) {
+        ISO_CUDA(ctx, cudaStreamSynchronize(s));
+        if (ctx->h_batch) cudaFreeHost(ctx->h_batch);
+        ctx->h_batch = nullptr;
+        ctx->h_batch_n = 0;
+        ISO_CUDA(ctx, cudaHostAlloc(&ctx->h_batch, (size_t)n * 8 * sizeof(unsigned long long), cudaHostAllocDefault));
+        ctx->h_batch_n = (size_t)n;
+    }
+    if (!ctx->s_capture) ISO_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->s_capture, cudaStreamNonBlocking));
+    for (cudaEvent_t* e : {&ctx->batch_fork, &ctx->batch_t0, &ctx->batch_t1})
+        if (!*e) ISO_CUDA(ctx, cudaEventCreateWithFlags(e, e == &ctx->batch_fork ? cudaEventDisableTiming : 0));
+    while ((int)ctx->lane_streams.size() < lay.lanes) {
+        cudaStream_t q;
+        cudaEvent_t e;
+        ISO_CUDA(ctx, cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking));
+        ctx->lane_streams.push_back(q);
+        ISO_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        ctx->lane_join.push_back(e);
+    }
+    return ISO_OK;
+}
+
+// What a captured graph depends on: lanes, buffers, requests and meshes.
+std::vector<unsigned char> batch_key(const iso_ctx* ctx, int lanes, int share, const iso_request* req,
+                                     const iso_mesh* out, int64_t n)
+{
+    std::vector<unsigned char> k;
+    auto put = [&](const void* p, size_t len) {
+        const unsigned char* c = static_cast<const unsigned char*>(p);
+        k.insert(k.end(), c, c + len);
+    };
+    const unsigned char count_only = out ? 0 : 1;
+    put(&count_only, 1);
+    put(&lanes, sizeof lanes);
+    put(&share, sizeof share);
+    put(&ctx->reverse, sizeof ctx->reverse);
+    put(&ctx->batch_arena, sizeof ctx->batch_arena);
+    put(&ctx->h_batch, sizeof ctx->h_batch);
+    put(&n, sizeof n);
+    put(req, (size_t)n * sizeof(iso_request));
+    for (int64_t r = 0; out && r < n; ++r) {
+        put(&out[r].points, sizeof out[r].points);
+        put(&out[r].normals, sizeof out[r].normals);
+        put(&out[r].tris, sizeof out[r].tris);
+        put(&out[r].index_bytes, sizeof out[r].index_bytes);
+        put(&out[r].cap_points, sizeof out[r].cap_points);
+        put(&out[r].cap_tris, sizeof out[r].cap_tris);
+    }
+    return k;
+}
+
+// The batch's work from `origin`: fork to the lanes, each lane's requests in
+// turn, join, the counters' copy to the host; all on origin's side of the join.
+void enqueue_batch(iso_ctx* ctx, const iso_request* req, const iso_mesh* out, int64_t n, std::vector<BatchItem>& items,
+                   const std::vector<int>& run, const BatchLayout& lay, cudaStream_t origin)
+{
+    char* arena = static_cast<char*>(ctx->batch_arena);
+    unsigned long long* counters = reinterpret_cast<unsigned long long*>(arena);
+    const bool prof = ctx->profiling;
+    ctx->profiling = false;  // no timing events between the lanes' kernels
+    cudaEventRecord(ctx->batch_fork, origin);
+    for (int l = 0; l < lay.lanes; ++l) cudaStreamWaitEvent(ctx->lane_streams[l], ctx->batch_fork, 0);
+    for (int r : run) {
+        BatchItem& it = items[r];
+        cudaStream_t ls = ctx->lane_streams[it.lane];
+        FeBuffers b;
+        carve(arena + lay.scratch_at[it.lane], it.g, it.pl.cp, b);
+        b.totals = counters + 8 * r;
+        b.fe2mc = reinterpret_cast<uint32_t*>(arena + lay.map_at[it.lane]);
+        PassMarks pm(ctx, ls);
+        const iso_algorithm algo = static_cast<iso_algorithm>(req[r].algorithm);
+        enqueue_count(ctx, algo, req[r].volume, it.g, req[r].isoval, it.pl, b, ls, pm);
+        if (out) enqueue_generate(ctx, algo, req[r].volume, it.g, req[r].isoval, it.pl, b, &out[r], ls, pm);
+    }
+    for (int l = 0; l < lay.lanes; ++l) {
+        cudaEventRecord(ctx->lane_join[l], ctx->lane_streams[l]);
+        cudaStreamWaitEvent(origin, ctx->lane_join[l], 0);
+    }
+    cudaMemcpyAsync(ctx->h_batch, counters, (size_t)n * 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                    origin);
+    ctx->profiling = prof;
+}
+
+// Capture the batch on the lanes and make ctx->batch_exec run it (updating
+// the executable graph in place when the topology allows).  out == nullptr:
+// passes 1-3 only (iso_count_batch).
+iso_status capture_batch(iso_ctx* ctx, const iso_request* req, const iso_mesh* out, int64_t n,
+                         std::vector<BatchItem>& items, const std::vector<int>& run, const BatchLayout& lay)
+{
+    cudaStream_t sc = ctx->s_capture;
+    const int slot = out ? 0 : 1;
+    cudaGraphExec_t& exec = ctx->batch_exec[slot];
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(sc, cudaStreamCaptureModeRelaxed);
+    if (e == cudaSuccess) {
+        enqueue_batch(ctx, req, out, n, items, run, lay, sc);
+        e = cudaStreamEndCapture(sc, &graph);
+    }
+    if (e != cudaSuccess || !graph) {
+        cudaGetLastError();
+        if (graph) cudaGraphDestroy(graph);
+        ctx->batch_key[slot].clear();
+        ctx->last_error = std::string("capturing the batch failed: ") + cudaGetErrorString(e);
+        return ISO_ERR_CUDA;
+    }
+    if (exec) {
+        cudaGraphExecUpdateResultInfo info;
+        if (cudaGraphExecUpdate(exec, graph, &info) != cudaSuccess) {
+            cudaGetLastError();
+            cudaGraphExecDestroy(exec);
+            exec = nullptr;
+        }
+    }
+    if (!exec) e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        exec = nullptr;
+        ctx->batch_key[slot].clear();
+        return cuda_fail(ctx, e, "cudaGraphInstantiate");
+    }
+    return ISO_OK;
+}
+
+// Prepare (lanes, buffers, graph) for `lanes` lanes; nothing runs.
+iso_status prepare_batch(iso_ctx* ctx, const iso_request* req, const iso_mesh* out, int64_t n,
+                         std::vector<BatchItem>& items, const std::vector<int>& run, int lanes, int share,
+                         cudaStream_t s)
+{
+    replan(ctx, items, run, share);
+    const BatchLayout lay = plan_batch(req, out, n, items, run, lanes);
+    std::lock_guard<std::mutex> lock(g_batch_mutex);
+    iso_status st = ensure_batch(ctx, lay, n, s);
+    if (st != ISO_OK) return st;
+    std::vector<unsigned char> key = batch_key(ctx, lanes, share, req, out, n);
+    const int slot = out ? 0 : 1;
+    if (ctx->batch_exec[slot] && key == ctx->batch_key[slot]) return ISO_OK;
+    st = capture_batch(ctx, req, out, n, items, run, lay);
+    if (st == ISO_OK) ctx->batch_key[slot].swap(key);
+    return st;
+}
+
+// Milliseconds of one run of the prepared batch (the best of two after one warm-up run).
+iso_status time_batch(iso_ctx* ctx, cudaGraphExec_t exec, cudaStream_t s, float& best)
+{
+    best = 1e30f;
+    for (int rep = 0; rep < 3; ++rep) {
+        ISO_CUDA(ctx, cudaEventRecord(ctx->batch_t0, s));
+        ISO_CUDA(ctx, cudaGraphLaunch(exec, s));
+        ISO_CUDA(ctx, cudaEventRecord(ctx->batch_t1, s));
+        ISO_CUDA(ctx, cudaEventSynchronize(ctx->batch_t1));
+        float ms = 0.f;
+        ISO_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->batch_t0, ctx->batch_t1));
+        if (rep > 0) best = std::min(best, ms);
+    }
+    return ISO_OK;
+}
+
+// iso_extract_device_async as a CUDA graph: the passes and the counters'
+// copy to result_host captured once, relaunched while the call's arguments,
+// the context's buffers and result_host stay the same (result_host must be
+// pinned: a pageable one takes the stream path).
+iso_status extract_graph(iso_ctx* ctx, iso_algorithm algo, const float* volume, const Grid& g, const iso_grid* grid,
+                         float isoval, const Plans& pl, FeBuffers& b, const iso_mesh* out, int64_t* result_host,
+                         cudaStream_t s)
+{
+    cudaPointerAttributes attr{};
+    if (cudaPointerGetAttributes(&attr, result_host) != cudaSuccess || attr.type != cudaMemoryTypeHost) {
+        cudaGetLastError();
+        PassMarks pm(ctx, s);
+        enqueue_count(ctx, algo, volume, g, isoval, pl, b, s, pm);
+        enqueue_generate(ctx, algo, volume, g, isoval, pl, b, out, s, pm);
+        ISO_CUDA(ctx, cudaGetLastError());
+        ISO_CUDA(ctx,
+                 cudaMemcpyAsync(result_host, b.totals, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+        return ISO_OK;
+    }
+    std::vector<unsigned char> key;
+    auto put = [&](const void* p, size_t len) {
+        const unsigned char* c = static_cast<const unsigned char*>(p);
+        key.insert(key.end(), c, c + len);
+    };
+    put(&algo, sizeof algo);
+    put(&volume, sizeof volume);
+    put(grid, sizeof *grid);
+    put(&isoval, sizeof isoval);
+    put(&out->points, sizeof out->points);
+    put(&out->normals, sizeof out->normals);
+    put(&out->tris, sizeof out->tris);
+    put(&out->index_bytes, sizeof out->index_bytes);
+    put(&out->cap_points, sizeof out->cap_points);
+    put(&out->cap_tris, sizeof out->cap_tris);
+    put(&result_host, sizeof result_host);
+    put(&ctx->scratch, sizeof ctx->scratch);
+    put(&ctx->fe2mc, sizeof ctx->fe2mc);
+    put(&ctx->reverse, sizeof ctx->reverse);
+    if (!ctx->one_exec || key != ctx->one_key) {
+        std::lock_guard<std::mutex> lock(g_batch_mutex);
+        if (!ctx->s_capture) ISO_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->s_capture, cudaStreamNonBlocking));
+        cudaStream_t sc = ctx->s_capture;
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(sc, cudaStreamCaptureModeRelaxed);
+        if (e == cudaSuccess) {
+            PassMarks pm(ctx, sc);
+            enqueue_count(ctx, algo, volume, g, isoval, pl, b, sc, pm);
+            enqueue_generate(ctx, algo, volume, g, isoval, pl, b, out, sc, pm);
+            cudaMemcpyAsync(result_host, b.totals, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, sc);
+            e = cudaStreamEndCapture(sc, &graph);
+        }
+        if (e != cudaSuccess || !graph) {
+            cudaGetLastError();
+            if (graph) cudaGraphDestroy(graph);
+            ctx->one_key.clear();
+            ctx->last_error = std::string("capturing the extraction failed: ") + cudaGetErrorString(e);
+            return ISO_ERR_CUDA;
+        }
+        if (ctx->one_exec) {
+            cudaGraphExecUpdateResultInfo info;
+            if (cudaGraphExecUpdate(ctx->one_exec, graph, &info) != cudaSuccess) {
+                cudaGetLastError();
+                cudaGraphExecDestroy(ctx->one_exec);
+                ctx->one_exec = nullptr;
+            }
+        }
+        if (!ctx->one_exec) e = cudaGraphInstantiate(&ctx->one_exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            ctx->one_exec = nullptr;
+            ctx->one_key.clear();
+            return cuda_fail(ctx, e, "cudaGraphInstantiate");
+        }
+        ctx->one_key.swap(key);
+    }
+    ISO_CUDA(ctx, cudaGraphLaunch(ctx->one_exec, s));
+    return ISO_OK;
+}
+
+}  // namespace capi
+
+extern "C" {
+
+iso_status iso_ctx_set_graph(iso_ctx* ctx, int enable)
+{
+    if (!ctx) return ISO_ERR_INVALID_ARG;
+    ctx->one_graph = enable ? 1 : 0;
+    if (!enable && ctx->one_exec) {
+        cudaGraphExecDestroy(ctx->one_exec);
+        ctx->one_exec = nullptr;
+        ctx->one_key.clear();
+    }
+    return ISO_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// iso_extract_batch (out != nullptr) and iso_count_batch (out == nullptr, the
+// counts into nV / nT): validate, tune the lanes if asked, run the graph.
+iso_status run_batch(iso_ctx* ctx, int64_t n, const iso_request* req, iso_mesh* out, int64_t* nV, int64_t* nT,
+                     iso_status* status, cudaStream_t s)
+{
+    ISO_CUDA(ctx, cudaSetDevice(ctx->device));
+    std::vector<iso_status> st((size_t)n, ISO_OK);
+    std::vector<BatchItem> items((size_t)n);
+    std::vector<int> run;  // requests with work
+    for (int64_t r = 0; r < n; ++r) {
+        if (out) {
+            if (check_mesh(&out[r]) != ISO_OK) {
+                st[r] = ISO_ERR_INVALID_ARG;
+                continue;
+            }
+            out[r].n_points = out[r].n_tris = 0;
+        } else {
+            nV[r] = nT[r] = 0;
+        }
+        Grid g;
+        if (!valid_algo(static_cast<iso_algorithm>(req[r].algorithm)) || !make_grid(&req[r].grid, g)) {
+            st[r] = ISO_ERR_INVALID_ARG;
+            continue;
+        }
+        if (empty_grid(g)) continue;
+        if (!req[r].volume) {
+            st[r] = ISO_ERR_INVALID_ARG;
+            continue;
+        }
+        items[r].g = g;
+        items[r].pl = make_plans(ctx, g);
+        if (out && req[r].algorithm == ISO_MC_DUPFREE && !items[r].pl.gp.fits) {
+            ctx->last_error = "the duplicate-free order needs rows of at most 1024 points";
+            st[r] = ISO_ERR_INVALID_ARG;
+            continue;
+        }
+        run.push_back((int)r);
+    }
+    iso_status rc = ISO_OK;
+    if (!run.empty() && !ctx->batch_graph) {  // the lanes launched directly, no graph
+        int lanes = ctx->batch_lanes > 0 ? ctx->batch_lanes : (ctx->batch_tuned > 0 ? ctx->batch_tuned : 8);
+        const int share = ctx->batch_share > 0 ? ctx->batch_share : std::max(1, ctx->batch_tuned_share);
+        lanes = std::min(lanes, std::max(1, (int)run.size()));
+        replan(ctx, items, run, share);
+        const BatchLayout lay = plan_batch(req, out, n, items, run, lanes);
+        {
+            std::lock_guard<std::mutex> lock(g_batch_mutex);
+            rc = ensure_batch(ctx, lay, n, s);
+        }
+        if (rc != ISO_OK) return rc;
+        enqueue_batch(ctx, req, out, n, items, run, lay, s);
+        ISO_CUDA(ctx, cudaGetLastError());
+        ISO_CUDA(ctx, cudaStreamSynchronize(s));
+    } else if (!run.empty()) {
+        int lanes = ctx->batch_lanes > 0 ? ctx->batch_lanes : ctx->batch_tuned;
+        int share = ctx->batch_share > 0 ? ctx->batch_share : ctx->batch_tuned_share;
+        if (lanes <= 0 || share <= 0) {  // autotuner: time the batch at each (lanes, split), keep the fastest
+            float best = 1e30f;
+            int best_l = 1, best_s = 1;
+            for (int L : kTuneLanes) {
+                if (lanes > 0 && L != lanes) continue;
+                if (L > 1 && L > (int)run.size()) break;
+                for (int S : kTuneShares) {
+                    if (share > 0 && S != share) continue;
+                    if (S > L) break;  // a request never has fewer SMs than nsm / lanes
+                    rc = prepare_batch(ctx, req, out, n, items, run, L, S, s);
+                    if (rc != ISO_OK) return rc;
+                    float ms;
+                    rc = time_batch(ctx, ctx->batch_exec[out ? 0 : 1], s, ms);
+                    if (rc != ISO_OK) return rc;
+                    if (ms < best) {
+                        best = ms;
+                        best_l = L;
+                        best_s = S;
+                    }
+                }
+            }
+            lanes = best_l;
+            share = best_s;
+            if (ctx->batch_lanes <= 0) ctx->batch_tuned = lanes;
+            if (ctx->batch_share <= 0) ctx->batch_tuned_share = share;
+        }
+        lanes = std::min(lanes, std::max(1, (int)run.size()));
+        rc = prepare_batch(ctx, req, out, n, items, run, lanes, share, s);
+        if (rc != ISO_OK) return rc;
+        ISO_CUDA(ctx, cudaGraphLaunch(ctx->batch_exec[out ? 0 : 1], s));
+        ISO_CUDA(ctx, cudaStreamSynchronize(s));
+    }
+    if (!run.empty()) {
+        for (int r : run) {
+            const unsigned long long* c = ctx->h_batch + 8 * (size_t)r;
+            if (out) {
+                st[r] = finish_counts(ctx, &out[r], (long long)c[0], (long long)c[1], (long long)c[3],
+                                      &out[r].n_points, &out[r].n_tris);
+            } else {
+                st[r] = finish_counts(ctx, nullptr, (long long)c[0], (long long)c[1], (long long)c[3], &nV[r], &nT[r]);
+            }
+        }
+    }
+    for (int64_t r = 0; r < n; ++r) {
+        if (status) status[r] = st[r];
+        if (rc == ISO_OK && st[r] != ISO_OK) rc = st[r];
+    }
+    return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+iso_status iso_extract_batch(iso_ctx* ctx, int64_t n, const iso_request* req, iso_mesh* out, iso_status* status,
+                             void* stream)
+{
+    if (!ctx || n < 0 || (n > 0 && (!req || !out))) return ISO_ERR_INVALID_ARG;
+    return run_batch(ctx, n, req, out, nullptr, nullptr, status, static_cast<cudaStream_t>(stream));
+}
+
+iso_status iso_count_batch(iso_ctx* ctx, int64_t n, const iso_request* req, int64_t* n_points, int64_t* n_tris,
+                           iso_status* status, void* stream)
+{
+    if (!ctx || n < 0 || (n > 0 && (!req || !n_points || !n_tris))) return ISO_ERR_INVALID_ARG;
+    return run_batch(ctx, n, req, nullptr, n_points, n_tris, status, static_cast<cudaStream_t>(stream));
+}
+
+iso_status iso_block_tris(iso_ctx* ctx, const float* volume, const iso_grid* grid, float isoval, int32_t* counts,
+                          void* stream)
+{
+    if (!ctx || !grid) return ISO_ERR_INVALID_ARG;
+    Grid g;
+    if (!make_grid(grid, g)) return ISO_ERR_INVALID_ARG;
+    if (empty_grid(g)) return ISO_OK;
+    if (!volume || !counts) return ISO_ERR_INVALID_ARG;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    ISO_CUDA(ctx, cudaSetDevice(ctx->device));
+    const Plans pl = make_plans(ctx, g);
+    FeBuffers b;
+    iso_status st = ensure_scratch(ctx, g, pl.cp, b, s);
+    if (st != ISO_OK) return st;
+    iso::launch_count(volume, g, isoval, ctx->d_cases, false, pl.cp, b, s);  // bit rows of the whole grid
+    ISO_CUDA(ctx, cudaMemsetAsync(counts, 0, sizeof(int32_t) * (size_t)iso::block_count(g), s));
+    iso::launch_block_tris(g, b.bits, counts, s);
+    ISO_CUDA(ctx, cudaGetLastError());
+    return ISO_OK;
+}
+
+iso_status iso_batch_set_lanes(iso_ctx* ctx, int lanes)
+{
+    if (!ctx || lanes < 0 || lanes > kMaxLanes) return ISO_ERR_INVALID_ARG;
+    ctx->batch_lanes = lanes;
+    if (lanes == 0) {  // tune again on the next batch, the split too
+        ctx->batch_tuned = 0;
+        ctx->batch_tuned_share = 0;
+    }
+    return ISO_OK;
+}
+
+iso_status iso_batch_set_split(iso_ctx* ctx, int share)
+{
+    if (!ctx || share < 0 || share > 64) return ISO_ERR_INVALID_ARG;
+    ctx->batch_share = share;
+    if (share == 0) ctx->batch_tuned_share = 0;  // tune again on the next batch
+    return ISO_OK;
+}
+
+int iso_batch_split(const iso_ctx* ctx)
+{
+    if (!ctx) return 0;
+    return ctx->batch_share > 0 ? ctx->batch_share : ctx->batch_tuned_share;
+}
+
+iso_status iso_batch_set_graph(iso_ctx* ctx, int enable)
+{
+    if (!ctx) return ISO_ERR_INVALID_ARG;
+    ctx->batch_graph = enable ? 1 : 0;
+    return ISO_OK;
+}
+
+int iso_batch_lanes(const iso_ctx* ctx)
+{
+    if (!ctx) return 0;
+    return ctx->batch_lanes > 0 ? ctx->batch_lanes : ctx->batch_tuned;
+}
+
+}  // extern "C"

@@ -1,85 +1,10 @@
 // C ABI of the extractor: contexts, scratch, the extraction entry points and
-// the pass-by-pass Flying Edges object.  See include/miniiso.h.
-#include <algorithm>
-#include <cstdio>
-#include <cstring>
-#include <mutex>
-#include <new>
-#include <string>
-#include <vector>
-
-#include "../../include/miniiso.h"
+// the pass-by-pass Flying Edges object.  See include/miniiso.h.  Batches and
+// graph mode live in batch.cu.
+#include "capi_internal.h"
 #include "case_table.h"
-#include "iso_device.cuh"
-#include "iso_kernels.h"
 
-using iso::CaseTables;
-using iso::FeBuffers;
-using iso::Grid;
-
-struct iso_ctx {
-    int device = 0;
-    int nsm = 0;
-    CaseTables* d_cases = nullptr;
-    // scratch of the one-shot entry points
-    void* scratch = nullptr;
-    size_t scratch_bytes = 0;
-    uint32_t* fe2mc = nullptr;
-    long long fe2mc_cap = 0;
-    // staging for the host entry points
-    float* d_volume = nullptr;
-    size_t d_volume_bytes = 0;
-    float* d_points = nullptr;
-    float* d_normals = nullptr;
-    void* d_tris = nullptr;
-    long long d_cap_points = 0, d_cap_tris = 0;
-    int d_index_bytes = 0;
-    unsigned long long* h_totals = nullptr;  // pinned, 4 entries
-    unsigned long long* h_slab = nullptr;    // pinned and mapped, 2 x 9 entries (slab counts)
-    unsigned long long* h_slab_dev = nullptr;  // its device address (written by k_slab_readback)
-    void* scratch_b = nullptr;               // second scratch set (streamed path: the next slab's counts)
-    size_t scratch_b_bytes = 0;
-    void* d_typed = nullptr;                 // typed volume samples before conversion
-    size_t d_typed_bytes = 0;
-    // streamed host entry point: copy streams, events, two device staging meshes
-    cudaStream_t s_h2d = nullptr, s_d2h = nullptr, s_cnt = nullptr;  // copies in / out, slab counts
-    std::vector<cudaEvent_t> sync_events;
-    float* st_points[2] = {nullptr, nullptr};
-    float* st_normals[2] = {nullptr, nullptr};
-    void* st_tris[2] = {nullptr, nullptr};
-    long long st_cap_points = 0, st_cap_tris = 0;
-    int st_index_bytes = 0;
-    // batched entry point (iso_extract_batch): lanes, their scratch, the captured graph
-    int batch_lanes = 0;        // set by iso_batch_set_lanes; 0: the autotuner's choice
-    int batch_tuned = 0;        // lanes the autotuner picked (0: not yet tuned)
-    int batch_graph = 1;        // capture batches as CUDA graphs (0: launch the lanes directly)
-    // iso_extract_device_async as a replayed CUDA graph (iso_ctx_set_graph)
-    int one_graph = 0;
-    cudaGraphExec_t one_exec = nullptr;
-    std::vector<unsigned char> one_key;
-    int batch_share = 0;        // set by iso_batch_set_split: a request's plans assume nsm / share SMs; 0: tuned
-    int batch_tuned_share = 0;  // the autotuner's share (0: not yet tuned)
-    cudaStream_t s_capture = nullptr;
-    std::vector<cudaStream_t> lane_streams;
-    std::vector<cudaEvent_t> lane_join;
-    cudaEvent_t batch_fork = nullptr, batch_t0 = nullptr, batch_t1 = nullptr;
-    void* batch_arena = nullptr;
-    size_t batch_arena_bytes = 0;
-    unsigned long long* h_batch = nullptr;  // pinned: 8 counters per request
-    size_t h_batch_n = 0;
-    // executable graphs of iso_extract_batch [0] and iso_count_batch [1], and what each was captured for
-    cudaGraphExec_t batch_exec[2] = {nullptr, nullptr};
-    std::vector<unsigned char> batch_key[2];
-    int reverse = 1;  // pass 4 walks the planes backwards (the count pass leaves the last ones in L2)
-    int stream_host = 1;  // iso_extract_host streams slabs (large grids)
-    std::string last_error;
-    // per-pass timing (iso_ctx_profile)
-    bool profiling = false;
-    std::vector<cudaEvent_t> event_pool;
-    size_t events_used = 0;
-    struct Span { int pass; cudaEvent_t begin, end; };
-    std::vector<Span> spans;
-};
+using namespace capi;
 
 struct iso_fe {
     iso_ctx* ctx = nullptr;
@@ -100,344 +25,6 @@ struct iso_fe {
 namespace {
 
 const char* kVersion = "miniiso-gb300 0.1 (sm_103a)";
-
-iso_status cuda_fail(iso_ctx* ctx, cudaError_t e, const char* what)
-{
-    if (ctx) {
-        ctx->last_error = std::string(what) + ": " + cudaGetErrorString(e);
-    }
-    return e == cudaErrorMemoryAllocation ? ISO_ERR_OOM : ISO_ERR_CUDA;
-}
-
-#define ISO_CUDA(ctx, call)                                      \
-    do {                                                         \
-        cudaError_t e_ = (call);                                 \
-        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
-    } while (0)
-
-size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
-
-// Derived per-case tables: the packed triangle lists, the first-appearance
-// edge order (marching cubes numbering) and the cut-edge masks.
-void build_case_tables(CaseTables& t)
-{
-    for (int c = 0; c < 256; ++c) {
-        const uint64_t w = kIsoCaseTris[c];
-        t.tris[c] = w;
-        uint16_t cut = 0;
-        for (int e = 0; e < 12; ++e) {
-            if (((c >> kIsoEdgeLo[e]) & 1) != ((c >> kIsoEdgeHi[e]) & 1)) cut |= (uint16_t)(1u << e);
-        }
-        t.cut[c] = cut;
-        uint64_t order = 0;
-        int n = 0;
-        uint16_t seen = 0;
-        for (int q = 0; q < 3 * iso_case_ntris(w); ++q) {
-            const int e = iso_case_edge(w, q);
-            if (!((seen >> e) & 1)) {
-                seen |= (uint16_t)(1u << e);
-                order |= (uint64_t)e << (4 * n);
-                ++n;
-            }
-        }
-        t.order[c] = order | ((uint64_t)n << 60);
-    }
-}
-
-bool valid_algo(iso_algorithm a)
-{
-    return a == ISO_FLYING_EDGES || a == ISO_MARCHING_CUBES || a == ISO_MC_DUPFREE;
-}
-
-bool make_grid(const iso_grid* gr, Grid& g)
-{
-    for (int a = 0; a < 3; ++a) {
-        if (gr->dims[a] < 1 || gr->dims[a] > (1ll << 30)) return false;
-    }
-    g.nx = (int)gr->dims[0];
-    g.ny = (int)gr->dims[1];
-    g.nz = (int)gr->dims[2];
-    g.W = (g.nx + 31) / 32;
-    g.R = (long long)g.ny * g.nz;
-    if ((long long)g.W * g.R > (1ll << 40)) return false;
-    g.kd = 0;
-    g.kr = 0;
-    g.ke = g.nz;
-    for (int a = 0; a < 3; ++a) {
-        g.sp[a] = gr->spacing[a];
-        g.zp[a] = gr->origin[a];
-    }
-    return true;
-}
-
-bool empty_grid(const Grid& g) { return g.nx < 2 || g.ny < 2 || g.nz < 2; }
-
-size_t scratch_size(const Grid& g, const iso::CountPlan& cp)
-{
-    const size_t R = (size_t)g.R;
-    return align256(R * 16) + align256(R * 8) + align256(R * 4) + align256(4 * R * 8) +
-           align256(4 * (size_t)cp.nseg * 8) + align256(8 * 8) + align256(R * (size_t)g.W * 4);
-}
-
-void carve(void* base, const Grid& g, const iso::CountPlan& cp, FeBuffers& b)
-{
-    const size_t R = (size_t)g.R;
-    char* p = static_cast<char*>(base);
-    b.rowcnt = reinterpret_cast<uint4*>(p); p += align256(R * 16);
-    b.trims = reinterpret_cast<uint2*>(p); p += align256(R * 8);
-    b.mccnt = reinterpret_cast<uint32_t*>(p); p += align256(R * 4);
-    b.starts = reinterpret_cast<unsigned long long*>(p); p += align256(4 * R * 8);
-    b.part = reinterpret_cast<unsigned long long*>(p); p += align256(4 * (size_t)cp.nseg * 8);
-    b.totals = reinterpret_cast<unsigned long long*>(p); p += align256(8 * 8);
-    b.bits = reinterpret_cast<uint32_t*>(p);
-}
-
-iso_status ensure_scratch(iso_ctx* ctx, const Grid& g, const iso::CountPlan& cp, FeBuffers& b, cudaStream_t s)
-{
-    const size_t need = scratch_size(g, cp);
-    if (need > ctx->scratch_bytes) {
-        if (ctx->scratch) {
-            ISO_CUDA(ctx, cudaStreamSynchronize(s));
-            cudaFree(ctx->scratch);
-            ctx->scratch = nullptr;
-            ctx->scratch_bytes = 0;
-        }
-        const size_t alloc = need + need / 4;
-        ISO_CUDA(ctx, cudaMalloc(&ctx->scratch, alloc));
-        ctx->scratch_bytes = alloc;
-    }
-    carve(ctx->scratch, g, cp, b);
-    b.fe2mc = ctx->fe2mc;
-    return ISO_OK;
-}
-
-// Device buffer for typed samples before their conversion to float.
-iso_status ensure_typed(iso_ctx* ctx, size_t bytes, cudaStream_t s)
-{
-    if (bytes <= ctx->d_typed_bytes) return ISO_OK;
-    ISO_CUDA(ctx, cudaStreamSynchronize(s));
-    cudaFree(ctx->d_typed);
-    ctx->d_typed = nullptr;
-    ctx->d_typed_bytes = 0;
-    ISO_CUDA(ctx, cudaMalloc(&ctx->d_typed, bytes));
-    ctx->d_typed_bytes = bytes;
-    return ISO_OK;
-}
-
-// The second scratch set (the streamed path counts slab q+1 while slab q
-// is generated from the first).
-iso_status ensure_scratch_b(iso_ctx* ctx, const Grid& g, const iso::CountPlan& cp, FeBuffers& b, cudaStream_t s)
-{
-    const size_t need = scratch_size(g, cp);
-    if (need > ctx->scratch_b_bytes) {
-        if (ctx->scratch_b) {
-            ISO_CUDA(ctx, cudaStreamSynchronize(s));
-            cudaFree(ctx->scratch_b);
-            ctx->scratch_b = nullptr;
-            ctx->scratch_b_bytes = 0;
-        }
-        const size_t alloc = need + need / 4;
-        ISO_CUDA(ctx, cudaMalloc(&ctx->scratch_b, alloc));
-        ctx->scratch_b_bytes = alloc;
-    }
-    carve(ctx->scratch_b, g, cp, b);
-    b.fe2mc = ctx->fe2mc;
-    return ISO_OK;
-}
-
-iso_status ensure_fe2mc(iso_ctx* ctx, long long cap, cudaStream_t s)
-{
-    if (cap > ctx->fe2mc_cap) {
-        if (ctx->fe2mc) {
-            ISO_CUDA(ctx, cudaStreamSynchronize(s));
-            cudaFree(ctx->fe2mc);
-            ctx->fe2mc = nullptr;
-            ctx->fe2mc_cap = 0;
-        }
-        const long long alloc = cap + cap / 4 + 1024;
-        ISO_CUDA(ctx, cudaMalloc(&ctx->fe2mc, (size_t)alloc * 4));
-        ctx->fe2mc_cap = alloc;
-    }
-    return ISO_OK;
-}
-
-iso_status check_mesh(const iso_mesh* m)
-{
-    if (!m) return ISO_ERR_INVALID_ARG;
-    if (m->index_bytes != 4 && m->index_bytes != 8) return ISO_ERR_INVALID_ARG;
-    if (m->cap_points < 0 || m->cap_tris < 0) return ISO_ERR_INVALID_ARG;
-    if (m->cap_points > 0 && (!m->points || !m->normals)) return ISO_ERR_INVALID_ARG;
-    if (m->cap_tris > 0 && !m->tris) return ISO_ERR_INVALID_ARG;
-    return ISO_OK;
-}
-
-// Largest vertex count a mesh may hold (32-bit indices address < 2^32).
-long long vertex_limit(const iso_mesh* m, long long cap)
-{
-    const long long lim = m->index_bytes == 4 ? 0xffffffffll : (1ll << 62);
-    return cap < lim ? cap : lim;
-}
-
-// Events between consecutive kernels while profiling.
-cudaEvent_t next_event(iso_ctx* ctx)
-{
-    if (ctx->events_used == ctx->event_pool.size()) {
-        cudaEvent_t e;
-        if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
-        ctx->event_pool.push_back(e);
-    }
-    return ctx->event_pool[ctx->events_used++];
-}
-
-struct PassMarks {
-    iso_ctx* ctx;
-    cudaStream_t s;
-    cudaEvent_t last = nullptr;
-    PassMarks(iso_ctx* c, cudaStream_t st) : ctx(c), s(st)
-    {
-        if (ctx->profiling && (last = next_event(ctx))) cudaEventRecord(last, s);
-    }
-    void mark(int pass)
-    {
-        if (!ctx->profiling || !last) return;
-        cudaEvent_t e = next_event(ctx);
-        if (!e) return;
-        cudaEventRecord(e, s);
-        ctx->spans.push_back({pass, last, e});
-        last = e;
-    }
-};
-
-// Plans of one extraction.
-struct Plans {
-    iso::CountPlan cp;
-    iso::GenPlan gp;
-};
-
-Plans make_plans(const iso_ctx* ctx, const Grid& g, int nsm = 0)
-{
-    Plans p;
-    const int n = nsm > 0 ? nsm : ctx->nsm;
-    p.cp = iso::count_plan(g, n);
-    p.gp = iso::gen_plan(g, n);
-    return p;
-}
-
-// Passes 1-3: counts, scan, row starts.
-void enqueue_count(iso_ctx* ctx, iso_algorithm algo, const float* vol, const Grid& g, float iso, const Plans& pl,
-                   FeBuffers& b, cudaStream_t s, PassMarks& pm)
-{
-    const bool mc = algo == ISO_MARCHING_CUBES;
-    iso::launch_count(vol, g, iso, ctx->d_cases, mc, pl.cp, b, s);
-    pm.mark(ISO_PASS_COUNT);
-    iso::launch_scan(g, pl.cp, algo == ISO_MC_DUPFREE ? iso::kScanDup : (mc ? iso::kScanMC : iso::kScanFE), b, s);
-    pm.mark(ISO_PASS_SCAN);
-}
-
-// Pass 4 into the mesh buffers of `out` (device memory).
-void enqueue_generate(iso_ctx* ctx, iso_algorithm algo, const float* vol, const Grid& g, float iso, const Plans& pl,
-                      const FeBuffers& b, const iso_mesh* out, cudaStream_t s, PassMarks& pm)
-{
-    const long long capV = vertex_limit(out, out->cap_points);
-    const long long capT = out->cap_tris;
-    const bool i4 = out->index_bytes == 4;
-    if (algo == ISO_FLYING_EDGES) {
-        if (pl.gp.fits) {
-            if (i4)
-                iso::launch_fe_gen_warps<uint32_t>(vol, g, iso, ctx->d_cases, b, pl.cp, pl.gp, capV, capT, out->points,
-                                                   out->normals, static_cast<uint32_t*>(out->tris), ctx->reverse, s);
-            else
-                iso::launch_fe_gen_warps<uint64_t>(vol, g, iso, ctx->d_cases, b, pl.cp, pl.gp, capV, capT, out->points,
-                                                   out->normals, static_cast<uint64_t*>(out->tris), ctx->reverse, s);
-            pm.mark(ISO_PASS_FE_GENERATE);
-            if (iso::launch_fe_vertices(vol, g, iso, b, pl.gp, capV, capT, out->points, out->normals, s))
-                pm.mark(ISO_PASS_VERTICES);
-            return;
-        } else {
-            if (i4)
-                iso::launch_fe_gen_rows<uint32_t>(vol, g, iso, ctx->d_cases, b, pl.cp, capV, capT, out->points, out->normals,
-                                                  static_cast<uint32_t*>(out->tris), ctx->nsm, s);
-            else
-                iso::launch_fe_gen_rows<uint64_t>(vol, g, iso, ctx->d_cases, b, pl.cp, capV, capT, out->points, out->normals,
-                                                  static_cast<uint64_t*>(out->tris), ctx->nsm, s);
-        }
-        pm.mark(ISO_PASS_FE_GENERATE);
-    } else if (algo == ISO_MC_DUPFREE) {  // vertices and triangles in one pass (make_plans checked fits)
-        if (i4)
-            iso::launch_dup_gen_warps<uint32_t>(vol, g, iso, ctx->d_cases, b, pl.cp, pl.gp, capV, capT, out->points,
-                                                out->normals, static_cast<uint32_t*>(out->tris), ctx->reverse, s);
-        else
-            iso::launch_dup_gen_warps<uint64_t>(vol, g, iso, ctx->d_cases, b, pl.cp, pl.gp, capV, capT, out->points,
-                                                out->normals, static_cast<uint64_t*>(out->tris), ctx->reverse, s);
-        pm.mark(ISO_PASS_MC_VERTICES);
-        if (iso::launch_dup_vertices(vol, g, iso, b, pl.gp, capV, capT, out->points, out->normals, s))
-            pm.mark(ISO_PASS_VERTICES);
-    } else {
-        const long long capM = capV < 0xffffffffll ? capV : 0xffffffffll;  // fe2mc holds 32-bit ids
-        if (pl.gp.fits && iso::mc_fused(g, pl.gp)) {  // owned vertices + FE-id triangles, vertices, remap
-            if (i4)
-                iso::launch_mc_gen_tris<uint32_t>(g, ctx->d_cases, b, pl.cp, pl.gp, capM, capT, out->points,
-                                                  static_cast<uint32_t*>(out->tris), ctx->reverse, s);
-            else
-                iso::launch_mc_gen_tris<uint64_t>(g, ctx->d_cases, b, pl.cp, pl.gp, capM, capT, out->points,
-                                                  static_cast<uint64_t*>(out->tris), ctx->reverse, s);
-            pm.mark(ISO_PASS_MC_VERTICES);
-            if (iso::launch_mc_vertices(vol, g, iso, b, pl.gp, capM, capT, out->points, out->normals, s))
-                pm.mark(ISO_PASS_VERTICES);
-            if (i4)
-                iso::launch_mc_remap<uint32_t>(b, pl.gp, capM, capT, static_cast<uint32_t*>(out->tris), s);
-            else
-                iso::launch_mc_remap<uint64_t>(b, pl.gp, capM, capT, static_cast<uint64_t*>(out->tris), s);
-            pm.mark(ISO_PASS_MC_TRIANGLES);
-            return;
-        }
-        if (pl.gp.fits)
-            iso::launch_mc_gen_warps(vol, g, iso, ctx->d_cases, b, pl.cp, pl.gp, capM, capT, out->points, out->normals,
-                                     ctx->reverse, s);
-        else
-            iso::launch_mc_vertices_rows(vol, g, iso, ctx->d_cases, b, pl.cp, capM, capT, out->points, out->normals,
-                                         ctx->nsm, s);
-        pm.mark(ISO_PASS_MC_VERTICES);
-        if (pl.gp.fits && iso::launch_mc_vertices(vol, g, iso, b, pl.gp, capM, capT, out->points, out->normals, s))
-            pm.mark(ISO_PASS_VERTICES);
-        if (pl.gp.fits) {
-            if (i4)
-                iso::launch_mc_tri_warps<uint32_t>(g, ctx->d_cases, b, pl.cp, pl.gp, capM, capT,
-                                                   static_cast<uint32_t*>(out->tris), s);
-            else
-                iso::launch_mc_tri_warps<uint64_t>(g, ctx->d_cases, b, pl.cp, pl.gp, capM, capT,
-                                                   static_cast<uint64_t*>(out->tris), s);
-        } else {
-            if (i4)
-                iso::launch_mc_triangles<uint32_t>(g, ctx->d_cases, b, pl.cp, capM, capT,
-                                                   static_cast<uint32_t*>(out->tris), ctx->nsm, s);
-            else
-                iso::launch_mc_triangles<uint64_t>(g, ctx->d_cases, b, pl.cp, capM, capT,
-                                                   static_cast<uint64_t*>(out->tris), ctx->nsm, s);
-        }
-        pm.mark(ISO_PASS_MC_TRIANGLES);
-    }
-}
-
-iso_status finish_counts(iso_ctx* ctx, const iso_mesh* out, long long V, long long T, long long status, int64_t* nV,
-                         int64_t* nT)
-{
-    *nV = V;
-    *nT = T;
-    if (status != 0) {
-        ctx->last_error = "a device-side wait timed out";
-        return ISO_ERR_TIMEOUT;
-    }
-    if (out && out->index_bytes == 4 && V > 0xffffffffll) {
-        ctx->last_error = "more than 2^32-1 vertices: use 64-bit indices";
-        return ISO_ERR_OVERFLOW;
-    }
-    if (out && (V > out->cap_points || T > out->cap_tris)) {
-        ctx->last_error = "output buffers too small";
-        return ISO_ERR_CAPACITY;
-    }
-    return ISO_OK;
-}
 
 // ---------------------------------------------------------------------------
 // z-slabs [k0, k1) of a decomposition along z.  The window of a slab: the
@@ -873,329 +460,6 @@ iso_status extract_host_streamed(iso_ctx* ctx, iso_algorithm algo, const void* v
 }
 
 
-// ---------------------------------------------------------------------------
-// Batched extraction.  The requests are spread over L lanes (streams, each
-// with its own scratch and, for Marching Cubes, its own FE -> MC map), the
-// largest requests first, each to the lane with the fewest cells so far; a
-// lane runs its requests one after the other (count, scan, generate,
-// vertices), the lanes run side by side.  The whole batch is captured once
-// as a CUDA graph: its 8-counter block per request (totals, device status,
-// work counter) lives in the batch arena, so the counts stay on the device
-// and the generate kernels check the capacities there; one copy at the end
-// brings every request's counters back.
-// ---------------------------------------------------------------------------
-struct BatchItem {
-    Grid g;
-    Plans pl;
-    int lane = 0;
-};
-
-constexpr int kMaxLanes = 64;
-constexpr int kTuneLanes[] = {1, 2, 4, 8, 16, 32, 64};
-// work splits: a request's count and generate plans size their grids and work
-// items for nsm / share SMs (several lanes share the GPU)
-constexpr int kTuneShares[] = {1, 2, 4, 8};
-
-void replan(iso_ctx* ctx, std::vector<BatchItem>& items, const std::vector<int>& run, int share)
-{
-    const int nsm = std::max(1, ctx->nsm / std::max(1, share));
-    for (int r : run) items[r].pl = make_plans(ctx, items[r].g, nsm);
-}
-
-// Lane of every request with work and the arena layout: counters of all n
-// requests, then per lane its scratch and FE -> MC map.
-struct BatchLayout {
-    int lanes = 1;
-    std::vector<size_t> scratch_at, scratch_bytes, map_at;
-    size_t bytes = 0;
-};
-
-BatchLayout plan_batch(const iso_request* req, const iso_mesh* out, int64_t n, std::vector<BatchItem>& items,
-                       const std::vector<int>& run, int lanes)
-{
-    BatchLayout lay;
-    lay.lanes = lanes;
-    std::vector<int> order(run);
-    auto cells = [&](int r) { return (double)(items[r].g.nx - 1) * (items[r].g.ny - 1) * (items[r].g.nz - 1); };
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cells(a) > cells(b); });
-    std::vector<double> load(lanes, 0.0);
-    std::vector<size_t> scratch(lanes, 0), map(lanes, 0);
-    for (int r : order) {
-        const int l = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-        items[r].lane = l;
-        load[l] += cells(r);
-        scratch[l] = std::max(scratch[l], scratch_size(items[r].g, items[r].pl.cp));
-        if (out && req[r].algorithm == ISO_MARCHING_CUBES) {
-            const long long capV = vertex_limit(&out[r], out[r].cap_points);
-            const long long capM = capV < 0xffffffffll ? capV : 0xffffffffll;
-            map[l] = std::max(map[l], (size_t)(capM + 1024) * 4);
-        }
-    }
-    size_t at = align256((size_t)n * 8 * sizeof(unsigned long long));
-    for (int l = 0; l < lanes; ++l) {
-        lay.scratch_at.push_back(at);
-        lay.scratch_bytes.push_back(scratch[l]);
-        at += align256(scratch[l]);
-        lay.map_at.push_back(at);
-        at += align256(map[l]);
-    }
-    lay.bytes = at;
-    return lay;
-}
-
-// Captures and the batch buffers' allocations of all contexts take turns: a
-// free (which synchronises the device) in one thread would invalidate a
-// capture running in another.
-std::mutex g_batch_mutex;
-
-// Batch buffers (the caller holds g_batch_mutex).  Only this context's work on
-// s uses them: the graphs and the lanes join back into s.
-iso_status ensure_batch(iso_ctx* ctx, const BatchLayout& lay, int64_t n, cudaStream_t s)
-{
-    if (lay.bytes > ctx->batch_arena_bytes) {
-        ISO_CUDA(ctx, cudaStreamSynchronize(s));
-        cudaFree(ctx->batch_arena);
-        ctx->batch_arena = nullptr;
-        ctx->batch_arena_bytes = 0;
-        ISO_CUDA(ctx, cudaMalloc(&ctx->batch_arena, lay.bytes));
-        ctx->batch_arena_bytes = lay.bytes;
-    }
-    if ((size_t)n > ctx->h_batch_n) {
-        ISO_CUDA(ctx, cudaStreamSynchronize(s));
-        if (ctx->h_batch) cudaFreeHost(ctx->h_batch);
-        ctx->h_batch = nullptr;
-        ctx->h_batch_n = 0;
-        ISO_CUDA(ctx, cudaHostAlloc(&ctx->h_batch, (size_t)n * 8 * sizeof(unsigned long long), cudaHostAllocDefault));
-        ctx->h_batch_n = (size_t)n;
-    }
-    if (!ctx->s_capture) ISO_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->s_capture, cudaStreamNonBlocking));
-    for (cudaEvent_t* e : {&ctx->batch_fork, &ctx->batch_t0, &ctx->batch_t1})
-        if (!*e) ISO_CUDA(ctx, cudaEventCreateWithFlags(e, e == &ctx->batch_fork ? cudaEventDisableTiming : 0));
-    while ((int)ctx->lane_streams.size() < lay.lanes) {
-        cudaStream_t q;
-        cudaEvent_t e;
-        ISO_CUDA(ctx, cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking));
-        ctx->lane_streams.push_back(q);
-        ISO_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-        ctx->lane_join.push_back(e);
-    }
-    return ISO_OK;
-}
-
-// What a captured graph depends on: lanes, buffers, requests and meshes.
-std::vector<unsigned char> batch_key(const iso_ctx* ctx, int lanes, int share, const iso_request* req,
-                                     const iso_mesh* out, int64_t n)
-{
-    std::vector<unsigned char> k;
-    auto put = [&](const void* p, size_t len) {
-        const unsigned char* c = static_cast<const unsigned char*>(p);
-        k.insert(k.end(), c, c + len);
-    };
-    const unsigned char count_only = out ? 0 : 1;
-    put(&count_only, 1);
-    put(&lanes, sizeof lanes);
-    put(&share, sizeof share);
-    put(&ctx->reverse, sizeof ctx->reverse);
-    put(&ctx->batch_arena, sizeof ctx->batch_arena);
-    put(&ctx->h_batch, sizeof ctx->h_batch);
-    put(&n, sizeof n);
-    put(req, (size_t)n * sizeof(iso_request));
-    for (int64_t r = 0; out && r < n; ++r) {
-        put(&out[r].points, sizeof out[r].points);
-        put(&out[r].normals, sizeof out[r].normals);
-        put(&out[r].tris, sizeof out[r].tris);
-        put(&out[r].index_bytes, sizeof out[r].index_bytes);
-        put(&out[r].cap_points, sizeof out[r].cap_points);
-        put(&out[r].cap_tris, sizeof out[r].cap_tris);
-    }
-    return k;
-}
-
-// The batch's work from `origin`: fork to the lanes, each lane's requests in
-// turn, join, the counters' copy to the host; all on origin's side of the join.
-void enqueue_batch(iso_ctx* ctx, const iso_request* req, const iso_mesh* out, int64_t n, std::vector<BatchItem>& items,
-                   const std::vector<int>& run, const BatchLayout& lay, cudaStream_t origin)
-{
-    char* arena = static_cast<char*>(ctx->batch_arena);
-    unsigned long long* counters = reinterpret_cast<unsigned long long*>(arena);
-    const bool prof = ctx->profiling;
-    ctx->profiling = false;  // no timing events between the lanes' kernels
-    cudaEventRecord(ctx->batch_fork, origin);
-    for (int l = 0; l < lay.lanes; ++l) cudaStreamWaitEvent(ctx->lane_streams[l], ctx->batch_fork, 0);
-    for (int r : run) {
-        BatchItem& it = items[r];
-        cudaStream_t ls = ctx->lane_streams[it.lane];
-        FeBuffers b;
-        carve(arena + lay.scratch_at[it.lane], it.g, it.pl.cp, b);
-        b.totals = counters + 8 * r;
-        b.fe2mc = reinterpret_cast<uint32_t*>(arena + lay.map_at[it.lane]);
-        PassMarks pm(ctx, ls);
-        const iso_algorithm algo = static_cast<iso_algorithm>(req[r].algorithm);
-        enqueue_count(ctx, algo, req[r].volume, it.g, req[r].isoval, it.pl, b, ls, pm);
-        if (out) enqueue_generate(ctx, algo, req[r].volume, it.g, req[r].isoval, it.pl, b, &out[r], ls, pm);
-    }
-    for (int l = 0; l < lay.lanes; ++l) {
-        cudaEventRecord(ctx->lane_join[l], ctx->lane_streams[l]);
-        cudaStreamWaitEvent(origin, ctx->lane_join[l], 0);
-    }
-    cudaMemcpyAsync(ctx->h_batch, counters, (size_t)n * 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
-                    origin);
-    ctx->profiling = prof;
-}
-
-// Capture the batch on the lanes and make ctx->batch_exec run it (updating
-// the executable graph in place when the topology allows).  out == nullptr:
-// passes 1-3 only (iso_count_batch).
-iso_status capture_batch(iso_ctx* ctx, const iso_request* req, const iso_mesh* out, int64_t n,
-                         std::vector<BatchItem>& items, const std::vector<int>& run, const BatchLayout& lay)
-{
-    cudaStream_t sc = ctx->s_capture;
-    const int slot = out ? 0 : 1;
-    cudaGraphExec_t& exec = ctx->batch_exec[slot];
-    cudaGraph_t graph = nullptr;
-    cudaError_t e = cudaStreamBeginCapture(sc, cudaStreamCaptureModeRelaxed);
-    if (e == cudaSuccess) {
-        enqueue_batch(ctx, req, out, n, items, run, lay, sc);
-        e = cudaStreamEndCapture(sc, &graph);
-    }
-    if (e != cudaSuccess || !graph) {
-        cudaGetLastError();
-        if (graph) cudaGraphDestroy(graph);
-        ctx->batch_key[slot].clear();
-        ctx->last_error = std::string("capturing the batch failed: ") + cudaGetErrorString(e);
-        return ISO_ERR_CUDA;
-    }
-    if (exec) {
-        cudaGraphExecUpdateResultInfo info;
-        if (cudaGraphExecUpdate(exec, graph, &info) != cudaSuccess) {
-            cudaGetLastError();
-            cudaGraphExecDestroy(exec);
-            exec = nullptr;
-        }
-    }
-    if (!exec) e = cudaGraphInstantiate(&exec, graph, 0);
-    cudaGraphDestroy(graph);
-    if (e != cudaSuccess) {
-        exec = nullptr;
-        ctx->batch_key[slot].clear();
-        return cuda_fail(ctx, e, "cudaGraphInstantiate");
-    }
-    return ISO_OK;
-}
-
-// Prepare (lanes, buffers, graph) for `lanes` lanes; nothing runs.
-iso_status prepare_batch(iso_ctx* ctx, const iso_request* req, const iso_mesh* out, int64_t n,
-                         std::vector<BatchItem>& items, const std::vector<int>& run, int lanes, int share,
-                         cudaStream_t s)
-{
-    replan(ctx, items, run, share);
-    const BatchLayout lay = plan_batch(req, out, n, items, run, lanes);
-    std::lock_guard<std::mutex> lock(g_batch_mutex);
-    iso_status st = ensure_batch(ctx, lay, n, s);
-    if (st != ISO_OK) return st;
-    std::vector<unsigned char> key = batch_key(ctx, lanes, share, req, out, n);
-    const int slot = out ? 0 : 1;
-    if (ctx->batch_exec[slot] && key == ctx->batch_key[slot]) return ISO_OK;
-    st = capture_batch(ctx, req, out, n, items, run, lay);
-    if (st == ISO_OK) ctx->batch_key[slot].swap(key);
-    return st;
-}
-
-// Milliseconds of one run of the prepared batch (the best of two after one warm-up run).
-iso_status time_batch(iso_ctx* ctx, cudaGraphExec_t exec, cudaStream_t s, float& best)
-{
-    best = 1e30f;
-    for (int rep = 0; rep < 3; ++rep) {
-        ISO_CUDA(ctx, cudaEventRecord(ctx->batch_t0, s));
-        ISO_CUDA(ctx, cudaGraphLaunch(exec, s));
-        ISO_CUDA(ctx, cudaEventRecord(ctx->batch_t1, s));
-        ISO_CUDA(ctx, cudaEventSynchronize(ctx->batch_t1));
-        float ms = 0.f;
-        ISO_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->batch_t0, ctx->batch_t1));
-        if (rep > 0) best = std::min(best, ms);
-    }
-    return ISO_OK;
-}
-
-// iso_extract_device_async as a CUDA graph: the passes and the counters'
-// copy to result_host captured once, relaunched while the call's arguments,
-// the context's buffers and result_host stay the same (result_host must be
-// pinned: a pageable one takes the stream path).
-iso_status extract_graph(iso_ctx* ctx, iso_algorithm algo, const float* volume, const Grid& g, const iso_grid* grid,
-                         float isoval, const Plans& pl, FeBuffers& b, const iso_mesh* out, int64_t* result_host,
-                         cudaStream_t s)
-{
-    cudaPointerAttributes attr{};
-    if (cudaPointerGetAttributes(&attr, result_host) != cudaSuccess || attr.type != cudaMemoryTypeHost) {
-        cudaGetLastError();
-        PassMarks pm(ctx, s);
-        enqueue_count(ctx, algo, volume, g, isoval, pl, b, s, pm);
-        enqueue_generate(ctx, algo, volume, g, isoval, pl, b, out, s, pm);
-        ISO_CUDA(ctx, cudaGetLastError());
-        ISO_CUDA(ctx,
-                 cudaMemcpyAsync(result_host, b.totals, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
-        return ISO_OK;
-    }
-    std::vector<unsigned char> key;
-    auto put = [&](const void* p, size_t len) {
-        const unsigned char* c = static_cast<const unsigned char*>(p);
-        key.insert(key.end(), c, c + len);
-    };
-    put(&algo, sizeof algo);
-    put(&volume, sizeof volume);
-    put(grid, sizeof *grid);
-    put(&isoval, sizeof isoval);
-    put(&out->points, sizeof out->points);
-    put(&out->normals, sizeof out->normals);
-    put(&out->tris, sizeof out->tris);
-    put(&out->index_bytes, sizeof out->index_bytes);
-    put(&out->cap_points, sizeof out->cap_points);
-    put(&out->cap_tris, sizeof out->cap_tris);
-    put(&result_host, sizeof result_host);
-    put(&ctx->scratch, sizeof ctx->scratch);
-    put(&ctx->fe2mc, sizeof ctx->fe2mc);
-    put(&ctx->reverse, sizeof ctx->reverse);
-    if (!ctx->one_exec || key != ctx->one_key) {
-        std::lock_guard<std::mutex> lock(g_batch_mutex);
-        if (!ctx->s_capture) ISO_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->s_capture, cudaStreamNonBlocking));
-        cudaStream_t sc = ctx->s_capture;
-        cudaGraph_t graph = nullptr;
-        cudaError_t e = cudaStreamBeginCapture(sc, cudaStreamCaptureModeRelaxed);
-        if (e == cudaSuccess) {
-            PassMarks pm(ctx, sc);
-            enqueue_count(ctx, algo, volume, g, isoval, pl, b, sc, pm);
-            enqueue_generate(ctx, algo, volume, g, isoval, pl, b, out, sc, pm);
-            cudaMemcpyAsync(result_host, b.totals, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, sc);
-            e = cudaStreamEndCapture(sc, &graph);
-        }
-        if (e != cudaSuccess || !graph) {
-            cudaGetLastError();
-            if (graph) cudaGraphDestroy(graph);
-            ctx->one_key.clear();
-            ctx->last_error = std::string("capturing the extraction failed: ") + cudaGetErrorString(e);
-            return ISO_ERR_CUDA;
-        }
-        if (ctx->one_exec) {
-            cudaGraphExecUpdateResultInfo info;
-            if (cudaGraphExecUpdate(ctx->one_exec, graph, &info) != cudaSuccess) {
-                cudaGetLastError();
-                cudaGraphExecDestroy(ctx->one_exec);
-                ctx->one_exec = nullptr;
-            }
-        }
-        if (!ctx->one_exec) e = cudaGraphInstantiate(&ctx->one_exec, graph, 0);
-        cudaGraphDestroy(graph);
-        if (e != cudaSuccess) {
-            ctx->one_exec = nullptr;
-            ctx->one_key.clear();
-            return cuda_fail(ctx, e, "cudaGraphInstantiate");
-        }
-        ctx->one_key.swap(key);
-    }
-    ISO_CUDA(ctx, cudaGraphLaunch(ctx->one_exec, s));
-    return ISO_OK;
-}
-
 }  // namespace
 
 extern "C" {
@@ -1461,205 +725,6 @@ iso_status iso_extract_device_async(iso_ctx* ctx, iso_algorithm algo, const floa
     ISO_CUDA(ctx, cudaGetLastError());
     ISO_CUDA(ctx, cudaMemcpyAsync(result_host, b.totals, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
     return ISO_OK;
-}
-
-iso_status iso_ctx_set_graph(iso_ctx* ctx, int enable)
-{
-    if (!ctx) return ISO_ERR_INVALID_ARG;
-    ctx->one_graph = enable ? 1 : 0;
-    if (!enable && ctx->one_exec) {
-        cudaGraphExecDestroy(ctx->one_exec);
-        ctx->one_exec = nullptr;
-        ctx->one_key.clear();
-    }
-    return ISO_OK;
-}
-
-}  // extern "C"
-
-namespace {
-
-// iso_extract_batch (out != nullptr) and iso_count_batch (out == nullptr, the
-// counts into nV / nT): validate, tune the lanes if asked, run the graph.
-iso_status run_batch(iso_ctx* ctx, int64_t n, const iso_request* req, iso_mesh* out, int64_t* nV, int64_t* nT,
-                     iso_status* status, cudaStream_t s)
-{
-    ISO_CUDA(ctx, cudaSetDevice(ctx->device));
-    std::vector<iso_status> st((size_t)n, ISO_OK);
-    std::vector<BatchItem> items((size_t)n);
-    std::vector<int> run;  // requests with work
-    for (int64_t r = 0; r < n; ++r) {
-        if (out) {
-            if (check_mesh(&out[r]) != ISO_OK) {
-                st[r] = ISO_ERR_INVALID_ARG;
-                continue;
-            }
-            out[r].n_points = out[r].n_tris = 0;
-        } else {
-            nV[r] = nT[r] = 0;
-        }
-        Grid g;
-        if (!valid_algo(static_cast<iso_algorithm>(req[r].algorithm)) || !make_grid(&req[r].grid, g)) {
-            st[r] = ISO_ERR_INVALID_ARG;
-            continue;
-        }
-        if (empty_grid(g)) continue;
-        if (!req[r].volume) {
-            st[r] = ISO_ERR_INVALID_ARG;
-            continue;
-        }
-        items[r].g = g;
-        items[r].pl = make_plans(ctx, g);
-        if (out && req[r].algorithm == ISO_MC_DUPFREE && !items[r].pl.gp.fits) {
-            ctx->last_error = "the duplicate-free order needs rows of at most 1024 points";
-            st[r] = ISO_ERR_INVALID_ARG;
-            continue;
-        }
-        run.push_back((int)r);
-    }
-    iso_status rc = ISO_OK;
-    if (!run.empty() && !ctx->batch_graph) {  // the lanes launched directly, no graph
-        int lanes = ctx->batch_lanes > 0 ? ctx->batch_lanes : (ctx->batch_tuned > 0 ? ctx->batch_tuned : 8);
-        const int share = ctx->batch_share > 0 ? ctx->batch_share : std::max(1, ctx->batch_tuned_share);
-        lanes = std::min(lanes, std::max(1, (int)run.size()));
-        replan(ctx, items, run, share);
-        const BatchLayout lay = plan_batch(req, out, n, items, run, lanes);
-        {
-            std::lock_guard<std::mutex> lock(g_batch_mutex);
-            rc = ensure_batch(ctx, lay, n, s);
-        }
-        if (rc != ISO_OK) return rc;
-        enqueue_batch(ctx, req, out, n, items, run, lay, s);
-        ISO_CUDA(ctx, cudaGetLastError());
-        ISO_CUDA(ctx, cudaStreamSynchronize(s));
-    } else if (!run.empty()) {
-        int lanes = ctx->batch_lanes > 0 ? ctx->batch_lanes : ctx->batch_tuned;
-        int share = ctx->batch_share > 0 ? ctx->batch_share : ctx->batch_tuned_share;
-        if (lanes <= 0 || share <= 0) {  // autotuner: time the batch at each (lanes, split), keep the fastest
-            float best = 1e30f;
-            int best_l = 1, best_s = 1;
-            for (int L : kTuneLanes) {
-                if (lanes > 0 && L != lanes) continue;
-                if (L > 1 && L > (int)run.size()) break;
-                for (int S : kTuneShares) {
-                    if (share > 0 && S != share) continue;
-                    if (S > L) break;  // a request never has fewer SMs than nsm / lanes
-                    rc = prepare_batch(ctx, req, out, n, items, run, L, S, s);
-                    if (rc != ISO_OK) return rc;
-                    float ms;
-                    rc = time_batch(ctx, ctx->batch_exec[out ? 0 : 1], s, ms);
-                    if (rc != ISO_OK) return rc;
-                    if (ms < best) {
-                        best = ms;
-                        best_l = L;
-                        best_s = S;
-                    }
-                }
-            }
-            lanes = best_l;
-            share = best_s;
-            if (ctx->batch_lanes <= 0) ctx->batch_tuned = lanes;
-            if (ctx->batch_share <= 0) ctx->batch_tuned_share = share;
-        }
-        lanes = std::min(lanes, std::max(1, (int)run.size()));
-        rc = prepare_batch(ctx, req, out, n, items, run, lanes, share, s);
-        if (rc != ISO_OK) return rc;
-        ISO_CUDA(ctx, cudaGraphLaunch(ctx->batch_exec[out ? 0 : 1], s));
-        ISO_CUDA(ctx, cudaStreamSynchronize(s));
-    }
-    if (!run.empty()) {
-        for (int r : run) {
-            const unsigned long long* c = ctx->h_batch + 8 * (size_t)r;
-            if (out) {
-                st[r] = finish_counts(ctx, &out[r], (long long)c[0], (long long)c[1], (long long)c[3],
-                                      &out[r].n_points, &out[r].n_tris);
-            } else {
-                st[r] = finish_counts(ctx, nullptr, (long long)c[0], (long long)c[1], (long long)c[3], &nV[r], &nT[r]);
-            }
-        }
-    }
-    for (int64_t r = 0; r < n; ++r) {
-        if (status) status[r] = st[r];
-        if (rc == ISO_OK && st[r] != ISO_OK) rc = st[r];
-    }
-    return rc;
-}
-
-}  // namespace
-
-extern "C" {
-
-iso_status iso_extract_batch(iso_ctx* ctx, int64_t n, const iso_request* req, iso_mesh* out, iso_status* status,
-                             void* stream)
-{
-    if (!ctx || n < 0 || (n > 0 && (!req || !out))) return ISO_ERR_INVALID_ARG;
-    return run_batch(ctx, n, req, out, nullptr, nullptr, status, static_cast<cudaStream_t>(stream));
-}
-
-iso_status iso_count_batch(iso_ctx* ctx, int64_t n, const iso_request* req, int64_t* n_points, int64_t* n_tris,
-                           iso_status* status, void* stream)
-{
-    if (!ctx || n < 0 || (n > 0 && (!req || !n_points || !n_tris))) return ISO_ERR_INVALID_ARG;
-    return run_batch(ctx, n, req, nullptr, n_points, n_tris, status, static_cast<cudaStream_t>(stream));
-}
-
-iso_status iso_block_tris(iso_ctx* ctx, const float* volume, const iso_grid* grid, float isoval, int32_t* counts,
-                          void* stream)
-{
-    if (!ctx || !grid) return ISO_ERR_INVALID_ARG;
-    Grid g;
-    if (!make_grid(grid, g)) return ISO_ERR_INVALID_ARG;
-    if (empty_grid(g)) return ISO_OK;
-    if (!volume || !counts) return ISO_ERR_INVALID_ARG;
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    ISO_CUDA(ctx, cudaSetDevice(ctx->device));
-    const Plans pl = make_plans(ctx, g);
-    FeBuffers b;
-    iso_status st = ensure_scratch(ctx, g, pl.cp, b, s);
-    if (st != ISO_OK) return st;
-    iso::launch_count(volume, g, isoval, ctx->d_cases, false, pl.cp, b, s);  // bit rows of the whole grid
-    ISO_CUDA(ctx, cudaMemsetAsync(counts, 0, sizeof(int32_t) * (size_t)iso::block_count(g), s));
-    iso::launch_block_tris(g, b.bits, counts, s);
-    ISO_CUDA(ctx, cudaGetLastError());
-    return ISO_OK;
-}
-
-iso_status iso_batch_set_lanes(iso_ctx* ctx, int lanes)
-{
-    if (!ctx || lanes < 0 || lanes > kMaxLanes) return ISO_ERR_INVALID_ARG;
-    ctx->batch_lanes = lanes;
-    if (lanes == 0) {  // tune again on the next batch, the split too
-        ctx->batch_tuned = 0;
-        ctx->batch_tuned_share = 0;
-    }
-    return ISO_OK;
-}
-
-iso_status iso_batch_set_split(iso_ctx* ctx, int share)
-{
-    if (!ctx || share < 0 || share > 64) return ISO_ERR_INVALID_ARG;
-    ctx->batch_share = share;
-    if (share == 0) ctx->batch_tuned_share = 0;  // tune again on the next batch
-    return ISO_OK;
-}
-
-int iso_batch_split(const iso_ctx* ctx)
-{
-    if (!ctx) return 0;
-    return ctx->batch_share > 0 ? ctx->batch_share : ctx->batch_tuned_share;
-}
-
-iso_status iso_batch_set_graph(iso_ctx* ctx, int enable)
-{
-    if (!ctx) return ISO_ERR_INVALID_ARG;
-    ctx->batch_graph = enable ? 1 : 0;
-    return ISO_OK;
-}
-
-int iso_batch_lanes(const iso_ctx* ctx)
-{
-    if (!ctx) return 0;
-    return ctx->batch_lanes > 0 ? ctx->batch_lanes : ctx->batch_tuned;
 }
 
 iso_status iso_extract_device(iso_ctx* ctx, iso_algorithm algo, const float* volume, const iso_grid* grid,

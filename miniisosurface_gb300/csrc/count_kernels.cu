@@ -406,6 +406,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_count_tma(const float* __restri
             wb = row_word_shift(buf, lead + (h + 1) * g.nx, g.nx, lw, lane & 7, lw == LPR - 1, iso);
             wa = row_ok ? wa : 0u;
             wb = hasY ? wb : 0u;
+            // the plain stores of the last points (lanes 0-2) may lie where the next copies write:
+            // each writer orders them before the async proxy, not only the lane that issues the copy
+            fence_proxy_async();
         }
         __syncwarp();  // every lane has read the buffer before it is refilled
         return true;

@@ -445,30 +445,6 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsign
                  : "memory");
 }
 
-// L2 prefetch of [src, src + bytes) by the TMA engine; src 16-byte aligned,
-// bytes a multiple of 16.
-__device__ __forceinline__ void bulk_prefetch_l2(const void* src, unsigned bytes)
-{
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
-}
-
-// L2 prefetch of the 128-byte line holding p.
-__device__ __forceinline__ void prefetch_l2_line(const void* p)
-{
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
-}
-
-__device__ __forceinline__ void cp_async4(void* dst, const void* src)
-{
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
-}
-
-// Arrive on `bar` once all cp.async of this thread have landed.
-__device__ __forceinline__ void cp_async_arrive(uint64_t* bar)
-{
-    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity)
 {
     unsigned ok;
@@ -530,26 +506,6 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity)
     return false;
 #endif
 }
-
-// Copy of rows of a plane slab into shared memory: one bulk copy (TMA engine)
-// when 16-byte aligned, else cp.async by all `nthreads` threads of `tid`.
-// Completion is signalled on `bar`, which must expect 1 arrival (BULK) or
-// nthreads arrivals (cp.async).
-template <bool BULK>
-__device__ __forceinline__ void slab_copy(float* dst, const float* src, int nfl, uint64_t* bar, int tid, int nthreads)
-{
-    if (BULK) {
-        if (tid == 0) {
-            fence_proxy_async();
-            mbar_arrive_expect_tx(bar, (unsigned)nfl * 4u);
-            bulk_copy_g2s(dst, src, (unsigned)nfl * 4u, bar);
-        }
-    } else {
-        for (int q = tid; q < nfl; q += nthreads) cp_async4(dst + q, src + q);
-        cp_async_arrive(bar);
-    }
-}
-
 
 // First vertex (comp 0), triangle (1) or MC vertex (2) of grid row r =
 // k*ny + j, from the scanned starts[3][R].

@@ -1,5 +1,7 @@
 // Host-side declarations of the kernel launchers (internal to the library).
 #pragma once
+#include <mutex>
+#include <unordered_map>
 #include <cstddef>
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -55,11 +57,20 @@ size_t dtype_bytes(int dtype);
 void launch_to_float(const void* in, int dtype, float* out, long long n, int nsm, cudaStream_t s);
 
 // Opt a kernel into `dyn` bytes of dynamic shared memory (needed once the
-// dynamic plus static shared memory passes the 48 KB default).
+// dynamic plus static shared memory passes the 48 KB default).  The limit
+// belongs to the kernel, not to the calling thread, so it is only ever raised,
+// under a lock: a thread setting a smaller limit for its own launch must not
+// lower it under another thread's larger launch of the same kernel.
 template <typename K>
 inline void allow_smem(K kern, size_t dyn)
 {
-    if (dyn > 16 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    if (dyn <= 16 * 1024) return;
+    static std::mutex m;
+    static std::unordered_map<const void*, size_t> raised;
+    std::lock_guard<std::mutex> lock(m);
+    size_t& cur = raised[reinterpret_cast<const void*>(kern)];
+    if (dyn > cur && cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn) == cudaSuccess)
+        cur = dyn;
 }
 CountPlan count_plan(const Grid& g, int nsm);
 GenPlan gen_plan(const Grid& g, int nsm);

@@ -174,7 +174,10 @@ class Server:
                     done = time.perf_counter() - t0
                     redo = [i for i, c in zip(take[:k], codes) if c == _lib.ISO_ERR_CAPACITY]
                     if any(c not in (0, _lib.ISO_ERR_CAPACITY) for c in codes) or (redo and self.predictor is None):
-                        raise RuntimeError("batch request failed: %s" % codes)
+                        bad = [(i, requests[i][1:], sizes[q], (m.n_points, m.n_tris), c)
+                               for q, (i, m, c) in enumerate(zip(take[:k], meshes, codes)) if c != 0]
+                        raise RuntimeError("batch request failed (request, (volume, iso, algorithm), sized, "
+                                           "reported, status): %s" % bad)
                     if redo:  # predicted too small: back to the head of the queue with the exact sizes
                         with cond:
                             for i, m, c in reversed(list(zip(take[:k], meshes, codes))):
