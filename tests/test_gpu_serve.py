@@ -63,3 +63,48 @@ def test_served_equals_alone_and_plain(M):
     cells = [int(np.prod([d - 1 for d in volumes[vi][1]])) for _, vi, _, _ in reqs]
     s = serve.summary(served, cells)
     assert s["p99_ms"] >= s["p50_ms"] > 0
+
+
+def test_concurrent_contexts_agree(M):
+    """Two contexts on two host threads extract batches at once, meshes freed every round: the widths 70 and 57
+    run the same count kernel with different shared-memory sizes, so one thread's launch setting must never
+    affect the other's.  Every request's status and counts must equal count_device."""
+    import threading
+    import torch
+    vols = pool(M)
+    volumes = [(v, d) for v, d, _, _ in vols]
+    rng = np.random.default_rng(9)
+    reqs = []
+    for i in range(24):
+        vi = (0, 3)[i % 2]  # 70 and 57 points wide
+        algo = M.FLYING_EDGES if i % 4 < 3 else M.MARCHING_CUBES
+        reqs.append((vi, float(np.float32(rng.uniform(vols[vi][2], vols[vi][3]))), algo))
+    ref = [M.count_device(volumes[vi][0], volumes[vi][1], iso, algo) for vi, iso, algo in reqs]
+    bad, errors = [], []
+
+    def work(seed):
+        try:
+            ctx = M.Context(0)
+            M.set_batch_lanes(3, ctx)
+            M.set_batch_graph(False, ctx)
+            s = torch.cuda.Stream()
+            r = np.random.default_rng(seed)
+            for it in range(80):
+                pick = r.choice(len(reqs), int(r.integers(1, 7)), replace=False)
+                rs = [M.Request(volumes[reqs[i][0]][0], volumes[reqs[i][0]][1], reqs[i][1], reqs[i][2]) for i in pick]
+                with torch.cuda.stream(s):
+                    ms = [M.DeviceMesh(ref[i][0], ref[i][1], 4) for i in pick]
+                codes = M.Batch(rs, ms).run(ctx, s.cuda_stream)
+                for q, i in enumerate(pick):
+                    if codes[q] != 0 or (ms[q].n_points, ms[q].n_tris) != ref[i]:
+                        bad.append((seed, it, int(i), ref[i], (ms[q].n_points, ms[q].n_tris), codes[q]))
+        except Exception as e:  # noqa: BLE001 -- reported below
+            errors.append(repr(e))
+
+    threads = [threading.Thread(target=work, args=(k,)) for k in (1, 2)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors[:2]
+    assert not bad, bad[:4]
