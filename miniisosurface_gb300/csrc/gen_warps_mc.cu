@@ -51,9 +51,36 @@ void launch_mc_gen_tris(const Grid& g, const CaseTables* cases, const FeBuffers&
 }
 
 // tris[i] = fe2mc[tris[i]] for the 3 T indices (T from the totals); nothing
-// when the mesh did not fit.  VEC (tris 16-byte aligned): four indices per
-// thread and step, one 16-byte load and store around four independent
-// gathers; the last n % 4 one by one.
+// when the mesh did not fit.  VEC (tris 16-byte aligned): groups of four
+// indices (one 16-byte load and store each), kRemapUnroll groups per thread
+// and step, all loaded before any gather so that 4 * kRemapUnroll gathers are
+// in flight; the last n % 4 indices one by one.
+constexpr int kRemapUnroll = 4;
+
+template <typename IndexT>
+__device__ __forceinline__ void load4(const IndexT* tris, unsigned long long q, IndexT (&v)[4])
+{
+    if (sizeof(IndexT) == 4) {
+        const uint4 a = reinterpret_cast<const uint4*>(tris)[q];
+        v[0] = (IndexT)a.x, v[1] = (IndexT)a.y, v[2] = (IndexT)a.z, v[3] = (IndexT)a.w;
+    } else {
+        const ulonglong2 a = reinterpret_cast<const ulonglong2*>(tris)[2 * q];
+        const ulonglong2 b = reinterpret_cast<const ulonglong2*>(tris)[2 * q + 1];
+        v[0] = (IndexT)a.x, v[1] = (IndexT)a.y, v[2] = (IndexT)b.x, v[3] = (IndexT)b.y;
+    }
+}
+
+template <typename IndexT>
+__device__ __forceinline__ void store4(IndexT* tris, unsigned long long q, const uint32_t (&m)[4])
+{
+    if (sizeof(IndexT) == 4) {
+        reinterpret_cast<uint4*>(tris)[q] = make_uint4(m[0], m[1], m[2], m[3]);
+    } else {
+        reinterpret_cast<ulonglong2*>(tris)[2 * q] = make_ulonglong2(m[0], m[1]);
+        reinterpret_cast<ulonglong2*>(tris)[2 * q + 1] = make_ulonglong2(m[2], m[3]);
+    }
+}
+
 template <typename IndexT, bool VEC>
 __global__ void k_mc_remap(IndexT* __restrict__ tris, const uint32_t* __restrict__ fe2mc,
                            const unsigned long long* __restrict__ totals, long long capV, long long capT)
@@ -65,25 +92,21 @@ __global__ void k_mc_remap(IndexT* __restrict__ tris, const uint32_t* __restrict
     unsigned long long done = 0;
     if (VEC) {
         const unsigned long long n4 = n / 4;
-        for (unsigned long long q = t0; q < n4; q += stride) {
-            IndexT v[4];
-            if (sizeof(IndexT) == 4) {
-                const uint4 a = reinterpret_cast<const uint4*>(tris)[q];
-                v[0] = (IndexT)a.x, v[1] = (IndexT)a.y, v[2] = (IndexT)a.z, v[3] = (IndexT)a.w;
-            } else {
-                const ulonglong2 a = reinterpret_cast<const ulonglong2*>(tris)[2 * q];
-                const ulonglong2 b = reinterpret_cast<const ulonglong2*>(tris)[2 * q + 1];
-                v[0] = (IndexT)a.x, v[1] = (IndexT)a.y, v[2] = (IndexT)b.x, v[3] = (IndexT)b.y;
-            }
-            uint32_t m[4];
+        for (unsigned long long q0 = t0; q0 < n4; q0 += kRemapUnroll * stride) {
+            IndexT v[kRemapUnroll][4];
+            uint32_t m[kRemapUnroll][4];
 #pragma unroll
-            for (int c = 0; c < 4; ++c) m[c] = __ldg(fe2mc + (unsigned long long)v[c]);
-            if (sizeof(IndexT) == 4) {
-                reinterpret_cast<uint4*>(tris)[q] = make_uint4(m[0], m[1], m[2], m[3]);
-            } else {
-                reinterpret_cast<ulonglong2*>(tris)[2 * q] = make_ulonglong2(m[0], m[1]);
-                reinterpret_cast<ulonglong2*>(tris)[2 * q + 1] = make_ulonglong2(m[2], m[3]);
-            }
+            for (int u = 0; u < kRemapUnroll; ++u)
+                if (q0 + u * stride < n4) load4(tris, q0 + u * stride, v[u]);
+#pragma unroll
+            for (int u = 0; u < kRemapUnroll; ++u)
+                if (q0 + u * stride < n4) {
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) m[u][c] = __ldg(fe2mc + (unsigned long long)v[u][c]);
+                }
+#pragma unroll
+            for (int u = 0; u < kRemapUnroll; ++u)
+                if (q0 + u * stride < n4) store4(tris, q0 + u * stride, m[u]);
         }
         done = 4 * n4;
     }
@@ -95,8 +118,8 @@ template <typename IndexT>
 void launch_mc_remap(const FeBuffers& b, const GenPlan& p, long long capV, long long capT, IndexT* tris,
                      cudaStream_t s)
 {
-    const long long wave = (long long)p.nsm * 8;
-    const long long need = (3 * capT / 4 + kThreads - 1) / kThreads;
+    const long long wave = (long long)p.nsm * 4;  // one wave at 64 registers
+    const long long need = (3 * capT / (4 * kRemapUnroll) + kThreads - 1) / kThreads;
     const unsigned blocks = (unsigned)std::max(1ll, std::min(wave, need));
     if ((reinterpret_cast<uintptr_t>(tris) & 15) == 0)
         k_mc_remap<IndexT, true><<<blocks, kThreads, 0, s>>>(tris, b.fe2mc, b.totals, capV, capT);
