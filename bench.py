@@ -18,8 +18,10 @@ One step = one full extraction (passes 1-4) of the volume.
               count          4 N                 (volume read; passes 1+2 fused)
               fe_generate    12 T                (uint32 triangles; with `vertices`)
                              4 N + 24 V + 12 T   (volume read, points+normals, triangles; alone)
-              mc_vertices    0                   (vertex records, FE -> MC map; with `vertices`)
-              mc_triangles   12 T
+              mc_vertices    12 T                (rows of up to 16 words: also the triangles, FE ids)
+                             0                   (vertex records, FE -> MC map; wider rows)
+              mc_triangles   0                   (rows of up to 16 words: the triangles remapped in place)
+                             12 T                (wider rows: the triangles through the map)
               vertices       4 N + 24 V          (pass-4 volume read, points+normals)
             intermediates (bit rows, counts, vertex records, maps) count nothing;
   pass4     pass 4 as one unit: 4 N + 24 V + 12 T over the summed time of its
@@ -610,9 +612,13 @@ def main():
                           "us_per_launch": 1e3 * ms_pass[p] / n_pass[p] if n_pass[p] else None}
                for p in range(npass) if n_pass[p]}
         split = "vertices" in per  # pass 4 as generate (triangles, vertex records) + vertices
+        # Marching Cubes over rows of up to 16 words: the owned-vertex pass also writes the triangles (FE ids),
+        # and the mc_triangles pass remaps them in place (an intermediate rewrite)
+        mc_fused = split and (DIMS[0] + 31) // 32 <= 16
         alg_bytes = {"classify": 4 * N, "count": 4 * N, "scan": 0,
                      "fe_generate": 12 * T if split else 4 * N + 24 * V + 12 * T, "vertices": 4 * N + 24 * V,
-                     "mc_vertices": 0 if split else 4 * N + 24 * V, "mc_triangles": 12 * T}
+                     "mc_vertices": (12 * T if mc_fused else 0) if split else 4 * N + 24 * V,
+                     "mc_triangles": 0 if mc_fused else 12 * T}
         dom = max(per, key=lambda k: per[k]["ms_total"])
         dom_s = per[dom]["us_per_launch"] * 1e-6
         achieved = alg_bytes[dom] / dom_s / 1e9
