@@ -174,3 +174,37 @@ def test_one_shot_graph_mode(M):
                     same(as_np(got), w, "graph mode %s rep %d" % (r.dims, rep))
     finally:
         M.set_graph(False, ctx)
+
+
+def test_batch_edge_cases(M):
+    """Empty batches, an invalid request beside valid ones (only it fails), a mesh with a bad index width, and
+    the count-only batch against count_device."""
+    import ctypes as C
+    from miniisosurface_gb300 import _lib
+    lib = _lib.load()
+    ctx = M.Context(0)
+    assert M.extract_batch([], ctx=ctx) == []
+    assert lib.iso_extract_batch(ctx.handle, 0, None, None, None, None) == _lib.ISO_OK
+    assert lib.iso_extract_batch(ctx.handle, -1, None, None, None, None) == _lib.ISO_ERR_INVALID_ARG
+    assert lib.iso_count_batch(ctx.handle, 2, None, None, None, None, None) == _lib.ISO_ERR_INVALID_ARG
+    reqs, _ = mixed_requests(M)
+    rs = [r for r, _ in reqs][:4]
+    sizes = [M.count_device(r.volume, r.dims, r.isoval, r.algorithm) for r in rs]
+    meshes = [M.DeviceMesh(v, t, 4) for v, t in sizes]
+    b = M.Batch(rs, meshes)
+    b.req[1].algorithm = 7  # no such algorithm
+    b.out[2].index_bytes = 3  # no such index width
+    st = lib.iso_extract_batch(ctx.handle, len(rs), b.req, b.out, b.status, None)
+    codes = [b.status[i] for i in range(len(rs))]
+    assert st == _lib.ISO_ERR_INVALID_ARG
+    assert codes == [_lib.ISO_OK, _lib.ISO_ERR_INVALID_ARG, _lib.ISO_ERR_INVALID_ARG, _lib.ISO_OK]
+    for i in (0, 3):
+        assert (b.out[i].n_points, b.out[i].n_tris) == sizes[i]
+        meshes[i].n_points, meshes[i].n_tris = b.out[i].n_points, b.out[i].n_tris
+        same(as_np(meshes[i]), plain(M, rs[i], 4), "edge-case batch request %d" % i)
+    allr = [r for r, _ in reqs]
+    arr = (_lib.IsoRequest * len(allr))(*[r.descriptor() for r in allr])
+    nv, nt = (C.c_int64 * len(allr))(), (C.c_int64 * len(allr))()
+    assert lib.iso_count_batch(ctx.handle, len(allr), arr, nv, nt, None, None) == _lib.ISO_OK
+    for i, r in enumerate(allr):
+        assert (nv[i], nt[i]) == M.count_device(r.volume, r.dims, r.isoval, r.algorithm), r.dims
