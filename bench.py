@@ -42,8 +42,8 @@ One step = one full extraction (passes 1-4) of the volume.
             [64, 768] per axis (blobs / noise); requests (volume, isovalue in
             its [p5, p95], Flying Edges) arrive as a Poisson stream at 0.5,
             1 and 2 times the plain loop's saturated rate.  served = the
-            serving loop (two slots, continuous batching, exact-count
-            admission under a 120 GB budget); plain = one request at a time
+            serving loop (three slots, batches of up to 64, continuous
+            batching, exact-count admission under a 120 GB budget); plain = one request at a time
             (iso_count_device, allocate, iso_extract_device); served_predicted
             = the serving loop sizing meshes with the trained output-size
             network instead of the count batch (fallbacks counted).  p50/p99
@@ -359,8 +359,8 @@ def served_leg(M, dev, nreq, seed=4, npool=8):
     cells = [int(np.prod([d - 1 for d in pool[vi][1]])) for vi, _ in picks]
     reqs_at = lambda times: [(float(t), vi, iso, M.FLYING_EDGES) for t, (vi, iso) in zip(times, picks)]
     from miniisosurface_gb300 import predictor as P
-    server = serve.Server(volumes, slots=2, max_batch=32, budget_bytes=120 << 30, lanes=8, device=dev.index or 0)
-    server_p = serve.Server(volumes, slots=2, max_batch=32, budget_bytes=120 << 30, lanes=8, device=dev.index or 0,
+    server = serve.Server(volumes, slots=3, max_batch=64, budget_bytes=120 << 30, lanes=8, device=dev.index or 0)
+    server_p = serve.Server(volumes, slots=3, max_batch=64, budget_bytes=120 << 30, lanes=8, device=dev.index or 0,
                             predictor=P.Predictor.load(device=dev)) if P.WEIGHTS.exists() else None
     serve.run_plain(volumes, reqs_at(np.zeros(nreq))[:8], device=dev.index or 0)  # warm-up
     server.run(reqs_at(np.zeros(nreq))[:16])

@@ -54,6 +54,29 @@ def admit(sizes, in_use, budget, index_bytes=4):
     return count, total
 
 
+def carve_meshes(sizes, index_bytes, device):
+    """Meshes of exactly the given (n_points, n_tris) as views into three
+    allocations for the whole batch (not three per request).  Each mesh's
+    triangles start on a 16-byte boundary (segments of a multiple of 4 rows)."""
+    import torch
+    nv = [max(int(v), 1) for v, _ in sizes]
+    nt = [(max(int(t), 1) + 3) // 4 * 4 for _, t in sizes]
+    pts = torch.empty((sum(nv), 3), dtype=torch.float32, device=device)
+    nrm = torch.empty((sum(nv), 3), dtype=torch.float32, device=device)
+    tri = torch.empty((sum(nt), 3), dtype=torch.int32 if index_bytes == 4 else torch.int64, device=device)
+    out, ov, ot = [], 0, 0
+    for (v, t), a, b in zip(sizes, nv, nt):
+        m = DeviceMesh.__new__(DeviceMesh)
+        m.index_bytes = index_bytes
+        m.points, m.normals = pts[ov:ov + a], nrm[ov:ov + a]
+        m.tris = tri[ot:ot + max(int(t), 1)]
+        m.n_points = m.n_tris = 0
+        out.append(m)
+        ov += a
+        ot += b
+    return out
+
+
 def poisson_arrivals(n, rate, seed=0):
     """n arrival times (seconds from the first) of a Poisson process of `rate` per second."""
     rng = np.random.default_rng(seed)
@@ -168,8 +191,7 @@ class Server:
                         state["batches"] += 1
                         cond.notify_all()
                     with torch.cuda.stream(stream):
-                        meshes = [DeviceMesh(v, t, self.index_bytes, torch.device("cuda", self.device))
-                                  for v, t in sizes[:k]]
+                        meshes = carve_meshes(sizes[:k], self.index_bytes, torch.device("cuda", self.device))
                     codes = Batch(reqs[:k], meshes).run(ctx, stream.cuda_stream)
                     done = time.perf_counter() - t0
                     redo = [i for i, c in zip(take[:k], codes) if c == _lib.ISO_ERR_CAPACITY]
