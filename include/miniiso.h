@@ -218,7 +218,7 @@ iso_status iso_count_batch(iso_ctx* ctx, int64_t n, const iso_request* req, int6
  *                       isovalue, so computed once per resident volume.
  *   iso_block_tris      exact triangles of every block at isoval (the count
  *                       pass's bit rows, summed per block): the training
- *                       labels and the reference the predictor is judged by.
+ *                       labels, and what the predictor's error is measured against.
  *   iso_mlp_forward     the network (ISO_MLP_IN -> 64 -> 64 -> 1, ReLU,
  *                       float32, ISO_MLP_PARAMS parameters) on n samples:
  *                       inputs of sample i are (min - iso[i]) / (max - min),
