@@ -546,12 +546,12 @@ __global__ void __launch_bounds__(kThreads) k_count_wide(const float* __restrict
 // ---------------------------------------------------------------------------
 // Exclusive scans of the per-row counts (vertices = x+y+z cuts, triangles,
 // MC vertices) over the R = ny*nz rows, in two launches over segments of
-// kSeg rows (256 threads x 8):
+// kSeg rows (256 threads x 4):
 //   k_scan_partial  one CTA per segment: segment totals
 //   k_scan_final    one CTA per segment: offset of the segment + scan inside
 //                   it -> starts[3][R]; grand totals.
 // ---------------------------------------------------------------------------
-constexpr int kScanPer = 8;
+constexpr int kScanPer = 4;  // 4 rather than 8 rows per thread: twice the CTAs, 15.2 -> 12.9 us at 512^3
 constexpr int kSeg = kThreads * kScanPer;
 
 // Scan modes: the components scanned per row.
