@@ -395,15 +395,27 @@ class Batch:
         return codes
 
 
-def extract_batch(requests, meshes=None, index_bytes=4, ctx=None, stream=None):
+def extract_batch(requests, meshes=None, index_bytes=4, ctx=None, stream=None, predictor=None):
     """Batched extraction (iso_extract_batch): a list of Request in, a list
     of DeviceMesh out, each what extract_device gives for its request.
 
     Meshes too small for their request (or none given) come back with the
     sizes needed from the first batch run; they are re-allocated at exactly
-    that size and those requests run again as one more batch.
+    that size and those requests run again as one more batch.  With a
+    predictor (predictor.Predictor) and no meshes, the meshes are sized by the
+    output-size network first (one launch for the whole batch), so most
+    requests run once.
     """
     requests = list(requests)
+    if meshes is None and predictor is not None and requests:
+        from .predictor import block_stats
+        stats = {}
+        for r in requests:  # each distinct volume's block statistics once
+            key = (r.volume.data_ptr(), r.dims)
+            if key not in stats:
+                stats[key] = block_stats(r.volume, r.dims, stream)
+        caps = predictor.capacities([(stats[(r.volume.data_ptr(), r.dims)], r.isoval) for r in requests], stream)
+        meshes = [DeviceMesh(v, t, index_bytes, r.volume.device) for (v, t), r in zip(caps, requests)]
     if meshes is None:
         meshes = [DeviceMesh(0, 0, index_bytes, r.volume.device) for r in requests]
     meshes = list(meshes)

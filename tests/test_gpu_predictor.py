@@ -156,3 +156,21 @@ def test_fused_prediction_matches_per_block_forward(M, trained):
                           torch.full((int(act.sum()),), iso, dtype=torch.float32, device=st.device))
         want = float(torch.clamp(y, min=0).sum()) * P.LABEL_SCALE
         assert abs(g - want) <= 1e-4 * max(want, 1.0), (g, want)
+
+
+def test_extract_batch_sized_by_the_network(M, trained):
+    """extract_batch with a predictor: meshes sized by the network, the batch run once (fallbacks at their exact
+    sizes), every mesh equal to its plain extraction."""
+    P, pred, _ = trained
+    reqs = []
+    for i, (dims, kind, iso) in enumerate(CASES[:4]):
+        v = dev(volume(M, dims, kind, 60 + i))
+        for d_iso in (0.0, 0.05):
+            reqs.append(M.Request(v, dims, iso + d_iso, M.FLYING_EDGES if i % 2 == 0 else M.MARCHING_CUBES))
+    for p in (pred, P.Predictor(pred.params, margin_t=0.3, v_per_t=0.3, slack=0)):  # the second always falls back
+        got = M.extract_batch(reqs, predictor=p)
+        for r, m in zip(reqs, got):
+            alone = M.extract_device(r.volume, r.dims, r.isoval, r.algorithm)
+            assert (m.n_points, m.n_tris) == (alone.n_points, alone.n_tris)
+            assert bool((m.points[: m.n_points] == alone.points[: alone.n_points]).all())
+            assert bool((m.tris[: m.n_tris] == alone.tris[: alone.n_tris]).all())
