@@ -189,7 +189,7 @@ __global__ void __launch_bounds__(kThreads) k_count_warps(const float* __restric
         words_scalar<NW>(rowptr(kb, jy), g.nx, g.W, hasY, lane, iso, B);
     }
     for (int k = kb; k < ke; ++k) {
-        const bool hasZ = k + 1 < g.nz, cell = hasY && hasZ;
+        const bool hasZ = k + 1 < g.nz;
         if (VEC4) {
             words_vec4<U, NW>(pc, nq, lane, iso, Cw);
             words_vec4<U, NW>(pd, nq, lane, iso, Dw);
