@@ -167,11 +167,13 @@ class Predictor:
 
     def capacities(self, items, stream=None):
         """(cap_points, cap_tris) of each (stats, iso)."""
-        out = []
-        for t in self.predict(items, stream):
-            ct = int(math.ceil(t * self.margin_t)) + self.slack
-            out.append((int(math.ceil(ct * self.v_per_t)) + self.slack, ct))
-        return out
+        return [self.capacity(t) for t in self.predict(items, stream)]
+
+    def capacity(self, predicted_tris):
+        """(cap_points, cap_tris) for a predicted triangle count: triangles times
+        margin_t plus slack, vertices v_per_t times that plus slack."""
+        ct = int(math.ceil(max(predicted_tris, 0.0) * self.margin_t)) + self.slack
+        return int(math.ceil(ct * self.v_per_t)) + self.slack, ct
 
     def save(self, path=WEIGHTS):
         head = np.array([self.margin_t, self.v_per_t, self.slack], dtype=np.float32)

@@ -1,5 +1,8 @@
-"""Serving loop host logic on CPU: admission by output bytes, Poisson arrivals."""
+"""Serving loop host logic on CPU: admission by output bytes, Poisson arrivals,
+meshes carved from one allocation per batch, the output-size network's
+capacity rule."""
 import numpy as np
+import pytest
 
 from miniisosurface_gb300.serve import admit, mesh_bytes, poisson_arrivals
 
@@ -39,3 +42,33 @@ def test_poisson_arrivals():
     assert t[0] == 0.0 and np.all(np.diff(t) >= 0)
     assert abs(np.mean(np.diff(t)) - 1 / 500.0) < 0.05 / 500.0
     assert np.array_equal(t, poisson_arrivals(20000, 500.0, seed=3))
+
+
+def test_carve_meshes_views():
+    """A batch's meshes as views of three allocations: exact capacities, no overlap, each triangle segment on a
+    16-byte boundary (a multiple of 4 rows of 3 x 4 bytes), empty meshes still one row."""
+    torch = pytest.importorskip("torch")
+    from miniisosurface_gb300.serve import carve_meshes
+    sizes = [(10, 17), (0, 0), (5, 4), (123, 250), (1, 1)]
+    for ib in (4, 8):
+        ms = carve_meshes(sizes, ib, torch.device("cpu"))
+        base = ms[0].tris.data_ptr()
+        end_p = end_t = None
+        for (v, t), m in zip(sizes, ms):
+            assert m.points.shape == (max(v, 1), 3) and m.normals.shape == (max(v, 1), 3)
+            assert m.tris.shape == (max(t, 1), 3)
+            assert (m.tris.data_ptr() - base) % 16 == 0
+            if end_p is not None:
+                assert m.points.data_ptr() >= end_p and m.tris.data_ptr() >= end_t
+            end_p = m.points.data_ptr() + m.points.numel() * 4
+            end_t = m.tris.data_ptr() + m.tris.numel() * ib
+            d = m.descriptor()
+            assert (d.cap_points, d.cap_tris, d.index_bytes) == (max(v, 1), max(t, 1), ib)
+
+
+def test_predictor_capacity_rule():
+    from miniisosurface_gb300.predictor import Predictor
+    p = Predictor(None, margin_t=1.25, v_per_t=0.5, slack=64)
+    assert p.capacity(0.0) == (96, 64)
+    assert p.capacity(-3.0) == (96, 64)
+    assert p.capacity(1000.0) == (int(np.ceil(1314 * 0.5)) + 64, 1314)
