@@ -27,8 +27,18 @@ One step = one full extraction (passes 1-4) of the volume.
   pass4     pass 4 as one unit: 4 N + 24 V + 12 T over the summed time of its
             kernels (generate, vertices)
   pipeline  the whole extraction: B = 8 N + 24 V + 12 T over the step
-  cpu_baseline  the oracle port of the reference's OpenMP Flying Edges on
-            all host cores, full volume, repeated for a bounded time.
+  mc        the same volume through Marching Cubes (value, roofline,
+            pipeline, per-pass split), and whether its triangle sequence equals
+            the Flying Edges one corner for corner
+  cpu_baseline  the reference's OpenMP Flying Edges on all host cores, full
+            volume, repeated for a bounded time: the oracle port where the
+            reference's programs are not built on this host, with the port's
+            measured speed relative to each program (oracle/port_factors.json);
+            legs: the four reference CPU paths (flyingEdgesSerial,
+            flyingEdgesOpenMP, mcSerial, mcOpenMP), one full extraction each
+  parity    the timed FE and MC meshes against the oracle, bit for bit, and the
+            FE points and normals against the reference's formulas evaluated
+            in float64 (max absolute, relative and ulp error)
   batched   64 volumes with per-axis dimensions uniform in [32, 320] (half
             Gaussian blobs, half value noise), each with 1-4 isovalues uniform
             in its field's [5th, 95th] percentile: Flying Edges over all
@@ -49,7 +59,8 @@ One step = one full extraction (passes 1-4) of the volume.
             network instead of the count batch (fallbacks counted).  p50/p99
             latency and throughput of each; outputs compared at one rate.
 
---impl reference runs that CPU implementation alone, rank 0 only.
+--impl reference runs those CPU paths alone, rank 0 only, without loading the
+product library (the volume comes from the oracle's own generator).
 Under torchrun (N > 1) every rank extracts its own replica (no collective in
 the data path); value = all ranks' cells / the slowest rank's time.
 """
@@ -154,48 +165,154 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(vol, seconds):
-    """Oracle port of the reference OpenMP Flying Edges, all host cores."""
+def _oracle():
     sys.path.insert(0, str(ROOT / "tests"))
     import oracle_lib
-
-    cores = os.cpu_count() or 1
-    runs, total = 0, 0.0
-    while runs == 0 or total < seconds:
-        oracle_lib.fe(vol, ISO, nthreads=cores)
-        total += oracle_lib.fe_wall_seconds()
-        runs += 1
-        if runs >= 50:
-            break
-    per = total / runs
-    return {"value": cells() / per / 1e6, "unit": METRIC, "cores": cores, "kind": "port",
-            "sample": "full 512^3 volume, %d extraction(s), %.2f s each (oracle port of "
-                      "flyingEdges/openmp, %d OpenMP threads)" % (runs, per, cores)}
+    return oracle_lib
 
 
-def _ref_program_seconds(prog, vol, cores, steps, warmup):
-    """Extraction wall time per run of the reference's own OpenMP Flying Edges
-    program (compiled from the reference sources into oracle/_ref), from the
-    "Total Program WALL Time" line of its YAML report."""
+def oracle_volume():
+    """The bench volume from the oracle's own generator (oracle/volgen_oracle.c),
+    bit-identical to the product's: the CPU arm never loads the product library."""
+    return _oracle().generate_value_noise(DIMS, NOISE["octaves"], NOISE["period"], NOISE["seed"])
+
+
+def port_factors():
+    """Program seconds / port seconds per reference program, measured where the
+    reference's programs were built (oracle/measure_port.py)."""
+    p = ROOT / "oracle" / "port_factors.json"
+    return json.loads(p.read_text()) if p.exists() else None
+
+
+# The reference's four CPU extraction programs and the oracle port of each:
+# (program, port kind, threads: 1 or all host cores)
+CPU_LEGS = (("flyingEdgesSerial", "fe", 1), ("flyingEdgesOpenMP", "fe", 0), ("mcSerial", "mc", 1),
+            ("mcOpenMP", "mc_openmp", 0))
+
+
+def _port_run(kind, vol, threads, keep=False):
+    """One extraction by the oracle port; (seconds, mesh or None)."""
+    O = _oracle()
+    if kind == "fe":
+        m = O.fe(vol, ISO, nthreads=threads)
+        t = O.fe_wall_seconds()
+    elif kind == "mc":
+        m = O.mc(vol, ISO)
+        t = O.mc_wall_seconds()
+    else:
+        m = O.mc_openmp(vol, ISO, nthreads=threads)
+        t = O.mc_wall_seconds()
+    return t, (m if keep else None)
+
+
+def _ref_program_seconds(prog, vin, threads, runs):
+    """Extraction wall time per run of one of the reference's own programs
+    (compiled from the reference sources into oracle/_ref), from the "Total
+    Program WALL Time" line of its YAML report; best of `runs`."""
     import re
-    import subprocess
     import tempfile
 
-    sys.path.insert(0, str(ROOT / "tests"))
-    import oracle_lib
-
+    best = None
     with tempfile.TemporaryDirectory() as td:
-        vin, vout, ym = os.path.join(td, "in.vtk"), os.path.join(td, "out.vtk"), os.path.join(td, "run.yaml")
-        oracle_lib.write_structured_points(vin, vol)
-        env = dict(os.environ, OMP_NUM_THREADS=str(cores))
-        times = []
-        for i in range(warmup + steps):
-            subprocess.run([str(prog), "-i", vin, "-o", vout, "-v", repr(float(ISO)), "-y", ym], env=env,
+        ym = os.path.join(td, "run.yaml")
+        for _ in range(runs):
+            subprocess.run([str(ROOT / "oracle" / "_ref" / prog), "-i", vin, "-o", os.path.join(td, "out.vtk"), "-v",
+                            repr(float(ISO)), "-y", ym], env=dict(os.environ, OMP_NUM_THREADS=str(threads)),
                            capture_output=True, check=True)
             m = re.search(r"Total Program WALL Time \(seconds\):\s*([0-9.eE+-]+)", Path(ym).read_text())
-            if i >= warmup:
-                times.append(float(m.group(1)))
-        return sum(times)
+            t = float(m.group(1))
+            best = t if best is None else min(best, t)
+    return best
+
+
+def cpu_legs(vol, cores, runs=1, keep=()):
+    """The four reference CPU paths on the full volume: the reference's own
+    programs where oracle/_ref holds them (built from the reference sources
+    on this host), else the oracle port.  Best of `runs`; the port's meshes of
+    the kinds in `keep` are returned for the parity check."""
+    import tempfile
+
+    factors = port_factors()
+    legs, meshes = {}, {}
+    td = None
+    for prog, kind, thr in CPU_LEGS:
+        threads = thr or cores
+        exe = ROOT / "oracle" / "_ref" / prog
+        t = None
+        if exe.exists():
+            try:
+                if td is None:
+                    td = tempfile.TemporaryDirectory()
+                    _oracle().write_structured_points(os.path.join(td.name, "in.vtk"), vol)
+                t = _ref_program_seconds(prog, os.path.join(td.name, "in.vtk"), threads, runs)
+                leg = {"kind": "reference", "program": prog}
+            except (OSError, subprocess.CalledProcessError):
+                t = None
+        if t is None:
+            best = None
+            for r in range(runs):
+                tr, mesh = _port_run(kind, vol, threads, keep=(kind in keep and r == 0))
+                if mesh is not None:
+                    meshes[kind] = mesh
+                best = tr if best is None else min(best, tr)
+            t = best
+            leg = {"kind": "port", "program": prog,
+                   "port_of": {"fe": "flyingEdges/{serial,openmp}/FlyingEdgesAlgorithm.cpp",
+                               "mc": "marchingCubes/serial/main.cpp:42-192",
+                               "mc_openmp": "marchingCubes/openmp/main.cpp:44-296"}[kind]}
+            f = factors and factors.get("legs", {}).get(prog)
+            if f:
+                # the port's time scaled by program / port seconds as measured on the build host
+                leg["port_vs_program"] = {"program_s_over_port_s": f["factor"], "measured_on": factors["host"],
+                                          "volume": factors["volume"]}
+                leg["program_equivalent_Mcells_s"] = cells() / (t * f["factor"]) / 1e6
+        leg.update({"threads": threads, "seconds": t, "value": cells() / t / 1e6, "unit": METRIC, "runs": runs})
+        legs[prog] = leg
+    if td is not None:
+        td.cleanup()
+    return legs, meshes
+
+
+def cpu_baseline(vol, seconds, cores):
+    """The reference's OpenMP Flying Edges on all host cores (the port unless
+    the program is built here), repeated for a bounded time."""
+    legs, _ = cpu_legs(vol, cores, runs=1)
+    fe = legs["flyingEdgesOpenMP"]
+    runs, total = 1, fe["seconds"]
+    if fe["kind"] == "port":
+        while total < seconds and runs < 50:
+            total += _port_run("fe", vol, cores)[0]
+            runs += 1
+    per = total / runs
+    out = {"value": cells() / per / 1e6, "unit": METRIC, "cores": cores, "kind": fe["kind"],
+           "sample": "full 512^3 volume, %d extraction(s), %.3f s each (%s of flyingEdges/openmp, %d OpenMP threads)"
+                     % (runs, per, "oracle port" if fe["kind"] == "port" else "the program", cores),
+           "legs": legs}
+    if "program_equivalent_Mcells_s" in fe:
+        out["program_equivalent_value"] = cells() / (per * fe["port_vs_program"]["program_s_over_port_s"]) / 1e6
+    return out
+
+
+def parity_check(vol, fe_mesh, mc_mesh, cores):
+    """The GPU meshes of the timed workload against the oracle port, bit for
+    bit, and the FE points and normals against the float64 evaluation of the
+    reference's formulas."""
+    O = _oracle()
+    out = {}
+    for name, mesh, ref_fn in (("fe", fe_mesh, lambda: O.fe(vol, ISO, nthreads=cores)),
+                               ("mc", mc_mesh, lambda: O.mc(vol, ISO))):
+        if mesh is None:
+            continue
+        p, n, t = mesh
+        rp, rn, rt, eov = ref_fn()
+        same = (p.shape == rp.shape and t.shape == rt.shape and np.array_equal(t.astype(np.uint64), rt) and
+                np.array_equal(p.view(np.uint32), rp.view(np.uint32)) and
+                np.array_equal(n.view(np.uint32), rn.view(np.uint32)))
+        out[name] = {"vertices": int(p.shape[0]), "triangles": int(t.shape[0]), "identical_to_oracle": bool(same)}
+        if name == "fe":
+            out[name]["fp64_error"] = O.fp64_error(vol, ISO, p, n, eov)
+        del rp, rn, rt, eov
+    return out
 
 
 def link_rates(dev, nbytes=256 << 20, reps=3):
@@ -407,43 +524,55 @@ def served_leg(M, dev, nreq, seed=4, npool=8):
 
 
 def run_reference(args, rank):
+    """The reference's CPU Flying Edges (OpenMP, all host cores) on the bench
+    volume, K timed steps; plus the serial and Marching Cubes programs once
+    each.  Only the oracle side runs here (its generator, its port, or the
+    reference's programs where oracle/_ref holds them): the product library
+    is never loaded."""
     if rank != 0:
         return
-    import miniisosurface_gb300 as M
-
-    sys.path.insert(0, str(ROOT / "tests"))
-    import oracle_lib
-
-    vol = M.generate_value_noise(DIMS, **NOISE)
+    vol = oracle_volume()
     cores = os.cpu_count() or 1
-    prog = ROOT / "oracle" / "_ref" / "flyingEdgesOpenMP"
-    t = None
-    if prog.exists():
-        try:
-            t = _ref_program_seconds(prog, vol, cores, args.steps, args.warmup)
-            kind, sample = "reference", ("full 512^3 volume per step, %d steps (the reference's flyingEdgesOpenMP "
-                                         "compiled from its sources, %d OpenMP threads, its own extraction wall "
-                                         "time)" % (args.steps, cores))
-        except (OSError, subprocess.CalledProcessError):
-            t = None
-    if t is None:
+    legs, _ = cpu_legs(vol, cores, runs=1)
+    fe = legs["flyingEdgesOpenMP"]
+    kind = fe["kind"]
+    if kind == "reference":
+        import tempfile
+        with tempfile.TemporaryDirectory() as td:
+            vin = os.path.join(td, "in.vtk")
+            _oracle().write_structured_points(vin, vol)
+            _ref_program_seconds(fe["program"], vin, cores, max(args.warmup, 1))
+            t = sum(_ref_program_seconds(fe["program"], vin, cores, 1) for _ in range(args.steps))
+        sample = ("full 512^3 volume per step, %d steps (the reference's flyingEdgesOpenMP compiled from its "
+                  "sources, %d OpenMP threads, its own extraction wall time)" % (args.steps, cores))
+    else:
         for _ in range(args.warmup):
-            oracle_lib.fe(vol, ISO, nthreads=cores)
-        t = 0.0
-        for _ in range(args.steps):
-            oracle_lib.fe(vol, ISO, nthreads=cores)
-            t += oracle_lib.fe_wall_seconds()
-        kind, sample = "port", ("full 512^3 volume per step, %d steps (oracle port of flyingEdges/openmp, %d OpenMP "
-                                "threads; the reference's own programs are not built on this host)"
-                                % (args.steps, cores))
+            _port_run("fe", vol, cores)
+        t = sum(_port_run("fe", vol, cores)[0] for _ in range(args.steps))
+        sample = ("full 512^3 volume per step, %d steps (oracle port of flyingEdges/openmp, %d OpenMP threads; the "
+                  "reference's programs are not built on this host)" % (args.steps, cores))
     value = cells() * args.steps / t / 1e6
+    cpu = {"value": value, "unit": METRIC, "cores": cores, "kind": kind, "sample": sample, "legs": legs,
+           "cpu_model": _cpu_model()}
+    if "port_vs_program" in fe:
+        cpu["program_equivalent_value"] = value / fe["port_vs_program"]["program_s_over_port_s"]
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": workload_config("fe"), "impl": "reference",
-            "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": kind, "sample": sample},
+            "config": workload_config("fe"), "impl": "reference", "cpu_baseline": cpu,
             "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def _cpu_model():
+    try:
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            if line.lower().startswith(("model name", "cpu model")):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.machine()
 
 
 def main():
@@ -477,68 +606,114 @@ def main():
     dvol = pinned.to(dev)
     ctx = M.Context(local)
     grid = M.make_grid(DIMS)
-    V, T = M.count_device(dvol, DIMS, ISO, algo, ctx=ctx)
-    out = M.DeviceMesh(V, T, 4, dev)
-    desc = out.descriptor()
-    res = torch.zeros(4, dtype=torch.int64).pin_memory()
     stream = torch.cuda.current_stream(dev)
     sh = C.c_void_p(stream.cuda_stream)
-
-    def step():
-        st = lib.iso_extract_device_async(ctx.handle, algo, dvol.data_ptr(), C.byref(grid), C.c_float(ISO),
-                                          C.byref(desc), C.c_void_p(res.data_ptr()), sh)
-        if st != 0:
-            _lib.check(st, ctx.handle)
-
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
-    assert int(res[0]) == V and int(res[1]) == T
-
-    # value: K steps of the device entry point in graph mode (the first call captures the
-    # passes, the steps relaunch the graph), no events between kernels
-    lib.iso_ctx_set_graph(ctx.handle, 1)
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
-    assert int(res[0]) == V and int(res[1]) == T
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.3)
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    t_wall = time.perf_counter()
-    e0.record(stream)
-    for _ in range(args.steps):
-        step()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    t_wall = time.perf_counter() - t_wall
-    if dist:
-        dist.barrier()
-    ms = e0.elapsed_time(e1)
-    lib.iso_ctx_set_graph(ctx.handle, 0)
 
-    # per-kernel attribution: K more steps on the stream path with CUDA events between the
-    # kernels (iso_ctx_profile), timed the same way
-    lib.iso_ctx_profile(ctx.handle, 1)
-    torch.cuda.synchronize()
-    p0 = torch.cuda.Event(enable_timing=True)
-    p1 = torch.cuda.Event(enable_timing=True)
-    p0.record(stream)
-    for _ in range(args.steps):
-        step()
-    p1.record(stream)
-    torch.cuda.synchronize()
-    lib.iso_ctx_profile(ctx.handle, 0)
-    ms_prof = p0.elapsed_time(p1)
-    npass = len(_lib.PASS_NAMES)
-    ms_pass = (C.c_double * npass)()
-    n_pass = (C.c_int64 * npass)()
-    _lib.check(lib.iso_ctx_profile_read(ctx.handle, ms_pass, n_pass), ctx.handle)
+    def device_run(a, barrier):
+        """K extractions of the resident volume through iso_extract_device_async in graph mode (the first
+        call captures the passes, the steps relaunch the graph), then K more on the stream path with CUDA
+        events between the kernels (iso_ctx_profile) for the per-pass split.  Returns the timings and the
+        mesh of the last step."""
+        V, T = M.count_device(dvol, DIMS, ISO, a, ctx=ctx)
+        out = M.DeviceMesh(V, T, 4, dev)
+        desc = out.descriptor()
+        res = torch.zeros(4, dtype=torch.int64).pin_memory()
+
+        def step():
+            st = lib.iso_extract_device_async(ctx.handle, a, dvol.data_ptr(), C.byref(grid), C.c_float(ISO),
+                                              C.byref(desc), C.c_void_p(res.data_ptr()), sh)
+            if st != 0:
+                _lib.check(st, ctx.handle)
+
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        assert int(res[0]) == V and int(res[1]) == T
+        lib.iso_ctx_set_graph(ctx.handle, 1)
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        assert int(res[0]) == V and int(res[1]) == T
+        if barrier and dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if barrier and dist:
+            dist.barrier()
+        ms = e0.elapsed_time(e1)
+        lib.iso_ctx_set_graph(ctx.handle, 0)
+        lib.iso_ctx_profile(ctx.handle, 1)
+        torch.cuda.synchronize()
+        p0 = torch.cuda.Event(enable_timing=True)
+        p1 = torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
+        for _ in range(args.steps):
+            step()
+        p1.record(stream)
+        torch.cuda.synchronize()
+        lib.iso_ctx_profile(ctx.handle, 0)
+        npass = len(_lib.PASS_NAMES)
+        ms_pass = (C.c_double * npass)()
+        n_pass = (C.c_int64 * npass)()
+        _lib.check(lib.iso_ctx_profile_read(ctx.handle, ms_pass, n_pass), ctx.handle)
+        names = _lib.PASS_NAMES
+        per = {names[q]: {"ms_total": ms_pass[q], "launches": int(n_pass[q]),
+                          "us_per_launch": 1e3 * ms_pass[q] / n_pass[q] if n_pass[q] else None}
+               for q in range(npass) if n_pass[q]}
+        # count + scan + row starts + generate per step (scan and row starts share one mark)
+        launches = int(sum(n_pass[q] for q in range(npass)) + n_pass[2])
+        return {"V": V, "T": T, "ms": ms, "ms_prof": p0.elapsed_time(p1), "per": per,
+                "launches": launches}, out
+
+    def roofline_of(r, peak, peak_kind):
+        """The dominant kernel of a device_run: algorithmic bytes per launch over its mean event time."""
+        V, T, per = r["V"], r["T"], r["per"]
+        split = "vertices" in per  # pass 4 as generate (triangles, vertex records) + vertices
+        # Marching Cubes over rows of up to 16 words: the owned-vertex pass also writes the triangles (FE ids),
+        # and the mc_triangles pass remaps them in place (an intermediate rewrite)
+        mc_fused = split and (DIMS[0] + 31) // 32 <= 16
+        alg_bytes = {"classify": 4 * N, "count": 4 * N, "scan": 0,
+                     "fe_generate": 12 * T if split else 4 * N + 24 * V + 12 * T, "vertices": 4 * N + 24 * V,
+                     "mc_vertices": (12 * T if mc_fused else 0) if split else 4 * N + 24 * V,
+                     "mc_triangles": 0 if mc_fused else 12 * T}
+        dom = max(per, key=lambda k: per[k]["ms_total"])
+        dom_s = per[dom]["us_per_launch"] * 1e-6
+        achieved = alg_bytes[dom] / dom_s / 1e9
+        traffic_path = ROOT / "profiles" / "traffic.json"
+        traffic = None
+        if traffic_path.exists():
+            traffic = json.loads(traffic_path.read_text()).get(dom)
+        p4 = [k for k in ("fe_generate", "mc_vertices", "mc_triangles", "vertices") if k in per]
+        p4_s = sum(per[k]["us_per_launch"] for k in p4) * 1e-6
+        p4_bytes = 4 * N + 24 * V + 12 * T
+        B = 8 * N + 24 * V + 12 * T
+        step_s = r["ms"] / args.steps / 1e3
+        prof_ms = sum(v["ms_total"] for v in per.values())
+        return ({"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                 "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+                 "traffic_source": ("profiles/traffic.json: dram__bytes_read.sum + dram__bytes_write.sum of one "
+                                    "ncu capture of this kernel on this workload (not measured in this run)"),
+                 "algorithmic_bytes_per_launch": alg_bytes[dom]},
+                {"bytes_per_step": B, "achieved_GBps": B / step_s / 1e9, "frac": B / step_s / 1e9 / peak,
+                 "per_pass": per, "profiled_ms_per_step": r["ms_prof"] / args.steps,
+                 "event_overhead_ms_per_step": (r["ms_prof"] - prof_ms) / args.steps},
+                {"passes": p4, "algorithmic_bytes": p4_bytes, "us": 1e6 * p4_s, "achieved_GBps": p4_bytes / p4_s / 1e9,
+                 "frac": p4_bytes / p4_s / 1e9 / peak})
+
+    run, out = device_run(algo, True)
+    V, T, ms = run["V"], run["T"], run["ms"]
+    # the other algorithm on the same volume (config 1 names Flying Edges and Marching Cubes)
+    other = M.MARCHING_CUBES if algo == M.FLYING_EDGES else M.FLYING_EDGES
+    run2, out2 = device_run(other, False)
 
     # e2e: host volume in, host mesh out, every step
     h_pts = torch.empty((V, 3), dtype=torch.float32).pin_memory()
@@ -606,47 +781,18 @@ def main():
         value = C_cells * args.steps * world / (ms / 1e3) / 1e6
         e2e_value = C_cells * args.e2e_steps * world / e2e_s / 1e6
         peak, peak_kind = hbm_peak()
-        B_total = 8 * N + 24 * V + 12 * T
-        names = _lib.PASS_NAMES
-        per = {names[p]: {"ms_total": ms_pass[p], "launches": int(n_pass[p]),
-                          "us_per_launch": 1e3 * ms_pass[p] / n_pass[p] if n_pass[p] else None}
-               for p in range(npass) if n_pass[p]}
-        split = "vertices" in per  # pass 4 as generate (triangles, vertex records) + vertices
-        # Marching Cubes over rows of up to 16 words: the owned-vertex pass also writes the triangles (FE ids),
-        # and the mc_triangles pass remaps them in place (an intermediate rewrite)
-        mc_fused = split and (DIMS[0] + 31) // 32 <= 16
-        alg_bytes = {"classify": 4 * N, "count": 4 * N, "scan": 0,
-                     "fe_generate": 12 * T if split else 4 * N + 24 * V + 12 * T, "vertices": 4 * N + 24 * V,
-                     "mc_vertices": (12 * T if mc_fused else 0) if split else 4 * N + 24 * V,
-                     "mc_triangles": 0 if mc_fused else 12 * T}
-        dom = max(per, key=lambda k: per[k]["ms_total"])
-        dom_s = per[dom]["us_per_launch"] * 1e-6
-        achieved = alg_bytes[dom] / dom_s / 1e9
-        prof_ms = sum(v["ms_total"] for v in per.values())
-        # pass 4 as one unit (the reference's pass: volume read, vertices, triangles), over the summed
-        # time of the kernels that make it up
-        p4 = [k for k in ("fe_generate", "mc_vertices", "mc_triangles", "vertices") if k in per]
-        p4_s = sum(per[k]["us_per_launch"] for k in p4) * 1e-6
-        p4_bytes = 4 * N + 24 * V + 12 * T
-        traffic_path = ROOT / "profiles" / "traffic.json"
-        traffic = None
-        if traffic_path.exists():
-            traffic = json.loads(traffic_path.read_text()).get(dom)
+        roof, pipe, p4 = roofline_of(run, peak, peak_kind)
+        roof2, pipe2, p42 = roofline_of(run2, peak, peak_kind)
+        # both algorithms emit the same triangle sequence (same corner points, bit for bit)
+        same_tris = (run["T"] == run2["T"] and bool(torch.equal(
+            out.points[out.tris[: run["T"]].long()], out2.points[out2.tris[: run2["T"]].long()])))
         line = {
             "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": workload_config(args.algorithm),
             "mesh": {"vertices": V, "triangles": T, "cells": C_cells},
-            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
-                         "algorithmic_bytes_per_launch": alg_bytes[dom]},
-            "pipeline": {"bytes_per_step": B_total, "achieved_GBps": B_total / (ms / args.steps / 1e3) / 1e9,
-                         "frac": B_total / (ms / args.steps / 1e3) / 1e9 / peak,
-                         "per_pass": per, "profiled_ms_per_step": ms_prof / args.steps,
-                         "event_overhead_ms_per_step": (ms_prof - prof_ms) / args.steps},
-            "pass4": {"passes": p4, "algorithmic_bytes": p4_bytes, "us": 1e6 * p4_s,
-                      "achieved_GBps": p4_bytes / p4_s / 1e9, "frac": p4_bytes / p4_s / 1e9 / peak},
+            "roofline": roof, "pipeline": pipe, "pass4": p4,
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": 4 * N,
                     "d2h_bytes_per_step": 24 * V + 12 * T, "ms_per_step": 1e3 * e2e_s / args.e2e_steps,
                     "link": link_floor(rates, 4 * N, 24 * V + 12 * T, 1e3 * e2e_s / args.e2e_steps)},
@@ -655,16 +801,28 @@ def main():
                           "h2d_bytes_per_step": 2 * N, "d2h_bytes_per_step": 24 * V16 + 12 * T16,
                           "ms_per_step": 1e3 * e2e16_s / args.e2e_steps,
                           "link": link_floor(rates, 2 * N, 24 * V16 + 12 * T16, 1e3 * e2e16_s / args.e2e_steps)},
-            # count + scan + row starts + generate per step (scan/row starts share one mark)
-            "gpu_launches": int(sum(n_pass[p] for p in range(npass)) + n_pass[2]),
+            "gpu_launches": run["launches"],
             "clocks": clk,
         }
+        line["mc" if other == M.MARCHING_CUBES else "fe"] = {
+            "workload": workload_config("mc" if other == M.MARCHING_CUBES else "fe")["workload"],
+            "value": C_cells * args.steps / (run2["ms"] / 1e3) / 1e6, "unit": METRIC,
+            "ms_per_step": run2["ms"] / args.steps, "mesh": {"vertices": run2["V"], "triangles": run2["T"]},
+            "roofline": roof2, "pipeline": pipe2, "pass4": p42, "gpu_launches": run2["launches"],
+            "same_triangle_sequence_as_" + args.algorithm: same_tris}
         if not args.no_batched:
             line["batched"] = batched_leg(M, lib, dev, args.batched_reps)
         if not args.no_served:
             line["served"] = served_leg(M, dev, args.served_requests)
         if not args.no_cpu_baseline:
-            line["cpu_baseline"] = cpu_baseline(vol_host, args.cpu_seconds)
+            cores = os.cpu_count() or 1
+            line["cpu_baseline"] = cpu_baseline(vol_host, args.cpu_seconds, cores)
+            line["cpu_baseline"]["cpu_model"] = _cpu_model()
+            fe_out, mc_out = (out, out2) if algo == M.FLYING_EDGES else (out2, out)
+            fe_r, mc_r = (run, run2) if algo == M.FLYING_EDGES else (run2, run)
+            host = lambda m, r: (m.points[: r["V"]].cpu().numpy(), m.normals[: r["V"]].cpu().numpy(),
+                                 m.tris[: r["T"]].cpu().numpy().astype(np.uint64))
+            line["parity"] = parity_check(vol_host, host(fe_out, fe_r), host(mc_out, mc_r), cores)
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

@@ -130,16 +130,21 @@ iso_status iso_count_device(iso_ctx* ctx, iso_algorithm algo, const float* volum
  * iso_count_device returns, for callers that must not allocate device memory
  * while they size a mesh (a solver that reserved the device for its own
  * pool, an allocator sizing a mesh before carving it from its arena, loops
- * that a device-wide cudaFree would stall).  No context: all scratch is a
- * fixed 16 MiB device array reserved when the library's module loads, so
- * grids of more than ISO_NOALLOC_MAX_ROWS rows (ny * nz) are rejected with
- * ISO_ERR_TOO_LARGE.  Runs on the calling thread's current device; volume
- * and counts are device pointers on it.  Enqueues the count on `stream` and
+ * that a device-wide cudaFree would stall).  No context: all scratch is one
+ * fixed 16 MiB device array, which a device holds from the time the
+ * library's module for this call loads until the process exits.  CUDA loads
+ * modules lazily by default, so the first call on a device loads it: make
+ * that call (a one-point grid will do) before reserving the device's memory,
+ * and before any stream capture.  Grids of more than ISO_NOALLOC_MAX_ROWS
+ * rows (ny * nz), or with rows of more than ISO_NOALLOC_MAX_ROW_POINTS
+ * points, are rejected with ISO_ERR_TOO_LARGE before anything is enqueued.
+ * ISO_MC_DUPFREE gives the ISO_MARCHING_CUBES counts (the same vertices in
+ * another order).  Runs on the calling thread's current device; volume and
+ * counts are device pointers on it.  Enqueues the count on `stream` and
  * returns: counts[0] = vertices, counts[1] = triangles once the stream gets
- * there.  The first call on a device does a one-time set-up (symbol lookup
- * and a synchronous copy of the case tables), so make it before any stream
- * capture.  Calls on one device must not overlap (other streams or host
- * threads): they share the scratch. */
+ * there.  Nothing is cached between calls.  Calls on one device must not
+ * overlap (other streams or host threads): they share the scratch. */
+#define ISO_NOALLOC_MAX_ROW_POINTS 858993459
 #define ISO_NOALLOC_MAX_ROWS (1 << 20)
 iso_status iso_count_device_noalloc(iso_algorithm algo, const float* volume, const iso_grid* grid, float isoval,
                                     int64_t* counts, void* stream);

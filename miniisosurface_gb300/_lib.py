@@ -20,6 +20,7 @@ ISO_ERR_FORMAT = 8
 ISO_ERR_STATE = 9
 ISO_ERR_TOO_LARGE = 10
 ISO_NOALLOC_MAX_ROWS = 1 << 20
+ISO_NOALLOC_MAX_ROW_POINTS = 858993459
 
 PASS_NAMES = ("classify", "count", "scan", "fe_generate", "mc_vertices", "mc_triangles", "vertices")
 

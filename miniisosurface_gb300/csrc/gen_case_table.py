@@ -17,6 +17,7 @@ they are derived from this word and the cube edge numbering (see
 Usage: python gen_case_table.py <path to MarchingCubesTables.h> [out.h]
 """
 import re
+import os
 import sys
 from pathlib import Path
 
@@ -91,8 +92,8 @@ static inline ISO_HD int iso_case_edge(uint64_t w, int t) { return (int)((w >> (
 
 
 def main():
-    src = Path(sys.argv[1] if len(sys.argv) > 1 else
-               "/root/reference/flyingEdges/util/MarchingCubesTables.h")
+    ref = Path(os.environ.get("MINIISO_REFERENCE", "/root/reference"))
+    src = Path(sys.argv[1]) if len(sys.argv) > 1 else ref / "flyingEdges" / "util" / "MarchingCubesTables.h"
     out = Path(sys.argv[2]) if len(sys.argv) > 2 else Path(__file__).with_name("case_table.h")
     cases = parse_case_triangles(src.read_text())
     out.write_text(HEADER % render(cases))

@@ -10,25 +10,33 @@
 //     from its own arena, which cannot re-enter a general allocator;
 //   * latency-bound loops sharing the device with other streams, where a
 //     cudaFree (which synchronises the whole device) would stall them.
-// It needs no context either: every byte it uses is a file-scope device
-// array, reserved when the module loads.
+// It needs no context either: every byte it uses is one file-scope device
+// array, which the device holds from the time this file's module loads until
+// the process exits.  With CUDA's lazy module loading (the default) the module
+// loads at the first call on a device, so a caller that is about to reserve
+// the device's memory makes that first call before it does (a call on a
+// one-point grid is enough), and before any stream capture.
 //
 // Scratch (g_scratch, kScratchBytes = 16 MiB + 256 B):
 //   [0, 256)     accumulators: vertices, triangles, MC vertices.  They MUST
 //                start at zero; every call clears them on its stream first.
 //   [256, ...)   one uint4 per grid row (vertices, triangles, MC vertices, 0),
 //                at most ISO_NOALLOC_MAX_ROWS = 2^20 rows (ny * nz); larger
-//                grids are rejected with ISO_ERR_TOO_LARGE before any launch.
+//                grids are rejected with ISO_ERR_TOO_LARGE before any launch,
+//                and so are rows of more than kMaxRowPoints points, whose
+//                triangle count could pass 2^32.
 // Every row record is written before it is read, so only the accumulators
 // need clearing.  Because the scratch is one array per device, calls on the
 // same device must not overlap: two calls in flight at once (other streams
 // or host threads) race on it.
 //
-// The first call on a device does the set-up, with that device current:
-// cudaGetSymbolAddress of the scratch and a synchronous copy of the case
-// tables into g_cases.  Later calls only enqueue a memset and three kernels.
-#include <mutex>
-
+// No state is kept between calls: each call looks up the array's device
+// address on the current device (cudaGetSymbolAddress, a host-side lookup
+// once the module is loaded), so a call after a cudaDeviceReset uses the
+// array of the freshly loaded module.  The counts need no case table: the
+// triangles and Marching Cubes vertices of 32 cells at a time come from
+// bit-parallel formulas over the cells' corner words (tris_of_word,
+// mc_verts_of_word), the ones the count pass of the other entry points uses.
 #include "../../include/miniiso.h"
 #include "case_table.h"
 #include "iso_device.cuh"
@@ -37,12 +45,13 @@ namespace iso {
 namespace {
 
 constexpr long long kMaxRows = ISO_NOALLOC_MAX_ROWS;
+// A row's record holds 32-bit counts: at most 5 (nx - 1) triangles and
+// 3 nx + 2 vertices, so rows are limited to (2^32 - 1) / 5 points.
+constexpr long long kMaxRowPoints = ISO_NOALLOC_MAX_ROW_POINTS;
 constexpr size_t kAccumBytes = 256;
 constexpr size_t kScratchBytes = kAccumBytes + 16 * (size_t)kMaxRows;
-constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
-static __device__ CaseTables g_cases;
 
 // Word c*32 + lane of a row, and word c*32 + 32 (uniform over the warp).
 __device__ __forceinline__ void na_chunk(const float* __restrict__ row, bool ok, int c, int nx, int lane, float iso,
@@ -66,13 +75,6 @@ template <bool MC>
 __global__ void __launch_bounds__(kThreads) k_na_rows(const float* __restrict__ vol, Grid g, float iso,
                                                       uint4* __restrict__ rows)
 {
-    __shared__ uint8_t s_ntris[256];
-    __shared__ uint16_t s_cut[256];
-    for (int c = threadIdx.x; c < 256; c += blockDim.x) {
-        s_ntris[c] = (uint8_t)iso_case_ntris(g_cases.tris[c]);
-        s_cut[c] = g_cases.cut[c];
-    }
-    __syncthreads();
     const int lane = threadIdx.x & 31;
     const long long r = (long long)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5);
     if (r >= g.R) return;
@@ -80,6 +82,7 @@ __global__ void __launch_bounds__(kThreads) k_na_rows(const float* __restrict__ 
     const bool hasY = j < g.ny - 1, hasZ = k < g.nz - 1, cell = hasY && hasZ;
     const int jy = hasY ? j + 1 : j, kz = hasZ ? k + 1 : k;
     auto rowptr = [&](int kk, int jj) { return vol + ((long long)kk * g.ny + jj) * g.nx; };
+    // per lane at most 3 * 32 cut edges and 5 * 32 triangles per word, over at most 2^20 words
     uint32_t nv = 0, nt = 0, nm = 0;
     const int nchunks = (g.W + 31) / 32;
     for (int c = 0; c < nchunks; ++c) {
@@ -101,22 +104,22 @@ __global__ void __launch_bounds__(kThreads) k_na_rows(const float* __restrict__ 
         nv += __popc((rw.a ^ rw.ash) & evalid);
         if (hasY) nv += __popc((rw.a ^ rw.b) & pvalid);
         if (hasZ) nv += __popc((rw.a ^ rw.c) & pvalid);
-        if (cell) {
-            for (uint32_t act = active_cells(rw, evalid); act; act &= act - 1) {
-                const int bit = __ffs(act) - 1;
-                const int cs = cube_case(rw, bit);
-                nt += s_ntris[cs];
-                if (MC) nm += __popc(mc_owned_edges(32 * w + bit == 0, j == 0, k == 0) & s_cut[cs]);
-            }
+        if (cell) {  // the word's 32 cells at once; corners 0..7 = a ash bsh b c csh dsh d
+            nt += tris_of_word(rw.a, rw.ash, rw.bsh, rw.b, rw.c, rw.csh, rw.dsh, rw.d, evalid);
+            if (MC)
+                nm += mc_verts_of_word(rw.a, rw.ash, rw.bsh, rw.b, rw.c, rw.csh, rw.dsh, rw.d, evalid, j == 0, k == 0,
+                                       w == 0);
         }
     }
+    // row totals in 64 bits (32 lanes), stored as 32-bit counts: rows are limited to kMaxRowPoints points
+    unsigned long long v = nv, t = nt, m = nm;
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) {
-        nv += __shfl_xor_sync(0xffffffffu, nv, d);
-        nt += __shfl_xor_sync(0xffffffffu, nt, d);
-        if (MC) nm += __shfl_xor_sync(0xffffffffu, nm, d);
+        v += __shfl_xor_sync(0xffffffffu, v, d);
+        t += __shfl_xor_sync(0xffffffffu, t, d);
+        if (MC) m += __shfl_xor_sync(0xffffffffu, m, d);
     }
-    if (lane == 0) rows[r] = make_uint4(nv, nt, nm, 0u);
+    if (lane == 0) rows[r] = make_uint4((uint32_t)v, (uint32_t)t, (uint32_t)m, 0u);
 }
 
 // Sums of the row records into the accumulators (which start at zero).
@@ -157,48 +160,27 @@ __global__ void k_na_finish(const unsigned long long* __restrict__ acc, int mc, 
     out[1] = (int64_t)acc[1];
 }
 
-struct DeviceSetup {
-    bool done = false;
-    unsigned char* scratch = nullptr;
-    int nsm = 0;
-};
-std::mutex g_setup_mutex;
-DeviceSetup g_setup[kMaxDevices];
-
-void host_case_tables(CaseTables& t)
+// The scratch array's address on the current device.  Looked up on every
+// call: the lookup is cheap once the module is loaded, and nothing cached can
+// outlive a cudaDeviceReset.
+cudaError_t scratch_address(unsigned char*& out)
 {
-    for (int c = 0; c < 256; ++c) {
-        const uint64_t w = kIsoCaseTris[c];
-        t.tris[c] = w;
-        uint16_t cut = 0;
-        for (int e = 0; e < 12; ++e) {
-            if (((c >> kIsoEdgeLo[e]) & 1) != ((c >> kIsoEdgeHi[e]) & 1)) cut |= (uint16_t)(1u << e);
-        }
-        t.cut[c] = cut;
-        t.order[c] = 0;  // not used by the count
-    }
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
+    out = static_cast<unsigned char*>(p);
+    return e != cudaSuccess ? e : (p ? cudaSuccess : cudaErrorInvalidSymbol);
 }
 
-// Once per device, with that device current.
-iso_status setup_device(int dev, DeviceSetup*& out)
+// A kThreads-wide launch that returns its own status.
+template <typename... Params, typename... Args>
+cudaError_t launch(void (*kern)(Params...), unsigned blocks, cudaStream_t s, Args... args)
 {
-    if (dev < 0 || dev >= kMaxDevices) return ISO_ERR_INVALID_ARG;
-    std::lock_guard<std::mutex> lock(g_setup_mutex);
-    DeviceSetup& s = g_setup[dev];
-    if (!s.done) {
-        void* p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_scratch) != cudaSuccess || p == nullptr) return ISO_ERR_CUDA;
-        CaseTables h;
-        host_case_tables(h);
-        if (cudaMemcpyToSymbol(g_cases, &h, sizeof(CaseTables)) != cudaSuccess) return ISO_ERR_CUDA;
-        int nsm = 0;
-        if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return ISO_ERR_CUDA;
-        s.scratch = static_cast<unsigned char*>(p);
-        s.nsm = nsm;
-        s.done = true;
-    }
-    out = &s;
-    return ISO_OK;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(blocks);
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    return cudaLaunchKernelEx(&cfg, kern, args...);
 }
 
 }  // namespace
@@ -209,7 +191,8 @@ extern "C" iso_status iso_count_device_noalloc(iso_algorithm algo, const float* 
 {
     using namespace iso;
     if (!volume || !grid || !counts) return ISO_ERR_INVALID_ARG;
-    if (algo != ISO_FLYING_EDGES && algo != ISO_MARCHING_CUBES) return ISO_ERR_INVALID_ARG;
+    // ISO_MC_DUPFREE numbers the same vertices as ISO_MARCHING_CUBES in another order: the same counts
+    if (algo != ISO_FLYING_EDGES && algo != ISO_MARCHING_CUBES && algo != ISO_MC_DUPFREE) return ISO_ERR_INVALID_ARG;
     Grid g{};
     for (int a = 0; a < 3; ++a) {
         if (grid->dims[a] < 1 || grid->dims[a] > (1ll << 30)) return ISO_ERR_INVALID_ARG;
@@ -223,25 +206,32 @@ extern "C" iso_status iso_count_device_noalloc(iso_algorithm algo, const float* 
         g.sp[a] = grid->spacing[a];
         g.zp[a] = grid->origin[a];
     }
-    if (g.R > kMaxRows) return ISO_ERR_TOO_LARGE;
-    int dev = 0;
+    if (g.R > kMaxRows || g.nx > kMaxRowPoints) return ISO_ERR_TOO_LARGE;
+    int dev = 0, nsm = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return ISO_ERR_CUDA;
-    DeviceSetup* su = nullptr;
-    const iso_status st = setup_device(dev, su);
-    if (st != ISO_OK) return st;
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return ISO_ERR_CUDA;
+    unsigned char* scratch = nullptr;
+    if (scratch_address(scratch) != cudaSuccess) return ISO_ERR_CUDA;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    unsigned long long* acc = reinterpret_cast<unsigned long long*>(su->scratch);
-    uint4* rows = reinterpret_cast<uint4*>(su->scratch + kAccumBytes);
+    unsigned long long* acc = reinterpret_cast<unsigned long long*>(scratch);
+    uint4* rows = reinterpret_cast<uint4*>(scratch + kAccumBytes);
+    // each launch's own status, so an earlier, unrelated error on this thread is neither reported nor cleared
     if (cudaMemsetAsync(acc, 0, kAccumBytes, s) != cudaSuccess) return ISO_ERR_CUDA;
-    const bool mc = algo == ISO_MARCHING_CUBES;
+    const bool mc = algo != ISO_FLYING_EDGES;
     if (g.nx >= 2 && g.ny >= 2 && g.nz >= 2) {  // a grid without cells has an empty mesh
         const unsigned blocks = (unsigned)((g.R + kThreads / 32 - 1) / (kThreads / 32));
-        if (mc) k_na_rows<true><<<blocks, kThreads, 0, s>>>(volume, g, isoval, rows);
-        else k_na_rows<false><<<blocks, kThreads, 0, s>>>(volume, g, isoval, rows);
+        const cudaError_t e = mc ? launch(k_na_rows<true>, blocks, s, volume, g, isoval, rows)
+                                 : launch(k_na_rows<false>, blocks, s, volume, g, isoval, rows);
+        if (e != cudaSuccess) return ISO_ERR_CUDA;
         long long sum_blocks = (g.R + kThreads - 1) / kThreads;
-        if (sum_blocks > 4ll * su->nsm) sum_blocks = 4ll * su->nsm;
-        k_na_sum<<<(unsigned)sum_blocks, kThreads, 0, s>>>(rows, g.R, acc);
+        if (sum_blocks > 4ll * nsm) sum_blocks = 4ll * nsm;
+        if (launch(k_na_sum, (unsigned)sum_blocks, s, (const uint4*)rows, g.R, acc) != cudaSuccess) return ISO_ERR_CUDA;
     }
-    k_na_finish<<<1, 1, 0, s>>>(acc, mc ? 1 : 0, counts);
-    return cudaGetLastError() == cudaSuccess ? ISO_OK : ISO_ERR_CUDA;
+    cudaLaunchConfig_t one = {};
+    one.gridDim = dim3(1);
+    one.blockDim = dim3(1);
+    one.stream = s;
+    if (cudaLaunchKernelEx(&one, k_na_finish, (const unsigned long long*)acc, mc ? 1 : 0, counts) != cudaSuccess)
+        return ISO_ERR_CUDA;
+    return ISO_OK;
 }

@@ -14,8 +14,9 @@
 # The reference's CMake files are not used (they need CMake >= 2.8 policies
 # that current CMake rejects); the source lists below are the ones those
 # CMakeLists.txt name.  Usage: sh oracle/build_ref.sh [reference root]
+# (default: $MINIISO_REFERENCE, else the checkout's usual place).
 set -e
-REF=${1:-/root/reference}
+REF=${1:-${MINIISO_REFERENCE:-/root/reference}}
 OUT=$(cd "$(dirname "$0")" && pwd)/_ref
 [ -d "$REF/flyingEdges" ] || { echo "no reference checkout at $REF" >&2; exit 1; }
 mkdir -p "$OUT"

@@ -38,6 +38,19 @@ struct oracle_fe {
 };
 
 static double g_last_wall = 0.0;
+
+/* std::vector<T>(n) value-initialises its n elements on the constructing
+ * thread, before any parallel region: the reference's constructor
+ * (FlyingEdgesAlgorithm.h:31-41) and pass 3 (openmp/FlyingEdgesAlgorithm.cpp:
+ * 329-331) pay that serial zero-fill inside the timed extraction, so the
+ * oracle allocates the same way (calloc could hand out untouched zero pages
+ * and move that cost into the parallel passes). */
+static void* zeroed(size_t n, size_t size)
+{
+    void* p = malloc(n * size);
+    if (p) memset(p, 0, n * size);
+    return p;
+}
 double oracle_last_wall_seconds(void) { return g_last_wall; }
 
 static double now_s(void)
@@ -70,10 +83,10 @@ oracle_fe* oracle_fe_create(const float* data, const size_t dims[3],
     for (int a = 0; a < 3; ++a) { fe->sp[a] = spacing[a]; fe->zp[a] = origin[a]; }
     fe->iso = isoval;
     fe->nthreads = nthreads > 0 ? nthreads : 1;
-    fe->ge = (grid_edge*)calloc(ny * nz, sizeof(grid_edge));
-    fe->tri_counter = (size_t*)calloc((ny - 1) * (nz - 1) + 1, sizeof(size_t));
-    fe->edge_cases = (unsigned char*)calloc((nx - 1) * ny * nz + 1, 1);
-    fe->cube_cases = (unsigned char*)calloc((nx - 1) * (ny - 1) * (nz - 1) + 1, 1);
+    fe->ge = (grid_edge*)zeroed(ny * nz, sizeof(grid_edge));
+    fe->tri_counter = (size_t*)zeroed((ny - 1) * (nz - 1) + 1, sizeof(size_t));
+    fe->edge_cases = (unsigned char*)zeroed((nx - 1) * ny * nz + 1, 1);
+    fe->cube_cases = (unsigned char*)zeroed((nx - 1) * (ny - 1) * (nz - 1) + 1, 1);
     return fe;
 }
 
@@ -234,10 +247,11 @@ void oracle_fe_pass3(oracle_fe* fe)
         tmp = g->zstart; g->zstart = acc; acc += tmp;
     }
     fe->n_points = acc;
-    fe->points = (float*)calloc(3 * fe->n_points + 1, sizeof(float));
-    fe->normals = (float*)calloc(3 * fe->n_points + 1, sizeof(float));
-    fe->tris = (size_t*)calloc(3 * fe->n_tris + 1, sizeof(size_t));
-    fe->edge_of_vertex = (size_t*)calloc(fe->n_points + 1, sizeof(size_t));
+    fe->points = (float*)zeroed(3 * fe->n_points + 1, sizeof(float));
+    fe->normals = (float*)zeroed(3 * fe->n_points + 1, sizeof(float));
+    fe->tris = (size_t*)zeroed(3 * fe->n_tris + 1, sizeof(size_t));
+    /* the vertices' edge ids are the oracle's own bookkeeping (no reference counterpart) */
+    fe->edge_of_vertex = (size_t*)malloc((fe->n_points + 1) * sizeof(size_t));
 }
 
 /* Image3D::getPosCube (flyingEdges/util/Image3D.cpp:45-87). */

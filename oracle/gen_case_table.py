@@ -9,6 +9,7 @@ Source: flyingEdges/util/MarchingCubesTables.h:303 (caseTriangles).
 Usage: python oracle/gen_case_table.py <path to MarchingCubesTables.h>
 """
 import re
+import os
 import sys
 from pathlib import Path
 
@@ -26,8 +27,8 @@ def parse(text):
 
 
 def main():
-    src = Path(sys.argv[1] if len(sys.argv) > 1 else
-               "/root/reference/flyingEdges/util/MarchingCubesTables.h")
+    ref = Path(os.environ.get("MINIISO_REFERENCE", "/root/reference"))
+    src = Path(sys.argv[1]) if len(sys.argv) > 1 else ref / "flyingEdges" / "util" / "MarchingCubesTables.h"
     cases = parse(src.read_text())
     lines = ["// Generated by oracle/gen_case_table.py -- do not edit.",
              "// Test infrastructure: triangle cases of miniIsosurface",

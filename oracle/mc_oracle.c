@@ -15,6 +15,9 @@
 #include <stdlib.h>
 #include <string.h>
 #include <time.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 static const unsigned char kLo[12] = {0, 1, 3, 0, 4, 5, 7, 4, 0, 1, 3, 2};
 static const unsigned char kHi[12] = {1, 2, 2, 3, 5, 6, 6, 7, 4, 5, 7, 6};
@@ -109,19 +112,23 @@ static void spush(svec* v, size_t x)
     v->p[v->n++] = x;
 }
 
-int oracle_mc_run(const float* data, const size_t dims[3], const float spacing[3],
-                  const float origin[3], float iso, oracle_mesh* out)
-{
-    memset(out, 0, sizeof(*out));
-    size_t nx = dims[0], ny = dims[1], nz = dims[2];
-    if (nx < 2 || ny < 2 || nz < 2) { g_mc_wall = 0.0; return 0; }
-    double t0 = now_s();
-    size_t nX = (nx - 1) * ny * nz, nY = nx * (ny - 1) * nz;
+/* The cells of z-section [zbeg, zend) x all y x all x, visited in (k, j, i)
+ * order, appended to a running mesh whose edge map persists across the
+ * sections one thread runs: sectionOfMarchingCubes
+ * (marchingCubes/openmp/main.cpp:44-154); with one section over the whole
+ * grid it is MarchingCubes() of marchingCubes/serial/main.cpp:42-192. */
+typedef struct {
     edge_map map;
-    map_init(&map, 1 << 16);
-    fvec pts = {0}, nrm = {0};
-    svec tris = {0}, eov = {0};
-    size_t pt_idx = 0;
+    fvec pts, nrm;
+    svec tris, eov;
+    size_t pt_idx;
+} mc_part;
+
+static void mc_section(const float* data, const size_t dims[3], const float spacing[3], const float origin[3],
+                       float iso, size_t zbeg, size_t zend, mc_part* part)
+{
+    size_t nx = dims[0], ny = dims[1], nz = dims[2];
+    size_t nX = (nx - 1) * ny * nz, nY = nx * (ny - 1) * nz;
     static const int dx[8] = {0, 1, 1, 0, 0, 1, 1, 0};
     static const int dy[8] = {0, 0, 1, 1, 0, 0, 1, 1};
     static const int dz[8] = {0, 0, 0, 0, 1, 1, 1, 1};
@@ -131,7 +138,7 @@ int oracle_mc_run(const float* data, const size_t dims[3], const float spacing[3
     static const int ez[12] = {0, 0, 0, 0, 1, 1, 1, 1, 0, 0, 0, 0};
     static const int axis[12] = {0, 1, 0, 1, 0, 1, 0, 1, 2, 2, 2, 2};
 #define V(i, j, k) data[(k) * nx * ny + (j) * nx + (i)]
-    for (size_t k = 0; k + 1 < nz; ++k)
+    for (size_t k = zbeg; k < zend; ++k)
     for (size_t j = 0; j + 1 < ny; ++j)
     for (size_t i = 0; i + 1 < nx; ++i) {
         float vals[8];
@@ -174,10 +181,10 @@ int oracle_mc_run(const float* data, const size_t dims[3], const float spacing[3
                 else if (axis[e] == 1) gid = nX + x + nx * y + nx * (ny - 1) * z;
                 else gid = nX + nY + x + nx * y + nx * ny * z;
                 size_t found;
-                if (map_find_or_insert(&map, gid, pt_idx, &found)) {
+                if (map_find_or_insert(&part->map, gid, part->pt_idx, &found)) {
                     tri[q] = found;
                 } else {
-                    tri[q] = pt_idx++;
+                    tri[q] = part->pt_idx++;
                     int v1 = kLo[e], v2 = kHi[e];
                     float w = (iso - vals[v1]) / (vals[v2] - vals[v1]);
                     float np[3], nn[3];
@@ -185,24 +192,113 @@ int oracle_mc_run(const float* data, const size_t dims[3], const float spacing[3
                         np[a] = pc[v1][a] + (w * (pc[v2][a] - pc[v1][a]));
                         nn[a] = gc[v1][a] + (w * (gc[v2][a] - gc[v1][a]));
                     }
-                    fpush3(&pts, np);
-                    fpush3(&nrm, nn);
-                    spush(&eov, gid);
+                    fpush3(&part->pts, np);
+                    fpush3(&part->nrm, nn);
+                    spush(&part->eov, gid);
                 }
             }
             if (tri[0] != tri[1] && tri[1] != tri[2] && tri[2] != tri[0]) {
-                spush(&tris, tri[0]); spush(&tris, tri[1]); spush(&tris, tri[2]);
+                spush(&part->tris, tri[0]); spush(&part->tris, tri[1]); spush(&part->tris, tri[2]);
             }
         }
     }
 #undef V
-    free(map.keys); free(map.vals);
-    out->n_points = pt_idx;
-    out->n_tris = tris.n / 3;
-    out->points = pts.p ? pts.p : (float*)calloc(1, sizeof(float));
-    out->normals = nrm.p ? nrm.p : (float*)calloc(1, sizeof(float));
-    out->tris = tris.p ? tris.p : (size_t*)calloc(1, sizeof(size_t));
-    out->edge_of_vertex = eov.p ? eov.p : (size_t*)calloc(1, sizeof(size_t));
+}
+
+static void part_to_mesh(mc_part* part, oracle_mesh* out)
+{
+    out->n_points = part->pt_idx;
+    out->n_tris = part->tris.n / 3;
+    out->points = part->pts.p ? part->pts.p : (float*)calloc(1, sizeof(float));
+    out->normals = part->nrm.p ? part->nrm.p : (float*)calloc(1, sizeof(float));
+    out->tris = part->tris.p ? part->tris.p : (size_t*)calloc(1, sizeof(size_t));
+    out->edge_of_vertex = part->eov.p ? part->eov.p : (size_t*)calloc(1, sizeof(size_t));
+}
+
+int oracle_mc_run(const float* data, const size_t dims[3], const float spacing[3],
+                  const float origin[3], float iso, oracle_mesh* out)
+{
+    memset(out, 0, sizeof(*out));
+    size_t nx = dims[0], ny = dims[1], nz = dims[2];
+    if (nx < 2 || ny < 2 || nz < 2) { g_mc_wall = 0.0; return 0; }
+    double t0 = now_s();
+    mc_part part;
+    memset(&part, 0, sizeof(part));
+    map_init(&part.map, 1 << 16);
+    mc_section(data, dims, spacing, origin, iso, 0, nz - 1, &part);
+    free(part.map.keys); free(part.map.vals);
+    part_to_mesh(&part, out);
+    g_mc_wall = now_s() - t0;
+    return 0;
+}
+
+/* util::Indexer (marchingCubes/util/util.h:56-78): the first index of section
+ * idx when n elements are split into nsec sections of grain or grain + 1. */
+static size_t section_begin(size_t n, size_t nsec, size_t idx)
+{
+    const size_t grain = n / nsec, split = (grain + 1) * nsec - n;
+    return idx <= split ? grain * idx : grain * split + (grain + 1) * (idx - split);
+}
+
+/* MarchingCubes() of marchingCubes/openmp/main.cpp:156-296 with its default
+ * sections (main.cpp:308-322, 405-410): nthreads z-sections (at most nz - 1),
+ * one x and one y section; each thread runs its sections with its own edge
+ * map, so a vertex on a seam between two threads' sections is made by both;
+ * the threads' meshes are appended one after another with their triangle
+ * indices offset.  The reference appends them in the order the threads
+ * finish (an omp critical section); this port appends them in thread order,
+ * so its output is deterministic. */
+int oracle_mc_openmp_run(const float* data, const size_t dims[3], const float spacing[3],
+                         const float origin[3], float iso, int nthreads, oracle_mesh* out)
+{
+    memset(out, 0, sizeof(*out));
+    size_t nx = dims[0], ny = dims[1], nz = dims[2];
+    if (nx < 2 || ny < 2 || nz < 2) { g_mc_wall = 0.0; return 0; }
+    double t0 = now_s();
+    int nt = nthreads > 0 ? nthreads : 1;
+    size_t nsec = (size_t)nt;
+    if (nsec > nz - 1) nsec = nz - 1;
+    mc_part* parts = (mc_part*)calloc((size_t)nt, sizeof(mc_part));
+    if (!parts) return 1;
+#pragma omp parallel num_threads(nt)
+    {
+#ifdef _OPENMP
+        const int t = omp_get_thread_num();
+#else
+        const int t = 0;
+#endif
+        mc_part* part = &parts[t];
+        map_init(&part->map, 1 << 16);
+        long s;
+#pragma omp for schedule(static) nowait
+        for (s = 0; s < (long)nsec; ++s) {
+            const size_t zb = section_begin(nz - 1, nsec, (size_t)s), ze = section_begin(nz - 1, nsec, (size_t)s + 1);
+            mc_section(data, dims, spacing, origin, iso, zb, ze, part);
+        }
+        free(part->map.keys); free(part->map.vals);
+    }
+    size_t nv = 0, ntr = 0;
+    for (int t = 0; t < nt; ++t) { nv += parts[t].pt_idx; ntr += parts[t].tris.n / 3; }
+    out->n_points = nv;
+    out->n_tris = ntr;
+    out->points = (float*)malloc(sizeof(float) * (3 * nv + 1));
+    out->normals = (float*)malloc(sizeof(float) * (3 * nv + 1));
+    out->tris = (size_t*)malloc(sizeof(size_t) * (3 * ntr + 1));
+    out->edge_of_vertex = (size_t*)malloc(sizeof(size_t) * (nv + 1));
+    size_t ov = 0, ot = 0;
+    for (int t = 0; t < nt; ++t) {
+        mc_part* p = &parts[t];
+        if (p->pt_idx) {
+            memcpy(out->points + 3 * ov, p->pts.p, sizeof(float) * 3 * p->pt_idx);
+            memcpy(out->normals + 3 * ov, p->nrm.p, sizeof(float) * 3 * p->pt_idx);
+            memcpy(out->edge_of_vertex + ov, p->eov.p, sizeof(size_t) * p->pt_idx);
+        }
+        for (size_t q = 0; q < p->tris.n; ++q) out->tris[3 * ot + q] = p->tris.p[q] + ov;
+        ov += p->pt_idx;
+        ot += p->tris.n / 3;
+        free(p->pts.p); free(p->nrm.p); free(p->tris.p); free(p->eov.p);
+    }
+    free(parts);
     g_mc_wall = now_s() - t0;
     return 0;
 }

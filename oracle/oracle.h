@@ -18,6 +18,7 @@
 #define ISO_ORACLE_H
 
 #include <stddef.h>
+#include <stdint.h>
 
 #ifdef __cplusplus
 extern "C" {
@@ -69,6 +70,13 @@ int oracle_mc_run(const float* data, const size_t dims[3], const float spacing[3
 int oracle_mc_dupfree_run(const float* data, const size_t dims[3], const float spacing[3],
                           const float origin[3], float isoval, oracle_mesh* out);
 
+/* The OpenMP Marching Cubes of marchingCubes/openmp/main.cpp:156-296 with
+ * its default sections (nthreads z-sections): vertices on the seams between
+ * threads' sections appear once per section.  The threads' meshes are
+ * appended in thread order. */
+int oracle_mc_openmp_run(const float* data, const size_t dims[3], const float spacing[3],
+                         const float origin[3], float isoval, int nthreads, oracle_mesh* out);
+
 void oracle_mesh_free(oracle_mesh* m);
 
 /* Triangles per block of `block`^3 cells at isovalue iso: each cell's case
@@ -80,7 +88,13 @@ void oracle_mesh_free(oracle_mesh* m);
  * (bx, by, bz) at (bz*nby + by)*nbx + bx, nb = ceil((n-1)/block). */
 void oracle_block_tris(const float* data, const size_t dims[3], float iso, int block, int* counts);
 
-/* Seconds of wall time of the last oracle_fe_run / oracle_mc_run call
+/* The seeded benchmark volumes (oracle/volgen_oracle.c), x fastest:
+ * Gaussian blobs and octaves of trilinear value noise.  Return 0 on success. */
+int oracle_generate_blobs(const size_t dims[3], int nblobs, uint64_t seed, float* out);
+int oracle_generate_value_noise(const size_t dims[3], int octaves, int period, uint64_t seed, float* out);
+
+/* Seconds of wall time of the last oracle_fe_run / oracle_mc_run (or
+ * oracle_mc_openmp_run) call
  * (extraction only, like the reference's "Total Program WALL Time"). */
 double oracle_last_wall_seconds(void);
 double oracle_mc_last_wall_seconds(void);

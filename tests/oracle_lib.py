@@ -15,6 +15,8 @@ ROOT = Path(__file__).resolve().parents[1]
 ORACLE_DIR = ROOT / "oracle"
 ORACLE_LIB = ORACLE_DIR / "lib" / "liboracle.so"
 REF_DIR = ORACLE_DIR / "_ref"
+# the miniIsosurface checkout read by the tests that compare with its sources (MINIISO_REFERENCE)
+REFERENCE = Path(os.environ.get("MINIISO_REFERENCE", "/root/reference"))
 
 
 class OracleMesh(C.Structure):
@@ -41,6 +43,9 @@ def lib():
         L.oracle_fe_run.argtypes = [C.c_void_p, sz3, f3, f3, C.c_float, C.c_int, C.POINTER(OracleMesh)]
         L.oracle_mc_run.argtypes = [C.c_void_p, sz3, f3, f3, C.c_float, C.POINTER(OracleMesh)]
         L.oracle_mc_dupfree_run.argtypes = [C.c_void_p, sz3, f3, f3, C.c_float, C.POINTER(OracleMesh)]
+        L.oracle_mc_openmp_run.argtypes = [C.c_void_p, sz3, f3, f3, C.c_float, C.c_int, C.POINTER(OracleMesh)]
+        L.oracle_generate_blobs.argtypes = [sz3, C.c_int, C.c_uint64, C.c_void_p]
+        L.oracle_generate_value_noise.argtypes = [sz3, C.c_int, C.c_int, C.c_uint64, C.c_void_p]
         L.oracle_mesh_free.argtypes = [C.POINTER(OracleMesh)]
         L.oracle_fe_create.restype = C.c_void_p
         L.oracle_fe_create.argtypes = [C.c_void_p, sz3, f3, f3, C.c_float, C.c_int]
@@ -121,6 +126,40 @@ def mc(vol, iso, spacing=(1, 1, 1), origin=(0, 0, 0)):
         return _mesh_to_numpy(m)
     finally:
         L.oracle_mesh_free(C.byref(m))
+
+
+def mc_openmp(vol, iso, spacing=(1, 1, 1), origin=(0, 0, 0), nthreads=1):
+    """Oracle port of marchingCubes/openmp: nthreads z-sections, seam vertices once per section."""
+    L = lib()
+    vol, dims, sp, org = _args(vol, spacing, origin)
+    if any(d < 2 for d in vol.shape):
+        return (np.zeros((0, 3), np.float32), np.zeros((0, 3), np.float32), np.zeros((0, 3), np.uint64),
+                np.zeros(0, np.uint64))
+    m = OracleMesh()
+    L.oracle_mc_openmp_run(vol.ctypes.data, dims, sp, org, C.c_float(iso), int(nthreads), C.byref(m))
+    try:
+        return _mesh_to_numpy(m)
+    finally:
+        L.oracle_mesh_free(C.byref(m))
+
+
+def generate_blobs(dims, nblobs=8, seed=0):
+    """The seeded Gaussian-blob volume (oracle/volgen_oracle.c), shape (nz, ny, nx)."""
+    nx, ny, nz = (int(d) for d in dims)
+    out = np.empty((nz, ny, nx), np.float32)
+    if lib().oracle_generate_blobs((C.c_size_t * 3)(nx, ny, nz), int(nblobs), C.c_uint64(seed), out.ctypes.data):
+        raise ValueError("oracle_generate_blobs failed")
+    return out
+
+
+def generate_value_noise(dims, octaves=4, period=64, seed=0):
+    """The seeded value-noise volume (oracle/volgen_oracle.c), shape (nz, ny, nx)."""
+    nx, ny, nz = (int(d) for d in dims)
+    out = np.empty((nz, ny, nx), np.float32)
+    if lib().oracle_generate_value_noise((C.c_size_t * 3)(nx, ny, nz), int(octaves), int(period), C.c_uint64(seed),
+                                         out.ctypes.data):
+        raise ValueError("oracle_generate_value_noise failed")
+    return out
 
 
 def mc_dupfree(vol, iso, spacing=(1, 1, 1), origin=(0, 0, 0)):
@@ -223,3 +262,75 @@ def run_ref(name, vol, iso, spacing=(1, 1, 1), origin=(0, 0, 0), threads=None):
                              check=True)
         pts, nrm, tri = read_polydata(vout)
         return pts, nrm, tri, res.stdout, Path(vout).read_bytes()
+
+
+# ---------------------------------------------------------------------------
+# FP64 interpolation error of a float32 mesh
+# ---------------------------------------------------------------------------
+def edge_points(edge_of_vertex, dims):
+    """(axis, lower end (i, j, k)) of each vertex from its global edge id
+    (marchingCubes/util/Image3D.cpp:168-256: x-edges, then y, then z)."""
+    nx, ny, nz = dims
+    nX = (nx - 1) * ny * nz
+    nY = nx * (ny - 1) * nz
+    e = np.asarray(edge_of_vertex).astype(np.int64)
+    axis = np.where(e < nX, 0, np.where(e < nX + nY, 1, 2))
+    loc = np.where(axis == 0, e, np.where(axis == 1, e - nX, e - nX - nY))
+    ex = np.array([nx - 1, nx, nx])[axis]
+    ey = np.array([ny, ny - 1, ny])[axis]
+    i = loc % ex
+    j = (loc // ex) % ey
+    k = loc // (ex * ey)
+    return axis, np.stack([i, j, k], 1)
+
+
+def fp64_error(vol, iso, points, normals, edge_of_vertex, spacing=(1, 1, 1), origin=(0, 0, 0), chunk=1 << 22):
+    """Max error of float32 points and normals against the reference's formulas
+    (FlyingEdgesAlgorithm.cpp:623-647, Image3D.cpp:45-188) evaluated in
+    float64 from the same float32 samples: absolute, relative to the largest
+    float64 magnitude, and in float32 ulps of the float64 value."""
+    nz, ny, nx = vol.shape
+    axis, lo_all = edge_points(edge_of_vertex, (nx, ny, nz))
+    spd, orgd = np.array(spacing, np.float64), np.array(origin, np.float64)
+    res = {"points": [0.0, 0.0, 0.0], "normals": [0.0, 0.0, 0.0]}  # abs, scale, ulps
+
+    def grad(ijk):
+        g = np.zeros((len(ijk), 3))
+        dims = (nx, ny, nz)
+        for a in range(3):
+            q0, q1 = ijk.copy(), ijk.copy()
+            first = ijk[:, a] == 0
+            last = ijk[:, a] == dims[a] - 1
+            q0[:, a] = np.where(last, ijk[:, a], ijk[:, a] + 1)
+            q1[:, a] = np.where(first, ijk[:, a], ijk[:, a] - 1)
+            run = np.where(first | last, spd[a], 2 * spd[a])
+            g[:, a] = (vol[q1[:, 2], q1[:, 1], q1[:, 0]].astype(np.float64) -
+                       vol[q0[:, 2], q0[:, 1], q0[:, 0]].astype(np.float64)) / run
+        return g
+
+    def ulps(got, ref):
+        r32 = ref.astype(np.float32)
+        sp = np.abs(np.spacing(r32)).astype(np.float64)
+        sp = np.where(sp > 0, sp, np.finfo(np.float32).tiny)
+        return np.abs(got.astype(np.float64) - ref) / sp
+
+    for s0 in range(0, len(axis), chunk):
+        a = axis[s0:s0 + chunk]
+        lo = lo_all[s0:s0 + chunk]
+        d = np.stack([a == 0, a == 1, a == 2], 1).astype(np.int64)
+        hi = lo + d
+        v0 = vol[lo[:, 2], lo[:, 1], lo[:, 0]].astype(np.float64)
+        v1 = vol[hi[:, 2], hi[:, 1], hi[:, 0]].astype(np.float64)
+        w = (float(iso) - v0) / (v1 - v0)
+        pos = orgd + (lo + w[:, None] * d) * spd
+        g0, g1 = grad(lo), grad(hi)
+        nrm = g0 + w[:, None] * (g1 - g0)
+        for key, ref, got in (("points", pos, points[s0:s0 + chunk]), ("normals", nrm, normals[s0:s0 + chunk])):
+            r = res[key]
+            r[0] = max(r[0], float(np.abs(got - ref).max()) if len(ref) else 0.0)
+            r[1] = max(r[1], float(np.abs(ref).max()) if len(ref) else 0.0)
+            r[2] = max(r[2], float(ulps(got, ref).max()) if len(ref) else 0.0)
+    out = {}
+    for key, (err, scale, u) in res.items():
+        out[key] = {"max_abs": err, "max_rel": err / scale if scale else 0.0, "max_ulps_of_fp64": u}
+    return out

@@ -29,3 +29,29 @@ def test_batch_workload_distribution():
                 assert lo - 1e-6 <= iso <= hi + 1e-6
     again = bench.batch_workload(M, seed=2, nvol=8)[1]
     assert again == reqs  # seeded
+
+
+def test_reference_arm_runs_without_the_product_library(tmp_path):
+    """bench.py --impl reference on a small volume, in a fresh process: it
+    prints its JSON line with the four CPU legs, and neither the product
+    package nor libminiiso.so is ever loaded."""
+    import json
+    import subprocess
+    import sys
+    from pathlib import Path
+
+    root = Path(__file__).resolve().parents[1]
+    code = (
+        "import sys, json; sys.argv = ['bench.py', '--impl', 'reference', '--steps', '2', '--warmup', '1'];"
+        "import bench; bench.DIMS = (40, 36, 30); bench.main();"
+        "maps = open('/proc/self/maps').read();"
+        "bad = [m for m in sys.modules if m.startswith('miniisosurface_gb300')];"
+        "assert not bad and 'libminiiso' not in maps, (bad, 'libminiiso' in maps)")
+    res = subprocess.run([sys.executable, "-c", code], cwd=root, capture_output=True, text=True, timeout=600)
+    assert res.returncode == 0, res.stderr[-2000:]
+    line = json.loads([x for x in res.stdout.splitlines() if x.startswith("{")][-1])
+    assert line["impl"] == "reference" and line["value"] > 0
+    legs = line["cpu_baseline"]["legs"]
+    assert set(legs) == {"flyingEdgesSerial", "flyingEdgesOpenMP", "mcSerial", "mcOpenMP"}
+    assert all(v["value"] > 0 and v["kind"] in ("reference", "port") for v in legs.values())
+    assert line["e2e"]["h2d_bytes_per_step"] == 0

@@ -15,7 +15,7 @@ import pytest
 import oracle_lib
 
 ROOT = Path(__file__).resolve().parents[1]
-REF = Path("/root/reference")
+REF = oracle_lib.REFERENCE
 COMPAT = ROOT / "tests" / "compat"
 
 

@@ -7,11 +7,14 @@ formulas in the same order with no FMA contraction; the stated tolerance of
 """
 import ctypes as C
 import os
+from pathlib import Path
 
 import numpy as np
 import pytest
 
 import oracle_lib
+
+ROOT = Path(__file__).resolve().parents[1]
 
 pytestmark = pytest.mark.gpu
 
@@ -335,6 +338,16 @@ def test_capacity_error_reports_sizes(M):
     assert (nv, nt) == (rp.shape[0], rt.shape[0])
 
 
+def _fp64_report(name, err):
+    import json
+
+    out = Path(os.environ.get("GRAFT_REPO_ROOT", ROOT)) / "gpurun_out"
+    if out.is_dir():
+        with open(out / "fp64_error.jsonl", "a") as f:
+            f.write(json.dumps({"case": name, **err}) + "\n")
+    print(name, err)
+
+
 def test_fp64_interpolation_error(M):
     """Max error of the float32 points/normals against the same formulas in
     double precision (reported; bounded by a few float32 ulps of the field)."""
@@ -342,51 +355,23 @@ def test_fp64_interpolation_error(M):
     sp, org = (0.7, 0.3, 1.1), (-1.0, 2.0, 0.5)
     p, n, t = gpu_extract(M, vol, 0.5, M.FLYING_EDGES, sp, org)
     _, _, _, eov = oracle_lib.fe(vol, 0.5, sp, org)
-    nz, ny, nx = vol.shape
-    nX = (nx - 1) * ny * nz
-    nY = nx * (ny - 1) * nz
-    e = eov.astype(np.int64)
-    axis = np.where(e < nX, 0, np.where(e < nX + nY, 1, 2))
-    loc = np.where(axis == 0, e, np.where(axis == 1, e - nX, e - nX - nY))
-    ex = np.array([nx - 1, nx, nx])[axis]
-    ey = np.array([ny, ny - 1, ny])[axis]
-    i = loc % ex
-    j = (loc // ex) % ey
-    k = loc // (ex * ey)
-    V = vol.astype(np.float64)
-    d = np.stack([axis == 0, axis == 1, axis == 2], 1).astype(np.int64)
-    lo = np.stack([i, j, k], 1)
-    hi = lo + d
-    v0 = V[lo[:, 2], lo[:, 1], lo[:, 0]]
-    v1 = V[hi[:, 2], hi[:, 1], hi[:, 0]]
-    w = (0.5 - v0) / (v1 - v0)
-    spd, orgd = np.array(sp, np.float64), np.array(org, np.float64)
-    pos = orgd + (lo + w[:, None] * d) * spd
-    perr = np.abs(pos - p).max()
-    scale = np.abs(pos).max()
-
-    def grad(ijk):
-        g = np.zeros((len(ijk), 3))
-        dims = (nx, ny, nz)
-        for a in range(3):
-            q0, q1 = ijk.copy(), ijk.copy()
-            run = np.full(len(ijk), 2 * spd[a])
-            first = ijk[:, a] == 0
-            last = ijk[:, a] == dims[a] - 1
-            q0[:, a] = np.where(last, ijk[:, a], ijk[:, a] + 1)
-            q1[:, a] = np.where(first, ijk[:, a], ijk[:, a] - 1)
-            run = np.where(first | last, spd[a], run)
-            g[:, a] = (V[q1[:, 2], q1[:, 1], q1[:, 0]] - V[q0[:, 2], q0[:, 1], q0[:, 0]]) / run
-        return g
-
-    g0, g1 = grad(lo), grad(hi)
-    nrm = g0 + w[:, None] * (g1 - g0)
-    nerr = np.abs(nrm - n).max()
-    nscale = np.abs(nrm).max()
-    print("fp64 max abs error: points %.3g (of %.3g), normals %.3g (of %.3g)" % (perr, scale, nerr, nscale))
+    err = oracle_lib.fp64_error(vol, 0.5, p, n, eov, sp, org)
+    _fp64_report("blobs64_spacing", err)
     eps = np.finfo(np.float32).eps
-    assert perr <= 8 * eps * scale
-    assert nerr <= 64 * eps * nscale
+    assert err["points"]["max_rel"] <= 8 * eps
+    assert err["normals"]["max_rel"] <= 64 * eps
+
+
+def test_fp64_error_config0(M):
+    """The FP64 error on the 128^3 Gaussian-blob volume at isovalue 0.5."""
+    vol = M.generate_blobs((128, 128, 128), 8, seed=0)
+    p, n, t = gpu_extract(M, vol, 0.5, M.FLYING_EDGES)
+    _, _, _, eov = oracle_lib.fe(vol, 0.5)
+    err = oracle_lib.fp64_error(vol, 0.5, p, n, eov)
+    _fp64_report("blobs128_iso0.5", err)
+    eps = np.finfo(np.float32).eps
+    assert err["points"]["max_rel"] <= 8 * eps
+    assert err["normals"]["max_rel"] <= 64 * eps
 
 
 def test_noise_512_bitexact(M):
@@ -395,6 +380,7 @@ def test_noise_512_bitexact(M):
     got = gpu_extract(M, vol, 0.0, M.FLYING_EDGES)
     ref = oracle_lib.fe(vol, 0.0, nthreads=os.cpu_count())
     assert_same_mesh(got, ref, "FE 512")
+    _fp64_report("noise512_iso0", oracle_lib.fp64_error(vol, 0.0, got[0], got[1], ref[3]))
     del got, ref
     got = gpu_extract(M, vol, 0.0, M.MARCHING_CUBES)
     ref = oracle_lib.mc(vol, 0.0)

@@ -7,8 +7,10 @@ from pathlib import Path
 import numpy as np
 import pytest
 
+import oracle_lib
+
 ROOT = Path(__file__).resolve().parents[1]
-REF_TABLES = Path("/root/reference/flyingEdges/util/MarchingCubesTables.h")
+REF_TABLES = oracle_lib.REFERENCE / "flyingEdges" / "util" / "MarchingCubesTables.h"
 
 
 def declared_functions():

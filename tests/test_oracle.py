@@ -163,3 +163,70 @@ def test_product_image_writer_readable_by_reference(built, tmp_path):
     back = M.loadImage(str(path))
     assert back.dims == img.dims and np.array_equal(back.data, img.data)
     assert back.spacing == img.spacing and back.zeroPos == img.zeroPos
+
+
+def test_oracle_generators_match_golden_and_product(built):
+    """The oracle's own volume generator (used by the CPU arm of the bench, which
+    must not load the product library) gives the pinned volume digests and the
+    product generator's volumes bit for bit."""
+    import hashlib
+    import json
+
+    import miniisosurface_gb300 as M
+
+    golden = {c["name"]: c for c in golden_cases()}
+    c0 = golden["blobs128_config0"]
+    vol = oracle_lib.generate_blobs(c0["gen"]["dims"], c0["gen"]["nblobs"], c0["gen"]["seed"])
+    assert hashlib.sha256(np.ascontiguousarray(vol, "<f4").tobytes()).hexdigest() == c0["volume_sha256"]
+    c1 = golden["noise96x80x72"]
+    g = c1["gen"]
+    vol = oracle_lib.generate_value_noise(g["dims"], g["octaves"], g["period"], g["seed"])
+    assert hashlib.sha256(np.ascontiguousarray(vol, "<f4").tobytes()).hexdigest() == c1["volume_sha256"]
+    for dims in ((33, 20, 17), (5, 64, 3)):
+        assert np.array_equal(oracle_lib.generate_value_noise(dims, 3, 8, 9), M.generate_value_noise(dims, 3, 8, seed=9))
+        assert np.array_equal(oracle_lib.generate_blobs(dims, 5, 11), M.generate_blobs(dims, 5, seed=11))
+
+
+def _tri_corners(p, t):
+    """Triangles as rows of their 9 corner coordinates (bit patterns), sorted."""
+    c = p[t.astype(np.int64)].reshape(len(t), 9).view(np.uint32)
+    return c[np.lexsort(c.T[::-1])]
+
+
+@pytest.mark.parametrize("threads", [1, 3, 8])
+def test_mc_openmp_port_sections(built, threads):
+    """The OpenMP Marching Cubes port: one thread is the serial mesh; with more
+    threads each z-section numbers its own vertices (seam vertices repeated),
+    and the triangles are the serial ones, corner for corner."""
+    vol = oracle_lib.generate_value_noise((30, 26, 40), 4, 8, 3)
+    sp, org = (0.5, 1.5, 0.75), (1.0, -2.0, 0.5)
+    sp_ = oracle_lib.mc(vol, 0.1, sp, org)
+    om = oracle_lib.mc_openmp(vol, 0.1, sp, org, nthreads=threads)
+    if threads == 1:
+        for x, y in zip(sp_, om):
+            assert np.array_equal(x, y)
+    else:
+        assert om[0].shape[0] > sp_[0].shape[0]  # vertices on the seams appear once per section
+        assert om[2].shape == sp_[2].shape
+        assert np.array_equal(_tri_corners(om[0], om[2]), _tri_corners(sp_[0], sp_[2]))
+        assert len(np.unique(om[3])) == sp_[0].shape[0]  # the same edges
+
+
+@pytest.mark.skipif(not oracle_lib.ref_available("mcOpenMP"), reason="reference programs not built here")
+@pytest.mark.parametrize("threads", [1, 4])
+def test_mc_openmp_port_vs_reference_program(built, threads):
+    """Against marchingCubes/openmp itself: the same vertex count (seams
+    included) and the same triangles corner for corner; with one thread the
+    same mesh bit for bit (the program appends its threads' meshes in the
+    order they finish, so only one thread fixes the order)."""
+    vol = oracle_lib.generate_value_noise((34, 29, 37), 4, 8, 5)
+    sp, org = (1.25, 0.5, 1.0), (0.0, 3.0, -1.0)
+    rp, rn, rt, _, _ = oracle_lib.run_ref("mcOpenMP", vol, 0.05, sp, org, threads=threads)
+    p, n, t, _ = oracle_lib.mc_openmp(vol, 0.05, sp, org, nthreads=threads)
+    assert rp.shape == p.shape and rt.shape == t.shape
+    if threads == 1:
+        assert np.array_equal(rt, t)
+        assert np.array_equal(rp.view(np.uint32), p.view(np.uint32))
+        assert np.array_equal(rn.view(np.uint32), n.view(np.uint32))
+    else:
+        assert np.array_equal(_tri_corners(rp, rt), _tri_corners(p, t))

@@ -54,6 +54,17 @@ def test_noalloc_matches_count_device(lib, algo_name):
         assert second == want, (dims, second, want)
 
 
+def test_noalloc_dupfree_counts_are_marching_cubes_counts(lib):
+    import torch
+    import miniisosurface_gb300 as M
+
+    dims = (70, 41, 33)
+    flat = torch.from_numpy(M.generate_value_noise(dims, 4, 16, seed=8).reshape(-1)).cuda()
+    want = M.count_device(flat, dims, 0.05, M.MARCHING_CUBES)
+    assert noalloc_counts(lib, flat, dims, 0.05, M.MC_DUPFREE) == want
+    assert noalloc_counts(lib, flat, dims, 0.05, M.MC_DUPFREE) == want
+
+
 def test_noalloc_empty_and_degenerate(lib):
     import torch
     import miniisosurface_gb300 as M
@@ -75,6 +86,13 @@ def test_noalloc_rejects_grids_beyond_its_scratch(lib):
                                       C.c_void_p(out.data_ptr()), None)
     assert st == _lib.ISO_ERR_TOO_LARGE
     assert b"allocation-free" in lib.iso_status_string(st)
+    torch.cuda.synchronize()
+    assert out.tolist() == [-1, -1]
+    # rows too long for the 32-bit row records: rejected the same way, before any launch
+    g = api.make_grid((_lib.ISO_NOALLOC_MAX_ROW_POINTS + 1, 2, 2))
+    st = lib.iso_count_device_noalloc(0, C.c_void_p(small.data_ptr()), C.byref(g), C.c_float(0.0),
+                                      C.c_void_p(out.data_ptr()), None)
+    assert st == _lib.ISO_ERR_TOO_LARGE
     torch.cuda.synchronize()
     assert out.tolist() == [-1, -1]
     # at the limit it runs
