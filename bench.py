@@ -15,6 +15,8 @@ One step = one full extraction (passes 1-4) of the volume.
             recorded between kernels on the extraction stream during a
             second timed region of K steps on the stream path (events cannot
             sit between a graph's kernels); algorithmic bytes per launch:
+              fe_single      4 N + 12 T          (volume read, uint32 triangles: passes 1-4 in one
+                                                  kernel, the vertices left to `vertices`)
               count          4 N                 (volume read; passes 1+2 fused)
               fe_generate    12 T                (uint32 triangles; with `vertices`)
                              4 N + 24 V + 12 T   (volume read, points+normals, triangles; alone)
@@ -25,7 +27,8 @@ One step = one full extraction (passes 1-4) of the volume.
               vertices       4 N + 24 V          (pass-4 volume read, points+normals)
             intermediates (bit rows, counts, vertex records, maps) count nothing;
   pass4     pass 4 as one unit: 4 N + 24 V + 12 T over the summed time of its
-            kernels (generate, vertices)
+            kernels (generate, vertices); with the single-pass kernel, passes
+            1-4: 8 N + 24 V + 12 T over fe_single + vertices
   pipeline  the whole extraction: B = 8 N + 24 V + 12 T over the step
   mc        the same volume through Marching Cubes (value, roofline,
             pipeline, per-pass split), and whether its triangle sequence equals
@@ -39,6 +42,9 @@ One step = one full extraction (passes 1-4) of the volume.
   parity    the timed FE and MC meshes against the oracle, bit for bit, and the
             FE points and normals against the reference's formulas evaluated
             in float64 (max absolute, relative and ulp error)
+  vtk_io    VTK legacy file IO: the volume read from a .vtk file into pinned
+            memory and copied to the device, the mesh copied back and written
+            as the reference's .vtk, in GB/s of file bytes
   batched   64 volumes with per-axis dimensions uniform in [32, 320] (half
             Gaussian blobs, half value noise), each with 1-4 isovalues uniform
             in its field's [5th, 95th] percentile: Flying Edges over all
@@ -97,6 +103,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-io", action="store_true")
     ap.add_argument("--batched-reps", type=int, default=5)
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--served-requests", type=int, default=160)
@@ -457,6 +464,58 @@ def batched_leg(M, lib, dev, reps):
     }
 
 
+def io_leg(M, lib, dev, vol_host, mesh, V, T, reps=3):
+    """VTK legacy IO throughput (row f1): the bench volume read from a
+    BINARY STRUCTURED_POINTS file into pinned host memory and copied to the
+    device (util::loadImage, flyingEdges/util/LoadImage.h:168-198), and the
+    extracted mesh copied back to pinned memory and written in the
+    reference's POLYDATA layout (util::saveTriangleMesh, SaveTriangleMesh.h:
+    33-118).  Files live in /dev/shm when it exists (memory-backed, so the
+    number is the library's parsing and byte-order work, not a disk)."""
+    import tempfile
+
+    import torch
+    from miniisosurface_gb300 import _lib
+
+    where = "/dev/shm" if os.path.isdir("/dev/shm") and os.access("/dev/shm", os.W_OK) else None
+    with tempfile.TemporaryDirectory(dir=where) as td:
+        vin, mout = os.path.join(td, "volume.vtk"), os.path.join(td, "mesh.vtk")
+        g = M.make_grid(DIMS)
+        _lib.check(lib.iso_vtk_write_image(os.fsencode(vin), C.byref(g), vol_host.ctypes.data))
+        fin = os.path.getsize(vin)
+        pinned = torch.empty(vol_host.size, dtype=torch.float32).pin_memory()
+        dbuf = torch.empty(vol_host.size, dtype=torch.float32, device=dev)
+        h_pts = torch.empty((V, 3), dtype=torch.float32).pin_memory()
+        h_nrm = torch.empty((V, 3), dtype=torch.float32).pin_memory()
+        h_tri = torch.empty((T, 3), dtype=torch.int32).pin_memory()
+        hm = _lib.IsoMesh()
+        hm.points, hm.normals, hm.tris = h_pts.data_ptr(), h_nrm.data_ptr(), h_tri.data_ptr()
+        hm.index_bytes, hm.n_points, hm.n_tris, hm.cap_points, hm.cap_tris = 4, V, T, V, T
+        t_read, t_write = [], []
+        for _ in range(reps):
+            gg = _lib.IsoGrid()
+            t0 = time.perf_counter()
+            _lib.check(lib.iso_vtk_read_image(os.fsencode(vin), C.byref(gg), C.c_void_p(pinned.data_ptr())))
+            dbuf.copy_(pinned, non_blocking=True)
+            torch.cuda.synchronize(dev)
+            t_read.append(time.perf_counter() - t0)
+            t0 = time.perf_counter()
+            h_pts.copy_(mesh.points[:V], non_blocking=True)
+            h_nrm.copy_(mesh.normals[:V], non_blocking=True)
+            h_tri.copy_(mesh.tris[:T], non_blocking=True)
+            torch.cuda.synchronize(dev)
+            _lib.check(lib.iso_vtk_write_mesh(os.fsencode(mout), C.byref(hm)))
+            t_write.append(time.perf_counter() - t0)
+        same = bool(torch.equal(dbuf.cpu(), torch.from_numpy(vol_host.reshape(-1))))
+        fout = os.path.getsize(mout)
+    r, w = min(t_read), min(t_write)
+    return {"filesystem": where or tempfile.gettempdir(), "threads": os.cpu_count(),
+            "read": {"file_bytes": fin, "ms": 1e3 * r, "GBps": fin / r / 1e9,
+                     "what": "iso_vtk_read_image into pinned memory + copy to the device", "volume_round_trip": same},
+            "write": {"file_bytes": fout, "ms": 1e3 * w, "GBps": fout / w / 1e9,
+                      "what": "mesh copied to pinned memory + iso_vtk_write_mesh (8-byte big-endian indices)"}}
+
+
 def served_leg(M, dev, nreq, seed=4, npool=8):
     """Serving loop vs the plain loop under Poisson arrivals (see the module notes)."""
     import torch
@@ -681,7 +740,7 @@ def main():
         # Marching Cubes over rows of up to 16 words: the owned-vertex pass also writes the triangles (FE ids),
         # and the mc_triangles pass remaps them in place (an intermediate rewrite)
         mc_fused = split and (DIMS[0] + 31) // 32 <= 16
-        alg_bytes = {"classify": 4 * N, "count": 4 * N, "scan": 0,
+        alg_bytes = {"classify": 4 * N, "count": 4 * N, "scan": 0, "fe_single": 4 * N + 12 * T,
                      "fe_generate": 12 * T if split else 4 * N + 24 * V + 12 * T, "vertices": 4 * N + 24 * V,
                      "mc_vertices": (12 * T if mc_fused else 0) if split else 4 * N + 24 * V,
                      "mc_triangles": 0 if mc_fused else 12 * T}
@@ -692,9 +751,10 @@ def main():
         traffic = None
         if traffic_path.exists():
             traffic = json.loads(traffic_path.read_text()).get(dom)
-        p4 = [k for k in ("fe_generate", "mc_vertices", "mc_triangles", "vertices") if k in per]
+        # single pass: passes 1-4 are the single kernel and the vertex kernel, over all their bytes
+        p4 = [k for k in ("fe_single", "fe_generate", "mc_vertices", "mc_triangles", "vertices") if k in per]
         p4_s = sum(per[k]["us_per_launch"] for k in p4) * 1e-6
-        p4_bytes = 4 * N + 24 * V + 12 * T
+        p4_bytes = (8 if "fe_single" in per else 4) * N + 24 * V + 12 * T
         B = 8 * N + 24 * V + 12 * T
         step_s = r["ms"] / args.steps / 1e3
         prof_ms = sum(v["ms_total"] for v in per.values())
@@ -810,6 +870,8 @@ def main():
             "ms_per_step": run2["ms"] / args.steps, "mesh": {"vertices": run2["V"], "triangles": run2["T"]},
             "roofline": roof2, "pipeline": pipe2, "pass4": p42, "gpu_launches": run2["launches"],
             "same_triangle_sequence_as_" + args.algorithm: same_tris}
+        if not args.no_io:
+            line["vtk_io"] = io_leg(M, lib, dev, vol_host, out, V, T)
         if not args.no_batched:
             line["batched"] = batched_leg(M, lib, dev, args.batched_reps)
         if not args.no_served:
