@@ -23,11 +23,9 @@
 //          and are classified into bit words ("value >= iso", set.ge per
 //          point); grid rows (jw+h, k) are counted -- cut x, y, z edges and the
 //          triangles of cell row (jw+h, k) (count_word) -- and their bit words
-//          and counts written; the item adds its rows' totals to its planes'
-//          accumulators.  No count waits for another item.  For each plane, the
-//          warp that counts its last row group (a per-plane counter) publishes
-//          the plane's totals at once (for all the planes it completed, before
-//          anything else), then scans the plane: it finds the totals of the
+//          and counts written.  No count waits for another item.  For each
+//          plane, the warp that counts its last row group (a per-plane counter)
+//          scans it: it publishes the plane's totals, finds the totals of the
 //          planes before it by a decoupled look-back over the planes (the
 //          single-pass scan of Merrill and Garland: 32 planes' flags at a time,
 //          back to the first plane that carries its inclusive prefix), writes
@@ -64,7 +62,6 @@ constexpr int kSingleCtasPerSm = 4;
 
 // Synchronisation words (zeroed before each launch):
 //   done[plane]      row groups of the plane counted so far
-//   sum[plane][2]    vertices and triangles of the row groups counted so far
 //   agg[plane][2]    vertices and triangles of the plane (ready bit 63, failed bit 62)
 //   incl[plane][2]   vertices and triangles of planes 0 .. plane (ready bit 63, failed bit 62)
 constexpr unsigned long long kFlagReady = 1ull << 63, kFlagFailed = 1ull << 62;
@@ -101,8 +98,8 @@ __host__ __device__ inline size_t single_warp_bytes(int nx, int W, int RPW)
 // Row groups of RPW rows.
 __host__ __device__ inline int single_groups(const Grid& g, int RPW) { return (g.ny + RPW - 1) / RPW; }
 
-// Layout of the synchronisation words: done[nz], sum[nz][2], agg[nz][2], incl[nz][2] (u64 each).
-__host__ __device__ inline size_t single_sync_words(const Grid& g) { return 7 * (size_t)g.nz; }
+// Layout of the synchronisation words: done[nz], agg[nz][2], incl[nz][2] (u64 each).
+__host__ __device__ inline size_t single_sync_words(const Grid& g) { return 5 * (size_t)g.nz; }
 
 template <typename IndexT, int RPW>
 __global__ void __launch_bounds__(kThreads, kSingleCtasPerSm) k_fe_single(
@@ -148,9 +145,8 @@ __global__ void __launch_bounds__(kThreads, kSingleCtasPerSm) k_fe_single(
     const int ngroups = single_groups(g, RPW);
     const int nruns = (nz + KC - 1) / KC;
     unsigned long long* done = sync;
-    unsigned long long* sum = sync + nz;
-    unsigned long long* agg = sync + 3 * (size_t)nz;
-    unsigned long long* incl = sync + 5 * (size_t)nz;
+    unsigned long long* agg = sync + nz;
+    unsigned long long* incl = sync + 3 * (size_t)nz;
     const long long nitems = (long long)(nruns + L) * ngroups;
     const bool in1 = lw + 1 < W;
     const uint32_t evalid = validmask(lw, nx - 1);  // x-edges / cells: i <= nx-2
@@ -263,13 +259,6 @@ __global__ void __launch_bounds__(kThreads, kSingleCtasPerSm) k_fe_single(
                     }
                 }
                 if (row_ok && lw == 0) rowcnt[rr] = make_uint4(rx, ry, rz, rt);
-                // the item's share of plane k's totals (each row's lane 0 holds the row)
-                const uint32_t iv = __reduce_add_sync(0xffffffffu, (row_ok && lw == 0) ? rx + ry + rz : 0u);
-                const uint32_t itr = __reduce_add_sync(0xffffffffu, (row_ok && lw == 0) ? rt : 0u);
-                if (lane == 0) {
-                    if (iv) atomicAdd(&sum[2 * k + 0], (unsigned long long)iv);
-                    if (itr) atomicAdd(&sum[2 * k + 1], (unsigned long long)itr);
-                }
                 a = c;
                 b = d;
             }
@@ -285,22 +274,37 @@ __global__ void __launch_bounds__(kThreads, kSingleCtasPerSm) k_fe_single(
                     if (atomicAdd(&done[k], 1ull) == (unsigned long long)(ngroups - 1)) lastm |= 1u << (k - k0);
             }
             lastm = __shfl_sync(0xffffffffu, lastm, 0);
-            if (lastm) {
-                __threadfence();  // the other groups' counts and sums (each fenced before its increment) are visible
-                // the totals of every plane this warp completed, published before any of them is scanned: the
-                // look-backs of later planes need only these
-                if (lane == 0) {
-                    for (uint32_t m2 = lastm; m2; m2 &= m2 - 1u) {
-                        const int k = k0 + __ffs(m2) - 1;
-                        st_release(&agg[2 * k + 0], kFlagReady | ld_acquire(&sum[2 * k + 0]));
-                        st_release(&agg[2 * k + 1], kFlagReady | ld_acquire(&sum[2 * k + 1]));
-                    }
-                }
-            }
+            if (lastm) __threadfence();  // the other groups' counts (each fenced before its increment) are visible
             for (; lastm; lastm &= lastm - 1u) {
                 // ---- scan plane k: this warp counted its last row group ----
                 const int k = k0 + __ffs(lastm) - 1;
                 const long long r0 = (long long)k * ny;
+                const int per = (ny + 31) / 32;  // consecutive rows per lane
+                unsigned long long lv = 0, lt = 0;
+                for (int u = 0; u < per; ++u) {
+                    const int jj = lane * per + u;
+                    if (jj < ny) {
+                        const uint4 cc = __ldcg(&rowcnt[r0 + jj]);
+                        lv += (unsigned long long)cc.x + cc.y + cc.z;
+                        lt += cc.w;
+                    }
+                }
+                unsigned long long iv = lv, it = lt;
+#pragma unroll
+                for (int dd = 1; dd < 32; dd <<= 1) {
+                    const unsigned long long yv = __shfl_up_sync(0xffffffffu, iv, dd);
+                    const unsigned long long yt = __shfl_up_sync(0xffffffffu, it, dd);
+                    if (lane >= dd) {
+                        iv += yv;
+                        it += yt;
+                    }
+                }
+                const unsigned long long planeV = __shfl_sync(0xffffffffu, iv, 31);
+                const unsigned long long planeT = __shfl_sync(0xffffffffu, it, 31);
+                if (lane == 0) {
+                    st_release(&agg[2 * k + 0], kFlagReady | planeV);
+                    st_release(&agg[2 * k + 1], kFlagReady | planeT);
+                }
                 // look back over the planes before k for their totals
                 unsigned long long pV = 0, pT = 0;
                 bool failed = false;
@@ -366,45 +370,24 @@ __global__ void __launch_bounds__(kThreads, kSingleCtasPerSm) k_fe_single(
                     }
                     continue;
                 }
-                // the rows' first vertex and triangle, 32 rows at a time (row c + lane), four chunks' counts
-                // loaded before they are scanned
-                unsigned long long cV = pV, cT = pT;
-                for (int c4 = 0; c4 < ny; c4 += 128) {
-                    uint4 cc[4];
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        const int jj = c4 + 32 * u + lane;
-                        cc[u] = jj < ny ? __ldcg(&rowcnt[r0 + jj]) : make_uint4(0u, 0u, 0u, 0u);
-                    }
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        const int jj = c4 + 32 * u + lane;
-                        const unsigned long long v = (unsigned long long)cc[u].x + cc[u].y + cc[u].z, t = cc[u].w;
-                        unsigned long long iv = v, it = t;
-#pragma unroll
-                        for (int dd = 1; dd < 32; dd <<= 1) {
-                            const unsigned long long yv = __shfl_up_sync(0xffffffffu, iv, dd);
-                            const unsigned long long yt = __shfl_up_sync(0xffffffffu, it, dd);
-                            if (lane >= dd) {
-                                iv += yv;
-                                it += yt;
-                            }
-                        }
-                        if (jj < ny) {
-                            starts[r0 + jj] = cV + iv - v;
-                            starts[R + r0 + jj] = cT + it - t;
-                        }
-                        cV += __shfl_sync(0xffffffffu, iv, 31);
-                        cT += __shfl_sync(0xffffffffu, it, 31);
+                unsigned long long sv = pV + iv - lv, st = pT + it - lt;  // first of the lane's rows
+                for (int u = 0; u < per; ++u) {
+                    const int jj = lane * per + u;
+                    if (jj < ny) {
+                        const uint4 cc = __ldcg(&rowcnt[r0 + jj]);
+                        starts[r0 + jj] = sv;
+                        starts[R + r0 + jj] = st;
+                        sv += (unsigned long long)cc.x + cc.y + cc.z;
+                        st += cc.w;
                     }
                 }
                 __threadfence();
                 if (lane == 0) {
-                    st_release(&incl[2 * k + 0], kFlagReady | cV);
-                    st_release(&incl[2 * k + 1], kFlagReady | cT);
+                    st_release(&incl[2 * k + 0], kFlagReady | (pV + planeV));
+                    st_release(&incl[2 * k + 1], kFlagReady | (pT + planeT));
                     if (k == nz - 1) {
-                        totals[0] = cV;
-                        totals[1] = cT;
+                        totals[0] = pV + planeV;
+                        totals[1] = pT + planeT;
                     }
                 }
             }
