@@ -116,9 +116,7 @@ enum {
     ISO_PASS_MC_VERTICES = 4,  /* pass 4, Marching Cubes vertices */
     ISO_PASS_MC_TRIANGLES = 5, /* pass 4, Marching Cubes triangles */
     ISO_PASS_VERTICES = 6,     /* pass 4, vertex points and normals from the generate pass's records */
-    ISO_PASS_FE_SINGLE = 7,    /* passes 1-4, Flying Edges in one kernel: counts, row starts (a single-pass
-                                  scan), triangles and vertex records */
-    ISO_NUM_PASSES = 8
+    ISO_NUM_PASSES = 7
 };
 iso_status iso_ctx_profile(iso_ctx* ctx, int enable);
 iso_status iso_ctx_profile_read(iso_ctx* ctx, double* ms, int64_t* launches);
@@ -152,9 +150,7 @@ iso_status iso_count_device_noalloc(iso_algorithm algo, const float* volume, con
                                     int64_t* counts, void* stream);
 
 /* Full extraction, volume and output in device memory.  Synchronises the
- * stream before returning.  If the buffers are too small nothing is written
- * past their capacities (the single-pass path of iso_ctx_set_single_pass
- * may have written part of the mesh within them),
+ * stream before returning.  If the buffers are too small nothing is written,
  * ISO_ERR_CAPACITY is returned and out->n_points / n_tris hold the sizes
  * needed.  Replaces the four passes + moveOutput() of
  * flyingEdges/serial/main.cpp:114-155 (ISO_FLYING_EDGES) and the
@@ -183,18 +179,6 @@ iso_status iso_extract_device_async(iso_ctx* ctx, iso_algorithm algo, const floa
  * while per-pass profiling (iso_ctx_profile) is on, calls take the stream
  * path.  The same capture rules as iso_extract_batch apply. */
 iso_status iso_ctx_set_graph(iso_ctx* ctx, int enable);
-
-/* Single-pass Flying Edges (no counterpart in the reference, whose four
- * passes each sweep the grid; on by default): iso_extract_device and
- * iso_extract_device_async run passes 1-4 of whole Flying Edges grids
- * (rows of at most 512 points and a multiple of 4, volume at a 16-byte
- * boundary) as one kernel -- counts, a single-pass scan of the row starts,
- * triangles and vertex records -- followed by the vertex kernel.  The output
- * is the same mesh as the pass-by-pass kernels'.  One difference: the totals
- * are known only at the end, so a mesh found too small has been written in
- * part (never past its capacities) when ISO_ERR_CAPACITY is returned.
- * enable = 0 selects the separate count, scan and generate kernels. */
-iso_status iso_ctx_set_single_pass(iso_ctx* ctx, int enable);
 
 /* Batched extraction (no counterpart in the reference, which extracts one
  * volume per call).  n requests -- each a volume in device memory with its

@@ -22,7 +22,7 @@ ISO_ERR_TOO_LARGE = 10
 ISO_NOALLOC_MAX_ROWS = 1 << 20
 ISO_NOALLOC_MAX_ROW_POINTS = 858993459
 
-PASS_NAMES = ("classify", "count", "scan", "fe_generate", "mc_vertices", "mc_triangles", "vertices", "fe_single")
+PASS_NAMES = ("classify", "count", "scan", "fe_generate", "mc_vertices", "mc_triangles", "vertices")
 
 ISO_FLYING_EDGES = 0
 ISO_MARCHING_CUBES = 1
@@ -85,7 +85,6 @@ SIGNATURES = {
     "iso_batch_set_lanes": (C.c_int, [C.c_void_p, C.c_int]),
     "iso_batch_set_graph": (C.c_int, [C.c_void_p, C.c_int]),
     "iso_ctx_set_graph": (C.c_int, [C.c_void_p, C.c_int]),
-    "iso_ctx_set_single_pass": (C.c_int, [C.c_void_p, C.c_int]),
     "iso_batch_set_split": (C.c_int, [C.c_void_p, C.c_int]),
     "iso_batch_split": (C.c_int, [C.c_void_p]),
     "iso_block_count": (C.c_int64, [C.POINTER(IsoGrid)]),

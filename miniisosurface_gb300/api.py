@@ -324,11 +324,8 @@ def extract_device(volume, dims, isoval, algorithm=FLYING_EDGES, spacing=(1, 1, 
         raise ValueError("volume must be a contiguous CUDA tensor")
     dcode = _dtype_code(volume.dtype)  # narrow types are converted to float32 on the device
     s = stream if stream is not None else torch.cuda.current_stream(volume.device).cuda_stream
-    if out is None:  # sized by a count first: a single-pass extraction into a mesh too small still runs through
-        nv, nt = (0, 0)
-        if dcode == _lib.ISO_FLOAT32:
-            nv, nt = count_device(volume, dims, isoval, algo, ctx=ctx, stream=stream)
-        out = DeviceMesh(nv, nt, index_bytes, volume.device)
+    if out is None:
+        out = DeviceMesh(0, 0, index_bytes, volume.device)
     for _ in range(2):
         m = out.descriptor()
         if dcode == _lib.ISO_FLOAT32:

@@ -130,7 +130,6 @@ std::vector<unsigned char> batch_key(const iso_ctx* ctx, int lanes, int share, c
     put(&lanes, sizeof lanes);
     put(&share, sizeof share);
     put(&ctx->reverse, sizeof ctx->reverse);
-    put(&ctx->single_pass, sizeof ctx->single_pass);
     put(&ctx->batch_arena, sizeof ctx->batch_arena);
     put(&ctx->h_batch, sizeof ctx->h_batch);
     put(&n, sizeof n);
@@ -264,7 +263,8 @@ iso_status extract_graph(iso_ctx* ctx, iso_algorithm algo, const float* volume, 
     if (cudaPointerGetAttributes(&attr, result_host) != cudaSuccess || attr.type != cudaMemoryTypeHost) {
         cudaGetLastError();
         PassMarks pm(ctx, s);
-        enqueue_extract(ctx, algo, volume, g, isoval, pl, b, out, s, pm);
+        enqueue_count(ctx, algo, volume, g, isoval, pl, b, s, pm);
+        enqueue_generate(ctx, algo, volume, g, isoval, pl, b, out, s, pm);
         ISO_CUDA(ctx, cudaGetLastError());
         ISO_CUDA(ctx,
                  cudaMemcpyAsync(result_host, b.totals, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
@@ -289,7 +289,6 @@ iso_status extract_graph(iso_ctx* ctx, iso_algorithm algo, const float* volume, 
     put(&ctx->scratch, sizeof ctx->scratch);
     put(&ctx->fe2mc, sizeof ctx->fe2mc);
     put(&ctx->reverse, sizeof ctx->reverse);
-    put(&ctx->single_pass, sizeof ctx->single_pass);
     if (!ctx->one_exec || key != ctx->one_key) {
         std::lock_guard<std::mutex> lock(g_batch_mutex);
         if (!ctx->s_capture) ISO_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->s_capture, cudaStreamNonBlocking));
@@ -298,7 +297,8 @@ iso_status extract_graph(iso_ctx* ctx, iso_algorithm algo, const float* volume, 
         cudaError_t e = cudaStreamBeginCapture(sc, cudaStreamCaptureModeRelaxed);
         if (e == cudaSuccess) {
             PassMarks pm(ctx, sc);
-            enqueue_extract(ctx, algo, volume, g, isoval, pl, b, out, sc, pm);
+            enqueue_count(ctx, algo, volume, g, isoval, pl, b, sc, pm);
+            enqueue_generate(ctx, algo, volume, g, isoval, pl, b, out, sc, pm);
             cudaMemcpyAsync(result_host, b.totals, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, sc);
             e = cudaStreamEndCapture(sc, &graph);
         }
@@ -343,13 +343,6 @@ iso_status iso_ctx_set_graph(iso_ctx* ctx, int enable)
         ctx->one_exec = nullptr;
         ctx->one_key.clear();
     }
-    return ISO_OK;
-}
-
-iso_status iso_ctx_set_single_pass(iso_ctx* ctx, int enable)
-{
-    if (!ctx) return ISO_ERR_INVALID_ARG;
-    ctx->single_pass = enable ? 1 : 0;
     return ISO_OK;
 }
 

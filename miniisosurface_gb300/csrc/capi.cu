@@ -720,7 +720,8 @@ iso_status iso_extract_device_async(iso_ctx* ctx, iso_algorithm algo, const floa
     if (ctx->one_graph && !ctx->profiling) return extract_graph(ctx, algo, volume, g, grid, isoval, pl, b, out,
                                                                 result_host, s);
     PassMarks pm(ctx, s);
-    enqueue_extract(ctx, algo, volume, g, isoval, pl, b, out, s, pm);
+    enqueue_count(ctx, algo, volume, g, isoval, pl, b, s, pm);
+    enqueue_generate(ctx, algo, volume, g, isoval, pl, b, out, s, pm);
     ISO_CUDA(ctx, cudaGetLastError());
     ISO_CUDA(ctx, cudaMemcpyAsync(result_host, b.totals, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
     return ISO_OK;

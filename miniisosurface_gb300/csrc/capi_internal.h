@@ -71,7 +71,6 @@ struct iso_ctx {
     cudaGraphExec_t batch_exec[2] = {nullptr, nullptr};
     std::vector<unsigned char> batch_key[2];
     int reverse = 1;  // pass 4 walks the planes backwards (the count pass leaves the last ones in L2)
-    int single_pass = 1;  // Flying Edges whole grids through k_fe_single (iso_ctx_set_single_pass)
     int stream_host = 1;  // iso_extract_host streams slabs (large grids)
     std::string last_error;
     // per-pass timing (iso_ctx_profile)
@@ -159,8 +158,7 @@ inline size_t scratch_size(const Grid& g, const iso::CountPlan& cp)
 {
     const size_t R = (size_t)g.R;
     return align256(R * 16) + align256(R * 8) + align256(R * 4) + align256(4 * R * 8) +
-           align256(4 * (size_t)cp.nseg * 8) + align256(8 * 8) + align256(R * (size_t)g.W * 4) +
-           align256(iso::fe_single_flag_bytes(g));
+           align256(4 * (size_t)cp.nseg * 8) + align256(8 * 8) + align256(R * (size_t)g.W * 4);
 }
 
 inline void carve(void* base, const Grid& g, const iso::CountPlan& cp, FeBuffers& b)
@@ -173,8 +171,7 @@ inline void carve(void* base, const Grid& g, const iso::CountPlan& cp, FeBuffers
     b.starts = reinterpret_cast<unsigned long long*>(p); p += align256(4 * R * 8);
     b.part = reinterpret_cast<unsigned long long*>(p); p += align256(4 * (size_t)cp.nseg * 8);
     b.totals = reinterpret_cast<unsigned long long*>(p); p += align256(8 * 8);
-    b.bits = reinterpret_cast<uint32_t*>(p); p += align256(R * (size_t)g.W * 4);
-    b.flags = reinterpret_cast<unsigned long long*>(p);
+    b.bits = reinterpret_cast<uint32_t*>(p);
 }
 
 inline iso_status ensure_scratch(iso_ctx* ctx, const Grid& g, const iso::CountPlan& cp, FeBuffers& b, cudaStream_t s)
@@ -402,30 +399,6 @@ inline void enqueue_generate(iso_ctx* ctx, iso_algorithm algo, const float* vol,
         }
         pm.mark(ISO_PASS_MC_TRIANGLES);
     }
-}
-
-// Passes 1-4 of a whole-volume extraction into the mesh buffers of `out`:
-// Flying Edges grids that k_fe_single takes run as that kernel and the
-// vertex kernel; everything else as the count pass, the scan and pass 4.
-inline void enqueue_extract(iso_ctx* ctx, iso_algorithm algo, const float* vol, const Grid& g, float iso,
-                            const Plans& pl, FeBuffers& b, const iso_mesh* out, cudaStream_t s, PassMarks& pm)
-{
-    if (algo == ISO_FLYING_EDGES && ctx->single_pass && iso::fe_single_fits(g, vol)) {
-        const long long capV = vertex_limit(out, out->cap_points);
-        const long long capT = out->cap_tris;
-        if (out->index_bytes == 4)
-            iso::launch_fe_single<uint32_t>(vol, g, iso, ctx->d_cases, b, b.flags, ctx->nsm, capV, capT, out->points,
-                                            static_cast<uint32_t*>(out->tris), s);
-        else
-            iso::launch_fe_single<uint64_t>(vol, g, iso, ctx->d_cases, b, b.flags, ctx->nsm, capV, capT, out->points,
-                                            static_cast<uint64_t*>(out->tris), s);
-        pm.mark(ISO_PASS_FE_SINGLE);
-        if (iso::launch_fe_single_vertices(vol, g, iso, b, ctx->nsm, capV, capT, out->points, out->normals, s))
-            pm.mark(ISO_PASS_VERTICES);
-        return;
-    }
-    enqueue_count(ctx, algo, vol, g, iso, pl, b, s, pm);
-    enqueue_generate(ctx, algo, vol, g, iso, pl, b, out, s, pm);
 }
 
 inline iso_status finish_counts(iso_ctx* ctx, const iso_mesh* out, long long V, long long T, long long status, int64_t* nV,

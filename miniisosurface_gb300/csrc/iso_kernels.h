@@ -23,7 +23,6 @@ struct FeBuffers {
     unsigned long long* totals = nullptr;  // 8      vertices, triangles, mc vertices, status, x cuts, y cuts
     uint32_t* bits = nullptr;              // R*W    bit rows (row-wise kernels only)
     uint32_t* fe2mc = nullptr;             // >= V   FE vertex index -> MC index
-    unsigned long long* flags = nullptr;   // synchronisation words of the single-pass kernel (fe_single.cu)
 };
 
 // Work split of the counting pass: blocks of J = 8 grid rows (a warp per
@@ -112,18 +111,6 @@ template <typename IndexT>
 void launch_fe_gen_warps(const float* vol, const Grid& g, float iso, const CaseTables* cases, const FeBuffers& b,
                          const CountPlan& cp, const GenPlan& p, long long capV, long long capT, float* points,
                          float* normals, IndexT* tris, int reverse, cudaStream_t s);
-// Flying Edges passes 1-4 in one kernel (fe_single.cu) for whole grids of
-// rows up to 16 words, 4-point multiples, 16-byte aligned volumes: counts,
-// row starts (starts[0..1][R]), totals, vertex records and triangles; then
-// launch_fe_single_vertices turns the records into vertices.
-bool fe_single_fits(const Grid& g, const float* vol);
-size_t fe_single_flag_bytes(const Grid& g);
-template <typename IndexT>
-void launch_fe_single(const float* vol, const Grid& g, float iso, const CaseTables* cases, const FeBuffers& b,
-                      unsigned long long* flags, int nsm, long long capV, long long capT, float* points, IndexT* tris,
-                      cudaStream_t s);
-bool launch_fe_single_vertices(const float* vol, const Grid& g, float iso, const FeBuffers& b, int nsm, long long capV,
-                               long long capT, float* points, float* normals, cudaStream_t s);
 bool launch_fe_vertices(const float* vol, const Grid& g, float iso, const FeBuffers& b, const GenPlan& p,
                         long long capV, long long capT, float* points, float* normals, cudaStream_t s);
 // Marching Cubes vertices from the records launch_mc_gen_warps wrote (false:
