@@ -15,8 +15,6 @@ One step = one full extraction (passes 1-4) of the volume.
             recorded between kernels on the extraction stream during a
             second timed region of K steps on the stream path (events cannot
             sit between a graph's kernels); algorithmic bytes per launch:
-              fe_single      4 N + 12 T          (volume read, uint32 triangles: passes 1-4 in one
-                                                  kernel, the vertices left to `vertices`)
               count          4 N                 (volume read; passes 1+2 fused)
               fe_generate    12 T                (uint32 triangles; with `vertices`)
                              4 N + 24 V + 12 T   (volume read, points+normals, triangles; alone)
@@ -27,8 +25,7 @@ One step = one full extraction (passes 1-4) of the volume.
               vertices       4 N + 24 V          (pass-4 volume read, points+normals)
             intermediates (bit rows, counts, vertex records, maps) count nothing;
   pass4     pass 4 as one unit: 4 N + 24 V + 12 T over the summed time of its
-            kernels (generate, vertices); with the single-pass kernel, passes
-            1-4: 8 N + 24 V + 12 T over fe_single + vertices
+            kernels (generate, vertices)
   pipeline  the whole extraction: B = 8 N + 24 V + 12 T over the step
   mc        the same volume through Marching Cubes (value, roofline,
             pipeline, per-pass split), and whether its triangle sequence equals
@@ -740,7 +737,7 @@ def main():
         # Marching Cubes over rows of up to 16 words: the owned-vertex pass also writes the triangles (FE ids),
         # and the mc_triangles pass remaps them in place (an intermediate rewrite)
         mc_fused = split and (DIMS[0] + 31) // 32 <= 16
-        alg_bytes = {"classify": 4 * N, "count": 4 * N, "scan": 0, "fe_single": 4 * N + 12 * T,
+        alg_bytes = {"classify": 4 * N, "count": 4 * N, "scan": 0,
                      "fe_generate": 12 * T if split else 4 * N + 24 * V + 12 * T, "vertices": 4 * N + 24 * V,
                      "mc_vertices": (12 * T if mc_fused else 0) if split else 4 * N + 24 * V,
                      "mc_triangles": 0 if mc_fused else 12 * T}
@@ -751,10 +748,9 @@ def main():
         traffic = None
         if traffic_path.exists():
             traffic = json.loads(traffic_path.read_text()).get(dom)
-        # single pass: passes 1-4 are the single kernel and the vertex kernel, over all their bytes
-        p4 = [k for k in ("fe_single", "fe_generate", "mc_vertices", "mc_triangles", "vertices") if k in per]
+        p4 = [k for k in ("fe_generate", "mc_vertices", "mc_triangles", "vertices") if k in per]
         p4_s = sum(per[k]["us_per_launch"] for k in p4) * 1e-6
-        p4_bytes = (8 if "fe_single" in per else 4) * N + 24 * V + 12 * T
+        p4_bytes = 4 * N + 24 * V + 12 * T
         B = 8 * N + 24 * V + 12 * T
         step_s = r["ms"] / args.steps / 1e3
         prof_ms = sum(v["ms_total"] for v in per.values())
