@@ -13,7 +13,10 @@ block statistics in one launch, and a request whose mesh was too small goes
 back to the head of the queue with the exact sizes the extraction reported.  Requests that arrive while other slots' batches
 are on the GPU are taken by the next free slot, so the batches of different
 slots overlap on the device (continuous batching); a request that does not
-fit waits at the head of the queue until memory frees up.
+fit waits at the head of the queue until memory frees up.  A slot that
+finds a single request waiting (light load) runs it with the plain calls --
+iso_count_device, a mesh of that size, iso_extract_device -- on its own
+context and stream, without the batch machinery.
 
 `run_plain` is the loop to compare with: one request at a time, in arrival
 order, iso_count_device then iso_extract_device.
@@ -126,6 +129,8 @@ class Server:
         self.index_bytes = index_bytes
         self.contexts = [Context(device) for _ in range(slots)]
         self.predictor = predictor
+        # a slot that finds a single request waiting runs it with the plain calls (no count batch, no lanes)
+        self.single_direct = True
         self.stats = None
         if predictor is not None:
             import torch
@@ -135,6 +140,45 @@ class Server:
         for c in self.contexts:  # every batch differs: lanes launched directly, no graph capture
             check(load().iso_batch_set_lanes(c.handle, int(lanes)), c.handle)
             check(load().iso_batch_set_graph(c.handle, 0), c.handle)
+
+    def _serve_one(self, i, req, requests, results, ctx, stream, state, cond, slot, t0, keep_meshes):
+        """A slot's batch of one request: iso_count_device, a mesh of that size, iso_extract_device."""
+        import torch
+
+        lib = load()
+        sh = C.c_void_p(stream.cuda_stream)
+        g = make_grid(req.dims, req.spacing, req.origin)
+        a = req.descriptor().algorithm
+        nv, nt = C.c_int64(), C.c_int64()
+        check(lib.iso_count_device(ctx.handle, a, req.volume.data_ptr(), C.byref(g), C.c_float(req.isoval),
+                                   C.byref(nv), C.byref(nt), sh), ctx.handle)
+        with cond:
+            while True:
+                k, nbytes = admit([(nv.value, nt.value)], state["in_use"], self.budget, self.index_bytes)
+                if k > 0 or state["error"]:
+                    break
+                cond.wait()
+            if k == 0:
+                return
+            state["in_use"] += nbytes
+            batch_no = state["batches"]
+            state["batches"] += 1
+        with torch.cuda.stream(stream):
+            m = DeviceMesh(nv.value, nt.value, self.index_bytes, torch.device("cuda", self.device))
+        d = m.descriptor()
+        check(lib.iso_extract_device(ctx.handle, a, req.volume.data_ptr(), C.byref(g), C.c_float(req.isoval),
+                                     C.byref(d), sh), ctx.handle)
+        done = time.perf_counter() - t0
+        m.n_points, m.n_tris = d.n_points, d.n_tris
+        r = results[i]
+        r.done = done
+        r.n_points, r.n_tris = m.n_points, m.n_tris
+        r.mesh = m if keep_meshes else None
+        r.slot, r.batch = slot, batch_no
+        del m
+        with cond:
+            state["in_use"] -= nbytes
+            cond.notify_all()
 
     def run(self, requests, keep_meshes=False):
         """Serve `requests` = [(arrival seconds, volume index, isovalue, algorithm)] in real time.
@@ -163,6 +207,12 @@ class Server:
                         take = [queue.popleft() for _ in range(min(len(queue), self.max_batch))]
                     reqs = [_request(self.volumes, *requests[i][1:]) for i in take]
                     n = len(reqs)
+                    if n == 1 and self.single_direct:
+                        # one request waiting (light load): the plain calls on this slot's context -- an exact
+                        # count and the extraction -- with none of the batch machinery around them
+                        self._serve_one(take[0], reqs[0], requests, results, ctx, stream, state, cond, slot, t0,
+                                        keep_meshes)
+                        continue
                     if self.predictor is not None:
                         guess = [i for i in take if i not in exact]
                         caps = self.predictor.capacities(

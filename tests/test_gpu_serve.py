@@ -51,6 +51,14 @@ def test_served_equals_alone_and_plain(M):
     served = server.run(reqs, keep_meshes=True)
     plain = serve.run_plain(volumes, reqs, keep_meshes=True)
     assert max(np.bincount([r.batch for r in served])) > 1, "no batch held more than one request"
+    # light load: one request at a time through the plain calls on a slot, the same meshes
+    slow = [(float(t) * 40.0, vi, iso, algo) for t, vi, iso, algo in reqs[:6]]
+    light = server.run(slow, keep_meshes=True)
+    for i, (t, vi, iso, algo) in enumerate(slow):
+        ref = M.extract_device(volumes[vi][0], volumes[vi][1], iso, algo)
+        assert (light[i].n_points, light[i].n_tris) == (ref.n_points, ref.n_tris)
+        for x, y in zip(as_np(light[i].mesh), as_np(ref)):
+            assert np.array_equal(x, y), "light-load request %d differs" % i
     assert len({r.slot for r in served}) == 2, "one slot did all the work"
     for i, (t, vi, iso, algo) in enumerate(reqs):
         alone = M.extract_device(volumes[vi][0], volumes[vi][1], iso, algo)
