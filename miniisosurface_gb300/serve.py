@@ -16,7 +16,9 @@ slots overlap on the device (continuous batching); a request that does not
 fit waits at the head of the queue until memory frees up.  A slot that
 finds a single request waiting (light load) runs it with the plain calls --
 iso_count_device, a mesh of that size, iso_extract_device -- on its own
-context and stream, without the batch machinery.
+context and stream, without the batch machinery; and a request that arrives
+while the queue is empty and no slot is working is run that way at once by
+the thread that receives it, with no hand-off to a slot.
 
 `run_plain` is the loop to compare with: one request at a time, in arrival
 order, iso_count_device then iso_extract_device.
@@ -128,6 +130,10 @@ class Server:
         self.device = device
         self.index_bytes = index_bytes
         self.contexts = [Context(device) for _ in range(slots)]
+        # light load: a request that arrives while the queue is empty and no slot is working is run at once by
+        # the thread that receives it (no hand-off to a slot), with the plain calls on this context
+        self.inline_ctx = Context(device)
+        self.inline_idle = True
         self.predictor = predictor
         # a slot that finds a single request waiting runs it with the plain calls (no count batch, no lanes)
         self.single_direct = True
@@ -141,7 +147,7 @@ class Server:
             check(load().iso_batch_set_lanes(c.handle, int(lanes)), c.handle)
             check(load().iso_batch_set_graph(c.handle, 0), c.handle)
 
-    def _serve_one(self, i, req, requests, results, ctx, stream, state, cond, slot, t0, keep_meshes):
+    def _serve_one(self, i, req, results, ctx, stream, state, cond, slot, t0, keep_meshes):
         """A slot's batch of one request: iso_count_device, a mesh of that size, iso_extract_device."""
         import torch
 
@@ -190,7 +196,7 @@ class Server:
         results = [None] * len(requests)
         queue = collections.deque()
         cond = threading.Condition()
-        state = {"fed": False, "in_use": 0, "error": None, "batches": 0, "fallbacks": 0}
+        state = {"fed": False, "in_use": 0, "error": None, "batches": 0, "fallbacks": 0, "busy": 0}
         exact = {}  # request -> exact (n_points, n_tris) after a mesh came out too small
         t0 = time.perf_counter() + 0.002
 
@@ -205,13 +211,16 @@ class Server:
                         if state["error"] or (not queue and state["fed"]):
                             return
                         take = [queue.popleft() for _ in range(min(len(queue), self.max_batch))]
+                        state["busy"] += 1
                     reqs = [_request(self.volumes, *requests[i][1:]) for i in take]
                     n = len(reqs)
                     if n == 1 and self.single_direct:
                         # one request waiting (light load): the plain calls on this slot's context -- an exact
                         # count and the extraction -- with none of the batch machinery around them
-                        self._serve_one(take[0], reqs[0], requests, results, ctx, stream, state, cond, slot, t0,
-                                        keep_meshes)
+                        self._serve_one(take[0], reqs[0], results, ctx, stream, state, cond, slot, t0, keep_meshes)
+                        with cond:
+                            state["busy"] -= 1
+                            cond.notify_all()
                         continue
                     if self.predictor is not None:
                         guess = [i for i in take if i not in exact]
@@ -269,6 +278,7 @@ class Server:
                     del meshes
                     with cond:
                         state["in_use"] -= nbytes
+                        state["busy"] -= 1
                         cond.notify_all()
             except BaseException as e:  # surfaced by run()
                 with cond:
@@ -287,8 +297,26 @@ class Server:
             with cond:
                 if state["error"]:
                     break
-                queue.append(i)
-                cond.notify_all()
+                inline = self.inline_idle and not queue and state["busy"] == 0
+                if inline:
+                    state["busy"] += 1  # the slots leave it alone
+                else:
+                    queue.append(i)
+                    cond.notify_all()
+            if inline:
+                failed = None
+                try:
+                    self._serve_one(i, _request(self.volumes, *requests[i][1:]), results, self.inline_ctx,
+                                    torch.cuda.current_stream(self.device), state, cond, -1, t0, keep_meshes)
+                except BaseException as e:  # surfaced after the slots have stopped
+                    failed = e
+                with cond:
+                    state["busy"] -= 1
+                    if failed is not None:
+                        state["error"] = failed
+                    cond.notify_all()
+                if failed is not None:
+                    break
         with cond:
             state["fed"] = True
             cond.notify_all()

@@ -59,7 +59,7 @@ def test_served_equals_alone_and_plain(M):
         assert (light[i].n_points, light[i].n_tris) == (ref.n_points, ref.n_tris)
         for x, y in zip(as_np(light[i].mesh), as_np(ref)):
             assert np.array_equal(x, y), "light-load request %d differs" % i
-    assert len({r.slot for r in served}) == 2, "one slot did all the work"
+    assert len({r.slot for r in served if r.slot >= 0}) == 2, "one slot did all the work"
     for i, (t, vi, iso, algo) in enumerate(reqs):
         alone = M.extract_device(volumes[vi][0], volumes[vi][1], iso, algo)
         a = as_np(alone)
