@@ -39,6 +39,10 @@ One step = one full extraction (passes 1-4) of the volume.
   parity    the timed FE and MC meshes against the oracle, bit for bit, and the
             FE points and normals against the reference's formulas evaluated
             in float64 (max absolute, relative and ulp error)
+  typed_device  the grid as int16 samples resident on the device:
+            iso_extract_device_typed reading them as they are (narrow reads),
+            the same call converting to a float32 copy first, and the float32
+            volume, ms per synchronising call
   vtk_io    VTK legacy file IO: the volume read from a .vtk file into pinned
             memory and copied to the device, the mesh copied back and written
             as the reference's .vtk, in GB/s of file bytes
@@ -101,6 +105,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-io", action="store_true")
+    ap.add_argument("--no-typed", action="store_true")
     ap.add_argument("--batched-reps", type=int, default=5)
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--served-requests", type=int, default=160)
@@ -459,6 +464,58 @@ def batched_leg(M, lib, dev, reps):
         "speedup_vs_plain": t_plain / t_batch, "speedup_vs_plain_async": t_async / t_batch,
         "identical_output": same,
     }
+
+
+def typed_device_leg(M, lib, dev, ctx, vol_host, V, T, steps=20):
+    """The bench grid as int16 samples resident on the device (noise x 8192,
+    rounded; f4): iso_extract_device_typed reading the samples as they are
+    (narrow reads), the same call converting them to a float32 copy first
+    (iso_ctx_set_narrow(ctx, 0)), and iso_extract_device on the float32
+    volume, each call synchronising, ms per extraction (CUDA events)."""
+    import torch
+    from miniisosurface_gb300 import _lib
+
+    vol16 = np.clip(np.round(vol_host * 8192.0), -32768, 32767).astype(np.int16)
+    d16 = torch.from_numpy(vol16.reshape(-1)).to(dev)
+    d32 = torch.from_numpy(vol_host.reshape(-1)).to(dev)
+    grid = M.make_grid(DIMS)
+    iso16 = float(ISO) * 8192.0
+    n16 = M.count_device(d16.float(), DIMS, iso16, ctx=ctx)
+    out = M.DeviceMesh(max(V, n16[0]), max(T, n16[1]), 4, dev)
+    desc = out.descriptor()
+    stream = torch.cuda.current_stream(dev)
+    sh = C.c_void_p(stream.cuda_stream)
+
+    def timed(fn):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    def typed():
+        _lib.check(lib.iso_extract_device_typed(ctx.handle, M.FLYING_EDGES, d16.data_ptr(), _lib.ISO_INT16,
+                                                C.byref(grid), C.c_float(iso16), C.byref(desc), sh), ctx.handle)
+
+    def plain32():
+        _lib.check(lib.iso_extract_device(ctx.handle, M.FLYING_EDGES, d32.data_ptr(), C.byref(grid), C.c_float(ISO),
+                                          C.byref(desc), sh), ctx.handle)
+
+    t_narrow = timed(typed)
+    nv, nt = desc.n_points, desc.n_tris
+    lib.iso_ctx_set_narrow(ctx.handle, 0)
+    t_conv = timed(typed)
+    lib.iso_ctx_set_narrow(ctx.handle, 1)
+    t_f32 = timed(plain32)
+    return {"field": "the bench noise x 8192, rounded to int16", "vertices": nv, "triangles": nt,
+            "int16_narrow_ms": t_narrow, "int16_converted_ms": t_conv, "float32_ms": t_f32,
+            "value_int16_narrow": cells() / (t_narrow / 1e3) / 1e6, "unit": METRIC,
+            "what": "one synchronising call per extraction, volume resident"}
 
 
 def io_leg(M, lib, dev, vol_host, mesh, V, T, reps=3):
@@ -868,6 +925,8 @@ def main():
             "same_triangle_sequence_as_" + args.algorithm: same_tris}
         if not args.no_io:
             line["vtk_io"] = io_leg(M, lib, dev, vol_host, out, V, T)
+        if not args.no_typed:
+            line["typed_device"] = typed_device_leg(M, lib, dev, ctx, vol_host, V, T)
         if not args.no_batched:
             line["batched"] = batched_leg(M, lib, dev, args.batched_reps)
         if not args.no_served:

@@ -318,6 +318,14 @@ iso_status iso_extract_slab(iso_ctx* ctx, iso_algorithm algo, const float* volum
  * (_host_typed); otherwise as iso_extract_device / iso_extract_host. */
 iso_status iso_extract_device_typed(iso_ctx* ctx, iso_algorithm algo, const void* volume, iso_dtype dtype,
                                     const iso_grid* grid, float isoval, iso_mesh* out, void* stream);
+/* Narrow reads for iso_extract_device_typed (no counterpart in the reference;
+ * on by default): 8- and 16-bit samples are read as they are by the count and
+ * vertex passes -- no float32 copy of the volume -- for Flying Edges and
+ * Marching Cubes over grids of rows of at most 512 points whose byte length is
+ * a multiple of 16, with the volume at a 16-byte boundary.  The samples are
+ * classified as the reference classifies their float conversion, so the mesh
+ * is the one the converted volume gives.  enable = 0 converts first. */
+iso_status iso_ctx_set_narrow(iso_ctx* ctx, int enable);
 iso_status iso_extract_host_typed(iso_ctx* ctx, iso_algorithm algo, const void* volume, iso_dtype dtype,
                                   const iso_grid* grid, float isoval, iso_mesh* out, void* stream);
 

@@ -85,6 +85,7 @@ SIGNATURES = {
     "iso_batch_set_lanes": (C.c_int, [C.c_void_p, C.c_int]),
     "iso_batch_set_graph": (C.c_int, [C.c_void_p, C.c_int]),
     "iso_ctx_set_graph": (C.c_int, [C.c_void_p, C.c_int]),
+    "iso_ctx_set_narrow": (C.c_int, [C.c_void_p, C.c_int]),
     "iso_batch_set_split": (C.c_int, [C.c_void_p, C.c_int]),
     "iso_batch_split": (C.c_int, [C.c_void_p]),
     "iso_block_count": (C.c_int64, [C.POINTER(IsoGrid)]),

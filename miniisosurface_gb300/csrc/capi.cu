@@ -846,6 +846,69 @@ iso_status iso_extract_host_typed(iso_ctx* ctx, iso_algorithm algo, const void* 
     return extract_host_impl(ctx, algo, volume, dtype, grid, isoval, out, stream);
 }
 
+// 8- and 16-bit samples read as they are (count_narrow.cu, k_vertices over the
+// sample type): Flying Edges and Marching Cubes over whole grids that
+// narrow_fits takes, with the scan and the generate passes of the float path.
+static iso_status extract_device_narrow(iso_ctx* ctx, iso_algorithm algo, const void* volume, int dtype,
+                                        const Grid& g, float isoval, iso_mesh* out, cudaStream_t s)
+{
+    const Plans pl = make_plans(ctx, g);
+    FeBuffers b;
+    iso_status st = ensure_scratch(ctx, g, pl.cp, b, s);
+    if (st != ISO_OK) return st;
+    const bool mc = algo == ISO_MARCHING_CUBES;
+    const long long capV = vertex_limit(out, out->cap_points);
+    const long long capT = out->cap_tris;
+    const bool i4 = out->index_bytes == 4;
+    PassMarks pm(ctx, s);
+    iso::launch_count_narrow(volume, dtype, g, isoval, mc, pl.cp, b, s);
+    pm.mark(ISO_PASS_COUNT);
+    iso::launch_scan(g, pl.cp, mc ? iso::kScanMC : iso::kScanFE, b, s);
+    pm.mark(ISO_PASS_SCAN);
+    if (!mc) {
+        if (i4)
+            iso::launch_fe_gen_warps<uint32_t>(nullptr, g, isoval, ctx->d_cases, b, pl.cp, pl.gp, capV, capT, out->points,
+                                               out->normals, static_cast<uint32_t*>(out->tris), ctx->reverse, s);
+        else
+            iso::launch_fe_gen_warps<uint64_t>(nullptr, g, isoval, ctx->d_cases, b, pl.cp, pl.gp, capV, capT, out->points,
+                                               out->normals, static_cast<uint64_t*>(out->tris), ctx->reverse, s);
+        pm.mark(ISO_PASS_FE_GENERATE);
+        if (iso::launch_fe_vertices_narrow(volume, dtype, g, isoval, b, pl.gp, capV, capT, out->points, out->normals, s))
+            pm.mark(ISO_PASS_VERTICES);
+    } else {
+        st = ensure_fe2mc(ctx, out->cap_points, s);
+        if (st != ISO_OK) return st;
+        b.fe2mc = ctx->fe2mc;
+        const long long capM = capV < 0xffffffffll ? capV : 0xffffffffll;  // fe2mc holds 32-bit ids
+        if (i4)
+            iso::launch_mc_gen_tris<uint32_t>(g, ctx->d_cases, b, pl.cp, pl.gp, capM, capT, out->points,
+                                              static_cast<uint32_t*>(out->tris), ctx->reverse, s);
+        else
+            iso::launch_mc_gen_tris<uint64_t>(g, ctx->d_cases, b, pl.cp, pl.gp, capM, capT, out->points,
+                                              static_cast<uint64_t*>(out->tris), ctx->reverse, s);
+        pm.mark(ISO_PASS_MC_VERTICES);
+        if (iso::launch_mc_vertices_narrow(volume, dtype, g, isoval, b, pl.gp, capM, capT, out->points, out->normals, s))
+            pm.mark(ISO_PASS_VERTICES);
+        if (i4)
+            iso::launch_mc_remap<uint32_t>(b, pl.gp, capM, capT, static_cast<uint32_t*>(out->tris), s);
+        else
+            iso::launch_mc_remap<uint64_t>(b, pl.gp, capM, capT, static_cast<uint64_t*>(out->tris), s);
+        pm.mark(ISO_PASS_MC_TRIANGLES);
+    }
+    ISO_CUDA(ctx, cudaGetLastError());
+    int64_t* res = reinterpret_cast<int64_t*>(ctx->h_totals);
+    ISO_CUDA(ctx, cudaMemcpyAsync(res, b.totals, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    ISO_CUDA(ctx, cudaStreamSynchronize(s));
+    return finish_counts(ctx, out, res[0], res[1], res[3], &out->n_points, &out->n_tris);
+}
+
+iso_status iso_ctx_set_narrow(iso_ctx* ctx, int enable)
+{
+    if (!ctx) return ISO_ERR_INVALID_ARG;
+    ctx->narrow = enable ? 1 : 0;
+    return ISO_OK;
+}
+
 iso_status iso_extract_device_typed(iso_ctx* ctx, iso_algorithm algo, const void* volume, iso_dtype dtype,
                                     const iso_grid* grid, float isoval, iso_mesh* out, void* stream)
 {
@@ -857,6 +920,14 @@ iso_status iso_extract_device_typed(iso_ctx* ctx, iso_algorithm algo, const void
     if (empty_grid(g) || !volume) return iso_extract_device(ctx, algo, nullptr, grid, isoval, out, stream);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     ISO_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (ctx->narrow && algo != ISO_MC_DUPFREE && iso::narrow_fits(g, volume, dtype)) {
+        iso_status st = check_mesh(out);
+        if (st != ISO_OK) return st;
+        out->n_points = out->n_tris = 0;
+        const Plans pl = make_plans(ctx, g);
+        if (pl.gp.fits && (algo == ISO_FLYING_EDGES || iso::mc_fused(g, pl.gp)))
+            return extract_device_narrow(ctx, algo, volume, dtype, g, isoval, out, s);
+    }
     const long long n = (long long)g.nx * g.ny * g.nz;
     if ((size_t)n * 4 > ctx->d_volume_bytes) {
         ISO_CUDA(ctx, cudaStreamSynchronize(s));

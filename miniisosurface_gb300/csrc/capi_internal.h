@@ -71,6 +71,7 @@ struct iso_ctx {
     cudaGraphExec_t batch_exec[2] = {nullptr, nullptr};
     std::vector<unsigned char> batch_key[2];
     int reverse = 1;  // pass 4 walks the planes backwards (the count pass leaves the last ones in L2)
+    int narrow = 1;   // iso_extract_device_typed reads 8- and 16-bit samples as they are (iso_ctx_set_narrow)
     int stream_host = 1;  // iso_extract_host streams slabs (large grids)
     std::string last_error;
     // per-pass timing (iso_ctx_profile)

@@ -1,6 +1,7 @@
 // Flying Edges pass 4 (two or four rows per warp, gen_pairs.cuh, for rows of up to 16
 // words; else one row per warp, gen_warps.cuh) and the plan of the
 // warp-per-row kernels.
+#include "../../include/miniiso.h"
 #include "gen_pairs.cuh"
 #include "gen_warps.cuh"
 
@@ -64,6 +65,32 @@ bool launch_fe_vertices(const float* vol, const Grid& g, float iso, const FeBuff
 {
     if (!fe_writes_records(g, p)) return false;
     launch_vertices_impl<false, 0>(vol, g, iso, b, p.kbeg, p.kend, p.nsm, capV, capT, points, normals, s);
+    return true;
+}
+
+bool launch_fe_vertices_narrow(const void* vol, int dtype, const Grid& g, float iso, const FeBuffers& b,
+                               const GenPlan& p, long long capV, long long capT, float* points, float* normals,
+                               cudaStream_t s)
+{
+    if (!fe_writes_records(g, p)) return false;
+    switch (dtype) {
+        case ISO_INT8:
+            launch_vertices_impl<false, 0, int8_t>(static_cast<const int8_t*>(vol), g, iso, b, p.kbeg, p.kend, p.nsm,
+                                                   capV, capT, points, normals, s);
+            break;
+        case ISO_UINT8:
+            launch_vertices_impl<false, 0, uint8_t>(static_cast<const uint8_t*>(vol), g, iso, b, p.kbeg, p.kend, p.nsm,
+                                                    capV, capT, points, normals, s);
+            break;
+        case ISO_INT16:
+            launch_vertices_impl<false, 0, int16_t>(static_cast<const int16_t*>(vol), g, iso, b, p.kbeg, p.kend, p.nsm,
+                                                    capV, capT, points, normals, s);
+            break;
+        default:
+            launch_vertices_impl<false, 0, uint16_t>(static_cast<const uint16_t*>(vol), g, iso, b, p.kbeg, p.kend,
+                                                     p.nsm, capV, capT, points, normals, s);
+            break;
+    }
     return true;
 }
 

@@ -3,6 +3,7 @@
 // in owner order with the Flying Edges -> MC index map, the vertices from the
 // records (vertices.cuh), then the triangles with their corners mapped; and
 // the duplicate-free order in one pass.
+#include "../../include/miniiso.h"
 #include "gen_pairs.cuh"
 #include "gen_warps.cuh"
 #include "vertices.cuh"
@@ -25,6 +26,32 @@ bool launch_mc_vertices(const float* vol, const Grid& g, float iso, const FeBuff
 {
     if (p.nsm <= 0) return false;
     launch_vertices_impl<true, 2>(vol, g, iso, b, p.kemit, p.kend, p.nsm, capV, capT, points, normals, s);
+    return true;
+}
+
+bool launch_mc_vertices_narrow(const void* vol, int dtype, const Grid& g, float iso, const FeBuffers& b,
+                               const GenPlan& p, long long capV, long long capT, float* points, float* normals,
+                               cudaStream_t s)
+{
+    if (p.nsm <= 0) return false;
+    switch (dtype) {
+        case ISO_INT8:
+            launch_vertices_impl<true, 2, int8_t>(static_cast<const int8_t*>(vol), g, iso, b, p.kemit, p.kend, p.nsm,
+                                                  capV, capT, points, normals, s);
+            break;
+        case ISO_UINT8:
+            launch_vertices_impl<true, 2, uint8_t>(static_cast<const uint8_t*>(vol), g, iso, b, p.kemit, p.kend, p.nsm,
+                                                   capV, capT, points, normals, s);
+            break;
+        case ISO_INT16:
+            launch_vertices_impl<true, 2, int16_t>(static_cast<const int16_t*>(vol), g, iso, b, p.kemit, p.kend, p.nsm,
+                                                   capV, capT, points, normals, s);
+            break;
+        default:
+            launch_vertices_impl<true, 2, uint16_t>(static_cast<const uint16_t*>(vol), g, iso, b, p.kemit, p.kend,
+                                                    p.nsm, capV, capT, points, normals, s);
+            break;
+    }
     return true;
 }
 

@@ -111,6 +111,19 @@ template <typename IndexT>
 void launch_fe_gen_warps(const float* vol, const Grid& g, float iso, const CaseTables* cases, const FeBuffers& b,
                          const CountPlan& cp, const GenPlan& p, long long capV, long long capT, float* points,
                          float* normals, IndexT* tris, int reverse, cudaStream_t s);
+// 8- and 16-bit samples read as they are (count_narrow.cu): whole grids of
+// rows up to 16 words whose byte length is a multiple of 16, the volume at a
+// 16-byte boundary.  The count pass over the samples, then the usual scan and
+// generate pass, then the vertex pass over the same samples.
+bool narrow_fits(const Grid& g, const void* vol, int dtype);
+void launch_count_narrow(const void* vol, int dtype, const Grid& g, float iso, bool mc, const CountPlan& p,
+                         FeBuffers& b, cudaStream_t s);
+bool launch_fe_vertices_narrow(const void* vol, int dtype, const Grid& g, float iso, const FeBuffers& b,
+                               const GenPlan& p, long long capV, long long capT, float* points, float* normals,
+                               cudaStream_t s);
+bool launch_mc_vertices_narrow(const void* vol, int dtype, const Grid& g, float iso, const FeBuffers& b,
+                               const GenPlan& p, long long capV, long long capT, float* points, float* normals,
+                               cudaStream_t s);
 bool launch_fe_vertices(const float* vol, const Grid& g, float iso, const FeBuffers& b, const GenPlan& p,
                         long long capV, long long capT, float* points, float* normals, cudaStream_t s);
 // Marching Cubes vertices from the records launch_mc_gen_warps wrote (false:

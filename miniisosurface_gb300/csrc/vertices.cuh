@@ -32,28 +32,37 @@ __device__ __forceinline__ void put_vertex_record(float* points, unsigned long l
 // operations of vertex_axis<a> on the same operands, so bit-identical to it
 // and to edge_vertex; written once for all three axes with the axis as data: a
 // warp of consecutive vertex ids mixes axes without diverging.
-__device__ __forceinline__ void vertex_any_axis(const float* __restrict__ vol, const Grid& g, const GradScale& gs,
+// A sample as the reference sees it: converted to float by a C cast
+// (flyingEdges/util/ConvertBuffer.h:45-72; exact for 8- and 16-bit samples).
+template <typename S>
+__device__ __forceinline__ float sample(const S* p)
+{
+    return (float)__ldg(p);
+}
+
+template <typename S>
+__device__ __forceinline__ void vertex_any_axis(const S* __restrict__ vol, const Grid& g, const GradScale& gs,
                                                 float iso, int a, int i, int j, int kk, int ci, int cj, int ck,
                                                 float3& pos, float3& nrm)
 {
     const long long sy = g.nx, sz = (long long)g.nx * g.ny;
-    const float* p0 = vol + ((long long)(kk - g.kd) * g.ny + j) * g.nx + i;
-    const float* p1 = p0 + (a == 0 ? 1 : (a == 1 ? sy : sz));
+    const S* p0 = vol + ((long long)(kk - g.kd) * g.ny + j) * g.nx + i;
+    const S* p1 = p0 + (a == 0 ? 1 : (a == 1 ? sy : sz));
     const int i1 = i + (a == 0), j1 = j + (a == 1), k1 = kk + (a == 2);
-    const float v0 = __ldg(p0), v1 = __ldg(p1);
+    const float v0 = sample(p0), v1 = sample(p1);
     // neighbours of P0 and P1 = P0 + e_a; the edge's own values stand in along a
-    const float xm0 = i > 0 ? __ldg(p0 - 1) : 0.f;
-    const float xp0 = a == 0 ? v1 : (i < g.nx - 1 ? __ldg(p0 + 1) : 0.f);
-    const float ym0 = j > 0 ? __ldg(p0 - sy) : 0.f;
-    const float yp0 = a == 1 ? v1 : (j < g.ny - 1 ? __ldg(p0 + sy) : 0.f);
-    const float zm0 = kk > 0 ? __ldg(p0 - sz) : 0.f;
-    const float zp0 = a == 2 ? v1 : (kk < g.nz - 1 ? __ldg(p0 + sz) : 0.f);
-    const float xm1 = a == 0 ? v0 : (i1 > 0 ? __ldg(p1 - 1) : 0.f);
-    const float xp1 = i1 < g.nx - 1 ? __ldg(p1 + 1) : 0.f;
-    const float ym1 = a == 1 ? v0 : (j1 > 0 ? __ldg(p1 - sy) : 0.f);
-    const float yp1 = j1 < g.ny - 1 ? __ldg(p1 + sy) : 0.f;
-    const float zm1 = a == 2 ? v0 : (k1 > 0 ? __ldg(p1 - sz) : 0.f);
-    const float zp1 = k1 < g.nz - 1 ? __ldg(p1 + sz) : 0.f;
+    const float xm0 = i > 0 ? sample(p0 - 1) : 0.f;
+    const float xp0 = a == 0 ? v1 : (i < g.nx - 1 ? sample(p0 + 1) : 0.f);
+    const float ym0 = j > 0 ? sample(p0 - sy) : 0.f;
+    const float yp0 = a == 1 ? v1 : (j < g.ny - 1 ? sample(p0 + sy) : 0.f);
+    const float zm0 = kk > 0 ? sample(p0 - sz) : 0.f;
+    const float zp0 = a == 2 ? v1 : (kk < g.nz - 1 ? sample(p0 + sz) : 0.f);
+    const float xm1 = a == 0 ? v0 : (i1 > 0 ? sample(p1 - 1) : 0.f);
+    const float xp1 = i1 < g.nx - 1 ? sample(p1 + 1) : 0.f;
+    const float ym1 = a == 1 ? v0 : (j1 > 0 ? sample(p1 - sy) : 0.f);
+    const float yp1 = j1 < g.ny - 1 ? sample(p1 + sy) : 0.f;
+    const float zm1 = a == 2 ? v0 : (k1 > 0 ? sample(p1 - sz) : 0.f);
+    const float zp1 = k1 < g.nz - 1 ? sample(p1 + sz) : 0.f;
     const float3 g0 = grad3(xm0, xp0, ym0, yp0, zm0, zp0, v0, i, j, kk, g, gs);
     const float3 g1 = grad3(xm1, xp1, ym1, yp1, zm1, zp1, v1, i1, j1, k1, g, gs);
     const float w = fdiv(fsub(iso, v0), fsub(v1, v0));
@@ -83,9 +92,9 @@ __device__ __forceinline__ uint2 vertex_record(const float* points, unsigned lon
 // -- one thread each, slot v = vertex vbase + v.  MC: the records carry the
 // owner cell.  The capacity test is the generate kernels': when it fails they
 // wrote no record and nothing is read here.
-template <bool MC, int COMP>
+template <bool MC, int COMP, typename S = float>
 __global__ void __launch_bounds__(kThreads, vertex_ctas_per_sm(MC))
-    k_vertices(const float* __restrict__ vol, Grid g, GradScale gs, float iso, int kbeg, int kend,
+    k_vertices(const S* __restrict__ vol, Grid g, GradScale gs, float iso, int kbeg, int kend,
                const unsigned long long* __restrict__ starts, const unsigned long long* __restrict__ totals,
                long long capV, long long capT, float* __restrict__ points, float* __restrict__ normals)
 {
@@ -119,14 +128,14 @@ __global__ void __launch_bounds__(kThreads, vertex_ctas_per_sm(MC))
             ck < 0 || ci > g.nx - 2 || cj > g.ny - 2 || (MC ? (ck < kbeg || ck >= kend) : (kk < kbeg || kk >= kend)))
             continue;
         float3 p, nm;
-        vertex_any_axis(vol, g, gs, iso, a, i, j, kk, ci, cj, ck, p, nm);
+        vertex_any_axis<S>(vol, g, gs, iso, a, i, j, kk, ci, cj, ck, p, nm);
         store_vertex(points, normals, v, p, nm);
     }
 }
 
 // Vertices of the rows of planes [k0, k1) from their records.
-template <bool MC, int COMP>
-inline void launch_vertices_impl(const float* vol, const Grid& g, float iso, const FeBuffers& b, int k0, int k1,
+template <bool MC, int COMP, typename S = float>
+inline void launch_vertices_impl(const S* vol, const Grid& g, float iso, const FeBuffers& b, int k0, int k1,
                                  int nsm, long long capV, long long capT, float* points, float* normals,
                                  cudaStream_t s)
 {
@@ -134,7 +143,7 @@ inline void launch_vertices_impl(const float* vol, const Grid& g, float iso, con
     // one wave, or fewer CTAs when the mesh cannot hold that many vertices (small grids in a batch)
     const long long wave = (long long)nsm * vertex_ctas_per_sm(MC);
     const unsigned blocks = (unsigned)std::min(wave, (capV + kThreads - 1) / kThreads);
-    k_vertices<MC, COMP><<<blocks, kThreads, 0, s>>>(vol, g, make_grad_scale(g), iso, k0, k1, b.starts, b.totals, capV,
+    k_vertices<MC, COMP, S><<<blocks, kThreads, 0, s>>>(vol, g, make_grad_scale(g), iso, k0, k1, b.starts, b.totals, capV,
                                                capT, points, normals);
 }
 
