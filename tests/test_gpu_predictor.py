@@ -127,7 +127,7 @@ def test_served_with_predictor_equals_alone(M, trained):
     small = P.Predictor(pred.params, margin_t=0.3, v_per_t=0.3, slack=0)
     for p in (pred, small):
         server = serve.Server(volumes, slots=2, max_batch=6, lanes=2, predictor=p)
-        server.single_direct = False  # every request through the network-sized batches
+        server.inline_idle = server.single_direct = False  # every request through the network-sized batches
         res = server.run(reqs, keep_meshes=True)
         if p is small:
             assert server.last_fallbacks > 0
