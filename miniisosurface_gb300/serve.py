@@ -17,8 +17,9 @@ fit waits at the head of the queue until memory frees up.  A slot that
 finds a single request waiting (light load) runs it with the plain calls --
 iso_count_device, a mesh of that size, iso_extract_device -- on its own
 context and stream, without the batch machinery; and a request that arrives
-while the queue is empty and no slot is working is run that way at once by
-the thread that receives it, with no hand-off to a slot.
+while the queue is empty, no slot is working and no later request is due yet
+is run that way at once by the thread that receives it, with no hand-off to
+a slot.
 
 `run_plain` is the loop to compare with: one request at a time, in arrival
 order, iso_count_device then iso_extract_device.
@@ -130,9 +131,9 @@ class Server:
         self.device = device
         self.index_bytes = index_bytes
         self.contexts = [Context(device) for _ in range(slots)]
-        # light load: a request that arrives while the queue is empty and no slot is working is run at once by
-        # the thread that receives it (no hand-off to a slot), with the plain calls on this context
-        self.inline_ctx = Context(device)
+        # light load: a request that arrives while the queue is empty, no slot is working and no later request
+        # is due yet is run at once by the thread that receives it (no hand-off to a slot), with the plain
+        # calls on slot 0's context (no slot runs meanwhile)
         self.inline_idle = True
         self.predictor = predictor
         # a slot that finds a single request waiting runs it with the plain calls (no count batch, no lanes)
@@ -288,7 +289,7 @@ class Server:
         threads = [threading.Thread(target=worker, args=(s,), daemon=True) for s in range(self.slots)]
         for th in threads:
             th.start()
-        for i in order:
+        for pos, i in enumerate(order):
             arrival = requests[i][0]
             results[i] = Result(i, arrival)
             wait = t0 + arrival - time.perf_counter()
@@ -297,7 +298,8 @@ class Server:
             with cond:
                 if state["error"]:
                     break
-                inline = self.inline_idle and not queue and state["busy"] == 0
+                due = pos + 1 < len(order) and t0 + requests[order[pos + 1]][0] <= time.perf_counter()
+                inline = self.inline_idle and not queue and state["busy"] == 0 and not due
                 if inline:
                     state["busy"] += 1  # the slots leave it alone
                 else:
@@ -306,7 +308,7 @@ class Server:
             if inline:
                 failed = None
                 try:
-                    self._serve_one(i, _request(self.volumes, *requests[i][1:]), results, self.inline_ctx,
+                    self._serve_one(i, _request(self.volumes, *requests[i][1:]), results, self.contexts[0],
                                     torch.cuda.current_stream(self.device), state, cond, -1, t0, keep_meshes)
                 except BaseException as e:  # surfaced after the slots have stopped
                     failed = e
