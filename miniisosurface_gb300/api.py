@@ -450,6 +450,13 @@ def set_batch_graph(enable, ctx=None):
     check(load().iso_batch_set_graph(ctx.handle, 1 if enable else 0), ctx.handle)
 
 
+def set_batch_fused(enable, ctx=None):
+    """Run a batch's Flying Edges requests of rows up to 512 points one launch per pass (default) or every
+    request on the lanes (iso_batch_set_fused)."""
+    ctx = ctx or default_context()
+    check(load().iso_batch_set_fused(ctx.handle, 1 if enable else 0), ctx.handle)
+
+
 def batch_lanes(ctx=None):
     ctx = ctx or default_context()
     return int(load().iso_batch_lanes(ctx.handle))

@@ -1,6 +1,9 @@
 // C ABI of the batched extraction and of graph mode (iso_extract_batch,
 // iso_count_batch, iso_batch_*, iso_ctx_set_graph) and the exact per-block
 // triangle counts of the output-size network (iso_block_tris).
+#include <map>
+
+#include "batch_kernels.cuh"
 #include "capi_internal.h"
 
 using namespace capi;
@@ -36,16 +39,257 @@ void replan(iso_ctx* ctx, std::vector<BatchItem>& items, const std::vector<int>&
     for (int r : run) items[r].pl = make_plans(ctx, items[r].g, nsm);
 }
 
+// ---------------------------------------------------------------------------
+// Fused requests.  Flying Edges requests whose rows fit the multi-row kernels
+// (up to 16 words, the volume at a 16-byte boundary) run together, one launch
+// per pass and kernel variant (batch_kernels.cuh): the count blocks of every
+// request of a count variant, the two scan phases of all of them, the vertex
+// prefix, the generate items of every request of a generate variant (rows
+// per warp, index width), and one vertex pass over all their slots.  Each
+// request has its own scratch, so nothing is shared between requests but the
+// launches.  The descriptors and launch lists are written into pinned host
+// memory before every run and copied in by the first node.
+// ---------------------------------------------------------------------------
+struct FusedGroup {
+    iso::CountVariant cv{};
+    int rpw = 0, index_bytes = 4;
+    std::vector<int> members;  // descriptor indices
+    unsigned total = 0;        // blocks (count, scan) or work items (generate)
+    size_t list_at = 0, first_at = 0;
+    size_t smem = 0;
+    int ws_bytes = 0;
+};
+
+struct FusedPlan {
+    std::vector<int> reqs;              // the batch request of descriptor d
+    std::vector<iso::BatchReq> proto;   // the descriptors without their buffers
+    std::vector<FusedGroup> count, gen;
+    FusedGroup all;                     // every descriptor: scans (first = segments), vertex prefix and pass
+    std::vector<unsigned char> meta;    // the upload block without the descriptors: lists and firsts
+    size_t upload = 0;                  // bytes copied in per run: descriptors, then meta
+    size_t vfirst_at = 0, work_at = 0;  // within the fused area
+    std::vector<size_t> scratch_at;     // within the fused area, per descriptor
+    size_t bytes = 0;                   // the fused area
+    size_t at = 0;                      // its offset in the arena
+    bool empty() const { return reqs.empty(); }
+};
+
+bool fusable(const iso_ctx* ctx, const iso_request& r, const BatchItem& it)
+{
+    return ctx->batch_fused && r.algorithm == ISO_FLYING_EDGES && it.pl.gp.fits && it.g.W <= 16 &&
+           (reinterpret_cast<uintptr_t>(r.volume) & 15) == 0;
+}
+
+// Groups, work split and layout of the fused requests fz (their plans are made for the whole GPU).  Returns
+// an empty plan when a launch would pass 2^31 blocks or items: those requests then take the lanes.
+FusedPlan plan_fused(iso_ctx* ctx, const iso_request* req, const iso_mesh* out, std::vector<BatchItem>& items,
+                     const std::vector<int>& fz)
+{
+    FusedPlan f;
+    if (fz.empty()) return f;
+    f.reqs = fz;
+    const int nf = (int)fz.size();
+    f.proto.resize(nf);
+    std::map<int, int> ckey, gkey;
+    const long long warps = (long long)ctx->nsm * 4 * 8;  // generate kernel: 4 CTAs of 8 warps per SM
+    long long gen_planes = 0;                              // row groups x planes over all generate groups
+    for (int d = 0; d < nf; ++d) {
+        const int r = fz[d];
+        BatchItem& it = items[r];
+        it.pl = make_plans(ctx, it.g);
+        const Grid& g = it.g;
+        iso::BatchReq& x = f.proto[d];
+        x = iso::BatchReq{};
+        x.vol = req[r].volume;
+        x.g = g;
+        x.gs = iso::make_grad_scale(g);
+        x.iso = req[r].isoval;
+        const iso::CountVariant cv = iso::count_variant(g);
+        x.count_KC = it.pl.cp.KC;
+        x.count_nyb = (g.ny + 8 * cv.rpw - 1) / (8 * cv.rpw);  // kCountRows warps of cv.rpw rows
+        x.nseg = it.pl.cp.nseg;
+        const int ck = cv.rpw | (cv.aligned ? 16 : 0) | (cv.full ? 32 : 0);
+        if (!ckey.count(ck)) {
+            ckey[ck] = (int)f.count.size();
+            f.count.emplace_back();
+            f.count.back().cv = cv;
+        }
+        FusedGroup& cg = f.count[ckey[ck]];
+        cg.members.push_back(d);
+        cg.smem = std::max(cg.smem, iso::count_batch_smem(g, cv));
+        f.all.members.push_back(d);
+        if (out) {
+            const int rpw = iso::gen_rows_per_warp(g.W);
+            const int gk = rpw | (out[r].index_bytes << 8);
+            if (!gkey.count(gk)) {
+                gkey[gk] = (int)f.gen.size();
+                f.gen.emplace_back();
+                f.gen.back().rpw = rpw;
+                f.gen.back().index_bytes = out[r].index_bytes;
+            }
+            FusedGroup& gg = f.gen[gkey[gk]];
+            gg.members.push_back(d);
+            gg.ws_bytes = std::max(gg.ws_bytes, (int)iso::gen_batch_ws_bytes(g.W, rpw));
+            x.gen_ngroups = (g.ny + rpw - 1) / rpw;
+            gen_planes += (long long)x.gen_ngroups * g.nz;
+        }
+    }
+    // generate items of KC planes: about sixteen per warp of one wave over all requests, at least 2 planes
+    long long KC = (gen_planes + 16 * warps - 1) / (16 * warps);
+    if (KC < 2) KC = 2;
+    const long long lim = 1ll << 31;
+    auto blocks_of = [&](const FusedGroup& grp, int what) -> long long {
+        long long t = 0;
+        for (int d : grp.members) {
+            const iso::BatchReq& x = f.proto[d];
+            if (what == 0) t += (long long)x.count_nyb * ((x.g.nz + x.count_KC - 1) / x.count_KC);
+            else if (what == 1) t += x.nseg;
+            else t += (long long)x.gen_ngroups * x.gen_nkc;
+        }
+        return t;
+    };
+    if (out) {
+        for (iso::BatchReq& x : f.proto) {
+            x.gen_KC = (int)std::min<long long>(KC, x.g.nz);
+            x.gen_nkc = (x.g.nz + x.gen_KC - 1) / x.gen_KC;
+        }
+    }
+    // lists (ints) and firsts (unsigned, one more than the members) of each launch
+    auto place = [&](FusedGroup& grp, int what) -> bool {
+        const long long t = blocks_of(grp, what);
+        if (t >= lim) return false;
+        grp.total = (unsigned)t;
+        const size_t m = grp.members.size();
+        grp.list_at = f.meta.size();
+        f.meta.resize(f.meta.size() + ((m * 4 + 15) & ~(size_t)15));
+        std::memcpy(f.meta.data() + grp.list_at, grp.members.data(), m * 4);
+        grp.first_at = f.meta.size();
+        f.meta.resize(f.meta.size() + (((m + 1) * 4 + 15) & ~(size_t)15));
+        unsigned* fs = reinterpret_cast<unsigned*>(f.meta.data() + grp.first_at);
+        unsigned run = 0;
+        for (size_t q = 0; q < m; ++q) {
+            fs[q] = run;
+            const iso::BatchReq& x = f.proto[grp.members[q]];
+            run += what == 0 ? (unsigned)(x.count_nyb * ((x.g.nz + x.count_KC - 1) / x.count_KC))
+                             : (what == 1 ? (unsigned)x.nseg : (unsigned)(x.gen_ngroups * x.gen_nkc));
+        }
+        fs[m] = run;
+        return true;
+    };
+    bool ok = place(f.all, 1);
+    for (FusedGroup& grp : f.count) ok = ok && place(grp, 0);
+    for (FusedGroup& grp : f.gen) ok = ok && place(grp, 2);
+    if (!ok) return FusedPlan{};
+    const size_t desc = ((size_t)nf * sizeof(iso::BatchReq) + 255) & ~(size_t)255;
+    f.upload = desc + f.meta.size();
+    size_t at = align256(f.upload);
+    f.vfirst_at = at;
+    at += align256((size_t)(nf + 1) * 8);
+    f.work_at = at;
+    at += align256(f.gen.size() * 4 + 4);
+    f.scratch_at.resize(nf);
+    for (int d = 0; d < nf; ++d) {
+        f.scratch_at[d] = at;
+        at += align256(scratch_size(items[fz[d]].g, items[fz[d]].pl.cp));
+    }
+    f.bytes = at;
+    return f;
+}
+
+// The fused requests' descriptors (buffers in the arena at f.at, meshes of out, counters of the batch) and
+// launch lists into ctx->h_fused.
+void fill_fused(iso_ctx* ctx, const FusedPlan& f, const iso_mesh* out, const std::vector<BatchItem>& items)
+{
+    char* base = static_cast<char*>(ctx->batch_arena) + f.at;
+    unsigned long long* counters = static_cast<unsigned long long*>(ctx->batch_arena);
+    iso::BatchReq* D = reinterpret_cast<iso::BatchReq*>(ctx->h_fused);
+    for (size_t d = 0; d < f.reqs.size(); ++d) {
+        const int r = f.reqs[d];
+        const BatchItem& it = items[r];
+        FeBuffers b;
+        carve(base + f.scratch_at[d], it.g, it.pl.cp, b);
+        iso::BatchReq x = f.proto[d];
+        x.rowcnt = b.rowcnt;
+        x.bits = b.bits;
+        x.starts = b.starts;
+        x.part = b.part;
+        x.totals = counters + 8 * (size_t)r;
+        if (out) {
+            x.points = out[r].points;
+            x.normals = out[r].normals;
+            x.tris = out[r].tris;
+            x.capV = vertex_limit(&out[r], out[r].cap_points);
+            x.capT = out[r].cap_tris;
+        }
+        D[d] = x;
+    }
+    const size_t desc = (f.reqs.size() * sizeof(iso::BatchReq) + 255) & ~(size_t)255;
+    std::memcpy(ctx->h_fused + desc, f.meta.data(), f.meta.size());
+}
+
+// The launches of one pass run side by side: the largest on s, the others on streams forked from it and
+// joined back into it.
+constexpr bool kFusedSideBySide = true;
+
+template <typename Launch>
+void fan_out(iso_ctx* ctx, const std::vector<FusedGroup>& groups, cudaStream_t s, Launch launch)
+{
+    std::vector<size_t> order(groups.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](size_t a, size_t b) { return groups[a].total > groups[b].total; });
+    const size_t side = kFusedSideBySide ? std::min(order.size(), ctx->fused_streams.size() + 1) : 1;
+    if (side > 1) {
+        cudaEventRecord(ctx->fused_fork, s);
+        for (size_t i = 1; i < side; ++i) cudaStreamWaitEvent(ctx->fused_streams[i - 1], ctx->fused_fork, 0);
+    }
+    for (size_t i = 0; i < order.size(); ++i)
+        launch(order[i], i < side && i > 0 ? ctx->fused_streams[i - 1] : s);
+    for (size_t i = 1; i < side; ++i) {
+        cudaEventRecord(ctx->fused_join[i - 1], ctx->fused_streams[i - 1]);
+        cudaStreamWaitEvent(s, ctx->fused_join[i - 1], 0);
+    }
+}
+
+// The fused chain on s: descriptors in, counts, scans and, for an extraction, the generate and vertex passes.
+void enqueue_fused(iso_ctx* ctx, const FusedPlan& f, bool extract, cudaStream_t s)
+{
+    char* base = static_cast<char*>(ctx->batch_arena) + f.at;
+    const size_t desc = (f.reqs.size() * sizeof(iso::BatchReq) + 255) & ~(size_t)255;
+    const iso::BatchReq* D = reinterpret_cast<const iso::BatchReq*>(base);
+    auto L = [&](const FusedGroup& g) { return reinterpret_cast<const int*>(base + desc + g.list_at); };
+    auto F = [&](const FusedGroup& g) { return reinterpret_cast<const unsigned*>(base + desc + g.first_at); };
+    const int nf = (int)f.reqs.size();
+    cudaMemcpyAsync(base, ctx->h_fused, f.upload, cudaMemcpyHostToDevice, s);
+    fan_out(ctx, f.count, s, [&](size_t q, cudaStream_t st) {
+        const FusedGroup& g = f.count[q];
+        iso::launch_count_batch(g.cv, D, L(g), F(g), (int)g.members.size(), g.total, g.smem, st);
+    });
+    iso::launch_scan_batch(D, L(f.all), F(f.all), nf, f.all.total, s);
+    if (!extract) return;
+    unsigned long long* vfirst = reinterpret_cast<unsigned long long*>(base + f.vfirst_at);
+    unsigned* work = reinterpret_cast<unsigned*>(base + f.work_at);
+    cudaMemsetAsync(work, 0, f.gen.size() * 4, s);
+    iso::launch_vfirst_batch(D, L(f.all), nf, vfirst, s);
+    fan_out(ctx, f.gen, s, [&](size_t q, cudaStream_t st) {
+        const FusedGroup& g = f.gen[q];
+        iso::launch_gen_batch(g.rpw, g.index_bytes, D, L(g), F(g), (int)g.members.size(), g.total, ctx->d_cases,
+                              work + q, g.ws_bytes, ctx->reverse, ctx->nsm, st);
+    });
+    iso::launch_vertices_batch(D, L(f.all), vfirst, nf, ctx->nsm, s);
+}
+
 // Lane of every request with work and the arena layout: counters of all n
-// requests, then per lane its scratch and FE -> MC map.
+// requests, then per lane its scratch and FE -> MC map, then the fused area.
 struct BatchLayout {
     int lanes = 1;
     std::vector<size_t> scratch_at, scratch_bytes, map_at;
+    FusedPlan fz;
     size_t bytes = 0;
 };
 
 BatchLayout plan_batch(const iso_request* req, const iso_mesh* out, int64_t n, std::vector<BatchItem>& items,
-                       const std::vector<int>& run, int lanes)
+                       const std::vector<int>& run, int lanes, const FusedPlan& fz)
 {
     BatchLayout lay;
     lay.lanes = lanes;
@@ -73,6 +317,9 @@ BatchLayout plan_batch(const iso_request* req, const iso_mesh* out, int64_t n, s
         lay.map_at.push_back(at);
         at += align256(map[l]);
     }
+    lay.fz = fz;
+    lay.fz.at = at;
+    at += fz.bytes;
     lay.bytes = at;
     return lay;
 }
@@ -102,9 +349,27 @@ iso_status ensure_batch(iso_ctx* ctx, const BatchLayout& lay, int64_t n, cudaStr
         ISO_CUDA(ctx, cudaHostAlloc(&ctx->h_batch, (size_t)n * 8 * sizeof(unsigned long long), cudaHostAllocDefault));
         ctx->h_batch_n = (size_t)n;
     }
+    if (lay.fz.upload > ctx->h_fused_bytes) {
+        ISO_CUDA(ctx, cudaStreamSynchronize(s));
+        if (ctx->h_fused) cudaFreeHost(ctx->h_fused);
+        ctx->h_fused = nullptr;
+        ctx->h_fused_bytes = 0;
+        ISO_CUDA(ctx, cudaHostAlloc(reinterpret_cast<void**>(&ctx->h_fused), lay.fz.upload, cudaHostAllocDefault));
+        ctx->h_fused_bytes = lay.fz.upload;
+    }
     if (!ctx->s_capture) ISO_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->s_capture, cudaStreamNonBlocking));
     for (cudaEvent_t* e : {&ctx->batch_fork, &ctx->batch_t0, &ctx->batch_t1})
         if (!*e) ISO_CUDA(ctx, cudaEventCreateWithFlags(e, e == &ctx->batch_fork ? cudaEventDisableTiming : 0));
+    const size_t side = std::max(lay.fz.count.size(), lay.fz.gen.size());
+    if (side > 1 && !ctx->fused_fork) ISO_CUDA(ctx, cudaEventCreateWithFlags(&ctx->fused_fork, cudaEventDisableTiming));
+    while (ctx->fused_streams.size() + 1 < side) {
+        cudaStream_t q;
+        cudaEvent_t e;
+        ISO_CUDA(ctx, cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking));
+        ctx->fused_streams.push_back(q);
+        ISO_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        ctx->fused_join.push_back(e);
+    }
     while ((int)ctx->lane_streams.size() < lay.lanes) {
         cudaStream_t q;
         cudaEvent_t e;
@@ -132,6 +397,8 @@ std::vector<unsigned char> batch_key(const iso_ctx* ctx, int lanes, int share, c
     put(&ctx->reverse, sizeof ctx->reverse);
     put(&ctx->batch_arena, sizeof ctx->batch_arena);
     put(&ctx->h_batch, sizeof ctx->h_batch);
+    put(&ctx->batch_fused, sizeof ctx->batch_fused);
+    put(&ctx->h_fused, sizeof ctx->h_fused);
     put(&n, sizeof n);
     put(req, (size_t)n * sizeof(iso_request));
     for (int64_t r = 0; out && r < n; ++r) {
@@ -154,6 +421,7 @@ void enqueue_batch(iso_ctx* ctx, const iso_request* req, const iso_mesh* out, in
     unsigned long long* counters = reinterpret_cast<unsigned long long*>(arena);
     const bool prof = ctx->profiling;
     ctx->profiling = false;  // no timing events between the lanes' kernels
+    cudaMemsetAsync(counters, 0, (size_t)n * 8 * sizeof(unsigned long long), origin);
     cudaEventRecord(ctx->batch_fork, origin);
     for (int l = 0; l < lay.lanes; ++l) cudaStreamWaitEvent(ctx->lane_streams[l], ctx->batch_fork, 0);
     for (int r : run) {
@@ -168,6 +436,7 @@ void enqueue_batch(iso_ctx* ctx, const iso_request* req, const iso_mesh* out, in
         enqueue_count(ctx, algo, req[r].volume, it.g, req[r].isoval, it.pl, b, ls, pm);
         if (out) enqueue_generate(ctx, algo, req[r].volume, it.g, req[r].isoval, it.pl, b, &out[r], ls, pm);
     }
+    if (!lay.fz.empty()) enqueue_fused(ctx, lay.fz, out != nullptr, origin);  // beside the lanes
     for (int l = 0; l < lay.lanes; ++l) {
         cudaEventRecord(ctx->lane_join[l], ctx->lane_streams[l]);
         cudaStreamWaitEvent(origin, ctx->lane_join[l], 0);
@@ -219,14 +488,16 @@ iso_status capture_batch(iso_ctx* ctx, const iso_request* req, const iso_mesh* o
 
 // Prepare (lanes, buffers, graph) for `lanes` lanes; nothing runs.
 iso_status prepare_batch(iso_ctx* ctx, const iso_request* req, const iso_mesh* out, int64_t n,
-                         std::vector<BatchItem>& items, const std::vector<int>& run, int lanes, int share,
-                         cudaStream_t s)
+                         std::vector<BatchItem>& items, const std::vector<int>& run, const FusedPlan& fz, int lanes,
+                         int share, cudaStream_t s)
 {
     replan(ctx, items, run, share);
-    const BatchLayout lay = plan_batch(req, out, n, items, run, lanes);
+    const BatchLayout lay = plan_batch(req, out, n, items, run, lanes, fz);
     std::lock_guard<std::mutex> lock(g_batch_mutex);
     iso_status st = ensure_batch(ctx, lay, n, s);
     if (st != ISO_OK) return st;
+    // before every run, replayed graph or not: the staging is shared by the context's graphs
+    if (!lay.fz.empty()) fill_fused(ctx, lay.fz, out, items);
     std::vector<unsigned char> key = batch_key(ctx, lanes, share, req, out, n);
     const int slot = out ? 0 : 1;
     if (ctx->batch_exec[slot] && key == ctx->batch_key[slot]) return ISO_OK;
@@ -388,34 +659,44 @@ iso_status run_batch(iso_ctx* ctx, int64_t n, const iso_request* req, iso_mesh* 
         }
         run.push_back((int)r);
     }
+    // the fused requests (one launch per pass) and the rest (lanes)
+    std::vector<int> fused, lane_run;
+    for (int r : run) (fusable(ctx, req[r], items[r]) ? fused : lane_run).push_back(r);
+    const FusedPlan fz = plan_fused(ctx, req, out, items, fused);
+    if (fz.empty() && !fused.empty()) lane_run = run;
     iso_status rc = ISO_OK;
-    if (!run.empty() && !ctx->batch_graph) {  // the lanes launched directly, no graph
+    if (!run.empty() && !ctx->batch_graph) {  // launched directly, no graph
         int lanes = ctx->batch_lanes > 0 ? ctx->batch_lanes : (ctx->batch_tuned > 0 ? ctx->batch_tuned : 8);
         const int share = ctx->batch_share > 0 ? ctx->batch_share : std::max(1, ctx->batch_tuned_share);
-        lanes = std::min(lanes, std::max(1, (int)run.size()));
-        replan(ctx, items, run, share);
-        const BatchLayout lay = plan_batch(req, out, n, items, run, lanes);
+        lanes = std::min(lanes, std::max(1, (int)lane_run.size()));
+        replan(ctx, items, lane_run, share);
+        const BatchLayout lay = plan_batch(req, out, n, items, lane_run, lanes, fz);
         {
             std::lock_guard<std::mutex> lock(g_batch_mutex);
             rc = ensure_batch(ctx, lay, n, s);
+            if (rc == ISO_OK && !lay.fz.empty()) fill_fused(ctx, lay.fz, out, items);
         }
         if (rc != ISO_OK) return rc;
-        enqueue_batch(ctx, req, out, n, items, run, lay, s);
+        enqueue_batch(ctx, req, out, n, items, lane_run, lay, s);
         ISO_CUDA(ctx, cudaGetLastError());
         ISO_CUDA(ctx, cudaStreamSynchronize(s));
     } else if (!run.empty()) {
         int lanes = ctx->batch_lanes > 0 ? ctx->batch_lanes : ctx->batch_tuned;
         int share = ctx->batch_share > 0 ? ctx->batch_share : ctx->batch_tuned_share;
+        if (lane_run.empty()) {  // every request fused: nothing to tune
+            lanes = std::max(lanes, 1);
+            share = std::max(share, 1);
+        }
         if (lanes <= 0 || share <= 0) {  // autotuner: time the batch at each (lanes, split), keep the fastest
             float best = 1e30f;
             int best_l = 1, best_s = 1;
             for (int L : kTuneLanes) {
                 if (lanes > 0 && L != lanes) continue;
-                if (L > 1 && L > (int)run.size()) break;
+                if (L > 1 && L > (int)lane_run.size()) break;
                 for (int S : kTuneShares) {
                     if (share > 0 && S != share) continue;
                     if (S > L) break;  // a request never has fewer SMs than nsm / lanes
-                    rc = prepare_batch(ctx, req, out, n, items, run, L, S, s);
+                    rc = prepare_batch(ctx, req, out, n, items, lane_run, fz, L, S, s);
                     if (rc != ISO_OK) return rc;
                     float ms;
                     rc = time_batch(ctx, ctx->batch_exec[out ? 0 : 1], s, ms);
@@ -432,8 +713,8 @@ iso_status run_batch(iso_ctx* ctx, int64_t n, const iso_request* req, iso_mesh* 
             if (ctx->batch_lanes <= 0) ctx->batch_tuned = lanes;
             if (ctx->batch_share <= 0) ctx->batch_tuned_share = share;
         }
-        lanes = std::min(lanes, std::max(1, (int)run.size()));
-        rc = prepare_batch(ctx, req, out, n, items, run, lanes, share, s);
+        lanes = std::min(lanes, std::max(1, (int)lane_run.size()));
+        rc = prepare_batch(ctx, req, out, n, items, lane_run, fz, lanes, share, s);
         if (rc != ISO_OK) return rc;
         ISO_CUDA(ctx, cudaGraphLaunch(ctx->batch_exec[out ? 0 : 1], s));
         ISO_CUDA(ctx, cudaStreamSynchronize(s));
@@ -518,6 +799,13 @@ int iso_batch_split(const iso_ctx* ctx)
 {
     if (!ctx) return 0;
     return ctx->batch_share > 0 ? ctx->batch_share : ctx->batch_tuned_share;
+}
+
+iso_status iso_batch_set_fused(iso_ctx* ctx, int enable)
+{
+    if (!ctx) return ISO_ERR_INVALID_ARG;
+    ctx->batch_fused = enable ? 1 : 0;
+    return ISO_OK;
 }
 
 iso_status iso_batch_set_graph(iso_ctx* ctx, int enable)

@@ -615,12 +615,16 @@ iso_status iso_ctx_destroy(iso_ctx* ctx)
         if (x) cudaGraphExecDestroy(x);
     if (ctx->one_exec) cudaGraphExecDestroy(ctx->one_exec);
     for (cudaStream_t q : ctx->lane_streams) cudaStreamDestroy(q);
+    for (cudaStream_t q : ctx->fused_streams) cudaStreamDestroy(q);
+    for (cudaEvent_t e : ctx->fused_join) cudaEventDestroy(e);
+    if (ctx->fused_fork) cudaEventDestroy(ctx->fused_fork);
     for (cudaEvent_t e : ctx->lane_join) cudaEventDestroy(e);
     for (cudaEvent_t e : {ctx->batch_fork, ctx->batch_t0, ctx->batch_t1})
         if (e) cudaEventDestroy(e);
     if (ctx->s_capture) cudaStreamDestroy(ctx->s_capture);
     cudaFree(ctx->batch_arena);
     if (ctx->h_batch) cudaFreeHost(ctx->h_batch);
+    if (ctx->h_fused) cudaFreeHost(ctx->h_fused);
     delete ctx;
     return ISO_OK;
 }

@@ -70,6 +70,12 @@ struct iso_ctx {
     // executable graphs of iso_extract_batch [0] and iso_count_batch [1], and what each was captured for
     cudaGraphExec_t batch_exec[2] = {nullptr, nullptr};
     std::vector<unsigned char> batch_key[2];
+    int batch_fused = 1;  // Flying Edges requests of rows up to 16 words run one launch per pass (iso_batch_set_fused)
+    unsigned char* h_fused = nullptr;  // pinned: the fused requests' descriptors and launch lists, copied in per run
+    size_t h_fused_bytes = 0;
+    std::vector<cudaStream_t> fused_streams;  // the fused launches of one pass side by side, and their joins
+    std::vector<cudaEvent_t> fused_join;
+    cudaEvent_t fused_fork = nullptr;
     int reverse = 1;  // pass 4 walks the planes backwards (the count pass leaves the last ones in L2)
     int narrow = 1;   // iso_extract_device_typed reads 8- and 16-bit samples as they are (iso_ctx_set_narrow)
     int stream_host = 1;  // iso_extract_host streams slabs (large grids)

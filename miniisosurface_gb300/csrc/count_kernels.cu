@@ -21,6 +21,7 @@
 //                  reference's row order: the first vertex / triangle / MC
 //                  vertex of every row (gridEdge xstart and triCounter after
 //                  pass 3) and the totals.
+#include "batch_kernels.cuh"
 #include "count_words.cuh"
 #include "iso_kernels.h"
 
@@ -261,17 +262,18 @@ __host__ __device__ inline int count_buffer_floats(int nx, int rpw, bool aligned
 // of every plane, RPW + 1 rows of its buffer.  FULL: every lane's word is
 // inside the row (nx = 32 * LPR).
 
+// Block blk of the grid: row block blk % nyb, plane column blk / nyb.
 template <bool MC, bool FULL, int RPW, bool ALIGNED>
-__global__ void __launch_bounds__(kThreads, 4) k_count_tma(const float* __restrict__ vol, Grid g, float iso, int KC,
-                                                        int nyb, uint4* __restrict__ rowcnt,
-                                                        uint2* __restrict__ trims, uint32_t* __restrict__ mccnt,
-                                                        uint32_t* __restrict__ bits_out,
-                                                        unsigned long long* __restrict__ status)
+__device__ __forceinline__ void count_tma_block(const float* __restrict__ vol, const Grid& g, float iso, int KC,
+                                                int nyb, int blk, uint4* __restrict__ rowcnt,
+                                                uint2* __restrict__ trims, uint32_t* __restrict__ mccnt,
+                                                uint32_t* __restrict__ bits_out,
+                                                unsigned long long* __restrict__ status)
 {
     constexpr int LPR = 32 / RPW, NBUF = RPW + 1;
     extern __shared__ __align__(16) unsigned char s_raw[];
     __shared__ uint64_t s_bar[kCountRows];
-    const int jb = blockIdx.x % nyb, kc = blockIdx.x / nyb;
+    const int jb = blk % nyb, kc = blk / nyb;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, h = lane / LPR, lw = lane % LPR;
     const int jw = jb * kCountRows * RPW + RPW * warp;
     if (jw >= g.ny) return;  // all the warp's rows past the grid
@@ -413,6 +415,31 @@ __global__ void __launch_bounds__(kThreads, 4) k_count_tma(const float* __restri
     }
 }
 
+template <bool MC, bool FULL, int RPW, bool ALIGNED>
+__global__ void __launch_bounds__(kThreads, 4) k_count_tma(const float* __restrict__ vol, Grid g, float iso, int KC,
+                                                        int nyb, uint4* __restrict__ rowcnt,
+                                                        uint2* __restrict__ trims, uint32_t* __restrict__ mccnt,
+                                                        uint32_t* __restrict__ bits_out,
+                                                        unsigned long long* __restrict__ status)
+{
+    count_tma_block<MC, FULL, RPW, ALIGNED>(vol, g, iso, KC, nyb, (int)blockIdx.x, rowcnt, trims, mccnt, bits_out,
+                                            status);
+}
+
+// The Flying Edges count blocks of a list of requests (batch_kernels.cuh), one launch.
+template <bool FULL, int RPW, bool ALIGNED>
+__global__ void __launch_bounds__(kThreads, 4) k_count_tma_batch(const BatchReq* __restrict__ reqs,
+                                                              const int* __restrict__ list,
+                                                              const unsigned* __restrict__ first, int m)
+{
+    const int q = batch_find(first, m, blockIdx.x);
+    const BatchReq* d = reqs + __ldg(&list[q]);
+    const Grid g = d->g;
+    count_tma_block<false, FULL, RPW, ALIGNED>(d->vol, g, d->iso, d->count_KC, d->count_nyb,
+                                               (int)(blockIdx.x - __ldg(&first[q])), d->rowcnt, nullptr, nullptr,
+                                               d->bits, d->totals + 3);
+}
+
 // Word c*32 + lane of a row and, uniform over the warp, word c*32 + 32 (the
 // source of lane 31's bit 32): 33 coalesced 128-byte loads.
 __device__ __forceinline__ void chunk_words(const float* __restrict__ row, bool ok, int c, int nx, int lane, float iso,
@@ -519,17 +546,18 @@ __device__ __forceinline__ void load_counts(const uint4* __restrict__ rowcnt, co
     }
 }
 
+// Segment blk of the scan: its totals into part[a * nseg + blk].
 template <int SM>
-__global__ void __launch_bounds__(kThreads) k_scan_partial(const uint4* __restrict__ rowcnt,
-                                                           const uint32_t* __restrict__ mccnt, long long R,
-                                                           unsigned long long* __restrict__ part, int nseg)
+__device__ __forceinline__ void scan_partial_block(const uint4* __restrict__ rowcnt,
+                                                   const uint32_t* __restrict__ mccnt, long long R,
+                                                   unsigned long long* __restrict__ part, int nseg, int blk)
 {
     constexpr int NC = ScanComps<SM>::n;
     __shared__ unsigned long long s_w[NC][kThreads / 32];
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     uint32_t v[4][kScanPer];
     unsigned long long s[4];
-    load_counts<SM>(rowcnt, mccnt, R, (long long)blockIdx.x * kSeg + (long long)t * kScanPer, v, s);
+    load_counts<SM>(rowcnt, mccnt, R, (long long)blk * kSeg + (long long)t * kScanPer, v, s);
 #pragma unroll
     for (int a = 0; a < NC; ++a) {
 #pragma unroll
@@ -540,16 +568,25 @@ __global__ void __launch_bounds__(kThreads) k_scan_partial(const uint4* __restri
     if (t < NC) {
         unsigned long long tot = 0;
         for (int w = 0; w < kThreads / 32; ++w) tot += s_w[t][w];
-        part[t * nseg + blockIdx.x] = tot;
+        part[t * nseg + blk] = tot;
     }
 }
 
 template <int SM>
-__global__ void __launch_bounds__(kThreads) k_scan_final(const uint4* __restrict__ rowcnt,
-                                                         const uint32_t* __restrict__ mccnt, long long R,
-                                                         const unsigned long long* __restrict__ part, int nseg,
-                                                         unsigned long long* __restrict__ starts,
-                                                         unsigned long long* __restrict__ totals)
+__global__ void __launch_bounds__(kThreads) k_scan_partial(const uint4* __restrict__ rowcnt,
+                                                           const uint32_t* __restrict__ mccnt, long long R,
+                                                           unsigned long long* __restrict__ part, int nseg)
+{
+    scan_partial_block<SM>(rowcnt, mccnt, R, part, nseg, (int)blockIdx.x);
+}
+
+// Segment blk: the starts of its rows from the segments' totals; segment 0 also writes the totals.
+template <int SM>
+__device__ __forceinline__ void scan_final_block(const uint4* __restrict__ rowcnt,
+                                                 const uint32_t* __restrict__ mccnt, long long R,
+                                                 const unsigned long long* __restrict__ part, int nseg,
+                                                 unsigned long long* __restrict__ starts,
+                                                 unsigned long long* __restrict__ totals, int blk)
 {
     constexpr int NC = ScanComps<SM>::n;
     __shared__ unsigned long long s_w[NC][kThreads / 32];
@@ -559,7 +596,7 @@ __global__ void __launch_bounds__(kThreads) k_scan_final(const uint4* __restrict
         unsigned long long b = 0, tot = 0;
         for (int q = lane; q < nseg; q += 32) {
             const unsigned long long x = part[warp * nseg + q];
-            if (q < (int)blockIdx.x) b += x;
+            if (q < blk) b += x;
             tot += x;
         }
 #pragma unroll
@@ -572,7 +609,7 @@ __global__ void __launch_bounds__(kThreads) k_scan_final(const uint4* __restrict
             s_tot[warp] = tot;
         }
     }
-    const long long b = (long long)blockIdx.x * kSeg + (long long)t * kScanPer;
+    const long long b = (long long)blk * kSeg + (long long)t * kScanPer;
     uint32_t v[4][kScanPer];
     unsigned long long s[4], inc[4];
     load_counts<SM>(rowcnt, mccnt, R, b, v, s);
@@ -587,7 +624,7 @@ __global__ void __launch_bounds__(kThreads) k_scan_final(const uint4* __restrict
         if (lane == 31) s_w[a][warp] = inc[a];
     }
     __syncthreads();
-    if (blockIdx.x == 0 && t == 0) {
+    if (blk == 0 && t == 0) {
         if (SM == kScanDup) {
             totals[0] = s_tot[0] + s_tot[2] + s_tot[3];
             totals[1] = s_tot[1];
@@ -609,6 +646,69 @@ __global__ void __launch_bounds__(kThreads) k_scan_final(const uint4* __restrict
             run += v[a][q];
         }
     }
+}
+
+template <int SM>
+__global__ void __launch_bounds__(kThreads) k_scan_final(const uint4* __restrict__ rowcnt,
+                                                         const uint32_t* __restrict__ mccnt, long long R,
+                                                         const unsigned long long* __restrict__ part, int nseg,
+                                                         unsigned long long* __restrict__ starts,
+                                                         unsigned long long* __restrict__ totals)
+{
+    scan_final_block<SM>(rowcnt, mccnt, R, part, nseg, starts, totals, (int)blockIdx.x);
+}
+
+// The Flying Edges scans of a list of requests, one launch per phase: block x is segment
+// x - first[q] of request list[q].
+__global__ void __launch_bounds__(kThreads) k_scan_partial_batch(const BatchReq* __restrict__ reqs,
+                                                                 const int* __restrict__ list,
+                                                                 const unsigned* __restrict__ first, int m)
+{
+    const int q = batch_find(first, m, blockIdx.x);
+    const BatchReq* d = reqs + __ldg(&list[q]);
+    scan_partial_block<kScanFE>(d->rowcnt, nullptr, d->g.R, d->part, d->nseg, (int)(blockIdx.x - __ldg(&first[q])));
+}
+
+__global__ void __launch_bounds__(kThreads) k_scan_final_batch(const BatchReq* __restrict__ reqs,
+                                                               const int* __restrict__ list,
+                                                               const unsigned* __restrict__ first, int m)
+{
+    const int q = batch_find(first, m, blockIdx.x);
+    const BatchReq* d = reqs + __ldg(&list[q]);
+    scan_final_block<kScanFE>(d->rowcnt, nullptr, d->g.R, d->part, d->nseg, d->starts, d->totals,
+                              (int)(blockIdx.x - __ldg(&first[q])));
+}
+
+// vfirst[q] = the vertices of requests list[0 .. q-1] whose meshes hold their counts (one CTA of 1024 threads,
+// each summing a run of consecutive requests).
+__global__ void __launch_bounds__(1024) k_batch_vfirst(const BatchReq* __restrict__ reqs, const int* __restrict__ list,
+                                                       int m, unsigned long long* __restrict__ vfirst)
+{
+    __shared__ unsigned long long s_w[32];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const int per = (m + 1023) / 1024, q0 = t * per, q1 = min(m, q0 + per);
+    auto verts = [&](int q) -> unsigned long long {
+        const BatchReq* d = reqs + __ldg(&list[q]);
+        const unsigned long long v = d->totals[0], tr = d->totals[1];
+        return ((long long)v <= d->capV && (long long)tr <= d->capT) ? v : 0ull;
+    };
+    unsigned long long mine = 0;
+    for (int q = q0; q < q1; ++q) mine += verts(q);
+    unsigned long long inc = mine;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xffffffffu, inc, d);
+        if (lane >= d) inc += y;
+    }
+    if (lane == 31) s_w[warp] = inc;
+    __syncthreads();
+    unsigned long long run = inc - mine;
+    for (int w = 0; w < warp; ++w) run += s_w[w];
+    for (int q = q0; q < q1; ++q) {
+        vfirst[q] = run;
+        run += verts(q);
+    }
+    if (t == 1023) vfirst[m] = run;
 }
 
 // gridEdge records {xl, xr, xstart, ystart, zstart} and triCounter for
@@ -733,6 +833,58 @@ void launch_count(const float* vol, const Grid& g, float iso, const CaseTables* 
     cudaMemsetAsync(b.totals + 3, 0, sizeof(unsigned long long), s);  // device status
     if (mc) count_launch<true>(p, vol, g, iso, cases, b, s);
     else count_launch<false>(p, vol, g, iso, cases, b, s);
+}
+
+CountVariant count_variant(const Grid& g)
+{
+    CountVariant v;
+    v.rpw = g.W <= 4 ? 8 : (g.W <= 8 ? 4 : 2);
+    v.aligned = g.nx % 4 == 0;
+    v.full = v.aligned && (g.nx >> 2) == 256 / v.rpw;  // nq = 32 * LPR / 4 points in quads
+    return v;
+}
+
+size_t count_batch_smem(const Grid& g, const CountVariant& v)
+{
+    return (size_t)kCountRows * count_buffer_floats(g.nx, v.rpw, v.aligned) * sizeof(float);
+}
+
+void launch_count_batch(const CountVariant& v, const BatchReq* reqs, const int* list, const unsigned* first, int m,
+                        unsigned blocks, size_t smem, cudaStream_t s)
+{
+#define ISO_TMA_BATCH(FULL, RPW, AL)                                                                           \
+    {                                                                                                          \
+        auto kern = k_count_tma_batch<FULL, RPW, AL>;                                                         \
+        allow_smem(kern, smem);                                                                                \
+        kern<<<blocks, kThreads, smem, s>>>(reqs, list, first, m);                                             \
+    }
+    if (!v.aligned) {
+        if (v.rpw == 8) ISO_TMA_BATCH(false, 8, false)
+        else if (v.rpw == 4) ISO_TMA_BATCH(false, 4, false)
+        else ISO_TMA_BATCH(false, 2, false)
+    } else if (v.rpw == 8) {
+        if (v.full) ISO_TMA_BATCH(true, 8, true)
+        else ISO_TMA_BATCH(false, 8, true)
+    } else if (v.rpw == 4) {
+        if (v.full) ISO_TMA_BATCH(true, 4, true)
+        else ISO_TMA_BATCH(false, 4, true)
+    } else {
+        if (v.full) ISO_TMA_BATCH(true, 2, true)
+        else ISO_TMA_BATCH(false, 2, true)
+    }
+#undef ISO_TMA_BATCH
+}
+
+void launch_scan_batch(const BatchReq* reqs, const int* list, const unsigned* first, int m, unsigned blocks,
+                       cudaStream_t s)
+{
+    k_scan_partial_batch<<<blocks, kThreads, 0, s>>>(reqs, list, first, m);
+    k_scan_final_batch<<<blocks, kThreads, 0, s>>>(reqs, list, first, m);
+}
+
+void launch_vfirst_batch(const BatchReq* reqs, const int* list, int m, unsigned long long* vfirst, cudaStream_t s)
+{
+    k_batch_vfirst<<<1, 1024, 0, s>>>(reqs, list, m, vfirst);
 }
 
 void launch_scan(const Grid& g, const CountPlan& p, int mode, FeBuffers& b, cudaStream_t s)

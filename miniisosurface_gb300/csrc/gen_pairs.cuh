@@ -24,6 +24,7 @@
 // vertex, many warps per SM to cover the latency of the volume gathers --
 // turns each record into the vertex's position and normal in place.
 #pragma once
+#include "batch_kernels.cuh"
 #include "gen_warps.cuh"
 #include "vertices.cuh"
 
@@ -50,33 +51,24 @@ __host__ __device__ inline size_t gen_pair_scratch_bytes(int W, int RPW, int mod
 // 139-177: cell order, then first appearance in the cell's triangle list)
 // get their ids, records for the rows from kemit on, and the FE -> MC map
 // entry of their edge.  kGenTri: the triangles, corners mapped through it.
-template <typename IndexT, int RPW, int MODE>
-__global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
-    const uint32_t* __restrict__ bits, Grid g, int KC, int ngroups, int nkc, int kbeg, int kend,
-    int kemit, unsigned long long vbase, unsigned long long tbase, int ws_bytes,
-    const CaseTables* __restrict__ cases, const uint4* __restrict__ rowcnt, RowStarts rs,
-    const unsigned long long* __restrict__ totals, unsigned int* __restrict__ work, long long capV, long long capT,
-    float* __restrict__ points, IndexT* __restrict__ tris, uint32_t* __restrict__ fe2mc, int reverse)
+// The kernel's per-case tables in shared memory.  s_tri: per case, each triangle corner as the nibble (edge-id
+// table row | point offset << 3) of fe_edge_rel, the triangle count in bits 60..63 (the packed triangle list
+// with edges replaced); s_order: the first-appearance order of the cut edges; s_cut: the cut edges.
+template <int MODE>
+struct GenPairTables {
+    static constexpr bool OWNS = MODE == kGenMC || MODE == kGenMCT;  // numbers the MC vertices its cells own
+    uint64_t tri[MODE == kGenMC ? 1 : 256];
+    uint64_t order[OWNS ? 256 : 1];
+    uint16_t cut[OWNS ? 256 : 1];
+};
+
+template <int MODE>
+__device__ __forceinline__ void gen_pair_tables(const CaseTables* __restrict__ cases, GenPairTables<MODE>& t)
 {
-    extern __shared__ __align__(16) unsigned char s_raw[];
-    // per case: each triangle corner as the nibble (edge-id table row | point offset << 3) of fe_edge_rel,
-    // the triangle count in bits 60..63 (the packed triangle list with edges replaced)
-    __shared__ uint64_t s_tri[MODE == kGenMC ? 1 : 256];
-    constexpr bool OWNS = MODE == kGenMC || MODE == kGenMCT;  // numbers the MC vertices its cells own
-    __shared__ uint64_t s_order[OWNS ? 256 : 1];  // first-appearance order, cut edges
-    __shared__ uint16_t s_cut[OWNS ? 256 : 1];
-    constexpr int LPR = 32 / RPW;  // lanes per row
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, h = lane / LPR, lw = lane % LPR;
-    const int W = g.W;
-    unsigned char* ws = s_raw + (size_t)warp * ws_bytes;
-    uint2* mb = reinterpret_cast<uint2*>(ws);                                    // [RPW][8][W]
-    uint32_t* rwt = reinterpret_cast<uint32_t*>(ws + (size_t)RPW * 8 * W * 8);  // [RPW][W][8]
-    uint32_t* cell = rwt + RPW * 8 * W;
-    unsigned char* list = reinterpret_cast<unsigned char*>(cell + kGenCells);
-    for (int c = tid; c < 256; c += kThreads) {
-        if (OWNS) {
-            s_order[c] = cases->order[c];
-            s_cut[c] = cases->cut[c];
+    for (int c = threadIdx.x; c < 256; c += kThreads) {
+        if (GenPairTables<MODE>::OWNS) {
+            t.order[c] = cases->order[c];
+            t.cut[c] = cases->cut[c];
             if (MODE == kGenMC) continue;
         }
         const uint64_t w = cases->tris[c];
@@ -86,25 +78,35 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
             const uint64_t nib = e < 12 ? (((0x776653524140ull >> (4 * e)) & 7u) | (((0xA22u >> e) & 1u) << 3)) : 0u;
             x |= nib << (4 * q);
         }
-        s_tri[c] = x;
+        t.tri[c] = x;
     }
-    __syncthreads();  // the only CTA barrier: from here on every warp runs alone
-    // Caller grows buffers.  Past this check every record slot and triangle index written below lies
-    // under the totals, because the count pass derives the counts and starts from the same bit words
-    // with the same masks (cut_masks, tris_of_word); the writes are not checked one by one.
-    if ((long long)totals[0] > capV || (long long)totals[1] > capT) return;
+}
 
+// Work item `item` of an extraction, run by one warp with its ws_bytes of shared memory at ws.
+template <typename IndexT, int RPW, int MODE>
+__device__ __forceinline__ void gen_pairs_item(
+    uint32_t item, unsigned char* ws, const GenPairTables<MODE>& tabs, const uint32_t* __restrict__ bits,
+    const Grid& g, int KC, int ngroups, int nkc, int kbeg, int kend, int kemit, unsigned long long vbase,
+    unsigned long long tbase, const uint4* __restrict__ rowcnt, const RowStarts& rs, float* __restrict__ points,
+    IndexT* __restrict__ tris, uint32_t* __restrict__ fe2mc, int reverse)
+{
+    constexpr bool OWNS = GenPairTables<MODE>::OWNS;
+    constexpr int LPR = 32 / RPW;  // lanes per row
+    const uint64_t* s_tri = tabs.tri;
+    const uint64_t* s_order = tabs.order;
+    const uint16_t* s_cut = tabs.cut;
+    const int lane = threadIdx.x & 31, h = lane / LPR, lw = lane % LPR;
+    const int W = g.W;
+    uint2* mb = reinterpret_cast<uint2*>(ws);                                    // [RPW][8][W]
+    uint32_t* rwt = reinterpret_cast<uint32_t*>(ws + (size_t)RPW * 8 * W * 8);  // [RPW][W][8]
+    uint32_t* cell = rwt + RPW * 8 * W;
+    unsigned char* list = reinterpret_cast<unsigned char*>(cell + kGenCells);
     const bool in1 = lw + 1 < W;
     const uint32_t evalid = validmask(lw, g.nx - 1);  // x-edges / cells: i <= nx-2
     const uint32_t pvalid = validmask(lw, g.nx);      // points: i <= nx-1
     uint2* mbh = mb + h * 8 * W;
     uint32_t* rwth = rwt + h * 8 * W;
-    const uint32_t nitems = (uint32_t)ngroups * (uint32_t)nkc;
-    for (;;) {
-        uint32_t item = 0u;
-        if (lane == 0) item = atomicAdd(work, 1u);
-        item = __shfl_sync(0xffffffffu, item, 0);
-        if (item >= nitems) break;
+    {
         const int col = (int)(item / (uint32_t)ngroups);
         const int kc = reverse ? nkc - 1 - col : col;
         const int jw = RPW * (int)(item % (uint32_t)ngroups);
@@ -358,6 +360,69 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
     }
 }
 
+// One wave of CTAs; every warp takes work items from the counter `work` until none is left.
+template <typename IndexT, int RPW, int MODE>
+__global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs(
+    const uint32_t* __restrict__ bits, Grid g, int KC, int ngroups, int nkc, int kbeg, int kend,
+    int kemit, unsigned long long vbase, unsigned long long tbase, int ws_bytes,
+    const CaseTables* __restrict__ cases, const uint4* __restrict__ rowcnt, RowStarts rs,
+    const unsigned long long* __restrict__ totals, unsigned int* __restrict__ work, long long capV, long long capT,
+    float* __restrict__ points, IndexT* __restrict__ tris, uint32_t* __restrict__ fe2mc, int reverse)
+{
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    __shared__ GenPairTables<MODE> tabs;
+    gen_pair_tables<MODE>(cases, tabs);
+    __syncthreads();  // the only CTA barrier: from here on every warp runs alone
+    // Caller grows buffers.  Past this check every record slot and triangle index written below lies
+    // under the totals, because the count pass derives the counts and starts from the same bit words
+    // with the same masks (cut_masks, tris_of_word); the writes are not checked one by one.
+    if ((long long)totals[0] > capV || (long long)totals[1] > capT) return;
+    unsigned char* ws = s_raw + (size_t)(threadIdx.x >> 5) * ws_bytes;
+    const uint32_t nitems = (uint32_t)ngroups * (uint32_t)nkc;
+    for (;;) {
+        uint32_t item = 0u;
+        if ((threadIdx.x & 31) == 0) item = atomicAdd(work, 1u);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= nitems) break;
+        gen_pairs_item<IndexT, RPW, MODE>(item, ws, tabs, bits, g, KC, ngroups, nkc, kbeg, kend, kemit, vbase, tbase,
+                                          rowcnt, rs, points, tris, fe2mc, reverse);
+    }
+}
+
+// The Flying Edges generate items of a list of requests (batch_kernels.cuh), one launch: item x is item
+// x - first[q] of request list[q]; the items of a request whose mesh cannot hold its counts are skipped.
+template <typename IndexT, int RPW>
+__global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs_batch(
+    const BatchReq* __restrict__ reqs, const int* __restrict__ list, const unsigned* __restrict__ first, int m,
+    const CaseTables* __restrict__ cases, unsigned int* __restrict__ work, int ws_bytes, int reverse)
+{
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    __shared__ GenPairTables<kGenFE> tabs;
+    gen_pair_tables<kGenFE>(cases, tabs);
+    __syncthreads();
+    unsigned char* ws = s_raw + (size_t)(threadIdx.x >> 5) * ws_bytes;
+    const uint32_t nitems = __ldg(&first[m]);
+    for (;;) {
+        uint32_t item = 0u;
+        if ((threadIdx.x & 31) == 0) item = atomicAdd(work, 1u);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= nitems) break;
+        const int q = batch_find(first, m, item);
+        const BatchReq* d = reqs + __ldg(&list[q]);
+        if ((long long)d->totals[0] > d->capV || (long long)d->totals[1] > d->capT) continue;
+        const Grid g = d->g;
+        RowStarts rs;
+        rs.starts = d->starts;
+        rs.R = g.R;
+        rs.ny = g.ny;
+        rs.kr = g.kr;
+        rs.add[0] = rs.add[1] = rs.add[2] = rs.add[3] = 0;
+        gen_pairs_item<IndexT, RPW, kGenFE>(item - __ldg(&first[q]), ws, tabs, d->bits, g, d->gen_KC, d->gen_ngroups,
+                                            d->gen_nkc, g.kr, g.ke, g.kr, 0ull, 0ull, d->rowcnt, rs, d->points,
+                                            static_cast<IndexT*>(d->tris), nullptr, reverse);
+    }
+}
+
 // Rows of up to 16 words (gen_plan's fits, and W <= 16) in MODE over the
 // plan's planes [kbeg, kend).
 template <typename IndexT, int MODE>
@@ -367,12 +432,13 @@ void launch_gen_pairs_impl(const Grid& g, const CaseTables* cases, const FeBuffe
 {
     const int nzw = p.kend - p.kbeg;
     if (nzw <= 0) return;
-    // items of KC planes: about four per warp of one wave, at least 4 planes
+    // items of KC planes: about sixteen per warp of one wave, at least 2 planes (the last items are short, so
+    // the warps finish together: 512^3 FE 181 -> 169 us against four per warp and 4 planes)
     const int rpw = g.W <= 4 ? 8 : (g.W <= 8 ? 4 : 2);
     const long long npairs = (g.ny + rpw - 1) / rpw;  // row groups
     const long long warps = (long long)nsm * kGenPairCtasPerSm * kGenRows;
-    long long KC = (npairs * nzw + 4 * warps - 1) / (4 * warps);
-    if (KC < 4) KC = 4;
+    long long KC = (npairs * nzw + 16 * warps - 1) / (16 * warps);
+    if (KC < 2) KC = 2;
     while (npairs * ((nzw + KC - 1) / KC) >= (1ll << 31)) KC *= 2;  // item numbers stay below 2^31
     if (KC > nzw) KC = nzw;
     const int nkc = (int)((nzw + KC - 1) / KC);

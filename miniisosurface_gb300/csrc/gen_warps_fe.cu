@@ -94,6 +94,86 @@ bool launch_fe_vertices_narrow(const void* vol, int dtype, const Grid& g, float 
     return true;
 }
 
+// The Flying Edges vertices of a list of requests (batch_kernels.cuh), one launch over the concatenation of
+// their slots: slot v belongs to request list[q] for vfirst[q] <= v < vfirst[q + 1].  A CTA takes chunks of
+// kVertexChunk consecutive slots (chunk c, c + gridDim.x, ...) and walks the requests a chunk overlaps -- one,
+// nearly always -- with the request's parameters in shared memory (every thread sees the same requests, so
+// the barriers are uniform); each thread loads its next slot's record before it works on the current one.
+constexpr int kVertexChunk = 4 * kThreads;
+
+__global__ void __launch_bounds__(kThreads, vertex_ctas_per_sm(false))
+    k_vertices_batch(const BatchReq* __restrict__ reqs, const int* __restrict__ list,
+                     const unsigned long long* __restrict__ vfirst, int m)
+{
+    __shared__ BatchReq s_d;
+    constexpr int kReqWords = (int)(sizeof(BatchReq) / 4);
+    const unsigned long long n = __ldg(&vfirst[m]);
+    for (unsigned long long base = (unsigned long long)blockIdx.x * kVertexChunk; base < n;
+         base += (unsigned long long)gridDim.x * kVertexChunk) {
+        const unsigned long long end = min(base + kVertexChunk, n);
+        int q = 0, hi = m - 1;  // the last q with vfirst[q] <= base
+        while (q < hi) {
+            const int mid = (q + hi + 1) >> 1;
+            if (__ldg(&vfirst[mid]) <= base) q = mid;
+            else hi = mid - 1;
+        }
+        for (; q < m; ++q) {
+            const unsigned long long v0 = __ldg(&vfirst[q]);
+            if (v0 >= end) break;
+            const unsigned long long lo = max(v0, base), v1 = min(__ldg(&vfirst[q + 1]), end);
+            if (v1 <= lo) continue;  // no slots of request q in the chunk
+            __syncthreads();         // the previous request's reads of s_d are done
+            if (threadIdx.x < kReqWords)
+                reinterpret_cast<uint32_t*>(&s_d)[threadIdx.x] =
+                    __ldg(reinterpret_cast<const uint32_t*>(reqs + __ldg(&list[q])) + threadIdx.x);
+            __syncthreads();
+            float* points = s_d.points;
+            unsigned long long v = lo + threadIdx.x;
+            uint2 next = v < v1 ? vertex_record(points, v - v0) : make_uint2(0u, 0u);
+            for (; v < v1; v += kThreads) {
+                const uint2 r = next;
+                if (v + kThreads < v1) next = vertex_record(points, v + kThreads - v0);
+                vertex_of_record<false, float>(s_d.vol, s_d.g, s_d.gs, s_d.iso, s_d.g.kr, s_d.g.ke, r, v - v0,
+                                               points, s_d.normals);
+            }
+        }
+    }
+}
+
+size_t gen_batch_ws_bytes(int W, int rpw) { return gen_pair_scratch_bytes(W, rpw, kGenFE); }
+
+void launch_gen_batch(int rpw, int index_bytes, const BatchReq* reqs, const int* list, const unsigned* first, int m,
+                      unsigned nitems, const CaseTables* cases, unsigned* work, int ws_bytes, int reverse, int nsm,
+                      cudaStream_t s)
+{
+    long long blocks = ((long long)nitems + kGenRows - 1) / kGenRows;
+    if (blocks > (long long)nsm * kGenPairCtasPerSm) blocks = (long long)nsm * kGenPairCtasPerSm;
+    if (blocks < 1) return;
+    const size_t smem = (size_t)kGenRows * ws_bytes;
+#define ISO_GEN_BATCH(T, R)                                                                                    \
+    {                                                                                                          \
+        auto kern = k_gen_pairs_batch<T, R>;                                                                   \
+        allow_smem(kern, smem);                                                                                \
+        kern<<<(unsigned)blocks, kThreads, smem, s>>>(reqs, list, first, m, cases, work, ws_bytes, reverse);    \
+    }
+    if (index_bytes == 4) {
+        if (rpw == 8) ISO_GEN_BATCH(uint32_t, 8)
+        else if (rpw == 4) ISO_GEN_BATCH(uint32_t, 4)
+        else ISO_GEN_BATCH(uint32_t, 2)
+    } else {
+        if (rpw == 8) ISO_GEN_BATCH(uint64_t, 8)
+        else if (rpw == 4) ISO_GEN_BATCH(uint64_t, 4)
+        else ISO_GEN_BATCH(uint64_t, 2)
+    }
+#undef ISO_GEN_BATCH
+}
+
+void launch_vertices_batch(const BatchReq* reqs, const int* list, const unsigned long long* vfirst, int m, int nsm,
+                           cudaStream_t s)
+{
+    k_vertices_batch<<<(unsigned)(nsm * vertex_ctas_per_sm(false)), kThreads, 0, s>>>(reqs, list, vfirst, m);
+}
+
 template void launch_fe_gen_warps<uint32_t>(const float*, const Grid&, float, const CaseTables*, const FeBuffers&,
                                             const CountPlan&, const GenPlan&, long long, long long, float*, float*,
                                             uint32_t*, int, cudaStream_t);

@@ -92,21 +92,13 @@ __device__ __forceinline__ uint2 vertex_record(const float* points, unsigned lon
 // -- one thread each, slot v = vertex vbase + v.  MC: the records carry the
 // owner cell.  The capacity test is the generate kernels': when it fails they
 // wrote no record and nothing is read here.
-template <bool MC, int COMP, typename S = float>
-__global__ void __launch_bounds__(kThreads, vertex_ctas_per_sm(MC))
-    k_vertices(const S* __restrict__ vol, Grid g, GradScale gs, float iso, int kbeg, int kend,
-               const unsigned long long* __restrict__ starts, const unsigned long long* __restrict__ totals,
-               long long capV, long long capT, float* __restrict__ points, float* __restrict__ normals)
+// The vertex of slot v from its record r (k_vertices, and the batch kernel of gen_warps_fe.cu).
+template <bool MC, typename S>
+__device__ __forceinline__ void vertex_of_record(const S* __restrict__ vol, const Grid& g, const GradScale& gs,
+                                                 float iso, int kbeg, int kend, uint2 r, unsigned long long v,
+                                                 float* __restrict__ points, float* __restrict__ normals)
 {
-    if ((long long)totals[0] > capV || (long long)totals[1] > capT) return;
-    auto first = [&](int p) { return p < g.ke ? starts[COMP * g.R + (long long)(p - g.kr) * g.ny] : totals[COMP]; };
-    const unsigned long long n = first(kend) - first(kbeg);
-    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
-    unsigned long long v = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
-    uint2 next = v < n ? vertex_record(points, v) : make_uint2(0u, 0u);
-    for (; v < n; v += stride) {
-        const uint2 r = next;
-        if (v + stride < n) next = vertex_record(points, v + stride);  // this thread's next slot
+    {
         const int i = (int)(r.x & 1023u), a = (int)((r.x >> 10) & 3u);
         int j, kk, ci, cj, ck;
         if (MC) {
@@ -126,12 +118,32 @@ __global__ void __launch_bounds__(kThreads, vertex_ctas_per_sm(MC))
         // every slot holds a record of the launch's rows; anything else is left alone, never read through
         if (a > 2 || i + (a == 0) >= g.nx || j + (a == 1) >= g.ny || kk + (a == 2) >= g.nz || ci < 0 || cj < 0 ||
             ck < 0 || ci > g.nx - 2 || cj > g.ny - 2 || (MC ? (ck < kbeg || ck >= kend) : (kk < kbeg || kk >= kend)))
-            continue;
+            return;
         float3 p, nm;
         vertex_any_axis<S>(vol, g, gs, iso, a, i, j, kk, ci, cj, ck, p, nm);
         store_vertex(points, normals, v, p, nm);
     }
 }
+
+template <bool MC, int COMP, typename S = float>
+__global__ void __launch_bounds__(kThreads, vertex_ctas_per_sm(MC))
+    k_vertices(const S* __restrict__ vol, Grid g, GradScale gs, float iso, int kbeg, int kend,
+               const unsigned long long* __restrict__ starts, const unsigned long long* __restrict__ totals,
+               long long capV, long long capT, float* __restrict__ points, float* __restrict__ normals)
+{
+    if ((long long)totals[0] > capV || (long long)totals[1] > capT) return;
+    auto first = [&](int p) { return p < g.ke ? starts[COMP * g.R + (long long)(p - g.kr) * g.ny] : totals[COMP]; };
+    const unsigned long long n = first(kend) - first(kbeg);
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    unsigned long long v = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    uint2 next = v < n ? vertex_record(points, v) : make_uint2(0u, 0u);
+    for (; v < n; v += stride) {
+        const uint2 r = next;
+        if (v + stride < n) next = vertex_record(points, v + stride);  // this thread's next slot
+        vertex_of_record<MC, S>(vol, g, gs, iso, kbeg, kend, r, v, points, normals);
+    }
+}
+
 
 // Vertices of the rows of planes [k0, k1) from their records.
 template <bool MC, int COMP, typename S = float>

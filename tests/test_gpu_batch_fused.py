@@ -1,0 +1,169 @@
+"""GPU: fused batches (iso_batch_set_fused, batch_kernels.cuh) -- the Flying
+Edges requests of rows up to 512 points run one launch per pass -- against the
+same batch on the lanes, against one iso_extract_device call per request and
+against the oracle.
+
+Bar: every request's mesh and counts bit-identical, whatever the count
+variant (rows per warp 8 / 4 / 2, row length a multiple of 4 points or not,
+rows of exactly 128 / 256 / 512 points), index width, graph or direct launch,
+with requests on the lanes beside them (Marching Cubes, long rows, a volume
+not at a 16-byte boundary), a mesh too small for its counts, and more than
+1,024 requests (several per thread of the vertex prefix).
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle_lib
+
+pytestmark = pytest.mark.gpu
+
+WIDTHS = [37, 64, 128, 150, 160, 256, 301, 300, 512]  # every count variant of rows up to 16 words
+
+
+@pytest.fixture(scope="module")
+def M(cuda):
+    import miniisosurface_gb300 as M
+    return M
+
+
+def dev(vol):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(vol, dtype=np.float32).reshape(-1)).cuda()
+
+
+def as_np(m):
+    return (m.points[: m.n_points].cpu().numpy().view(np.uint32), m.normals[: m.n_points].cpu().numpy().view(np.uint32),
+            m.tris[: m.n_tris].cpu().numpy().astype(np.uint64))
+
+
+def same(a, b, what):
+    for x, y, name in zip(a, b, ("points", "normals", "triangles")):
+        assert x.shape == y.shape, "%s: %s shape %s vs %s" % (what, name, x.shape, y.shape)
+        assert np.array_equal(x, y), "%s: %s differ" % (what, name)
+
+
+def requests(M):
+    """(request, index bytes, host volume): the nine widths, two index widths, blobs and noise, spacing and
+    origin, with lane requests mixed in."""
+    import torch
+    out = []
+    for i, nx in enumerate(WIDTHS):
+        dims = (nx, 20 + 7 * i, 11 + 3 * i)
+        vol = M.generate_blobs(dims, 6, seed=i) if i % 2 else M.generate_value_noise(dims, 3, 16, seed=i)
+        lo, hi = np.percentile(vol, [20, 80])
+        iso = float(np.float32(lo + (hi - lo) * (0.3 + 0.05 * i)))
+        sp = (1.0, 1.0, 1.0) if i % 3 else (0.5, 1.25, 2.0)
+        org = (0.0, 0.0, 0.0) if i % 4 else (-3.0, 1.5, 0.25)
+        out.append((M.Request(dev(vol), dims, iso, M.FLYING_EDGES, sp, org), 8 if i % 4 == 3 else 4, vol))
+    # on the lanes: Marching Cubes, rows longer than 16 words, a volume one sample past a 16-byte boundary
+    v = M.generate_value_noise((70, 30, 25), 3, 16, seed=40)
+    out.append((M.Request(dev(v), (70, 30, 25), 0.0, M.MARCHING_CUBES), 4, v))
+    v = M.generate_value_noise((700, 12, 9), 3, 16, seed=41)
+    out.append((M.Request(dev(v), (700, 12, 9), 0.0, M.FLYING_EDGES), 4, v))
+    v = M.generate_value_noise((96, 40, 30), 3, 16, seed=42)
+    flat = torch.zeros(v.size + 1, dtype=torch.float32, device="cuda")
+    flat[1:] = dev(v)
+    out.append((M.Request(flat[1:], (96, 40, 30), 0.0, M.FLYING_EDGES), 4, v))
+    # no surface, and a two-point grid
+    v = M.generate_value_noise((48, 20, 10), 3, 16, seed=43)
+    out.append((M.Request(dev(v), (48, 20, 10), 10.0, M.FLYING_EDGES), 4, v))
+    v = np.array([[[0.0, 1.0], [1.0, 0.0]], [[1.0, 0.0], [0.0, 1.0]]], dtype=np.float32)
+    out.append((M.Request(dev(v), (2, 2, 2), 0.5, M.FLYING_EDGES), 4, v))
+    return out
+
+
+def run(M, reqs, fused, graph=True, lanes=3, ctx=None):
+    ctx = ctx or M.default_context()
+    M.set_batch_fused(fused, ctx)
+    M.set_batch_graph(graph, ctx)
+    M.set_batch_lanes(lanes, ctx)
+    M.set_batch_split(1, ctx)
+    try:
+        return [as_np(m) for m in M.extract_batch([r for r, _, _ in reqs], [M.DeviceMesh(0, 0, ib) for _, ib, _ in reqs],
+                                                  ctx=ctx)]
+    finally:
+        M.set_batch_fused(True, ctx)
+        M.set_batch_graph(True, ctx)
+        M.set_batch_lanes(0, ctx)
+        M.set_batch_split(0, ctx)
+
+
+def test_fused_equals_lanes_plain_and_oracle(M):
+    reqs = requests(M)
+    fused = run(M, reqs, True)
+    lanes = run(M, reqs, False)
+    direct = run(M, reqs, True, graph=False)
+    for i, ((r, ib, vol), a, b, c) in enumerate(zip(reqs, fused, lanes, direct)):
+        what = "request %d %s" % (i, r.dims)
+        same(a, b, what + " fused vs lanes")
+        same(a, c, what + " graph vs direct")
+        p = M.extract_device(r.volume, r.dims, r.isoval, r.algorithm, r.spacing, r.origin, index_bytes=ib)
+        same(a, as_np(p), what + " fused vs plain")
+    for i in (0, 4, 8):  # unaligned 8 rows per warp, aligned 4, full 2
+        r, ib, vol = reqs[i]
+        ref = oracle_lib.fe(vol, r.isoval, r.spacing, r.origin)
+        same(fused[i], (ref[0].view(np.uint32), ref[1].view(np.uint32), ref[2].astype(np.uint64)),
+             "request %d vs oracle" % i)
+
+
+def test_fused_capacity_replay_and_counts(M):
+    from miniisosurface_gb300 import _lib
+    lib = _lib.load()
+    reqs = requests(M)
+    rs = [r for r, _, _ in reqs]
+    sizes = [M.count_device(r.volume, r.dims, r.isoval, r.algorithm) for r in rs]
+    ctx = M.Context(0)
+    M.set_batch_lanes(2, ctx)
+    M.set_batch_split(1, ctx)
+    meshes = [M.DeviceMesh(v, t, ib) for (v, t), (_, ib, _) in zip(sizes, reqs)]
+    small, small_t = 2, 5  # fused requests: one point too few, one triangle too few
+    meshes[small] = M.DeviceMesh(sizes[small][0] - 1, sizes[small][1], reqs[small][1])
+    meshes[small_t] = M.DeviceMesh(sizes[small_t][0], sizes[small_t][1] - 1, reqs[small_t][1])
+    b = M.Batch(rs, meshes)
+    want = [as_np(M.extract_device(r.volume, r.dims, r.isoval, r.algorithm, r.spacing, r.origin, index_bytes=ib))
+            for r, ib, _ in reqs]
+    for rep in range(3):  # capture, then replays of the graph over poisoned outputs
+        for m in meshes:
+            if m.points.numel():
+                m.points.fill_(7.0)
+            if m.tris.numel():
+                m.tris.fill_(-1)
+        codes = b.run(ctx)
+        for i, c in enumerate(codes):
+            bad = i in (small, small_t)
+            assert c == (_lib.ISO_ERR_CAPACITY if bad else _lib.ISO_OK), (rep, i, c)
+            assert (meshes[i].n_points, meshes[i].n_tris) == sizes[i], (rep, i)
+            if not bad:
+                same(as_np(meshes[i]), want[i], "rep %d request %d" % (rep, i))
+    # counts only, fused and on the lanes
+    arr = (_lib.IsoRequest * len(rs))(*[r.descriptor() for r in rs])
+    for fused in (1, 0):
+        lib.iso_batch_set_fused(ctx.handle, fused)
+        nv, nt = (C.c_int64 * len(rs))(), (C.c_int64 * len(rs))()
+        assert lib.iso_count_batch(ctx.handle, len(rs), arr, nv, nt, None, None) == _lib.ISO_OK
+        assert [(nv[i], nt[i]) for i in range(len(rs))] == sizes, fused
+    lib.iso_batch_set_fused(ctx.handle, 1)
+
+
+def test_fused_many_requests(M):
+    """1,100 small requests over 25 volumes (several per thread of the vertex prefix), direct launch."""
+    import torch
+    rng = np.random.default_rng(3)
+    vols = []
+    for v in range(25):
+        dims = tuple(int(x) for x in rng.integers(6, 40, size=3))
+        vols.append((dims, dev(M.generate_value_noise(dims, 2, 8, seed=100 + v))))
+    reqs = []
+    for q in range(1100):
+        dims, dv = vols[q % len(vols)]
+        reqs.append((M.Request(dv, dims, float(np.float32(rng.uniform(-0.3, 0.3))), M.FLYING_EDGES), 4, None))
+    fused = run(M, reqs, True, graph=False, lanes=4)
+    lanes = run(M, reqs, False, graph=False, lanes=4)
+    for i, (a, b) in enumerate(zip(fused, lanes)):
+        same(a, b, "request %d" % i)
+    for i in range(0, 1100, 97):
+        r = reqs[i][0]
+        same(fused[i], as_np(M.extract_device(r.volume, r.dims, r.isoval)), "request %d vs plain" % i)
+    torch.cuda.synchronize()
