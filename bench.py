@@ -439,17 +439,30 @@ def batched_leg(M, lib, dev, reps):
             best.append(time.perf_counter() - t0)
         return statistics.median(best)
 
+    # every request on the lanes (iso_batch_set_fused 0), the autotuner's lanes and split
+    M.set_batch_fused(False, ctx)
     M.set_batch_lanes(0, ctx)
-    batched()  # the autotuner's first batch
+    M.set_batch_split(0, ctx)
+    batched()
     lanes, split = M.batch_lanes(ctx), M.batch_split(ctx)
+    t_lanes = seconds(batched)
+    lanes_m = [(m.points[: m.n_points].clone(), m.normals[: m.n_points].clone(), m.tris[: m.n_tris].clone())
+               for m in batch_m]
+    # the default: one launch per pass and kernel variant for all of them
+    M.set_batch_fused(True, ctx)
+    M.set_batch_lanes(0, ctx)
+    M.set_batch_split(0, ctx)
+    batched()
     t_batch = seconds(batched)
     t_plain = seconds(plain)
     t_async = seconds(plain_async)
     same = True
-    for a, b in zip(plain_m, batch_m):
+    for a, b, l in zip(plain_m, batch_m, lanes_m):
         same &= bool(torch.equal(a.points[: b.n_points], b.points[: b.n_points]))
         same &= bool(torch.equal(a.normals[: b.n_points], b.normals[: b.n_points]))
         same &= bool(torch.equal(a.tris[: b.n_tris], b.tris[: b.n_tris]))
+        same &= all(bool(torch.equal(x, y)) for x, y in zip(l, (b.points[: b.n_points], b.normals[: b.n_points],
+                                                                 b.tris[: b.n_tris])))
     same &= all((b.n_points, b.n_tris) == s for b, s in zip(batch_m, sizes))
     mc = lambda s: cells / s / 1e6
     return {
@@ -459,9 +472,12 @@ def batched_leg(M, lib, dev, reps):
         "vertices": int(sum(s[0] for s in sizes)), "triangles": int(sum(s[1] for s in sizes)),
         "plain": {"ms": 1e3 * t_plain, "value": mc(t_plain), "unit": METRIC},
         "plain_async": {"ms": 1e3 * t_async, "value": mc(t_async), "unit": METRIC},
-        "batched": {"ms": 1e3 * t_batch, "value": mc(t_batch), "unit": METRIC, "lanes": lanes,
-                    "split": split},
+        "batched": {"ms": 1e3 * t_batch, "value": mc(t_batch), "unit": METRIC,
+                    "what": "one launch per pass and kernel variant, the variants side by side (iso_batch_set_fused)"},
+        "batched_lanes": {"ms": 1e3 * t_lanes, "value": mc(t_lanes), "unit": METRIC, "lanes": lanes, "split": split,
+                          "what": "every request's passes on one of L streams, one CUDA graph"},
         "speedup_vs_plain": t_plain / t_batch, "speedup_vs_plain_async": t_async / t_batch,
+        "speedup_vs_lanes": t_lanes / t_batch,
         "identical_output": same,
     }
 
@@ -592,10 +608,12 @@ def served_leg(M, dev, nreq, seed=4, npool=8):
     server = serve.Server(volumes, slots=3, max_batch=64, budget_bytes=120 << 30, lanes=8, device=dev.index or 0)
     server_p = serve.Server(volumes, slots=3, max_batch=64, budget_bytes=120 << 30, lanes=8, device=dev.index or 0,
                             predictor=P.Predictor.load(device=dev)) if P.WEIGHTS.exists() else None
-    serve.run_plain(volumes, reqs_at(np.zeros(nreq))[:8], device=dev.index or 0)  # warm-up
-    server.run(reqs_at(np.zeros(nreq))[:16])
+    # warm-up: the plain loop, and one saturated pass of each server (its slots' batch buffers reach the
+    # sizes the timed runs need)
+    serve.run_plain(volumes, reqs_at(np.zeros(nreq))[:8], device=dev.index or 0)
+    server.run(reqs_at(np.zeros(nreq)))
     if server_p:
-        server_p.run(reqs_at(np.zeros(nreq))[:16])
+        server_p.run(reqs_at(np.zeros(nreq)))
 
     def served_p(times, keep=False):
         res = server_p.run(reqs_at(times), keep_meshes=keep)
