@@ -286,13 +286,15 @@ int iso_batch_split(const iso_ctx* ctx);
  * library's own calls take turns with captures). */
 iso_status iso_batch_set_graph(iso_ctx* ctx, int enable);
 int iso_batch_lanes(const iso_ctx* ctx);
-/* Whether the context's batches run their Flying Edges requests of rows up
- * to 512 points (volume at a 16-byte boundary) fused (1, the default): one
- * kernel launch per pass and kernel variant covers all of them, each request
- * with its own scratch, instead of the passes of each request on a lane.  The
- * other requests take the lanes beside them.  The meshes are the same either
- * way.  0: every request on the lanes. */
-iso_status iso_batch_set_fused(iso_ctx* ctx, int enable);
+/* How the context's batches run their Flying Edges requests of rows up to
+ * 512 points (volume at a 16-byte boundary): fused, one kernel launch per
+ * pass and kernel variant covering all of them, each request with its own
+ * scratch, or each request's passes on a lane.  The other requests take the
+ * lanes beside the fused launches.  The meshes are the same either way.
+ * mode 0: every request on the lanes; 1 (the default): fused when a batch
+ * holds at least 16 such requests (fewer run faster on the lanes); 2: always
+ * fused.  Other modes: ISO_ERR_INVALID_ARG. */
+iso_status iso_batch_set_fused(iso_ctx* ctx, int mode);
 
 /* z-slabs: the grid split along z into slabs of planes [k0, k1), for
  * sharding over GPUs or streaming a volume that does not fit (no counterpart

@@ -450,11 +450,11 @@ def set_batch_graph(enable, ctx=None):
     check(load().iso_batch_set_graph(ctx.handle, 1 if enable else 0), ctx.handle)
 
 
-def set_batch_fused(enable, ctx=None):
-    """Run a batch's Flying Edges requests of rows up to 512 points one launch per pass (default) or every
-    request on the lanes (iso_batch_set_fused)."""
+def set_batch_fused(mode, ctx=None):
+    """How a batch runs its Flying Edges requests of rows up to 512 points (iso_batch_set_fused): False / 0 on the
+    lanes, True / 1 (default) one launch per pass when at least 16 of them, 2 always one launch per pass."""
     ctx = ctx or default_context()
-    check(load().iso_batch_set_fused(ctx.handle, 1 if enable else 0), ctx.handle)
+    check(load().iso_batch_set_fused(ctx.handle, int(mode)), ctx.handle)
 
 
 def batch_lanes(ctx=None):

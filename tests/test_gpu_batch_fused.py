@@ -74,9 +74,10 @@ def requests(M):
     return out
 
 
-def run(M, reqs, fused, graph=True, lanes=3, ctx=None):
+def run(M, reqs, mode, graph=True, lanes=3, ctx=None):
+    """The batch with iso_batch_set_fused(mode): 0 lanes, 1 the default, 2 always fused."""
     ctx = ctx or M.default_context()
-    M.set_batch_fused(fused, ctx)
+    M.set_batch_fused(mode, ctx)
     M.set_batch_graph(graph, ctx)
     M.set_batch_lanes(lanes, ctx)
     M.set_batch_split(1, ctx)
@@ -92,12 +93,14 @@ def run(M, reqs, fused, graph=True, lanes=3, ctx=None):
 
 def test_fused_equals_lanes_plain_and_oracle(M):
     reqs = requests(M)
-    fused = run(M, reqs, True)
-    lanes = run(M, reqs, False)
-    direct = run(M, reqs, True, graph=False)
-    for i, ((r, ib, vol), a, b, c) in enumerate(zip(reqs, fused, lanes, direct)):
+    fused = run(M, reqs, 2)
+    lanes = run(M, reqs, 0)
+    direct = run(M, reqs, 2, graph=False)
+    auto = run(M, reqs, 1)  # the default: 9 requests qualify, fewer than 16, so all of them on the lanes
+    for i, ((r, ib, vol), a, b, c, d) in enumerate(zip(reqs, fused, lanes, direct, auto)):
         what = "request %d %s" % (i, r.dims)
         same(a, b, what + " fused vs lanes")
+        same(a, d, what + " fused vs default")
         same(a, c, what + " graph vs direct")
         p = M.extract_device(r.volume, r.dims, r.isoval, r.algorithm, r.spacing, r.origin, index_bytes=ib)
         same(a, as_np(p), what + " fused vs plain")
@@ -117,6 +120,7 @@ def test_fused_capacity_replay_and_counts(M):
     ctx = M.Context(0)
     M.set_batch_lanes(2, ctx)
     M.set_batch_split(1, ctx)
+    M.set_batch_fused(2, ctx)
     meshes = [M.DeviceMesh(v, t, ib) for (v, t), (_, ib, _) in zip(sizes, reqs)]
     small, small_t = 2, 5  # fused requests: one point too few, one triangle too few
     meshes[small] = M.DeviceMesh(sizes[small][0] - 1, sizes[small][1], reqs[small][1])
@@ -139,16 +143,18 @@ def test_fused_capacity_replay_and_counts(M):
                 same(as_np(meshes[i]), want[i], "rep %d request %d" % (rep, i))
     # counts only, fused and on the lanes
     arr = (_lib.IsoRequest * len(rs))(*[r.descriptor() for r in rs])
-    for fused in (1, 0):
+    for fused in (2, 0):
         lib.iso_batch_set_fused(ctx.handle, fused)
         nv, nt = (C.c_int64 * len(rs))(), (C.c_int64 * len(rs))()
         assert lib.iso_count_batch(ctx.handle, len(rs), arr, nv, nt, None, None) == _lib.ISO_OK
         assert [(nv[i], nt[i]) for i in range(len(rs))] == sizes, fused
     lib.iso_batch_set_fused(ctx.handle, 1)
+    assert lib.iso_batch_set_fused(ctx.handle, 3) == _lib.ISO_ERR_INVALID_ARG
 
 
 def test_fused_many_requests(M):
-    """1,100 small requests over 25 volumes (several per thread of the vertex prefix), direct launch."""
+    """1,100 small requests over 25 volumes (several per thread of the vertex prefix), direct launch, fused by
+    default (more than 16 requests)."""
     import torch
     rng = np.random.default_rng(3)
     vols = []
@@ -159,8 +165,8 @@ def test_fused_many_requests(M):
     for q in range(1100):
         dims, dv = vols[q % len(vols)]
         reqs.append((M.Request(dv, dims, float(np.float32(rng.uniform(-0.3, 0.3))), M.FLYING_EDGES), 4, None))
-    fused = run(M, reqs, True, graph=False, lanes=4)
-    lanes = run(M, reqs, False, graph=False, lanes=4)
+    fused = run(M, reqs, 1, graph=False, lanes=4)
+    lanes = run(M, reqs, 0, graph=False, lanes=4)
     for i, (a, b) in enumerate(zip(fused, lanes)):
         same(a, b, "request %d" % i)
     for i in range(0, 1100, 97):

@@ -48,14 +48,17 @@ def test_served_equals_alone_and_plain(M):
     sizes = [M.count_device(volumes[vi][0], volumes[vi][1], iso, algo) for _, vi, iso, algo in reqs]
     budget = 3 * int(np.mean([serve.mesh_bytes(v, t) for v, t in sizes]))
     server = serve.Server(volumes, slots=2, max_batch=8, budget_bytes=budget, lanes=3)
-    # continuous batching itself: every request through the slots' batches
+    # continuous batching itself: every request through the slots' batches, a slot starting beside a running
+    # one as soon as anything waits
     server.inline_idle = server.single_direct = False
+    server.overlap_backlog = 1
     served = server.run(reqs, keep_meshes=True)
     server.inline_idle = server.single_direct = True
+    server.overlap_backlog = 4
     plain = serve.run_plain(volumes, reqs, keep_meshes=True)
     assert max(np.bincount([r.batch for r in served])) > 1, "no batch held more than one request"
-    # light load (the defaults): requests that find the server idle run at once on the receiving thread, one
-    # waiting request runs alone on a slot; the same meshes
+    # light load (the defaults): requests that find the server idle run at once on the receiving thread, a
+    # slot starts beside running work only behind a backlog; the same meshes
     slow = [(float(t) * 40.0, vi, iso, algo) for t, vi, iso, algo in reqs[:6]]
     light = server.run(slow, keep_meshes=True)
     assert any(r.slot == -1 for r in light), "no request ran on the receiving thread"
