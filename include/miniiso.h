@@ -204,6 +204,25 @@ typedef struct iso_request {
 } iso_request;
 iso_status iso_extract_batch(iso_ctx* ctx, int64_t n, const iso_request* req, iso_mesh* out, iso_status* status,
                              void* stream);
+/* Batched extraction into one packed output, with no host round trip
+ * between a request's counts and its mesh: request r's vertices go to
+ * points / normals [point_first[r], point_first[r] + n_points[r]) and its
+ * triangles to tris [tri_first[r], tri_first[r] + n_tris[r]) (index_bytes 4
+ * or 8 per index, three per triangle), each request's indices counting from
+ * its own first vertex, as in its own mesh.  point_first / tri_first are the
+ * sums of the counts of the requests before it, so the meshes lie one after
+ * another.  A request placed past cap_points or cap_tris (or with 2^32
+ * vertices or more and 32-bit indices) writes nothing and gets
+ * ISO_ERR_CAPACITY (ISO_ERR_OVERFLOW) with its sizes; the others complete.
+ * Every request must be Flying Edges with rows of at most 512 points and its
+ * volume at a 16-byte boundary (else ISO_ERR_INVALID_ARG for it).  All passes
+ * of all requests run as one launch per pass and kernel variant.  The five
+ * output arrays have n entries; status may be NULL.  Synchronises the stream;
+ * returns ISO_OK or the first failing request's status. */
+iso_status iso_extract_batch_packed(iso_ctx* ctx, int64_t n, const iso_request* req, float* points, float* normals,
+                                    void* tris, int32_t index_bytes, int64_t cap_points, int64_t cap_tris,
+                                    int64_t* point_first, int64_t* tri_first, int64_t* n_points, int64_t* n_tris,
+                                    iso_status* status, void* stream);
 
 /* Counts only (passes 1-3) of a batch of requests, the same lanes and graph
  * as iso_extract_batch without the generate passes: n_points[r] / n_tris[r]

@@ -80,6 +80,10 @@ SIGNATURES = {
                                    C.POINTER(IsoMesh), C.c_void_p]),
     "iso_extract_batch": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(IsoRequest), C.POINTER(IsoMesh),
                                     C.POINTER(C.c_int), C.c_void_p]),
+    "iso_extract_batch_packed": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(IsoRequest), C.c_void_p, C.c_void_p,
+                                           C.c_void_p, C.c_int32, C.c_int64, C.c_int64, C.POINTER(C.c_int64),
+                                           C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                           C.POINTER(C.c_int), C.c_void_p]),
     "iso_count_batch": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(IsoRequest), C.POINTER(C.c_int64),
                                   C.POINTER(C.c_int64), C.POINTER(C.c_int), C.c_void_p]),
     "iso_batch_set_lanes": (C.c_int, [C.c_void_p, C.c_int]),

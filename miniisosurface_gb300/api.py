@@ -395,6 +395,68 @@ class Batch:
         return codes
 
 
+class PackedBuffers:
+    """Device buffers of packed batches (iso_extract_batch_packed), reused from batch to batch and grown
+    (a quarter more than asked) when a batch needs more."""
+
+    def __init__(self, cap_points=0, cap_tris=0, index_bytes=4, device="cuda"):
+        self.index_bytes = index_bytes
+        self.device = device
+        self.points = self.normals = self.tris = None
+        self.reserve(cap_points, cap_tris)
+
+    def reserve(self, cap_points, cap_tris):
+        import torch
+        have_p = self.points.shape[0] if self.points is not None else 0
+        have_t = self.tris.shape[0] if self.tris is not None else 0
+        if cap_points > have_p or self.points is None:
+            n = max(cap_points + cap_points // 4, 1)
+            self.points = self.normals = None
+            self.points = torch.empty((n, 3), dtype=torch.float32, device=self.device)
+            self.normals = torch.empty((n, 3), dtype=torch.float32, device=self.device)
+        if cap_tris > have_t or self.tris is None:
+            n = max(cap_tris + cap_tris // 4, 1)
+            self.tris = None
+            self.tris = torch.empty((n, 3), dtype=torch.int32 if self.index_bytes == 4 else torch.int64,
+                                    device=self.device)
+
+
+def extract_batch_packed(requests, buffers=None, index_bytes=4, ctx=None, stream=None):
+    """Batched extraction into one set of buffers (iso_extract_batch_packed): a list of Request (Flying Edges,
+    rows of at most 512 points) in, one DeviceMesh per request out, each a view into `buffers` (a
+    PackedBuffers, made or grown as needed) holding what extract_device gives for its request.  A batch that
+    does not fit grows the buffers to its total and runs again."""
+    import torch
+    lib = load()
+    requests = list(requests)
+    n = len(requests)
+    if buffers is None:
+        buffers = PackedBuffers(0, 0, index_bytes, requests[0].volume.device if requests else "cuda")
+    ctx = ctx or default_context()
+    s = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    req = (_lib.IsoRequest * max(n, 1))(*[r.descriptor() for r in requests])
+    pf, tf, nv, nt = [(C.c_int64 * max(n, 1))() for _ in range(4)]
+    status = (C.c_int * max(n, 1))()
+    for _ in range(2):
+        st = lib.iso_extract_batch_packed(ctx.handle, n, req, _ptr(buffers.points), _ptr(buffers.normals),
+                                          _ptr(buffers.tris), buffers.index_bytes, buffers.points.shape[0],
+                                          buffers.tris.shape[0], pf, tf, nv, nt, status, C.c_void_p(s))
+        if st != _lib.ISO_ERR_CAPACITY:
+            break
+        buffers.reserve(sum(nv[i] for i in range(n)), sum(nt[i] for i in range(n)))
+    check(st, ctx.handle)
+    out = []
+    for i in range(n):
+        m = DeviceMesh.__new__(DeviceMesh)
+        m.index_bytes = buffers.index_bytes
+        m.points = buffers.points[pf[i]: pf[i] + max(nv[i], 1)]
+        m.normals = buffers.normals[pf[i]: pf[i] + max(nv[i], 1)]
+        m.tris = buffers.tris[tf[i]: tf[i] + max(nt[i], 1)]
+        m.n_points, m.n_tris = nv[i], nt[i]
+        out.append(m)
+    return out, buffers
+
+
 def extract_batch(requests, meshes=None, index_bytes=4, ctx=None, stream=None, predictor=None):
     """Batched extraction (iso_extract_batch): a list of Request in, a list
     of DeviceMesh out, each what extract_device gives for its request.

@@ -87,8 +87,9 @@ bool fusable(const iso_ctx* ctx, const iso_request& r, const BatchItem& it)
 // Groups, work split and layout of the fused requests fz (their plans are made for the whole GPU).  Returns
 // an empty plan when a launch would pass 2^31 blocks or items: those requests then take the lanes.
 FusedPlan plan_fused(iso_ctx* ctx, const iso_request* req, const iso_mesh* out, std::vector<BatchItem>& items,
-                     const std::vector<int>& fz)
+                     const std::vector<int>& fz, const iso::PackedOut* pk = nullptr)
 {
+    const bool extract = out || pk;
     FusedPlan f;
     if (fz.empty()) return f;
     f.reqs = fz;
@@ -122,14 +123,15 @@ FusedPlan plan_fused(iso_ctx* ctx, const iso_request* req, const iso_mesh* out, 
         cg.members.push_back(d);
         cg.smem = std::max(cg.smem, iso::count_batch_smem(g, cv));
         f.all.members.push_back(d);
-        if (out) {
+        if (extract) {
             const int rpw = iso::gen_rows_per_warp(g.W);
-            const int gk = rpw | (out[r].index_bytes << 8);
+            const int ib = out ? out[r].index_bytes : pk->index_bytes;
+            const int gk = rpw | (ib << 8);
             if (!gkey.count(gk)) {
                 gkey[gk] = (int)f.gen.size();
                 f.gen.emplace_back();
                 f.gen.back().rpw = rpw;
-                f.gen.back().index_bytes = out[r].index_bytes;
+                f.gen.back().index_bytes = ib;
             }
             FusedGroup& gg = f.gen[gkey[gk]];
             gg.members.push_back(d);
@@ -152,7 +154,7 @@ FusedPlan plan_fused(iso_ctx* ctx, const iso_request* req, const iso_mesh* out, 
         }
         return t;
     };
-    if (out) {
+    if (extract) {
         for (iso::BatchReq& x : f.proto) {
             x.gen_KC = (int)std::min<long long>(KC, x.g.nz);
             x.gen_nkc = (x.g.nz + x.gen_KC - 1) / x.gen_KC;
@@ -201,7 +203,7 @@ FusedPlan plan_fused(iso_ctx* ctx, const iso_request* req, const iso_mesh* out, 
 }
 
 // The fused requests' descriptors (buffers in the arena at f.at, meshes of out, counters of the batch) and
-// launch lists into ctx->h_fused.
+// launch lists into ctx->h_fused.  A packed batch's mesh pointers and capacities are set on the device.
 void fill_fused(iso_ctx* ctx, const FusedPlan& f, const iso_mesh* out, const std::vector<BatchItem>& items)
 {
     char* base = static_cast<char*>(ctx->batch_arena) + f.at;
@@ -255,8 +257,10 @@ void fan_out(iso_ctx* ctx, const std::vector<FusedGroup>& groups, cudaStream_t s
     }
 }
 
-// The fused chain on s: descriptors in, counts, scans and, for an extraction, the generate and vertex passes.
-void enqueue_fused(iso_ctx* ctx, const FusedPlan& f, bool extract, cudaStream_t s)
+// The fused chain on s: descriptors in, counts, scans and, for an extraction, the generate and vertex passes
+// (pk: into one packed output, each request placed on the device after its counts).
+void enqueue_fused(iso_ctx* ctx, const FusedPlan& f, bool extract, cudaStream_t s,
+                   const iso::PackedOut* pk = nullptr)
 {
     char* base = static_cast<char*>(ctx->batch_arena) + f.at;
     const size_t desc = (f.reqs.size() * sizeof(iso::BatchReq) + 255) & ~(size_t)255;
@@ -274,7 +278,10 @@ void enqueue_fused(iso_ctx* ctx, const FusedPlan& f, bool extract, cudaStream_t 
     unsigned long long* vfirst = reinterpret_cast<unsigned long long*>(base + f.vfirst_at);
     unsigned* work = reinterpret_cast<unsigned*>(base + f.work_at);
     cudaMemsetAsync(work, 0, f.gen.size() * 4, s);
-    iso::launch_vfirst_batch(D, L(f.all), nf, vfirst, s);
+    if (pk)
+        iso::launch_place_batch(reinterpret_cast<iso::BatchReq*>(base), L(f.all), nf, *pk, vfirst, s);
+    else
+        iso::launch_vfirst_batch(D, L(f.all), nf, vfirst, s);
     fan_out(ctx, f.gen, s, [&](size_t q, cudaStream_t st) {
         const FusedGroup& g = f.gen[q];
         iso::launch_gen_batch(g.rpw, g.index_bytes, D, L(g), F(g), (int)g.members.size(), g.total, ctx->d_cases,
@@ -748,9 +755,106 @@ iso_status run_batch(iso_ctx* ctx, int64_t n, const iso_request* req, iso_mesh* 
     return rc;
 }
 
+// iso_extract_batch_packed: every request fused, one call, no host round trip between its counts and its mesh.
+iso_status run_batch_packed(iso_ctx* ctx, int64_t n, const iso_request* req, const iso::PackedOut& pk,
+                            int64_t* point_first, int64_t* tri_first, int64_t* n_points, int64_t* n_tris,
+                            iso_status* status, cudaStream_t s)
+{
+    ISO_CUDA(ctx, cudaSetDevice(ctx->device));
+    std::vector<iso_status> st((size_t)n, ISO_OK);
+    std::vector<BatchItem> items((size_t)n);
+    std::vector<int> run;
+    for (int64_t r = 0; r < n; ++r) {
+        point_first[r] = tri_first[r] = n_points[r] = n_tris[r] = 0;
+        Grid g;
+        if (!valid_algo(static_cast<iso_algorithm>(req[r].algorithm)) || !make_grid(&req[r].grid, g)) {
+            st[r] = ISO_ERR_INVALID_ARG;
+            continue;
+        }
+        if (empty_grid(g)) continue;
+        items[r].g = g;
+        items[r].pl = make_plans(ctx, g);
+        if (!req[r].volume || req[r].algorithm != ISO_FLYING_EDGES || g.W > 16 || !items[r].pl.gp.fits ||
+            (reinterpret_cast<uintptr_t>(req[r].volume) & 15) != 0) {
+            ctx->last_error = "a packed batch takes Flying Edges requests of rows up to 512 points, volumes at "
+                              "16-byte boundaries";
+            st[r] = ISO_ERR_INVALID_ARG;
+            continue;
+        }
+        run.push_back((int)r);
+    }
+    iso_status rc = ISO_OK;
+    if (!run.empty()) {
+        const FusedPlan fz = plan_fused(ctx, req, nullptr, items, run, &pk);
+        if (fz.empty()) {
+            ctx->last_error = "the packed batch is too large for one launch per pass";
+            return ISO_ERR_INVALID_ARG;
+        }
+        const BatchLayout lay = plan_batch(req, nullptr, n, items, std::vector<int>(), 1, fz);
+        {
+            std::lock_guard<std::mutex> lock(g_batch_mutex);
+            rc = ensure_batch(ctx, lay, n, s);
+            if (rc == ISO_OK) fill_fused(ctx, lay.fz, nullptr, items);
+        }
+        if (rc != ISO_OK) return rc;
+        unsigned long long* counters = static_cast<unsigned long long*>(ctx->batch_arena);
+        const bool prof = ctx->profiling;
+        ctx->profiling = false;
+        cudaMemsetAsync(counters, 0, (size_t)n * 8 * sizeof(unsigned long long), s);
+        enqueue_fused(ctx, lay.fz, true, s, &pk);
+        cudaMemcpyAsync(ctx->h_batch, counters, (size_t)n * 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                        s);
+        ctx->profiling = prof;
+        ISO_CUDA(ctx, cudaGetLastError());
+        ISO_CUDA(ctx, cudaStreamSynchronize(s));
+        for (int r : run) {
+            const unsigned long long* c = ctx->h_batch + 8 * (size_t)r;
+            n_points[r] = (int64_t)c[0];
+            n_tris[r] = (int64_t)c[1];
+            point_first[r] = (int64_t)c[4];
+            tri_first[r] = (int64_t)c[5];
+            if (c[3]) {
+                ctx->last_error = "a device-side wait timed out";
+                st[r] = ISO_ERR_TIMEOUT;
+            } else if (pk.index_bytes == 4 && c[0] > 0xffffffffull) {
+                ctx->last_error = "more than 2^32-1 vertices: use 64-bit indices";
+                st[r] = ISO_ERR_OVERFLOW;
+            } else if ((long long)(c[4] + c[0]) > pk.cap_points || (long long)(c[5] + c[1]) > pk.cap_tris) {
+                ctx->last_error = "output buffers too small";
+                st[r] = ISO_ERR_CAPACITY;
+            }
+        }
+    }
+    for (int64_t r = 0; r < n; ++r) {
+        if (status) status[r] = st[r];
+        if (rc == ISO_OK && st[r] != ISO_OK) rc = st[r];
+    }
+    return rc;
+}
+
 }  // namespace
 
 extern "C" {
+
+iso_status iso_extract_batch_packed(iso_ctx* ctx, int64_t n, const iso_request* req, float* points, float* normals,
+                                    void* tris, int32_t index_bytes, int64_t cap_points, int64_t cap_tris,
+                                    int64_t* point_first, int64_t* tri_first, int64_t* n_points, int64_t* n_tris,
+                                    iso_status* status, void* stream)
+{
+    if (!ctx || n < 0 || (n > 0 && (!req || !point_first || !tri_first || !n_points || !n_tris)) ||
+        (index_bytes != 4 && index_bytes != 8) || cap_points < 0 || cap_tris < 0 ||
+        (cap_points > 0 && (!points || !normals)) || (cap_tris > 0 && !tris))
+        return ISO_ERR_INVALID_ARG;
+    iso::PackedOut pk;
+    pk.points = points;
+    pk.normals = normals;
+    pk.tris = tris;
+    pk.index_bytes = index_bytes;
+    pk.cap_points = cap_points;
+    pk.cap_tris = cap_tris;
+    return run_batch_packed(ctx, n, req, pk, point_first, tri_first, n_points, n_tris, status,
+                            static_cast<cudaStream_t>(stream));
+}
 
 iso_status iso_extract_batch(iso_ctx* ctx, int64_t n, const iso_request* req, iso_mesh* out, iso_status* status,
                              void* stream)

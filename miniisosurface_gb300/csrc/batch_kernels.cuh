@@ -34,6 +34,15 @@ struct BatchReq {
     int gen_KC, gen_ngroups, gen_nkc;       // generate: items of (row group, run of gen_KC planes)
 };
 
+// Packed output of a batch (iso_extract_batch_packed): every request's mesh in one set of buffers.
+struct PackedOut {
+    float* points;
+    float* normals;
+    void* tris;
+    int index_bytes;
+    long long cap_points, cap_tris;
+};
+
 // Index of the request of block or item x: the last q in [0, m) with first[q] <= x (first[0] = 0, ascending).
 __device__ __forceinline__ int batch_find(const unsigned* __restrict__ first, int m, unsigned x)
 {
@@ -61,6 +70,12 @@ void launch_count_batch(const CountVariant& v, const BatchReq* reqs, const int* 
 void launch_scan_batch(const BatchReq* reqs, const int* list, const unsigned* first, int m, unsigned blocks,
                        cudaStream_t s);
 void launch_vfirst_batch(const BatchReq* reqs, const int* list, int m, unsigned long long* vfirst, cudaStream_t s);
+// Packed output: places request list[q]'s mesh after those of list[0 .. q-1] (vertices and triangles), writes its
+// descriptor's mesh pointers and capacities (-1 when its range ends past a capacity, or it has 2^32 vertices or
+// more with 32-bit indices: it is left out) and its offsets into totals[4] and totals[5], and vfirst over the
+// placed requests.
+void launch_place_batch(BatchReq* reqs, const int* list, int m, const PackedOut& out, unsigned long long* vfirst,
+                        cudaStream_t s);
 void launch_gen_batch(int rpw, int index_bytes, const BatchReq* reqs, const int* list, const unsigned* first, int m,
                       unsigned nitems, const CaseTables* cases, unsigned* work, int ws_bytes, int reverse, int nsm,
                       cudaStream_t s);

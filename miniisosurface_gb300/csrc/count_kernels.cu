@@ -711,6 +711,79 @@ __global__ void __launch_bounds__(1024) k_batch_vfirst(const BatchReq* __restric
     if (t == 1023) vfirst[m] = run;
 }
 
+// Block-wide exclusive sums of two values per thread (one CTA of 1024 threads): returns this thread's offsets.
+__device__ __forceinline__ void block_excl2(unsigned long long a, unsigned long long b, unsigned long long& ea,
+                                            unsigned long long& eb, unsigned long long* s_a, unsigned long long* s_b)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned long long ia = a, ib = b;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const unsigned long long ya = __shfl_up_sync(0xffffffffu, ia, d), yb = __shfl_up_sync(0xffffffffu, ib, d);
+        if (lane >= d) {
+            ia += ya;
+            ib += yb;
+        }
+    }
+    if (lane == 31) {
+        s_a[warp] = ia;
+        s_b[warp] = ib;
+    }
+    __syncthreads();
+    ea = ia - a;
+    eb = ib - b;
+    for (int w = 0; w < warp; ++w) {
+        ea += s_a[w];
+        eb += s_b[w];
+    }
+    __syncthreads();  // s_a / s_b free for the next call
+}
+
+// The packed placement (launch_place_batch): one CTA of 1024 threads, each over a run of consecutive requests.
+// Request list[q] goes to vertex offset vat and triangle offset tat, the sums of the counts before it; it is
+// placed when both ranges end within the capacities and, for 32-bit indices, its vertices number below 2^32.
+// vfirst sums the vertices of the placed requests only.
+__global__ void __launch_bounds__(1024) k_batch_place(BatchReq* __restrict__ reqs, const int* __restrict__ list, int m,
+                                                      PackedOut o, unsigned long long* __restrict__ vfirst)
+{
+    __shared__ unsigned long long s_a[32], s_b[32];
+    const int t = threadIdx.x;
+    const int per = (m + 1023) / 1024, q0 = t * per, q1 = min(m, q0 + per);
+    unsigned long long sv = 0, st = 0;
+    for (int q = q0; q < q1; ++q) {
+        const unsigned long long* tot = reqs[__ldg(&list[q])].totals;
+        sv += tot[0];
+        st += tot[1];
+    }
+    unsigned long long vat, tat;
+    block_excl2(sv, st, vat, tat, s_a, s_b);
+    unsigned long long placed = 0;  // vertices of this thread's placed requests
+    for (int q = q0; q < q1; ++q) {
+        BatchReq* d = reqs + __ldg(&list[q]);
+        const unsigned long long V = d->totals[0], T = d->totals[1];
+        const bool ok = vat + V <= (unsigned long long)o.cap_points && tat + T <= (unsigned long long)o.cap_tris &&
+                        (o.index_bytes == 8 || V <= 0xffffffffull);
+        d->points = o.points + 3 * vat;
+        d->normals = o.normals + 3 * vat;
+        d->tris = static_cast<char*>(o.tris) + 3 * tat * (unsigned long long)o.index_bytes;
+        d->capV = ok ? (long long)V : -1;
+        d->capT = ok ? (long long)T : -1;
+        d->totals[4] = vat;
+        d->totals[5] = tat;
+        placed += ok ? V : 0ull;
+        vat += V;
+        tat += T;
+    }
+    unsigned long long at, unused;
+    block_excl2(placed, 0ull, at, unused, s_a, s_b);
+    for (int q = q0; q < q1; ++q) {
+        const BatchReq* d = reqs + __ldg(&list[q]);
+        vfirst[q] = at;
+        at += d->capV >= 0 ? d->totals[0] : 0ull;
+    }
+    if (t == 1023) vfirst[m] = at;
+}
+
 // gridEdge records {xl, xr, xstart, ystart, zstart} and triCounter for
 // inspection (counts before the scan, offsets after it).
 __global__ void k_grid_edges(Grid g, RowStarts rs, const uint4* __restrict__ rowcnt, const uint2* __restrict__ trims,
@@ -885,6 +958,12 @@ void launch_scan_batch(const BatchReq* reqs, const int* list, const unsigned* fi
 void launch_vfirst_batch(const BatchReq* reqs, const int* list, int m, unsigned long long* vfirst, cudaStream_t s)
 {
     k_batch_vfirst<<<1, 1024, 0, s>>>(reqs, list, m, vfirst);
+}
+
+void launch_place_batch(BatchReq* reqs, const int* list, int m, const PackedOut& out, unsigned long long* vfirst,
+                        cudaStream_t s)
+{
+    k_batch_place<<<1, 1024, 0, s>>>(reqs, list, m, out, vfirst);
 }
 
 void launch_scan(const Grid& g, const CountPlan& p, int mode, FeBuffers& b, cudaStream_t s)

@@ -33,7 +33,7 @@ import time
 import numpy as np
 
 from . import _lib
-from .api import Batch, Context, DeviceMesh, Request, make_grid
+from .api import FLYING_EDGES, _algo, Batch, Context, DeviceMesh, PackedBuffers, Request, extract_batch_packed, make_grid
 from ._lib import check, load
 
 
@@ -134,6 +134,12 @@ class Server:
         self.index_bytes = index_bytes
         self.contexts = [Context(device) for _ in range(slots)]
         self._singles = {}  # id(context) -> its single-request mesh
+        # without a network, a slot's Flying Edges requests of rows up to 512 points run as one packed batch
+        # (iso_extract_batch_packed: counts and meshes in one call, into the slot's buffers), the rest as a count
+        # batch and an extraction batch
+        self.packed = predictor is None
+        self._packed = {}  # id(context) -> its PackedBuffers
+        self._streams = None
         # light load: while no slot is working and fewer than overlap_backlog requests wait, the thread that
         # receives them runs the oldest at once (no hand-off to a slot), with the plain calls on slot 0's
         # context (no slot runs meanwhile)
@@ -173,6 +179,63 @@ class Server:
                                torch.device("cuda", self.device))
             self._singles[id(ctx)] = m
         return m
+
+    @staticmethod
+    def _packable(req):
+        return _algo(req.algorithm) == FLYING_EDGES and req.dims[0] <= 512 and req.volume.data_ptr() % 16 == 0
+
+    def _serve_packed(self, take, reqs, results, ctx, stream, state, cond, slot, t0, keep_meshes):
+        """A slot's packed batch: one iso_extract_batch_packed into the slot's buffers (grown, and the batch
+        run again, when it does not fit); the buffers count against the budget while it runs."""
+        import torch
+
+        bufs = self._packed.get(id(ctx))
+        if bufs is None:
+            with torch.cuda.stream(stream):
+                bufs = PackedBuffers(0, 0, self.index_bytes, torch.device("cuda", self.device))
+            self._packed[id(ctx)] = bufs
+        with cond:
+            while True:
+                nbytes = mesh_bytes(bufs.points.shape[0], bufs.tris.shape[0], self.index_bytes)
+                k, _ = admit([(bufs.points.shape[0], bufs.tris.shape[0])], state["in_use"], self.budget,
+                             self.index_bytes)
+                if k > 0 or state["error"]:
+                    break
+                state["admitting"] += 1
+                cond.wait()
+                state["admitting"] -= 1
+            if k == 0:
+                return
+            state["in_use"] += nbytes
+            batch_no = state["batches"]
+            state["batches"] += 1
+        try:
+            with torch.cuda.stream(stream):
+                meshes, _ = extract_batch_packed(reqs, buffers=bufs, index_bytes=self.index_bytes, ctx=ctx,
+                                                 stream=stream.cuda_stream)
+                if keep_meshes:  # meshes of their own: the buffers serve the slot's next batch
+                    kept = []
+                    for m in meshes:
+                        c = DeviceMesh(m.n_points, m.n_tris, self.index_bytes, torch.device("cuda", self.device))
+                        c.points[: m.n_points].copy_(m.points[: m.n_points])
+                        c.normals[: m.n_points].copy_(m.normals[: m.n_points])
+                        c.tris[: m.n_tris].copy_(m.tris[: m.n_tris])
+                        c.n_points, c.n_tris = m.n_points, m.n_tris
+                        kept.append(c)
+                    stream.synchronize()
+                    meshes = kept
+            done = time.perf_counter() - t0
+            for i, m in zip(take, meshes):
+                r = results[i]
+                r.done = done
+                r.n_points, r.n_tris = m.n_points, m.n_tris
+                r.mesh = m if keep_meshes else None
+                r.slot, r.batch = slot, batch_no
+        finally:
+            with cond:
+                state["in_use"] -= nbytes
+                if state["admitting"]:
+                    cond.notify_all()
 
     def _serve_one(self, i, req, results, ctx, stream, state, cond, slot, t0, keep_meshes):
         """A request run alone (light load): one iso_extract_device into the context's single-request mesh,
@@ -261,9 +324,12 @@ class Server:
             if queue or state["admitting"]:
                 cond.notify_all()
 
+        if self._streams is None:  # one stream per slot for the server's life (the allocator caches per stream)
+            self._streams = [torch.cuda.Stream(self.device) for _ in range(self.slots)]
+
         def worker(slot):
             ctx = self.contexts[slot]
-            stream = torch.cuda.Stream(self.device)
+            stream = self._streams[slot]
             try:
                 while True:
                     with cond:
@@ -289,6 +355,20 @@ class Server:
                             state["busy"] -= 1
                             wake()
                         continue
+                    if self.packed:
+                        pk = [q for q in range(n) if self._packable(reqs[q])]
+                        if pk:
+                            self._serve_packed([take[q] for q in pk], [reqs[q] for q in pk], results, ctx, stream,
+                                               state, cond, slot, t0, keep_meshes)
+                            rest = [q for q in range(n) if q not in set(pk)]
+                            take = [take[q] for q in rest]
+                            reqs = [reqs[q] for q in rest]
+                            n = len(reqs)
+                        if n == 0:
+                            with cond:
+                                state["busy"] -= 1
+                                wake()
+                            continue
                     if self.predictor is not None:
                         guess = [i for i in take if i not in exact]
                         caps = self.predictor.capacities(

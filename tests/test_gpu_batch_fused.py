@@ -173,3 +173,88 @@ def test_fused_many_requests(M):
         r = reqs[i][0]
         same(fused[i], as_np(M.extract_device(r.volume, r.dims, r.isoval)), "request %d vs plain" % i)
     torch.cuda.synchronize()
+
+
+def test_packed_batch(M):
+    """iso_extract_batch_packed: the fused requests' meshes one after another in one set of buffers, each
+    equal to its own extraction; a capacity that holds the first three meshes; requests the packed batch
+    does not take; the Python helper growing its buffers."""
+    from miniisosurface_gb300 import _lib
+    lib = _lib.load()
+    reqs = requests(M)
+    take = [q for q, (r, _, _) in enumerate(reqs) if r.algorithm == M.FLYING_EDGES and r.dims[0] <= 512 and
+            r.volume.data_ptr() % 16 == 0]
+    rs = [reqs[q][0] for q in take]
+    want = [as_np(M.extract_device(r.volume, r.dims, r.isoval, r.algorithm, r.spacing, r.origin, index_bytes=ib))
+            for r, ib in ((reqs[q][0], reqs[q][1]) for q in take)]
+    for ib in (4, 8):
+        meshes, bufs = M.extract_batch_packed(rs, index_bytes=ib)
+        at_v = at_t = 0
+        for q, (m, w) in enumerate(zip(meshes, want)):
+            same(as_np(m), w, "packed request %d, %d-byte indices" % (q, ib))
+            assert m.points.data_ptr() == bufs.points.data_ptr() + 12 * at_v  # one after another
+            assert m.tris.data_ptr() == bufs.tris.data_ptr() + 3 * ib * at_t
+            at_v += m.n_points
+            at_t += m.n_tris
+        meshes2, bufs2 = M.extract_batch_packed(rs, buffers=bufs, index_bytes=ib)  # reused, no growth
+        assert bufs2 is bufs and bufs2.points.data_ptr() == bufs.points.data_ptr()
+        for q, (m, w) in enumerate(zip(meshes2, want)):
+            same(as_np(m), w, "packed again request %d" % q)
+    # room for the first three meshes only
+    n = len(rs)
+    nv = [len(w[0]) for w in want]
+    nt = [len(w[2]) for w in want]
+    cap_p, cap_t = sum(nv[:3]), sum(nt[:3])
+    bufs = M.PackedBuffers(cap_p, cap_t, 4)
+    arr = (_lib.IsoRequest * n)(*[r.descriptor() for r in rs])
+    pf, tf, gv, gt = [(C.c_int64 * n)() for _ in range(4)]
+    st = (C.c_int * n)()
+    rc = lib.iso_extract_batch_packed(M.default_context().handle, n, arr, bufs.points.data_ptr(),
+                                      bufs.normals.data_ptr(), bufs.tris.data_ptr(), 4, cap_p, cap_t, pf, tf, gv, gt,
+                                      st, None)
+    assert rc == _lib.ISO_ERR_CAPACITY
+    for q in range(n):
+        assert (gv[q], gt[q]) == (nv[q], nt[q]) and pf[q] == sum(nv[:q]) and tf[q] == sum(nt[:q])
+        placed = pf[q] + nv[q] <= cap_p and tf[q] + nt[q] <= cap_t
+        assert st[q] == (_lib.ISO_OK if placed else _lib.ISO_ERR_CAPACITY), q
+        if placed:
+            got = (bufs.points[pf[q]: pf[q] + nv[q]].cpu().numpy().view(np.uint32),
+                   bufs.normals[pf[q]: pf[q] + nv[q]].cpu().numpy().view(np.uint32),
+                   bufs.tris[tf[q]: tf[q] + nt[q]].cpu().numpy().astype(np.uint64))
+            same(got, want[q], "capacity-limited request %d" % q)
+    # the whole list: the requests outside the packed path are refused, the rest complete
+    alln = len(reqs)
+    arr = (_lib.IsoRequest * alln)(*[r.descriptor() for r, _, _ in reqs])
+    pf, tf, gv, gt = [(C.c_int64 * alln)() for _ in range(4)]
+    st = (C.c_int * alln)()
+    bufs = M.PackedBuffers(sum(nv), sum(nt), 4)
+    rc = lib.iso_extract_batch_packed(M.default_context().handle, alln, arr, bufs.points.data_ptr(),
+                                      bufs.normals.data_ptr(), bufs.tris.data_ptr(), 4, bufs.points.shape[0],
+                                      bufs.tris.shape[0], pf, tf, gv, gt, st, None)
+    assert rc == _lib.ISO_ERR_INVALID_ARG
+    k = 0
+    for q in range(alln):
+        if q in take:
+            assert st[q] == _lib.ISO_OK
+            got = (bufs.points[pf[q]: pf[q] + gv[q]].cpu().numpy().view(np.uint32),
+                   bufs.normals[pf[q]: pf[q] + gv[q]].cpu().numpy().view(np.uint32),
+                   bufs.tris[tf[q]: tf[q] + gt[q]].cpu().numpy().astype(np.uint64))
+            same(got, want[k], "mixed list request %d" % q)
+            k += 1
+        elif reqs[q][0].dims == (2, 2, 2) or reqs[q][0].dims[0] < 2:
+            pass
+        else:
+            assert st[q] == _lib.ISO_ERR_INVALID_ARG, q
+
+
+def test_packed_many_requests(M):
+    rng = np.random.default_rng(5)
+    vols = []
+    for v in range(20):
+        dims = tuple(int(x) for x in rng.integers(6, 60, size=3))
+        vols.append((dims, dev(M.generate_value_noise(dims, 2, 8, seed=300 + v))))
+    rs = [M.Request(vols[q % 20][1], vols[q % 20][0], float(np.float32(rng.uniform(-0.3, 0.3)))) for q in range(1500)]
+    meshes, _ = M.extract_batch_packed(rs)
+    for q in range(0, 1500, 61):
+        r = rs[q]
+        same(as_np(meshes[q]), as_np(M.extract_device(r.volume, r.dims, r.isoval)), "request %d" % q)
