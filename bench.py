@@ -454,6 +454,14 @@ def batched_leg(M, lib, dev, reps):
     M.set_batch_split(0, ctx)
     batched()
     t_batch = seconds(batched)
+    # packed: counts, placement and meshes in one call into reused buffers (no meshes sized beforehand)
+    packed_state = {"bufs": None, "meshes": None}
+
+    def packed():
+        packed_state["meshes"], packed_state["bufs"] = M.extract_batch_packed(
+            requests, buffers=packed_state["bufs"], ctx=ctx, stream=stream.cuda_stream)
+
+    t_packed = seconds(packed)
     t_plain = seconds(plain)
     t_async = seconds(plain_async)
     same = True
@@ -464,6 +472,11 @@ def batched_leg(M, lib, dev, reps):
         same &= all(bool(torch.equal(x, y)) for x, y in zip(l, (b.points[: b.n_points], b.normals[: b.n_points],
                                                                  b.tris[: b.n_tris])))
     same &= all((b.n_points, b.n_tris) == s for b, s in zip(batch_m, sizes))
+    for a, p, sz in zip(plain_m, packed_state["meshes"], sizes):  # the plain meshes hold the counted sizes
+        same &= (p.n_points, p.n_tris) == sz
+        same &= bool(torch.equal(a.points[: sz[0]], p.points[: p.n_points]))
+        same &= bool(torch.equal(a.normals[: sz[0]], p.normals[: p.n_points]))
+        same &= bool(torch.equal(a.tris[: sz[1]], p.tris[: p.n_tris]))
     mc = lambda s: cells / s / 1e6
     return {
         "workload": "64 volumes, dims uniform in [32, 320] per axis, half blobs / half value noise, "
@@ -476,6 +489,9 @@ def batched_leg(M, lib, dev, reps):
                     "what": "one launch per pass and kernel variant, the variants side by side (iso_batch_set_fused)"},
         "batched_lanes": {"ms": 1e3 * t_lanes, "value": mc(t_lanes), "unit": METRIC, "lanes": lanes, "split": split,
                           "what": "every request's passes on one of L streams, one CUDA graph"},
+        "batched_packed": {"ms": 1e3 * t_packed, "value": mc(t_packed), "unit": METRIC,
+                           "what": "iso_extract_batch_packed: counts, placement and meshes in one call (the other "
+                                   "rows' meshes were sized beforehand by count calls outside the timing)"},
         "speedup_vs_plain": t_plain / t_batch, "speedup_vs_plain_async": t_async / t_batch,
         "speedup_vs_lanes": t_lanes / t_batch,
         "identical_output": same,
