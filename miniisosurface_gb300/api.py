@@ -356,14 +356,18 @@ class Request:
         self.algorithm = algorithm
         self.spacing = spacing
         self.origin = origin
+        self._desc = None
 
     def descriptor(self):
-        r = _lib.IsoRequest()
-        r.volume = _ptr(self.volume)
-        r.grid = make_grid(self.dims, self.spacing, self.origin)
-        r.isoval = self.isoval
-        r.algorithm = _algo(self.algorithm)
-        return r
+        """The iso_request of this request (built once; copies of it go into the C arrays)."""
+        if self._desc is None:
+            r = _lib.IsoRequest()
+            r.volume = _ptr(self.volume)
+            r.grid = make_grid(self.dims, self.spacing, self.origin)
+            r.isoval = self.isoval
+            r.algorithm = _algo(self.algorithm)
+            self._desc = r
+        return self._desc
 
 
 class Batch:
