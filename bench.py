@@ -645,22 +645,24 @@ def served_leg(M, dev, nreq, seed=4, npool=8):
         _, sat_p = served_p(np.zeros(nreq))
         out["saturated"]["served_predicted"] = sat_p
         out["saturated"]["speedup_predicted"] = sat_p["requests_per_s"] / sat["requests_per_s"]
-    identical = None
+    # identical meshes: one untimed run of each loop at half the plain capacity, keeping every mesh (the
+    # server copies kept meshes out of its reused buffers, which the timed runs below do not do)
+    times = serve.poisson_arrivals(nreq, 0.5 * sat["requests_per_s"], seed=seed + 5)
+    p = serve.run_plain(volumes, reqs_at(times), device=dev.index or 0, keep_meshes=True)
+    s = server.run(reqs_at(times), keep_meshes=True)
+    sp = server_p.run(reqs_at(times), keep_meshes=True) if server_p else []
+    same = lambda a, b: ((a.n_points, a.n_tris) == (b.n_points, b.n_tris) and
+                         torch.equal(a.mesh.points[: a.n_points], b.mesh.points[: b.n_points]) and
+                         torch.equal(a.mesh.normals[: a.n_points], b.mesh.normals[: b.n_points]) and
+                         torch.equal(a.mesh.tris[: a.n_tris], b.mesh.tris[: b.n_tris]))
+    identical = all(same(a, b) for a, b in zip(p, s)) and all(same(a, b) for a, b in zip(p, sp))
+    del p, s, sp
     for f in (0.5, 1.0, 2.0):
         rate = f * sat["requests_per_s"]
         times = serve.poisson_arrivals(nreq, rate, seed=seed + int(10 * f))
-        keep = identical is None
-        p = serve.run_plain(volumes, reqs_at(times), device=dev.index or 0, keep_meshes=keep)
-        s = server.run(reqs_at(times), keep_meshes=keep)
-        sp, sp_sum = served_p(times, keep) if server_p else ([], None)
-        if keep:
-            same = lambda a, b: ((a.n_points, a.n_tris) == (b.n_points, b.n_tris) and
-                                 torch.equal(a.mesh.points[: a.n_points], b.mesh.points[: b.n_points]) and
-                                 torch.equal(a.mesh.normals[: a.n_points], b.mesh.normals[: b.n_points]) and
-                                 torch.equal(a.mesh.tris[: a.n_tris], b.mesh.tris[: b.n_tris]))
-            identical = all(same(a, b) for a, b in zip(p, s)) and all(same(a, b) for a, b in zip(p, sp))
-            for r in p + s + sp:
-                r.mesh = None
+        p = serve.run_plain(volumes, reqs_at(times), device=dev.index or 0)
+        s = server.run(reqs_at(times))
+        sp, sp_sum = served_p(times) if server_p else ([], None)
         entry = {"rate_per_s": rate, "x_plain_capacity": f, "plain": serve.summary(p, cells),
                  "served": serve.summary(s, cells)}
         if sp_sum:
