@@ -680,7 +680,16 @@ iso_status run_batch(iso_ctx* ctx, int64_t n, const iso_request* req, iso_mesh* 
         fused.clear();
         lane_run = run;
     }
-    const FusedPlan fz = plan_fused(ctx, req, out, items, fused);
+    FusedPlan fz = plan_fused(ctx, req, out, items, fused);
+    if (ctx->batch_fused == 1 && !fz.empty() && fz.bytes > ctx->batch_arena_bytes) {
+        // every fused request holds its own scratch at once: past half the free memory, the lanes instead
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+            cudaGetLastError();  // the call's own error; the batch reports its own failures later
+        } else if (fz.bytes > free_b / 2) {
+            fz = FusedPlan{};
+        }
+    }
     if (fz.empty() && !fused.empty()) lane_run = run;
     iso_status rc = ISO_OK;
     if (!run.empty() && !ctx->batch_graph) {  // launched directly, no graph
