@@ -134,10 +134,10 @@ class Server:
         self.index_bytes = index_bytes
         self.contexts = [Context(device) for _ in range(slots)]
         self._singles = {}  # id(context) -> its single-request mesh
-        # without a network, a slot's Flying Edges requests of rows up to 512 points run as one packed batch
-        # (iso_extract_batch_packed: counts and meshes in one call, into the slot's buffers), the rest as a count
-        # batch and an extraction batch
-        self.packed = predictor is None
+        # a slot's Flying Edges requests of rows up to 512 points run as one packed batch (iso_extract_batch_packed:
+        # counts and meshes in one call, into the slot's buffers); the rest are sized by a count batch, or by the
+        # network when there is one, and run as an extraction batch
+        self.packed = True
         self._packed = {}  # id(context) -> its PackedBuffers
         self._streams = None
         # light load: while no slot is working and fewer than overlap_backlog requests wait, the thread that

@@ -128,6 +128,7 @@ def test_served_with_predictor_equals_alone(M, trained):
     for p in (pred, small):
         server = serve.Server(volumes, slots=2, max_batch=6, lanes=2, predictor=p)
         server.inline_idle = server.single_direct = False  # every request through the network-sized batches
+        server.packed = False
         server.overlap_backlog = 1
         res = server.run(reqs, keep_meshes=True)
         if p is small:
