@@ -624,12 +624,13 @@ def served_leg(M, dev, nreq, seed=4, npool=8):
     server = serve.Server(volumes, slots=3, max_batch=64, budget_bytes=120 << 30, lanes=8, device=dev.index or 0)
     server_p = serve.Server(volumes, slots=3, max_batch=64, budget_bytes=120 << 30, lanes=8, device=dev.index or 0,
                             predictor=P.Predictor.load(device=dev)) if P.WEIGHTS.exists() else None
-    # warm-up: the plain loop, and one saturated pass of each server (its slots' batch buffers reach the
-    # sizes the timed runs need)
+    # warm-up: the plain loop, and two saturated passes of each server (its slots' buffers reach the sizes
+    # the timed runs need)
     serve.run_plain(volumes, reqs_at(np.zeros(nreq))[:8], device=dev.index or 0)
-    server.run(reqs_at(np.zeros(nreq)))
-    if server_p:
-        server_p.run(reqs_at(np.zeros(nreq)))
+    for _ in range(2):
+        server.run(reqs_at(np.zeros(nreq)))
+        if server_p:
+            server_p.run(reqs_at(np.zeros(nreq)))
 
     def served_p(times, keep=False):
         res = server_p.run(reqs_at(times), keep_meshes=keep)

@@ -364,6 +364,13 @@ class Server:
                             take = [take[q] for q in rest]
                             reqs = [reqs[q] for q in rest]
                             n = len(reqs)
+                        if n and self.predictor is None and self.single_direct:
+                            # the rest (rows longer than 512 points: large grids that fill the GPU alone) one
+                            # after another, one extraction call each (one count pass, not a count batch and an
+                            # extraction batch that count twice)
+                            for i, req in zip(take, reqs):
+                                self._serve_one(i, req, results, ctx, stream, state, cond, slot, t0, keep_meshes)
+                            n = 0
                         if n == 0:
                             with cond:
                                 state["busy"] -= 1
