@@ -74,6 +74,9 @@ struct FusedPlan {
     bool empty() const { return reqs.empty(); }
 };
 
+// Bytes of n descriptors at the start of the upload block (the lists and firsts follow, 256-byte aligned).
+inline size_t desc_bytes(size_t n) { return (n * sizeof(iso::BatchReq) + 255) & ~(size_t)255; }
+
 // Fewest fusable requests that run fused by default (iso_batch_set_fused 1): serving batches of 2-8 requests
 // ran 4-8% faster on the lanes, the 157-request batch 11% faster fused.
 constexpr int kFuseMin = 16;
@@ -186,8 +189,7 @@ FusedPlan plan_fused(iso_ctx* ctx, const iso_request* req, const iso_mesh* out, 
     for (FusedGroup& grp : f.count) ok = ok && place(grp, 0);
     for (FusedGroup& grp : f.gen) ok = ok && place(grp, 2);
     if (!ok) return FusedPlan{};
-    const size_t desc = ((size_t)nf * sizeof(iso::BatchReq) + 255) & ~(size_t)255;
-    f.upload = desc + f.meta.size();
+    f.upload = desc_bytes(nf) + f.meta.size();
     size_t at = align256(f.upload);
     f.vfirst_at = at;
     at += align256((size_t)(nf + 1) * 8);
@@ -229,14 +231,11 @@ void fill_fused(iso_ctx* ctx, const FusedPlan& f, const iso_mesh* out, const std
         }
         D[d] = x;
     }
-    const size_t desc = (f.reqs.size() * sizeof(iso::BatchReq) + 255) & ~(size_t)255;
-    std::memcpy(ctx->h_fused + desc, f.meta.data(), f.meta.size());
+    std::memcpy(ctx->h_fused + desc_bytes(f.reqs.size()), f.meta.data(), f.meta.size());
 }
 
 // The launches of one pass run side by side: the largest on s, the others on streams forked from it and
-// joined back into it.
-constexpr bool kFusedSideBySide = true;
-
+// joined back into it (2.94 -> 2.77 ms on the 157-request batch against one after another).
 template <typename Launch>
 void fan_out(iso_ctx* ctx, const std::vector<FusedGroup>& groups, cudaStream_t s, Launch launch)
 {
@@ -244,7 +243,7 @@ void fan_out(iso_ctx* ctx, const std::vector<FusedGroup>& groups, cudaStream_t s
     for (size_t i = 0; i < order.size(); ++i) order[i] = i;
     std::stable_sort(order.begin(), order.end(),
                      [&](size_t a, size_t b) { return groups[a].total > groups[b].total; });
-    const size_t side = kFusedSideBySide ? std::min(order.size(), ctx->fused_streams.size() + 1) : 1;
+    const size_t side = std::min(order.size(), ctx->fused_streams.size() + 1);
     if (side > 1) {
         cudaEventRecord(ctx->fused_fork, s);
         for (size_t i = 1; i < side; ++i) cudaStreamWaitEvent(ctx->fused_streams[i - 1], ctx->fused_fork, 0);
@@ -263,7 +262,7 @@ void enqueue_fused(iso_ctx* ctx, const FusedPlan& f, bool extract, cudaStream_t 
                    const iso::PackedOut* pk = nullptr)
 {
     char* base = static_cast<char*>(ctx->batch_arena) + f.at;
-    const size_t desc = (f.reqs.size() * sizeof(iso::BatchReq) + 255) & ~(size_t)255;
+    const size_t desc = desc_bytes(f.reqs.size());
     const iso::BatchReq* D = reinterpret_cast<const iso::BatchReq*>(base);
     auto L = [&](const FusedGroup& g) { return reinterpret_cast<const int*>(base + desc + g.list_at); };
     auto F = [&](const FusedGroup& g) { return reinterpret_cast<const unsigned*>(base + desc + g.first_at); };
