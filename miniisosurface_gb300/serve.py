@@ -213,6 +213,11 @@ class Server:
             with torch.cuda.stream(stream):
                 meshes, _ = extract_batch_packed(reqs, buffers=bufs, index_bytes=self.index_bytes, ctx=ctx,
                                                  stream=stream.cuda_stream)
+                grown = mesh_bytes(bufs.points.shape[0], bufs.tris.shape[0], self.index_bytes)
+                if grown != nbytes:  # the buffers grew for this batch: count what they hold now
+                    with cond:
+                        state["in_use"] += grown - nbytes
+                    nbytes = grown
                 if keep_meshes:  # meshes of their own: the buffers serve the slot's next batch
                     kept = []
                     for m in meshes:
@@ -270,6 +275,10 @@ class Server:
                                         C.byref(d), sh)
             if st == _lib.ISO_ERR_CAPACITY:  # a mesh larger than any before: grow, run again
                 m = self._single_mesh(ctx, stream, d.n_points, d.n_tris)
+                grown = mesh_bytes(m.points.shape[0], m.tris.shape[0], self.index_bytes)
+                with cond:
+                    state["in_use"] += grown - nbytes
+                nbytes = grown
                 d = m.descriptor()
                 st = lib.iso_extract_device(ctx.handle, a, req.volume.data_ptr(), C.byref(g),
                                             C.c_float(req.isoval), C.byref(d), sh)
