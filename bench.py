@@ -452,7 +452,8 @@ def batched_leg(M, lib, dev, reps):
     M.set_batch_fused(True, ctx)
     M.set_batch_lanes(0, ctx)
     M.set_batch_split(0, ctx)
-    batched()
+    batched()  # the fused work split's autotuner runs here
+    fused_split = M.batch_fused_split(ctx)
     t_batch = seconds(batched)
     # packed: counts, placement and meshes in one call into reused buffers (no meshes sized beforehand)
     packed_state = {"bufs": None, "meshes": None}
@@ -486,7 +487,8 @@ def batched_leg(M, lib, dev, reps):
         "plain": {"ms": 1e3 * t_plain, "value": mc(t_plain), "unit": METRIC},
         "plain_async": {"ms": 1e3 * t_async, "value": mc(t_async), "unit": METRIC},
         "batched": {"ms": 1e3 * t_batch, "value": mc(t_batch), "unit": METRIC,
-                    "what": "one launch per pass and kernel variant, the variants side by side (iso_batch_set_fused)"},
+                    "what": "one launch per pass and kernel variant, the variants side by side (iso_batch_set_fused)",
+                    "count_planes": fused_split[0], "items_per_warp": fused_split[1]},
         "batched_lanes": {"ms": 1e3 * t_lanes, "value": mc(t_lanes), "unit": METRIC, "lanes": lanes, "split": split,
                           "what": "every request's passes on one of L streams, one CUDA graph"},
         "batched_packed": {"ms": 1e3 * t_packed, "value": mc(t_packed), "unit": METRIC,

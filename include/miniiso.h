@@ -314,6 +314,13 @@ int iso_batch_lanes(const iso_ctx* ctx);
  * holds at least 16 such requests (fewer run faster on the lanes); 2: always
  * fused.  Other modes: ISO_ERR_INVALID_ARG. */
 iso_status iso_batch_set_fused(iso_ctx* ctx, int mode);
+/* The fused launches' work split: count blocks of at least *count_planes
+ * planes, generate work items sized for about *items_per_warp per warp of
+ * one wave.  The context's first graph-mode batch with fused requests times
+ * 8, 16, 32 planes x 16, 32, 64 items per warp and keeps the fastest (both 0
+ * before that; the defaults 16 and 32 are used meanwhile).
+ * iso_batch_set_lanes(ctx, 0) also makes it tune again. */
+iso_status iso_batch_fused_split(const iso_ctx* ctx, int* count_planes, int* items_per_warp);
 
 /* z-slabs: the grid split along z into slabs of planes [k0, k1), for
  * sharding over GPUs or streaming a volume that does not fit (no counterpart

@@ -89,6 +89,7 @@ SIGNATURES = {
     "iso_batch_set_lanes": (C.c_int, [C.c_void_p, C.c_int]),
     "iso_batch_set_graph": (C.c_int, [C.c_void_p, C.c_int]),
     "iso_batch_set_fused": (C.c_int, [C.c_void_p, C.c_int]),
+    "iso_batch_fused_split": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "iso_ctx_set_graph": (C.c_int, [C.c_void_p, C.c_int]),
     "iso_ctx_set_narrow": (C.c_int, [C.c_void_p, C.c_int]),
     "iso_batch_set_split": (C.c_int, [C.c_void_p, C.c_int]),

@@ -523,6 +523,14 @@ def set_batch_fused(mode, ctx=None):
     check(load().iso_batch_set_fused(ctx.handle, int(mode)), ctx.handle)
 
 
+def batch_fused_split(ctx=None):
+    """(count planes, items per warp) of the fused launches as the autotuner chose them ((0, 0) before)."""
+    ctx = ctx or default_context()
+    kc, ipw = C.c_int(), C.c_int()
+    check(load().iso_batch_fused_split(ctx.handle, C.byref(kc), C.byref(ipw)), ctx.handle)
+    return kc.value, ipw.value
+
+
 def batch_lanes(ctx=None):
     ctx = ctx or default_context()
     return int(load().iso_batch_lanes(ctx.handle))

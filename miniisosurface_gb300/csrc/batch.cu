@@ -89,9 +89,17 @@ bool fusable(const iso_ctx* ctx, const iso_request& r, const BatchItem& it)
 
 // Groups, work split and layout of the fused requests fz (their plans are made for the whole GPU).  Returns
 // an empty plan when a launch would pass 2^31 blocks or items: those requests then take the lanes.
+// Work split of the fused launches: count blocks of at least kc planes, generate items for about ipw per warp
+// of one wave (the autotuner's candidates; 0: the defaults).
+constexpr int kFusedKC[] = {8, 16, 32};
+constexpr int kFusedIPW[] = {16, 32, 64};
+constexpr int kFusedKCDefault = 16, kFusedIPWDefault = 32;
+
 FusedPlan plan_fused(iso_ctx* ctx, const iso_request* req, const iso_mesh* out, std::vector<BatchItem>& items,
-                     const std::vector<int>& fz, const iso::PackedOut* pk = nullptr)
+                     const std::vector<int>& fz, const iso::PackedOut* pk = nullptr, int kc_min = 0, int ipw = 0)
 {
+    if (kc_min <= 0) kc_min = ctx->fused_kc > 0 ? ctx->fused_kc : kFusedKCDefault;
+    if (ipw <= 0) ipw = ctx->fused_ipw > 0 ? ctx->fused_ipw : kFusedIPWDefault;
     const bool extract = out || pk;
     FusedPlan f;
     if (fz.empty()) return f;
@@ -113,7 +121,7 @@ FusedPlan plan_fused(iso_ctx* ctx, const iso_request* req, const iso_mesh* out, 
         x.gs = iso::make_grad_scale(g);
         x.iso = req[r].isoval;
         const iso::CountVariant cv = iso::count_variant(g);
-        x.count_KC = std::max(it.pl.cp.KC, 16);  // at least 16 planes per block (small grids: 2.77 -> 2.72 ms)
+        x.count_KC = std::max(it.pl.cp.KC, kc_min);  // at least 16 planes per block: 157 small grids 2.77 -> 2.72 ms
         x.count_nyb = (g.ny + 8 * cv.rpw - 1) / (8 * cv.rpw);  // kCountRows warps of cv.rpw rows
         x.nseg = it.pl.cp.nseg;
         const int ck = cv.rpw | (cv.aligned ? 16 : 0) | (cv.full ? 32 : 0);
@@ -143,8 +151,8 @@ FusedPlan plan_fused(iso_ctx* ctx, const iso_request* req, const iso_mesh* out, 
             gen_planes += (long long)x.gen_ngroups * g.nz;
         }
     }
-    // generate items of KC planes: about 32 per warp of one wave over all requests, at least 2 planes
-    long long KC = (gen_planes + 32 * warps - 1) / (32 * warps);
+    // generate items of KC planes: about ipw per warp of one wave over all requests, at least 2 planes
+    long long KC = (gen_planes + ipw * warps - 1) / (ipw * warps);
     if (KC < 2) KC = 2;
     const long long lim = 1ll << 31;
     auto blocks_of = [&](const FusedGroup& grp, int what) -> long long {
@@ -709,7 +717,34 @@ iso_status run_batch(iso_ctx* ctx, int64_t n, const iso_request* req, iso_mesh* 
     } else if (!run.empty()) {
         int lanes = ctx->batch_lanes > 0 ? ctx->batch_lanes : ctx->batch_tuned;
         int share = ctx->batch_share > 0 ? ctx->batch_share : ctx->batch_tuned_share;
-        if (lane_run.empty()) {  // every request fused: nothing to tune
+        if (!fz.empty() && (ctx->fused_kc <= 0 || ctx->fused_ipw <= 0)) {
+            // autotuner of the fused launches' work split: time the batch at each (count planes, items per
+            // warp) with the lanes as they stand, keep the fastest
+            const int tl = std::min(std::max(lanes, 1), std::max(1, (int)lane_run.size()));
+            const int ts = std::max(share, 1);
+            float best = 1e30f;
+            int best_kc = kFusedKCDefault, best_ipw = kFusedIPWDefault;
+            for (int kc : kFusedKC) {
+                for (int ipw : kFusedIPW) {
+                    const FusedPlan cand = plan_fused(ctx, req, out, items, fused, nullptr, kc, ipw);
+                    if (cand.empty()) continue;
+                    rc = prepare_batch(ctx, req, out, n, items, lane_run, cand, tl, ts, s);
+                    if (rc != ISO_OK) return rc;
+                    float ms;
+                    rc = time_batch(ctx, ctx->batch_exec[out ? 0 : 1], s, ms);
+                    if (rc != ISO_OK) return rc;
+                    if (ms < best) {
+                        best = ms;
+                        best_kc = kc;
+                        best_ipw = ipw;
+                    }
+                }
+            }
+            ctx->fused_kc = best_kc;
+            ctx->fused_ipw = best_ipw;
+            fz = plan_fused(ctx, req, out, items, fused);
+        }
+        if (lane_run.empty()) {  // every request fused: no lanes to tune
             lanes = std::max(lanes, 1);
             share = std::max(share, 1);
         }
@@ -903,9 +938,10 @@ iso_status iso_batch_set_lanes(iso_ctx* ctx, int lanes)
 {
     if (!ctx || lanes < 0 || lanes > kMaxLanes) return ISO_ERR_INVALID_ARG;
     ctx->batch_lanes = lanes;
-    if (lanes == 0) {  // tune again on the next batch, the split too
+    if (lanes == 0) {  // tune again on the next batch, the split and the fused work split too
         ctx->batch_tuned = 0;
         ctx->batch_tuned_share = 0;
+        ctx->fused_kc = ctx->fused_ipw = 0;
     }
     return ISO_OK;
 }
@@ -928,6 +964,14 @@ iso_status iso_batch_set_fused(iso_ctx* ctx, int mode)
 {
     if (!ctx || mode < 0 || mode > 2) return ISO_ERR_INVALID_ARG;
     ctx->batch_fused = mode;
+    return ISO_OK;
+}
+
+iso_status iso_batch_fused_split(const iso_ctx* ctx, int* count_planes, int* items_per_warp)
+{
+    if (!ctx || !count_planes || !items_per_warp) return ISO_ERR_INVALID_ARG;
+    *count_planes = ctx->fused_kc;
+    *items_per_warp = ctx->fused_ipw;
     return ISO_OK;
 }
 

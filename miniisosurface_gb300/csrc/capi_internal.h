@@ -71,6 +71,7 @@ struct iso_ctx {
     cudaGraphExec_t batch_exec[2] = {nullptr, nullptr};
     std::vector<unsigned char> batch_key[2];
     int batch_fused = 1;  // iso_batch_set_fused: 0 lanes only, 1 fused from kFuseMin requests, 2 always fused
+    int fused_kc = 0, fused_ipw = 0;  // the autotuner's fused work split (0: not yet tuned)
     unsigned char* h_fused = nullptr;  // pinned: the fused requests' descriptors and launch lists, copied in per run
     size_t h_fused_bytes = 0;
     std::vector<cudaStream_t> fused_streams;  // the fused launches of one pass side by side, and their joins

@@ -258,3 +258,23 @@ def test_packed_many_requests(M):
     for q in range(0, 1500, 61):
         r = rs[q]
         same(as_np(meshes[q]), as_np(M.extract_device(r.volume, r.dims, r.isoval)), "request %d" % q)
+
+
+def test_fused_split_autotuner(M):
+    """The first graph-mode batch with fused requests times the fused work splits and keeps one of them; the
+    meshes equal the plain calls' whatever split it keeps."""
+    rng = np.random.default_rng(11)
+    rs = []
+    for q in range(20):
+        dims = tuple(int(x) for x in rng.integers(20, 140, size=3))
+        rs.append(M.Request(dev(M.generate_value_noise(dims, 3, 16, seed=500 + q)), dims, 0.0))
+    ctx = M.Context(0)
+    M.set_batch_lanes(0, ctx)
+    assert M.batch_fused_split(ctx) == (0, 0)
+    meshes = M.extract_batch(rs, [M.DeviceMesh(0, 0, 4) for _ in rs], ctx=ctx)
+    kc, ipw = M.batch_fused_split(ctx)
+    assert kc in (8, 16, 32) and ipw in (16, 32, 64), (kc, ipw)
+    for q, (r, m) in enumerate(zip(rs, meshes)):
+        same(as_np(m), as_np(M.extract_device(r.volume, r.dims, r.isoval)), "request %d" % q)
+    M.set_batch_lanes(0, ctx)  # tunes again on the next batch
+    assert M.batch_fused_split(ctx) == (0, 0)
