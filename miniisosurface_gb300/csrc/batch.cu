@@ -402,9 +402,10 @@ iso_status ensure_batch(iso_ctx* ctx, const BatchLayout& lay, int64_t n, cudaStr
     return ISO_OK;
 }
 
-// What a captured graph depends on: lanes, buffers, requests and meshes.
+// What a captured graph depends on: lanes, buffers, requests and meshes, and the fused launches' geometry
+// (each launch's grid and shared memory; the descriptors and lists are copied in by the graph at every run).
 std::vector<unsigned char> batch_key(const iso_ctx* ctx, int lanes, int share, const iso_request* req,
-                                     const iso_mesh* out, int64_t n)
+                                     const iso_mesh* out, int64_t n, const FusedPlan& fz)
 {
     std::vector<unsigned char> k;
     auto put = [&](const void* p, size_t len) {
@@ -422,6 +423,26 @@ std::vector<unsigned char> batch_key(const iso_ctx* ctx, int lanes, int share, c
     put(&ctx->h_fused, sizeof ctx->h_fused);
     put(&n, sizeof n);
     put(req, (size_t)n * sizeof(iso_request));
+    const size_t nf = fz.reqs.size();
+    put(&nf, sizeof nf);
+    put(&fz.at, sizeof fz.at);
+    put(&fz.upload, sizeof fz.upload);
+    put(&fz.all.total, sizeof fz.all.total);
+    for (const std::vector<FusedGroup>* gs : {&fz.count, &fz.gen}) {
+        for (const FusedGroup& g : *gs) {
+            put(&g.total, sizeof g.total);
+            put(&g.smem, sizeof g.smem);
+            put(&g.ws_bytes, sizeof g.ws_bytes);
+            put(&g.rpw, sizeof g.rpw);
+            put(&g.index_bytes, sizeof g.index_bytes);
+            const int cv[3] = {g.cv.rpw, g.cv.aligned ? 1 : 0, g.cv.full ? 1 : 0};  // no padding bytes in the key
+            put(cv, sizeof cv);
+            put(&g.list_at, sizeof g.list_at);
+            put(&g.first_at, sizeof g.first_at);
+        }
+        const size_t sep = gs->size();
+        put(&sep, sizeof sep);
+    }
     for (int64_t r = 0; out && r < n; ++r) {
         put(&out[r].points, sizeof out[r].points);
         put(&out[r].normals, sizeof out[r].normals);
@@ -519,7 +540,7 @@ iso_status prepare_batch(iso_ctx* ctx, const iso_request* req, const iso_mesh* o
     if (st != ISO_OK) return st;
     // before every run, replayed graph or not: the staging is shared by the context's graphs
     if (!lay.fz.empty()) fill_fused(ctx, lay.fz, out, items);
-    std::vector<unsigned char> key = batch_key(ctx, lanes, share, req, out, n);
+    std::vector<unsigned char> key = batch_key(ctx, lanes, share, req, out, n, lay.fz);
     const int slot = out ? 0 : 1;
     if (ctx->batch_exec[slot] && key == ctx->batch_key[slot]) return ISO_OK;
     st = capture_batch(ctx, req, out, n, items, run, lay);

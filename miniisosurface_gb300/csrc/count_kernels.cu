@@ -287,6 +287,9 @@ __device__ __forceinline__ void count_tma_block(const float* __restrict__ vol, c
     const int j = jw + h;
     const bool row_ok = j < g.ny;
     const int kb = g.kr + kc * KC, ke = min(kb + KC, g.ke);
+    if (kb >= ke) {  // a block past the grid's last plane column: nothing to copy (no launch makes one today)
+        return;
+    }
     const bool hasY = row_ok && j < g.ny - 1;
     const int nq = g.nx >> 2;
     const int nrows = min(NBUF, g.ny - jw);
@@ -666,7 +669,9 @@ __global__ void __launch_bounds__(kThreads) k_scan_partial_batch(const BatchReq*
 {
     const int q = batch_find(first, m, blockIdx.x);
     const BatchReq* d = reqs + __ldg(&list[q]);
-    scan_partial_block<kScanFE>(d->rowcnt, nullptr, d->g.R, d->part, d->nseg, (int)(blockIdx.x - __ldg(&first[q])));
+    const int blk = (int)(blockIdx.x - __ldg(&first[q]));
+    if (blk >= d->nseg) return;  // past the request's segments (the launch holds exactly first[m] blocks)
+    scan_partial_block<kScanFE>(d->rowcnt, nullptr, d->g.R, d->part, d->nseg, blk);
 }
 
 __global__ void __launch_bounds__(kThreads) k_scan_final_batch(const BatchReq* __restrict__ reqs,
@@ -675,8 +680,9 @@ __global__ void __launch_bounds__(kThreads) k_scan_final_batch(const BatchReq* _
 {
     const int q = batch_find(first, m, blockIdx.x);
     const BatchReq* d = reqs + __ldg(&list[q]);
-    scan_final_block<kScanFE>(d->rowcnt, nullptr, d->g.R, d->part, d->nseg, d->starts, d->totals,
-                              (int)(blockIdx.x - __ldg(&first[q])));
+    const int blk = (int)(blockIdx.x - __ldg(&first[q]));
+    if (blk >= d->nseg) return;
+    scan_final_block<kScanFE>(d->rowcnt, nullptr, d->g.R, d->part, d->nseg, d->starts, d->totals, blk);
 }
 
 // vfirst[q] = the vertices of requests list[0 .. q-1] whose meshes hold their counts (one CTA of 1024 threads,

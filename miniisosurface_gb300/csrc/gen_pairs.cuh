@@ -410,6 +410,7 @@ __global__ void __launch_bounds__(kThreads, kGenPairCtasPerSm) k_gen_pairs_batch
         const int q = batch_find(first, m, item);
         const BatchReq* d = reqs + __ldg(&list[q]);
         if ((long long)d->totals[0] > d->capV || (long long)d->totals[1] > d->capT) continue;
+        if (item - __ldg(&first[q]) >= (uint32_t)d->gen_ngroups * (uint32_t)d->gen_nkc) continue;  // past its items
         const Grid g = d->g;
         RowStarts rs;
         rs.starts = d->starts;

@@ -271,7 +271,11 @@ def test_fused_split_autotuner(M):
     ctx = M.Context(0)
     M.set_batch_lanes(0, ctx)
     assert M.batch_fused_split(ctx) == (0, 0)
-    meshes = M.extract_batch(rs, [M.DeviceMesh(0, 0, 4) for _ in rs], ctx=ctx)
+    # meshes of the exact sizes, so that every candidate's graph runs the generate and vertex passes too (each
+    # candidate has its own launch geometry: its graph must be captured anew, not replayed)
+    sizes = [M.count_device(r.volume, r.dims, r.isoval, ctx=ctx) for r in rs]
+    meshes = [M.DeviceMesh(v, t, 4) for v, t in sizes]
+    assert all(c == 0 for c in M.Batch(rs, meshes).run(ctx))
     kc, ipw = M.batch_fused_split(ctx)
     assert kc in (8, 16, 32) and ipw in (16, 32, 64), (kc, ipw)
     for q, (r, m) in enumerate(zip(rs, meshes)):
