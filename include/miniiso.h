@@ -216,9 +216,12 @@ iso_status iso_extract_batch(iso_ctx* ctx, int64_t n, const iso_request* req, is
  * ISO_ERR_CAPACITY (ISO_ERR_OVERFLOW) with its sizes; the others complete.
  * Every request must be Flying Edges with rows of at most 512 points and its
  * volume at a 16-byte boundary (else ISO_ERR_INVALID_ARG for it).  All passes
- * of all requests run as one launch per pass and kernel variant.  The five
- * output arrays have n entries; status may be NULL.  Synchronises the stream;
- * returns ISO_OK or the first failing request's status. */
+ * of all requests run as one launch per pass and kernel variant, each request
+ * with its own scratch held at once (about 60 + 4 * ceil(nx / 32) bytes per
+ * grid row), so a batch too large for the device's free memory fails with
+ * ISO_ERR_OOM: split it.  The five output arrays have n entries; status may be
+ * NULL.  Synchronises the stream; returns ISO_OK or the first failing
+ * request's status. */
 iso_status iso_extract_batch_packed(iso_ctx* ctx, int64_t n, const iso_request* req, float* points, float* normals,
                                     void* tris, int32_t index_bytes, int64_t cap_points, int64_t cap_tris,
                                     int64_t* point_first, int64_t* tri_first, int64_t* n_points, int64_t* n_tris,
