@@ -339,11 +339,13 @@ def test_capacity_error_reports_sizes(M):
 
 
 def _fp64_report(name, err):
+    """Print the case's FP64 error; with MINIISO_REPORT_DIR set (an existing folder), also append it to
+    fp64_error.jsonl there."""
     import json
 
-    out = Path(os.environ.get("GRAFT_REPO_ROOT", ROOT)) / "gpurun_out"
-    if out.is_dir():
-        with open(out / "fp64_error.jsonl", "a") as f:
+    out = os.environ.get("MINIISO_REPORT_DIR")
+    if out and Path(out).is_dir():
+        with open(Path(out) / "fp64_error.jsonl", "a") as f:
             f.write(json.dumps({"case": name, **err}) + "\n")
     print(name, err)
 
