@@ -14,8 +14,6 @@ import pytest
 
 import oracle_lib
 
-ROOT = Path(__file__).resolve().parents[1]
-
 pytestmark = pytest.mark.gpu
 
 POS_ULP_TOL = 0  # measured: 0 ulp; the contract allows 2
