@@ -9,7 +9,7 @@ from .api import (FLYING_EDGES, MARCHING_CUBES, MC_DUPFREE, Batch, Context, Devi
                   default_context, extract, extract_batch, extract_typed, extract_device, file_not_found,
                   generate_blobs, generate_value_noise, loadImage, make_grid, saveImage, saveTriangleMesh,
                   set_batch_graph, set_batch_lanes, set_batch_split, batch_split, set_graph, set_batch_fused,
-                  PackedBuffers, extract_batch_packed, batch_fused_split)
+                  PackedBuffers, PackedMesh, extract_batch_packed, batch_fused_split)
 from .builder import build, library_path
 
 __all__ = [
@@ -17,7 +17,7 @@ __all__ = [
     "Image3D", "MarchingCubes", "Request", "TriangleMesh", "bad_format", "batch_lanes", "build", "count_device",
     "default_context", "extract", "extract_batch", "extract_typed", "set_batch_graph", "set_batch_lanes",
     "set_batch_split", "batch_split", "set_graph", "set_batch_fused", "PackedBuffers",
-    "extract_batch_packed", "batch_fused_split",
+    "extract_batch_packed", "batch_fused_split", "PackedMesh",
     "extract_device", "file_not_found", "generate_blobs", "generate_value_noise", "library_path", "loadImage",
     "make_grid", "saveImage", "saveTriangleMesh",
 ]

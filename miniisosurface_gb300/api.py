@@ -425,11 +425,36 @@ class PackedBuffers:
                                     device=self.device)
 
 
+class PackedMesh:
+    """One request's mesh inside a packed batch's buffers: its offsets and counts, with the DeviceMesh views
+    (points, normals, tris) made when they are read."""
+
+    __slots__ = ("buffers", "point_first", "tri_first", "n_points", "n_tris", "index_bytes")
+
+    def __init__(self, buffers, point_first, tri_first, n_points, n_tris):
+        self.buffers = buffers
+        self.point_first, self.tri_first = point_first, tri_first
+        self.n_points, self.n_tris = n_points, n_tris
+        self.index_bytes = buffers.index_bytes
+
+    @property
+    def points(self):
+        return self.buffers.points[self.point_first: self.point_first + max(self.n_points, 1)]
+
+    @property
+    def normals(self):
+        return self.buffers.normals[self.point_first: self.point_first + max(self.n_points, 1)]
+
+    @property
+    def tris(self):
+        return self.buffers.tris[self.tri_first: self.tri_first + max(self.n_tris, 1)]
+
+
 def extract_batch_packed(requests, buffers=None, index_bytes=4, ctx=None, stream=None):
     """Batched extraction into one set of buffers (iso_extract_batch_packed): a list of Request (Flying Edges,
-    rows of at most 512 points) in, one DeviceMesh per request out, each a view into `buffers` (a
-    PackedBuffers, made or grown as needed) holding what extract_device gives for its request.  A batch that
-    does not fit grows the buffers to its total and runs again."""
+    rows of at most 512 points) in, one PackedMesh per request out (points, normals and tris views into
+    `buffers`, a PackedBuffers made or grown as needed) holding what extract_device gives for its request.
+    Returns (meshes, buffers).  A batch that does not fit grows the buffers to its total and runs again."""
     import torch
     lib = load()
     requests = list(requests)
@@ -449,16 +474,7 @@ def extract_batch_packed(requests, buffers=None, index_bytes=4, ctx=None, stream
             break
         buffers.reserve(sum(nv[i] for i in range(n)), sum(nt[i] for i in range(n)))
     check(st, ctx.handle)
-    out = []
-    for i in range(n):
-        m = DeviceMesh.__new__(DeviceMesh)
-        m.index_bytes = buffers.index_bytes
-        m.points = buffers.points[pf[i]: pf[i] + max(nv[i], 1)]
-        m.normals = buffers.normals[pf[i]: pf[i] + max(nv[i], 1)]
-        m.tris = buffers.tris[tf[i]: tf[i] + max(nt[i], 1)]
-        m.n_points, m.n_tris = nv[i], nt[i]
-        out.append(m)
-    return out, buffers
+    return [PackedMesh(buffers, pf[i], tf[i], nv[i], nt[i]) for i in range(n)], buffers
 
 
 def extract_batch(requests, meshes=None, index_bytes=4, ctx=None, stream=None, predictor=None):
