@@ -3,26 +3,29 @@ which extracts one volume per program run).
 
 Requests for (resident volume, isovalue) pairs arrive over time.  Worker
 slots -- each a context and a CUDA stream driven by its own host thread --
-take every request that is waiting when they become free, count them in one
-batch (iso_count_batch), admit them in arrival order while their meshes fit
-the device-memory budget beside the meshes of the other slots' batches, and
-extract the admitted ones in one batch (iso_extract_batch) into meshes of
-exactly the counted size.  With a predictor (predictor.Predictor) the count
-batch is skipped: the network sizes every mesh from the resident volumes'
-block statistics in one launch, and a request whose mesh was too small goes
-back to the head of the queue with the exact sizes the extraction reported.  Requests that arrive while other slots' batches
-are on the GPU are taken by the next free slot, so the batches of different
-slots overlap on the device (continuous batching); a request that does not
-fit waits at the head of the queue until memory frees up.  A slot that
-finds a single request waiting (light load) runs it with the plain calls --
-iso_count_device, a mesh of that size, iso_extract_device -- on its own
-context and stream, without the batch machinery.  While no slot is working
-and only a few requests wait, the thread that receives them runs them that
-way itself, oldest first, with no hand-off to a slot; a slot starts work
-beside running work only behind a backlog.
+take every request that is waiting when they become free:
+
+* Flying Edges requests with rows of at most 512 points run as one packed
+  batch (iso_extract_batch_packed): counts, placement and meshes in one call,
+  into the slot's reused buffers;
+* the others, without a network, run one after another, one iso_extract_device
+  call each into the context's reused single-request mesh (one count pass); with
+  a network (predictor.Predictor), it sizes them from the resident volumes'
+  block statistics and they run as one iso_extract_batch, a request whose mesh
+  was too small going back to the head of the queue with the exact sizes the
+  extraction reported (with `packed` off, the network or one iso_count_batch
+  sizes every request of the batch).
+
+A slot admits its work while it fits the device-memory budget beside the other
+slots' (reused buffers count at their size); what does not fit waits.  Requests
+that arrive while other slots work are taken by the next free slot, so the
+slots' work overlaps on the device (continuous batching), but a slot starts
+beside running work only behind a backlog.  While no slot is working and only a
+few requests wait, the thread that receives them runs them itself, oldest
+first, one extraction call each, with no hand-off to a slot.
 
 `run_plain` is the loop to compare with: one request at a time, in arrival
-order, iso_count_device then iso_extract_device.
+order, iso_count_device, a mesh of exactly that size, iso_extract_device.
 """
 import collections
 import ctypes as C
