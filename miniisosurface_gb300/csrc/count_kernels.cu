@@ -2,7 +2,7 @@
 // on sm_103a, with pass 1 (x-edge classification, trims) fused into pass 2
 // (cube cases, per-row counts):
 //
-//   k_count_tma    (rows up to 512 points, 16-byte aligned) a CTA owns a block
+//   k_count_tma    (rows up to 1024 points, 16-byte aligned) a CTA owns a block
 //   k_count_warps  (up to 2048) of 16 or 32 grid rows (k_count_tma: a half- or
 //                  quarter-warp per row) / 8 rows (k_count_warps: a warp per row) and a run of
 //                  KC planes and marches along z.  Each row's words of plane
@@ -244,7 +244,7 @@ __host__ __device__ inline int count_buffer_floats(int nx, int rpw, bool aligned
     return aligned ? (rpw + 1) * nx : (((rpw + 1) * nx + 3) + 3) & ~3;
 }
 
-// Rows of up to 16 words (nx <= 512), several per warp so
+// Rows of up to 32 words (nx <= 1024), several per warp up to 16 words so
 // that no lane idles on words past a short row: the counts of k_count_warps,
 // with the volume brought in by the TMA bulk engine.  A warp's grid rows
 // jw .. jw+RPW-1 read rows jw .. jw+RPW of every plane (A and B of each
@@ -257,7 +257,7 @@ __host__ __device__ inline int count_buffer_floats(int nx, int rpw, bool aligned
 // from the rows' first point rounded down to 16 bytes to their last rounded
 // down, the last few points come by plain loads, and row_word_shift builds
 // the words at the rows' offsets in the buffer.
-// RPW grid rows per warp (2: rows of up to 16 words, 4: up to 8, 8: up to 4), LPR =
+// RPW grid rows per warp (1: rows of 17-32 words, 2: up to 16, 4: up to 8, 8: up to 4), LPR =
 // 32 / RPW lanes per row; a warp's rows jw .. jw+RPW-1 read rows jw .. jw+RPW
 // of every plane, RPW + 1 rows of its buffer.  FULL: every lane's word is
 // inside the row (nx = 32 * LPR).
@@ -348,8 +348,10 @@ __device__ __forceinline__ void count_tma_block(const float* __restrict__ vol, c
         __syncwarp();  // every lane has read the buffer before it is refilled
         return true;
     };
-    // per-row totals: rows 2p, 2p+1 of the warp in the two 16-bit halves of reduction p
+    // per-row totals: rows 2p, 2p+1 of the warp in the two 16-bit halves of reduction p (one row per warp:
+    // the warp's sum)
     auto row_sum = [&](uint32_t v) -> uint32_t {
+        if (RPW == 1) return __reduce_add_sync(0xffffffffu, v);
         const int sh = 16 * (h & 1);
         uint32_t mine = 0u;
 #pragma unroll
@@ -852,8 +854,8 @@ static void count_launch(const CountPlan& p, const float* vol, const Grid& g, fl
     const bool vec4 = g.W <= 64 && (g.nx % 4 == 0) && ((reinterpret_cast<uintptr_t>(vol) & 15) == 0);
     uint2* trims = p.trims ? b.trims : nullptr;  // the kernels skip the trims when null
     const bool base16 = (reinterpret_cast<uintptr_t>(vol) & 15) == 0;
-    if (base16 && g.W <= 16) {  // 8 rows per warp up to 4 words, 4 up to 8, else 2; planes through TMA
-        const int rpw = g.W <= 4 ? 8 : (g.W <= 8 ? 4 : 2);
+    if (base16 && g.W <= 32) {  // 8 rows per warp up to 4 words, 4 up to 8, 2 up to 16, else 1; planes via TMA
+        const int rpw = g.W <= 4 ? 8 : (g.W <= 8 ? 4 : (g.W <= 16 ? 2 : 1));
         const bool aligned = g.nx % 4 == 0;
         const int rows = kCountRows * rpw;
         const int nyb2 = (g.ny + rows - 1) / rows;
@@ -870,7 +872,11 @@ static void count_launch(const CountPlan& p, const float* vol, const Grid& g, fl
         if (!aligned) {
             if (rpw == 8) ISO_TMA(false, 8, false)
             else if (rpw == 4) ISO_TMA(false, 4, false)
-            else ISO_TMA(false, 2, false)
+            else if (rpw == 2) ISO_TMA(false, 2, false)
+            else ISO_TMA(false, 1, false)
+        } else if (rpw == 1) {
+            if (nq == 256) ISO_TMA(true, 1, true)
+            else ISO_TMA(false, 1, true)
         } else if (rpw == 8) {
             if (nq == 32) ISO_TMA(true, 8, true)
             else ISO_TMA(false, 8, true)

@@ -663,10 +663,11 @@ void launch_gen_warps_impl(const float* vol, const Grid& g, float iso, const Cas
 {
     const int nzw = p.kend - p.kbeg;
     if (nzw <= 0) return;
-    // items of KC planes: about four per warp of one wave, at least 4 planes
+    // items of KC planes: about eight per warp of one wave, at least 2 planes (667 x 228 x 724: FE 635 -> 631,
+    // MC 687 -> 676 us against four per warp and 4 planes; sixteen per warp: 644 / 680)
     const long long warps = (long long)p.nsm * kGenCtasPerSm * kGenRows;
-    long long KC = ((long long)g.ny * nzw + 4 * warps - 1) / (4 * warps);
-    if (KC < 4) KC = 4;
+    long long KC = ((long long)g.ny * nzw + 8 * warps - 1) / (8 * warps);
+    if (KC < 2) KC = 2;
     while ((long long)g.ny * ((nzw + KC - 1) / KC) >= (1ll << 31)) KC *= 2;  // item numbers stay below 2^31
     if (KC > nzw) KC = nzw;
     const int nkc = (int)((nzw + KC - 1) / KC);

@@ -101,10 +101,12 @@ def test_wide_rows_multi_chunk(M):
     both(M, vol, -0.05)
 
 
-@pytest.mark.parametrize("dims", [(600, 9, 7), (1000, 7, 6), (1024, 5, 5)])
+@pytest.mark.parametrize("dims", [(600, 9, 7), (1000, 7, 6), (1024, 5, 5), (513, 10, 6), (557, 8, 6),
+                                  (1023, 6, 5)])
 def test_rows_of_17_to_32_words(M, dims):
-    """Rows of 545-1024 points: one grid row per warp in pass 4 (Flying Edges
-    vertices through the per-axis queues), the multi-word count kernels."""
+    """Rows of 513-1024 points: one grid row per warp in pass 4 (Flying Edges
+    vertices through the per-axis queues) and in the bulk-copy count pass (rows
+    a multiple of 4 points long, 1024 points, and not: 513, 557, 1023)."""
     vol = M.generate_value_noise(dims, 4, 16, seed=sum(dims))
     both(M, vol, 0.0)
 
